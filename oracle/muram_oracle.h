@@ -1,0 +1,73 @@
+/* CPU restatement of MURaM's MHD time-step hot path (test infrastructure).
+ *
+ * This oracle is the checker for the GPU library: only tests, the smoke check
+ * and the CPU-baseline leg of the benchmark call it.  Every routine restates
+ * the arithmetic of the reference function it names, in the same operation
+ * order (built with -ffp-contract=off), on a structure-of-arrays state:
+ *
+ *   U[v*N + i + sx*(j + sy*k)],  v = rho, M_x, M_y, M_z, e, B_x, B_y, B_z
+ *   sx = nx+4, sy = ny+4, sz = nz+4, N = sx*sy*sz   (two ghost layers)
+ */
+#ifndef MURAM_ORACLE_H
+#define MURAM_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct {
+  int nx, ny, nz;       /* interior cells per dimension (dimension 0 = x = vertical) */
+  int periodic_x;       /* 1: periodic x; 0: closed x (mirror ghosts, physical x boundaries) */
+  double dx[3];
+  /* RunData subset */
+  double CFL, CFL_tvd, dt, time, outcad;
+  int autostep;
+  /* PhysicsData subset */
+  double grav, va_max, va_adjust, max_fill;
+  double tvd_h[4], tvd_cs[4], tvd[10], tvd_h_bnd[2], tvd_visc_bnd[2], tvd_eta_bnd[2], tvd_coeff[4];
+  double tchk[4];
+  double rt_cfl, rt_tstep, rt_update;
+  /* RT stub: constant optical depth, zero Qtot, constant dt_rad */
+  double tau0, dt_rad;
+  /* values the reference keeps in globals / function statics */
+  double inv_va2max, v_lim, e_lim, va_max_old;
+  int va_ini_flag;
+  double last_cfl;
+  int tvd_two_half_steps;
+} mo_params;
+
+typedef struct mo_eos mo_eos;
+
+void mo_default_params(mo_params* p, int nx, int ny, int nz, double dx);
+mo_eos* mo_eos_load(const char* path);
+void mo_eos_free(mo_eos* e);
+int mo_eos_dims(const mo_eos* e, int* dims4);
+
+/* src/Add_Sources_Integrate_SR.C:475-502 */
+void mo_save_cons(const mo_params* p, const double* U, double* U0);
+/* src/cons_to_prim.C:78-266 (aux may be NULL to skip T, n_e, rho_i, nu_in) */
+void mo_cons_to_prim(const mo_params* p, const mo_eos* eos, double* U, double* pres, double* temp,
+                     double* ne, double* rhoi, double* amb);
+/* src/Adjust_Valf_Max.C:25-150; stats[5] receives the local max/sum values */
+void mo_adjust_valf_max(mo_params* p, const double* U, const double* pres, double* stats);
+/* src/mhdres_SR.C:27-854 (ideal MHD branch); returns dt_mhd */
+double mo_mhd_residual(const mo_params* p, const double* U, const double* pres, double* R);
+/* src/solver.C:487-548; returns 0 or a negative error code */
+int mo_sync_timestep(mo_params* p, double dt_rad, double dt_mhd, double* cfl);
+/* src/Add_Sources_Integrate_SR.C:38-472 (no-diagnostics branch) */
+void mo_source_integrate_tcheck(const mo_params* p, double* U, const double* U0, double* R, int stage);
+/* src/exchange.C:532-783 on one rank plus the closed-x mirror rule */
+void mo_boundaries(const mo_params* p, double* U);
+void mo_exchange_only(const mo_params* p, double* U);
+/* src/tvdlimit_SR.C:33-695 */
+void mo_tvdlimit(const mo_params* p, double* U, const double* pres, double dt_tvd);
+/* src/Add_Sources_Integrate_SR.C:534-625 */
+void mo_tcheck(const mo_params* p, double* U);
+/* One full step in the order of src/solver.C:109-365; returns 0 or a negative error code.
+ * Scratch: U0, R (8N each) and pres, temp, ne, rhoi, amb (N each). */
+int mo_step(mo_params* p, const mo_eos* eos, double* U, double* U0, double* R, double* aux5);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

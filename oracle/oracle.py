@@ -1,0 +1,147 @@
+"""ctypes binding of the C restatement (oracle/muram_oracle.c).
+
+Test infrastructure: the checker the GPU path is compared against.  Only
+tests/, ``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py``
+import this module.  ``build()`` compiles the shared library with the
+oracle's Makefile (gcc, -O2 -ffp-contract=off).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libmuram_oracle.so")
+
+
+class MoParams(C.Structure):
+    _fields_ = [
+        ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("periodic_x", C.c_int),
+        ("dx", C.c_double * 3),
+        ("CFL", C.c_double), ("CFL_tvd", C.c_double), ("dt", C.c_double), ("time", C.c_double),
+        ("outcad", C.c_double), ("autostep", C.c_int),
+        ("grav", C.c_double), ("va_max", C.c_double), ("va_adjust", C.c_double), ("max_fill", C.c_double),
+        ("tvd_h", C.c_double * 4), ("tvd_cs", C.c_double * 4), ("tvd", C.c_double * 10),
+        ("tvd_h_bnd", C.c_double * 2), ("tvd_visc_bnd", C.c_double * 2), ("tvd_eta_bnd", C.c_double * 2),
+        ("tvd_coeff", C.c_double * 4), ("tchk", C.c_double * 4),
+        ("rt_cfl", C.c_double), ("rt_tstep", C.c_double), ("rt_update", C.c_double),
+        ("tau0", C.c_double), ("dt_rad", C.c_double),
+        ("inv_va2max", C.c_double), ("v_lim", C.c_double), ("e_lim", C.c_double), ("va_max_old", C.c_double),
+        ("va_ini_flag", C.c_int), ("last_cfl", C.c_double), ("tvd_two_half_steps", C.c_int),
+    ]
+
+
+_lib = None
+
+
+def build():
+    subprocess.run(["make", "-s", "-C", HERE, "all"], check=True)
+    return LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = C.CDLL(LIB_PATH)
+        dp = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+        P = C.POINTER(MoParams)
+        L.mo_default_params.argtypes = [P, C.c_int, C.c_int, C.c_int, C.c_double]
+        L.mo_eos_load.restype = C.c_void_p
+        L.mo_eos_load.argtypes = [C.c_char_p]
+        L.mo_eos_free.argtypes = [C.c_void_p]
+        L.mo_save_cons.argtypes = [P, dp, dp]
+        L.mo_cons_to_prim.argtypes = [P, C.c_void_p, dp, dp, dp, dp, dp, dp]
+        L.mo_adjust_valf_max.argtypes = [P, dp, dp, dp]
+        L.mo_mhd_residual.restype = C.c_double
+        L.mo_mhd_residual.argtypes = [P, dp, dp, dp]
+        L.mo_sync_timestep.restype = C.c_int
+        L.mo_sync_timestep.argtypes = [P, C.c_double, C.c_double, C.POINTER(C.c_double)]
+        L.mo_source_integrate_tcheck.argtypes = [P, dp, dp, dp, C.c_int]
+        L.mo_boundaries.argtypes = [P, dp]
+        L.mo_exchange_only.argtypes = [P, dp]
+        L.mo_tvdlimit.argtypes = [P, dp, dp, C.c_double]
+        L.mo_tcheck.argtypes = [P, dp]
+        L.mo_step.restype = C.c_int
+        L.mo_step.argtypes = [P, C.c_void_p, dp, dp, dp, dp]
+        _lib = L
+    return _lib
+
+
+class Eos:
+    def __init__(self, path):
+        self.ptr = lib().mo_eos_load(path.encode())
+        if not self.ptr:
+            raise OSError(f"cannot load EOS table {path}")
+
+    def __del__(self):
+        if getattr(self, "ptr", None) and _lib is not None:
+            _lib.mo_eos_free(self.ptr)
+            self.ptr = None
+
+
+def make_params(nx, ny, nz, dx=3.2e6, dy=None, dz=None, periodic_x=True, **kw):
+    p = MoParams()
+    lib().mo_default_params(C.byref(p), nx, ny, nz, dx)
+    p.dx[1] = dx if dy is None else dy
+    p.dx[2] = dx if dz is None else dz
+    p.periodic_x = 1 if periodic_x else 0
+    for k, v in kw.items():
+        if isinstance(v, (list, tuple)):
+            arr = getattr(p, k)
+            for i, x in enumerate(v):
+                arr[i] = x
+        else:
+            setattr(p, k, v)
+    return p
+
+
+def params_from_harness(hp):
+    """Build MoParams from the harness key/value dict used by oracle.refrun."""
+    kw = {}
+    simple = {"CFL": "CFL", "CFL_tvd": "CFL_tvd", "grav": "grav", "va_max": "va_max",
+              "va_adjust": "va_adjust", "max_fill": "max_fill", "tau0": "tau0", "dt_rad": "dt_rad"}
+    for k, a in simple.items():
+        if k in hp:
+            kw[a] = float(hp[k])
+    for k in ("tvd_h", "tvd_cs", "tvd_coeff", "tvd_h_bnd", "tvd_visc_bnd", "tvd_eta_bnd"):
+        if k in hp:
+            kw[k] = [float(x) for x in hp[k]]
+    p = make_params(int(hp["nx"]), int(hp["ny"]), int(hp["nz"]), float(hp.get("dx", 3.2e6)),
+                    float(hp.get("dy", hp.get("dx", 3.2e6))), float(hp.get("dz", hp.get("dx", 3.2e6))),
+                    periodic_x=bool(int(hp.get("periodic_x", 1))), **kw)
+    tvd_keys = ["tvd_rholev", "tvd_rholog", "tvd_qrho", "tvd_Bpar", "tvd_vhyp", "tvd_Qdiff_bnd",
+                "tvd_pm_v", "tvd_pm_B", "tvd_vmax_lim", "tvd_CME_thresh"]
+    for i, k in enumerate(tvd_keys):
+        if k in hp:
+            p.tvd[i] = float(hp[k])
+    tchk_keys = ["tchk_eps_min", "tchk_rho_min", "tchk_eps_max", "tchk_vmax"]
+    for i, k in enumerate(tchk_keys):
+        if k in hp:
+            p.tchk[i] = float(hp[k])
+    return p
+
+
+class State:
+    """Scratch buffers for full steps on the oracle."""
+
+    def __init__(self, p, U):
+        self.p = p
+        self.U = np.ascontiguousarray(U, dtype=np.float64).copy()
+        self.U0 = np.zeros_like(self.U)
+        self.R = np.zeros_like(self.U)
+        self.aux = np.zeros((5,) + self.U.shape[1:])
+        lib().mo_boundaries(C.byref(p), self.U)
+
+    def step(self, eos, n=1):
+        dts = []
+        for _ in range(n):
+            rc = lib().mo_step(C.byref(self.p), eos.ptr, self.U, self.U0, self.R, self.aux)
+            if rc:
+                raise RuntimeError(f"oracle step failed: {rc}")
+            dts.append((self.p.dt, self.p.last_cfl))
+        return dts
