@@ -1,0 +1,347 @@
+#!/usr/bin/env python
+"""Benchmark of the MURaM MHD time step on GB300: cell-updates/s.
+
+Default workload (N=1): the stratified convection-style box, 128 (vertical,
+MURaM dimension 0) x 384 x 384 cells at 16 km, closed top/bottom, periodic
+horizontally, gravity 2.74e4 cm/s^2, seeded random velocity and field, in FP32
+storage and arithmetic; the FP64 mode of the same box is timed too and reported
+under "fp64".  One step = SaveCons, 4 RK stages (residual, sources, update,
+Tcheck), Sync_timestep, TVD and TCheck, ghost fill -- the whole time step.
+
+--impl reference times the reference algorithm on the host cores (the oracle's
+C restatement, or the reference harness where it was built) on bounded samples
+of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "MHD cell-updates/s per RK4 step"
+UNIT = "cell-updates/s"
+WORKLOAD = dict(nx=128, ny=384, nz=384, dx=1.6e6, grav=2.74e4, periodic_x=0)
+DATA_DIR = os.path.join(ROOT, "muram_main_gb300", "_data")
+EOS_BENCH = os.path.join(DATA_DIR, "eos_bench.dat")
+# CPU sample: the full vertical extent with a 32 x 32 horizontal patch
+SAMPLE = dict(nx=128, ny=32, nz=32)
+
+
+def world():
+    return int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def make_state(nx, ny, nz, seed):
+    from muram_main_gb300 import eos_table, initial
+    eos_table.ensure_table(EOS_BENCH, "bench")
+    tab = initial.EosTable(EOS_BENCH)
+    return initial.stratified_box(tab, nx, ny, nz, dx=WORKLOAD["dx"], grav=WORKLOAD["grav"], seed=seed)
+
+
+# ----------------------------------------------------------------- CPU side
+def _cpu_worker(args):
+    seed, steps = args
+    import numpy as np  # noqa: F401
+    from oracle import oracle as O
+    U = make_state(SAMPLE["nx"], SAMPLE["ny"], SAMPLE["nz"], seed)
+    p = O.make_params(SAMPLE["nx"], SAMPLE["ny"], SAMPLE["nz"], WORKLOAD["dx"], periodic_x=False,
+                      grav=WORKLOAD["grav"])
+    st = O.State(p, U)
+    eos = O.Eos(EOS_BENCH)
+    st.step(eos, 1)  # warm-up
+    t0 = time.perf_counter()
+    st.step(eos, steps)
+    dt = time.perf_counter() - t0
+    return SAMPLE["nx"] * SAMPLE["ny"] * SAMPLE["nz"] * steps, dt
+
+
+def cpu_baseline(cores, steps_per_core):
+    """Oracle (C restatement of the reference path) on `cores` spawned processes,
+    each advancing its own 128x32x32 column of the workload; aggregate rate."""
+    from oracle import oracle as O
+    O.build()
+    from muram_main_gb300 import eos_table
+    eos_table.ensure_table(EOS_BENCH, "bench")
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        res = pool.map(_cpu_worker, [(1000 + i, steps_per_core) for i in range(cores)])
+    cells = sum(r[0] for r in res)
+    wall = max(r[1] for r in res)
+    return cells / wall, wall
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._proc = None
+
+    def start(self):
+        try:
+            self._proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self._proc = None
+            return
+        threading.Thread(target=self._read, daemon=True).start()
+
+    def _read(self):
+        for line in self._proc.stdout:
+            if self._stop.is_set():
+                break
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 8:
+                self.samples.append(parts)
+
+    def stop(self):
+        self._stop.set()
+        if self._proc:
+            self._proc.terminate()
+            try:
+                self._proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self._proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[4 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+# -------------------------------------------------------------- GPU timing
+def time_device(g, steps, warmup):
+    """Device-resident throughput: CUDA events on the library's stream."""
+    import torch
+    stream = torch.cuda.ExternalStream(g.stream)
+    g.enqueue_steps(warmup)
+    g.synchronize()
+    n0 = g.launch_count
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    g.enqueue_steps(steps)
+    e1.record(stream)
+    e1.synchronize()
+    g.synchronize()
+    return e0.elapsed_time(e1), g.launch_count - n0
+
+
+def time_e2e(g, steps, U):
+    """End to end through the C ABI: per step the host state (pinned, cState
+    layout, float64) goes to the device, one fused step runs, the result comes back."""
+    import numpy as np
+    import torch
+    from muram_main_gb300 import gpumhd
+    aos = np.ascontiguousarray(np.moveaxis(U, 0, -1))
+    h_in = torch.from_numpy(aos.reshape(-1)).pin_memory()
+    h_out = torch.empty_like(h_in).pin_memory()
+    nbytes = h_in.numel() * 8
+    g.upload_ptr(gpumhd.FIELD_U, h_in.data_ptr())
+    g.run_steps(1)
+    g.download_ptr(gpumhd.FIELD_U, h_out.data_ptr())
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        g.upload_ptr(gpumhd.FIELD_U, h_in.data_ptr())
+        g.enqueue_steps(1)
+        g.download_ptr(gpumhd.FIELD_U, h_out.data_ptr())
+    g.synchronize()
+    return (time.perf_counter() - t0) * 1e3, nbytes, nbytes
+
+
+def words_per_cell(phase):
+    """Algorithmic words moved per interior cell by one launch of each kernel
+    (state words: 8 conserved variables + pressure)."""
+    if phase == "stage1":
+        return 8 + 1 + 8 + 1          # read U, p; write U', p'
+    if phase in ("stage2", "stage3"):
+        return 8 + 1 + 8 + 8 + 1      # read U, p, U0; write U', p'
+    if phase == "stage4":
+        return 8 + 1 + 8 + 8          # read U, p, U0; write U'
+    if phase in ("tvd_x", "tvd_y"):
+        return 8 + 1 + 8              # read U, stale p; write U
+    if phase == "tvd_z":
+        return 8 + 1 + 8 + 1          # + next step's pressure
+    return 0
+
+
+def load_traffic():
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(path):
+        with open(path) as fh:
+            return json.load(fh)
+    return {}
+
+
+def run_ours(args):
+    import numpy as np  # noqa: F401
+    import torch
+    from muram_main_gb300 import build, eos_table, gpumhd
+    ws, rank, lrank = world()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    torch.cuda.set_device(lrank)
+    build.build()
+    eos_table.ensure_table(EOS_BENCH, "bench")
+    wl = WORKLOAD
+    n_cells = wl["nx"] * wl["ny"] * wl["nz"]
+    U = make_state(wl["nx"], wl["ny"], wl["nz"], seed=7 + rank)
+    peaks = {}
+    pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(pk):
+        with open(pk) as fh:
+            peaks = json.load(fh)
+    peak_gbs = float(peaks.get("hbm_gbs", 6800.0))
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+
+    def context(prec):
+        p = gpumhd.default_params(wl["nx"], wl["ny"], wl["nz"], wl["dx"], precision=prec,
+                                  periodic_x=wl["periodic_x"], grav=wl["grav"])
+        g = gpumhd.MuramGPU(p, device=lrank, eos_path=EOS_BENCH)
+        g.upload_state(U)
+        return g
+
+    # FP32 headline
+    g = context(32)
+    g.run_steps(1)  # builds the graph
+    clocks = ClockSampler(lrank)
+    clocks.start()
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    ms, launches = time_device(g, args.steps, args.warmup)
+    clocks.stop()
+    if ws > 1:
+        t = torch.tensor([ms], dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = ws * n_cells * args.steps / (ms / 1e3)
+    dt, cfl, sim_t, two_half = g.step_info()
+    phases = g.profile_steps(2)
+    # dominant kernel family: the RK stage kernel or the TVD sweep kernel
+    fam = {"stage": ["stage1", "stage2", "stage3", "stage4"], "tvd": ["tvd_x", "tvd_y", "tvd_z"]}
+    tot = {k: sum(phases[p] for p in v) for k, v in fam.items()}
+    dom = max(tot, key=tot.get)
+    launches_dom = fam[dom]
+    mean_ms = tot[dom] / len(launches_dom)
+    bytes_per_launch = sum(words_per_cell(p) for p in launches_dom) / len(launches_dom) * 4 * n_cells
+    achieved = bytes_per_launch / (mean_ms / 1e3) / 1e9
+    traffic = load_traffic().get(f"{dom}_f32_bytes_per_cell")
+    roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak_gbs, "unit": "GB/s",
+                "frac": round(achieved / peak_gbs, 4),
+                "traffic": (traffic * n_cells if traffic else None),
+                "kernel": f"k_stage (FP32, RK stages 1-4)" if dom == "stage" else "k_tvd_sweep (FP32, x/y/z)",
+                "algorithmic_bytes_per_launch": bytes_per_launch, "mean_launch_ms": round(mean_ms, 4),
+                "peak_source": f"{peak_src} hbm_gbs"}
+    # whole-step bytes against HBM
+    step_bytes = sum(words_per_cell(p) for p in fam["stage"] + fam["tvd"]) * 4 * n_cells
+    step_ms = ms / args.steps
+    # end to end through the C ABI with host buffers
+    e2e_ms, h2d, d2h = time_e2e(g, max(2, min(args.steps, 5)), U)
+    e2e_steps = max(2, min(args.steps, 5))
+    e2e_value = ws * n_cells * e2e_steps / (e2e_ms / 1e3)
+    g.close()
+    del g
+    # FP64 mode of the same box
+    g64 = context(64)
+    g64.run_steps(1)
+    ms64, _ = time_device(g64, max(2, args.steps // 4), 2)
+    value64 = ws * n_cells * max(2, args.steps // 4) / (ms64 / 1e3)
+    g64.close()
+    del g64
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded stratified box, generated EOS table 3000x3000)",
+        "config": {"workload": "stratified 128(vertical) x 384 x 384 at 16 km, closed top/bottom, gravity 2.74e4",
+                   "cells": n_cells, "precision": "fp32 storage+arithmetic",
+                   "l2": "inputs larger than L2 (state 0.64 GB per buffer)",
+                   "tvd_branch": "two half steps" if two_half else "single", "dt_s": dt, "cfl": cfl,
+                   "graph": "one CUDA graph per step", "replicas": ws},
+        "roofline": roofline,
+        "step_hbm_gbs": round(step_bytes / (step_ms / 1e3) / 1e9, 1),
+        "phases_ms": {k: round(v, 4) for k, v in phases.items()},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches,
+        "clocks": clocks.summary(),
+        "fp64": {"value": value64, "unit": UNIT, "ms_per_step": ms64 / max(2, args.steps // 4),
+                 "fp32_over_fp64": value / value64},
+    }
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        cores = min(os.cpu_count() or 1, 16)
+        rate, wall = cpu_baseline(cores, 2)
+        line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+                                "sample": f"{cores} processes x 2 steps of a {SAMPLE['nx']}x{SAMPLE['ny']}x"
+                                          f"{SAMPLE['nz']} column of the workload (FP64), {wall:.1f} s"}
+    if rank == 0:
+        print(json.dumps(line))
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+def run_reference(args):
+    ws, rank, _ = world()
+    if rank != 0:
+        return
+    cores = min(os.cpu_count() or 1, 16)
+    steps = max(1, min(args.steps, 3))
+    t0 = time.perf_counter()
+    rate, wall = cpu_baseline(cores, steps)
+    line = {
+        "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": ws, "steps": steps, "warmup": 1,
+        "ms_per_step": SAMPLE["nx"] * SAMPLE["ny"] * SAMPLE["nz"] * cores / rate * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded stratified box, generated EOS table 3000x3000)",
+        "config": {"workload": "stratified 128(vertical) x 384 x 384 at 16 km, closed top/bottom, gravity 2.74e4",
+                   "sample": "128x32x32 columns, one per core"},
+        "impl": "reference",
+        "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{cores} processes x {steps} steps of a 128x32x32 column (FP64)"},
+        "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "wall_s": round(time.perf_counter() - t0, 2),
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,136 @@
+/* gpumhd: GB300-native MURaM MHD time-step hot path, C ABI.
+ *
+ * The library owns the grid state on one GPU and exposes one entry point per
+ * reference routine on MURaM's time-step path (src/solver.C:109-365), so a
+ * MURaM build can route each call through it, plus a fused entry point that
+ * advances whole time steps on the device.
+ *
+ * State layout seen by the host: MURaM's GridData arrays, i.e. cState records
+ * of 8 doubles (rho, M_x, M_y, M_z, e, B_x, B_y, B_z) in x-fastest order over
+ * the local box including 2 ghost layers, node = i + sx*(j + sy*k),
+ * sx = nx+4, sy = ny+4 (include/grid.H:109-121, src/grid.C:197-199).
+ * Dimension 0 (x) is vertical.  On the device the state is stored as a
+ * structure of arrays in FP64 or FP32 (gpumhd_params.precision).
+ *
+ * Every function returns GPUMHD_OK (0) or a negative status; the reference
+ * calls MPI_Abort in the corresponding situations instead.
+ * A context is bound to one device and one CUDA stream and is not thread-safe.
+ * Calls are ordered on the context's stream; functions that return host
+ * scalars synchronise on them.
+ */
+#ifndef GPUMHD_H
+#define GPUMHD_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GPUMHD_OK 0
+#define GPUMHD_E_INVALID (-1)   /* bad argument or unsupported configuration */
+#define GPUMHD_E_CUDA (-2)      /* CUDA runtime error (message in gpumhd_last_error) */
+#define GPUMHD_E_EOS (-3)       /* EOS file missing or malformed (src/eos_init.C:74-77 aborts) */
+#define GPUMHD_E_BAD_DT (-4)    /* invalid dt_rad or dt_mhd (src/solver.C:497-507 aborts) */
+#define GPUMHD_E_CFL (-5)       /* cfl >= 2 (src/solver.C:530-534 aborts) */
+#define GPUMHD_E_ORDER (-6)     /* call made before the state it needs exists */
+#define GPUMHD_E_NOMEM (-7)     /* device allocation failed */
+
+/* Plain-data mirror of the RunData / PhysicsData / GridData fields the path
+ * reads (include/run.H:6-80, include/physics.H:80-206, include/grid.H:8-125). */
+typedef struct gpumhd_params {
+  int nx, ny, nz;        /* interior cells (GridData::lsize); each >= 4 */
+  int periodic_x;        /* GridData::periods[0]; y and z are periodic */
+  int precision;         /* 64: FP64 state and arithmetic; 32: FP32 state and arithmetic */
+  int pad0;
+  double dx[3];          /* GridData::dx */
+  /* RunData */
+  double CFL, CFL_tvd, dt, time, outcad;
+  int autostep;          /* RunData::autostep (dt computed from the CFL condition) */
+  int pad1;
+  /* PhysicsData::params */
+  double grav, va_max, va_adjust, max_fill;
+  /* PhysicsData TVD settings */
+  double tvd_h[4], tvd_cs[4], tvd[10], tvd_h_bnd[2], tvd_visc_bnd[2], tvd_eta_bnd[2], tvd_coeff[4];
+  double tchk[4];        /* eps_min, rho_min, eps_max, vmax */
+  double rt_cfl, rt_tstep, rt_update;
+  /* radiative transfer stays outside the path: constant optical depth,
+   * zero radiative heating, constant radiative time step */
+  double tau0, dt_rad;
+} gpumhd_params;
+
+typedef struct gpumhd_ctx gpumhd_ctx;
+
+/* Fill p with the reference defaults (src/run.C:8-56, include/physics.H:111-198). */
+int gpumhd_default_params(gpumhd_params* p, int nx, int ny, int nz, double dx);
+
+/* Create a context on CUDA device `device`; allocates the device state
+ * (GridData::Init, src/grid.C:147-348). */
+int gpumhd_create(const gpumhd_params* p, int device, gpumhd_ctx** out);
+int gpumhd_destroy(gpumhd_ctx* ctx);
+/* Replace the run parameters (e.g. after the host changed Run.dt); the grid
+ * shape and precision must not change. */
+int gpumhd_set_params(gpumhd_ctx* ctx, const gpumhd_params* p);
+int gpumhd_get_params(gpumhd_ctx* ctx, gpumhd_params* p);
+/* Text of the last error on this context (or on context creation when ctx is NULL). */
+const char* gpumhd_last_error(gpumhd_ctx* ctx);
+
+/* eos_init (src/eos_init.C:57-212): read the binary EOS table and upload it. */
+int gpumhd_eos_init(gpumhd_ctx* ctx, const char* path);
+
+/* ACCH::UpdateGPU / ACCH::UpdateCPU of the GridData arrays (src/ACCH.C:114-158):
+ * which = 0: U, 1: U0, 2: Res (cState arrays, 8 doubles per node);
+ * which = 3..7: pres, temp, ne, rhoi, amb (one double per node). */
+int gpumhd_upload(gpumhd_ctx* ctx, int which, const double* host);
+int gpumhd_download(gpumhd_ctx* ctx, int which, double* host);
+
+/* SaveCons (include/src_int_tck.H:10, src/Add_Sources_Integrate_SR.C:475-531). */
+int gpumhd_save_cons(gpumhd_ctx* ctx);
+/* ConsToPrim (include/eos.H:39, src/cons_to_prim.C:78-266). */
+int gpumhd_cons_to_prim(gpumhd_ctx* ctx);
+/* Adjust_Valf_Max (include/limit_va.H:7, src/Adjust_Valf_Max.C:25-150). */
+int gpumhd_adjust_valf_max(gpumhd_ctx* ctx);
+/* The globals inv_va2max, v_lim, e_lim (include/limit_va.H:5). */
+int gpumhd_get_limits(gpumhd_ctx* ctx, double* inv_va2max, double* v_lim, double* e_lim);
+/* MHD_Residual (include/mhd_tvd.H:5, src/mhdres_SR.C:27-854): Res += residual,
+ * *dt_mhd = dxmin / cmax. */
+int gpumhd_mhd_residual(gpumhd_ctx* ctx, double* dt_mhd);
+/* Sync_timestep (src/solver.C:487-548, file-local in the reference). */
+int gpumhd_sync_timestep(gpumhd_ctx* ctx, double dt_rad, double dt_mhd, double* cfl);
+/* Source_Integrate_Tcheck (include/src_int_tck.H:8-9, src/Add_Sources_Integrate_SR.C:38-472). */
+int gpumhd_source_integrate_tcheck(gpumhd_ctx* ctx, int stage);
+/* TVDlimit (include/mhd_tvd.H:6, src/tvdlimit_SR.C:33-695). */
+int gpumhd_tvdlimit(gpumhd_ctx* ctx, double dt_tvd);
+/* TCheck (include/src_int_tck.H:7, src/Add_Sources_Integrate_SR.C:534-625). */
+int gpumhd_tcheck(gpumhd_ctx* ctx);
+/* exchange_grid_acc (include/exchange.H:8, src/exchange.C:532-783) on one GPU:
+ * periodic ghost fill; with_bc = 1 also applies the closed-x mirror rule
+ * (SetBoundaryConditions with OPEN_TOP = 0, src/boundary_pdmp_1_fftw3.C:415-447). */
+int gpumhd_exchange(gpumhd_ctx* ctx, int with_bc);
+
+/* Fused path: advance `nsteps` full time steps (SaveCons, 4 RK stages,
+ * Sync_timestep, TVD, TCheck, boundaries; src/solver.C:109-365) entirely on
+ * the device.  Equivalent to the per-routine calls above on U in conserved
+ * form with filled ghosts.  dt_out (may be NULL) receives dt of each step.
+ * With capture = 1 the step sequence is recorded once as a CUDA graph and
+ * replayed. */
+int gpumhd_run_steps(gpumhd_ctx* ctx, int nsteps, double* dt_out, int capture);
+/* Enqueue `nsteps` fused steps without synchronising or reading results. */
+int gpumhd_enqueue_steps(gpumhd_ctx* ctx, int nsteps);
+/* Wait for the context's stream and report any device-side error flag. */
+int gpumhd_synchronize(gpumhd_ctx* ctx);
+/* Device-side step diagnostics after gpumhd_synchronize: dt, cfl, time,
+ * and whether the last step took the two-half-step TVD branch. */
+int gpumhd_step_info(gpumhd_ctx* ctx, double* dt, double* cfl, double* time, int* tvd_two_half);
+
+/* Run `nsteps` fused steps without graph capture, timing each launch with CUDA
+ * events on the context's stream; ms_phase[11] receives the mean duration of:
+ * step control, RK stages 1-4, TVD x/y/z sweeps, second-half TVD x/y/z sweeps. */
+int gpumhd_profile_steps(gpumhd_ctx* ctx, int nsteps, double* ms_phase);
+/* The CUDA stream the context enqueues on (a cudaStream_t). */
+void* gpumhd_stream(gpumhd_ctx* ctx);
+/* Number of kernel launches the context has enqueued so far. */
+long long gpumhd_launch_count(gpumhd_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,871 @@
+// Host side of the gpumhd C ABI (include/gpumhd.h).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include "../../include/gpumhd.h"
+#include "gpumhd_launch.cuh"
+
+using namespace gpumhd;
+
+struct gpumhd_ctx {
+  gpumhd_params p;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool f32 = false;
+  size_t rsz = 8;
+  Consts c{};
+  // device memory
+  void* S[3] = {nullptr, nullptr, nullptr};   // state buffers (8N each)
+  int iU = 0, iU0 = 1, iRes = 2;              // per-routine roles
+  void* P[2] = {nullptr, nullptr};            // pressure buffers (N each)
+  int iP = 0;
+  void* aux[4] = {nullptr, nullptr, nullptr, nullptr};  // temp, ne, rhoi, amb
+  void* T = nullptr;                          // TVD scratch of the per-routine path (8N)
+  double* staging = nullptr;                  // host-layout transfer buffer (8N doubles)
+  Dyn* dyn = nullptr;
+  double* dt_hist = nullptr;
+  int dt_hist_cap = 0;
+  Dyn hdyn{};                                  // host mirror of the per-routine scalars
+  // EOS
+  double* d_xeps = nullptr;
+  double* d_xlr = nullptr;
+  float* d_tab[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  float4* d_pquad = nullptr;
+  float* d_inv_xeps = nullptr;
+  float* d_inv_xlr = nullptr;
+  double* d_prof = nullptr;
+  bool eos_loaded = false;
+  // per-routine state flags
+  bool have_pres = false;
+  // fused path
+  bool fused_ready = false;
+  cudaGraphExec_t graph = nullptr;
+  long long launches = 0;
+  char err[1024] = {0};
+};
+
+static char g_create_err[1024];
+
+static int fail(gpumhd_ctx* ctx, int code, const char* fmt, ...) {
+  char* buf = ctx ? ctx->err : g_create_err;
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, 1024, fmt, ap);
+  va_end(ap);
+  return code;
+}
+
+#define CK(call)                                                                              \
+  do {                                                                                        \
+    cudaError_t e_ = (call);                                                                  \
+    if (e_ != cudaSuccess) return fail(ctx, GPUMHD_E_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+  } while (0)
+
+static int check_launch(gpumhd_ctx* ctx, int n) {
+  ctx->launches += n;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(ctx, GPUMHD_E_CUDA, "kernel launch: %s", cudaGetErrorString(e));
+  return GPUMHD_OK;
+}
+
+extern "C" int gpumhd_default_params(gpumhd_params* p, int nx, int ny, int nz, double dx) {
+  if (!p) return GPUMHD_E_INVALID;
+  memset(p, 0, sizeof *p);
+  p->nx = nx; p->ny = ny; p->nz = nz;
+  p->periodic_x = 1;
+  p->precision = 64;
+  p->dx[0] = p->dx[1] = p->dx[2] = dx;
+  p->CFL = 0.8; p->CFL_tvd = 0.95; p->dt = 0.0; p->autostep = 1; p->time = 0.0; p->outcad = 0.0;
+  p->grav = 0.0; p->va_max = 1e7; p->va_adjust = 0.0; p->max_fill = 1000.;
+  for (int i = 0; i < 4; i++) { p->tvd_h[i] = 2.0; p->tvd_cs[i] = 0.2; p->tvd_coeff[i] = 1.0; }
+  const double tvd[10] = {1.0e-11, 1.0, 10.0, 0.2, 1.0, 1.0, 1.0, 1.0, 0.75, 100.0};
+  for (int i = 0; i < 10; i++) p->tvd[i] = tvd[i];
+  p->tvd_h_bnd[0] = p->tvd_h_bnd[1] = 1e-6;
+  p->tvd_visc_bnd[0] = p->tvd_visc_bnd[1] = 1.0;
+  p->tvd_eta_bnd[0] = p->tvd_eta_bnd[1] = 1.0;
+  p->tchk[0] = 1.0e11; p->tchk[1] = 1.0e-16; p->tchk[2] = 4.0e15; p->tchk[3] = 100.0e5;
+  p->rt_cfl = 0.5; p->rt_tstep = 0.0; p->rt_update = 1;
+  p->tau0 = 1.0; p->dt_rad = 1e9;
+  return GPUMHD_OK;
+}
+
+static inline double stdmax(double a, double b) { return (a < b) ? b : a; }
+static inline double stdmin(double a, double b) { return (b < a) ? b : a; }
+
+// Run constants derived from the parameters, computed with the host math
+// library exactly as the reference computes them.
+static int fill_consts(gpumhd_ctx* ctx) {
+  const gpumhd_params& p = ctx->p;
+  Consts& c = ctx->c;
+  Geom& g = c.g;
+  g.nx = p.nx; g.ny = p.ny; g.nz = p.nz;
+  g.sx = p.nx + 2 * GH; g.sy = p.ny + 2 * GH; g.sz = p.nz + 2 * GH;
+  g.N = (long long)g.sx * g.sy * g.sz;
+  g.periodic_x = p.periodic_x ? 1 : 0;
+  for (int d = 0; d < 3; d++) {
+    c.dx[d] = p.dx[d];
+    c.w1[d] = 8. / (12. * p.dx[d]);
+    c.w2[d] = -1. / (12. * p.dx[d]);
+    c.idx[d] = 1. / p.dx[d];
+  }
+  c.dxmin = p.dx[0];
+  for (int d = 1; d < 3; d++) c.dxmin = stdmin(c.dxmin, p.dx[d]);
+  c.rho_min = p.tchk[1];
+  c.eps_min = p.tchk[0];
+  c.rho_lev = pow(p.tvd[0], 2);
+  c.rho_log = (int)p.tvd[1];
+  c.q_rho_max = log(p.tvd[2]);
+  c.visc_coeff_bot = stdmin(1.0, p.tvd_visc_bnd[0]);
+  c.visc_slope_bot = stdmax(0.0, p.tvd_visc_bnd[0] - 1.0);
+  c.visc_coeff_top = stdmin(1.0, p.tvd_visc_bnd[1]);
+  c.visc_slope_top = stdmax(0.0, p.tvd_visc_bnd[1] - 1.0);
+  c.eta_coeff_bot = stdmin(1.0, p.tvd_eta_bnd[0]);
+  c.eta_slope_bot = stdmax(0.0, p.tvd_eta_bnd[0] - 1.0);
+  c.eta_coeff_top = stdmin(1.0, p.tvd_eta_bnd[1]);
+  c.eta_slope_top = stdmax(0.0, p.tvd_eta_bnd[1] - 1.0);
+  c.B_par_diff = p.tvd[3]; c.vhyp = p.tvd[4];
+  c.pm_v = p.tvd[6]; c.pm_B = p.tvd[7]; c.vmax_lim = p.tvd[8]; c.CME_thresh = p.tvd[9];
+  for (int i = 0; i < 4; i++) { c.tvd_h[i] = p.tvd_h[i]; c.tvd_cs[i] = p.tvd_cs[i]; c.tvd_coeff[i] = p.tvd_coeff[i]; }
+  c.need_coeff = (p.tvd_coeff[0] * p.tvd_coeff[1] * p.tvd_coeff[2] * p.tvd_coeff[3] != 1.0) ? 1 : 0;
+  c.CZ = (double)(p.tau0 > 1.0e-5);
+  c.tchk_vmax = p.tchk[3];
+  c.tchk_eps_max = p.tchk[2];
+  c.gx = -p.grav;
+  c.rt_cfl = p.rt_cfl;
+  c.CFL = p.CFL; c.CFL_tvd = p.CFL_tvd; c.dt_rad = p.dt_rad; c.rt_tstep = p.rt_tstep; c.outcad = p.outcad;
+  c.va_max = p.va_max; c.va_adjust = p.va_adjust; c.max_fill = p.max_fill;
+  c.autostep = p.autostep;
+  // vertical boundary profiles of TVDlimit (src/tvdlimit_SR.C:132-149)
+  const double h_bnd_bot = p.tvd_h_bnd[0] < 1 ? p.tvd_h_bnd[0] : p.tvd_h_bnd[0] / double(p.nx);
+  const double h_bnd_top = p.tvd_h_bnd[1] < 1 ? p.tvd_h_bnd[1] : p.tvd_h_bnd[1] / double(p.nx);
+  std::vector<double> prof(3 * (size_t)g.sx);
+  const double gxmax0 = p.dx[0] * p.nx;
+  for (int i = 0; i < g.sx; i++) {
+    double hh = (0.0 + (0.5 + (i - GH)) * p.dx[0]) / gxmax0;
+    double vv = stdmax(0.0, 1.0 - 0.5 * (1.0 - hh) / h_bnd_top);
+    prof[g.sx + i] = stdmin(1.0, vv * vv);  // hft
+    vv = stdmax(0.0, 1.0 - 0.5 * hh / h_bnd_bot);
+    prof[i] = stdmin(1.0, vv * vv);          // hfb
+    prof[2 * g.sx + i] = (hh < 1 - 2 * h_bnd_top) ? 1.0 : p.tvd[5];
+  }
+  if (!ctx->d_prof) CK(cudaMalloc(&ctx->d_prof, sizeof(double) * 3 * g.sx));
+  CK(cudaMemcpy(ctx->d_prof, prof.data(), sizeof(double) * 3 * g.sx, cudaMemcpyHostToDevice));
+  c.hfb = ctx->d_prof;
+  c.hft = ctx->d_prof + g.sx;
+  c.qft = ctx->d_prof + 2 * g.sx;
+  return GPUMHD_OK;
+}
+
+// Host restatement of the Adjust_Valf_Max limit update (src/Adjust_Valf_Max.C:83-144)
+// from the five reduced statistics.
+static void adjust_limits(gpumhd_ctx* ctx, const double st[5]) {
+  const gpumhd_params& p = ctx->p;
+  Dyn& d = ctx->hdyn;
+  const double g0 = st[0], g1 = sqrt(st[1]), g2 = st[2];
+  double va_max;
+  if (p.va_adjust > 0.0) {
+    const double cs_fac = 2.0, vv_fac = 3.0, eps_decay = 0.99;
+    if (d.va_ini_flag) {
+      d.v_lim = fmin(g0, p.tchk[3]);
+      d.e_lim = fmin(g2, p.tchk[2]);
+      d.va_max_old = 0.0;
+      d.va_ini_flag = 0;
+    } else {
+      if (st[3] >= 4 * p.max_fill) d.v_lim *= 1.04;
+      else if (st[3] >= p.max_fill) d.v_lim *= 1.01;
+      else if (st[3] < 0.5 * p.max_fill) d.v_lim *= 0.99;
+      if (st[4] >= 4 * p.max_fill) d.e_lim *= 1.04;
+      else if (st[4] >= p.max_fill) d.e_lim *= 1.01;
+      else if (st[4] < 0.5 * p.max_fill) d.e_lim *= 0.99;
+    }
+    va_max = fmax(p.va_max, p.va_adjust * vv_fac * g0);
+    va_max = fmax(va_max, p.va_adjust * cs_fac * g1);
+    va_max = fmax(va_max, d.va_max_old * eps_decay);
+    d.v_lim = fmax(d.v_lim, p.va_max / vv_fac);
+    d.v_lim = fmin(d.v_lim, p.tchk[3]);
+    d.e_lim = fmax(d.e_lim, pow(p.va_max / cs_fac, 2));
+    d.e_lim = fmin(d.e_lim, p.tchk[2]);
+  } else {
+    va_max = p.va_max;
+    d.v_lim = p.tchk[3];
+    d.e_lim = p.tchk[2];
+  }
+  d.inv_va2max = 1.0 / pow(va_max, 2);
+  d.va_max_old = va_max;
+  const double vml = p.tvd[8];
+  d.vsqr_diff = vml < 1.0 ? pow(vml * d.v_lim, 2.0) : pow(vml, 2.0);
+}
+
+static int push_dyn(gpumhd_ctx* ctx) {
+  CK(cudaMemcpyAsync(ctx->dyn, &ctx->hdyn, sizeof(Dyn), cudaMemcpyHostToDevice, ctx->stream));
+  return GPUMHD_OK;
+}
+static int pull_dyn(gpumhd_ctx* ctx) {
+  CK(cudaMemcpyAsync(&ctx->hdyn, ctx->dyn, sizeof(Dyn), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return GPUMHD_OK;
+}
+
+extern "C" int gpumhd_create(const gpumhd_params* p, int device, gpumhd_ctx** out) {
+  gpumhd_ctx* ctx = nullptr;
+  if (!p || !out) return fail(nullptr, GPUMHD_E_INVALID, "null argument");
+  *out = nullptr;
+  if (p->nx < 4 || p->ny < 4 || p->nz < 4) return fail(nullptr, GPUMHD_E_INVALID, "grid must have >= 4 interior cells per dimension");
+  if (p->precision != 64 && p->precision != 32) return fail(nullptr, GPUMHD_E_INVALID, "precision must be 32 or 64");
+  if (!(p->dx[0] > 0 && p->dx[1] > 0 && p->dx[2] > 0)) return fail(nullptr, GPUMHD_E_INVALID, "dx must be positive");
+  ctx = new gpumhd_ctx();
+  ctx->p = *p;
+  ctx->device = device;
+  ctx->f32 = (p->precision == 32);
+  ctx->rsz = ctx->f32 ? 4 : 8;
+  cudaError_t e = cudaSetDevice(device);
+  if (e != cudaSuccess) {
+    fail(nullptr, GPUMHD_E_CUDA, "cudaSetDevice(%d): %s", device, cudaGetErrorString(e));
+    delete ctx;
+    return GPUMHD_E_CUDA;
+  }
+  int rc = GPUMHD_OK;
+  do {
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) { rc = GPUMHD_E_CUDA; break; }
+    e = ctx->f32 ? Launch<float>::setup() : Launch<double>::setup();
+    if (e != cudaSuccess) { rc = fail(ctx, GPUMHD_E_CUDA, "kernel setup: %s", cudaGetErrorString(e)); break; }
+    rc = fill_consts(ctx);
+    if (rc) break;
+    const long long N = ctx->c.g.N;
+    for (int b = 0; b < 3; b++)
+      if (cudaMalloc(&ctx->S[b], 8 * N * ctx->rsz) != cudaSuccess) { rc = GPUMHD_E_NOMEM; break; }
+    if (rc) break;
+    for (int b = 0; b < 2; b++)
+      if (cudaMalloc(&ctx->P[b], N * ctx->rsz) != cudaSuccess) { rc = GPUMHD_E_NOMEM; break; }
+    if (rc) break;
+    if (cudaMalloc(&ctx->dyn, sizeof(Dyn)) != cudaSuccess) { rc = GPUMHD_E_NOMEM; break; }
+    for (int b = 0; b < 3; b++) cudaMemsetAsync(ctx->S[b], 0, 8 * N * ctx->rsz, ctx->stream);
+    for (int b = 0; b < 2; b++) cudaMemsetAsync(ctx->P[b], 0, N * ctx->rsz, ctx->stream);
+    memset(&ctx->hdyn, 0, sizeof(Dyn));
+    ctx->hdyn.dt = p->dt;
+    ctx->hdyn.time = p->time;
+    ctx->hdyn.va_ini_flag = 1;
+    ctx->hdyn.inv_va2max = 1.0 / pow(p->va_max, 2);
+    ctx->hdyn.v_lim = 0.0;
+    ctx->hdyn.e_lim = 0.0;
+    const double vml = p->tvd[8];
+    ctx->hdyn.vsqr_diff = vml < 1.0 ? pow(vml * p->tchk[3], 2.0) : pow(vml, 2.0);
+    rc = push_dyn(ctx);
+    if (rc) break;
+    if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) { rc = GPUMHD_E_CUDA; break; }
+  } while (0);
+  if (rc) {
+    if (rc == GPUMHD_E_NOMEM) fail(nullptr, rc, "device allocation of the grid state failed");
+    else fail(nullptr, rc, "%s", ctx->err[0] ? ctx->err : "context creation failed");
+    gpumhd_destroy(ctx);
+    return rc;
+  }
+  *out = ctx;
+  return GPUMHD_OK;
+}
+
+extern "C" int gpumhd_destroy(gpumhd_ctx* ctx) {
+  if (!ctx) return GPUMHD_OK;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  if (ctx->graph) cudaGraphExecDestroy(ctx->graph);
+  for (void* q : ctx->S) cudaFree(q);
+  for (void* q : ctx->P) cudaFree(q);
+  for (void* q : ctx->aux) cudaFree(q);
+  cudaFree(ctx->T);
+  cudaFree(ctx->staging);
+  cudaFree(ctx->dyn);
+  cudaFree(ctx->dt_hist);
+  cudaFree(ctx->d_xeps);
+  cudaFree(ctx->d_xlr);
+  for (float* q : ctx->d_tab) cudaFree(q);
+  cudaFree(ctx->d_pquad);
+  cudaFree(ctx->d_inv_xeps);
+  cudaFree(ctx->d_inv_xlr);
+  cudaFree(ctx->d_prof);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return GPUMHD_OK;
+}
+
+extern "C" const char* gpumhd_last_error(gpumhd_ctx* ctx) { return ctx ? ctx->err : g_create_err; }
+
+extern "C" int gpumhd_get_params(gpumhd_ctx* ctx, gpumhd_params* p) {
+  if (!ctx || !p) return GPUMHD_E_INVALID;
+  *p = ctx->p;
+  p->dt = ctx->hdyn.dt;
+  p->time = ctx->hdyn.time;
+  return GPUMHD_OK;
+}
+
+extern "C" int gpumhd_set_params(gpumhd_ctx* ctx, const gpumhd_params* p) {
+  if (!ctx || !p) return GPUMHD_E_INVALID;
+  if (p->nx != ctx->p.nx || p->ny != ctx->p.ny || p->nz != ctx->p.nz || p->precision != ctx->p.precision ||
+      (p->periodic_x != 0) != (ctx->p.periodic_x != 0))
+    return fail(ctx, GPUMHD_E_INVALID, "grid shape, boundaries and precision are fixed at creation");
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaStreamSynchronize(ctx->stream));
+  const Consts keep = ctx->c;
+  ctx->p = *p;
+  int rc = fill_consts(ctx);
+  if (rc) return rc;
+  // EOS pointers and values survive a parameter change
+  Consts& c = ctx->c;
+  c.N_eps = keep.N_eps; c.N_lr = keep.N_lr; c.eps_off = keep.eps_off; c.xeps0 = keep.xeps0; c.xlr0 = keep.xlr0;
+  c.xepsN = keep.xepsN; c.xlrN = keep.xlrN; c.inv_del_eps = keep.inv_del_eps; c.inv_del_lr = keep.inv_del_lr;
+  c.eps_max = keep.eps_max; c.xeps = keep.xeps; c.xlr = keep.xlr;
+  for (int t = 0; t < 6; t++) c.tab[t] = keep.tab[t];
+  c.pquad = keep.pquad; c.inv_exp_xeps = keep.inv_exp_xeps; c.inv_exp_xlr = keep.inv_exp_xlr;
+  c.c_pres = keep.c_pres; c.c_temp = keep.c_temp; c.kb = keep.kb; c.mun_mh = keep.mun_mh;
+  ctx->hdyn.dt = p->dt;
+  ctx->hdyn.time = p->time;
+  if (ctx->graph) { cudaGraphExecDestroy(ctx->graph); ctx->graph = nullptr; }
+  return push_dyn(ctx);
+}
+
+// eos_init (src/eos_init.C:57-212): table axes in double from the float header,
+// entries divided by del_eps*del_lr in double and stored as float.
+extern "C" int gpumhd_eos_init(gpumhd_ctx* ctx, const char* path) {
+  if (!ctx || !path) return GPUMHD_E_INVALID;
+  FILE* f = fopen(path, "rb");
+  if (!f) return fail(ctx, GPUMHD_E_EOS, "eos_init: EOS file - %s not found", path);
+  float h[14];
+  if (fread(h, sizeof(float), 14, f) != 14) { fclose(f); return fail(ctx, GPUMHD_E_EOS, "eos_init: short header in %s", path); }
+  const int N_eps = (int)h[0], N_lr = (int)h[1], N_lp3 = (int)h[2], N_s3 = (int)h[3];
+  if (N_eps < 2 || N_lr < 2 || N_eps > 100000 || N_lr > 100000 || N_lp3 < 0 || N_s3 < 0)
+    { fclose(f); return fail(ctx, GPUMHD_E_EOS, "eos_init: bad table sizes in %s", path); }
+  const double eps0 = (double)h[4], eps1 = (double)h[5], lr0 = (double)h[6], lr1 = (double)h[7];
+  const double eps_off = (double)h[12];
+  const double del_eps = (eps1 - eps0) / (double(N_eps - 1));
+  const double del_lr = (lr1 - lr0) / (double(N_lr - 1));
+  std::vector<double> xeps(N_eps), xlr(N_lr);
+  for (int i = 0; i < N_eps; i++) xeps[i] = eps0 + del_eps * ((double)i);
+  for (int i = 0; i < N_lr; i++) xlr[i] = lr0 + del_lr * ((double)i);
+  const size_t n = (size_t)N_eps * N_lr;
+  std::vector<float> buf(6 * n);
+  if (fread(buf.data(), sizeof(float), 6 * n, f) != 6 * n) { fclose(f); return fail(ctx, GPUMHD_E_EOS, "eos_init: truncated tables in %s", path); }
+  fclose(f);
+  std::vector<float> tab(6 * n);
+  const double scale = del_eps * del_lr;
+  for (int t = 0; t < 6; t++)
+    for (int i = 0; i < N_eps; i++)
+      for (int j = 0; j < N_lr; j++)
+        tab[t * n + (size_t)i * N_lr + j] = (float)(((double)buf[t * n + (size_t)j * N_eps + i]) / scale);
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaStreamSynchronize(ctx->stream));
+  cudaFree(ctx->d_xeps); cudaFree(ctx->d_xlr);
+  for (float*& q : ctx->d_tab) { cudaFree(q); q = nullptr; }
+  cudaFree(ctx->d_pquad); cudaFree(ctx->d_inv_xeps); cudaFree(ctx->d_inv_xlr);
+  ctx->d_pquad = nullptr; ctx->d_inv_xeps = nullptr; ctx->d_inv_xlr = nullptr;
+  CK(cudaMalloc(&ctx->d_xeps, sizeof(double) * N_eps));
+  CK(cudaMalloc(&ctx->d_xlr, sizeof(double) * N_lr));
+  CK(cudaMemcpy(ctx->d_xeps, xeps.data(), sizeof(double) * N_eps, cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(ctx->d_xlr, xlr.data(), sizeof(double) * N_lr, cudaMemcpyHostToDevice));
+  for (int t = 0; t < 6; t++) {
+    CK(cudaMalloc(&ctx->d_tab[t], sizeof(float) * n));
+    CK(cudaMemcpy(ctx->d_tab[t], tab.data() + t * n, sizeof(float) * n, cudaMemcpyHostToDevice));
+  }
+  if (ctx->f32) {
+    // pressure patches: ln p = T00 + fe*a/.. re-expanded about the lower corner
+    std::vector<float4> quad(n);
+    for (int i = 0; i < N_eps - 1; i++)
+      for (int j = 0; j < N_lr - 1; j++) {
+        const double T00 = (double)tab[(size_t)i * N_lr + j] * scale;
+        const double T01 = (double)tab[(size_t)i * N_lr + j + 1] * scale;
+        const double T10 = (double)tab[(size_t)(i + 1) * N_lr + j] * scale;
+        const double T11 = (double)tab[(size_t)(i + 1) * N_lr + j + 1] * scale;
+        float4 q;
+        q.x = (float)exp(T00);
+        q.y = (float)((T10 - T00) / del_eps);
+        q.z = (float)((T01 - T00) / del_lr);
+        q.w = (float)((T11 - T10 - T01 + T00) / (del_eps * del_lr));
+        quad[(size_t)i * N_lr + j] = q;
+      }
+    std::vector<float> ie(N_eps), ir(N_lr);
+    for (int i = 0; i < N_eps; i++) ie[i] = (float)exp(-xeps[i]);
+    for (int j = 0; j < N_lr; j++) ir[j] = (float)exp(-xlr[j]);
+    CK(cudaMalloc(&ctx->d_pquad, sizeof(float4) * n));
+    CK(cudaMemcpy(ctx->d_pquad, quad.data(), sizeof(float4) * n, cudaMemcpyHostToDevice));
+    CK(cudaMalloc(&ctx->d_inv_xeps, sizeof(float) * N_eps));
+    CK(cudaMalloc(&ctx->d_inv_xlr, sizeof(float) * N_lr));
+    CK(cudaMemcpy(ctx->d_inv_xeps, ie.data(), sizeof(float) * N_eps, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->d_inv_xlr, ir.data(), sizeof(float) * N_lr, cudaMemcpyHostToDevice));
+  }
+  Consts& c = ctx->c;
+  c.N_eps = N_eps; c.N_lr = N_lr;
+  c.eps_off = eps_off;
+  c.xeps0 = xeps[0]; c.xlr0 = xlr[0]; c.xepsN = xeps[N_eps - 1]; c.xlrN = xlr[N_lr - 1];
+  c.inv_del_eps = 1.0 / del_eps;
+  c.inv_del_lr = 1.0 / del_lr;
+  c.eps_max = exp(xeps[N_eps - 1]) - eps_off;
+  c.xeps = ctx->d_xeps; c.xlr = ctx->d_xlr;
+  for (int t = 0; t < 6; t++) c.tab[t] = ctx->d_tab[t];
+  c.pquad = ctx->d_pquad; c.inv_exp_xeps = ctx->d_inv_xeps; c.inv_exp_xlr = ctx->d_inv_xlr;
+  // ConsToPrim's ideal-gas constants (src/cons_to_prim.C:60-99)
+  volatile double eos_gamma = 1.65, eos_mu = 0.62, eos_mu_n = 1.3, mh = 1.67262158e-24, kb = 1.380622e-16;
+  const double Rgas = 8.314e7;
+  c.c_temp = (eos_gamma - 1.) * eos_mu / Rgas;
+  c.c_pres = (eos_gamma - 1.);
+  c.kb = kb;
+  c.mun_mh = eos_mu_n * mh;
+  ctx->eos_loaded = true;
+  if (ctx->graph) { cudaGraphExecDestroy(ctx->graph); ctx->graph = nullptr; }
+  return GPUMHD_OK;
+}
+
+static void* field_ptr(gpumhd_ctx* ctx, int which, int* nf, int* rc) {
+  *rc = GPUMHD_OK;
+  if (which >= 0 && which <= 2) {
+    *nf = 8;
+    return ctx->S[which == 0 ? ctx->iU : (which == 1 ? ctx->iU0 : ctx->iRes)];
+  }
+  *nf = 1;
+  if (which == 3) return ctx->P[ctx->iP];
+  if (which >= 4 && which <= 7) {
+    void*& a = ctx->aux[which - 4];
+    if (!a) {
+      if (cudaMalloc(&a, ctx->c.g.N * ctx->rsz) != cudaSuccess) { *rc = GPUMHD_E_NOMEM; return nullptr; }
+      cudaMemsetAsync(a, 0, ctx->c.g.N * ctx->rsz, ctx->stream);
+    }
+    return a;
+  }
+  *rc = GPUMHD_E_INVALID;
+  return nullptr;
+}
+
+static int ensure_staging(gpumhd_ctx* ctx) {
+  if (!ctx->staging) CK(cudaMalloc(&ctx->staging, sizeof(double) * 8 * ctx->c.g.N));
+  return GPUMHD_OK;
+}
+
+extern "C" int gpumhd_upload(gpumhd_ctx* ctx, int which, const double* host) {
+  if (!ctx || !host) return GPUMHD_E_INVALID;
+  CK(cudaSetDevice(ctx->device));
+  int nf, rc;
+  void* dst = field_ptr(ctx, which, &nf, &rc);
+  if (rc) return fail(ctx, rc, "upload: bad field %d", which);
+  rc = ensure_staging(ctx);
+  if (rc) return rc;
+  const long long N = ctx->c.g.N;
+  CK(cudaMemcpyAsync(ctx->staging, host, sizeof(double) * nf * N, cudaMemcpyHostToDevice, ctx->stream));
+  if (ctx->f32) Launch<float>::aos_to_soa(N, nf, ctx->staging, (float*)dst, ctx->stream);
+  else Launch<double>::aos_to_soa(N, nf, ctx->staging, (double*)dst, ctx->stream);
+  if (which == 0) ctx->fused_ready = false;
+  if (which == 3) ctx->have_pres = true;
+  return check_launch(ctx, 1);
+}
+
+extern "C" int gpumhd_download(gpumhd_ctx* ctx, int which, double* host) {
+  if (!ctx || !host) return GPUMHD_E_INVALID;
+  CK(cudaSetDevice(ctx->device));
+  int nf, rc;
+  void* src = field_ptr(ctx, which, &nf, &rc);
+  if (rc) return fail(ctx, rc, "download: bad field %d", which);
+  rc = ensure_staging(ctx);
+  if (rc) return rc;
+  const long long N = ctx->c.g.N;
+  if (ctx->f32) Launch<float>::soa_to_aos(N, nf, (const float*)src, ctx->staging, ctx->stream);
+  else Launch<double>::soa_to_aos(N, nf, (const double*)src, ctx->staging, ctx->stream);
+  rc = check_launch(ctx, 1);
+  if (rc) return rc;
+  CK(cudaMemcpyAsync(host, ctx->staging, sizeof(double) * nf * N, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  return GPUMHD_OK;
+}
+
+#define DISPATCH(call_f, call_d) (ctx->f32 ? (call_f) : (call_d))
+
+extern "C" int gpumhd_save_cons(gpumhd_ctx* ctx) {
+  if (!ctx) return GPUMHD_E_INVALID;
+  CK(cudaSetDevice(ctx->device));
+  if (ctx->f32) Launch<float>::save_cons(ctx->c, (const float*)ctx->S[ctx->iU], (float*)ctx->S[ctx->iU0], ctx->stream);
+  else Launch<double>::save_cons(ctx->c, (const double*)ctx->S[ctx->iU], (double*)ctx->S[ctx->iU0], ctx->stream);
+  return check_launch(ctx, 1);
+}
+
+extern "C" int gpumhd_cons_to_prim(gpumhd_ctx* ctx) {
+  if (!ctx) return GPUMHD_E_INVALID;
+  if (!ctx->eos_loaded) return fail(ctx, GPUMHD_E_ORDER, "ConsToPrim before eos_init");
+  CK(cudaSetDevice(ctx->device));
+  int nf, rc;
+  void* a[4];
+  for (int t = 0; t < 4; t++) {
+    a[t] = field_ptr(ctx, 4 + t, &nf, &rc);
+    if (rc) return fail(ctx, rc, "allocation of the EOS output fields failed");
+  }
+  if (ctx->f32)
+    Launch<float>::cons_to_prim(ctx->c, (float*)ctx->S[ctx->iU], (float*)ctx->P[ctx->iP], (float*)a[0], (float*)a[1],
+                                (float*)a[2], (float*)a[3], ctx->stream);
+  else
+    Launch<double>::cons_to_prim(ctx->c, (double*)ctx->S[ctx->iU], (double*)ctx->P[ctx->iP], (double*)a[0],
+                                 (double*)a[1], (double*)a[2], (double*)a[3], ctx->stream);
+  ctx->have_pres = true;
+  ctx->fused_ready = false;
+  return check_launch(ctx, 1);
+}
+
+static int reset_accumulators(gpumhd_ctx* ctx) {
+  ctx->hdyn.cmax_bits = 0;
+  ctx->hdyn.stat_max_bits[0] = ctx->hdyn.stat_max_bits[1] = ctx->hdyn.stat_max_bits[2] = 0;
+  ctx->hdyn.stat_cnt[0] = ctx->hdyn.stat_cnt[1] = 0;
+  return push_dyn(ctx);
+}
+
+static double bits_to_double(unsigned long long b) {
+  double d;
+  memcpy(&d, &b, sizeof d);
+  return d;
+}
+
+extern "C" int gpumhd_adjust_valf_max(gpumhd_ctx* ctx) {
+  if (!ctx) return GPUMHD_E_INVALID;
+  if (!ctx->have_pres) return fail(ctx, GPUMHD_E_ORDER, "Adjust_Valf_Max needs ConsToPrim first");
+  CK(cudaSetDevice(ctx->device));
+  int rc = reset_accumulators(ctx);
+  if (rc) return rc;
+  if (ctx->f32) Launch<float>::adjust_stats(ctx->c, (const float*)ctx->S[ctx->iU], (const float*)ctx->P[ctx->iP], ctx->dyn, ctx->stream);
+  else Launch<double>::adjust_stats(ctx->c, (const double*)ctx->S[ctx->iU], (const double*)ctx->P[ctx->iP], ctx->dyn, ctx->stream);
+  rc = check_launch(ctx, 1);
+  if (rc) return rc;
+  rc = pull_dyn(ctx);
+  if (rc) return rc;
+  double st[5];
+  for (int q = 0; q < 3; q++) st[q] = bits_to_double(ctx->hdyn.stat_max_bits[q]);
+  st[3] = (double)ctx->hdyn.stat_cnt[0];
+  st[4] = (double)ctx->hdyn.stat_cnt[1];
+  adjust_limits(ctx, st);
+  return push_dyn(ctx);
+}
+
+extern "C" int gpumhd_get_limits(gpumhd_ctx* ctx, double* inv_va2max, double* v_lim, double* e_lim) {
+  if (!ctx) return GPUMHD_E_INVALID;
+  if (inv_va2max) *inv_va2max = ctx->hdyn.inv_va2max;
+  if (v_lim) *v_lim = ctx->hdyn.v_lim;
+  if (e_lim) *e_lim = ctx->hdyn.e_lim;
+  return GPUMHD_OK;
+}
+
+extern "C" int gpumhd_mhd_residual(gpumhd_ctx* ctx, double* dt_mhd) {
+  if (!ctx) return GPUMHD_E_INVALID;
+  if (!ctx->have_pres) return fail(ctx, GPUMHD_E_ORDER, "MHD_Residual needs ConsToPrim first");
+  CK(cudaSetDevice(ctx->device));
+  int rc = reset_accumulators(ctx);
+  if (rc) return rc;
+  if (ctx->f32) {
+    Launch<float>::stage(ctx->c, (const float*)ctx->S[ctx->iU], (const float*)ctx->P[ctx->iP], nullptr, nullptr, nullptr,
+                         (float*)ctx->S[ctx->iRes], ctx->dyn, 0, true, 0, ctx->stream);
+    Launch<float>::cmax_faces(ctx->c, (const float*)ctx->S[ctx->iU], (const float*)ctx->P[ctx->iP], ctx->dyn, ctx->stream);
+  } else {
+    Launch<double>::stage(ctx->c, (const double*)ctx->S[ctx->iU], (const double*)ctx->P[ctx->iP], nullptr, nullptr,
+                          nullptr, (double*)ctx->S[ctx->iRes], ctx->dyn, 0, true, 0, ctx->stream);
+    Launch<double>::cmax_faces(ctx->c, (const double*)ctx->S[ctx->iU], (const double*)ctx->P[ctx->iP], ctx->dyn, ctx->stream);
+  }
+  rc = check_launch(ctx, 2);
+  if (rc) return rc;
+  rc = pull_dyn(ctx);
+  if (rc) return rc;
+  const double cmax = bits_to_double(ctx->hdyn.cmax_bits);
+  if (dt_mhd) *dt_mhd = ctx->c.dxmin / cmax;
+  return GPUMHD_OK;
+}
+
+// Sync_timestep (src/solver.C:487-548) for one rank.
+extern "C" int gpumhd_sync_timestep(gpumhd_ctx* ctx, double dt_rad, double dt_mhd, double* cfl) {
+  if (!ctx) return GPUMHD_E_INVALID;
+  const gpumhd_params& p = ctx->p;
+  auto bad = [](double a) { return (a != a) || (a <= 0.) || (a == INFINITY); };
+  double r0 = dt_rad, r1 = dt_mhd;
+  if (bad(r0)) return fail(ctx, GPUMHD_E_BAD_DT, "Invalid time step: dt_rad = %g", r0);
+  if (bad(r1)) return fail(ctx, GPUMHD_E_BAD_DT, "Invalid time step: dt_mhd = %g", r1);
+  const double dt_min_rt = p.rt_tstep * p.CFL * r1;
+  if (r0 < dt_min_rt) r0 = stdmax(r0, dt_min_rt);
+  const double dt_min = stdmin(r0, r1);
+  double dt = stdmin(r0, p.CFL * r1);
+  if (p.outcad > 0) {
+    const double num = ctx->hdyn.time / p.outcad;
+    const int ce = (int)num;
+    const double rem = (num == (double)ce) ? 0.0 : (ce + 1) * p.outcad - ctx->hdyn.time;
+    if (rem > 0.0) dt = stdmin(dt, rem);
+  }
+  if (p.autostep) ctx->hdyn.dt = dt;
+  const double c = ctx->hdyn.dt / dt_min;
+  ctx->hdyn.cfl = c;
+  if (cfl) *cfl = c;
+  if (c >= 2.) return fail(ctx, GPUMHD_E_CFL, "Invalid time step: CFL = %g", c);
+  return push_dyn(ctx);
+}
+
+extern "C" int gpumhd_source_integrate_tcheck(gpumhd_ctx* ctx, int stage) {
+  if (!ctx || stage < 1 || stage > 4) return GPUMHD_E_INVALID;
+  CK(cudaSetDevice(ctx->device));
+  if (ctx->f32)
+    Launch<float>::source_integrate(ctx->c, (float*)ctx->S[ctx->iU], (const float*)ctx->S[ctx->iU0],
+                                    (float*)ctx->S[ctx->iRes], ctx->dyn, stage, ctx->stream);
+  else
+    Launch<double>::source_integrate(ctx->c, (double*)ctx->S[ctx->iU], (const double*)ctx->S[ctx->iU0],
+                                     (double*)ctx->S[ctx->iRes], ctx->dyn, stage, ctx->stream);
+  return check_launch(ctx, 1);
+}
+
+extern "C" int gpumhd_exchange(gpumhd_ctx* ctx, int with_bc) {
+  if (!ctx) return GPUMHD_E_INVALID;
+  CK(cudaSetDevice(ctx->device));
+  if (ctx->f32) Launch<float>::fill_ghosts(ctx->c, (float*)ctx->S[ctx->iU], 8, with_bc, ctx->stream);
+  else Launch<double>::fill_ghosts(ctx->c, (double*)ctx->S[ctx->iU], 8, with_bc, ctx->stream);
+  return check_launch(ctx, 1);
+}
+
+extern "C" int gpumhd_tcheck(gpumhd_ctx* ctx) {
+  if (!ctx) return GPUMHD_E_INVALID;
+  CK(cudaSetDevice(ctx->device));
+  if (ctx->f32) Launch<float>::tcheck(ctx->c, (float*)ctx->S[ctx->iU], ctx->dyn, ctx->stream);
+  else Launch<double>::tcheck(ctx->c, (double*)ctx->S[ctx->iU], ctx->dyn, ctx->stream);
+  return check_launch(ctx, 1);
+}
+
+// TVDlimit: three in-place sweeps; each sweep reads a copy of the state so that
+// pencil chunks never see a neighbour's partial update.
+extern "C" int gpumhd_tvdlimit(gpumhd_ctx* ctx, double dt_tvd) {
+  if (!ctx) return GPUMHD_E_INVALID;
+  if (!ctx->have_pres) return fail(ctx, GPUMHD_E_ORDER, "TVDlimit needs the pressure of a ConsToPrim call");
+  CK(cudaSetDevice(ctx->device));
+  const long long N = ctx->c.g.N;
+  if (!ctx->T) CK(cudaMalloc(&ctx->T, 8 * N * ctx->rsz));
+  ctx->hdyn.dt_tvd = dt_tvd;
+  ctx->hdyn.two_half = 0;
+  int rc = push_dyn(ctx);
+  if (rc) return rc;
+  for (int d = 0; d < 3; d++) {
+    CK(cudaMemcpyAsync(ctx->T, ctx->S[ctx->iU], 8 * N * ctx->rsz, cudaMemcpyDeviceToDevice, ctx->stream));
+    if (ctx->f32)
+      Launch<float>::tvd(ctx->c, d, 0, 0, (const float*)ctx->T, (const float*)ctx->P[ctx->iP], (float*)ctx->S[ctx->iU],
+                         nullptr, ctx->dyn, ctx->stream);
+    else
+      Launch<double>::tvd(ctx->c, d, 0, 0, (const double*)ctx->T, (const double*)ctx->P[ctx->iP],
+                          (double*)ctx->S[ctx->iU], nullptr, ctx->dyn, ctx->stream);
+    rc = check_launch(ctx, 1);
+    if (rc) return rc;
+  }
+  return GPUMHD_OK;
+}
+
+// ------------------------------------------------------------- fused path
+// One fused step: step control, four RK stages, two TVD passes (the second
+// returns at once unless the step takes two half passes).  With ev != NULL an
+// event is recorded before each of the 11 launches and after the last.
+static int enqueue_one_step(gpumhd_ctx* ctx, cudaEvent_t* ev = nullptr) {
+  const Consts& c = ctx->c;
+  cudaStream_t s = ctx->stream;
+  int k = 0;
+  auto mark = [&]() { if (ev) cudaEventRecord(ev[k++], s); };
+  const int a = ctx->iU, b = ctx->iU0, d = ctx->iRes;  // a: state, b and d: work buffers
+  const int pa = ctx->iP, pb = 1 - ctx->iP;
+  mark();
+  k_step_begin<<<1, 32, 0, s>>>(c, ctx->dyn, ctx->dt_hist, ctx->dt_hist_cap);
+  if (ctx->f32) {
+    using L = Launch<float>;
+    float* const* S = (float* const*)ctx->S;
+    float* const* P = (float* const*)ctx->P;
+    mark();
+    L::stage(c, S[a], P[pa], S[a], S[b], P[pb], nullptr, ctx->dyn, 1, false, 1, s);
+    mark();
+    L::stage(c, S[b], P[pb], S[a], S[d], P[pa], nullptr, ctx->dyn, 2, false, 1, s);
+    mark();
+    L::stage(c, S[d], P[pa], S[a], S[b], P[pb], nullptr, ctx->dyn, 3, false, 1, s);
+    mark();
+    L::stage(c, S[b], P[pb], S[a], S[a], nullptr, nullptr, ctx->dyn, 4, false, 0, s);
+    mark();
+    L::tvd(c, 0, 0, 0, S[a], P[pb], S[d], nullptr, ctx->dyn, s);
+    mark();
+    L::tvd(c, 1, 0, 0, S[d], P[pb], S[b], nullptr, ctx->dyn, s);
+    mark();
+    L::tvd(c, 2, 1, 0, S[b], P[pb], S[a], P[pa], ctx->dyn, s);
+    mark();
+    L::tvd(c, 0, 0, 1, S[a], P[pb], S[d], nullptr, ctx->dyn, s);
+    mark();
+    L::tvd(c, 1, 0, 1, S[d], P[pb], S[b], nullptr, ctx->dyn, s);
+    mark();
+    L::tvd(c, 2, 2, 1, S[b], P[pb], S[a], P[pa], ctx->dyn, s);
+  } else {
+    using L = Launch<double>;
+    double* const* S = (double* const*)ctx->S;
+    double* const* P = (double* const*)ctx->P;
+    mark();
+    L::stage(c, S[a], P[pa], S[a], S[b], P[pb], nullptr, ctx->dyn, 1, false, 1, s);
+    mark();
+    L::stage(c, S[b], P[pb], S[a], S[d], P[pa], nullptr, ctx->dyn, 2, false, 1, s);
+    mark();
+    L::stage(c, S[d], P[pa], S[a], S[b], P[pb], nullptr, ctx->dyn, 3, false, 1, s);
+    mark();
+    L::stage(c, S[b], P[pb], S[a], S[a], nullptr, nullptr, ctx->dyn, 4, false, 0, s);
+    mark();
+    L::tvd(c, 0, 0, 0, S[a], P[pb], S[d], nullptr, ctx->dyn, s);
+    mark();
+    L::tvd(c, 1, 0, 0, S[d], P[pb], S[b], nullptr, ctx->dyn, s);
+    mark();
+    L::tvd(c, 2, 1, 0, S[b], P[pb], S[a], P[pa], ctx->dyn, s);
+    mark();
+    L::tvd(c, 0, 0, 1, S[a], P[pb], S[d], nullptr, ctx->dyn, s);
+    mark();
+    L::tvd(c, 1, 0, 1, S[d], P[pb], S[b], nullptr, ctx->dyn, s);
+    mark();
+    L::tvd(c, 2, 2, 1, S[b], P[pb], S[a], P[pa], ctx->dyn, s);
+  }
+    mark();
+  return check_launch(ctx, 11);
+}
+
+static int fused_prepare(gpumhd_ctx* ctx, int nsteps) {
+  if (!ctx->eos_loaded) return fail(ctx, GPUMHD_E_ORDER, "time steps before eos_init");
+  if (ctx->p.va_adjust > 0.0)
+    return fail(ctx, GPUMHD_E_INVALID, "the fused step supports va_adjust = 0; use the per-routine calls");
+  if (nsteps > ctx->dt_hist_cap) {
+    if (ctx->graph) { cudaGraphExecDestroy(ctx->graph); ctx->graph = nullptr; }
+    cudaFree(ctx->dt_hist);
+    ctx->dt_hist = nullptr;
+    int cap = nsteps < 1024 ? 1024 : nsteps;
+    CK(cudaMalloc(&ctx->dt_hist, sizeof(double) * cap));
+    ctx->dt_hist_cap = cap;
+  }
+  if (!ctx->fused_ready) {
+    // exchange + boundaries before the loop (src/solver.C:80-81), then the
+    // pressure, CFL speed and statistics of the initial state
+    int rc0 = pull_dyn(ctx);
+    if (rc0) return rc0;
+    Dyn& d = ctx->hdyn;
+    d.va_ini_flag = 0;
+    d.inv_va2max = 1.0 / pow(ctx->p.va_max, 2);
+    d.v_lim = ctx->p.tchk[3];
+    d.e_lim = ctx->p.tchk[2];
+    const double vml = ctx->p.tvd[8];
+    d.vsqr_diff = vml < 1.0 ? pow(vml * d.v_lim, 2.0) : pow(vml, 2.0);
+    d.err = 0;
+    int rc = reset_accumulators(ctx);
+    if (rc) return rc;
+    if (ctx->f32) {
+      Launch<float>::fill_ghosts(ctx->c, (float*)ctx->S[ctx->iU], 8, 1, ctx->stream);
+      Launch<float>::init_pass(ctx->c, (const float*)ctx->S[ctx->iU], (float*)ctx->P[ctx->iP], ctx->dyn, ctx->stream);
+    } else {
+      Launch<double>::fill_ghosts(ctx->c, (double*)ctx->S[ctx->iU], 8, 1, ctx->stream);
+      Launch<double>::init_pass(ctx->c, (const double*)ctx->S[ctx->iU], (double*)ctx->P[ctx->iP], ctx->dyn, ctx->stream);
+    }
+    rc = check_launch(ctx, 2);
+    if (rc) return rc;
+    ctx->fused_ready = true;
+  }
+  return GPUMHD_OK;
+}
+
+extern "C" int gpumhd_enqueue_steps(gpumhd_ctx* ctx, int nsteps) {
+  if (!ctx || nsteps < 0) return GPUMHD_E_INVALID;
+  CK(cudaSetDevice(ctx->device));
+  int rc = fused_prepare(ctx, nsteps);
+  if (rc) return rc;
+  for (int s = 0; s < nsteps; s++) {
+    if (ctx->graph) {
+      CK(cudaGraphLaunch(ctx->graph, ctx->stream));
+      ctx->launches += 11;
+    } else {
+      rc = enqueue_one_step(ctx);
+      if (rc) return rc;
+    }
+  }
+  // the fused step uses U0 and Res as work space; Res returns to zero as after
+  // Source_Integrate_Tcheck, so per-routine calls can follow
+  if (nsteps > 0) CK(cudaMemsetAsync(ctx->S[ctx->iRes], 0, 8 * ctx->c.g.N * ctx->rsz, ctx->stream));
+  ctx->have_pres = true;
+  return GPUMHD_OK;
+}
+
+static int capture_graph(gpumhd_ctx* ctx) {
+  if (ctx->graph) return GPUMHD_OK;
+  cudaGraph_t g = nullptr;
+  CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+  int rc = enqueue_one_step(ctx);
+  cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
+  if (rc) { if (g) cudaGraphDestroy(g); return rc; }
+  if (e != cudaSuccess) return fail(ctx, GPUMHD_E_CUDA, "graph capture: %s", cudaGetErrorString(e));
+  ctx->launches -= 11;  // capture records, it does not launch
+  e = cudaGraphInstantiate(&ctx->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) { ctx->graph = nullptr; return fail(ctx, GPUMHD_E_CUDA, "graph instantiate: %s", cudaGetErrorString(e)); }
+  return GPUMHD_OK;
+}
+
+extern "C" int gpumhd_synchronize(gpumhd_ctx* ctx) {
+  if (!ctx) return GPUMHD_E_INVALID;
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaStreamSynchronize(ctx->stream));
+  int rc = pull_dyn(ctx);
+  if (rc) return rc;
+  switch (ctx->hdyn.err) {
+    case 0: return GPUMHD_OK;
+    case ERR_BAD_DT_RAD: return fail(ctx, GPUMHD_E_BAD_DT, "Invalid time step: dt_rad");
+    case ERR_BAD_DT_MHD: return fail(ctx, GPUMHD_E_BAD_DT, "Invalid time step: dt_mhd = %g", ctx->hdyn.dt_mhd);
+    case ERR_CFL: return fail(ctx, GPUMHD_E_CFL, "Invalid time step: CFL = %g", ctx->hdyn.cfl);
+    default: return fail(ctx, GPUMHD_E_CUDA, "device error flag %d", ctx->hdyn.err);
+  }
+}
+
+extern "C" int gpumhd_run_steps(gpumhd_ctx* ctx, int nsteps, double* dt_out, int capture) {
+  if (!ctx || nsteps < 0) return GPUMHD_E_INVALID;
+  CK(cudaSetDevice(ctx->device));
+  int rc = fused_prepare(ctx, nsteps);
+  if (rc) return rc;
+  // dt history restarts at this call
+  ctx->hdyn.steps_done = 0;
+  CK(cudaMemcpyAsync(&ctx->dyn->steps_done, &ctx->hdyn.steps_done, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+  if (capture) {
+    rc = capture_graph(ctx);
+    if (rc) return rc;
+  }
+  rc = gpumhd_enqueue_steps(ctx, nsteps);
+  if (rc) return rc;
+  rc = gpumhd_synchronize(ctx);
+  if (rc) return rc;
+  if (dt_out && nsteps > 0)
+    CK(cudaMemcpy(dt_out, ctx->dt_hist, sizeof(double) * nsteps, cudaMemcpyDeviceToHost));
+  return GPUMHD_OK;
+}
+
+extern "C" int gpumhd_profile_steps(gpumhd_ctx* ctx, int nsteps, double* ms_phase) {
+  if (!ctx || nsteps < 1 || !ms_phase) return GPUMHD_E_INVALID;
+  CK(cudaSetDevice(ctx->device));
+  int rc = fused_prepare(ctx, nsteps);
+  if (rc) return rc;
+  cudaEvent_t ev[12];
+  for (int q = 0; q < 12; q++) CK(cudaEventCreate(&ev[q]));
+  for (int q = 0; q < 11; q++) ms_phase[q] = 0.0;
+  for (int st = 0; st < nsteps && rc == 0; st++) {
+    rc = enqueue_one_step(ctx, ev);
+    if (rc) break;
+    if (cudaEventSynchronize(ev[11]) != cudaSuccess) { rc = fail(ctx, GPUMHD_E_CUDA, "event sync failed"); break; }
+    for (int q = 0; q < 11; q++) {
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, ev[q], ev[q + 1]);
+      ms_phase[q] += ms / nsteps;
+    }
+  }
+  for (int q = 0; q < 12; q++) cudaEventDestroy(ev[q]);
+  if (rc) return rc;
+  CK(cudaMemsetAsync(ctx->S[ctx->iRes], 0, 8 * ctx->c.g.N * ctx->rsz, ctx->stream));
+  return gpumhd_synchronize(ctx);
+}
+
+extern "C" int gpumhd_step_info(gpumhd_ctx* ctx, double* dt, double* cfl, double* time, int* tvd_two_half) {
+  if (!ctx) return GPUMHD_E_INVALID;
+  if (dt) *dt = ctx->hdyn.dt;
+  if (cfl) *cfl = ctx->hdyn.cfl;
+  if (time) *time = ctx->hdyn.time;
+  if (tvd_two_half) *tvd_two_half = ctx->hdyn.two_half;
+  return GPUMHD_OK;
+}
+
+extern "C" void* gpumhd_stream(gpumhd_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+extern "C" long long gpumhd_launch_count(gpumhd_ctx* ctx) { return ctx ? ctx->launches : 0; }

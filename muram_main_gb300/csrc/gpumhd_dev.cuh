@@ -1,0 +1,275 @@
+// Device-side data structures and per-cell arithmetic of the MURaM MHD step.
+//
+// Templates take the state type R (double or float).  The FP64 instantiation
+// is compiled without FMA contraction and follows the reference's operation
+// order term by term, so that it rounds like the reference's CPU build; the
+// FP32 instantiation uses the same formulas in float (with contraction) and
+// an interpolation form of the pressure lookup that keeps float accuracy.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace gpumhd {
+
+constexpr int NV = 8;   // rho, M_x, M_y, M_z, e, B_x, B_y, B_z
+constexpr int GH = 2;   // ghost layers
+
+struct Geom {
+  int nx, ny, nz;       // interior
+  int sx, sy, sz;       // with ghosts
+  long long N;          // sx*sy*sz
+  int periodic_x;
+  int pad;
+};
+
+// Constants of a run (copied by value into every kernel).
+struct Consts {
+  Geom g;
+  double dx[3], w1[3], w2[3], idx[3], dxmin;
+  // EOS (src/eos_init.C:57-212)
+  int N_eps, N_lr;
+  double eps_off, xeps0, xlr0, xepsN, xlrN, inv_del_eps, inv_del_lr, eps_max;
+  const double* xeps;
+  const double* xlr;
+  const float* tab[6];         // [i_eps*N_lr + j_rho], divided by del_eps*del_lr
+  const float4* pquad;         // FP32 pressure patches {exp(T00), a, b, c}
+  const float* inv_exp_xeps;   // exp(-xeps[i])
+  const float* inv_exp_xlr;    // exp(-xlr[j])
+  double c_pres, c_temp, kb, mun_mh;
+  // TVD (src/tvdlimit_SR.C:41-205)
+  double rho_min, eps_min, rho_lev, q_rho_max;
+  int rho_log, need_coeff;
+  double visc_coeff_bot, visc_slope_bot, visc_coeff_top, visc_slope_top;
+  double eta_coeff_bot, eta_slope_bot, eta_coeff_top, eta_slope_top;
+  double B_par_diff, vhyp, pm_v, pm_B, vmax_lim, CME_thresh;
+  double tvd_h[4], tvd_cs[4], tvd_coeff[4];
+  double CZ;                   // (double)(Tau > 1e-5) for the constant optical depth
+  const double* hfb;           // vertical boundary profiles, length sx
+  const double* hft;
+  const double* qft;
+  // Tcheck and sources
+  double tchk_vmax, tchk_eps_max;
+  double gx;                   // PhysicsData::g[0] = -grav
+  double rt_cfl;
+  double CFL, CFL_tvd, dt_rad, rt_tstep, outcad;
+  double va_max, va_adjust, max_fill;
+  int autostep;
+  int pad2;
+};
+
+// Values that change during a run; live in device memory.
+struct Dyn {
+  double dt, cfl, time;
+  double inv_va2max, v_lim, e_lim, va_max_old;
+  int va_ini_flag, two_half, err, steps_done;
+  double dt_tvd;
+  double vsqr_diff;     // pow(vmax_lim*v_lim, 2) or pow(vmax_lim, 2), from the host (src/tvdlimit_SR.C:194-197)
+  // accumulators of the last reduction pass
+  unsigned long long cmax_bits;
+  unsigned long long stat_max_bits[3];
+  unsigned long long stat_cnt[2];
+  double dt_mhd;
+};
+
+enum { ERR_BAD_DT_RAD = 1, ERR_BAD_DT_MHD = 2, ERR_CFL = 3 };
+
+// ---------------------------------------------------------------- helpers
+// std::max / std::min semantics: the first argument wins ties and NaNs.
+template <class R> __device__ __forceinline__ R smax(R a, R b) { return (a < b) ? b : a; }
+template <class R> __device__ __forceinline__ R smin(R a, R b) { return (b < a) ? b : a; }
+
+// The reference's 1e-100 floors; float cannot hold 1e-100, so FP32 uses 1e-30.
+template <class R> __device__ __forceinline__ R tiny100();
+template <> __device__ __forceinline__ double tiny100<double>() { return 1e-100; }
+template <> __device__ __forceinline__ float tiny100<float>() { return 1e-30f; }
+
+__device__ __forceinline__ double d_log(double x) { return log(x); }
+__device__ __forceinline__ float d_log(float x) { return logf(x); }
+__device__ __forceinline__ double d_exp(double x) { return exp(x); }
+__device__ __forceinline__ float d_exp(float x) { return expf(x); }
+__device__ __forceinline__ double d_sqrt(double x) { return sqrt(x); }
+__device__ __forceinline__ float d_sqrt(float x) { return sqrtf(x); }
+__device__ __forceinline__ double d_fmax(double a, double b) { return fmax(a, b); }
+__device__ __forceinline__ float d_fmax(float a, float b) { return fmaxf(a, b); }
+__device__ __forceinline__ double d_fmin(double a, double b) { return fmin(a, b); }
+__device__ __forceinline__ float d_fmin(float a, float b) { return fminf(a, b); }
+__device__ __forceinline__ double d_fabs(double a) { return fabs(a); }
+__device__ __forceinline__ float d_fabs(float a) { return fabsf(a); }
+
+// Double -> int conversion as x86-64 performs it for the reference's (int)
+// casts: out-of-range and NaN give INT_MIN.
+__device__ __forceinline__ int cvt_x86(double x) {
+  return (x >= -2147483648.0 && x < 2147483648.0) ? (int)x : (int)0x80000000;
+}
+
+__device__ __forceinline__ bool bad_pos(double a) { return (a != a) || (a <= 0.) || (a == (double)INFINITY); }
+
+__device__ __forceinline__ long long cidx(const Geom& g, int i, int j, int k) {
+  return (long long)i + (long long)g.sx * ((long long)j + (long long)g.sy * (long long)k);
+}
+
+// Order-preserving bits for non-negative doubles (cmax, maxima); NaN never stored.
+__device__ __forceinline__ void atomic_max_nonneg(unsigned long long* dst, double v) {
+  if (v == v && v > 0.0) atomicMax(dst, (unsigned long long)__double_as_longlong(v));
+}
+
+template <class R>
+__device__ __forceinline__ R warp_max_nonnan(R v) {
+  // NaN-ignoring maximum across the warp (values >= 0)
+  for (int o = 16; o > 0; o >>= 1) {
+    R w = __shfl_xor_sync(0xffffffffu, v, o);
+    v = (v < w) ? w : v;   // NaN in w is never taken; NaN in v is replaced by any w
+    if (v != v) v = w;
+  }
+  return v;
+}
+
+// ------------------------------------------------------------------- EOS
+struct C2POut {
+  double pres, temp, ne, rhoi, amb;
+};
+
+// Full ConsToPrim arithmetic for one cell given primitives (src/cons_to_prim.C:148-243).
+__device__ inline C2POut c2p_eos_full(const Consts& c, double d, double ei, double dn) {
+  const double eps = ei * dn + c.eps_off;
+  const double lgr = log(d);
+  const double ep = log(eps);
+  const double lr = lgr;
+  int i_d = cvt_x86((lr - c.xlr0) * c.inv_del_lr);
+  i_d = max(0, i_d);
+  i_d = min(c.N_lr - 2, i_d);
+  int i_e = cvt_x86((ep - c.xeps0) * c.inv_del_eps);
+  i_e = max(0, i_e);
+  i_e = min(c.N_eps - 2, i_e);
+  const double xe0 = c.xeps[i_e], xe1 = c.xeps[i_e + 1];
+  const double xr0 = c.xlr[i_d], xr1 = c.xlr[i_d + 1];
+  const double c0 = (ep - xe0) * (lr - xr0);
+  const double c1 = (ep - xe0) * (xr1 - lr);
+  const double c2 = (xe1 - ep) * (lr - xr0);
+  const double c3 = (xe1 - ep) * (xr1 - lr);
+  const long long a11 = (long long)(i_e + 1) * c.N_lr + (i_d + 1);
+  const long long a10 = (long long)(i_e + 1) * c.N_lr + i_d;
+  const long long a01 = (long long)i_e * c.N_lr + (i_d + 1);
+  const long long a00 = (long long)i_e * c.N_lr + i_d;
+  double out[6];
+#pragma unroll
+  for (int t = 0; t < 6; t++) {
+    if (t == 2) { out[t] = 0.0; continue; }
+    const float* T = c.tab[t];
+    double s = c0 * (double)T[a11];
+    s += c1 * (double)T[a10];
+    s += c2 * (double)T[a01];
+    s += c3 * (double)T[a00];
+    out[t] = exp(s);
+  }
+  double pr = out[0], tm = out[1], nl = out[3];
+  if (lgr < c.xlr0) {
+    pr = c.c_pres * ei;
+    tm = c.c_temp * eps;
+    nl = pr / (tm * c.kb) - d / c.mun_mh;
+  }
+  if (eps > 0.8 * c.eps_max) {
+    double xx = smax(0.0, 5.0 * (c.eps_max - eps) / c.eps_max);
+    pr = pr * xx + (1.0 - xx) * c.c_pres * ei;
+    tm = tm * xx + (1.0 - xx) * c.c_temp * eps;
+    nl = pr / (tm * c.kb) - d / c.mun_mh;
+  }
+  if (bad_pos(pr) || bad_pos(tm)) {
+    pr = c.c_pres * ei;
+    tm = c.c_temp * eps;
+  }
+  if (nl == (double)INFINITY) nl = pr / (tm * c.kb) - d / c.mun_mh;
+  if ((nl < 1.0) || (nl != nl) || (nl == (double)INFINITY)) nl = 1.0;
+  C2POut o;
+  o.pres = pr; o.temp = tm; o.ne = nl; o.rhoi = out[4]; o.amb = out[5];
+  return o;
+}
+
+// Pressure only, FP64.  Inside the table (and away from the high-eps blend)
+// none of ConsToPrim's fallbacks can fire, so the result is exp() of the
+// bilinear sum; elsewhere the full routine decides.
+__device__ __forceinline__ double eos_pres(const Consts& c, double d, double ei, double dn) {
+  const double eps = ei * dn + c.eps_off;
+  const double lgr = log(d);
+  const double ep = log(eps);
+  if (!(lgr >= c.xlr0 && lgr < c.xlrN + 1.0 && ep > c.xeps0 - 1.0 && ep < c.xepsN + 1.0 &&
+        !(eps > 0.8 * c.eps_max)))
+    return c2p_eos_full(c, d, ei, dn).pres;
+  const double lr = lgr;
+  int i_d = (int)((lr - c.xlr0) * c.inv_del_lr);
+  i_d = max(0, i_d);
+  i_d = min(c.N_lr - 2, i_d);
+  int i_e = (int)((ep - c.xeps0) * c.inv_del_eps);
+  i_e = max(0, i_e);
+  i_e = min(c.N_eps - 2, i_e);
+  const double xe0 = __ldg(c.xeps + i_e), xe1 = __ldg(c.xeps + i_e + 1);
+  const double xr0 = __ldg(c.xlr + i_d), xr1 = __ldg(c.xlr + i_d + 1);
+  const double c0 = (ep - xe0) * (lr - xr0);
+  const double c1 = (ep - xe0) * (xr1 - lr);
+  const double c2 = (xe1 - ep) * (lr - xr0);
+  const double c3 = (xe1 - ep) * (xr1 - lr);
+  const float* T = c.tab[0];
+  const long long r1 = (long long)(i_e + 1) * c.N_lr + i_d;
+  const long long r0 = (long long)i_e * c.N_lr + i_d;
+  double s = c0 * (double)__ldg(T + r1 + 1);
+  s += c1 * (double)__ldg(T + r1);
+  s += c2 * (double)__ldg(T + r0 + 1);
+  s += c3 * (double)__ldg(T + r0);
+  return exp(s);
+}
+
+// Pressure only, FP32.  The bilinear patch of ln p is re-expanded around its
+// lower corner, p = P00 * exp(fe*a + fr*b + fe*fr*c), with the offsets
+// fe = ln(eps) - xeps[i] and fr = ln(rho) - xlr[j] taken as logs of ratios
+// near one; this keeps ~1e-7 relative accuracy where the direct float sum of
+// the pre-divided table terms would lose ~1e-6.
+__device__ __forceinline__ float eos_pres(const Consts& c, float d, float ei, float dn) {
+  const float eps = ei * dn + (float)c.eps_off;
+  const float lgr = logf(d);
+  const float ep = logf(eps);
+  if (!(lgr >= (float)c.xlr0 && lgr < (float)c.xlrN + 1.0f && ep > (float)c.xeps0 - 1.0f &&
+        ep < (float)c.xepsN + 1.0f && !(eps > 0.8f * (float)c.eps_max)))
+    return (float)c2p_eos_full(c, (double)d, (double)ei, 1.0 / (double)d).pres;
+  int i_d = (int)((lgr - (float)c.xlr0) * (float)c.inv_del_lr);
+  i_d = max(0, min(c.N_lr - 2, i_d));
+  int i_e = (int)((ep - (float)c.xeps0) * (float)c.inv_del_eps);
+  i_e = max(0, min(c.N_eps - 2, i_e));
+  const float fe = logf(eps * __ldg(c.inv_exp_xeps + i_e));
+  const float fr = logf(d * __ldg(c.inv_exp_xlr + i_d));
+  const float4 q = __ldg(c.pquad + (long long)i_e * c.N_lr + i_d);
+  return q.x * expf(fe * q.y + fr * q.z + fe * fr * q.w);
+}
+
+// ------------------------------------------------------------ Tcheck cell
+// src/Add_Sources_Integrate_SR.C:444-465 and :600-617
+template <class R>
+__device__ __forceinline__ void tcheck_cell(const Consts& c, R vmax, R eps_max, R& d, R& m1, R& m2, R& m3, R& e) {
+  const R rho_min = (R)c.rho_min, eps_min = (R)c.eps_min;
+  R dn = d_fmax(rho_min, d);
+  R vv = d_sqrt(m1 * m1 + m2 * m2 + m3 * m3) / dn;
+  R s = vmax / d_fmax(vmax, vv);
+  R ekin = (R)0.5 * dn * vv * vv;
+  R lo = eps_min * dn + ekin * s * s;
+  R up = eps_max * dn + ekin * s * s;
+  e = d_fmin(d_fmax(e, lo), up);
+  d = dn;
+  m1 *= s;
+  m2 *= s;
+  m3 *= s;
+}
+
+// Characteristic speed of MHD_Residual's CFL condition (src/mhdres_SR.C:310-328)
+template <class R>
+__device__ __forceinline__ R cmax_cell(R d, R v1, R v2, R v3, R b1, R b2, R b3, R p, R inv_va2max) {
+  R dn = (R)1.0 / d;
+  R vv = v1 * v1 + v2 * v2 + v3 * v3;
+  R bb = b1 * b1 + b2 * b2 + b3 * b3;
+  R va2 = bb * dn;
+  R x2 = va2 * inv_va2max, x4 = x2 * x2, s = (R)1.0 + x2;
+  R lf = s / (s + x4);
+  R cs2 = (R)(5.0 / 3.0) * p * dn;
+  vv = d_sqrt(vv);
+  return vv + (R)0.0 + d_sqrt(smax(cs2, lf * (cs2 + va2)));
+}
+
+}  // namespace gpumhd

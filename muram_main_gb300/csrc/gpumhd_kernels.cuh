@@ -1,0 +1,886 @@
+// Kernels of the MURaM MHD time step (templated on the state type R).
+//
+//  k_stage      one RK stage: residual (MHD_Residual), sources, Boris
+//               correction, update and Tcheck (Source_Integrate_Tcheck), and
+//               the next stage's pressure (ConsToPrim), in one pass; or, in
+//               residual mode, MHD_Residual alone (Res += residual).
+//  k_tvd_sweep  one directional TVDlimit sweep; the last sweep of a step
+//               also applies TCheck, the ghost fill and the next step's
+//               pressure, CFL speed and Adjust_Valf_Max statistics.
+//  small kernels: ConsToPrim, Adjust_Valf_Max statistics, Source_Integrate,
+//               SaveCons, TCheck, ghost fill, layout conversion, step control.
+#pragma once
+#include "gpumhd_dev.cuh"
+
+namespace gpumhd {
+
+// ----------------------------------------------------------- ghost images
+// Every interior cell within two cells of a face has a ghost image across it:
+// periodic dimensions copy, the closed x dimension mirrors (M_x, B_y, B_z
+// change sign).  xmirror = 0 restricts the images to the periodic dimensions
+// (the exchange between TVD half steps does not apply the x boundary rule).
+struct Images {
+  int n;
+  long long idx[8];
+  unsigned char flip[8];
+};
+
+__device__ __forceinline__ Images images_of(const Geom& g, int i, int j, int k, bool xmirror) {
+  int xs[2], ys[2], zs[2];
+  unsigned char xf[2] = {0, 0};
+  int nxo = 1, nyo = 1, nzo = 1;
+  xs[0] = i; ys[0] = j; zs[0] = k;
+  const int I = i - GH, J = j - GH, K = k - GH;
+  if (g.periodic_x) {
+    if (I < GH) xs[nxo++] = i + g.nx;
+    else if (I >= g.nx - GH) xs[nxo++] = i - g.nx;
+  } else if (xmirror) {
+    if (I < GH) { xs[nxo] = 2 * GH - 1 - i; xf[nxo++] = 1; }
+    else if (I >= g.nx - GH) { xs[nxo] = 2 * GH + 2 * g.nx - 1 - i; xf[nxo++] = 1; }
+  }
+  if (J < GH) ys[nyo++] = j + g.ny;
+  else if (J >= g.ny - GH) ys[nyo++] = j - g.ny;
+  if (K < GH) zs[nzo++] = k + g.nz;
+  else if (K >= g.nz - GH) zs[nzo++] = k - g.nz;
+  Images im;
+  im.n = 0;
+  for (int c = 0; c < nzo; c++)
+    for (int b = 0; b < nyo; b++)
+      for (int a = 0; a < nxo; a++) {
+        im.idx[im.n] = cidx(g, xs[a], ys[b], zs[c]);
+        im.flip[im.n] = xf[a];
+        im.n++;
+      }
+  return im;
+}
+
+template <class R>
+__device__ __forceinline__ void store_state(const Geom& g, R* __restrict__ U, const Images& im, const R v[NV]) {
+  for (int m = 0; m < im.n; m++) {
+    const long long id = im.idx[m];
+    const bool f = im.flip[m];
+#pragma unroll
+    for (int q = 0; q < NV; q++) {
+      R x = v[q];
+      if (f && (q == 1 || q == 6 || q == 7)) x = -x;
+      U[(long long)q * g.N + id] = x;
+    }
+  }
+}
+
+// -------------------------------------------------------------- primitives
+// 11 per-cell values the residual's fluxes need.
+enum { P_D, P_V1, P_V2, P_V3, P_EI, P_B1, P_B2, P_B3, P_P, P_EK, P_PM, NPRIM };
+
+// From conserved variables as ConsToPrim forms them (src/cons_to_prim.C:148-159),
+// then the residual's kinetic and magnetic pressure terms (src/mhdres_SR.C:310-317).
+template <class R>
+__device__ __forceinline__ void prim_from_cons(R d, R m1, R m2, R m3, R e, R& v1, R& v2, R& v3, R& ei) {
+  R dn = (R)1.0 / d;
+  v1 = m1 * dn;
+  v2 = m2 * dn;
+  v3 = m3 * dn;
+  R vv = v1 * v1 + v2 * v2 + v3 * v3;
+  ei = e - (R)0.5 * vv * d;
+}
+
+template <class R, bool PRIM_IN>
+__device__ __forceinline__ void load_prim11(const Geom& g, const R* __restrict__ U, const R* __restrict__ P,
+                                            long long id, R* out, int stride) {
+  R d = U[id];
+  R a1 = U[g.N + id], a2 = U[2 * g.N + id], a3 = U[3 * g.N + id], a4 = U[4 * g.N + id];
+  R b1 = U[5 * g.N + id], b2 = U[6 * g.N + id], b3 = U[7 * g.N + id];
+  R v1, v2, v3, ei;
+  if (PRIM_IN) { v1 = a1; v2 = a2; v3 = a3; ei = a4; }
+  else prim_from_cons(d, a1, a2, a3, a4, v1, v2, v3, ei);
+  R vv = v1 * v1 + v2 * v2 + v3 * v3;
+  R bb = b1 * b1 + b2 * b2 + b3 * b3;
+  out[P_D * stride] = d;
+  out[P_V1 * stride] = v1;
+  out[P_V2 * stride] = v2;
+  out[P_V3 * stride] = v3;
+  out[P_EI * stride] = ei;
+  out[P_B1 * stride] = b1;
+  out[P_B2 * stride] = b2;
+  out[P_B3 * stride] = b3;
+  out[P_P * stride] = P[id];
+  out[P_EK * stride] = (R)0.5 * d * vv;
+  out[P_PM * stride] = (R)0.5 * bb;
+}
+
+// The 12 directional quantities whose 4th-order derivative the residual takes
+// along D1 (src/mhdres_SR.C:330-347): F0..F4, the two induction fluxes other
+// than component D1 (which is identically zero), the Maxwell stress (3), and
+// B along the two other directions (for curl B x B).
+template <int D1> struct Dirs;
+template <> struct Dirs<0> { static constexpr int d2 = 1, d3 = 2, fa = 6, fb = 7; };
+template <> struct Dirs<1> { static constexpr int d2 = 0, d3 = 2, fa = 5, fb = 7; };
+template <> struct Dirs<2> { static constexpr int d2 = 0, d3 = 1, fa = 5, fb = 6; };
+constexpr int NF = 12;
+
+template <class R, int D1>
+__device__ __forceinline__ void flux12(const R* p, int s, R* f, int fs) {
+  const R d = p[P_D * s], v1 = p[P_V1 * s], v2 = p[P_V2 * s], v3 = p[P_V3 * s];
+  const R ei = p[P_EI * s], b1 = p[P_B1 * s], b2 = p[P_B2 * s], b3 = p[P_B3 * s];
+  const R pr = p[P_P * s], ekin = p[P_EK * s], pmag = p[P_PM * s];
+  const R vel = D1 == 0 ? v1 : (D1 == 1 ? v2 : v3);
+  const R mag = D1 == 0 ? b1 : (D1 == 1 ? b2 : b3);
+  const R p1 = D1 == 0 ? (R)1.0 : (R)0.0, p2 = D1 == 1 ? (R)1.0 : (R)0.0, p3 = D1 == 2 ? (R)1.0 : (R)0.0;
+  const R mflx = vel * d;
+  f[0 * fs] = mflx;
+  f[1 * fs] = mflx * v1 + p1 * pr;
+  f[2 * fs] = mflx * v2 + p2 * pr;
+  f[3 * fs] = mflx * v3 + p3 * pr;
+  f[4 * fs] = vel * (ei + ekin + pr);
+  const R F5 = vel * b1 - v1 * mag, F6 = vel * b2 - v2 * mag, F7 = vel * b3 - v3 * mag;
+  f[5 * fs] = Dirs<D1>::fa == 5 ? F5 : F6;
+  f[6 * fs] = Dirs<D1>::fb == 7 ? F7 : F6;
+  f[7 * fs] = mag * b1 - p1 * pmag;
+  f[8 * fs] = mag * b2 - p2 * pmag;
+  f[9 * fs] = mag * b3 - p3 * pmag;
+  f[10 * fs] = Dirs<D1>::d2 == 0 ? b1 : b2;
+  f[11 * fs] = Dirs<D1>::d3 == 1 ? b2 : b3;
+}
+
+// One direction's contribution (src/mhdres_SR.C:361-412) added to R in place:
+// res = 0 - D(F); res[1..3] += Lorentz; res[4] += v . Lorentz; R += res.
+// fm2..fp2 point at the 12 quantities of cells c-2, c-1, c+1, c+2 (stride fs).
+template <class R, int D1>
+__device__ __forceinline__ void add_direction(R* Racc, const R* fm2, const R* fm1, const R* fp1, const R* fp2, int fs,
+                                              R w1, R w2, const R* cen, R lf) {
+  R Dq[NF];
+#pragma unroll
+  for (int q = 0; q < NF; q++) Dq[q] = w1 * (fp1[q * fs] - fm1[q * fs]) + w2 * (fp2[q * fs] - fm2[q * fs]);
+  R res[NV];
+  res[0] = (R)0.0 - Dq[0];
+  res[1] = (R)0.0 - Dq[1];
+  res[2] = (R)0.0 - Dq[2];
+  res[3] = (R)0.0 - Dq[3];
+  res[4] = (R)0.0 - Dq[4];
+  res[5] = (R)0.0;
+  res[6] = (R)0.0;
+  res[7] = (R)0.0;
+  res[Dirs<D1>::fa] = (R)0.0 - Dq[5];
+  res[Dirs<D1>::fb] = (R)0.0 - Dq[6];
+  const R dB2 = Dq[10], dB3 = Dq[11];
+  const R Bd1 = cen[P_B1 + D1];
+  const R Bd2 = cen[P_B1 + Dirs<D1>::d2], Bd3 = cen[P_B1 + Dirs<D1>::d3];
+  R cbb[3];
+  cbb[D1] = -Bd2 * dB2 - Bd3 * dB3;
+  cbb[Dirs<D1>::d2] = Bd1 * dB2;
+  cbb[Dirs<D1>::d3] = Bd1 * dB3;
+  const R lrt0 = lf * Dq[7] + ((R)1.0 - lf) * cbb[0];
+  const R lrt1 = lf * Dq[8] + ((R)1.0 - lf) * cbb[1];
+  const R lrt2 = lf * Dq[9] + ((R)1.0 - lf) * cbb[2];
+  res[1] += lrt0;
+  res[2] += lrt1;
+  res[3] += lrt2;
+  res[4] += cen[P_V1] * lrt0 + cen[P_V2] * lrt1 + cen[P_V3] * lrt2;
+#pragma unroll
+  for (int q = 0; q < NV; q++) Racc[q] += res[q];
+}
+
+// ------------------------------------------------------------ stage kernel
+template <int TX, int TY>
+struct StageSmem {
+  static constexpr int PW = TX + 4, PH = TY + 4;
+  static constexpr int NPP = PW * PH;
+  static constexpr int FBN = (PW * TY > TX * PH) ? PW * TY : TX * PH;
+  static constexpr int NZ = TX * TY;
+  template <class R>
+  static constexpr size_t bytes() { return sizeof(R) * ((size_t)NPRIM * NPP + (size_t)NF * FBN + (size_t)5 * NF * NZ); }
+};
+
+// RESID = false: fused RK stage.  Uin: conserved state with filled ghosts,
+//   Pin: its pressure (ghosts included), U0: the step's initial state,
+//   Uout/Pout: the new state and its pressure (interior and ghost images).
+// RESID = true: MHD_Residual.  Uin holds primitives (after ConsToPrim),
+//   Res += residual over the interior, dyn->cmax_bits gets the interior CFL speed.
+template <class R, int TX, int TY, bool RESID>
+__global__ void __launch_bounds__(TX* TY) k_stage(Consts c, const R* __restrict__ Uin, const R* __restrict__ Pin,
+                                                  const R* __restrict__ U0, R* __restrict__ Uout,
+                                                  R* __restrict__ Pout, R* __restrict__ Res, Dyn* __restrict__ dyn,
+                                                  int stage, int zc, int write_pres) {
+  using S = StageSmem<TX, TY>;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  R* PP = reinterpret_cast<R*>(smem_raw);
+  R* FB = PP + NPRIM * S::NPP;
+  R* FZ = FB + NF * S::FBN;
+  const Geom& g = c.g;
+  if (!RESID && dyn->err) return;
+  const int tid = threadIdx.x;
+  const int tx = tid % TX, ty = tid / TX;
+  const int x0 = GH + blockIdx.x * TX, y0 = GH + blockIdx.y * TY;
+  const int zb = GH + blockIdx.z * zc;
+  const int ze = min(zb + zc, GH + g.nz);
+  const int i = x0 + tx, j = y0 + ty;
+  const bool active = (i < GH + g.nx) && (j < GH + g.ny);
+  const R inv_va2max = (R)dyn->inv_va2max;
+  const R w1x = (R)c.w1[0], w2x = (R)c.w2[0], w1y = (R)c.w1[1], w2y = (R)c.w2[1], w1z = (R)c.w1[2], w2z = (R)c.w2[2];
+  R prim[NPRIM];
+
+  // z-flux ring: slot of plane kk is (kk - zb + 2) mod 5
+  auto zslot = [&](int kk) { return ((kk - zb + 2) % 5 + 5) % 5; };
+  auto fill_z = [&](int kk) {
+    if (!active) return;
+    load_prim11<R, RESID>(g, Uin, Pin, cidx(g, i, j, kk), prim, 1);
+    flux12<R, 2>(prim, 1, FZ + (size_t)zslot(kk) * NF * S::NZ + tid, S::NZ);
+  };
+  for (int kk = zb - 2; kk < zb + 2; kk++) fill_z(kk);
+
+  for (int k = zb; k < ze; k++) {
+    fill_z(k + 2);
+    // center plane primitives over the cross-shaped halo
+    const int ncross = S::PW * TY + 4 * TX;
+    for (int m = tid; m < ncross; m += TX * TY) {
+      int lx, ly;
+      if (m < S::PW * TY) { lx = m % S::PW - 2; ly = m / S::PW; }
+      else { int r = m - S::PW * TY; lx = r % TX; int q = r / TX; ly = q < 2 ? q - 2 : TY + q - 2; }
+      const int gi = x0 + lx, gj = y0 + ly;
+      R* dst = PP + (ly + 2) * S::PW + (lx + 2);
+      if (gi >= 0 && gi < g.sx && gj >= 0 && gj < g.sy)
+        load_prim11<R, RESID>(g, Uin, Pin, cidx(g, gi, gj, k), dst, S::NPP);
+      else
+        for (int q = 0; q < NPRIM; q++) dst[q * S::NPP] = (R)1.0;
+    }
+    __syncthreads();
+    // x fluxes on (TX+4) x TY
+    for (int m = tid; m < S::PW * TY; m += TX * TY) {
+      const int lx = m % S::PW, ly = m / S::PW;
+      flux12<R, 0>(PP + (ly + 2) * S::PW + lx, S::NPP, FB + ly * S::PW + lx, S::FBN);
+    }
+    __syncthreads();
+    R Racc[NV];
+    R cen[NPRIM];
+    R lf = (R)0;
+    const int pc = (ty + 2) * S::PW + (tx + 2);
+    if (active) {
+#pragma unroll
+      for (int q = 0; q < NPRIM; q++) cen[q] = PP[q * S::NPP + pc];
+      const long long id = cidx(g, i, j, k);
+      if (RESID) {
+#pragma unroll
+        for (int q = 0; q < NV; q++) Racc[q] = Res[(long long)q * g.N + id];
+      } else {
+#pragma unroll
+        for (int q = 0; q < NV; q++) Racc[q] = (R)0.0;
+      }
+      // Boris factor at the cell (src/mhdres_SR.C:310-323)
+      const R dn = (R)1.0 / cen[P_D];
+      const R bb = cen[P_B1] * cen[P_B1] + cen[P_B2] * cen[P_B2] + cen[P_B3] * cen[P_B3];
+      const R va2 = bb * dn;
+      const R x2 = va2 * inv_va2max, x4 = x2 * x2, s = (R)1.0 + x2;
+      lf = s / (s + x4);
+      const R* fb = FB + ty * S::PW + (tx + 2);
+      add_direction<R, 0>(Racc, fb - 2, fb - 1, fb + 1, fb + 2, S::FBN, w1x, w2x, cen, lf);
+    }
+    __syncthreads();
+    // y fluxes on TX x (TY+4)
+    for (int m = tid; m < TX * S::PH; m += TX * TY) {
+      const int lx = m % TX, ly = m / TX;
+      flux12<R, 1>(PP + ly * S::PW + (lx + 2), S::NPP, FB + ly * TX + lx, S::FBN);
+    }
+    __syncthreads();
+    if (active) {
+      const R* fb = FB + (ty + 2) * TX + tx;
+      add_direction<R, 1>(Racc, fb - 2 * TX, fb - TX, fb + TX, fb + 2 * TX, S::FBN, w1y, w2y, cen, lf);
+      const R* zm2 = FZ + (size_t)zslot(k - 2) * NF * S::NZ + tid;
+      const R* zm1 = FZ + (size_t)zslot(k - 1) * NF * S::NZ + tid;
+      const R* zp1 = FZ + (size_t)zslot(k + 1) * NF * S::NZ + tid;
+      const R* zp2 = FZ + (size_t)zslot(k + 2) * NF * S::NZ + tid;
+      add_direction<R, 2>(Racc, zm2, zm1, zp1, zp2, S::NZ, w1z, w2z, cen, lf);
+      const long long id = cidx(g, i, j, k);
+      if (RESID) {
+#pragma unroll
+        for (int q = 0; q < NV; q++) Res[(long long)q * g.N + id] = Racc[q];
+        R cm = cmax_cell<R>(cen[P_D], cen[P_V1], cen[P_V2], cen[P_V3], cen[P_B1], cen[P_B2], cen[P_B3], cen[P_P],
+                            inv_va2max);
+        atomic_max_nonneg(&dyn->cmax_bits, (double)cm);
+      } else {
+        // sources, Boris correction, update, Tcheck (src/Add_Sources_Integrate_SR.C:331-465)
+        const double dtd = dyn->dt;
+        const R dt = (R)dtd;
+        const R wdt = (R)(dtd / (double)(4 + 1 - stage));
+        const R invRdt = (R)(c.rt_cfl / dtd);
+        const R rh = cen[P_D], vx = cen[P_V1], vy = cen[P_V2], vz = cen[P_V3];
+        const R bx = cen[P_B1], by = cen[P_B2], bz = cen[P_B3];
+        R dn = invRdt * cen[P_EI];
+        R efaci = (dn > (R)0 && dn < (R)INFINITY) ? (R)1.0 : dn / d_fmax(dn, (R)0.0);
+        dn = (R)c.gx * rh - (R)0.0;
+        const R edmp = dn * vx;
+        Racc[1] += dn;
+        Racc[4] += edmp + (R)0.0 * efaci;
+        const R rd = Racc[0];
+        R fx = Racc[1], fy = Racc[2], fz = Racc[3];
+        const R bb = bx * bx + by * by + bz * bz;
+        const R va2 = bb / rh;
+        const R x2 = va2 * inv_va2max, x4 = x2 * x2;
+        const R bf = x4 / ((R)1 + x2 + x4);
+        fx -= vx * rd;
+        fy -= vy * rd;
+        fz -= vz * rd;
+        const R q = (fx * bx + fy * by + fz * bz) / d_fmax(tiny100<R>(), bb);
+        const R b0 = -bf * (fx - q * bx), b1 = -bf * (fy - q * by), b2 = -bf * (fz - q * bz);
+        const R b3 = b0 * vx + b1 * vy + b2 * vz;
+        Racc[1] += b0;
+        Racc[2] += b1;
+        Racc[3] += b2;
+        Racc[4] += b3;
+        R un[NV];
+#pragma unroll
+        for (int v = 0; v < NV; v++) un[v] = U0[(long long)v * g.N + id] + wdt * Racc[v];
+        const R vmax = (R)(dyn->v_lim > 0.0 ? dyn->v_lim : c.tchk_vmax);
+        const R emax = (R)(dyn->e_lim > 0.0 ? dyn->e_lim : c.tchk_eps_max);
+        tcheck_cell<R>(c, vmax, emax, un[0], un[1], un[2], un[3], un[4]);
+        const Images im = images_of(g, i, j, k, true);
+        store_state<R>(g, Uout, im, un);
+        if (write_pres) {
+          R v1, v2, v3, ei;
+          prim_from_cons(un[0], un[1], un[2], un[3], un[4], v1, v2, v3, ei);
+          const R pr = eos_pres(c, un[0], ei, (R)1.0 / un[0]);
+          for (int m = 0; m < im.n; m++) Pout[im.idx[m]] = pr;
+        }
+        (void)dt;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// --------------------------------------------------------------- TVD sweep
+// Per-cell quantities of TVDlimit's pencil (src/tvdlimit_SR.C:269-377).
+template <class R>
+struct TCell {
+  R q[NV];        // rho (log), v, eps (log), B
+  R cm, he, hv, hB, BC2, bsqr, vsqr, hd, hb, ht, qt;
+};
+
+struct TvdArgs {
+  int dir;               // 0, 1, 2
+  int mode;              // 0: plain sweep; 1: z sweep of the first (or only) TVD pass; 2: z sweep of the second half pass
+  int only_two_half;     // return at once unless the step takes two half TVD passes
+  int td;                // chunk length along the sweep
+  int na, nb, a0, b0;    // pencil ranges: a fastest (coalesced), b second
+  long long sa, sb, sd;  // strides of a, b and along the sweep
+  int n1;                // interior cells along the sweep
+};
+
+template <class R>
+__device__ __forceinline__ void tvd_load(const Consts& c, const R* __restrict__ U, const R* __restrict__ P, long long id,
+                                         int xi, R cmax_t, R fac0, bool hyper, R inv_va2max, TCell<R>& t) {
+  const Geom& g = c.g;
+  const R rho_min = (R)c.rho_min;
+  R d = smax(rho_min, U[id]);
+  R v1 = U[g.N + id], v2 = U[2 * g.N + id], v3 = U[3 * g.N + id], e = U[4 * g.N + id];
+  R b5 = U[5 * g.N + id], b6 = U[6 * g.N + id], b7 = U[7 * g.N + id];
+  t.hb = (R)c.hfb[xi];
+  t.ht = (R)c.hft[xi];
+  t.qt = (R)c.qft[xi];
+  R dn = (R)1.0 / d;
+  v1 = v1 * dn;
+  v2 = v2 * dn;
+  v3 = v3 * dn;
+  R vv = v1 * v1 + v2 * v2 + v3 * v3;
+  R bb = b5 * b5 + b6 * b6 + b7 * b7;
+  e = e * dn - (R)0.5 * vv;
+  t.vsqr = vv;
+  t.bsqr = bb;
+  vv = d_sqrt(vv);
+  R va2 = bb * dn;
+  R x2 = va2 * inv_va2max, x4 = x2 * x2, s = (R)1.0 + x2;
+  R lf = s / (s + x4);
+  R cs2 = (R)(5.0 / 3.0) * P[id] * dn;
+  R cfast = d_sqrt(va2 + cs2);
+  const R CZ = (R)c.CZ;
+  R CME = ((R)1.0 - CZ) * ((R)(vv >= (R)c.CME_thresh * cfast));
+  dn = d * d;
+  R rf = smin(lf, dn / (dn + (R)c.rho_lev));
+  R hh = (R)1.0 - t.hb - t.ht;
+  R cf = t.hb * (R)c.tvd_cs[0] + (rf * (R)c.tvd_cs[1] + ((R)1.0 - rf) * (R)c.tvd_cs[2]) * hh + t.ht * (R)c.tvd_cs[3];
+  cf = smax(cf, CME);
+  cs2 *= cf * cf;
+  t.cm = (R)0.0 + vv + d_sqrt(smax(cs2, lf * (cs2 + va2)));
+  const R h0 = (R)c.tvd_h[0], h1 = (R)c.tvd_h[1], h2 = (R)c.tvd_h[2], h3 = (R)c.tvd_h[3];
+  t.he = t.hb * h0 + (rf * h1 + ((R)1.0 - rf) * h2) * hh + t.ht * h3;
+  t.hv = t.hb * h0 + (rf * h1 + ((R)1.0 - rf) * h2 * (R)c.pm_v) * hh + t.ht * h3 * (R)c.pm_v;
+  t.hB = t.hb * h0 + (rf * h1 + ((R)1.0 - rf) * h2 * (R)c.pm_B) * hh + t.ht * h3 * (R)c.pm_B;
+  t.he *= ((R)1.0 - CME);
+  t.hv *= ((R)1.0 - CME);
+  t.BC2 = (R)1.0 - lf;
+  t.hd = (R)0;
+  if (hyper) {
+    R h = (R)c.vhyp * d_sqrt(t.vsqr);
+    t.hd = fac0 * smax((R)0.0, smin(h, cmax_t - t.cm));
+  }
+  if (c.rho_log) {
+    d = d_log(d);
+    e = d_log(e);
+  }
+  t.q[0] = d; t.q[1] = v1; t.q[2] = v2; t.q[3] = v3; t.q[4] = e; t.q[5] = b5; t.q[6] = b6; t.q[7] = b7;
+}
+
+// Limited slope at the middle cell b (src/tvdlimit_SR.C:388-434)
+template <class R>
+__device__ __forceinline__ void tvd_slope(const Consts& c, const TCell<R>& a, const TCell<R>& b, const TCell<R>& n,
+                                          R vsqr_diff, R* slp) {
+#pragma unroll
+  for (int v = 0; v < NV; v++) {
+    R sl = b.q[v] - a.q[v];
+    R sr = n.q[v] - b.q[v];
+    R slm = (R)0.25 * (sl + sr);
+    R lower = smin(smin(sl, sr), slm);
+    R upper = smax(smax(sl, sr), slm);
+    slp[v] = smax((R)0.0, lower) + smin((R)0.0, upper);
+  }
+  if (c.visc_slope_bot > 0.0 || c.visc_slope_top > 0.0) {
+    R cf = ((R)1.0 - (R)c.visc_slope_bot * b.hb) * ((R)1.0 - (R)c.visc_slope_top * b.ht);
+    slp[1] *= cf; slp[2] *= cf; slp[3] *= cf;
+  }
+  if (c.eta_slope_bot > 0.0 || c.eta_slope_top > 0.0) {
+    R cf = ((R)1.0 - (R)c.eta_slope_bot * b.hb) * ((R)1.0 - (R)c.eta_slope_top * b.ht);
+    slp[5] *= cf; slp[6] *= cf; slp[7] *= cf;
+  }
+  R qr = c.rho_log ? d_fabs(b.q[0] - n.q[0]) : d_fabs(d_log(b.q[0]) - d_log(n.q[0]));
+  if (qr > (R)c.q_rho_max) slp[0] = (R)0.0;
+  if (c.vmax_lim > 0.0 && b.vsqr > vsqr_diff) { slp[1] = (R)0.0; slp[2] = (R)0.0; slp[3] = (R)0.0; }
+}
+
+// Interface flux between cells a (index ia) and b, plus its resistive-heating
+// term (src/tvdlimit_SR.C:436-557, 559-563, 608-614).  am = cell left of a,
+// bp = cell right of b (hyperdiffusion stencil).
+template <class R, int DIR>
+__device__ __forceinline__ void tvd_flux(const Consts& c, const TCell<R>& am, const TCell<R>& a, const TCell<R>& b,
+                                         const TCell<R>& bp, const R* sa, const R* sb, int ia, int sz, R fac0,
+                                         R cmax_t, bool hyper, int istart, R* F, R& qres) {
+#pragma unroll
+  for (int v = 0; v < NV; v++) {
+    R sl = b.q[v] - a.q[v];
+    R sl_lim = b.q[v] - a.q[v] - (sa[v] + sb[v]);
+    R dn = (v >= 1 && v <= 3) ? a.hv : ((v >= 5) ? a.hB : a.he);
+    R rf = d_fabs(sl_lim) / smax(tiny100<R>(), d_fabs(sl));
+    R cf = smax((R)0.0, smin(sl_lim, sl)) + smin((R)0.0, smax(sl_lim, sl));
+    F[v] = smax((R)0.0, (R)1.0 + dn * (rf - (R)1.0)) * cf;
+  }
+  R fac = fac0 * smin(cmax_t, smax(a.cm, b.cm));
+#pragma unroll
+  for (int v = 0; v < NV; v++) F[v] *= fac;
+  F[5 + DIR] *= (R)c.B_par_diff;
+  if (c.need_coeff) {
+    F[0] *= (R)c.tvd_coeff[0];
+    R cf = smax((R)c.tvd_coeff[1], (R)c.visc_coeff_bot * a.hb + (R)c.visc_coeff_top * a.ht);
+    F[1] *= cf; F[2] *= cf; F[3] *= cf;
+    F[4] *= (R)c.tvd_coeff[2];
+    cf = smax((R)c.tvd_coeff[3], (R)c.eta_coeff_bot * a.hb + (R)c.eta_coeff_top * a.ht);
+    F[5] *= cf; F[6] *= cf; F[7] *= cf;
+  }
+  if (DIR == 0 && hyper && ia >= istart) {
+    R dn = smax(a.hd, b.hd);
+    F[0] -= dn * ((R)0.125 * (bp.q[0] - am.q[0]) - (R)0.375 * (b.q[0] - a.q[0]));
+    F[1] -= dn * ((R)0.125 * (bp.q[1] - am.q[1]) - (R)0.375 * (b.q[1] - a.q[1]));
+    F[4] -= dn * ((R)0.125 * (bp.q[4] - am.q[4]) - (R)0.375 * (b.q[4] - a.q[4]));
+  }
+  R f0 = F[0], f1 = F[1], f2 = F[2], f3 = F[3], f4 = F[4];
+  R u[5];
+#pragma unroll
+  for (int v = 0; v < 5; v++) u[v] = (R)0.5 * (a.q[v] + sa[v] + b.q[v] - sb[v]);
+  if (c.rho_log) {
+    u[0] = d_exp(u[0]);
+    f0 *= u[0];
+    u[4] = d_exp(u[4]);
+    f4 *= u[4];
+  }
+  const R CZ = (R)c.CZ;
+  R min_cz = f0 * smin(CZ, CZ);
+  f1 *= u[0]; f1 += u[1] * min_cz;
+  f2 *= u[0]; f2 += u[2] * min_cz;
+  f3 *= u[0]; f3 += u[3] * min_cz;
+  f4 *= u[0];
+  f4 += (u[4] * min_cz) + a.qt * (u[1] * f1 + u[2] * f2 + u[3] * f3);
+  F[0] = f0; F[1] = f1; F[2] = f2; F[3] = f3; F[4] = f4;
+  if (DIR == 0 && !c.g.periodic_x) {
+    if (ia == sz - GH - 1) F[5] = (R)0.0;
+    if (ia == GH - 1) F[5] = (R)0.0;
+  }
+  qres = (b.q[5] - a.q[5]) * F[5] + (b.q[6] - a.q[6]) * F[6] + (b.q[7] - a.q[7]) * F[7];
+}
+
+template <class R, int DIR>
+__global__ void __launch_bounds__(128) k_tvd_sweep(Consts c, const R* __restrict__ Uin, const R* __restrict__ Pst,
+                                                   R* __restrict__ Uout, R* __restrict__ Pout, Dyn* __restrict__ dyn,
+                                                   TvdArgs ta) {
+  const Geom& g = c.g;
+  if (dyn->err) return;
+  if (ta.only_two_half && !dyn->two_half) return;   // second half pass not taken this step
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int nch = (ta.n1 + ta.td - 1) / ta.td;
+  const long long total = (long long)ta.na * ta.nb * nch;
+  bool live = t < total;
+  int a = 0, b = 0, ch = 0;
+  if (live) {
+    a = (int)(t % ta.na);
+    long long r = t / ta.na;
+    b = (int)(r % ta.nb);
+    ch = (int)(r / ta.nb);
+  }
+  const int aa = ta.a0 + a, bb = ta.b0 + b;
+  const long long base = (long long)aa * ta.sa + (long long)bb * ta.sb;
+  const int sz = ta.n1 + 2 * GH;
+  const int p0 = GH + ch * ta.td;
+  const int p1 = min(p0 + ta.td, GH + ta.n1);
+  const double dt_tvd = dyn->dt_tvd;
+  const R dtt = (R)dt_tvd;
+  const R cmax_t = (R)(0.975 * c.dx[DIR] / dt_tvd);
+  const R fac0 = (R)(0.5 * c.idx[DIR]);
+  const R inv_va2max = (R)dyn->inv_va2max;
+  const R vsqr_diff = (R)dyn->vsqr_diff;
+  const bool hyper = (DIR == 0) && (c.vhyp > 0.0);
+  const int istart = 1 + (c.g.periodic_x ? 0 : GH);
+  // final pass: TCheck, full ghost images, next step's pressure and statistics;
+  // half_images: after the first of two half passes only the periodic exchange
+  const bool final_pass = (ta.mode == 2) || (ta.mode == 1 && !dyn->two_half);
+  const bool half_images = (ta.mode == 1) && dyn->two_half;
+  R cmax_loc = (R)0;
+  R st_v = (R)0, st_c = (R)0, st_e = (R)0;
+  unsigned long long cnt_v = 0, cnt_e = 0;
+  if (live) {
+    auto xi_of = [&](int pos) { return DIR == 0 ? pos : aa; };
+    TCell<R> cm1, c0, c1, c2;
+    R s0[NV], s1[NV], Fm[NV], F0[NV];
+    R qm, q0;
+    {
+      TCell<R> cmm;
+      tvd_load<R>(c, Uin, Pst, base + (long long)(p0 - 2) * ta.sd, xi_of(p0 - 2), cmax_t, fac0, hyper, inv_va2max, cmm);
+      tvd_load<R>(c, Uin, Pst, base + (long long)(p0 - 1) * ta.sd, xi_of(p0 - 1), cmax_t, fac0, hyper, inv_va2max, cm1);
+      tvd_load<R>(c, Uin, Pst, base + (long long)p0 * ta.sd, xi_of(p0), cmax_t, fac0, hyper, inv_va2max, c0);
+      tvd_load<R>(c, Uin, Pst, base + (long long)(p0 + 1) * ta.sd, xi_of(p0 + 1), cmax_t, fac0, hyper, inv_va2max, c1);
+      R sm[NV];
+      tvd_slope<R>(c, cmm, cm1, c0, vsqr_diff, sm);
+      tvd_slope<R>(c, cm1, c0, c1, vsqr_diff, s0);
+      tvd_flux<R, DIR>(c, cmm, cm1, c0, c1, sm, s0, p0 - 1, sz, fac0, cmax_t, hyper, istart, Fm, qm);
+    }
+    for (int pos = p0; pos < p1; pos++) {
+      tvd_load<R>(c, Uin, Pst, base + (long long)(pos + 2) * ta.sd, xi_of(pos + 2), cmax_t, fac0, hyper, inv_va2max, c2);
+      tvd_slope<R>(c, c0, c1, c2, vsqr_diff, s1);
+      tvd_flux<R, DIR>(c, cm1, c0, c1, c2, s0, s1, pos, sz, fac0, cmax_t, hyper, istart, F0, q0);
+      // update of cell pos (src/tvdlimit_SR.C:565-657)
+      R res[NV];
+#pragma unroll
+      for (int v = 0; v < NV; v++) res[v] = dtt * (F0[v] - Fm[v]);
+      res[4] += ((R)1.0 - c0.qt) * (res[1] * c0.q[1] + res[2] * c0.q[2] + res[3] * c0.q[3]);
+      {
+        R dn = (res[1] * c0.q[5] + res[2] * c0.q[6] + res[3] * c0.q[7]) / smax(tiny100<R>(), c0.bsqr);
+        R b0 = -c0.BC2 * (res[1] - dn * c0.q[5]);
+        R b1 = -c0.BC2 * (res[2] - dn * c0.q[6]);
+        R b2 = -c0.BC2 * (res[3] - dn * c0.q[7]);
+        R b3 = b0 * c0.q[1] + b1 * c0.q[2] + b2 * c0.q[3];
+        res[1] += b0; res[2] += b1; res[3] += b2; res[4] += b3;
+      }
+      {
+        R qres = (R)0.5 * (q0 + qm) * c0.qt;
+        res[4] += dtt * qres;
+      }
+      const long long id = base + (long long)pos * ta.sd;
+      R u[NV];
+#pragma unroll
+      for (int v = 0; v < NV; v++) u[v] = Uin[(long long)v * g.N + id] + res[v];
+      u[0] = smax((R)c.rho_min, u[0]);
+      u[4] = smax(u[4], (R)c.eps_min * u[0] + (R)0.5 * (u[1] * u[1] + u[2] * u[2] + u[3] * u[3]) / u[0]);
+      if (ta.mode == 0) {
+#pragma unroll
+        for (int v = 0; v < NV; v++) Uout[(long long)v * g.N + id] = u[v];
+      } else if (half_images) {
+        // first of two half steps: exchange (periodic dimensions) only
+        int ci = DIR == 0 ? pos : aa, cj = DIR == 1 ? pos : (DIR == 0 ? aa : bb), ck = DIR == 2 ? pos : bb;
+        store_state<R>(g, Uout, images_of(g, ci, cj, ck, false), u);
+      } else if (final_pass) {
+        const R vmax = (R)(dyn->v_lim > 0.0 ? dyn->v_lim : c.tchk_vmax);
+        const R emax = (R)(dyn->e_lim > 0.0 ? dyn->e_lim : c.tchk_eps_max);
+        tcheck_cell<R>(c, vmax, emax, u[0], u[1], u[2], u[3], u[4]);
+        int ci = DIR == 0 ? pos : aa, cj = DIR == 1 ? pos : (DIR == 0 ? aa : bb), ck = DIR == 2 ? pos : bb;
+        const Images im = images_of(g, ci, cj, ck, true);
+        store_state<R>(g, Uout, im, u);
+        // next step's stage-1 pressure, CFL speed and Adjust_Valf_Max statistics
+        R v1, v2, v3, ei;
+        prim_from_cons(u[0], u[1], u[2], u[3], u[4], v1, v2, v3, ei);
+        const R pr = eos_pres(c, u[0], ei, (R)1.0 / u[0]);
+        for (int m = 0; m < im.n; m++) Pout[im.idx[m]] = pr;
+        R cmv = cmax_cell<R>(u[0], v1, v2, v3, u[5], u[6], u[7], pr, inv_va2max);
+        cmax_loc = smax(cmax_loc, cmv);
+        R vabs = d_sqrt(v1 * v1 + v2 * v2 + v3 * v3);
+        R cs = (R)(5 / 3.) * pr / u[0];
+        R ee = ei / u[0];
+        st_v = d_fmax(st_v, vabs);
+        st_c = d_fmax(st_c, cs);
+        st_e = d_fmax(st_e, ee);
+        if ((double)vabs >= dyn->v_lim * 0.95) cnt_v++;
+        if ((double)ee >= dyn->e_lim * 0.95) cnt_e++;
+      }
+      // shift the window
+      cm1 = c0; c0 = c1; c1 = c2;
+#pragma unroll
+      for (int v = 0; v < NV; v++) { s0[v] = s1[v]; Fm[v] = F0[v]; }
+      qm = q0;
+    }
+  }
+  if (final_pass) {
+    {
+      R m = warp_max_nonnan(cmax_loc);
+      R a1 = warp_max_nonnan(st_v), a2 = warp_max_nonnan(st_c), a3 = warp_max_nonnan(st_e);
+      for (int o = 16; o > 0; o >>= 1) {
+        cnt_v += __shfl_xor_sync(0xffffffffu, cnt_v, o);
+        cnt_e += __shfl_xor_sync(0xffffffffu, cnt_e, o);
+      }
+      if ((threadIdx.x & 31) == 0) {
+        atomic_max_nonneg(&dyn->cmax_bits, (double)m);
+        atomic_max_nonneg(&dyn->stat_max_bits[0], (double)a1);
+        atomic_max_nonneg(&dyn->stat_max_bits[1], (double)a2);
+        atomic_max_nonneg(&dyn->stat_max_bits[2], (double)a3);
+        if (cnt_v) atomicAdd(&dyn->stat_cnt[0], cnt_v);
+        if (cnt_e) atomicAdd(&dyn->stat_cnt[1], cnt_e);
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------- small kernels
+// ConsToPrim over the whole box (src/cons_to_prim.C:78-266).
+template <class R>
+__global__ void k_cons_to_prim(Consts c, R* __restrict__ U, R* __restrict__ P, R* __restrict__ T, R* __restrict__ Ne,
+                               R* __restrict__ Ri, R* __restrict__ Am) {
+  const Geom& g = c.g;
+  for (long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x; id < g.N; id += (long long)gridDim.x * blockDim.x) {
+    R d = U[id];
+    R v1, v2, v3, ei;
+    prim_from_cons(d, U[g.N + id], U[2 * g.N + id], U[3 * g.N + id], U[4 * g.N + id], v1, v2, v3, ei);
+    const R dn = (R)1.0 / d;
+    C2POut o = c2p_eos_full(c, (double)d, (double)ei, (double)dn);
+    if (sizeof(R) == 4) o.pres = (double)eos_pres(c, d, ei, dn);
+    U[g.N + id] = v1;
+    U[2 * g.N + id] = v2;
+    U[3 * g.N + id] = v3;
+    U[4 * g.N + id] = ei;
+    P[id] = (R)o.pres;
+    if (T) { T[id] = (R)o.temp; Ne[id] = (R)o.ne; Ri[id] = (R)o.rhoi; Am[id] = (R)o.amb; }
+  }
+}
+
+// Fused-path initial pass: pressure of the conserved state over the whole box,
+// CFL speed and Adjust_Valf_Max statistics over the interior.
+template <class R>
+__global__ void k_init_pass(Consts c, const R* __restrict__ U, R* __restrict__ P, Dyn* __restrict__ dyn) {
+  const Geom& g = c.g;
+  R cm_loc = 0, sv = 0, sc = 0, se = 0;
+  unsigned long long nv = 0, ne = 0;
+  const R inv_va2max = (R)dyn->inv_va2max;
+  for (long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x; id < g.N; id += (long long)gridDim.x * blockDim.x) {
+    R d = U[id];
+    R v1, v2, v3, ei;
+    prim_from_cons(d, U[g.N + id], U[2 * g.N + id], U[3 * g.N + id], U[4 * g.N + id], v1, v2, v3, ei);
+    R pr = eos_pres(c, d, ei, (R)1.0 / d);
+    P[id] = pr;
+    const int i = (int)(id % g.sx), j = (int)((id / g.sx) % g.sy), k = (int)(id / ((long long)g.sx * g.sy));
+    if (i >= GH && i < GH + g.nx && j >= GH && j < GH + g.ny && k >= GH && k < GH + g.nz) {
+      cm_loc = smax(cm_loc, cmax_cell<R>(d, v1, v2, v3, U[5 * g.N + id], U[6 * g.N + id], U[7 * g.N + id], pr, inv_va2max));
+      R vabs = d_sqrt(v1 * v1 + v2 * v2 + v3 * v3);
+      R cs = (R)(5 / 3.) * pr / d;
+      R ee = ei / d;
+      sv = d_fmax(sv, vabs);
+      sc = d_fmax(sc, cs);
+      se = d_fmax(se, ee);
+      if ((double)vabs >= dyn->v_lim * 0.95) nv++;
+      if ((double)ee >= dyn->e_lim * 0.95) ne++;
+    }
+  }
+  R m = warp_max_nonnan(cm_loc);
+  R a1 = warp_max_nonnan(sv), a2 = warp_max_nonnan(sc), a3 = warp_max_nonnan(se);
+  for (int o = 16; o > 0; o >>= 1) {
+    nv += __shfl_xor_sync(0xffffffffu, nv, o);
+    ne += __shfl_xor_sync(0xffffffffu, ne, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomic_max_nonneg(&dyn->cmax_bits, (double)m);
+    atomic_max_nonneg(&dyn->stat_max_bits[0], (double)a1);
+    atomic_max_nonneg(&dyn->stat_max_bits[1], (double)a2);
+    atomic_max_nonneg(&dyn->stat_max_bits[2], (double)a3);
+    if (nv) atomicAdd(&dyn->stat_cnt[0], nv);
+    if (ne) atomicAdd(&dyn->stat_cnt[1], ne);
+  }
+}
+
+// Adjust_Valf_Max statistics over the interior of a primitive state
+// (src/Adjust_Valf_Max.C:58-81).
+template <class R>
+__global__ void k_adjust_stats(Consts c, const R* __restrict__ U, const R* __restrict__ P, Dyn* __restrict__ dyn) {
+  const Geom& g = c.g;
+  const long long n = (long long)g.nx * g.ny * g.nz;
+  R sv = 0, sc = 0, se = 0;
+  unsigned long long nv = 0, ne = 0;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const int i = GH + (int)(t % g.nx), j = GH + (int)((t / g.nx) % g.ny), k = GH + (int)(t / ((long long)g.nx * g.ny));
+    const long long id = cidx(g, i, j, k);
+    R d = U[id], v1 = U[g.N + id], v2 = U[2 * g.N + id], v3 = U[3 * g.N + id], ei = U[4 * g.N + id];
+    R vabs = d_sqrt(v1 * v1 + v2 * v2 + v3 * v3);
+    R ee = ei / d;
+    sv = d_fmax(sv, vabs);
+    sc = d_fmax(sc, (R)(5 / 3.) * P[id] / d);
+    se = d_fmax(se, ee);
+    if ((double)vabs >= dyn->v_lim * 0.95) nv++;
+    if ((double)ee >= dyn->e_lim * 0.95) ne++;
+  }
+  R a1 = warp_max_nonnan(sv), a2 = warp_max_nonnan(sc), a3 = warp_max_nonnan(se);
+  for (int o = 16; o > 0; o >>= 1) {
+    nv += __shfl_xor_sync(0xffffffffu, nv, o);
+    ne += __shfl_xor_sync(0xffffffffu, ne, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomic_max_nonneg(&dyn->stat_max_bits[0], (double)a1);
+    atomic_max_nonneg(&dyn->stat_max_bits[1], (double)a2);
+    atomic_max_nonneg(&dyn->stat_max_bits[2], (double)a3);
+    if (nv) atomicAdd(&dyn->stat_cnt[0], nv);
+    if (ne) atomicAdd(&dyn->stat_cnt[1], ne);
+  }
+}
+
+// CFL speed on the face ghost cells the residual's pencils include
+// (one coordinate in the ghost range, the other two interior).
+template <class R>
+__global__ void k_cmax_faces(Consts c, const R* __restrict__ U, const R* __restrict__ P, Dyn* __restrict__ dyn) {
+  const Geom& g = c.g;
+  const long long nfx = 2LL * GH * g.ny * g.nz, nfy = 2LL * GH * g.nx * g.nz, nfz = 2LL * GH * g.nx * g.ny;
+  const R inv_va2max = (R)dyn->inv_va2max;
+  R cm = 0;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < nfx + nfy + nfz; t += (long long)gridDim.x * blockDim.x) {
+    int i, j, k;
+    if (t < nfx) {
+      int q = (int)(t % (2 * GH)); long long r = t / (2 * GH);
+      i = q < GH ? q : g.nx + q; j = GH + (int)(r % g.ny); k = GH + (int)(r / g.ny);
+    } else if (t < nfx + nfy) {
+      long long u = t - nfx; int q = (int)(u % (2 * GH)); long long r = u / (2 * GH);
+      j = q < GH ? q : g.ny + q; i = GH + (int)(r % g.nx); k = GH + (int)(r / g.nx);
+    } else {
+      long long u = t - nfx - nfy; int q = (int)(u % (2 * GH)); long long r = u / (2 * GH);
+      k = q < GH ? q : g.nz + q; i = GH + (int)(r % g.nx); j = GH + (int)(r / g.nx);
+    }
+    const long long id = cidx(g, i, j, k);
+    cm = smax(cm, cmax_cell<R>(U[id], U[g.N + id], U[2 * g.N + id], U[3 * g.N + id], U[5 * g.N + id], U[6 * g.N + id],
+                               U[7 * g.N + id], P[id], inv_va2max));
+  }
+  R m = warp_max_nonnan(cm);
+  if ((threadIdx.x & 31) == 0) atomic_max_nonneg(&dyn->cmax_bits, (double)m);
+}
+
+// Source_Integrate_Tcheck (src/Add_Sources_Integrate_SR.C:297-467) on a primitive U.
+template <class R>
+__global__ void k_source_integrate(Consts c, R* __restrict__ U, const R* __restrict__ U0, R* __restrict__ Res,
+                                   const Dyn* __restrict__ dyn, int stage) {
+  const Geom& g = c.g;
+  const long long n = (long long)g.nx * g.ny * g.nz;
+  const double dtd = dyn->dt;
+  const R wdt = (R)(dtd / (double)(4 + 1 - stage));
+  const R invRdt = (R)(c.rt_cfl / dtd);
+  const R inv_va2max = (R)dyn->inv_va2max;
+  const R vmax = (R)(dyn->v_lim > 0.0 ? dyn->v_lim : c.tchk_vmax);
+  const R emax = (R)(dyn->e_lim > 0.0 ? dyn->e_lim : c.tchk_eps_max);
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const int i = GH + (int)(t % g.nx), j = GH + (int)((t / g.nx) % g.ny), k = GH + (int)(t / ((long long)g.nx * g.ny));
+    const long long id = cidx(g, i, j, k);
+    R r[NV], u[NV];
+#pragma unroll
+    for (int v = 0; v < NV; v++) { r[v] = Res[(long long)v * g.N + id]; u[v] = U[(long long)v * g.N + id]; }
+    R dn = invRdt * u[4];
+    R efaci = dn / d_fmax(dn, (R)0.0);
+    dn = (R)c.gx * u[0] - (R)0.0;
+    R edmp = dn * u[1];
+    r[1] += dn;
+    r[4] += edmp + (R)0.0 * efaci;
+    const R rh = u[0], rd = r[0], vx = u[1], vy = u[2], vz = u[3], bx = u[5], by = u[6], bz = u[7];
+    R fx = r[1], fy = r[2], fz = r[3];
+    const R bb = bx * bx + by * by + bz * bz;
+    const R va2 = bb / rh;
+    const R x2 = va2 * inv_va2max, x4 = x2 * x2;
+    const R bf = x4 / ((R)1 + x2 + x4);
+    fx -= vx * rd;
+    fy -= vy * rd;
+    fz -= vz * rd;
+    const R q = (fx * bx + fy * by + fz * bz) / d_fmax(tiny100<R>(), bb);
+    const R b0 = -bf * (fx - q * bx), b1 = -bf * (fy - q * by), b2 = -bf * (fz - q * bz);
+    const R b3 = b0 * vx + b1 * vy + b2 * vz;
+    r[1] += b0; r[2] += b1; r[3] += b2; r[4] += b3;
+    R un[NV];
+#pragma unroll
+    for (int v = 0; v < NV; v++) {
+      un[v] = U0[(long long)v * g.N + id] + wdt * r[v];
+      Res[(long long)v * g.N + id] = (R)0;
+    }
+    tcheck_cell<R>(c, vmax, emax, un[0], un[1], un[2], un[3], un[4]);
+#pragma unroll
+    for (int v = 0; v < NV; v++) U[(long long)v * g.N + id] = un[v];
+  }
+}
+
+template <class R>
+__global__ void k_save_cons(Geom g, const R* __restrict__ U, R* __restrict__ U0) {
+  const long long n = (long long)g.nx * g.ny * g.nz;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const int i = GH + (int)(t % g.nx), j = GH + (int)((t / g.nx) % g.ny), k = GH + (int)(t / ((long long)g.nx * g.ny));
+    const long long id = cidx(g, i, j, k);
+#pragma unroll
+    for (int v = 0; v < NV; v++) U0[(long long)v * g.N + id] = U[(long long)v * g.N + id];
+  }
+}
+
+template <class R>
+__global__ void k_tcheck(Consts c, R* __restrict__ U, const Dyn* __restrict__ dyn) {
+  const Geom& g = c.g;
+  const long long n = (long long)g.nx * g.ny * g.nz;
+  const R vmax = (R)(dyn->v_lim > 0.0 ? dyn->v_lim : c.tchk_vmax);
+  const R emax = (R)(dyn->e_lim > 0.0 ? dyn->e_lim : c.tchk_eps_max);
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const int i = GH + (int)(t % g.nx), j = GH + (int)((t / g.nx) % g.ny), k = GH + (int)(t / ((long long)g.nx * g.ny));
+    const long long id = cidx(g, i, j, k);
+    R d = U[id], m1 = U[g.N + id], m2 = U[2 * g.N + id], m3 = U[3 * g.N + id], e = U[4 * g.N + id];
+    tcheck_cell<R>(c, vmax, emax, d, m1, m2, m3, e);
+    U[id] = d; U[g.N + id] = m1; U[2 * g.N + id] = m2; U[3 * g.N + id] = m3; U[4 * g.N + id] = e;
+  }
+}
+
+// Ghost fill: each ghost cell takes the value of the interior cell it images
+// (periodic wrap; for closed x with with_bc, mirror with M_x, B_y, B_z flipped).
+// Without with_bc a closed x leaves the x ghosts and the y/z ghosts outside the
+// interior x range untouched, like exchange_grid_acc without the boundary call.
+template <class R>
+__global__ void k_fill_ghosts(Geom g, R* __restrict__ U, int nfield, int with_bc) {
+  for (long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x; id < g.N; id += (long long)gridDim.x * blockDim.x) {
+    int i = (int)(id % g.sx), j = (int)((id / g.sx) % g.sy), k = (int)(id / ((long long)g.sx * g.sy));
+    const bool gx = (i < GH || i >= GH + g.nx), gy = (j < GH || j >= GH + g.ny), gz = (k < GH || k >= GH + g.nz);
+    if (!gx && !gy && !gz) continue;
+    bool flip = false;
+    if (gx) {
+      if (g.periodic_x) i = i < GH ? i + g.nx : i - g.nx;
+      else if (with_bc) { i = i < GH ? 2 * GH - 1 - i : 2 * GH + 2 * g.nx - 1 - i; flip = true; }
+      else continue;
+    }
+    if (gy) j = j < GH ? j + g.ny : j - g.ny;
+    if (gz) k = k < GH ? k + g.nz : k - g.nz;
+    const long long src = cidx(g, i, j, k);
+    for (int v = 0; v < nfield; v++) {
+      R x = U[(long long)v * g.N + src];
+      if (flip && (v == 1 || v == 6 || v == 7)) x = -x;
+      U[(long long)v * g.N + id] = x;
+    }
+  }
+}
+
+// Host cState (AoS, double) <-> device SoA (R)
+template <class R>
+__global__ void k_aos_to_soa(long long N, int nf, const double* __restrict__ A, R* __restrict__ S) {
+  for (long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x; id < N; id += (long long)gridDim.x * blockDim.x)
+    for (int v = 0; v < nf; v++) S[(long long)v * N + id] = (R)A[id * nf + v];
+}
+template <class R>
+__global__ void k_soa_to_aos(long long N, int nf, const R* __restrict__ S, double* __restrict__ A) {
+  for (long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x; id < N; id += (long long)gridDim.x * blockDim.x)
+    for (int v = 0; v < nf; v++) A[id * nf + v] = (double)S[(long long)v * N + id];
+}
+
+}  // namespace gpumhd

@@ -1,0 +1,158 @@
+// Kernel launchers, instantiated once per state type in its own translation
+// unit (FP64 without FMA contraction, FP32 with it).
+#pragma once
+#include "gpumhd_kernels.cuh"
+
+namespace gpumhd {
+
+// Step control for the fused path (one thread): the Adjust_Valf_Max limits,
+// Sync_timestep (src/solver.C:487-548) on the CFL speed accumulated by the
+// previous pass, the TVD branch (src/solver.C:325-339) and Run.Advance.
+__global__ void k_step_begin(Consts c, Dyn* dyn, double* dt_hist, int dt_hist_cap);
+
+template <class R>
+struct Launch {
+  static int stage_smem_bytes();
+  static cudaError_t setup();
+  static void stage(const Consts& c, const R* Uin, const R* Pin, const R* U0, R* Uout, R* Pout, R* Res, Dyn* dyn,
+                    int stage, bool resid, int write_pres, cudaStream_t s);
+  static void tvd(const Consts& c, int dir, int mode, int only_two_half, const R* Uin, const R* Pst, R* Uout, R* Pout,
+                  Dyn* dyn, cudaStream_t s);
+  static void cons_to_prim(const Consts& c, R* U, R* P, R* T, R* Ne, R* Ri, R* Am, cudaStream_t s);
+  static void init_pass(const Consts& c, const R* U, R* P, Dyn* dyn, cudaStream_t s);
+  static void adjust_stats(const Consts& c, const R* U, const R* P, Dyn* dyn, cudaStream_t s);
+  static void cmax_faces(const Consts& c, const R* U, const R* P, Dyn* dyn, cudaStream_t s);
+  static void source_integrate(const Consts& c, R* U, const R* U0, R* Res, const Dyn* dyn, int stage, cudaStream_t s);
+  static void save_cons(const Consts& c, const R* U, R* U0, cudaStream_t s);
+  static void tcheck(const Consts& c, R* U, const Dyn* dyn, cudaStream_t s);
+  static void fill_ghosts(const Consts& c, R* U, int nfield, int with_bc, cudaStream_t s);
+  static void aos_to_soa(long long N, int nf, const double* A, R* S, cudaStream_t s);
+  static void soa_to_aos(long long N, int nf, const R* S, double* A, cudaStream_t s);
+};
+
+// Tile shapes of the stage kernel per state type.
+template <class R> struct StageTile;
+template <> struct StageTile<double> { static constexpr int TX = 16, TY = 8; };
+template <> struct StageTile<float> { static constexpr int TX = 32, TY = 8; };
+
+inline int grid_for(long long n, int block) {
+  long long b = (n + block - 1) / block;
+  if (b > 152LL * 32) b = 152LL * 32;
+  if (b < 1) b = 1;
+  return (int)b;
+}
+
+#ifdef GPUMHD_LAUNCH_IMPL
+template <class R>
+int Launch<R>::stage_smem_bytes() {
+  return (int)StageSmem<StageTile<R>::TX, StageTile<R>::TY>::template bytes<R>();
+}
+
+template <class R>
+cudaError_t Launch<R>::setup() {
+  constexpr int TX = StageTile<R>::TX, TY = StageTile<R>::TY;
+  const int bytes = stage_smem_bytes();
+  cudaError_t e = cudaFuncSetAttribute(k_stage<R, TX, TY, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(k_stage<R, TX, TY, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
+template <class R>
+void Launch<R>::stage(const Consts& c, const R* Uin, const R* Pin, const R* U0, R* Uout, R* Pout, R* Res, Dyn* dyn,
+                      int stage, bool resid, int write_pres, cudaStream_t s) {
+  constexpr int TX = StageTile<R>::TX, TY = StageTile<R>::TY;
+  const Geom& g = c.g;
+  const int bx = (g.nx + TX - 1) / TX, by = (g.ny + TY - 1) / TY;
+  // z chunk: enough blocks for several waves, at least 8 planes per block
+  const long long want = 152LL * 8;
+  int nzc = (int)((want + (long long)bx * by - 1) / ((long long)bx * by));
+  int zc = (g.nz + nzc - 1) / nzc;
+  if (zc < 8) zc = 8;
+  if (zc > g.nz) zc = g.nz;
+  const int bz = (g.nz + zc - 1) / zc;
+  dim3 grid(bx, by, bz);
+  const int bytes = stage_smem_bytes();
+  if (resid)
+    k_stage<R, TX, TY, true><<<grid, TX * TY, bytes, s>>>(c, Uin, Pin, U0, Uout, Pout, Res, dyn, stage, zc, write_pres);
+  else
+    k_stage<R, TX, TY, false><<<grid, TX * TY, bytes, s>>>(c, Uin, Pin, U0, Uout, Pout, Res, dyn, stage, zc, write_pres);
+}
+
+template <class R>
+void Launch<R>::tvd(const Consts& c, int dir, int mode, int only_two_half, const R* Uin, const R* Pst, R* Uout,
+                    R* Pout, Dyn* dyn, cudaStream_t s) {
+  const Geom& g = c.g;
+  TvdArgs ta;
+  ta.dir = dir;
+  ta.mode = mode;
+  ta.only_two_half = only_two_half;
+  ta.td = 32;
+  const long long sx = 1, sy = g.sx, sz = (long long)g.sx * g.sy;
+  // pencil ranges of TVDlimit's three sweeps (src/tvdlimit_SR.C:199-205, 671-672)
+  if (dir == 0) {
+    ta.na = g.sy; ta.a0 = 0; ta.sa = sy;
+    ta.nb = g.sz; ta.b0 = 0; ta.sb = sz;
+    ta.sd = sx; ta.n1 = g.nx;
+  } else if (dir == 1) {
+    ta.na = g.nx; ta.a0 = GH; ta.sa = sx;
+    ta.nb = g.sz; ta.b0 = 0; ta.sb = sz;
+    ta.sd = sy; ta.n1 = g.ny;
+  } else {
+    ta.na = g.nx; ta.a0 = GH; ta.sa = sx;
+    ta.nb = g.ny; ta.b0 = GH; ta.sb = sy;
+    ta.sd = sz; ta.n1 = g.nz;
+  }
+  const long long nch = (ta.n1 + ta.td - 1) / ta.td;
+  const long long total = (long long)ta.na * ta.nb * nch;
+  const int block = 128;
+  const long long blocks = (total + block - 1) / block;
+  if (dir == 0) k_tvd_sweep<R, 0><<<(unsigned)blocks, block, 0, s>>>(c, Uin, Pst, Uout, Pout, dyn, ta);
+  else if (dir == 1) k_tvd_sweep<R, 1><<<(unsigned)blocks, block, 0, s>>>(c, Uin, Pst, Uout, Pout, dyn, ta);
+  else k_tvd_sweep<R, 2><<<(unsigned)blocks, block, 0, s>>>(c, Uin, Pst, Uout, Pout, dyn, ta);
+}
+
+template <class R>
+void Launch<R>::cons_to_prim(const Consts& c, R* U, R* P, R* T, R* Ne, R* Ri, R* Am, cudaStream_t s) {
+  k_cons_to_prim<R><<<grid_for(c.g.N, 256), 256, 0, s>>>(c, U, P, T, Ne, Ri, Am);
+}
+template <class R>
+void Launch<R>::init_pass(const Consts& c, const R* U, R* P, Dyn* dyn, cudaStream_t s) {
+  k_init_pass<R><<<grid_for(c.g.N, 256), 256, 0, s>>>(c, U, P, dyn);
+}
+template <class R>
+void Launch<R>::adjust_stats(const Consts& c, const R* U, const R* P, Dyn* dyn, cudaStream_t s) {
+  k_adjust_stats<R><<<grid_for((long long)c.g.nx * c.g.ny * c.g.nz, 256), 256, 0, s>>>(c, U, P, dyn);
+}
+template <class R>
+void Launch<R>::cmax_faces(const Consts& c, const R* U, const R* P, Dyn* dyn, cudaStream_t s) {
+  const Geom& g = c.g;
+  long long n = 2LL * GH * ((long long)g.ny * g.nz + (long long)g.nx * g.nz + (long long)g.nx * g.ny);
+  k_cmax_faces<R><<<grid_for(n, 256), 256, 0, s>>>(c, U, P, dyn);
+}
+template <class R>
+void Launch<R>::source_integrate(const Consts& c, R* U, const R* U0, R* Res, const Dyn* dyn, int stage, cudaStream_t s) {
+  k_source_integrate<R><<<grid_for((long long)c.g.nx * c.g.ny * c.g.nz, 256), 256, 0, s>>>(c, U, U0, Res, dyn, stage);
+}
+template <class R>
+void Launch<R>::save_cons(const Consts& c, const R* U, R* U0, cudaStream_t s) {
+  k_save_cons<R><<<grid_for((long long)c.g.nx * c.g.ny * c.g.nz, 256), 256, 0, s>>>(c.g, U, U0);
+}
+template <class R>
+void Launch<R>::tcheck(const Consts& c, R* U, const Dyn* dyn, cudaStream_t s) {
+  k_tcheck<R><<<grid_for((long long)c.g.nx * c.g.ny * c.g.nz, 256), 256, 0, s>>>(c, U, dyn);
+}
+template <class R>
+void Launch<R>::fill_ghosts(const Consts& c, R* U, int nfield, int with_bc, cudaStream_t s) {
+  k_fill_ghosts<R><<<grid_for(c.g.N, 256), 256, 0, s>>>(c.g, U, nfield, with_bc);
+}
+template <class R>
+void Launch<R>::aos_to_soa(long long N, int nf, const double* A, R* S, cudaStream_t s) {
+  k_aos_to_soa<R><<<grid_for(N, 256), 256, 0, s>>>(N, nf, A, S);
+}
+template <class R>
+void Launch<R>::soa_to_aos(long long N, int nf, const R* S, double* A, cudaStream_t s) {
+  k_soa_to_aos<R><<<grid_for(N, 256), 256, 0, s>>>(N, nf, S, A);
+}
+#endif
+
+}  // namespace gpumhd

@@ -1,0 +1,50 @@
+// FP64 kernels: compiled with --fmad=false so that every product and sum
+// rounds separately, as in the reference's no-FMA builds.
+#define GPUMHD_LAUNCH_IMPL
+#include "gpumhd_launch.cuh"
+
+namespace gpumhd {
+
+template struct Launch<double>;
+
+__global__ void k_step_begin(Consts c, Dyn* dyn, double* dt_hist, int dt_hist_cap) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  if (dyn->err) return;
+  // Adjust_Valf_Max without va_adjust (src/Adjust_Valf_Max.C:136-142); the
+  // fused path runs only in that mode, so the limits are the run constants.
+  dyn->v_lim = c.tchk_vmax;
+  dyn->e_lim = c.tchk_eps_max;
+  const double cmax = __longlong_as_double((long long)dyn->cmax_bits);
+  const double dt_mhd = c.dxmin / cmax;
+  dyn->dt_mhd = dt_mhd;
+  // Sync_timestep (src/solver.C:487-548) on one rank
+  double r0 = c.dt_rad, r1 = dt_mhd;
+  if (bad_pos(r0)) { dyn->err = ERR_BAD_DT_RAD; return; }
+  if (bad_pos(r1)) { dyn->err = ERR_BAD_DT_MHD; return; }
+  const double dt_min_rt = c.rt_tstep * c.CFL * r1;
+  if (r0 < dt_min_rt) r0 = smax(r0, dt_min_rt);
+  const double dt_min = smin(r0, r1);
+  double dt = smin(r0, c.CFL * r1);
+  if (c.outcad > 0) {
+    const double num = dyn->time / c.outcad;
+    const int ce = cvt_x86(num);
+    const double rem = (num == (double)ce) ? 0.0 : (ce + 1) * c.outcad - dyn->time;
+    if (rem > 0.0) dt = smin(dt, rem);
+  }
+  if (c.autostep) dyn->dt = dt;
+  const double cfl = dyn->dt / dt_min;
+  dyn->cfl = cfl;
+  if (cfl >= 2.) { dyn->err = ERR_CFL; return; }
+  // TVD branch (src/solver.C:325-339)
+  dyn->two_half = (cfl <= c.CFL_tvd) ? 0 : 1;
+  dyn->dt_tvd = dyn->two_half ? 0.5 * dyn->dt : dyn->dt;
+  if (dt_hist && dyn->steps_done >= 0 && dyn->steps_done < dt_hist_cap) dt_hist[dyn->steps_done] = dyn->dt;
+  dyn->steps_done += 1;
+  dyn->time += dyn->dt;
+  // the last TVD pass of this step accumulates the next step's values
+  dyn->cmax_bits = 0ULL;
+  dyn->stat_max_bits[0] = dyn->stat_max_bits[1] = dyn->stat_max_bits[2] = 0ULL;
+  dyn->stat_cnt[0] = dyn->stat_cnt[1] = 0ULL;
+}
+
+}  // namespace gpumhd

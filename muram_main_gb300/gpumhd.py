@@ -1,0 +1,306 @@
+"""Python host layer over the gpumhd C ABI (include/gpumhd.h).
+
+``MuramGPU`` mirrors the MURaM routines on the time-step path: each method has
+the reference routine's name and meaning, operating on the device-resident
+GridData of one context.  Host arrays use the reference's cState layout
+(float64 records of 8 values, x fastest, two ghost layers), or the package's
+structure-of-arrays view (8, sz, sy, sx) which ``upload_state`` /
+``download_state`` convert.
+
+The CUDA library must be built (``muram_main_gb300.build.build()``); loading
+fails loudly when it is missing -- there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+OK = 0
+E_INVALID = -1
+E_CUDA = -2
+E_EOS = -3
+E_BAD_DT = -4
+E_CFL = -5
+E_ORDER = -6
+E_NOMEM = -7
+
+FIELD_U, FIELD_U0, FIELD_RES, FIELD_PRES, FIELD_TEMP, FIELD_NE, FIELD_RHOI, FIELD_AMB = range(8)
+
+
+class GpumhdError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"gpumhd error {code}: {msg}")
+        self.code = code
+
+
+class Params(C.Structure):
+    """ctypes mirror of ``gpumhd_params``."""
+    _fields_ = [
+        ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("periodic_x", C.c_int),
+        ("precision", C.c_int), ("pad0", C.c_int),
+        ("dx", C.c_double * 3),
+        ("CFL", C.c_double), ("CFL_tvd", C.c_double), ("dt", C.c_double), ("time", C.c_double),
+        ("outcad", C.c_double), ("autostep", C.c_int), ("pad1", C.c_int),
+        ("grav", C.c_double), ("va_max", C.c_double), ("va_adjust", C.c_double), ("max_fill", C.c_double),
+        ("tvd_h", C.c_double * 4), ("tvd_cs", C.c_double * 4), ("tvd", C.c_double * 10),
+        ("tvd_h_bnd", C.c_double * 2), ("tvd_visc_bnd", C.c_double * 2), ("tvd_eta_bnd", C.c_double * 2),
+        ("tvd_coeff", C.c_double * 4), ("tchk", C.c_double * 4),
+        ("rt_cfl", C.c_double), ("rt_tstep", C.c_double), ("rt_update", C.c_double),
+        ("tau0", C.c_double), ("dt_rad", C.c_double),
+    ]
+
+
+EXPORTS = [
+    "gpumhd_default_params", "gpumhd_create", "gpumhd_destroy", "gpumhd_set_params", "gpumhd_get_params",
+    "gpumhd_last_error", "gpumhd_eos_init", "gpumhd_upload", "gpumhd_download", "gpumhd_save_cons",
+    "gpumhd_cons_to_prim", "gpumhd_adjust_valf_max", "gpumhd_get_limits", "gpumhd_mhd_residual",
+    "gpumhd_sync_timestep", "gpumhd_source_integrate_tcheck", "gpumhd_tvdlimit", "gpumhd_tcheck",
+    "gpumhd_exchange", "gpumhd_run_steps", "gpumhd_enqueue_steps", "gpumhd_synchronize", "gpumhd_step_info",
+    "gpumhd_stream", "gpumhd_launch_count", "gpumhd_profile_steps",
+]
+
+_lib = None
+
+
+def library_path():
+    return _build.LIB
+
+
+def load(build_if_missing=True):
+    """Load libgpumhd.so (building it first if needed) and declare its signatures."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(_build.LIB):
+        if not build_if_missing:
+            raise OSError(f"gpumhd library not built: {_build.LIB}")
+        _build.build()
+    L = C.CDLL(_build.LIB)
+    vp = C.c_void_p
+    dp = C.POINTER(C.c_double)
+    P = C.POINTER(Params)
+    sig = {
+        "gpumhd_default_params": (C.c_int, [P, C.c_int, C.c_int, C.c_int, C.c_double]),
+        "gpumhd_create": (C.c_int, [P, C.c_int, C.POINTER(vp)]),
+        "gpumhd_destroy": (C.c_int, [vp]),
+        "gpumhd_set_params": (C.c_int, [vp, P]),
+        "gpumhd_get_params": (C.c_int, [vp, P]),
+        "gpumhd_last_error": (C.c_char_p, [vp]),
+        "gpumhd_eos_init": (C.c_int, [vp, C.c_char_p]),
+        "gpumhd_upload": (C.c_int, [vp, C.c_int, dp]),
+        "gpumhd_download": (C.c_int, [vp, C.c_int, dp]),
+        "gpumhd_save_cons": (C.c_int, [vp]),
+        "gpumhd_cons_to_prim": (C.c_int, [vp]),
+        "gpumhd_adjust_valf_max": (C.c_int, [vp]),
+        "gpumhd_get_limits": (C.c_int, [vp, dp, dp, dp]),
+        "gpumhd_mhd_residual": (C.c_int, [vp, dp]),
+        "gpumhd_sync_timestep": (C.c_int, [vp, C.c_double, C.c_double, dp]),
+        "gpumhd_source_integrate_tcheck": (C.c_int, [vp, C.c_int]),
+        "gpumhd_tvdlimit": (C.c_int, [vp, C.c_double]),
+        "gpumhd_tcheck": (C.c_int, [vp]),
+        "gpumhd_exchange": (C.c_int, [vp, C.c_int]),
+        "gpumhd_run_steps": (C.c_int, [vp, C.c_int, dp, C.c_int]),
+        "gpumhd_enqueue_steps": (C.c_int, [vp, C.c_int]),
+        "gpumhd_synchronize": (C.c_int, [vp]),
+        "gpumhd_step_info": (C.c_int, [vp, dp, dp, dp, C.POINTER(C.c_int)]),
+        "gpumhd_profile_steps": (C.c_int, [vp, C.c_int, dp]),
+        "gpumhd_stream": (vp, [vp]),
+        "gpumhd_launch_count": (C.c_longlong, [vp]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def default_params(nx, ny, nz, dx=3.2e6, precision=64, **kw):
+    p = Params()
+    load().gpumhd_default_params(C.byref(p), nx, ny, nz, dx)
+    p.precision = precision
+    for k, v in kw.items():
+        if k in ("dy", "dz"):
+            p.dx[1 if k == "dy" else 2] = v
+        elif isinstance(v, (list, tuple, np.ndarray)):
+            arr = getattr(p, k)
+            for i, x in enumerate(v):
+                arr[i] = float(x)
+        else:
+            setattr(p, k, v)
+    return p
+
+
+def _dptr(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class MuramGPU:
+    """One device-resident MURaM grid (a gpumhd context)."""
+
+    def __init__(self, params, device=0, eos_path=None):
+        L = load()
+        self._L = L
+        self.params = params
+        h = C.c_void_p()
+        rc = L.gpumhd_create(C.byref(params), device, C.byref(h))
+        if rc != OK:
+            raise GpumhdError(rc, L.gpumhd_last_error(None).decode())
+        self._h = h
+        self.shape = (params.nz + 4, params.ny + 4, params.nx + 4)
+        if eos_path is not None:
+            self.eos_init(eos_path)
+
+    def _chk(self, rc):
+        if rc != OK:
+            raise GpumhdError(rc, self._L.gpumhd_last_error(self._h).decode())
+        return rc
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.gpumhd_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # -- data movement (ACCH::UpdateGPU / UpdateCPU)
+    def upload(self, which, aos):
+        a = np.ascontiguousarray(aos, dtype=np.float64)
+        self._chk(self._L.gpumhd_upload(self._h, which, _dptr(a)))
+
+    def download(self, which):
+        nf = 8 if which <= FIELD_RES else 1
+        out = np.empty(int(np.prod(self.shape)) * nf, dtype=np.float64)
+        self._chk(self._L.gpumhd_download(self._h, which, _dptr(out)))
+        return out
+
+    def upload_state(self, U, which=FIELD_U):
+        """U: (8, sz, sy, sx) float64 structure of arrays."""
+        self.upload(which, np.moveaxis(np.asarray(U, dtype=np.float64), 0, -1))
+
+    def download_state(self, which=FIELD_U):
+        a = self.download(which)
+        return np.ascontiguousarray(np.moveaxis(a.reshape(self.shape + (8,)), -1, 0))
+
+    def download_field(self, which):
+        return self.download(which).reshape(self.shape)
+
+    def upload_field(self, which, f):
+        self.upload(which, np.asarray(f, dtype=np.float64).reshape(-1))
+
+    # -- the reference routines
+    def eos_init(self, path):
+        self._chk(self._L.gpumhd_eos_init(self._h, os.fsencode(path)))
+
+    def SaveCons(self):
+        self._chk(self._L.gpumhd_save_cons(self._h))
+
+    def ConsToPrim(self):
+        self._chk(self._L.gpumhd_cons_to_prim(self._h))
+
+    def Adjust_Valf_Max(self):
+        self._chk(self._L.gpumhd_adjust_valf_max(self._h))
+
+    def limits(self):
+        a, b, c = C.c_double(), C.c_double(), C.c_double()
+        self._chk(self._L.gpumhd_get_limits(self._h, C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value, c.value
+
+    def MHD_Residual(self):
+        dt = C.c_double()
+        self._chk(self._L.gpumhd_mhd_residual(self._h, C.byref(dt)))
+        return dt.value
+
+    def Sync_timestep(self, dt_rad, dt_mhd):
+        cfl = C.c_double()
+        self._chk(self._L.gpumhd_sync_timestep(self._h, dt_rad, dt_mhd, C.byref(cfl)))
+        return cfl.value
+
+    def Source_Integrate_Tcheck(self, stage):
+        self._chk(self._L.gpumhd_source_integrate_tcheck(self._h, stage))
+
+    def TVDlimit(self, dt_tvd):
+        self._chk(self._L.gpumhd_tvdlimit(self._h, dt_tvd))
+
+    def TCheck(self):
+        self._chk(self._L.gpumhd_tcheck(self._h))
+
+    def exchange_grid(self, with_bc=True):
+        self._chk(self._L.gpumhd_exchange(self._h, 1 if with_bc else 0))
+
+    def step_reference_order(self, dt_rad=None):
+        """One step through the per-routine entry points in ComputeSolution's
+        order (src/solver.C:109-365); returns (dt, cfl)."""
+        p = self.params
+        dt_rad = p.dt_rad if dt_rad is None else dt_rad
+        cfl = 0.0
+        self.SaveCons()
+        for stage in range(1, 5):
+            self.ConsToPrim()
+            if stage == 1:
+                self.Adjust_Valf_Max()
+            dt_mhd = self.MHD_Residual()
+            if stage == 1:
+                cfl = self.Sync_timestep(dt_rad, dt_mhd)
+            self.Source_Integrate_Tcheck(stage)
+            self.exchange_grid(True)
+        dt = self.step_info()[0]
+        if cfl <= p.CFL_tvd:
+            self.TVDlimit(dt)
+        else:
+            self.TVDlimit(0.5 * dt)
+            self.exchange_grid(False)
+            self.TVDlimit(0.5 * dt)
+        self.TCheck()
+        self.exchange_grid(True)
+        return dt, cfl
+
+    # -- fused path
+    def run_steps(self, nsteps, capture=True):
+        dts = np.zeros(max(nsteps, 1))
+        self._chk(self._L.gpumhd_run_steps(self._h, nsteps, _dptr(dts), 1 if capture else 0))
+        return dts[:nsteps]
+
+    def enqueue_steps(self, nsteps):
+        self._chk(self._L.gpumhd_enqueue_steps(self._h, nsteps))
+
+    def synchronize(self):
+        self._chk(self._L.gpumhd_synchronize(self._h))
+
+    def step_info(self):
+        dt, cfl, t = C.c_double(), C.c_double(), C.c_double()
+        two = C.c_int()
+        self._chk(self._L.gpumhd_step_info(self._h, C.byref(dt), C.byref(cfl), C.byref(t), C.byref(two)))
+        return dt.value, cfl.value, t.value, two.value
+
+    PHASES = ["step_control", "stage1", "stage2", "stage3", "stage4", "tvd_x", "tvd_y", "tvd_z",
+              "tvd2_x", "tvd2_y", "tvd2_z"]
+
+    def profile_steps(self, nsteps=2):
+        """Mean duration (ms) of each launch of a fused step, timed with CUDA events."""
+        ms = np.zeros(11)
+        self._chk(self._L.gpumhd_profile_steps(self._h, nsteps, _dptr(ms)))
+        return dict(zip(self.PHASES, ms.tolist()))
+
+    def upload_ptr(self, which, ptr):
+        """Upload from a raw host pointer (e.g. pinned memory) in cState layout."""
+        self._chk(self._L.gpumhd_upload(self._h, which, C.cast(ptr, C.POINTER(C.c_double))))
+
+    def download_ptr(self, which, ptr):
+        self._chk(self._L.gpumhd_download(self._h, which, C.cast(ptr, C.POINTER(C.c_double))))
+
+    @property
+    def stream(self):
+        return self._L.gpumhd_stream(self._h)
+
+    @property
+    def launch_count(self):
+        return self._L.gpumhd_launch_count(self._h)

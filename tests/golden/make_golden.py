@@ -1,0 +1,71 @@
+"""Generate the golden fixtures of the MHD step from the reference itself.
+
+Runs the reference MURaM hot-path sources (compiled unchanged by
+``make -C oracle ref``) through ``oracle/refrun.py`` on small seeded boxes and
+stores, per case, the initial state and the PCAST-style snapshots around each
+routine of one traced step, the state after several steps, and the per-step
+dt.  The EOS table is the committed ``eos_small.dat``.
+
+Usage (in a checkout with the reference sources available):
+    python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import hashlib
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from muram_main_gb300 import initial  # noqa: E402
+from oracle import refrun  # noqa: E402
+
+EOS = os.path.join(HERE, "eos_small.dat")
+
+
+def cases():
+    eos = initial.EosTable(EOS)
+    yield "periodic", dict(nx=12, ny=8, nz=6, dx=3.2e6, periodic_x=1), \
+        initial.periodic_box(eos, 12, 8, 6, seed=11), dict(steps=3, trace_step=1)
+    yield "closed_gravity", dict(nx=16, ny=8, nz=6, dx=1.6e6, periodic_x=0, grav=2.74e4), \
+        initial.stratified_box(eos, 16, 8, 6, dx=1.6e6, seed=12), dict(steps=3, trace_step=2)
+    yield "two_half_tvd", dict(nx=8, ny=8, nz=6, dx=3.2e6, periodic_x=1, CFL=1.2, CFL_tvd=1.0), \
+        initial.periodic_box(eos, 8, 8, 6, seed=13, v_rms=3.0e5, b_rms_gauss=400.0), dict(steps=3, trace_step=1)
+
+
+KEEP = ["init_U", "s1_c2p_U", "s1_c2p_aux", "s1_res_R", "s1_res_dt", "s1_si_U", "s1_bc_U", "s2_c2p_U",
+        "s4_bc_U", "s4_c2p_aux", "tvd_U", "tck_U", "end_U", "final_U", "dts", "limits"]
+
+
+def main():
+    if not refrun.available():
+        refrun.build()
+    manifest = []
+    for name, hp, U, run in cases():
+        hp = dict(hp)
+        hp["eos"] = EOS
+        out = refrun.run(U, hp, **run)
+        arrays = {k: out[k] for k in KEEP if k in out}
+        arrays["input_U"] = U
+        arrays["trace_step"] = np.array(run["trace_step"])
+        arrays["steps"] = np.array(run["steps"])
+        meta = {k: v for k, v in hp.items() if k != "eos"}
+        for k, v in meta.items():
+            arrays["param_" + k] = np.array(v)
+        path = os.path.join(HERE, f"{name}.npz")
+        np.savez_compressed(path, **arrays)
+        h = hashlib.sha256(open(path, "rb").read()).hexdigest()[:16]
+        manifest.append(f"{name}.npz {h} {out['summary'].strip().replace(chr(10), ' ')}")
+        print(manifest[-1])
+    with open(os.path.join(HERE, "MANIFEST.txt"), "w") as fh:
+        fh.write("# golden fixtures from the reference harness (make_golden.py)\n")
+        fh.write(f"eos_small.dat {hashlib.sha256(open(EOS, 'rb').read()).hexdigest()}\n")
+        fh.write("\n".join(manifest) + "\n")
+
+
+if __name__ == "__main__":
+    main()

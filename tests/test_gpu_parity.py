@@ -1,0 +1,161 @@
+"""GPU parity through the C ABI against the reference's golden fixtures and the oracle.
+
+FP64 tolerance: relative L-infinity (max |gpu - ref| / max |ref| per field)
+of 1e-12 -- the bar for the FP64 GPU mode.  The GPU's exp/log differ from the
+host C library by at most a few ulp, so exact equality is not expected where
+the EOS is involved; the observed errors are printed.
+FP32 tolerance: relative L2 per field of 1e-5 after the run.
+"""
+import numpy as np
+import pytest
+
+import helpers as H
+from muram_main_gb300 import gpumhd, initial
+
+TOL64 = 1e-12
+TOL32_L2 = 1e-5
+
+pytestmark = pytest.mark.gpu
+
+
+def ctx_for(hp, precision=64):
+    return gpumhd.MuramGPU(H.gpu_params(hp, precision), eos_path=H.EOS_SMALL)
+
+
+def check(name, got, ref, tol=TOL64):
+    e = H.rel_linf(got, ref)
+    print(f"{name}: rel Linf per field {np.array2string(e, precision=2)}")
+    assert np.all(e <= tol), (name, e)
+
+
+def test_cons_to_prim(gpu_lib):
+    d, hp = H.load_case("periodic")
+    g = ctx_for(hp)
+    g.upload_state(d["init_U"])
+    g.ConsToPrim()
+    check("ConsToPrim U", g.download_state(), d["s1_c2p_U"])
+    aux = np.stack([g.download_field(w) for w in range(gpumhd.FIELD_PRES, gpumhd.FIELD_AMB + 1)])
+    check("ConsToPrim pres/temp/ne/rhoi/amb", aux, d["s1_c2p_aux"])
+
+
+def test_mhd_residual_and_dt(gpu_lib):
+    d, hp = H.load_case("periodic")
+    g = ctx_for(hp)
+    g.upload_state(d["s1_c2p_U"])
+    g.upload_field(gpumhd.FIELD_PRES, d["s1_c2p_aux"][0])
+    g.upload_state(np.zeros_like(d["s1_c2p_U"]), gpumhd.FIELD_RES)
+    g.Adjust_Valf_Max()
+    assert list(g.limits()) == list(d["limits"][:3])
+    dt = g.MHD_Residual()
+    assert abs(dt / d["s1_res_dt"][0] - 1) <= TOL64
+    check("MHD_Residual", g.download_state(gpumhd.FIELD_RES), d["s1_res_R"])
+
+
+def test_source_integrate_and_exchange(gpu_lib):
+    d, hp = H.load_case("periodic")
+    g = ctx_for(hp)
+    g.upload_state(d["s1_c2p_U"])
+    g.upload_state(d["init_U"], gpumhd.FIELD_U0)
+    g.upload_state(d["s1_res_R"], gpumhd.FIELD_RES)
+    g.upload_field(gpumhd.FIELD_PRES, d["s1_c2p_aux"][0])
+    g.Adjust_Valf_Max()
+    cfl = g.Sync_timestep(g.params.dt_rad, float(d["s1_res_dt"][0]))
+    assert g.step_info()[0] == d["dts"][0] and cfl == d["dts"][1]
+    g.Source_Integrate_Tcheck(1)
+    check("Source_Integrate_Tcheck", g.download_state(), d["s1_si_U"])
+    assert not g.download_state(gpumhd.FIELD_RES).any()
+    g.exchange_grid(True)
+    check("exchange+BC", g.download_state(), d["s1_bc_U"])
+
+
+@pytest.mark.parametrize("name", H.CASES)
+def test_tvd_and_tcheck(gpu_lib, name):
+    d, hp = H.load_case(name)
+    g = ctx_for(hp)
+    t = int(d["trace_step"])
+    dt = float(d["dts"][3 * (t - 1)])
+    cfl = float(d["dts"][3 * (t - 1) + 1])
+    g.upload_state(d["s4_bc_U"])
+    g.upload_field(gpumhd.FIELD_PRES, d["s4_c2p_aux"][0])
+    g.upload_field(gpumhd.FIELD_PRES, d["s4_c2p_aux"][0])
+    if cfl <= g.params.CFL_tvd:
+        g.TVDlimit(dt)
+    else:
+        g.TVDlimit(0.5 * dt)
+        g.exchange_grid(False)
+        g.TVDlimit(0.5 * dt)
+    check(f"TVDlimit[{name}]", g.download_state(), d["tvd_U"])
+    g.TCheck()
+    check(f"TCheck[{name}]", g.download_state(), d["tck_U"])
+    g.exchange_grid(True)
+    check(f"final exchange[{name}]", g.download_state(), d["end_U"])
+
+
+@pytest.mark.parametrize("name", H.CASES)
+def test_reference_order_steps(gpu_lib, name):
+    d, hp = H.load_case(name)
+    g = ctx_for(hp)
+    g.upload_state(d["input_U"])
+    g.exchange_grid(True)
+    dts = [g.step_reference_order()[0] for _ in range(int(d["steps"]))]
+    assert np.allclose(dts, d["dts"].reshape(-1, 3)[:, 0], rtol=TOL64, atol=0)
+    check(f"per-routine steps[{name}]", g.download_state(), d["final_U"])
+
+
+@pytest.mark.parametrize("name", H.CASES)
+@pytest.mark.parametrize("capture", [0, 1])
+def test_fused_steps(gpu_lib, name, capture):
+    d, hp = H.load_case(name)
+    g = ctx_for(hp)
+    g.upload_state(d["input_U"])
+    dts = g.run_steps(int(d["steps"]), capture=bool(capture))
+    assert np.allclose(dts, d["dts"].reshape(-1, 3)[:, 0], rtol=TOL64, atol=0)
+    check(f"fused steps[{name}, graph={capture}]", g.download_state(), d["final_U"])
+    assert g.step_info()[3] == (1 if name == "two_half_tvd" else 0)
+
+
+def _oracle_run(hp, U, steps):
+    from oracle import oracle as O
+    eos = O.Eos(H.EOS_SMALL)
+    st = O.State(H.oracle_params(hp), U)
+    dts = st.step(eos, steps)
+    return st.U, dts
+
+
+def test_fused_vs_oracle_anisotropic(gpu_lib):
+    tab = initial.EosTable(H.EOS_SMALL)
+    hp = dict(nx=40, ny=24, nz=20, dx=2.4e6, dy=3.2e6, dz=4.0e6)
+    U = initial.periodic_box(tab, 40, 24, 20, dx=2.4e6, dy=3.2e6, dz=4.0e6, seed=77)
+    ref, dts_ref = _oracle_run(hp, U, 12)
+    p = gpumhd.default_params(40, 24, 20, 2.4e6, dy=3.2e6, dz=4.0e6)
+    g = gpumhd.MuramGPU(p, eos_path=H.EOS_SMALL)
+    g.upload_state(U)
+    dts = g.run_steps(12)
+    assert np.allclose(dts, [x[0] for x in dts_ref], rtol=TOL64, atol=0)
+    check("fused vs oracle, 40x24x20, 12 steps", g.download_state(), ref)
+
+
+def test_fused_fp64_100_steps(gpu_lib):
+    """The FP64 bar: relative L-infinity <= 1e-12 after 100 steps (32^3 periodic box)."""
+    tab = initial.EosTable(H.EOS_SMALL)
+    hp = dict(nx=32, ny=32, nz=32)
+    U = initial.periodic_box(tab, 32, 32, 32, seed=5)
+    ref, _ = _oracle_run(hp, U, 100)
+    g = gpumhd.MuramGPU(gpumhd.default_params(32, 32, 32, 3.2e6), eos_path=H.EOS_SMALL)
+    g.upload_state(U)
+    g.run_steps(100)
+    check("FP64 fused vs oracle, 32^3, 100 steps", H.interior(g.download_state()), H.interior(ref))
+
+
+def test_fused_fp32_error_vs_fp64_oracle(gpu_lib):
+    """FP32 storage and arithmetic: relative L2 per field after 100 steps."""
+    tab = initial.EosTable(H.EOS_SMALL)
+    hp = dict(nx=32, ny=32, nz=32)
+    U = initial.periodic_box(tab, 32, 32, 32, seed=5)
+    ref, _ = _oracle_run(hp, U, 100)
+    g = gpumhd.MuramGPU(gpumhd.default_params(32, 32, 32, 3.2e6, precision=32), eos_path=H.EOS_SMALL)
+    g.upload_state(U)
+    g.run_steps(100)
+    e = H.rel_l2(H.interior(g.download_state()), H.interior(ref))
+    print("FP32 vs FP64 oracle rel L2 per field:", np.array2string(e, precision=2))
+    assert np.all(e <= TOL32_L2), e

@@ -1,0 +1,114 @@
+"""The C restatement (oracle) against the reference's own outputs.
+
+The golden fixtures were produced by the reference MURaM sources compiled
+unchanged (tests/golden/make_golden.py); every comparison here is bit-exact.
+When the reference harness binary is present (it is built only where the
+reference sources exist), extra seeded cases are compared live.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import helpers as H
+from muram_main_gb300 import initial
+from oracle import oracle as O
+from oracle import refrun
+
+
+@pytest.fixture(scope="module")
+def eos():
+    return O.Eos(H.EOS_SMALL)
+
+
+@pytest.mark.parametrize("name", H.CASES)
+def test_full_steps_bitexact(name, eos):
+    d, hp = H.load_case(name)
+    st = O.State(H.oracle_params(hp), d["input_U"])
+    assert np.array_equal(st.U, d["init_U"])
+    dts = st.step(eos, int(d["steps"]))
+    ref = d["dts"].reshape(-1, 3)
+    assert [x[0] for x in dts] == list(ref[:, 0])
+    assert [x[1] for x in dts] == list(ref[:, 1])
+    assert np.array_equal(st.U, d["final_U"])
+
+
+def test_routines_bitexact_periodic(eos):
+    d, hp = H.load_case("periodic")
+    p = H.oracle_params(hp)
+    L = O.lib()
+    U = d["init_U"].copy()
+    aux = np.zeros((5,) + U.shape[1:])
+    L.mo_cons_to_prim(C.byref(p), eos.ptr, U, aux[0], aux[1], aux[2], aux[3], aux[4])
+    assert np.array_equal(U, d["s1_c2p_U"])
+    assert np.array_equal(aux, d["s1_c2p_aux"])
+    L.mo_adjust_valf_max(C.byref(p), U, aux[0], np.zeros(5))
+    assert [p.inv_va2max, p.v_lim, p.e_lim] == list(d["limits"][:3])
+    R = np.zeros_like(U)
+    dt = L.mo_mhd_residual(C.byref(p), U, aux[0], R)
+    assert dt == d["s1_res_dt"][0]
+    assert np.array_equal(R, d["s1_res_R"])
+    cfl = C.c_double()
+    assert L.mo_sync_timestep(C.byref(p), p.dt_rad, dt, C.byref(cfl)) == 0
+    assert p.dt == d["dts"][0]
+    U0 = d["init_U"].copy()
+    L.mo_source_integrate_tcheck(C.byref(p), U, U0, R, 1)
+    assert np.array_equal(U, d["s1_si_U"])
+    assert not R.any()
+    L.mo_boundaries(C.byref(p), U)
+    assert np.array_equal(U, d["s1_bc_U"])
+    # TVD of the traced step on its stage-4 state with the stale pressure
+    U = d["s4_bc_U"].copy()
+    L.mo_tvdlimit(C.byref(p), U, np.ascontiguousarray(d["s4_c2p_aux"][0]), p.dt)
+    assert np.array_equal(U, d["tvd_U"])
+    L.mo_tcheck(C.byref(p), U)
+    assert np.array_equal(U, d["tck_U"])
+    L.mo_boundaries(C.byref(p), U)
+    assert np.array_equal(U, d["end_U"])
+
+
+def test_eos_interpolation_exact_at_nodes(eos):
+    """Known answer: at a table node the bilinear lookup returns exp of the node value."""
+    t = initial.EosTable(H.EOS_SMALL)
+    i, j = 37, 61
+    ee = float(np.exp(t.xeps[i]) - t.eps_off)
+    rho = float(np.exp(t.xlr[j]))
+    lnT = float(t.tables[1][i, j]) * t.del_eps * t.del_lr
+    assert abs(t.T_interp(ee, rho) / np.exp(lnT) - 1.0) < 1e-6
+
+
+def test_uniform_state_is_stationary(eos):
+    """Known answer: a uniform state at rest has zero residual and an unchanged TVD pass."""
+    p = O.make_params(8, 8, 8, 3.2e6)
+    U = np.zeros((8, 12, 12, 12))
+    U[0] = 3e-7
+    U[4] = 3e-7 * 6e11
+    U[5] = 1.0
+    L = O.lib()
+    aux = np.zeros((5,) + U.shape[1:])
+    W = U.copy()
+    L.mo_cons_to_prim(C.byref(p), eos.ptr, W, aux[0], aux[1], aux[2], aux[3], aux[4])
+    L.mo_adjust_valf_max(C.byref(p), W, aux[0], np.zeros(5))
+    R = np.zeros_like(U)
+    L.mo_mhd_residual(C.byref(p), W, aux[0], R)
+    assert np.all(H.interior(R) == 0.0)
+    V = U.copy()
+    p.dt = 1.0
+    L.mo_tvdlimit(C.byref(p), V, aux[0], 1.0)
+    assert np.allclose(V, U, rtol=1e-15, atol=0)
+
+
+@pytest.mark.skipif(not refrun.available(), reason="reference harness not built here")
+@pytest.mark.parametrize("seed", [101, 202])
+def test_live_reference_random_boxes(seed, eos):
+    """Extra seeded boxes, anisotropic and non-cubic, run by the reference and the oracle."""
+    tab = initial.EosTable(H.EOS_SMALL)
+    rng = np.random.default_rng(seed)
+    nx, ny, nz = (int(v) for v in rng.integers(5, 11, size=3))
+    U = initial.periodic_box(tab, nx, ny, nz, dx=2.4e6, dy=3.2e6, dz=4.0e6, seed=seed,
+                             v_rms=float(rng.uniform(0.5e5, 3e5)), b_rms_gauss=float(rng.uniform(20, 600)))
+    hp = dict(nx=nx, ny=ny, nz=nz, dx=2.4e6, dy=3.2e6, dz=4.0e6, eos=H.EOS_SMALL)
+    ref = refrun.run(U, hp, steps=4)
+    st = O.State(H.oracle_params(hp), U)
+    st.step(eos, 4)
+    assert np.array_equal(st.U, ref["final_U"])
