@@ -14,18 +14,30 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_BIN = os.path.join(HERE, "_ref", "muram_ref_harness")
+DROPIN_BIN = os.path.join(HERE, "_ref", "muram_gpu_dropin")
+# where the reference sources are mounted in the build container
+REF_ROOT = os.environ.get("MURAM_REF", "/root/reference")
 
 
 def available():
     return os.path.exists(REF_BIN)
 
 
-def build(ref_root="/root/reference"):
+def build(ref_root=REF_ROOT):
     """Compile the reference harness if the reference sources exist."""
     if not os.path.isdir(ref_root):
         return False
     subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={ref_root}", "-j8"], check=True)
     return available()
+
+
+def build_dropin(ref_root=REF_ROOT):
+    """Link the reference harness against the MURaM-side shim and libgpumhd.so
+    instead of the reference's hot-path objects (a link-level drop-in check)."""
+    if not os.path.isdir(ref_root):
+        return False
+    subprocess.run(["make", "-s", "-C", HERE, "dropin", f"REF={ref_root}", "-j8"], check=True)
+    return os.path.exists(DROPIN_BIN)
 
 
 def run(U, params, steps=1, trace_step=0, keep=None):

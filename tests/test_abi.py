@@ -71,3 +71,24 @@ def test_create_rejects_bad_grid_without_gpu_work():
     h = C.c_void_p()
     assert L.gpumhd_create(C.byref(p), 0, C.byref(h)) == gpumhd.E_INVALID
     assert b">= 4" in L.gpumhd_last_error(None)
+
+
+def test_dropin_links_in_place_of_reference_routines():
+    """The MURaM-side shim, linked with the reference's non-hot-path objects and
+    the harness that calls the routines by their reference names, resolves every
+    hot-path routine to the shim (link-level drop-in; needs the reference sources)."""
+    from oracle import refrun
+    if not os.path.isdir(refrun.REF_ROOT):
+        pytest.skip("reference sources not available")
+    build.build()
+    assert refrun.build_dropin()
+    out = subprocess.run(["nm", "-C", refrun.DROPIN_BIN], capture_output=True, text=True, check=True).stdout
+    shim_obj = os.path.join(os.path.dirname(refrun.DROPIN_BIN), "obj", "gpumhd_muram_shim.o")
+    shim_syms = subprocess.run(["nm", "-C", "--defined-only", shim_obj], capture_output=True, text=True,
+                               check=True).stdout
+    for fn in ("SaveCons(", "ConsToPrim(", "Adjust_Valf_Max(", "MHD_Residual(", "Source_Integrate_Tcheck(",
+               "TVDlimit(", "TCheck(", "exchange_grid_acc(", "SetBoundaryConditions("):
+        assert fn in shim_syms, fn
+        assert out.count(" T " + fn) == 1, fn
+    ldd = subprocess.run(["ldd", refrun.DROPIN_BIN], capture_output=True, text=True, check=True).stdout
+    assert "libgpumhd.so" in ldd
