@@ -50,7 +50,10 @@ def build(force=False, verbose=False):
     nvcc = nvcc_path()
     common = [nvcc, "-std=c++17", ARCH, "-O3", "-lineinfo", "-Xcompiler", "-fPIC,-ffp-contract=off",
               "-I", INCLUDE, "-c"]
-    units = [("kernels_f64.cu", ["--fmad=false"]), ("kernels_f32.cu", ["--fmad=true"]),
+    # FP32: contraction, approximate division and square root (within the
+    # FP32 mode's error budget); FP64: every operation IEEE-rounded.
+    units = [("kernels_f64.cu", ["--fmad=false"]),
+             ("kernels_f32.cu", ["--fmad=true", "-prec-div=false", "-prec-sqrt=false"]),
              ("gpumhd.cu", ["--fmad=false"])]
     procs = []
     objs = []

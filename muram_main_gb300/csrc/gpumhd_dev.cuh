@@ -218,26 +218,41 @@ __device__ __forceinline__ double eos_pres(const Consts& c, double d, double ei,
   return exp(s);
 }
 
+// ln(1+t) and exp(d) for the small arguments of the FP32 pressure patch:
+// truncated Taylor series (errors below 1e-9 for |t| <= 0.03, |d| <= 0.1),
+// the library functions outside that range.
+__device__ __forceinline__ float log1p_small(float t) {
+  if (fabsf(t) > 0.03f) return logf(1.0f + t);
+  return t * (1.0f + t * (-0.5f + t * (0.33333334f + t * (-0.25f + t * 0.2f))));
+}
+__device__ __forceinline__ float exp_small(float d) {
+  if (fabsf(d) > 0.1f) return expf(d);
+  return 1.0f + d * (1.0f + d * (0.5f + d * (0.16666667f + d * (0.041666668f + d * (0.008333334f + d * 0.0013888889f)))));
+}
+
 // Pressure only, FP32.  The bilinear patch of ln p is re-expanded around its
 // lower corner, p = P00 * exp(fe*a + fr*b + fe*fr*c), with the offsets
-// fe = ln(eps) - xeps[i] and fr = ln(rho) - xlr[j] taken as logs of ratios
-// near one; this keeps ~1e-7 relative accuracy where the direct float sum of
-// the pre-divided table terms would lose ~1e-6.
+// fe = ln(eps) - xeps[i] and fr = ln(rho) - xlr[j] taken as ln of ratios near
+// one; this keeps ~1e-7 relative accuracy where the direct float sum of the
+// pre-divided table terms would lose ~1e-6.  The cell index only needs the
+// hardware log2: an index off by one at a cell edge selects the neighbouring
+// patch, which agrees there to the table's rounding.
 __device__ __forceinline__ float eos_pres(const Consts& c, float d, float ei, float dn) {
+  constexpr float LN2 = 0.69314718f;
   const float eps = ei * dn + (float)c.eps_off;
-  const float lgr = logf(d);
-  const float ep = logf(eps);
-  if (!(lgr >= (float)c.xlr0 && lgr < (float)c.xlrN + 1.0f && ep > (float)c.xeps0 - 1.0f &&
+  const float lgr = __log2f(d) * LN2;
+  const float ep = __log2f(eps) * LN2;
+  if (!(lgr >= (float)c.xlr0 + 0.01f && lgr < (float)c.xlrN + 1.0f && ep > (float)c.xeps0 - 1.0f &&
         ep < (float)c.xepsN + 1.0f && !(eps > 0.8f * (float)c.eps_max)))
     return (float)c2p_eos_full(c, (double)d, (double)ei, 1.0 / (double)d).pres;
   int i_d = (int)((lgr - (float)c.xlr0) * (float)c.inv_del_lr);
   i_d = max(0, min(c.N_lr - 2, i_d));
   int i_e = (int)((ep - (float)c.xeps0) * (float)c.inv_del_eps);
   i_e = max(0, min(c.N_eps - 2, i_e));
-  const float fe = logf(eps * __ldg(c.inv_exp_xeps + i_e));
-  const float fr = logf(d * __ldg(c.inv_exp_xlr + i_d));
+  const float fe = log1p_small(eps * __ldg(c.inv_exp_xeps + i_e) - 1.0f);
+  const float fr = log1p_small(d * __ldg(c.inv_exp_xlr + i_d) - 1.0f);
   const float4 q = __ldg(c.pquad + (long long)i_e * c.N_lr + i_d);
-  return q.x * expf(fe * q.y + fr * q.z + fe * fr * q.w);
+  return q.x * exp_small(fe * q.y + fr * q.z + fe * fr * q.w);
 }
 
 // ------------------------------------------------------------ Tcheck cell

@@ -20,52 +20,66 @@ namespace gpumhd {
 // change sign).  xmirror = 0 restricts the images to the periodic dimensions
 // (the exchange between TVD half steps does not apply the x boundary rule).
 struct Images {
-  int n;
-  long long idx[8];
-  unsigned char flip[8];
+  int xa, ya, za;   // index of the image across x / y / z, -1 if none
+  int xf;           // the x image is a mirror (sign flips)
 };
 
 __device__ __forceinline__ Images images_of(const Geom& g, int i, int j, int k, bool xmirror) {
-  int xs[2], ys[2], zs[2];
-  unsigned char xf[2] = {0, 0};
-  int nxo = 1, nyo = 1, nzo = 1;
-  xs[0] = i; ys[0] = j; zs[0] = k;
+  Images im;
+  im.xa = -1; im.ya = -1; im.za = -1; im.xf = 0;
   const int I = i - GH, J = j - GH, K = k - GH;
   if (g.periodic_x) {
-    if (I < GH) xs[nxo++] = i + g.nx;
-    else if (I >= g.nx - GH) xs[nxo++] = i - g.nx;
+    if (I < GH) im.xa = i + g.nx;
+    else if (I >= g.nx - GH) im.xa = i - g.nx;
   } else if (xmirror) {
-    if (I < GH) { xs[nxo] = 2 * GH - 1 - i; xf[nxo++] = 1; }
-    else if (I >= g.nx - GH) { xs[nxo] = 2 * GH + 2 * g.nx - 1 - i; xf[nxo++] = 1; }
+    if (I < GH) { im.xa = 2 * GH - 1 - i; im.xf = 1; }
+    else if (I >= g.nx - GH) { im.xa = 2 * GH + 2 * g.nx - 1 - i; im.xf = 1; }
   }
-  if (J < GH) ys[nyo++] = j + g.ny;
-  else if (J >= g.ny - GH) ys[nyo++] = j - g.ny;
-  if (K < GH) zs[nzo++] = k + g.nz;
-  else if (K >= g.nz - GH) zs[nzo++] = k - g.nz;
-  Images im;
-  im.n = 0;
-  for (int c = 0; c < nzo; c++)
-    for (int b = 0; b < nyo; b++)
-      for (int a = 0; a < nxo; a++) {
-        im.idx[im.n] = cidx(g, xs[a], ys[b], zs[c]);
-        im.flip[im.n] = xf[a];
-        im.n++;
-      }
+  if (J < GH) im.ya = j + g.ny;
+  else if (J >= g.ny - GH) im.ya = j - g.ny;
+  if (K < GH) im.za = k + g.nz;
+  else if (K >= g.nz - GH) im.za = k - g.nz;
   return im;
 }
 
+// Calls f(index, mirrored) for the cell itself and each of its ghost images.
+template <class F>
+__device__ __forceinline__ void for_images(const Geom& g, int i, int j, int k, const Images& im, F f) {
+#pragma unroll
+  for (int c = 0; c < 2; c++) {
+    const int kk = c ? im.za : k;
+    if (kk < 0) continue;
+#pragma unroll
+    for (int b = 0; b < 2; b++) {
+      const int jj = b ? im.ya : j;
+      if (jj < 0) continue;
+#pragma unroll
+      for (int a = 0; a < 2; a++) {
+        const int ii = a ? im.xa : i;
+        if (ii < 0) continue;
+        f(cidx(g, ii, jj, kk), a && im.xf);
+      }
+    }
+  }
+}
+
 template <class R>
-__device__ __forceinline__ void store_state(const Geom& g, R* __restrict__ U, const Images& im, const R v[NV]) {
-  for (int m = 0; m < im.n; m++) {
-    const long long id = im.idx[m];
-    const bool f = im.flip[m];
+__device__ __forceinline__ void store_state(const Geom& g, R* __restrict__ U, int i, int j, int k, const Images& im,
+                                            const R v[NV]) {
+  for_images(g, i, j, k, im, [&](long long id, bool f) {
 #pragma unroll
     for (int q = 0; q < NV; q++) {
       R x = v[q];
       if (f && (q == 1 || q == 6 || q == 7)) x = -x;
       U[(long long)q * g.N + id] = x;
     }
-  }
+  });
+}
+
+template <class R>
+__device__ __forceinline__ void store_scalar(const Geom& g, R* __restrict__ P, int i, int j, int k, const Images& im,
+                                             R v) {
+  for_images(g, i, j, k, im, [&](long long id, bool) { P[id] = v; });
 }
 
 // -------------------------------------------------------------- primitives
@@ -181,6 +195,40 @@ __device__ __forceinline__ void add_direction(R* Racc, const R* fm2, const R* fm
 }
 
 // ------------------------------------------------------------ stage kernel
+// Shared memory holds 12 values per cell contiguously (primitives padded to
+// 12, or the 12 flux quantities), moved with 16-byte vector accesses.  With a
+// 12-float stride the 128-bit accesses of a quarter warp to consecutive cells
+// hit distinct banks; FP64 keeps the 12-value stride (2-way conflicts) to fit
+// two blocks per SM.
+template <class R> struct CellW { static constexpr int W = 12; };
+
+__device__ __forceinline__ void load_cell(const float* p, float v[12]) {
+  const float4* q = reinterpret_cast<const float4*>(p);
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    float4 t = q[a];
+    v[4 * a] = t.x; v[4 * a + 1] = t.y; v[4 * a + 2] = t.z; v[4 * a + 3] = t.w;
+  }
+}
+__device__ __forceinline__ void store_cell(float* p, const float v[12]) {
+  float4* q = reinterpret_cast<float4*>(p);
+#pragma unroll
+  for (int a = 0; a < 3; a++) q[a] = make_float4(v[4 * a], v[4 * a + 1], v[4 * a + 2], v[4 * a + 3]);
+}
+__device__ __forceinline__ void load_cell(const double* p, double v[12]) {
+  const double2* q = reinterpret_cast<const double2*>(p);
+#pragma unroll
+  for (int a = 0; a < 6; a++) {
+    double2 t = q[a];
+    v[2 * a] = t.x; v[2 * a + 1] = t.y;
+  }
+}
+__device__ __forceinline__ void store_cell(double* p, const double v[12]) {
+  double2* q = reinterpret_cast<double2*>(p);
+#pragma unroll
+  for (int a = 0; a < 6; a++) q[a] = make_double2(v[2 * a], v[2 * a + 1]);
+}
+
 template <int TX, int TY>
 struct StageSmem {
   static constexpr int PW = TX + 4, PH = TY + 4;
@@ -188,7 +236,9 @@ struct StageSmem {
   static constexpr int FBN = (PW * TY > TX * PH) ? PW * TY : TX * PH;
   static constexpr int NZ = TX * TY;
   template <class R>
-  static constexpr size_t bytes() { return sizeof(R) * ((size_t)NPRIM * NPP + (size_t)NF * FBN + (size_t)5 * NF * NZ); }
+  static constexpr size_t bytes() {
+    return sizeof(R) * CellW<R>::W * ((size_t)NPP + (size_t)FBN + (size_t)5 * NZ);
+  }
 };
 
 // RESID = false: fused RK stage.  Uin: conserved state with filled ghosts,
@@ -203,9 +253,10 @@ __global__ void __launch_bounds__(TX* TY) k_stage(Consts c, const R* __restrict_
                                                   int stage, int zc, int write_pres) {
   using S = StageSmem<TX, TY>;
   extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int CW = CellW<R>::W;
   R* PP = reinterpret_cast<R*>(smem_raw);
-  R* FB = PP + NPRIM * S::NPP;
-  R* FZ = FB + NF * S::FBN;
+  R* FB = PP + CW * S::NPP;
+  R* FZ = FB + CW * S::FBN;
   const Geom& g = c.g;
   if (!RESID && dyn->err) return;
   const int tid = threadIdx.x;
@@ -217,14 +268,18 @@ __global__ void __launch_bounds__(TX* TY) k_stage(Consts c, const R* __restrict_
   const bool active = (i < GH + g.nx) && (j < GH + g.ny);
   const R inv_va2max = (R)dyn->inv_va2max;
   const R w1x = (R)c.w1[0], w2x = (R)c.w2[0], w1y = (R)c.w1[1], w2y = (R)c.w2[1], w1z = (R)c.w1[2], w2z = (R)c.w2[2];
-  R prim[NPRIM];
+  R prim[NF];
+  R fl[NF];
+  prim[NPRIM] = (R)0;
 
   // z-flux ring: slot of plane kk is (kk - zb + 2) mod 5
   auto zslot = [&](int kk) { return ((kk - zb + 2) % 5 + 5) % 5; };
+  auto zcell = [&](int kk) { return FZ + ((size_t)zslot(kk) * S::NZ + tid) * CW; };
   auto fill_z = [&](int kk) {
     if (!active) return;
     load_prim11<R, RESID>(g, Uin, Pin, cidx(g, i, j, kk), prim, 1);
-    flux12<R, 2>(prim, 1, FZ + (size_t)zslot(kk) * NF * S::NZ + tid, S::NZ);
+    flux12<R, 2>(prim, 1, fl, 1);
+    store_cell(zcell(kk), fl);
   };
   for (int kk = zb - 2; kk < zb + 2; kk++) fill_z(kk);
 
@@ -237,26 +292,28 @@ __global__ void __launch_bounds__(TX* TY) k_stage(Consts c, const R* __restrict_
       if (m < S::PW * TY) { lx = m % S::PW - 2; ly = m / S::PW; }
       else { int r = m - S::PW * TY; lx = r % TX; int q = r / TX; ly = q < 2 ? q - 2 : TY + q - 2; }
       const int gi = x0 + lx, gj = y0 + ly;
-      R* dst = PP + (ly + 2) * S::PW + (lx + 2);
+      R* dst = PP + ((ly + 2) * S::PW + (lx + 2)) * CW;
       if (gi >= 0 && gi < g.sx && gj >= 0 && gj < g.sy)
-        load_prim11<R, RESID>(g, Uin, Pin, cidx(g, gi, gj, k), dst, S::NPP);
+        load_prim11<R, RESID>(g, Uin, Pin, cidx(g, gi, gj, k), prim, 1);
       else
-        for (int q = 0; q < NPRIM; q++) dst[q * S::NPP] = (R)1.0;
+        for (int q = 0; q < NPRIM; q++) prim[q] = (R)1.0;
+      store_cell(dst, prim);
     }
     __syncthreads();
     // x fluxes on (TX+4) x TY
     for (int m = tid; m < S::PW * TY; m += TX * TY) {
       const int lx = m % S::PW, ly = m / S::PW;
-      flux12<R, 0>(PP + (ly + 2) * S::PW + lx, S::NPP, FB + ly * S::PW + lx, S::FBN);
+      load_cell(PP + ((ly + 2) * S::PW + lx) * CW, prim);
+      flux12<R, 0>(prim, 1, fl, 1);
+      store_cell(FB + (ly * S::PW + lx) * CW, fl);
     }
     __syncthreads();
     R Racc[NV];
-    R cen[NPRIM];
+    R cen[NF];
     R lf = (R)0;
     const int pc = (ty + 2) * S::PW + (tx + 2);
     if (active) {
-#pragma unroll
-      for (int q = 0; q < NPRIM; q++) cen[q] = PP[q * S::NPP + pc];
+      load_cell(PP + pc * CW, cen);
       const long long id = cidx(g, i, j, k);
       if (RESID) {
 #pragma unroll
@@ -271,24 +328,36 @@ __global__ void __launch_bounds__(TX* TY) k_stage(Consts c, const R* __restrict_
       const R va2 = bb * dn;
       const R x2 = va2 * inv_va2max, x4 = x2 * x2, s = (R)1.0 + x2;
       lf = s / (s + x4);
-      const R* fb = FB + ty * S::PW + (tx + 2);
-      add_direction<R, 0>(Racc, fb - 2, fb - 1, fb + 1, fb + 2, S::FBN, w1x, w2x, cen, lf);
+      const R* fb = FB + (ty * S::PW + (tx + 2)) * CW;
+      R n0[NF], n1[NF], n2[NF], n3[NF];
+      load_cell(fb - 2 * CW, n0);
+      load_cell(fb - CW, n1);
+      load_cell(fb + CW, n2);
+      load_cell(fb + 2 * CW, n3);
+      add_direction<R, 0>(Racc, n0, n1, n2, n3, 1, w1x, w2x, cen, lf);
     }
     __syncthreads();
     // y fluxes on TX x (TY+4)
     for (int m = tid; m < TX * S::PH; m += TX * TY) {
       const int lx = m % TX, ly = m / TX;
-      flux12<R, 1>(PP + ly * S::PW + (lx + 2), S::NPP, FB + ly * TX + lx, S::FBN);
+      load_cell(PP + (ly * S::PW + (lx + 2)) * CW, prim);
+      flux12<R, 1>(prim, 1, fl, 1);
+      store_cell(FB + (ly * TX + lx) * CW, fl);
     }
     __syncthreads();
     if (active) {
-      const R* fb = FB + (ty + 2) * TX + tx;
-      add_direction<R, 1>(Racc, fb - 2 * TX, fb - TX, fb + TX, fb + 2 * TX, S::FBN, w1y, w2y, cen, lf);
-      const R* zm2 = FZ + (size_t)zslot(k - 2) * NF * S::NZ + tid;
-      const R* zm1 = FZ + (size_t)zslot(k - 1) * NF * S::NZ + tid;
-      const R* zp1 = FZ + (size_t)zslot(k + 1) * NF * S::NZ + tid;
-      const R* zp2 = FZ + (size_t)zslot(k + 2) * NF * S::NZ + tid;
-      add_direction<R, 2>(Racc, zm2, zm1, zp1, zp2, S::NZ, w1z, w2z, cen, lf);
+      const R* fb = FB + ((ty + 2) * TX + tx) * CW;
+      R n0[NF], n1[NF], n2[NF], n3[NF];
+      load_cell(fb - 2 * TX * CW, n0);
+      load_cell(fb - TX * CW, n1);
+      load_cell(fb + TX * CW, n2);
+      load_cell(fb + 2 * TX * CW, n3);
+      add_direction<R, 1>(Racc, n0, n1, n2, n3, 1, w1y, w2y, cen, lf);
+      load_cell(zcell(k - 2), n0);
+      load_cell(zcell(k - 1), n1);
+      load_cell(zcell(k + 1), n2);
+      load_cell(zcell(k + 2), n3);
+      add_direction<R, 2>(Racc, n0, n1, n2, n3, 1, w1z, w2z, cen, lf);
       const long long id = cidx(g, i, j, k);
       if (RESID) {
 #pragma unroll
@@ -333,12 +402,12 @@ __global__ void __launch_bounds__(TX* TY) k_stage(Consts c, const R* __restrict_
         const R emax = (R)(dyn->e_lim > 0.0 ? dyn->e_lim : c.tchk_eps_max);
         tcheck_cell<R>(c, vmax, emax, un[0], un[1], un[2], un[3], un[4]);
         const Images im = images_of(g, i, j, k, true);
-        store_state<R>(g, Uout, im, un);
+        store_state<R>(g, Uout, i, j, k, im, un);
         if (write_pres) {
           R v1, v2, v3, ei;
           prim_from_cons(un[0], un[1], un[2], un[3], un[4], v1, v2, v3, ei);
           const R pr = eos_pres(c, un[0], ei, (R)1.0 / un[0]);
-          for (int m = 0; m < im.n; m++) Pout[im.idx[m]] = pr;
+          store_scalar<R>(g, Pout, i, j, k, im, pr);
         }
         (void)dt;
       }
@@ -591,19 +660,19 @@ __global__ void __launch_bounds__(128) k_tvd_sweep(Consts c, const R* __restrict
       } else if (half_images) {
         // first of two half steps: exchange (periodic dimensions) only
         int ci = DIR == 0 ? pos : aa, cj = DIR == 1 ? pos : (DIR == 0 ? aa : bb), ck = DIR == 2 ? pos : bb;
-        store_state<R>(g, Uout, images_of(g, ci, cj, ck, false), u);
+        store_state<R>(g, Uout, ci, cj, ck, images_of(g, ci, cj, ck, false), u);
       } else if (final_pass) {
         const R vmax = (R)(dyn->v_lim > 0.0 ? dyn->v_lim : c.tchk_vmax);
         const R emax = (R)(dyn->e_lim > 0.0 ? dyn->e_lim : c.tchk_eps_max);
         tcheck_cell<R>(c, vmax, emax, u[0], u[1], u[2], u[3], u[4]);
         int ci = DIR == 0 ? pos : aa, cj = DIR == 1 ? pos : (DIR == 0 ? aa : bb), ck = DIR == 2 ? pos : bb;
         const Images im = images_of(g, ci, cj, ck, true);
-        store_state<R>(g, Uout, im, u);
+        store_state<R>(g, Uout, ci, cj, ck, im, u);
         // next step's stage-1 pressure, CFL speed and Adjust_Valf_Max statistics
         R v1, v2, v3, ei;
         prim_from_cons(u[0], u[1], u[2], u[3], u[4], v1, v2, v3, ei);
         const R pr = eos_pres(c, u[0], ei, (R)1.0 / u[0]);
-        for (int m = 0; m < im.n; m++) Pout[im.idx[m]] = pr;
+        store_scalar<R>(g, Pout, ci, cj, ck, im, pr);
         R cmv = cmax_cell<R>(u[0], v1, v2, v3, u[5], u[6], u[7], pr, inv_va2max);
         cmax_loc = smax(cmax_loc, cmv);
         R vabs = d_sqrt(v1 * v1 + v2 * v2 + v3 * v3);
@@ -640,6 +709,92 @@ __global__ void __launch_bounds__(128) k_tvd_sweep(Consts c, const R* __restrict
       }
     }
   }
+}
+
+// --------------------------------------------------- TVD sweep along x, by lanes
+// The x pencils are contiguous in memory, so here a warp holds 32 consecutive
+// cells of one pencil, one per lane (coalesced loads and stores), and the
+// stencil neighbours come from warp shuffles: 28 cells are updated per warp,
+// the two lanes at each end are the sweep's halo.  Same arithmetic as
+// k_tvd_sweep<R, 0>; used for the plain (mode 0) x sweep.
+template <class R>
+__device__ __forceinline__ R shfl(R v, int src) { return __shfl_sync(0xffffffffu, v, src); }
+
+template <class R>
+__device__ __forceinline__ void shfl_cell(const TCell<R>& in, TCell<R>& out, int src) {
+#pragma unroll
+  for (int v = 0; v < NV; v++) out.q[v] = shfl(in.q[v], src);
+  out.cm = shfl(in.cm, src); out.he = shfl(in.he, src); out.hv = shfl(in.hv, src); out.hB = shfl(in.hB, src);
+  out.BC2 = shfl(in.BC2, src); out.bsqr = shfl(in.bsqr, src); out.vsqr = shfl(in.vsqr, src);
+  out.hd = shfl(in.hd, src); out.hb = shfl(in.hb, src); out.ht = shfl(in.ht, src); out.qt = shfl(in.qt, src);
+}
+
+template <class R>
+__global__ void __launch_bounds__(128) k_tvd_sweep_xlanes(Consts c, const R* __restrict__ Uin, const R* __restrict__ Pst,
+                                                          R* __restrict__ Uout, Dyn* __restrict__ dyn, int only_two_half) {
+  const Geom& g = c.g;
+  if (dyn->err) return;
+  if (only_two_half && !dyn->two_half) return;
+  constexpr int OUT = 28;
+  const int lane = threadIdx.x & 31;
+  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int nseg = (g.nx + OUT - 1) / OUT;
+  const long long npen = (long long)g.sy * g.sz;
+  if (warp >= npen * nseg) return;   // whole warps exit together
+  const int seg = (int)(warp % nseg);
+  const long long pen = warp / nseg;
+  const int j = (int)(pen % g.sy), k = (int)(pen / g.sy);
+  const long long base = cidx(g, 0, j, k);
+  const int pos = GH + OUT * seg - 2 + lane;          // this lane's cell along x
+  const int posc = min(pos, g.sx - 1);                 // clamped for the tail of the last segment
+  const double dt_tvd = dyn->dt_tvd;
+  const R dtt = (R)dt_tvd;
+  const R cmax_t = (R)(0.975 * c.dx[0] / dt_tvd);
+  const R fac0 = (R)(0.5 * c.idx[0]);
+  const R inv_va2max = (R)dyn->inv_va2max;
+  const R vsqr_diff = (R)dyn->vsqr_diff;
+  const bool hyper = c.vhyp > 0.0;
+  const int istart = 1 + (g.periodic_x ? 0 : GH);
+  const int sz = g.nx + 2 * GH;
+  TCell<R> c0, cl, cr, crr;
+  tvd_load<R>(c, Uin, Pst, base + posc, posc, cmax_t, fac0, hyper, inv_va2max, c0);
+  shfl_cell(c0, cl, max(lane - 1, 0));
+  shfl_cell(c0, cr, min(lane + 1, 31));
+  shfl_cell(c0, crr, min(lane + 2, 31));
+  R s0[NV], s1[NV], F[NV], Fm[NV];
+  tvd_slope<R>(c, cl, c0, cr, vsqr_diff, s0);
+#pragma unroll
+  for (int v = 0; v < NV; v++) s1[v] = shfl(s0[v], min(lane + 1, 31));
+  R qr;
+  tvd_flux<R, 0>(c, cl, c0, cr, crr, s0, s1, pos, sz, fac0, cmax_t, hyper, istart, F, qr);
+#pragma unroll
+  for (int v = 0; v < NV; v++) Fm[v] = shfl(F[v], max(lane - 1, 0));
+  const R qm = shfl(qr, max(lane - 1, 0));
+  if (lane < 2 || lane >= 30 || pos >= GH + g.nx) return;
+  R res[NV];
+#pragma unroll
+  for (int v = 0; v < NV; v++) res[v] = dtt * (F[v] - Fm[v]);
+  res[4] += ((R)1.0 - c0.qt) * (res[1] * c0.q[1] + res[2] * c0.q[2] + res[3] * c0.q[3]);
+  {
+    R dn = (res[1] * c0.q[5] + res[2] * c0.q[6] + res[3] * c0.q[7]) / smax(tiny100<R>(), c0.bsqr);
+    R b0 = -c0.BC2 * (res[1] - dn * c0.q[5]);
+    R b1 = -c0.BC2 * (res[2] - dn * c0.q[6]);
+    R b2 = -c0.BC2 * (res[3] - dn * c0.q[7]);
+    R b3 = b0 * c0.q[1] + b1 * c0.q[2] + b2 * c0.q[3];
+    res[1] += b0; res[2] += b1; res[3] += b2; res[4] += b3;
+  }
+  {
+    R qres = (R)0.5 * (qr + qm) * c0.qt;
+    res[4] += dtt * qres;
+  }
+  const long long id = base + pos;
+  R u[NV];
+#pragma unroll
+  for (int v = 0; v < NV; v++) u[v] = Uin[(long long)v * g.N + id] + res[v];
+  u[0] = smax((R)c.rho_min, u[0]);
+  u[4] = smax(u[4], (R)c.eps_min * u[0] + (R)0.5 * (u[1] * u[1] + u[2] * u[2] + u[3] * u[3]) / u[0]);
+#pragma unroll
+  for (int v = 0; v < NV; v++) Uout[(long long)v * g.N + id] = u[v];
 }
 
 // ---------------------------------------------------------- small kernels

@@ -106,6 +106,13 @@ void Launch<R>::tvd(const Consts& c, int dir, int mode, int only_two_half, const
   const long long total = (long long)ta.na * ta.nb * nch;
   const int block = 128;
   const long long blocks = (total + block - 1) / block;
+  if (dir == 0 && mode == 0) {
+    // contiguous pencils: one cell per lane, 28 updates per warp
+    const long long warps = (long long)g.sy * g.sz * ((g.nx + 27) / 28);
+    const long long nb = (warps * 32 + block - 1) / block;
+    k_tvd_sweep_xlanes<R><<<(unsigned)nb, block, 0, s>>>(c, Uin, Pst, Uout, dyn, only_two_half);
+    return;
+  }
   if (dir == 0) k_tvd_sweep<R, 0><<<(unsigned)blocks, block, 0, s>>>(c, Uin, Pst, Uout, Pout, dyn, ta);
   else if (dir == 1) k_tvd_sweep<R, 1><<<(unsigned)blocks, block, 0, s>>>(c, Uin, Pst, Uout, Pout, dyn, ta);
   else k_tvd_sweep<R, 2><<<(unsigned)blocks, block, 0, s>>>(c, Uin, Pst, Uout, Pout, dyn, ta);
