@@ -40,6 +40,7 @@ struct gpumhd_ctx {
   float* d_inv_xeps = nullptr;
   float* d_inv_xlr = nullptr;
   double* d_prof = nullptr;
+  float* d_prof_f = nullptr;
   bool eos_loaded = false;
   // per-routine state flags
   bool have_pres = false;
@@ -97,6 +98,34 @@ extern "C" int gpumhd_default_params(gpumhd_params* p, int nx, int ny, int nz, d
 
 static inline double stdmax(double a, double b) { return (a < b) ? b : a; }
 static inline double stdmin(double a, double b) { return (b < a) ? b : a; }
+
+// Copy the run constants into the kernels' per-type sets (FP64: unchanged
+// values; FP32: rounded once here).
+template <class R>
+static void fill_kc(const Consts& c, KC<R>& k, const R* prof) {
+  k.eps_off = (R)c.eps_off; k.xeps0 = (R)c.xeps0; k.xlr0 = (R)c.xlr0; k.xepsN = (R)c.xepsN; k.xlrN = (R)c.xlrN;
+  k.inv_del_eps = (R)c.inv_del_eps; k.inv_del_lr = (R)c.inv_del_lr; k.eps_max = (R)c.eps_max;
+  k.rho_min = (R)c.rho_min; k.eps_min = (R)c.eps_min; k.rho_lev = (R)c.rho_lev; k.q_rho_max = (R)c.q_rho_max;
+  k.visc_coeff_bot = (R)c.visc_coeff_bot; k.visc_slope_bot = (R)c.visc_slope_bot;
+  k.visc_coeff_top = (R)c.visc_coeff_top; k.visc_slope_top = (R)c.visc_slope_top;
+  k.eta_coeff_bot = (R)c.eta_coeff_bot; k.eta_slope_bot = (R)c.eta_slope_bot;
+  k.eta_coeff_top = (R)c.eta_coeff_top; k.eta_slope_top = (R)c.eta_slope_top;
+  k.B_par_diff = (R)c.B_par_diff; k.vhyp = (R)c.vhyp; k.pm_v = (R)c.pm_v; k.pm_B = (R)c.pm_B;
+  k.CME_thresh = (R)c.CME_thresh;
+  for (int i = 0; i < 4; i++) { k.tvd_h[i] = (R)c.tvd_h[i]; k.tvd_cs[i] = (R)c.tvd_cs[i]; k.tvd_coeff[i] = (R)c.tvd_coeff[i]; }
+  k.CZ = (R)c.CZ; k.tchk_vmax = (R)c.tchk_vmax; k.tchk_eps_max = (R)c.tchk_eps_max; k.gx = (R)c.gx;
+  for (int d = 0; d < 3; d++) { k.w1[d] = (R)c.w1[d]; k.w2[d] = (R)c.w2[d]; }
+  k.hfb = prof; k.hft = prof + c.g.sx; k.qft = prof + 2 * c.g.sx;
+  k.has_visc_slope = (c.visc_slope_bot > 0.0 || c.visc_slope_top > 0.0);
+  k.has_eta_slope = (c.eta_slope_bot > 0.0 || c.eta_slope_top > 0.0);
+  k.has_vmax_lim = (c.vmax_lim > 0.0);
+  k.has_vhyp = (c.vhyp > 0.0);
+}
+
+static void fill_kcs(gpumhd_ctx* ctx) {
+  fill_kc<double>(ctx->c, ctx->c.kd, ctx->d_prof);
+  fill_kc<float>(ctx->c, ctx->c.kf, ctx->d_prof_f);
+}
 
 // Run constants derived from the parameters, computed with the host math
 // library exactly as the reference computes them.
@@ -156,9 +185,13 @@ static int fill_consts(gpumhd_ctx* ctx) {
   }
   if (!ctx->d_prof) CK(cudaMalloc(&ctx->d_prof, sizeof(double) * 3 * g.sx));
   CK(cudaMemcpy(ctx->d_prof, prof.data(), sizeof(double) * 3 * g.sx, cudaMemcpyHostToDevice));
+  std::vector<float> proff(prof.begin(), prof.end());
+  if (!ctx->d_prof_f) CK(cudaMalloc(&ctx->d_prof_f, sizeof(float) * 3 * g.sx));
+  CK(cudaMemcpy(ctx->d_prof_f, proff.data(), sizeof(float) * 3 * g.sx, cudaMemcpyHostToDevice));
   c.hfb = ctx->d_prof;
   c.hft = ctx->d_prof + g.sx;
   c.qft = ctx->d_prof + 2 * g.sx;
+  fill_kcs(ctx);
   return GPUMHD_OK;
 }
 
@@ -289,6 +322,7 @@ extern "C" int gpumhd_destroy(gpumhd_ctx* ctx) {
   cudaFree(ctx->d_inv_xeps);
   cudaFree(ctx->d_inv_xlr);
   cudaFree(ctx->d_prof);
+  cudaFree(ctx->d_prof_f);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return GPUMHD_OK;
@@ -323,6 +357,7 @@ extern "C" int gpumhd_set_params(gpumhd_ctx* ctx, const gpumhd_params* p) {
   for (int t = 0; t < 6; t++) c.tab[t] = keep.tab[t];
   c.pquad = keep.pquad; c.inv_exp_xeps = keep.inv_exp_xeps; c.inv_exp_xlr = keep.inv_exp_xlr;
   c.c_pres = keep.c_pres; c.c_temp = keep.c_temp; c.kb = keep.kb; c.mun_mh = keep.mun_mh;
+  fill_kcs(ctx);
   ctx->hdyn.dt = p->dt;
   ctx->hdyn.time = p->time;
   if (ctx->graph) { cudaGraphExecDestroy(ctx->graph); ctx->graph = nullptr; }
@@ -414,6 +449,7 @@ extern "C" int gpumhd_eos_init(gpumhd_ctx* ctx, const char* path) {
   c.c_pres = (eos_gamma - 1.);
   c.kb = kb;
   c.mun_mh = eos_mu_n * mh;
+  fill_kcs(ctx);
   ctx->eos_loaded = true;
   if (ctx->graph) { cudaGraphExecDestroy(ctx->graph); ctx->graph = nullptr; }
   return GPUMHD_OK;

@@ -22,6 +22,25 @@ struct Geom {
   int pad;
 };
 
+// Run constants in the kernel's own type, converted once on the host: the
+// FP32 kernels never touch the (slow) FP64 pipe for them, and the FP64 copies
+// are the original values.
+template <class R>
+struct KC {
+  R eps_off, xeps0, xlr0, xepsN, xlrN, inv_del_eps, inv_del_lr, eps_max;
+  R rho_min, eps_min, rho_lev, q_rho_max;
+  R visc_coeff_bot, visc_slope_bot, visc_coeff_top, visc_slope_top;
+  R eta_coeff_bot, eta_slope_bot, eta_coeff_top, eta_slope_top;
+  R B_par_diff, vhyp, pm_v, pm_B, CME_thresh;
+  R tvd_h[4], tvd_cs[4], tvd_coeff[4];
+  R CZ, tchk_vmax, tchk_eps_max, gx;
+  R w1[3], w2[3];
+  const R* hfb;   // vertical boundary profiles, length sx
+  const R* hft;
+  const R* qft;
+  int has_visc_slope, has_eta_slope, has_vmax_lim, has_vhyp;
+};
+
 // Constants of a run (copied by value into every kernel).
 struct Consts {
   Geom g;
@@ -55,7 +74,13 @@ struct Consts {
   double va_max, va_adjust, max_fill;
   int autostep;
   int pad2;
+  KC<float> kf;
+  KC<double> kd;
 };
+
+template <class R> __device__ __forceinline__ const KC<R>& kc(const Consts& c);
+template <> __device__ __forceinline__ const KC<float>& kc<float>(const Consts& c) { return c.kf; }
+template <> __device__ __forceinline__ const KC<double>& kc<double>(const Consts& c) { return c.kd; }
 
 // Values that change during a run; live in device memory.
 struct Dyn {
@@ -239,15 +264,16 @@ __device__ __forceinline__ float exp_small(float d) {
 // patch, which agrees there to the table's rounding.
 __device__ __forceinline__ float eos_pres(const Consts& c, float d, float ei, float dn) {
   constexpr float LN2 = 0.69314718f;
-  const float eps = ei * dn + (float)c.eps_off;
+  const KC<float>& k = c.kf;
+  const float eps = ei * dn + k.eps_off;
   const float lgr = __log2f(d) * LN2;
   const float ep = __log2f(eps) * LN2;
-  if (!(lgr >= (float)c.xlr0 + 0.01f && lgr < (float)c.xlrN + 1.0f && ep > (float)c.xeps0 - 1.0f &&
-        ep < (float)c.xepsN + 1.0f && !(eps > 0.8f * (float)c.eps_max)))
+  if (!(lgr >= k.xlr0 + 0.01f && lgr < k.xlrN + 1.0f && ep > k.xeps0 - 1.0f && ep < k.xepsN + 1.0f &&
+        !(eps > 0.8f * k.eps_max)))
     return (float)c2p_eos_full(c, (double)d, (double)ei, 1.0 / (double)d).pres;
-  int i_d = (int)((lgr - (float)c.xlr0) * (float)c.inv_del_lr);
+  int i_d = (int)((lgr - k.xlr0) * k.inv_del_lr);
   i_d = max(0, min(c.N_lr - 2, i_d));
-  int i_e = (int)((ep - (float)c.xeps0) * (float)c.inv_del_eps);
+  int i_e = (int)((ep - k.xeps0) * k.inv_del_eps);
   i_e = max(0, min(c.N_eps - 2, i_e));
   const float fe = log1p_small(eps * __ldg(c.inv_exp_xeps + i_e) - 1.0f);
   const float fr = log1p_small(d * __ldg(c.inv_exp_xlr + i_d) - 1.0f);
@@ -259,7 +285,7 @@ __device__ __forceinline__ float eos_pres(const Consts& c, float d, float ei, fl
 // src/Add_Sources_Integrate_SR.C:444-465 and :600-617
 template <class R>
 __device__ __forceinline__ void tcheck_cell(const Consts& c, R vmax, R eps_max, R& d, R& m1, R& m2, R& m3, R& e) {
-  const R rho_min = (R)c.rho_min, eps_min = (R)c.eps_min;
+  const R rho_min = kc<R>(c).rho_min, eps_min = kc<R>(c).eps_min;
   R dn = d_fmax(rho_min, d);
   R vv = d_sqrt(m1 * m1 + m2 * m2 + m3 * m3) / dn;
   R s = vmax / d_fmax(vmax, vv);

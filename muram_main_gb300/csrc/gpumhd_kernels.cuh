@@ -266,8 +266,15 @@ __global__ void __launch_bounds__(TX* TY) k_stage(Consts c, const R* __restrict_
   const int ze = min(zb + zc, GH + g.nz);
   const int i = x0 + tx, j = y0 + ty;
   const bool active = (i < GH + g.nx) && (j < GH + g.ny);
+  const KC<R>& kk_ = kc<R>(c);
   const R inv_va2max = (R)dyn->inv_va2max;
-  const R w1x = (R)c.w1[0], w2x = (R)c.w2[0], w1y = (R)c.w1[1], w2y = (R)c.w2[1], w1z = (R)c.w1[2], w2z = (R)c.w2[2];
+  const R w1x = kk_.w1[0], w2x = kk_.w2[0], w1y = kk_.w1[1], w2y = kk_.w2[1], w1z = kk_.w1[2], w2z = kk_.w2[2];
+  // per-step scalars, converted once (src/Add_Sources_Integrate_SR.C:44, 84-85)
+  const double dtd = RESID ? 1.0 : dyn->dt;
+  const R wdt = (R)(dtd / (double)(4 + 1 - stage));
+  const R invRdt = (R)(c.rt_cfl / dtd);
+  const R vmax = (R)(dyn->v_lim > 0.0 ? dyn->v_lim : c.tchk_vmax);
+  const R emax = (R)(dyn->e_lim > 0.0 ? dyn->e_lim : c.tchk_eps_max);
   R prim[NF];
   R fl[NF];
   prim[NPRIM] = (R)0;
@@ -367,15 +374,11 @@ __global__ void __launch_bounds__(TX* TY) k_stage(Consts c, const R* __restrict_
         atomic_max_nonneg(&dyn->cmax_bits, (double)cm);
       } else {
         // sources, Boris correction, update, Tcheck (src/Add_Sources_Integrate_SR.C:331-465)
-        const double dtd = dyn->dt;
-        const R dt = (R)dtd;
-        const R wdt = (R)(dtd / (double)(4 + 1 - stage));
-        const R invRdt = (R)(c.rt_cfl / dtd);
         const R rh = cen[P_D], vx = cen[P_V1], vy = cen[P_V2], vz = cen[P_V3];
         const R bx = cen[P_B1], by = cen[P_B2], bz = cen[P_B3];
         R dn = invRdt * cen[P_EI];
         R efaci = (dn > (R)0 && dn < (R)INFINITY) ? (R)1.0 : dn / d_fmax(dn, (R)0.0);
-        dn = (R)c.gx * rh - (R)0.0;
+        dn = kk_.gx * rh - (R)0.0;
         const R edmp = dn * vx;
         Racc[1] += dn;
         Racc[4] += edmp + (R)0.0 * efaci;
@@ -398,8 +401,6 @@ __global__ void __launch_bounds__(TX* TY) k_stage(Consts c, const R* __restrict_
         R un[NV];
 #pragma unroll
         for (int v = 0; v < NV; v++) un[v] = U0[(long long)v * g.N + id] + wdt * Racc[v];
-        const R vmax = (R)(dyn->v_lim > 0.0 ? dyn->v_lim : c.tchk_vmax);
-        const R emax = (R)(dyn->e_lim > 0.0 ? dyn->e_lim : c.tchk_eps_max);
         tcheck_cell<R>(c, vmax, emax, un[0], un[1], un[2], un[3], un[4]);
         const Images im = images_of(g, i, j, k, true);
         store_state<R>(g, Uout, i, j, k, im, un);
@@ -409,7 +410,6 @@ __global__ void __launch_bounds__(TX* TY) k_stage(Consts c, const R* __restrict_
           const R pr = eos_pres(c, un[0], ei, (R)1.0 / un[0]);
           store_scalar<R>(g, Pout, i, j, k, im, pr);
         }
-        (void)dt;
       }
     }
     __syncthreads();
@@ -438,13 +438,14 @@ template <class R>
 __device__ __forceinline__ void tvd_load(const Consts& c, const R* __restrict__ U, const R* __restrict__ P, long long id,
                                          int xi, R cmax_t, R fac0, bool hyper, R inv_va2max, TCell<R>& t) {
   const Geom& g = c.g;
-  const R rho_min = (R)c.rho_min;
+  const KC<R>& k = kc<R>(c);
+  const R rho_min = k.rho_min;
   R d = smax(rho_min, U[id]);
   R v1 = U[g.N + id], v2 = U[2 * g.N + id], v3 = U[3 * g.N + id], e = U[4 * g.N + id];
   R b5 = U[5 * g.N + id], b6 = U[6 * g.N + id], b7 = U[7 * g.N + id];
-  t.hb = (R)c.hfb[xi];
-  t.ht = (R)c.hft[xi];
-  t.qt = (R)c.qft[xi];
+  t.hb = k.hfb[xi];
+  t.ht = k.hft[xi];
+  t.qt = k.qft[xi];
   R dn = (R)1.0 / d;
   v1 = v1 * dn;
   v2 = v2 * dn;
@@ -460,25 +461,25 @@ __device__ __forceinline__ void tvd_load(const Consts& c, const R* __restrict__ 
   R lf = s / (s + x4);
   R cs2 = (R)(5.0 / 3.0) * P[id] * dn;
   R cfast = d_sqrt(va2 + cs2);
-  const R CZ = (R)c.CZ;
-  R CME = ((R)1.0 - CZ) * ((R)(vv >= (R)c.CME_thresh * cfast));
+  const R CZ = k.CZ;
+  R CME = ((R)1.0 - CZ) * ((R)(vv >= k.CME_thresh * cfast));
   dn = d * d;
-  R rf = smin(lf, dn / (dn + (R)c.rho_lev));
+  R rf = smin(lf, dn / (dn + k.rho_lev));
   R hh = (R)1.0 - t.hb - t.ht;
-  R cf = t.hb * (R)c.tvd_cs[0] + (rf * (R)c.tvd_cs[1] + ((R)1.0 - rf) * (R)c.tvd_cs[2]) * hh + t.ht * (R)c.tvd_cs[3];
+  R cf = t.hb * k.tvd_cs[0] + (rf * k.tvd_cs[1] + ((R)1.0 - rf) * k.tvd_cs[2]) * hh + t.ht * k.tvd_cs[3];
   cf = smax(cf, CME);
   cs2 *= cf * cf;
   t.cm = (R)0.0 + vv + d_sqrt(smax(cs2, lf * (cs2 + va2)));
-  const R h0 = (R)c.tvd_h[0], h1 = (R)c.tvd_h[1], h2 = (R)c.tvd_h[2], h3 = (R)c.tvd_h[3];
+  const R h0 = k.tvd_h[0], h1 = k.tvd_h[1], h2 = k.tvd_h[2], h3 = k.tvd_h[3];
   t.he = t.hb * h0 + (rf * h1 + ((R)1.0 - rf) * h2) * hh + t.ht * h3;
-  t.hv = t.hb * h0 + (rf * h1 + ((R)1.0 - rf) * h2 * (R)c.pm_v) * hh + t.ht * h3 * (R)c.pm_v;
-  t.hB = t.hb * h0 + (rf * h1 + ((R)1.0 - rf) * h2 * (R)c.pm_B) * hh + t.ht * h3 * (R)c.pm_B;
+  t.hv = t.hb * h0 + (rf * h1 + ((R)1.0 - rf) * h2 * k.pm_v) * hh + t.ht * h3 * k.pm_v;
+  t.hB = t.hb * h0 + (rf * h1 + ((R)1.0 - rf) * h2 * k.pm_B) * hh + t.ht * h3 * k.pm_B;
   t.he *= ((R)1.0 - CME);
   t.hv *= ((R)1.0 - CME);
   t.BC2 = (R)1.0 - lf;
   t.hd = (R)0;
   if (hyper) {
-    R h = (R)c.vhyp * d_sqrt(t.vsqr);
+    R h = k.vhyp * d_sqrt(t.vsqr);
     t.hd = fac0 * smax((R)0.0, smin(h, cmax_t - t.cm));
   }
   if (c.rho_log) {
@@ -501,17 +502,18 @@ __device__ __forceinline__ void tvd_slope(const Consts& c, const TCell<R>& a, co
     R upper = smax(smax(sl, sr), slm);
     slp[v] = smax((R)0.0, lower) + smin((R)0.0, upper);
   }
-  if (c.visc_slope_bot > 0.0 || c.visc_slope_top > 0.0) {
-    R cf = ((R)1.0 - (R)c.visc_slope_bot * b.hb) * ((R)1.0 - (R)c.visc_slope_top * b.ht);
+  const KC<R>& k = kc<R>(c);
+  if (k.has_visc_slope) {
+    R cf = ((R)1.0 - k.visc_slope_bot * b.hb) * ((R)1.0 - k.visc_slope_top * b.ht);
     slp[1] *= cf; slp[2] *= cf; slp[3] *= cf;
   }
-  if (c.eta_slope_bot > 0.0 || c.eta_slope_top > 0.0) {
-    R cf = ((R)1.0 - (R)c.eta_slope_bot * b.hb) * ((R)1.0 - (R)c.eta_slope_top * b.ht);
+  if (k.has_eta_slope) {
+    R cf = ((R)1.0 - k.eta_slope_bot * b.hb) * ((R)1.0 - k.eta_slope_top * b.ht);
     slp[5] *= cf; slp[6] *= cf; slp[7] *= cf;
   }
   R qr = c.rho_log ? d_fabs(b.q[0] - n.q[0]) : d_fabs(d_log(b.q[0]) - d_log(n.q[0]));
-  if (qr > (R)c.q_rho_max) slp[0] = (R)0.0;
-  if (c.vmax_lim > 0.0 && b.vsqr > vsqr_diff) { slp[1] = (R)0.0; slp[2] = (R)0.0; slp[3] = (R)0.0; }
+  if (qr > k.q_rho_max) slp[0] = (R)0.0;
+  if (k.has_vmax_lim && b.vsqr > vsqr_diff) { slp[1] = (R)0.0; slp[2] = (R)0.0; slp[3] = (R)0.0; }
 }
 
 // Interface flux between cells a (index ia) and b, plus its resistive-heating
@@ -533,13 +535,14 @@ __device__ __forceinline__ void tvd_flux(const Consts& c, const TCell<R>& am, co
   R fac = fac0 * smin(cmax_t, smax(a.cm, b.cm));
 #pragma unroll
   for (int v = 0; v < NV; v++) F[v] *= fac;
-  F[5 + DIR] *= (R)c.B_par_diff;
+  const KC<R>& k = kc<R>(c);
+  F[5 + DIR] *= k.B_par_diff;
   if (c.need_coeff) {
-    F[0] *= (R)c.tvd_coeff[0];
-    R cf = smax((R)c.tvd_coeff[1], (R)c.visc_coeff_bot * a.hb + (R)c.visc_coeff_top * a.ht);
+    F[0] *= k.tvd_coeff[0];
+    R cf = smax(k.tvd_coeff[1], k.visc_coeff_bot * a.hb + k.visc_coeff_top * a.ht);
     F[1] *= cf; F[2] *= cf; F[3] *= cf;
-    F[4] *= (R)c.tvd_coeff[2];
-    cf = smax((R)c.tvd_coeff[3], (R)c.eta_coeff_bot * a.hb + (R)c.eta_coeff_top * a.ht);
+    F[4] *= k.tvd_coeff[2];
+    cf = smax(k.tvd_coeff[3], k.eta_coeff_bot * a.hb + k.eta_coeff_top * a.ht);
     F[5] *= cf; F[6] *= cf; F[7] *= cf;
   }
   if (DIR == 0 && hyper && ia >= istart) {
@@ -558,7 +561,7 @@ __device__ __forceinline__ void tvd_flux(const Consts& c, const TCell<R>& am, co
     u[4] = d_exp(u[4]);
     f4 *= u[4];
   }
-  const R CZ = (R)c.CZ;
+  const R CZ = k.CZ;
   R min_cz = f0 * smin(CZ, CZ);
   f1 *= u[0]; f1 += u[1] * min_cz;
   f2 *= u[0]; f2 += u[2] * min_cz;
@@ -602,7 +605,11 @@ __global__ void __launch_bounds__(128) k_tvd_sweep(Consts c, const R* __restrict
   const R fac0 = (R)(0.5 * c.idx[DIR]);
   const R inv_va2max = (R)dyn->inv_va2max;
   const R vsqr_diff = (R)dyn->vsqr_diff;
-  const bool hyper = (DIR == 0) && (c.vhyp > 0.0);
+  const bool hyper = (DIR == 0) && kc<R>(c).has_vhyp;
+  const KC<R>& kk_ = kc<R>(c);
+  const R vmax = (R)(dyn->v_lim > 0.0 ? dyn->v_lim : c.tchk_vmax);
+  const R emax = (R)(dyn->e_lim > 0.0 ? dyn->e_lim : c.tchk_eps_max);
+  const R vlim95 = (R)(dyn->v_lim * 0.95), elim95 = (R)(dyn->e_lim * 0.95);
   const int istart = 1 + (c.g.periodic_x ? 0 : GH);
   // final pass: TCheck, full ghost images, next step's pressure and statistics;
   // half_images: after the first of two half passes only the periodic exchange
@@ -652,8 +659,8 @@ __global__ void __launch_bounds__(128) k_tvd_sweep(Consts c, const R* __restrict
       R u[NV];
 #pragma unroll
       for (int v = 0; v < NV; v++) u[v] = Uin[(long long)v * g.N + id] + res[v];
-      u[0] = smax((R)c.rho_min, u[0]);
-      u[4] = smax(u[4], (R)c.eps_min * u[0] + (R)0.5 * (u[1] * u[1] + u[2] * u[2] + u[3] * u[3]) / u[0]);
+      u[0] = smax(kk_.rho_min, u[0]);
+      u[4] = smax(u[4], kk_.eps_min * u[0] + (R)0.5 * (u[1] * u[1] + u[2] * u[2] + u[3] * u[3]) / u[0]);
       if (ta.mode == 0) {
 #pragma unroll
         for (int v = 0; v < NV; v++) Uout[(long long)v * g.N + id] = u[v];
@@ -662,8 +669,6 @@ __global__ void __launch_bounds__(128) k_tvd_sweep(Consts c, const R* __restrict
         int ci = DIR == 0 ? pos : aa, cj = DIR == 1 ? pos : (DIR == 0 ? aa : bb), ck = DIR == 2 ? pos : bb;
         store_state<R>(g, Uout, ci, cj, ck, images_of(g, ci, cj, ck, false), u);
       } else if (final_pass) {
-        const R vmax = (R)(dyn->v_lim > 0.0 ? dyn->v_lim : c.tchk_vmax);
-        const R emax = (R)(dyn->e_lim > 0.0 ? dyn->e_lim : c.tchk_eps_max);
         tcheck_cell<R>(c, vmax, emax, u[0], u[1], u[2], u[3], u[4]);
         int ci = DIR == 0 ? pos : aa, cj = DIR == 1 ? pos : (DIR == 0 ? aa : bb), ck = DIR == 2 ? pos : bb;
         const Images im = images_of(g, ci, cj, ck, true);
@@ -681,8 +686,8 @@ __global__ void __launch_bounds__(128) k_tvd_sweep(Consts c, const R* __restrict
         st_v = d_fmax(st_v, vabs);
         st_c = d_fmax(st_c, cs);
         st_e = d_fmax(st_e, ee);
-        if ((double)vabs >= dyn->v_lim * 0.95) cnt_v++;
-        if ((double)ee >= dyn->e_lim * 0.95) cnt_e++;
+        if (vabs >= vlim95) cnt_v++;
+        if (ee >= elim95) cnt_e++;
       }
       // shift the window
       cm1 = c0; c0 = c1; c1 = c2;
@@ -737,64 +742,67 @@ __global__ void __launch_bounds__(128) k_tvd_sweep_xlanes(Consts c, const R* __r
   if (only_two_half && !dyn->two_half) return;
   constexpr int OUT = 28;
   const int lane = threadIdx.x & 31;
-  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nseg = (g.nx + OUT - 1) / OUT;
-  const long long npen = (long long)g.sy * g.sz;
-  if (warp >= npen * nseg) return;   // whole warps exit together
-  const int seg = (int)(warp % nseg);
-  const long long pen = warp / nseg;
-  const int j = (int)(pen % g.sy), k = (int)(pen / g.sy);
-  const long long base = cidx(g, 0, j, k);
-  const int pos = GH + OUT * seg - 2 + lane;          // this lane's cell along x
-  const int posc = min(pos, g.sx - 1);                 // clamped for the tail of the last segment
+  const long long total = (long long)g.sy * g.sz * nseg;
+  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
   const double dt_tvd = dyn->dt_tvd;
   const R dtt = (R)dt_tvd;
   const R cmax_t = (R)(0.975 * c.dx[0] / dt_tvd);
   const R fac0 = (R)(0.5 * c.idx[0]);
   const R inv_va2max = (R)dyn->inv_va2max;
   const R vsqr_diff = (R)dyn->vsqr_diff;
-  const bool hyper = c.vhyp > 0.0;
+  const bool hyper = kc<R>(c).has_vhyp;
+  const KC<R>& kk_ = kc<R>(c);
   const int istart = 1 + (g.periodic_x ? 0 : GH);
   const int sz = g.nx + 2 * GH;
-  TCell<R> c0, cl, cr, crr;
-  tvd_load<R>(c, Uin, Pst, base + posc, posc, cmax_t, fac0, hyper, inv_va2max, c0);
-  shfl_cell(c0, cl, max(lane - 1, 0));
-  shfl_cell(c0, cr, min(lane + 1, 31));
-  shfl_cell(c0, crr, min(lane + 2, 31));
-  R s0[NV], s1[NV], F[NV], Fm[NV];
-  tvd_slope<R>(c, cl, c0, cr, vsqr_diff, s0);
+  // whole warps stride over (pencil, segment) pairs together
+  for (long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; warp < total; warp += nwarps) {
+    const int seg = (int)(warp % nseg);
+    const long long pen = warp / nseg;
+    const int j = (int)(pen % g.sy), k = (int)(pen / g.sy);
+    const long long base = cidx(g, 0, j, k);
+    const int pos = GH + OUT * seg - 2 + lane;          // this lane's cell along x
+    const int posc = min(pos, g.sx - 1);                 // clamped for the tail of the last segment
+    TCell<R> c0, cl, cr, crr;
+    tvd_load<R>(c, Uin, Pst, base + posc, posc, cmax_t, fac0, hyper, inv_va2max, c0);
+    shfl_cell(c0, cl, max(lane - 1, 0));
+    shfl_cell(c0, cr, min(lane + 1, 31));
+    shfl_cell(c0, crr, min(lane + 2, 31));
+    R s0[NV], s1[NV], F[NV], Fm[NV];
+    tvd_slope<R>(c, cl, c0, cr, vsqr_diff, s0);
 #pragma unroll
-  for (int v = 0; v < NV; v++) s1[v] = shfl(s0[v], min(lane + 1, 31));
-  R qr;
-  tvd_flux<R, 0>(c, cl, c0, cr, crr, s0, s1, pos, sz, fac0, cmax_t, hyper, istart, F, qr);
+    for (int v = 0; v < NV; v++) s1[v] = shfl(s0[v], min(lane + 1, 31));
+    R qr;
+    tvd_flux<R, 0>(c, cl, c0, cr, crr, s0, s1, pos, sz, fac0, cmax_t, hyper, istart, F, qr);
 #pragma unroll
-  for (int v = 0; v < NV; v++) Fm[v] = shfl(F[v], max(lane - 1, 0));
-  const R qm = shfl(qr, max(lane - 1, 0));
-  if (lane < 2 || lane >= 30 || pos >= GH + g.nx) return;
-  R res[NV];
+    for (int v = 0; v < NV; v++) Fm[v] = shfl(F[v], max(lane - 1, 0));
+    const R qm = shfl(qr, max(lane - 1, 0));
+    if (lane < 2 || lane >= 30 || pos >= GH + g.nx) continue;
+    R res[NV];
 #pragma unroll
-  for (int v = 0; v < NV; v++) res[v] = dtt * (F[v] - Fm[v]);
-  res[4] += ((R)1.0 - c0.qt) * (res[1] * c0.q[1] + res[2] * c0.q[2] + res[3] * c0.q[3]);
-  {
-    R dn = (res[1] * c0.q[5] + res[2] * c0.q[6] + res[3] * c0.q[7]) / smax(tiny100<R>(), c0.bsqr);
-    R b0 = -c0.BC2 * (res[1] - dn * c0.q[5]);
-    R b1 = -c0.BC2 * (res[2] - dn * c0.q[6]);
-    R b2 = -c0.BC2 * (res[3] - dn * c0.q[7]);
-    R b3 = b0 * c0.q[1] + b1 * c0.q[2] + b2 * c0.q[3];
-    res[1] += b0; res[2] += b1; res[3] += b2; res[4] += b3;
+    for (int v = 0; v < NV; v++) res[v] = dtt * (F[v] - Fm[v]);
+    res[4] += ((R)1.0 - c0.qt) * (res[1] * c0.q[1] + res[2] * c0.q[2] + res[3] * c0.q[3]);
+    {
+      R dn = (res[1] * c0.q[5] + res[2] * c0.q[6] + res[3] * c0.q[7]) / smax(tiny100<R>(), c0.bsqr);
+      R b0 = -c0.BC2 * (res[1] - dn * c0.q[5]);
+      R b1 = -c0.BC2 * (res[2] - dn * c0.q[6]);
+      R b2 = -c0.BC2 * (res[3] - dn * c0.q[7]);
+      R b3 = b0 * c0.q[1] + b1 * c0.q[2] + b2 * c0.q[3];
+      res[1] += b0; res[2] += b1; res[3] += b2; res[4] += b3;
+    }
+    {
+      R qres = (R)0.5 * (qr + qm) * c0.qt;
+      res[4] += dtt * qres;
+    }
+    const long long id = base + pos;
+    R u[NV];
+#pragma unroll
+    for (int v = 0; v < NV; v++) u[v] = Uin[(long long)v * g.N + id] + res[v];
+    u[0] = smax(kk_.rho_min, u[0]);
+    u[4] = smax(u[4], kk_.eps_min * u[0] + (R)0.5 * (u[1] * u[1] + u[2] * u[2] + u[3] * u[3]) / u[0]);
+#pragma unroll
+    for (int v = 0; v < NV; v++) Uout[(long long)v * g.N + id] = u[v];
   }
-  {
-    R qres = (R)0.5 * (qr + qm) * c0.qt;
-    res[4] += dtt * qres;
-  }
-  const long long id = base + pos;
-  R u[NV];
-#pragma unroll
-  for (int v = 0; v < NV; v++) u[v] = Uin[(long long)v * g.N + id] + res[v];
-  u[0] = smax((R)c.rho_min, u[0]);
-  u[4] = smax(u[4], (R)c.eps_min * u[0] + (R)0.5 * (u[1] * u[1] + u[2] * u[2] + u[3] * u[3]) / u[0]);
-#pragma unroll
-  for (int v = 0; v < NV; v++) Uout[(long long)v * g.N + id] = u[v];
 }
 
 // ---------------------------------------------------------- small kernels
@@ -827,6 +835,7 @@ __global__ void k_init_pass(Consts c, const R* __restrict__ U, R* __restrict__ P
   R cm_loc = 0, sv = 0, sc = 0, se = 0;
   unsigned long long nv = 0, ne = 0;
   const R inv_va2max = (R)dyn->inv_va2max;
+  const R vlim95 = (R)(dyn->v_lim * 0.95), elim95 = (R)(dyn->e_lim * 0.95);
   for (long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x; id < g.N; id += (long long)gridDim.x * blockDim.x) {
     R d = U[id];
     R v1, v2, v3, ei;
@@ -842,8 +851,8 @@ __global__ void k_init_pass(Consts c, const R* __restrict__ U, R* __restrict__ P
       sv = d_fmax(sv, vabs);
       sc = d_fmax(sc, cs);
       se = d_fmax(se, ee);
-      if ((double)vabs >= dyn->v_lim * 0.95) nv++;
-      if ((double)ee >= dyn->e_lim * 0.95) ne++;
+      if (vabs >= vlim95) nv++;
+      if (ee >= elim95) ne++;
     }
   }
   R m = warp_max_nonnan(cm_loc);
@@ -870,6 +879,7 @@ __global__ void k_adjust_stats(Consts c, const R* __restrict__ U, const R* __res
   const long long n = (long long)g.nx * g.ny * g.nz;
   R sv = 0, sc = 0, se = 0;
   unsigned long long nv = 0, ne = 0;
+  const R vlim95 = (R)(dyn->v_lim * 0.95), elim95 = (R)(dyn->e_lim * 0.95);
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
     const int i = GH + (int)(t % g.nx), j = GH + (int)((t / g.nx) % g.ny), k = GH + (int)(t / ((long long)g.nx * g.ny));
     const long long id = cidx(g, i, j, k);
@@ -879,8 +889,8 @@ __global__ void k_adjust_stats(Consts c, const R* __restrict__ U, const R* __res
     sv = d_fmax(sv, vabs);
     sc = d_fmax(sc, (R)(5 / 3.) * P[id] / d);
     se = d_fmax(se, ee);
-    if ((double)vabs >= dyn->v_lim * 0.95) nv++;
-    if ((double)ee >= dyn->e_lim * 0.95) ne++;
+    if (vabs >= vlim95) nv++;
+    if (ee >= elim95) ne++;
   }
   R a1 = warp_max_nonnan(sv), a2 = warp_max_nonnan(sc), a3 = warp_max_nonnan(se);
   for (int o = 16; o > 0; o >>= 1) {
@@ -944,7 +954,7 @@ __global__ void k_source_integrate(Consts c, R* __restrict__ U, const R* __restr
     for (int v = 0; v < NV; v++) { r[v] = Res[(long long)v * g.N + id]; u[v] = U[(long long)v * g.N + id]; }
     R dn = invRdt * u[4];
     R efaci = dn / d_fmax(dn, (R)0.0);
-    dn = (R)c.gx * u[0] - (R)0.0;
+    dn = kc<R>(c).gx * u[0] - (R)0.0;
     R edmp = dn * u[1];
     r[1] += dn;
     r[4] += edmp + (R)0.0 * efaci;

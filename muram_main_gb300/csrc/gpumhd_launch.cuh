@@ -109,7 +109,8 @@ void Launch<R>::tvd(const Consts& c, int dir, int mode, int only_two_half, const
   if (dir == 0 && mode == 0) {
     // contiguous pencils: one cell per lane, 28 updates per warp
     const long long warps = (long long)g.sy * g.sz * ((g.nx + 27) / 28);
-    const long long nb = (warps * 32 + block - 1) / block;
+    long long nb = (warps * 32 + block - 1) / block;
+    if (nb > 152LL * 16) nb = 152LL * 16;   // grid-stride: a few waves of resident blocks
     k_tvd_sweep_xlanes<R><<<(unsigned)nb, block, 0, s>>>(c, Uin, Pst, Uout, dyn, only_two_half);
     return;
   }
