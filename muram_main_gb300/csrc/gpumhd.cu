@@ -236,6 +236,9 @@ static void adjust_limits(gpumhd_ctx* ctx, const double st[5]) {
 }
 
 static int push_dyn(gpumhd_ctx* ctx) {
+  const Consts& c = ctx->c;
+  derive_one<float>(ctx->hdyn, c.dx, c.idx, c.rt_cfl, c.tchk_vmax, c.tchk_eps_max, ctx->hdyn.rf);
+  derive_one<double>(ctx->hdyn, c.dx, c.idx, c.rt_cfl, c.tchk_vmax, c.tchk_eps_max, ctx->hdyn.rd);
   CK(cudaMemcpyAsync(ctx->dyn, &ctx->hdyn, sizeof(Dyn), cudaMemcpyHostToDevice, ctx->stream));
   return GPUMHD_OK;
 }

@@ -82,6 +82,16 @@ template <class R> __device__ __forceinline__ const KC<R>& kc(const Consts& c);
 template <> __device__ __forceinline__ const KC<float>& kc<float>(const Consts& c) { return c.kf; }
 template <> __device__ __forceinline__ const KC<double>& kc<double>(const Consts& c) { return c.kd; }
 
+// Per-step scalars in a kernel's type, derived from the double values once
+// per step (host for the per-routine calls, k_step_begin on the device).
+template <class R>
+struct DynR {
+  R dt_tvd, cmax_t[3], fac0[3];      // TVDlimit: dt, 0.975*dx/dt, 0.5/dx (src/tvdlimit_SR.C:230, 455-457)
+  R inv_va2max, vsqr_diff;
+  R vmax, emax, vlim95, elim95;      // Tcheck limits, Adjust_Valf_Max thresholds
+  R wdt[5], invRdt;                  // dt/(5-stage), rt_cfl/dt (src/Add_Sources_Integrate_SR.C:44, 85)
+};
+
 // Values that change during a run; live in device memory.
 struct Dyn {
   double dt, cfl, time;
@@ -94,9 +104,34 @@ struct Dyn {
   unsigned long long stat_max_bits[3];
   unsigned long long stat_cnt[2];
   double dt_mhd;
+  DynR<float> rf;
+  DynR<double> rd;
 };
 
+template <class R> __device__ __forceinline__ const DynR<R>& dynr(const Dyn* d);
+template <> __device__ __forceinline__ const DynR<float>& dynr<float>(const Dyn* d) { return d->rf; }
+template <> __device__ __forceinline__ const DynR<double>& dynr<double>(const Dyn* d) { return d->rd; }
+
 enum { ERR_BAD_DT_RAD = 1, ERR_BAD_DT_MHD = 2, ERR_CFL = 3 };
+
+template <class R>
+__host__ __device__ inline void derive_one(const Dyn& d, const double dx[3], const double idx[3], double rt_cfl,
+                                           double tchk_vmax, double tchk_eps_max, DynR<R>& r) {
+  r.dt_tvd = (R)d.dt_tvd;
+  for (int q = 0; q < 3; q++) {
+    r.cmax_t[q] = (R)(0.975 * dx[q] / d.dt_tvd);
+    r.fac0[q] = (R)(0.5 * idx[q]);
+  }
+  r.inv_va2max = (R)d.inv_va2max;
+  r.vsqr_diff = (R)d.vsqr_diff;
+  r.vmax = (R)(d.v_lim > 0.0 ? d.v_lim : tchk_vmax);
+  r.emax = (R)(d.e_lim > 0.0 ? d.e_lim : tchk_eps_max);
+  r.vlim95 = (R)(d.v_lim * 0.95);
+  r.elim95 = (R)(d.e_lim * 0.95);
+  r.wdt[0] = (R)0;
+  for (int st = 1; st <= 4; st++) r.wdt[st] = (R)(d.dt / (double)(4 + 1 - st));
+  r.invRdt = (R)(rt_cfl / d.dt);
+}
 
 // ---------------------------------------------------------------- helpers
 // std::max / std::min semantics: the first argument wins ties and NaNs.

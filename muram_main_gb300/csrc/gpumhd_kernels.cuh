@@ -267,14 +267,14 @@ __global__ void __launch_bounds__(TX* TY) k_stage(Consts c, const R* __restrict_
   const int i = x0 + tx, j = y0 + ty;
   const bool active = (i < GH + g.nx) && (j < GH + g.ny);
   const KC<R>& kk_ = kc<R>(c);
-  const R inv_va2max = (R)dyn->inv_va2max;
+  const DynR<R>& dr = dynr<R>(dyn);
+  const R inv_va2max = dr.inv_va2max;
   const R w1x = kk_.w1[0], w2x = kk_.w2[0], w1y = kk_.w1[1], w2y = kk_.w2[1], w1z = kk_.w1[2], w2z = kk_.w2[2];
-  // per-step scalars, converted once (src/Add_Sources_Integrate_SR.C:44, 84-85)
-  const double dtd = RESID ? 1.0 : dyn->dt;
-  const R wdt = (R)(dtd / (double)(4 + 1 - stage));
-  const R invRdt = (R)(c.rt_cfl / dtd);
-  const R vmax = (R)(dyn->v_lim > 0.0 ? dyn->v_lim : c.tchk_vmax);
-  const R emax = (R)(dyn->e_lim > 0.0 ? dyn->e_lim : c.tchk_eps_max);
+  // per-step scalars (src/Add_Sources_Integrate_SR.C:44, 84-85)
+  const R wdt = dr.wdt[(stage >= 1 && stage <= 4) ? stage : 0];
+  const R invRdt = dr.invRdt;
+  const R vmax = dr.vmax;
+  const R emax = dr.emax;
   R prim[NF];
   R fl[NF];
   prim[NPRIM] = (R)0;
@@ -599,17 +599,17 @@ __global__ void __launch_bounds__(128) k_tvd_sweep(Consts c, const R* __restrict
   const int sz = ta.n1 + 2 * GH;
   const int p0 = GH + ch * ta.td;
   const int p1 = min(p0 + ta.td, GH + ta.n1);
-  const double dt_tvd = dyn->dt_tvd;
-  const R dtt = (R)dt_tvd;
-  const R cmax_t = (R)(0.975 * c.dx[DIR] / dt_tvd);
-  const R fac0 = (R)(0.5 * c.idx[DIR]);
-  const R inv_va2max = (R)dyn->inv_va2max;
-  const R vsqr_diff = (R)dyn->vsqr_diff;
+  const DynR<R>& dr = dynr<R>(dyn);
+  const R dtt = dr.dt_tvd;
+  const R cmax_t = dr.cmax_t[DIR];
+  const R fac0 = dr.fac0[DIR];
+  const R inv_va2max = dr.inv_va2max;
+  const R vsqr_diff = dr.vsqr_diff;
   const bool hyper = (DIR == 0) && kc<R>(c).has_vhyp;
   const KC<R>& kk_ = kc<R>(c);
-  const R vmax = (R)(dyn->v_lim > 0.0 ? dyn->v_lim : c.tchk_vmax);
-  const R emax = (R)(dyn->e_lim > 0.0 ? dyn->e_lim : c.tchk_eps_max);
-  const R vlim95 = (R)(dyn->v_lim * 0.95), elim95 = (R)(dyn->e_lim * 0.95);
+  const R vmax = dr.vmax;
+  const R emax = dr.emax;
+  const R vlim95 = dr.vlim95, elim95 = dr.elim95;
   const int istart = 1 + (c.g.periodic_x ? 0 : GH);
   // final pass: TCheck, full ghost images, next step's pressure and statistics;
   // half_images: after the first of two half passes only the periodic exchange
@@ -745,12 +745,12 @@ __global__ void __launch_bounds__(128) k_tvd_sweep_xlanes(Consts c, const R* __r
   const int nseg = (g.nx + OUT - 1) / OUT;
   const long long total = (long long)g.sy * g.sz * nseg;
   const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
-  const double dt_tvd = dyn->dt_tvd;
-  const R dtt = (R)dt_tvd;
-  const R cmax_t = (R)(0.975 * c.dx[0] / dt_tvd);
-  const R fac0 = (R)(0.5 * c.idx[0]);
-  const R inv_va2max = (R)dyn->inv_va2max;
-  const R vsqr_diff = (R)dyn->vsqr_diff;
+  const DynR<R>& dr = dynr<R>(dyn);
+  const R dtt = dr.dt_tvd;
+  const R cmax_t = dr.cmax_t[0];
+  const R fac0 = dr.fac0[0];
+  const R inv_va2max = dr.inv_va2max;
+  const R vsqr_diff = dr.vsqr_diff;
   const bool hyper = kc<R>(c).has_vhyp;
   const KC<R>& kk_ = kc<R>(c);
   const int istart = 1 + (g.periodic_x ? 0 : GH);
@@ -834,8 +834,8 @@ __global__ void k_init_pass(Consts c, const R* __restrict__ U, R* __restrict__ P
   const Geom& g = c.g;
   R cm_loc = 0, sv = 0, sc = 0, se = 0;
   unsigned long long nv = 0, ne = 0;
-  const R inv_va2max = (R)dyn->inv_va2max;
-  const R vlim95 = (R)(dyn->v_lim * 0.95), elim95 = (R)(dyn->e_lim * 0.95);
+  const R inv_va2max = dynr<R>(dyn).inv_va2max;
+  const R vlim95 = dynr<R>(dyn).vlim95, elim95 = dynr<R>(dyn).elim95;
   for (long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x; id < g.N; id += (long long)gridDim.x * blockDim.x) {
     R d = U[id];
     R v1, v2, v3, ei;
@@ -879,7 +879,7 @@ __global__ void k_adjust_stats(Consts c, const R* __restrict__ U, const R* __res
   const long long n = (long long)g.nx * g.ny * g.nz;
   R sv = 0, sc = 0, se = 0;
   unsigned long long nv = 0, ne = 0;
-  const R vlim95 = (R)(dyn->v_lim * 0.95), elim95 = (R)(dyn->e_lim * 0.95);
+  const R vlim95 = dynr<R>(dyn).vlim95, elim95 = dynr<R>(dyn).elim95;
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
     const int i = GH + (int)(t % g.nx), j = GH + (int)((t / g.nx) % g.ny), k = GH + (int)(t / ((long long)g.nx * g.ny));
     const long long id = cidx(g, i, j, k);
@@ -912,7 +912,7 @@ template <class R>
 __global__ void k_cmax_faces(Consts c, const R* __restrict__ U, const R* __restrict__ P, Dyn* __restrict__ dyn) {
   const Geom& g = c.g;
   const long long nfx = 2LL * GH * g.ny * g.nz, nfy = 2LL * GH * g.nx * g.nz, nfz = 2LL * GH * g.nx * g.ny;
-  const R inv_va2max = (R)dyn->inv_va2max;
+  const R inv_va2max = dynr<R>(dyn).inv_va2max;
   R cm = 0;
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < nfx + nfy + nfz; t += (long long)gridDim.x * blockDim.x) {
     int i, j, k;
@@ -940,12 +940,12 @@ __global__ void k_source_integrate(Consts c, R* __restrict__ U, const R* __restr
                                    const Dyn* __restrict__ dyn, int stage) {
   const Geom& g = c.g;
   const long long n = (long long)g.nx * g.ny * g.nz;
-  const double dtd = dyn->dt;
-  const R wdt = (R)(dtd / (double)(4 + 1 - stage));
-  const R invRdt = (R)(c.rt_cfl / dtd);
-  const R inv_va2max = (R)dyn->inv_va2max;
-  const R vmax = (R)(dyn->v_lim > 0.0 ? dyn->v_lim : c.tchk_vmax);
-  const R emax = (R)(dyn->e_lim > 0.0 ? dyn->e_lim : c.tchk_eps_max);
+  const DynR<R>& dr = dynr<R>(dyn);
+  const R wdt = dr.wdt[stage];
+  const R invRdt = dr.invRdt;
+  const R inv_va2max = dr.inv_va2max;
+  const R vmax = dr.vmax;
+  const R emax = dr.emax;
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
     const int i = GH + (int)(t % g.nx), j = GH + (int)((t / g.nx) % g.ny), k = GH + (int)(t / ((long long)g.nx * g.ny));
     const long long id = cidx(g, i, j, k);
@@ -998,8 +998,8 @@ template <class R>
 __global__ void k_tcheck(Consts c, R* __restrict__ U, const Dyn* __restrict__ dyn) {
   const Geom& g = c.g;
   const long long n = (long long)g.nx * g.ny * g.nz;
-  const R vmax = (R)(dyn->v_lim > 0.0 ? dyn->v_lim : c.tchk_vmax);
-  const R emax = (R)(dyn->e_lim > 0.0 ? dyn->e_lim : c.tchk_eps_max);
+  const R vmax = dynr<R>(dyn).vmax;
+  const R emax = dynr<R>(dyn).emax;
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
     const int i = GH + (int)(t % g.nx), j = GH + (int)((t / g.nx) % g.ny), k = GH + (int)(t / ((long long)g.nx * g.ny));
     const long long id = cidx(g, i, j, k);

@@ -12,6 +12,7 @@ __global__ void k_step_begin(Consts c, Dyn* dyn, double* dt_hist, int dt_hist_ca
 
 template <class R>
 struct Launch {
+  static int resident_stage_blocks;   // stage blocks resident on the whole GPU at once
   static int stage_smem_bytes();
   static cudaError_t setup();
   static void stage(const Consts& c, const R* Uin, const R* Pin, const R* U0, R* Uout, R* Pout, R* Res, Dyn* dyn,
@@ -33,7 +34,7 @@ struct Launch {
 // Tile shapes of the stage kernel per state type.
 template <class R> struct StageTile;
 template <> struct StageTile<double> { static constexpr int TX = 16, TY = 8; };
-template <> struct StageTile<float> { static constexpr int TX = 32, TY = 8; };
+template <> struct StageTile<float> { static constexpr int TX = 16, TY = 16; };
 
 inline int grid_for(long long n, int block) {
   long long b = (n + block - 1) / block;
@@ -49,12 +50,23 @@ int Launch<R>::stage_smem_bytes() {
 }
 
 template <class R>
+int Launch<R>::resident_stage_blocks = 0;
+
+template <class R>
 cudaError_t Launch<R>::setup() {
   constexpr int TX = StageTile<R>::TX, TY = StageTile<R>::TY;
   const int bytes = stage_smem_bytes();
   cudaError_t e = cudaFuncSetAttribute(k_stage<R, TX, TY, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
   if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(k_stage<R, TX, TY, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  e = cudaFuncSetAttribute(k_stage<R, TX, TY, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e != cudaSuccess) return e;
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_stage<R, TX, TY, false>, TX * TY, bytes);
+  if (e != cudaSuccess) return e;
+  resident_stage_blocks = (per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
+  return cudaSuccess;
 }
 
 template <class R>
@@ -63,12 +75,21 @@ void Launch<R>::stage(const Consts& c, const R* Uin, const R* Pin, const R* U0, 
   constexpr int TX = StageTile<R>::TX, TY = StageTile<R>::TY;
   const Geom& g = c.g;
   const int bx = (g.nx + TX - 1) / TX, by = (g.ny + TY - 1) / TY;
-  // z chunk: enough blocks for several waves, at least 8 planes per block
-  const long long want = 152LL * 8;
-  int nzc = (int)((want + (long long)bx * by - 1) / ((long long)bx * by));
-  int zc = (g.nz + nzc - 1) / nzc;
-  if (zc < 8) zc = 8;
-  if (zc > g.nz) zc = g.nz;
+  // z chunk length: each block computes 4 extra z-flux planes before its
+  // first output plane, and a partly filled last wave idles the GPU; pick the
+  // chunk count that maximises (useful share of the waves) / (1 + 4/zc).
+  const long long bxy = (long long)bx * by;
+  const int res = resident_stage_blocks > 0 ? resident_stage_blocks : 304;
+  int zc = g.nz;
+  double best = -1.0;
+  for (int nzc = 1; nzc <= 64 && nzc <= g.nz; nzc++) {
+    const int zcc = (g.nz + nzc - 1) / nzc;
+    if (zcc < 4 && nzc > 1) break;
+    const long long blocks = bxy * ((g.nz + zcc - 1) / zcc);
+    const long long waves = (blocks + res - 1) / res;
+    const double eff = ((double)blocks / (double)(waves * res)) / (1.0 + 4.0 / zcc);
+    if (eff > best + 1e-9) { best = eff; zc = zcc; }
+  }
   const int bz = (g.nz + zc - 1) / zc;
   dim3 grid(bx, by, bz);
   const int bytes = stage_smem_bytes();

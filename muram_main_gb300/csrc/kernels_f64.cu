@@ -41,6 +41,8 @@ __global__ void k_step_begin(Consts c, Dyn* dyn, double* dt_hist, int dt_hist_ca
   if (dt_hist && dyn->steps_done >= 0 && dyn->steps_done < dt_hist_cap) dt_hist[dyn->steps_done] = dyn->dt;
   dyn->steps_done += 1;
   dyn->time += dyn->dt;
+  derive_one<float>(*dyn, c.dx, c.idx, c.rt_cfl, c.tchk_vmax, c.tchk_eps_max, dyn->rf);
+  derive_one<double>(*dyn, c.dx, c.idx, c.rt_cfl, c.tchk_vmax, c.tchk_eps_max, dyn->rd);
   // the last TVD pass of this step accumulates the next step's values
   dyn->cmax_bits = 0ULL;
   dyn->stat_max_bits[0] = dyn->stat_max_bits[1] = dyn->stat_max_bits[2] = 0ULL;
