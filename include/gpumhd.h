@@ -125,6 +125,22 @@ int gpumhd_step_info(gpumhd_ctx* ctx, double* dt, double* cfl, double* time, int
  * events on the context's stream; ms_phase[11] receives the mean duration of:
  * step control, RK stages 1-4, TVD x/y/z sweeps, second-half TVD x/y/z sweeps. */
 int gpumhd_profile_steps(gpumhd_ctx* ctx, int nsteps, double* ms_phase);
+/* MHD_Residual's CFL time step, dt_mhd = dxmin / cmax, computed with no device
+ * allocation at all.  No counterpart in the reference: it exists for callers
+ * that own their device arrays and must not allocate -- e.g. a MURaM build
+ * whose fields belong to the OpenACC runtime, or a time-step loop that cannot
+ * afford cudaMalloc's device-wide synchronisation.  Inputs are the caller's
+ * device arrays in this library's FP64 layout: U_prim holds primitives as
+ * ConsToPrim leaves them (8 fields of (nx+4)(ny+4)(nz+4) doubles, x fastest),
+ * pres the pressure; dx[3] and inv_va2max are host values; dt_out is a device
+ * double the result is written to, in stream order on `stream` (a
+ * cudaStream_t, NULL for the default stream).  Scratch: a fixed 32 KiB
+ * __device__ array, one partial per z plane, so nz + 4 must not exceed 4096
+ * (GPUMHD_E_INVALID otherwise).  The first call on each device looks up that
+ * array's device address; make it before any stream capture.  All calls share
+ * the array: calls that overlap on the GPU race. */
+int gpumhd_cfl_dt_noalloc(const double* U_prim, const double* pres, int nx, int ny, int nz, const double dx[3],
+                          double inv_va2max, void* stream, double* dt_out);
 /* The CUDA stream the context enqueues on (a cudaStream_t). */
 void* gpumhd_stream(gpumhd_ctx* ctx);
 /* Number of kernel launches the context has enqueued so far. */

@@ -54,7 +54,8 @@ def build(force=False, verbose=False):
     # FP32 mode's error budget); FP64: every operation IEEE-rounded.
     units = [("kernels_f64.cu", ["--fmad=false"]),
              ("kernels_f32.cu", ["--fmad=true", "-prec-div=false", "-prec-sqrt=false"]),
-             ("gpumhd.cu", ["--fmad=false"])]
+             ("gpumhd.cu", ["--fmad=false"]),
+             ("noalloc.cu", ["--fmad=false"])]
     procs = []
     objs = []
     for src, extra in units:

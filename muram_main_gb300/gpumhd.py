@@ -60,7 +60,7 @@ EXPORTS = [
     "gpumhd_cons_to_prim", "gpumhd_adjust_valf_max", "gpumhd_get_limits", "gpumhd_mhd_residual",
     "gpumhd_sync_timestep", "gpumhd_source_integrate_tcheck", "gpumhd_tvdlimit", "gpumhd_tcheck",
     "gpumhd_exchange", "gpumhd_run_steps", "gpumhd_enqueue_steps", "gpumhd_synchronize", "gpumhd_step_info",
-    "gpumhd_stream", "gpumhd_launch_count", "gpumhd_profile_steps",
+    "gpumhd_stream", "gpumhd_launch_count", "gpumhd_profile_steps", "gpumhd_cfl_dt_noalloc",
 ]
 
 _lib = None
@@ -108,6 +108,7 @@ def load(build_if_missing=True):
         "gpumhd_synchronize": (C.c_int, [vp]),
         "gpumhd_step_info": (C.c_int, [vp, dp, dp, dp, C.POINTER(C.c_int)]),
         "gpumhd_profile_steps": (C.c_int, [vp, C.c_int, dp]),
+        "gpumhd_cfl_dt_noalloc": (C.c_int, [vp, vp, C.c_int, C.c_int, C.c_int, dp, C.c_double, vp, vp]),
         "gpumhd_stream": (vp, [vp]),
         "gpumhd_launch_count": (C.c_longlong, [vp]),
     }
