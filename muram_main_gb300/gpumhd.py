@@ -264,6 +264,35 @@ class MuramGPU:
         self.exchange_grid(True)
         return dt, cfl
 
+    # -- result / restart files (src/io_xysl.C OutputSolution, RestoreSolution)
+    def OutputSolution(self, path, it, resfile="result", backup=True):
+        """Download U and write result_prim_0..7, Header and backup.dat."""
+        from . import muram_io
+        dt, _, t, _ = self.step_info()
+        inv_va2max = self.limits()[0]
+        p = self.params
+        muram_io.write_result(self.download_state(), path, it, tuple(p.dx), time=t, dt=dt,
+                              inv_va2max=inv_va2max, resfile=resfile, backup=backup)
+
+    def RestoreSolution(self, path, it, resfile="result"):
+        """Read one output, convert it to conserved variables, upload it as U
+        and U0, fill the ghosts and set the run time (backup.dat's when the
+        directory has one, as RestoreSolution reads it, else the Header's);
+        returns that time."""
+        from . import muram_io
+        p = self.params
+        U = muram_io.read_result(path, it, resfile, shape_xyz=(p.nx, p.ny, p.nz))
+        if os.path.exists(os.path.join(path, "backup.dat")):
+            t = muram_io.read_backup(path)["time"]
+        else:
+            t = muram_io.read_header(path, it)["time"]
+        p.time = t
+        self._chk(self._L.gpumhd_set_params(self._h, C.byref(p)))
+        self.upload_state(U)
+        self.upload_state(U, FIELD_U0)
+        self.exchange_grid(True)
+        return t
+
     # -- fused path
     def run_steps(self, nsteps, capture=True):
         dts = np.zeros(max(nsteps, 1))
