@@ -34,6 +34,11 @@ extern "C" {
 #define GPUMHD_E_ORDER (-6)     /* call made before the state it needs exists */
 #define GPUMHD_E_NOMEM (-7)     /* device allocation failed */
 
+/* Largest box, ghosts included ((nx+4)(ny+4)(nz+4)), that a context accepts:
+ * the kernels address the 8 state arrays with 32-bit offsets (8*N < 2^32).
+ * 1024 x 1024 x 256 interior cells is 2.75e8. */
+#define GPUMHD_MAX_CELLS 536870911LL
+
 /* Plain-data mirror of the RunData / PhysicsData / GridData fields the path
  * reads (include/run.H:6-80, include/physics.H:80-206, include/grid.H:8-125). */
 typedef struct gpumhd_params {

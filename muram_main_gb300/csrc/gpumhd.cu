@@ -136,6 +136,7 @@ static int fill_consts(gpumhd_ctx* ctx) {
   g.nx = p.nx; g.ny = p.ny; g.nz = p.nz;
   g.sx = p.nx + 2 * GH; g.sy = p.ny + 2 * GH; g.sz = p.nz + 2 * GH;
   g.N = (long long)g.sx * g.sy * g.sz;
+  g.N32 = (unsigned)g.N;
   g.periodic_x = p.periodic_x ? 1 : 0;
   for (int d = 0; d < 3; d++) {
     c.dx[d] = p.dx[d];
@@ -254,6 +255,9 @@ extern "C" int gpumhd_create(const gpumhd_params* p, int device, gpumhd_ctx** ou
   *out = nullptr;
   if (p->nx < 4 || p->ny < 4 || p->nz < 4) return fail(nullptr, GPUMHD_E_INVALID, "grid must have >= 4 interior cells per dimension");
   if (p->precision != 64 && p->precision != 32) return fail(nullptr, GPUMHD_E_INVALID, "precision must be 32 or 64");
+  if ((long long)(p->nx + 4) * (p->ny + 4) * (p->nz + 4) > GPUMHD_MAX_CELLS)
+    return fail(nullptr, GPUMHD_E_INVALID, "grid too large: (nx+4)(ny+4)(nz+4) must not exceed %lld cells",
+                (long long)GPUMHD_MAX_CELLS);
   if (!(p->dx[0] > 0 && p->dx[1] > 0 && p->dx[2] > 0)) return fail(nullptr, GPUMHD_E_INVALID, "dx must be positive");
   ctx = new gpumhd_ctx();
   ctx->p = *p;

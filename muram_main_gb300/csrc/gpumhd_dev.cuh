@@ -19,7 +19,7 @@ struct Geom {
   int sx, sy, sz;       // with ghosts
   long long N;          // sx*sy*sz
   int periodic_x;
-  int pad;
+  unsigned N32;         // N as 32-bit: every offset q*N + cell of the 8 state arrays is below 2^32
 };
 
 // Run constants in the kernel's own type, converted once on the host: the
@@ -166,6 +166,11 @@ __device__ __forceinline__ bool bad_pos(double a) { return (a != a) || (a <= 0.)
 
 __device__ __forceinline__ long long cidx(const Geom& g, int i, int j, int k) {
   return (long long)i + (long long)g.sx * ((long long)j + (long long)g.sy * (long long)k);
+}
+
+// 32-bit cell offset for the hot kernels (8*N < 2^32 is enforced at context creation).
+__device__ __forceinline__ unsigned cidx32(const Geom& g, int i, int j, int k) {
+  return (unsigned)i + (unsigned)g.sx * ((unsigned)j + (unsigned)g.sy * (unsigned)k);
 }
 
 // Order-preserving bits for non-negative doubles (cmax, maxima); NaN never stored.

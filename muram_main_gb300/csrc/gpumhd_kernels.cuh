@@ -43,7 +43,9 @@ __device__ __forceinline__ Images images_of(const Geom& g, int i, int j, int k, 
 }
 
 // Calls f(index, mirrored) for the cell itself and each of its ghost images.
-template <class F>
+// IDX32: 32-bit offsets (the stage kernel) or 64-bit (the TVD sweeps, where
+// the 64-bit form compiles to fewer registers).
+template <bool IDX32, class F>
 __device__ __forceinline__ void for_images(const Geom& g, int i, int j, int k, const Images& im, F f) {
 #pragma unroll
   for (int c = 0; c < 2; c++) {
@@ -57,29 +59,31 @@ __device__ __forceinline__ void for_images(const Geom& g, int i, int j, int k, c
       for (int a = 0; a < 2; a++) {
         const int ii = a ? im.xa : i;
         if (ii < 0) continue;
-        f(cidx(g, ii, jj, kk), a && im.xf);
+        if (IDX32) f((unsigned long long)cidx32(g, ii, jj, kk), a && im.xf);
+        else f((unsigned long long)cidx(g, ii, jj, kk), a && im.xf);
       }
     }
   }
 }
 
-template <class R>
+template <class R, bool IDX32 = false>
 __device__ __forceinline__ void store_state(const Geom& g, R* __restrict__ U, int i, int j, int k, const Images& im,
                                             const R v[NV]) {
-  for_images(g, i, j, k, im, [&](long long id, bool f) {
+  for_images<IDX32>(g, i, j, k, im, [&](unsigned long long id, bool f) {
 #pragma unroll
     for (int q = 0; q < NV; q++) {
       R x = v[q];
       if (f && (q == 1 || q == 6 || q == 7)) x = -x;
-      U[(long long)q * g.N + id] = x;
+      if (IDX32) U[(unsigned)id + (unsigned)q * g.N32] = x;
+      else U[(long long)q * g.N + (long long)id] = x;
     }
   });
 }
 
-template <class R>
+template <class R, bool IDX32 = false>
 __device__ __forceinline__ void store_scalar(const Geom& g, R* __restrict__ P, int i, int j, int k, const Images& im,
                                              R v) {
-  for_images(g, i, j, k, im, [&](long long id, bool) { P[id] = v; });
+  for_images<IDX32>(g, i, j, k, im, [&](unsigned long long id, bool) { P[id] = v; });
 }
 
 // -------------------------------------------------------------- primitives
@@ -98,28 +102,50 @@ __device__ __forceinline__ void prim_from_cons(R d, R m1, R m2, R m3, R e, R& v1
   ei = e - (R)0.5 * vv * d;
 }
 
+// The 9 stored values of a cell (state and pressure), as loaded from memory.
+template <class R>
+struct Raw9 {
+  R v[9];
+};
+
+template <class R>
+__device__ __forceinline__ void load_raw(const Geom& g, const R* __restrict__ U, const R* __restrict__ P, unsigned id,
+                                         Raw9<R>& r) {
+#pragma unroll
+  for (int q = 0; q < NV; q++) r.v[q] = U[id + (unsigned)q * g.N32];
+  r.v[8] = P[id];
+}
+
+__device__ __forceinline__ void fill_raw_one(Raw9<float>& r) {
+#pragma unroll
+  for (int q = 0; q < 9; q++) r.v[q] = 1.0f;
+}
+__device__ __forceinline__ void fill_raw_one(Raw9<double>& r) {
+#pragma unroll
+  for (int q = 0; q < 9; q++) r.v[q] = 1.0;
+}
+
 template <class R, bool PRIM_IN>
-__device__ __forceinline__ void load_prim11(const Geom& g, const R* __restrict__ U, const R* __restrict__ P,
-                                            long long id, R* out, int stride) {
-  R d = U[id];
-  R a1 = U[g.N + id], a2 = U[2 * g.N + id], a3 = U[3 * g.N + id], a4 = U[4 * g.N + id];
-  R b1 = U[5 * g.N + id], b2 = U[6 * g.N + id], b3 = U[7 * g.N + id];
+__device__ __forceinline__ void prim_of_raw(const Raw9<R>& r, R* out) {
+  R d = r.v[0];
+  R a1 = r.v[1], a2 = r.v[2], a3 = r.v[3], a4 = r.v[4];
+  R b1 = r.v[5], b2 = r.v[6], b3 = r.v[7];
   R v1, v2, v3, ei;
   if (PRIM_IN) { v1 = a1; v2 = a2; v3 = a3; ei = a4; }
   else prim_from_cons(d, a1, a2, a3, a4, v1, v2, v3, ei);
   R vv = v1 * v1 + v2 * v2 + v3 * v3;
   R bb = b1 * b1 + b2 * b2 + b3 * b3;
-  out[P_D * stride] = d;
-  out[P_V1 * stride] = v1;
-  out[P_V2 * stride] = v2;
-  out[P_V3 * stride] = v3;
-  out[P_EI * stride] = ei;
-  out[P_B1 * stride] = b1;
-  out[P_B2 * stride] = b2;
-  out[P_B3 * stride] = b3;
-  out[P_P * stride] = P[id];
-  out[P_EK * stride] = (R)0.5 * d * vv;
-  out[P_PM * stride] = (R)0.5 * bb;
+  out[P_D] = d;
+  out[P_V1] = v1;
+  out[P_V2] = v2;
+  out[P_V3] = v3;
+  out[P_EI] = ei;
+  out[P_B1] = b1;
+  out[P_B2] = b2;
+  out[P_B3] = b3;
+  out[P_P] = r.v[8];
+  out[P_EK] = (R)0.5 * d * vv;
+  out[P_PM] = (R)0.5 * bb;
 }
 
 // The 12 directional quantities whose 4th-order derivative the residual takes
@@ -158,13 +184,30 @@ __device__ __forceinline__ void flux12(const R* p, int s, R* f, int fs) {
 
 // One direction's contribution (src/mhdres_SR.C:361-412) added to R in place:
 // res = 0 - D(F); res[1..3] += Lorentz; res[4] += v . Lorentz; R += res.
-// fm2..fp2 point at the 12 quantities of cells c-2, c-1, c+1, c+2 (stride fs).
-template <class R, int D1>
-__device__ __forceinline__ void add_direction(R* Racc, const R* fm2, const R* fm1, const R* fp1, const R* fp2, int fs,
-                                              R w1, R w2, const R* cen, R lf) {
-  R Dq[NF];
+// fm2..fp2 point at the 12 consecutive quantities of cells c-2, c-1, c+1, c+2.
+__device__ __forceinline__ void deriv12(double* Dq, const double* fm2, const double* fm1, const double* fp1,
+                                        const double* fp2, double w1, double w2) {
 #pragma unroll
-  for (int q = 0; q < NF; q++) Dq[q] = w1 * (fp1[q * fs] - fm1[q * fs]) + w2 * (fp2[q * fs] - fm2[q * fs]);
+  for (int q = 0; q < NF; q++) Dq[q] = w1 * (fp1[q] - fm1[q]) + w2 * (fp2[q] - fm2[q]);
+}
+__device__ __forceinline__ void deriv12(float* Dq, const float* fm2, const float* fm1, const float* fp1,
+                                        const float* fp2, float w1, float w2) {
+  const float2 neg = make_float2(-1.0f, -1.0f), W1 = make_float2(w1, w1), W2 = make_float2(w2, w2);
+#pragma unroll
+  for (int q = 0; q < NF; q += 2) {
+    const float2 d1 = __ffma2_rn(make_float2(fm1[q], fm1[q + 1]), neg, make_float2(fp1[q], fp1[q + 1]));
+    const float2 d2 = __ffma2_rn(make_float2(fm2[q], fm2[q + 1]), neg, make_float2(fp2[q], fp2[q + 1]));
+    const float2 r = __ffma2_rn(W1, d1, __fmul2_rn(W2, d2));
+    Dq[q] = r.x;
+    Dq[q + 1] = r.y;
+  }
+}
+
+template <class R, int D1>
+__device__ __forceinline__ void add_direction(R* Racc, const R* fm2, const R* fm1, const R* fp1, const R* fp2, R w1,
+                                              R w2, const R* cen, R lf) {
+  R Dq[NF];
+  deriv12(Dq, fm2, fm1, fp1, fp2, w1, w2);
   R res[NV];
   res[0] = (R)0.0 - Dq[0];
   res[1] = (R)0.0 - Dq[1];
@@ -229,15 +272,18 @@ __device__ __forceinline__ void store_cell(double* p, const double v[12]) {
   for (int a = 0; a < 6; a++) q[a] = make_double2(v[2 * a], v[2 * a + 1]);
 }
 
+// Shared memory of one stage block: the x fluxes of (TX+4) x TY cells, the y
+// fluxes of TX x (TY+4) cells (12 quantities each) and each thread's ring of
+// five z-flux planes.
 template <int TX, int TY>
 struct StageSmem {
   static constexpr int PW = TX + 4, PH = TY + 4;
-  static constexpr int NPP = PW * PH;
-  static constexpr int FBN = (PW * TY > TX * PH) ? PW * TY : TX * PH;
+  static constexpr int FXN = PW * TY;
+  static constexpr int FYN = TX * PH;
   static constexpr int NZ = TX * TY;
   template <class R>
   static constexpr size_t bytes() {
-    return sizeof(R) * CellW<R>::W * ((size_t)NPP + (size_t)FBN + (size_t)5 * NZ);
+    return sizeof(R) * CellW<R>::W * ((size_t)FXN + (size_t)FYN + (size_t)5 * NZ);
   }
 };
 
@@ -246,17 +292,29 @@ struct StageSmem {
 //   Uout/Pout: the new state and its pressure (interior and ghost images).
 // RESID = true: MHD_Residual.  Uin holds primitives (after ConsToPrim),
 //   Res += residual over the interior, dyn->cmax_bits gets the interior CFL speed.
+//
+// A block owns a TX x TY column tile and marches along z.  Per plane, each
+// thread converts its own cell to primitives and computes that cell's x and y
+// fluxes (into shared memory) and its column's z flux two planes ahead (into
+// its private ring); the first 4*(TX+TY) threads also compute the x or y flux
+// of one cell of the tile's two-cell halo.  After one barrier every thread
+// takes the three fourth-order derivatives of its cell.  All global loads of
+// the next plane are issued before the barrier, so their latency overlaps this
+// plane's arithmetic.
 template <class R, int TX, int TY, bool RESID>
-__global__ void __launch_bounds__(TX* TY) k_stage(Consts c, const R* __restrict__ Uin, const R* __restrict__ Pin,
-                                                  const R* __restrict__ U0, R* __restrict__ Uout,
-                                                  R* __restrict__ Pout, R* __restrict__ Res, Dyn* __restrict__ dyn,
-                                                  int stage, int zc, int write_pres) {
+__global__ void __launch_bounds__(TX* TY, 2) k_stage(Consts c, const R* __restrict__ Uin, const R* __restrict__ Pin,
+                                                     const R* __restrict__ U0, R* __restrict__ Uout,
+                                                     R* __restrict__ Pout, R* __restrict__ Res, Dyn* __restrict__ dyn,
+                                                     int stage, int zc, int write_pres) {
   using S = StageSmem<TX, TY>;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int CW = CellW<R>::W;
-  R* PP = reinterpret_cast<R*>(smem_raw);
-  R* FB = PP + CW * S::NPP;
-  R* FZ = FB + CW * S::FBN;
+  constexpr int NT = TX * TY;
+  constexpr int NH = 4 * TY + 4 * TX;  // halo cells: two columns each side (x), two rows each side (y)
+  static_assert(NH <= NT, "every halo cell needs a thread");
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  R* FX = reinterpret_cast<R*>(smem_raw);   // x flux of (lx, ly) at ((ly * PW) + lx + 2) * CW
+  R* FY = FX + CW * S::FXN;                 // y flux of (lx, ly) at (((ly + 2) * TX) + lx) * CW
+  R* FZ = FY + CW * S::FYN;
   const Geom& g = c.g;
   if (!RESID && dyn->err) return;
   const int tid = threadIdx.x;
@@ -266,6 +324,24 @@ __global__ void __launch_bounds__(TX* TY) k_stage(Consts c, const R* __restrict_
   const int ze = min(zb + zc, GH + g.nz);
   const int i = x0 + tx, j = y0 + ty;
   const bool active = (i < GH + g.nx) && (j < GH + g.ny);
+  const bool own_in = (i < g.sx) && (j < g.sy);
+  // this thread's halo cell (tid < NH): x-halo cells first (4 per row), then y-halo rows
+  int hlx = 0, hly = 0;
+  const bool hx = tid < 4 * TY;
+  if (tid < NH) {
+    if (hx) {
+      const int c4 = tid & 3;
+      hlx = c4 < 2 ? c4 - 2 : TX + c4 - 2;
+      hly = tid >> 2;
+    } else {
+      const int r = tid - 4 * TY;
+      hlx = r % TX;
+      const int q = r / TX;
+      hly = q < 2 ? q - 2 : TY + q - 2;
+    }
+  }
+  const int hi = x0 + hlx, hj = y0 + hly;
+  const bool h_in = (tid < NH) && hi >= 0 && hi < g.sx && hj >= 0 && hj < g.sy;
   const KC<R>& kk_ = kc<R>(c);
   const DynR<R>& dr = dynr<R>(dyn);
   const R inv_va2max = dr.inv_va2max;
@@ -278,97 +354,113 @@ __global__ void __launch_bounds__(TX* TY) k_stage(Consts c, const R* __restrict_
   R prim[NF];
   R fl[NF];
   prim[NPRIM] = (R)0;
+  fl[NPRIM] = (R)0;
 
   // z-flux ring: slot of plane kk is (kk - zb + 2) mod 5
-  auto zslot = [&](int kk) { return ((kk - zb + 2) % 5 + 5) % 5; };
-  auto zcell = [&](int kk) { return FZ + ((size_t)zslot(kk) * S::NZ + tid) * CW; };
-  auto fill_z = [&](int kk) {
-    if (!active) return;
-    load_prim11<R, RESID>(g, Uin, Pin, cidx(g, i, j, kk), prim, 1);
-    flux12<R, 2>(prim, 1, fl, 1);
-    store_cell(zcell(kk), fl);
-  };
-  for (int kk = zb - 2; kk < zb + 2; kk++) fill_z(kk);
-
-  for (int k = zb; k < ze; k++) {
-    fill_z(k + 2);
-    // center plane primitives over the cross-shaped halo
-    const int ncross = S::PW * TY + 4 * TX;
-    for (int m = tid; m < ncross; m += TX * TY) {
-      int lx, ly;
-      if (m < S::PW * TY) { lx = m % S::PW - 2; ly = m / S::PW; }
-      else { int r = m - S::PW * TY; lx = r % TX; int q = r / TX; ly = q < 2 ? q - 2 : TY + q - 2; }
-      const int gi = x0 + lx, gj = y0 + ly;
-      R* dst = PP + ((ly + 2) * S::PW + (lx + 2)) * CW;
-      if (gi >= 0 && gi < g.sx && gj >= 0 && gj < g.sy)
-        load_prim11<R, RESID>(g, Uin, Pin, cidx(g, gi, gj, k), prim, 1);
-      else
-        for (int q = 0; q < NPRIM; q++) prim[q] = (R)1.0;
-      store_cell(dst, prim);
-    }
-    __syncthreads();
-    // x fluxes on (TX+4) x TY
-    for (int m = tid; m < S::PW * TY; m += TX * TY) {
-      const int lx = m % S::PW, ly = m / S::PW;
-      load_cell(PP + ((ly + 2) * S::PW + lx) * CW, prim);
-      flux12<R, 0>(prim, 1, fl, 1);
-      store_cell(FB + (ly * S::PW + lx) * CW, fl);
-    }
-    __syncthreads();
-    R Racc[NV];
-    R cen[NF];
-    R lf = (R)0;
-    const int pc = (ty + 2) * S::PW + (tx + 2);
+  R* const zring = FZ + (size_t)tid * CW;
+  auto zcell = [&](int sl) { return zring + sl * (S::NZ * CW); };
+  auto slot_add = [](int sl, int d) { return sl + d >= 5 ? sl + d - 5 : sl + d; };
+  // zr: the column at plane k+2; orw: the own cell at plane k; hrw: the halo
+  // cell at plane k (cells outside the array read as 1, their fluxes unused)
+  Raw9<R> zr, orw, hrw;
+  fill_raw_one(orw);
+  fill_raw_one(hrw);
+  const unsigned plane = (unsigned)g.sx * (unsigned)g.sy;
+  const unsigned own0 = cidx32(g, i, j, 0), halo0 = cidx32(g, hi, hj, 0);
+  for (int kk = zb - 2; kk < zb + 2; kk++) {
     if (active) {
-      load_cell(PP + pc * CW, cen);
-      const long long id = cidx(g, i, j, k);
+      load_raw<R>(g, Uin, Pin, own0 + (unsigned)kk * plane, zr);
+      prim_of_raw<R, RESID>(zr, prim);
+      flux12<R, 2>(prim, 1, fl, 1);
+      store_cell(zcell(kk - zb + 2), fl);
+    }
+  }
+  if (active) load_raw<R>(g, Uin, Pin, own0 + (unsigned)(zb + 2) * plane, zr);
+  if (own_in) load_raw<R>(g, Uin, Pin, own0 + (unsigned)zb * plane, orw);
+  if (h_in) load_raw<R>(g, Uin, Pin, halo0 + (unsigned)zb * plane, hrw);
+
+  int s0 = 2;  // ring slot of plane k
+  for (int k = zb; k < ze; k++, s0 = slot_add(s0, 1)) {
+    R cen[NF];
+    if (active) {
+      prim_of_raw<R, RESID>(zr, prim);
+      flux12<R, 2>(prim, 1, fl, 1);
+      store_cell(zcell(slot_add(s0, 2)), fl);
+    }
+    prim_of_raw<R, RESID>(orw, cen);
+    cen[NPRIM] = (R)0;
+    flux12<R, 0>(cen, 1, fl, 1);
+    store_cell(FX + (ty * S::PW + tx + 2) * CW, fl);
+    flux12<R, 1>(cen, 1, fl, 1);
+    store_cell(FY + ((ty + 2) * TX + tx) * CW, fl);
+    if (tid < NH) {
+      prim_of_raw<R, RESID>(hrw, prim);
+      if (hx) {
+        flux12<R, 0>(prim, 1, fl, 1);
+        store_cell(FX + (hly * S::PW + hlx + 2) * CW, fl);
+      } else {
+        flux12<R, 1>(prim, 1, fl, 1);
+        store_cell(FY + ((hly + 2) * TX + hlx) * CW, fl);
+      }
+    }
+    // next plane's loads, in flight during this plane's derivatives
+    const unsigned id = own0 + (unsigned)k * plane;
+    if (k + 1 < ze) {
+      if (active) load_raw<R>(g, Uin, Pin, id + 3 * plane, zr);
+      if (own_in) load_raw<R>(g, Uin, Pin, id + plane, orw);
+      if (h_in) load_raw<R>(g, Uin, Pin, halo0 + (unsigned)(k + 1) * plane, hrw);
+    }
+    // this cell's U0 (fused stage) or Res (residual mode), used at the end
+    R base[NV];
+    if (active) {
+      const R* src = RESID ? Res : U0;
+#pragma unroll
+      for (int q = 0; q < NV; q++) base[q] = src[id + (unsigned)q * g.N32];
+    }
+    __syncthreads();
+    if (active) {
+      R Racc[NV];
       if (RESID) {
 #pragma unroll
-        for (int q = 0; q < NV; q++) Racc[q] = Res[(long long)q * g.N + id];
+        for (int q = 0; q < NV; q++) Racc[q] = base[q];
       } else {
 #pragma unroll
         for (int q = 0; q < NV; q++) Racc[q] = (R)0.0;
       }
       // Boris factor at the cell (src/mhdres_SR.C:310-323)
-      const R dn = (R)1.0 / cen[P_D];
-      const R bb = cen[P_B1] * cen[P_B1] + cen[P_B2] * cen[P_B2] + cen[P_B3] * cen[P_B3];
-      const R va2 = bb * dn;
-      const R x2 = va2 * inv_va2max, x4 = x2 * x2, s = (R)1.0 + x2;
-      lf = s / (s + x4);
-      const R* fb = FB + (ty * S::PW + (tx + 2)) * CW;
+      R lf;
+      {
+        const R dn = (R)1.0 / cen[P_D];
+        const R bb = cen[P_B1] * cen[P_B1] + cen[P_B2] * cen[P_B2] + cen[P_B3] * cen[P_B3];
+        const R va2 = bb * dn;
+        const R x2 = va2 * inv_va2max, x4 = x2 * x2, s = (R)1.0 + x2;
+        lf = s / (s + x4);
+      }
       R n0[NF], n1[NF], n2[NF], n3[NF];
-      load_cell(fb - 2 * CW, n0);
-      load_cell(fb - CW, n1);
-      load_cell(fb + CW, n2);
-      load_cell(fb + 2 * CW, n3);
-      add_direction<R, 0>(Racc, n0, n1, n2, n3, 1, w1x, w2x, cen, lf);
-    }
-    __syncthreads();
-    // y fluxes on TX x (TY+4)
-    for (int m = tid; m < TX * S::PH; m += TX * TY) {
-      const int lx = m % TX, ly = m / TX;
-      load_cell(PP + (ly * S::PW + (lx + 2)) * CW, prim);
-      flux12<R, 1>(prim, 1, fl, 1);
-      store_cell(FB + (ly * TX + lx) * CW, fl);
-    }
-    __syncthreads();
-    if (active) {
-      const R* fb = FB + ((ty + 2) * TX + tx) * CW;
-      R n0[NF], n1[NF], n2[NF], n3[NF];
-      load_cell(fb - 2 * TX * CW, n0);
-      load_cell(fb - TX * CW, n1);
-      load_cell(fb + TX * CW, n2);
-      load_cell(fb + 2 * TX * CW, n3);
-      add_direction<R, 1>(Racc, n0, n1, n2, n3, 1, w1y, w2y, cen, lf);
-      load_cell(zcell(k - 2), n0);
-      load_cell(zcell(k - 1), n1);
-      load_cell(zcell(k + 1), n2);
-      load_cell(zcell(k + 2), n3);
-      add_direction<R, 2>(Racc, n0, n1, n2, n3, 1, w1z, w2z, cen, lf);
-      const long long id = cidx(g, i, j, k);
+      {
+        const R* fb = FX + (ty * S::PW + tx + 2) * CW;
+        load_cell(fb - 2 * CW, n0);
+        load_cell(fb - CW, n1);
+        load_cell(fb + CW, n2);
+        load_cell(fb + 2 * CW, n3);
+        add_direction<R, 0>(Racc, n0, n1, n2, n3, w1x, w2x, cen, lf);
+      }
+      {
+        const R* fb = FY + ((ty + 2) * TX + tx) * CW;
+        load_cell(fb - 2 * TX * CW, n0);
+        load_cell(fb - TX * CW, n1);
+        load_cell(fb + TX * CW, n2);
+        load_cell(fb + 2 * TX * CW, n3);
+        add_direction<R, 1>(Racc, n0, n1, n2, n3, w1y, w2y, cen, lf);
+      }
+      load_cell(zcell(slot_add(s0, 3)), n0);
+      load_cell(zcell(slot_add(s0, 4)), n1);
+      load_cell(zcell(slot_add(s0, 1)), n2);
+      load_cell(zcell(slot_add(s0, 2)), n3);
+      add_direction<R, 2>(Racc, n0, n1, n2, n3, w1z, w2z, cen, lf);
       if (RESID) {
 #pragma unroll
-        for (int q = 0; q < NV; q++) Res[(long long)q * g.N + id] = Racc[q];
+        for (int q = 0; q < NV; q++) Res[id + (unsigned)q * g.N32] = Racc[q];
         R cm = cmax_cell<R>(cen[P_D], cen[P_V1], cen[P_V2], cen[P_V3], cen[P_B1], cen[P_B2], cen[P_B3], cen[P_P],
                             inv_va2max);
         atomic_max_nonneg(&dyn->cmax_bits, (double)cm);
@@ -400,15 +492,15 @@ __global__ void __launch_bounds__(TX* TY) k_stage(Consts c, const R* __restrict_
         Racc[4] += b3;
         R un[NV];
 #pragma unroll
-        for (int v = 0; v < NV; v++) un[v] = U0[(long long)v * g.N + id] + wdt * Racc[v];
+        for (int v = 0; v < NV; v++) un[v] = base[v] + wdt * Racc[v];
         tcheck_cell<R>(c, vmax, emax, un[0], un[1], un[2], un[3], un[4]);
         const Images im = images_of(g, i, j, k, true);
-        store_state<R>(g, Uout, i, j, k, im, un);
+        store_state<R, true>(g, Uout, i, j, k, im, un);
         if (write_pres) {
           R v1, v2, v3, ei;
           prim_from_cons(un[0], un[1], un[2], un[3], un[4], v1, v2, v3, ei);
           const R pr = eos_pres(c, un[0], ei, (R)1.0 / un[0]);
-          store_scalar<R>(g, Pout, i, j, k, im, pr);
+          store_scalar<R, true>(g, Pout, i, j, k, im, pr);
         }
       }
     }

@@ -99,7 +99,7 @@ extern "C" int gpumhd_cfl_dt_noalloc(const double* U_prim, const double* pres, i
   g.sx = nx + 2 * GH; g.sy = ny + 2 * GH; g.sz = nz + 2 * GH;
   g.N = (long long)g.sx * g.sy * g.sz;
   g.periodic_x = 1;
-  g.pad = 0;
+  g.N32 = (unsigned)g.N;
   double dxmin = dx[0];
   for (int d = 1; d < 3; d++) dxmin = (dx[d] < dxmin) ? dx[d] : dxmin;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
