@@ -45,7 +45,9 @@ typedef struct gpumhd_params {
   int nx, ny, nz;        /* interior cells (GridData::lsize); each >= 4 */
   int periodic_x;        /* GridData::periods[0]; y and z are periodic */
   int precision;         /* 64: FP64 state and arithmetic; 32: FP32 state and arithmetic */
-  int pad0;
+  int stage_kernel;      /* 0: TMA / tensor-memory stage kernel where the box allows it
+                            ((nx+4)*sizeof(real) a multiple of 16 bytes), else plain loads;
+                            1: always the plain-load stage kernel (same results) */
   double dx[3];          /* GridData::dx */
   /* RunData */
   double CFL, CFL_tvd, dt, time, outcad;

@@ -1,4 +1,5 @@
 // Host side of the gpumhd C ABI (include/gpumhd.h).
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -48,6 +49,11 @@ struct gpumhd_ctx {
   bool fused_ready = false;
   cudaGraphExec_t graph = nullptr;
   long long launches = 0;
+  // TMA descriptors of the state (x, y, z, variable) and pressure (x, y, z)
+  // buffers for the TMA / tensor-memory stage kernel; tma = false: plain loads
+  bool tma = false;
+  CUtensorMap mapS[3];
+  CUtensorMap mapP[2];
   char err[1024] = {0};
 };
 
@@ -249,12 +255,69 @@ static int pull_dyn(gpumhd_ctx* ctx) {
   return GPUMHD_OK;
 }
 
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_tiled_fn() {
+  static EncodeTiledFn fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(f);
+  }
+  return fn;
+}
+
+// Tensor maps of the three state and two pressure buffers, boxes of one plane
+// tile with its halo ((TX+4) x (TY+4) x 1 [x 8 variables]).  TMA needs every
+// row stride to be a multiple of 16 bytes: (nx+4)*sizeof(real) % 16 == 0.
+template <class R>
+static bool make_tensor_maps(gpumhd_ctx* ctx) {
+  constexpr int TX = StageTile<R>::TX, TY = StageTile<R>::TY;
+  const Geom& g = ctx->c.g;
+  const cuuint64_t esz = sizeof(R);
+  if (((cuuint64_t)g.sx * esz) % 16 != 0) return false;
+  EncodeTiledFn enc = encode_tiled_fn();
+  if (!enc) return false;
+  const CUtensorMapDataType dt = sizeof(R) == 4 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT32 : CU_TENSOR_MAP_DATA_TYPE_FLOAT64;
+  const cuuint64_t dimU[4] = {(cuuint64_t)g.sx, (cuuint64_t)g.sy, (cuuint64_t)g.sz, 8};
+  const cuuint64_t strU[3] = {g.sx * esz, (cuuint64_t)g.sx * g.sy * esz, (cuuint64_t)g.N * esz};
+  const cuuint32_t boxU[4] = {TX + 4, TY + 4, 1, 8};
+  const cuuint32_t one[4] = {1, 1, 1, 1};
+  for (int b = 0; b < 3; b++)
+    if (enc(&ctx->mapS[b], dt, 4, ctx->S[b], dimU, strU, boxU, one, CU_TENSOR_MAP_INTERLEAVE_NONE,
+            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) !=
+        CUDA_SUCCESS)
+      return false;
+  for (int b = 0; b < 2; b++)
+    if (enc(&ctx->mapP[b], dt, 3, ctx->P[b], dimU, strU, boxU, one, CU_TENSOR_MAP_INTERLEAVE_NONE,
+            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) !=
+        CUDA_SUCCESS)
+      return false;
+  return true;
+}
+
+// Tensor maps for a stage launch reading state buffer b and pressure buffer pb
+// (both null: the plain-load kernel).
+static const CUtensorMap* map_u(const gpumhd_ctx* ctx, int b) {
+  return (ctx->tma && ctx->p.stage_kernel == 0) ? &ctx->mapS[b] : nullptr;
+}
+static const CUtensorMap* map_p(const gpumhd_ctx* ctx, int pb) {
+  return (ctx->tma && ctx->p.stage_kernel == 0) ? &ctx->mapP[pb] : nullptr;
+}
+
 extern "C" int gpumhd_create(const gpumhd_params* p, int device, gpumhd_ctx** out) {
   gpumhd_ctx* ctx = nullptr;
   if (!p || !out) return fail(nullptr, GPUMHD_E_INVALID, "null argument");
   *out = nullptr;
   if (p->nx < 4 || p->ny < 4 || p->nz < 4) return fail(nullptr, GPUMHD_E_INVALID, "grid must have >= 4 interior cells per dimension");
   if (p->precision != 64 && p->precision != 32) return fail(nullptr, GPUMHD_E_INVALID, "precision must be 32 or 64");
+  if (p->stage_kernel != 0 && p->stage_kernel != 1) return fail(nullptr, GPUMHD_E_INVALID, "stage_kernel must be 0 or 1");
   if ((long long)(p->nx + 4) * (p->ny + 4) * (p->nz + 4) > GPUMHD_MAX_CELLS)
     return fail(nullptr, GPUMHD_E_INVALID, "grid too large: (nx+4)(ny+4)(nz+4) must not exceed %lld cells",
                 (long long)GPUMHD_MAX_CELLS);
@@ -285,6 +348,7 @@ extern "C" int gpumhd_create(const gpumhd_params* p, int device, gpumhd_ctx** ou
       if (cudaMalloc(&ctx->P[b], N * ctx->rsz) != cudaSuccess) { rc = GPUMHD_E_NOMEM; break; }
     if (rc) break;
     if (cudaMalloc(&ctx->dyn, sizeof(Dyn)) != cudaSuccess) { rc = GPUMHD_E_NOMEM; break; }
+    ctx->tma = ctx->f32 ? make_tensor_maps<float>(ctx) : make_tensor_maps<double>(ctx);
     for (int b = 0; b < 3; b++) cudaMemsetAsync(ctx->S[b], 0, 8 * N * ctx->rsz, ctx->stream);
     for (int b = 0; b < 2; b++) cudaMemsetAsync(ctx->P[b], 0, N * ctx->rsz, ctx->stream);
     memset(&ctx->hdyn, 0, sizeof(Dyn));
@@ -602,11 +666,13 @@ extern "C" int gpumhd_mhd_residual(gpumhd_ctx* ctx, double* dt_mhd) {
   if (rc) return rc;
   if (ctx->f32) {
     Launch<float>::stage(ctx->c, (const float*)ctx->S[ctx->iU], (const float*)ctx->P[ctx->iP], nullptr, nullptr, nullptr,
-                         (float*)ctx->S[ctx->iRes], ctx->dyn, 0, true, 0, ctx->stream);
+                         (float*)ctx->S[ctx->iRes], ctx->dyn, 0, true, 0, ctx->stream, map_u(ctx, ctx->iU),
+                         map_p(ctx, ctx->iP));
     Launch<float>::cmax_faces(ctx->c, (const float*)ctx->S[ctx->iU], (const float*)ctx->P[ctx->iP], ctx->dyn, ctx->stream);
   } else {
     Launch<double>::stage(ctx->c, (const double*)ctx->S[ctx->iU], (const double*)ctx->P[ctx->iP], nullptr, nullptr,
-                          nullptr, (double*)ctx->S[ctx->iRes], ctx->dyn, 0, true, 0, ctx->stream);
+                          nullptr, (double*)ctx->S[ctx->iRes], ctx->dyn, 0, true, 0, ctx->stream,
+                          map_u(ctx, ctx->iU), map_p(ctx, ctx->iP));
     Launch<double>::cmax_faces(ctx->c, (const double*)ctx->S[ctx->iU], (const double*)ctx->P[ctx->iP], ctx->dyn, ctx->stream);
   }
   rc = check_launch(ctx, 2);
@@ -716,13 +782,13 @@ static int enqueue_one_step(gpumhd_ctx* ctx, cudaEvent_t* ev = nullptr) {
     float* const* S = (float* const*)ctx->S;
     float* const* P = (float* const*)ctx->P;
     mark();
-    L::stage(c, S[a], P[pa], S[a], S[b], P[pb], nullptr, ctx->dyn, 1, false, 1, s);
+    L::stage(c, S[a], P[pa], S[a], S[b], P[pb], nullptr, ctx->dyn, 1, false, 1, s, map_u(ctx, a), map_p(ctx, pa));
     mark();
-    L::stage(c, S[b], P[pb], S[a], S[d], P[pa], nullptr, ctx->dyn, 2, false, 1, s);
+    L::stage(c, S[b], P[pb], S[a], S[d], P[pa], nullptr, ctx->dyn, 2, false, 1, s, map_u(ctx, b), map_p(ctx, pb));
     mark();
-    L::stage(c, S[d], P[pa], S[a], S[b], P[pb], nullptr, ctx->dyn, 3, false, 1, s);
+    L::stage(c, S[d], P[pa], S[a], S[b], P[pb], nullptr, ctx->dyn, 3, false, 1, s, map_u(ctx, d), map_p(ctx, pa));
     mark();
-    L::stage(c, S[b], P[pb], S[a], S[a], nullptr, nullptr, ctx->dyn, 4, false, 0, s);
+    L::stage(c, S[b], P[pb], S[a], S[a], nullptr, nullptr, ctx->dyn, 4, false, 0, s, map_u(ctx, b), map_p(ctx, pb));
     mark();
     L::tvd(c, 0, 0, 0, S[a], P[pb], S[d], nullptr, ctx->dyn, s);
     mark();
@@ -740,13 +806,13 @@ static int enqueue_one_step(gpumhd_ctx* ctx, cudaEvent_t* ev = nullptr) {
     double* const* S = (double* const*)ctx->S;
     double* const* P = (double* const*)ctx->P;
     mark();
-    L::stage(c, S[a], P[pa], S[a], S[b], P[pb], nullptr, ctx->dyn, 1, false, 1, s);
+    L::stage(c, S[a], P[pa], S[a], S[b], P[pb], nullptr, ctx->dyn, 1, false, 1, s, map_u(ctx, a), map_p(ctx, pa));
     mark();
-    L::stage(c, S[b], P[pb], S[a], S[d], P[pa], nullptr, ctx->dyn, 2, false, 1, s);
+    L::stage(c, S[b], P[pb], S[a], S[d], P[pa], nullptr, ctx->dyn, 2, false, 1, s, map_u(ctx, b), map_p(ctx, pb));
     mark();
-    L::stage(c, S[d], P[pa], S[a], S[b], P[pb], nullptr, ctx->dyn, 3, false, 1, s);
+    L::stage(c, S[d], P[pa], S[a], S[b], P[pb], nullptr, ctx->dyn, 3, false, 1, s, map_u(ctx, d), map_p(ctx, pa));
     mark();
-    L::stage(c, S[b], P[pb], S[a], S[a], nullptr, nullptr, ctx->dyn, 4, false, 0, s);
+    L::stage(c, S[b], P[pb], S[a], S[a], nullptr, nullptr, ctx->dyn, 4, false, 0, s, map_u(ctx, b), map_p(ctx, pb));
     mark();
     L::tvd(c, 0, 0, 0, S[a], P[pb], S[d], nullptr, ctx->dyn, s);
     mark();
@@ -852,6 +918,7 @@ extern "C" int gpumhd_synchronize(gpumhd_ctx* ctx) {
     case ERR_BAD_DT_RAD: return fail(ctx, GPUMHD_E_BAD_DT, "Invalid time step: dt_rad");
     case ERR_BAD_DT_MHD: return fail(ctx, GPUMHD_E_BAD_DT, "Invalid time step: dt_mhd = %g", ctx->hdyn.dt_mhd);
     case ERR_CFL: return fail(ctx, GPUMHD_E_CFL, "Invalid time step: CFL = %g", ctx->hdyn.cfl);
+    case ERR_WAIT_TIMEOUT: return fail(ctx, GPUMHD_E_CUDA, "a device-side wait for a TMA copy timed out");
     default: return fail(ctx, GPUMHD_E_CUDA, "device error flag %d", ctx->hdyn.err);
   }
 }

@@ -1,7 +1,7 @@
 // Kernel launchers, instantiated once per state type in its own translation
 // unit (FP64 without FMA contraction, FP32 with it).
 #pragma once
-#include "gpumhd_kernels.cuh"
+#include "gpumhd_stage_tm.cuh"
 
 namespace gpumhd {
 
@@ -13,10 +13,13 @@ __global__ void k_step_begin(Consts c, Dyn* dyn, double* dt_hist, int dt_hist_ca
 template <class R>
 struct Launch {
   static int resident_stage_blocks;   // stage blocks resident on the whole GPU at once
+  static int resident_tm_blocks;      // the same for the TMA / tensor-memory stage kernel
   static int stage_smem_bytes();
   static cudaError_t setup();
+  // mu / mp: tensor maps of Uin / Pin for the TMA kernel (both null: k_stage)
   static void stage(const Consts& c, const R* Uin, const R* Pin, const R* U0, R* Uout, R* Pout, R* Res, Dyn* dyn,
-                    int stage, bool resid, int write_pres, cudaStream_t s);
+                    int stage, bool resid, int write_pres, cudaStream_t s, const CUtensorMap* mu = nullptr,
+                    const CUtensorMap* mp = nullptr);
   static void tvd(const Consts& c, int dir, int mode, int only_two_half, const R* Uin, const R* Pst, R* Uout, R* Pout,
                   Dyn* dyn, cudaStream_t s);
   static void cons_to_prim(const Consts& c, R* U, R* P, R* T, R* Ne, R* Ri, R* Am, cudaStream_t s);
@@ -51,6 +54,8 @@ int Launch<R>::stage_smem_bytes() {
 
 template <class R>
 int Launch<R>::resident_stage_blocks = 0;
+template <class R>
+int Launch<R>::resident_tm_blocks = 0;
 
 template <class R>
 cudaError_t Launch<R>::setup() {
@@ -66,20 +71,31 @@ cudaError_t Launch<R>::setup() {
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_stage<R, TX, TY, false>, TX * TY, bytes);
   if (e != cudaSuccess) return e;
   resident_stage_blocks = (per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
+  const int tb = (int)StageTm<R, TX, TY>::BYTES;
+  e = cudaFuncSetAttribute(k_stage_tm<R, TX, TY, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, tb);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(k_stage_tm<R, TX, TY, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, tb);
+  if (e != cudaSuccess) return e;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_stage_tm<R, TX, TY, false>, TX * TY, tb);
+  if (e != cudaSuccess) return e;
+  resident_tm_blocks = (per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
   return cudaSuccess;
 }
 
 template <class R>
 void Launch<R>::stage(const Consts& c, const R* Uin, const R* Pin, const R* U0, R* Uout, R* Pout, R* Res, Dyn* dyn,
-                      int stage, bool resid, int write_pres, cudaStream_t s) {
+                      int stage, bool resid, int write_pres, cudaStream_t s, const CUtensorMap* mu,
+                      const CUtensorMap* mp) {
   constexpr int TX = StageTile<R>::TX, TY = StageTile<R>::TY;
   const Geom& g = c.g;
+  const bool tma = mu && mp;
   const int bx = (g.nx + TX - 1) / TX, by = (g.ny + TY - 1) / TY;
   // z chunk length: each block computes 4 extra z-flux planes before its
   // first output plane, and a partly filled last wave idles the GPU; pick the
   // chunk count that maximises (useful share of the waves) / (1 + 4/zc).
   const long long bxy = (long long)bx * by;
-  const int res = resident_stage_blocks > 0 ? resident_stage_blocks : 304;
+  const int res0 = tma ? resident_tm_blocks : resident_stage_blocks;
+  const int res = res0 > 0 ? res0 : 304;
   int zc = g.nz;
   double best = -1.0;
   for (int nzc = 1; nzc <= 64 && nzc <= g.nz; nzc++) {
@@ -92,6 +108,16 @@ void Launch<R>::stage(const Consts& c, const R* Uin, const R* Pin, const R* U0, 
   }
   const int bz = (g.nz + zc - 1) / zc;
   dim3 grid(bx, by, bz);
+  if (tma) {
+    const int bytes = (int)StageTm<R, TX, TY>::BYTES;
+    if (resid)
+      k_stage_tm<R, TX, TY, true><<<grid, TX * TY, bytes, s>>>(*mu, *mp, c, U0, Uout, Pout, Res, dyn, stage, zc,
+                                                               write_pres);
+    else
+      k_stage_tm<R, TX, TY, false><<<grid, TX * TY, bytes, s>>>(*mu, *mp, c, U0, Uout, Pout, Res, dyn, stage, zc,
+                                                                write_pres);
+    return;
+  }
   const int bytes = stage_smem_bytes();
   if (resid)
     k_stage<R, TX, TY, true><<<grid, TX * TY, bytes, s>>>(c, Uin, Pin, U0, Uout, Pout, Res, dyn, stage, zc, write_pres);

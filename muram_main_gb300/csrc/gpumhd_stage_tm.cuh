@@ -1,0 +1,511 @@
+// RK stage kernel with TMA plane loads and a tensor-memory z-flux ring.
+//
+// Same arithmetic as k_stage (gpumhd_kernels.cuh), different data movement:
+//
+//  * the state and pressure of each z plane under the block's tile, with its
+//    two-cell halo ((TX+4) x (TY+4) cells, 9 arrays), arrive in shared memory
+//    by one cp.async.bulk.tensor per array group, issued by one thread three
+//    planes ahead and tracked by an mbarrier per slot of a four-plane ring;
+//  * each thread's five-plane ring of z fluxes (12 quantities) lives in tensor
+//    memory (tcgen05.st / tcgen05.ld, one TMEM lane per thread), which leaves
+//    shared memory to the plane tiles and the x / y flux buffers.
+//
+// Every mbarrier wait is bounded (about one second); on expiry the kernel sets
+// ERR_WAIT_TIMEOUT in the step-control block, waits (bounded) for the copies it
+// issued, releases its tensor memory and returns.
+#pragma once
+#include <cuda.h>
+
+#include "gpumhd_kernels.cuh"
+
+namespace gpumhd {
+
+enum { ERR_WAIT_TIMEOUT = 4 };
+
+namespace tm {
+
+constexpr long long WAIT_CYCLES = 2000000000LL;  // ~1 s at the GB300 SM clock
+
+__device__ __forceinline__ unsigned su32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long* b, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long* b, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(b)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* b, unsigned parity) {
+  unsigned ok;
+  asm volatile(
+      "{\n"
+      " .reg .pred p;\n"
+      " mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      " selp.u32 %0, 1, 0, p;\n"
+      "}\n"
+      : "=r"(ok)
+      : "r"(su32(b)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Wait for completion of phase `parity`; false after WAIT_CYCLES.
+__device__ __forceinline__ bool mbar_wait(unsigned long long* b, unsigned parity) {
+  if (mbar_try_wait(b, parity)) return true;
+  const long long t0 = clock64();
+  while (!mbar_try_wait(b, parity))
+    if (clock64() - t0 > WAIT_CYCLES) return false;
+  return true;
+}
+
+__device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* m, int c0, int c1, int c2, int c3,
+                                            unsigned long long* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], "
+      "[%6];" ::"r"(su32(dst)),
+      "l"(reinterpret_cast<unsigned long long>(m)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(su32(bar))
+      : "memory");
+}
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* m, int c0, int c1, int c2,
+                                            unsigned long long* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+      "[%5];" ::"r"(su32(dst)),
+      "l"(reinterpret_cast<unsigned long long>(m)), "r"(c0), "r"(c1), "r"(c2), "r"(su32(bar))
+      : "memory");
+}
+
+// Tensor memory: allocation by one warp, per-thread lane access (32x32b shape).
+__device__ __forceinline__ void tmem_alloc(unsigned* dst, unsigned ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(dst)), "r"(ncols)
+               : "memory");
+}
+__device__ __forceinline__ void tmem_relinquish() {
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(unsigned taddr, unsigned ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tmem_st4(unsigned t, unsigned a, unsigned b, unsigned c, unsigned d) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1, %2, %3, %4};" ::"r"(t), "r"(a), "r"(b), "r"(c),
+               "r"(d)
+               : "memory");
+}
+__device__ __forceinline__ void tmem_ld4(unsigned t, unsigned& a, unsigned& b, unsigned& c, unsigned& d) {
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x4.b32 {%0, %1, %2, %3}, [%4];"
+               : "=r"(a), "=r"(b), "=r"(c), "=r"(d)
+               : "r"(t)
+               : "memory");
+}
+__device__ __forceinline__ void tmem_wait_st() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+// Waits for this thread's tensor-memory loads; the 16 registers pass through
+// the instruction so that no use of them is scheduled before it.
+__device__ __forceinline__ void tmem_wait_ld16(unsigned* r) {
+  asm volatile("tcgen05.wait::ld.sync.aligned;"
+               : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]),
+                 "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]), "+r"(r[15])
+               :
+               : "memory");
+}
+
+}  // namespace tm
+
+// Shared-memory layout of one k_stage_tm block.
+template <class R, int TX, int TY>
+struct StageTm {
+  static constexpr int BX = TX + 4, BY = TY + 4;  // TMA box of one plane (x, y)
+  static constexpr int BOXN = BX * BY;
+  static constexpr unsigned UB = (unsigned)(sizeof(R) * BOXN * NV);  // state box bytes ([v][y][x])
+  static constexpr unsigned PB = (unsigned)(sizeof(R) * BOXN);       // pressure box bytes, right after
+  static constexpr size_t TILE = ((size_t)UB + PB + 127) / 128 * 128;
+  static constexpr int NSLOT = 4;
+  static constexpr int FXN = BX * TY, FYN = TX * BY;
+  static constexpr size_t OFF_FX = NSLOT * TILE;
+  static constexpr size_t OFF_FY = OFF_FX + sizeof(R) * 12 * FXN;
+  static constexpr size_t OFF_BAR = OFF_FY + sizeof(R) * 12 * FYN;
+  static constexpr size_t OFF_MISC = OFF_BAR + 8 * NSLOT;  // TMEM address, flags
+  static constexpr size_t BYTES = OFF_MISC + 16 + 128;     // + alignment slack
+  // tensor memory: per thread 5 slots x 12 quantities (32-bit columns)
+  static constexpr int WPQ = sizeof(R) / 4;              // columns per value
+  static constexpr int SLOT_COLS = 12 * WPQ;
+  static constexpr int NWARP = TX * TY / 32;
+  static constexpr int WARP_COLS = 64 * WPQ;             // column block of each warp sharing a lane quadrant
+  static constexpr int TMEM_COLS = ((NWARP + 3) / 4) * WARP_COLS;
+  static_assert(5 * SLOT_COLS <= WARP_COLS, "z ring fits the warp's column block");
+  static_assert(TMEM_COLS == 32 || TMEM_COLS == 64 || TMEM_COLS == 128 || TMEM_COLS == 256, "TMEM allocation size");
+};
+
+// 12 flux quantities to tensor-memory slot `col` of this thread's lane.
+__device__ __forceinline__ void tm_store12(unsigned ta, const float* f) {
+#pragma unroll
+  for (int a = 0; a < 3; a++)
+    tm::tmem_st4(ta + 4 * a, __float_as_uint(f[4 * a]), __float_as_uint(f[4 * a + 1]), __float_as_uint(f[4 * a + 2]),
+                 __float_as_uint(f[4 * a + 3]));
+}
+__device__ __forceinline__ void tm_store12(unsigned ta, const double* f) {
+#pragma unroll
+  for (int a = 0; a < 6; a++) {
+    const unsigned long long u0 = __double_as_longlong(f[2 * a]), u1 = __double_as_longlong(f[2 * a + 1]);
+    tm::tmem_st4(ta + 4 * a, (unsigned)u0, (unsigned)(u0 >> 32), (unsigned)u1, (unsigned)(u1 >> 32));
+  }
+}
+
+// z derivative of the 12 quantities from the ring slots of planes k-2, k-1,
+// k+1, k+2 (column addresses m2, m1, p1, p2), in the order of deriv12.
+__device__ __forceinline__ void tm_deriv12(float* Dq, unsigned m2, unsigned m1, unsigned p1, unsigned p2, float w1,
+                                           float w2) {
+  const float2 neg = make_float2(-1.0f, -1.0f), W1 = make_float2(w1, w1), W2 = make_float2(w2, w2);
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    unsigned r[16];
+    tm::tmem_ld4(m2 + 4 * a, r[0], r[1], r[2], r[3]);
+    tm::tmem_ld4(m1 + 4 * a, r[4], r[5], r[6], r[7]);
+    tm::tmem_ld4(p1 + 4 * a, r[8], r[9], r[10], r[11]);
+    tm::tmem_ld4(p2 + 4 * a, r[12], r[13], r[14], r[15]);
+    tm::tmem_wait_ld16(r);
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      const float2 a2 = make_float2(__uint_as_float(r[2 * h]), __uint_as_float(r[2 * h + 1]));
+      const float2 a1 = make_float2(__uint_as_float(r[4 + 2 * h]), __uint_as_float(r[5 + 2 * h]));
+      const float2 b1 = make_float2(__uint_as_float(r[8 + 2 * h]), __uint_as_float(r[9 + 2 * h]));
+      const float2 b2 = make_float2(__uint_as_float(r[12 + 2 * h]), __uint_as_float(r[13 + 2 * h]));
+      const float2 d1 = __ffma2_rn(a1, neg, b1);
+      const float2 d2 = __ffma2_rn(a2, neg, b2);
+      const float2 res = __ffma2_rn(W1, d1, __fmul2_rn(W2, d2));
+      Dq[4 * a + 2 * h] = res.x;
+      Dq[4 * a + 2 * h + 1] = res.y;
+    }
+  }
+}
+__device__ __forceinline__ void tm_deriv12(double* Dq, unsigned m2, unsigned m1, unsigned p1, unsigned p2, double w1,
+                                           double w2) {
+#pragma unroll
+  for (int a = 0; a < 6; a++) {
+    unsigned r[16];
+    tm::tmem_ld4(m2 + 4 * a, r[0], r[1], r[2], r[3]);
+    tm::tmem_ld4(m1 + 4 * a, r[4], r[5], r[6], r[7]);
+    tm::tmem_ld4(p1 + 4 * a, r[8], r[9], r[10], r[11]);
+    tm::tmem_ld4(p2 + 4 * a, r[12], r[13], r[14], r[15]);
+    tm::tmem_wait_ld16(r);
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      auto dbl = [&](int o) {
+        return __longlong_as_double((long long)(((unsigned long long)r[o + 1] << 32) | (unsigned long long)r[o]));
+      };
+      const double a2 = dbl(2 * h), a1 = dbl(4 + 2 * h), b1 = dbl(8 + 2 * h), b2 = dbl(12 + 2 * h);
+      Dq[2 * a + h] = w1 * (b1 - a1) + w2 * (b2 - a2);
+    }
+  }
+}
+
+// Residual terms of one direction from its derivatives Dq (the part of
+// add_direction after the differences, src/mhdres_SR.C:373-412).
+template <class R, int D1>
+__device__ __forceinline__ void apply_direction(R* Racc, const R* Dq, const R* cen, R lf) {
+  R res[NV];
+  res[0] = (R)0.0 - Dq[0];
+  res[1] = (R)0.0 - Dq[1];
+  res[2] = (R)0.0 - Dq[2];
+  res[3] = (R)0.0 - Dq[3];
+  res[4] = (R)0.0 - Dq[4];
+  res[5] = (R)0.0;
+  res[6] = (R)0.0;
+  res[7] = (R)0.0;
+  res[Dirs<D1>::fa] = (R)0.0 - Dq[5];
+  res[Dirs<D1>::fb] = (R)0.0 - Dq[6];
+  const R dB2 = Dq[10], dB3 = Dq[11];
+  const R Bd1 = cen[P_B1 + D1];
+  const R Bd2 = cen[P_B1 + Dirs<D1>::d2], Bd3 = cen[P_B1 + Dirs<D1>::d3];
+  R cbb[3];
+  cbb[D1] = -Bd2 * dB2 - Bd3 * dB3;
+  cbb[Dirs<D1>::d2] = Bd1 * dB2;
+  cbb[Dirs<D1>::d3] = Bd1 * dB3;
+  const R lrt0 = lf * Dq[7] + ((R)1.0 - lf) * cbb[0];
+  const R lrt1 = lf * Dq[8] + ((R)1.0 - lf) * cbb[1];
+  const R lrt2 = lf * Dq[9] + ((R)1.0 - lf) * cbb[2];
+  res[1] += lrt0;
+  res[2] += lrt1;
+  res[3] += lrt2;
+  res[4] += cen[P_V1] * lrt0 + cen[P_V2] * lrt1 + cen[P_V3] * lrt2;
+#pragma unroll
+  for (int q = 0; q < NV; q++) Racc[q] += res[q];
+}
+
+// Launch: grid (ceil(nx/TX), ceil(ny/TY), z chunks), TX*TY threads,
+// StageTm::BYTES of dynamic shared memory.  mapU: the input state as a 4-D
+// tensor (x, y, z, variable), box (TX+4, TY+4, 1, 8); mapP: its pressure,
+// box (TX+4, TY+4, 1).  Other arguments as k_stage.
+template <class R, int TX, int TY, bool RESID>
+__global__ void __launch_bounds__(TX* TY, 2)
+    k_stage_tm(const __grid_constant__ CUtensorMap mapU, const __grid_constant__ CUtensorMap mapP, Consts c,
+               const R* __restrict__ U0, R* __restrict__ Uout, R* __restrict__ Pout, R* __restrict__ Res,
+               Dyn* __restrict__ dyn, int stage, int zc, int write_pres) {
+  using L = StageTm<R, TX, TY>;
+  constexpr int CW = CellW<R>::W;
+  constexpr int NT = TX * TY;
+  constexpr int NH = 4 * TY + 4 * TX;
+  static_assert(NH <= NT, "every halo cell needs a thread");
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* sm = smem_raw + ((128u - (tm::su32(smem_raw) & 127u)) & 127u);
+  R* FX = reinterpret_cast<R*>(sm + L::OFF_FX);
+  R* FY = reinterpret_cast<R*>(sm + L::OFF_FY);
+  unsigned long long* bar = reinterpret_cast<unsigned long long*>(sm + L::OFF_BAR);
+  unsigned* misc = reinterpret_cast<unsigned*>(sm + L::OFF_MISC);  // [0] TMEM base, [1] skip, [2] timeout
+  const Geom& g = c.g;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int tx = tid % TX, ty = tid / TX;
+  if (tid == 0) {
+    misc[1] = RESID ? 0u : (unsigned)(*(volatile int*)&dyn->err);
+    misc[2] = 0u;
+    for (int s = 0; s < L::NSLOT; s++) tm::mbar_init(&bar[s], 1);
+    tm::fence_mbar_init();
+    tm::fence_proxy_async();
+  }
+  __syncthreads();
+  if (misc[1]) return;  // an earlier launch of the step failed (uniform for the block)
+  if (warp == 0) {
+    tm::tmem_alloc(&misc[0], L::TMEM_COLS);
+    tm::tmem_relinquish();
+  }
+  tm::tc_fence_before();
+  __syncthreads();
+  tm::tc_fence_after();
+  const unsigned tmem = misc[0];
+  // this thread's lane (its warp's quadrant) and its warp's column block
+  const unsigned ta = tmem + ((unsigned)((warp & 3) * 32) << 16) + (unsigned)((warp >> 2) * L::WARP_COLS);
+
+  const int bx0 = blockIdx.x * TX, by0 = blockIdx.y * TY;  // box origin = tile origin - 2 (x0 - GH, y0 - GH)
+  const int x0 = GH + bx0, y0 = GH + by0;
+  const int zb = GH + blockIdx.z * zc;
+  const int ze = min(zb + zc, GH + g.nz);
+  const int i = x0 + tx, j = y0 + ty;
+  const bool active = (i < GH + g.nx) && (j < GH + g.ny);
+  int hlx = 0, hly = 0;
+  const bool hx = tid < 4 * TY;
+  if (tid < NH) {
+    if (hx) {
+      const int c4 = tid & 3;
+      hlx = c4 < 2 ? c4 - 2 : TX + c4 - 2;
+      hly = tid >> 2;
+    } else {
+      const int r = tid - 4 * TY;
+      hlx = r % TX;
+      const int q = r / TX;
+      hly = q < 2 ? q - 2 : TY + q - 2;
+    }
+  }
+  const KC<R>& kk_ = kc<R>(c);
+  const DynR<R>& dr = dynr<R>(dyn);
+  const R inv_va2max = dr.inv_va2max;
+  // per-step scalars (src/Add_Sources_Integrate_SR.C:44, 84-85)
+  const R wdt = dr.wdt[(stage >= 1 && stage <= 4) ? stage : 0];
+  const R invRdt = dr.invRdt;
+  const R vmax = dr.vmax;
+  const R emax = dr.emax;
+  R prim[NF];
+  R fl[NF];
+  prim[NPRIM] = (R)0;
+  fl[NPRIM] = (R)0;
+
+  // plane tiles: plane p is tile t = p - (zb - 2), slot t % 4, phase (t / 4) % 2
+  const int p_first = zb - 2;
+  auto tile = [&](int p) { return reinterpret_cast<const R*>(sm + (size_t)((p - p_first) & 3) * L::TILE); };
+  auto issue = [&](int p) {  // one thread
+    const int t = p - p_first, sl = t & 3;
+    unsigned char* dst = sm + (size_t)sl * L::TILE;
+    tm::fence_proxy_async();
+    tm::mbar_arrive_expect_tx(&bar[sl], L::UB + L::PB);
+    tm::tma_load_4d(dst, &mapU, bx0, by0, p, 0, &bar[sl]);
+    tm::tma_load_3d(dst + L::UB, &mapP, bx0, by0, p, &bar[sl]);
+  };
+  bool timed_out = false;
+  auto wait_tile = [&](int p) {
+    const int t = p - p_first;
+    if (!tm::mbar_wait(&bar[t & 3], (unsigned)((t >> 2) & 1))) timed_out = true;
+  };
+  // cell offsets inside a tile: own cell and halo cell
+  const int o_own = (ty + 2) * L::BX + (tx + 2);
+  const int o_halo = (hly + 2) * L::BX + (hlx + 2);
+  auto raw_at = [&](const R* T, int o, Raw9<R>& r) {
+#pragma unroll
+    for (int q = 0; q < 9; q++) r.v[q] = T[q * L::BOXN + o];
+  };
+  // z-flux ring in tensor memory: slot s at columns s * SLOT_COLS
+  auto zcol = [&](int s) { return ta + (unsigned)(s * L::SLOT_COLS); };
+  auto slot_add = [](int sl, int d) { return sl + d >= 5 ? sl + d - 5 : sl + d; };
+
+  if (tid == 0)
+    for (int p = zb - 2; p < zb + 2; p++) issue(p);
+  for (int p = zb - 2; p < zb + 2; p++) {
+    wait_tile(p);
+    __syncwarp();
+    Raw9<R> r;
+    raw_at(tile(p), o_own, r);
+    prim_of_raw<R, RESID>(r, prim);
+    flux12<R, 2>(prim, 1, fl, 1);
+    tm_store12(zcol(p - zb + 2), fl);
+  }
+  tm::tmem_wait_st();
+  __syncthreads();
+  if (tid == 0) issue(zb + 2);
+
+  const unsigned plane = (unsigned)g.sx * (unsigned)g.sy;
+  const unsigned own0 = cidx32(g, i, j, 0);
+  int s0 = 2;  // ring slot of plane k
+  for (int k = zb; k < ze; k++, s0 = slot_add(s0, 1)) {
+    if (tid == 0 && k + 1 < ze) issue(k + 3);
+    // z flux of plane k+2 (all lanes: tensor-memory stores are warp-wide)
+    wait_tile(k + 2);
+    __syncwarp();
+    {
+      Raw9<R> r;
+      raw_at(tile(k + 2), o_own, r);
+      prim_of_raw<R, RESID>(r, prim);
+      flux12<R, 2>(prim, 1, fl, 1);
+      tm_store12(zcol(slot_add(s0, 2)), fl);
+    }
+    // own cell: primitives and x / y fluxes; halo cell: its x or y flux
+    R cen[NF];
+    {
+      const R* T = tile(k);
+      Raw9<R> r;
+      raw_at(T, o_own, r);
+      prim_of_raw<R, RESID>(r, cen);
+      cen[NPRIM] = (R)0;
+      flux12<R, 0>(cen, 1, fl, 1);
+      store_cell(FX + (ty * L::BX + tx + 2) * CW, fl);
+      flux12<R, 1>(cen, 1, fl, 1);
+      store_cell(FY + ((ty + 2) * TX + tx) * CW, fl);
+      if (tid < NH) {
+        raw_at(T, o_halo, r);
+        prim_of_raw<R, RESID>(r, prim);
+        if (hx) {
+          flux12<R, 0>(prim, 1, fl, 1);
+          store_cell(FX + (hly * L::BX + hlx + 2) * CW, fl);
+        } else {
+          flux12<R, 1>(prim, 1, fl, 1);
+          store_cell(FY + ((hly + 2) * TX + hlx) * CW, fl);
+        }
+      }
+    }
+    const unsigned id = own0 + (unsigned)k * plane;
+    R base[NV];
+    if (active) {
+      const R* src = RESID ? Res : U0;
+#pragma unroll
+      for (int q = 0; q < NV; q++) base[q] = src[id + (unsigned)q * g.N32];
+    }
+    tm::tmem_wait_st();
+    __syncthreads();
+    // z derivative (all lanes), then the cell's residual and update
+    R Dz[NF];
+    __syncwarp();
+    tm_deriv12(Dz, zcol(slot_add(s0, 3)), zcol(slot_add(s0, 4)), zcol(slot_add(s0, 1)), zcol(slot_add(s0, 2)),
+               kk_.w1[2], kk_.w2[2]);
+    if (active) {
+      R Racc[NV];
+      if (RESID) {
+#pragma unroll
+        for (int q = 0; q < NV; q++) Racc[q] = base[q];
+      } else {
+#pragma unroll
+        for (int q = 0; q < NV; q++) Racc[q] = (R)0.0;
+      }
+      // Boris factor at the cell (src/mhdres_SR.C:310-323)
+      R lf;
+      {
+        const R dn = (R)1.0 / cen[P_D];
+        const R bb = cen[P_B1] * cen[P_B1] + cen[P_B2] * cen[P_B2] + cen[P_B3] * cen[P_B3];
+        const R va2 = bb * dn;
+        const R x2 = va2 * inv_va2max, x4 = x2 * x2, s = (R)1.0 + x2;
+        lf = s / (s + x4);
+      }
+      {
+        R Dq[NF];
+        const R* fb = FX + (ty * L::BX + tx + 2) * CW;
+        deriv12(Dq, fb - 2 * CW, fb - CW, fb + CW, fb + 2 * CW, kk_.w1[0], kk_.w2[0]);
+        apply_direction<R, 0>(Racc, Dq, cen, lf);
+      }
+      {
+        R Dq[NF];
+        const R* fb = FY + ((ty + 2) * TX + tx) * CW;
+        deriv12(Dq, fb - 2 * TX * CW, fb - TX * CW, fb + TX * CW, fb + 2 * TX * CW, kk_.w1[1], kk_.w2[1]);
+        apply_direction<R, 1>(Racc, Dq, cen, lf);
+      }
+      apply_direction<R, 2>(Racc, Dz, cen, lf);
+      if (RESID) {
+#pragma unroll
+        for (int q = 0; q < NV; q++) Res[id + (unsigned)q * g.N32] = Racc[q];
+        R cm = cmax_cell<R>(cen[P_D], cen[P_V1], cen[P_V2], cen[P_V3], cen[P_B1], cen[P_B2], cen[P_B3], cen[P_P],
+                            inv_va2max);
+        atomic_max_nonneg(&dyn->cmax_bits, (double)cm);
+      } else {
+        // sources, Boris correction, update, Tcheck (src/Add_Sources_Integrate_SR.C:331-465)
+        const R rh = cen[P_D], vx = cen[P_V1], vy = cen[P_V2], vz = cen[P_V3];
+        const R bx = cen[P_B1], by = cen[P_B2], bz = cen[P_B3];
+        R dn = invRdt * cen[P_EI];
+        R efaci = (dn > (R)0 && dn < (R)INFINITY) ? (R)1.0 : dn / d_fmax(dn, (R)0.0);
+        dn = kk_.gx * rh - (R)0.0;
+        const R edmp = dn * vx;
+        Racc[1] += dn;
+        Racc[4] += edmp + (R)0.0 * efaci;
+        const R rd = Racc[0];
+        R fx = Racc[1], fy = Racc[2], fz = Racc[3];
+        const R bb = bx * bx + by * by + bz * bz;
+        const R va2 = bb / rh;
+        const R x2 = va2 * inv_va2max, x4 = x2 * x2;
+        const R bf = x4 / ((R)1 + x2 + x4);
+        fx -= vx * rd;
+        fy -= vy * rd;
+        fz -= vz * rd;
+        const R q = (fx * bx + fy * by + fz * bz) / d_fmax(tiny100<R>(), bb);
+        const R b0 = -bf * (fx - q * bx), b1 = -bf * (fy - q * by), b2 = -bf * (fz - q * bz);
+        const R b3 = b0 * vx + b1 * vy + b2 * vz;
+        Racc[1] += b0;
+        Racc[2] += b1;
+        Racc[3] += b2;
+        Racc[4] += b3;
+        R un[NV];
+#pragma unroll
+        for (int v = 0; v < NV; v++) un[v] = base[v] + wdt * Racc[v];
+        tcheck_cell<R>(c, vmax, emax, un[0], un[1], un[2], un[3], un[4]);
+        const Images im = images_of(g, i, j, k, true);
+        store_state<R, true>(g, Uout, i, j, k, im, un);
+        if (write_pres) {
+          R v1, v2, v3, ei;
+          prim_from_cons(un[0], un[1], un[2], un[3], un[4], v1, v2, v3, ei);
+          const R pr = eos_pres(c, un[0], ei, (R)1.0 / un[0]);
+          store_scalar<R, true>(g, Pout, i, j, k, im, pr);
+        }
+      }
+    }
+    __syncthreads();
+  }
+
+  // teardown: report an expired wait, let issued copies land, free tensor memory
+  if (timed_out) atomicExch(&misc[2], 1u);
+  tm::tc_fence_before();
+  __syncthreads();
+  if (misc[2]) {
+    if (tid == 0) {
+      atomicExch(&dyn->err, (int)ERR_WAIT_TIMEOUT);
+      // the last four tiles issued are the only ones that can be in flight
+      const int p_last = max(ze + 1, zb + 2);
+      for (int p = max(p_first, p_last - 3); p <= p_last; p++) {
+        const int t = p - p_first;
+        tm::mbar_wait(&bar[t & 3], (unsigned)((t >> 2) & 1));
+      }
+    }
+    __syncthreads();
+  }
+  if (warp == 0) {
+    __syncwarp();
+    tm::tmem_dealloc(tmem, L::TMEM_COLS);
+  }
+}
+
+}  // namespace gpumhd

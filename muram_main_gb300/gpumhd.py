@@ -41,7 +41,7 @@ class Params(C.Structure):
     """ctypes mirror of ``gpumhd_params``."""
     _fields_ = [
         ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("periodic_x", C.c_int),
-        ("precision", C.c_int), ("pad0", C.c_int),
+        ("precision", C.c_int), ("stage_kernel", C.c_int),
         ("dx", C.c_double * 3),
         ("CFL", C.c_double), ("CFL_tvd", C.c_double), ("dt", C.c_double), ("time", C.c_double),
         ("outcad", C.c_double), ("autostep", C.c_int), ("pad1", C.c_int),

@@ -18,8 +18,15 @@ TOL32_L2 = 1e-5
 pytestmark = pytest.mark.gpu
 
 
-def ctx_for(hp, precision=64):
-    return gpumhd.MuramGPU(H.gpu_params(hp, precision), eos_path=H.EOS_SMALL)
+# stage_kernel 0: TMA plane loads + tensor-memory z ring (where the box allows
+# it); 1: the plain-load stage kernel.  Both must meet the same bars.
+KERNELS = [0, 1]
+
+
+def ctx_for(hp, precision=64, stage_kernel=0):
+    p = H.gpu_params(hp, precision)
+    p.stage_kernel = stage_kernel
+    return gpumhd.MuramGPU(p, eos_path=H.EOS_SMALL)
 
 
 def check(name, got, ref, tol=TOL64):
@@ -38,9 +45,10 @@ def test_cons_to_prim(gpu_lib):
     check("ConsToPrim pres/temp/ne/rhoi/amb", aux, d["s1_c2p_aux"])
 
 
-def test_mhd_residual_and_dt(gpu_lib):
+@pytest.mark.parametrize("kernel", KERNELS)
+def test_mhd_residual_and_dt(gpu_lib, kernel):
     d, hp = H.load_case("periodic")
-    g = ctx_for(hp)
+    g = ctx_for(hp, stage_kernel=kernel)
     g.upload_state(d["s1_c2p_U"])
     g.upload_field(gpumhd.FIELD_PRES, d["s1_c2p_aux"][0])
     g.upload_state(np.zeros_like(d["s1_c2p_U"]), gpumhd.FIELD_RES)
@@ -104,13 +112,14 @@ def test_reference_order_steps(gpu_lib, name):
 
 @pytest.mark.parametrize("name", H.CASES)
 @pytest.mark.parametrize("capture", [0, 1])
-def test_fused_steps(gpu_lib, name, capture):
+@pytest.mark.parametrize("kernel", KERNELS)
+def test_fused_steps(gpu_lib, name, capture, kernel):
     d, hp = H.load_case(name)
-    g = ctx_for(hp)
+    g = ctx_for(hp, stage_kernel=kernel)
     g.upload_state(d["input_U"])
     dts = g.run_steps(int(d["steps"]), capture=bool(capture))
     assert np.allclose(dts, d["dts"].reshape(-1, 3)[:, 0], rtol=TOL64, atol=0)
-    check(f"fused steps[{name}, graph={capture}]", g.download_state(), d["final_U"])
+    check(f"fused steps[{name}, graph={capture}, kernel={kernel}]", g.download_state(), d["final_U"])
     assert g.step_info()[3] == (1 if name == "two_half_tvd" else 0)
 
 
@@ -122,12 +131,13 @@ def _oracle_run(hp, U, steps):
     return st.U, dts
 
 
-def test_fused_vs_oracle_anisotropic(gpu_lib):
+@pytest.mark.parametrize("kernel", KERNELS)
+def test_fused_vs_oracle_anisotropic(gpu_lib, kernel):
     tab = initial.EosTable(H.EOS_SMALL)
     hp = dict(nx=40, ny=24, nz=20, dx=2.4e6, dy=3.2e6, dz=4.0e6)
     U = initial.periodic_box(tab, 40, 24, 20, dx=2.4e6, dy=3.2e6, dz=4.0e6, seed=77)
     ref, dts_ref = _oracle_run(hp, U, 12)
-    p = gpumhd.default_params(40, 24, 20, 2.4e6, dy=3.2e6, dz=4.0e6)
+    p = gpumhd.default_params(40, 24, 20, 2.4e6, dy=3.2e6, dz=4.0e6, stage_kernel=kernel)
     g = gpumhd.MuramGPU(p, eos_path=H.EOS_SMALL)
     g.upload_state(U)
     dts = g.run_steps(12)
@@ -147,15 +157,50 @@ def test_fused_fp64_100_steps(gpu_lib):
     check("FP64 fused vs oracle, 32^3, 100 steps", H.interior(g.download_state()), H.interior(ref))
 
 
-def test_fused_fp32_error_vs_fp64_oracle(gpu_lib):
+@pytest.mark.parametrize("kernel", KERNELS)
+def test_fused_fp32_error_vs_fp64_oracle(gpu_lib, kernel):
     """FP32 storage and arithmetic: relative L2 per field after 100 steps."""
     tab = initial.EosTable(H.EOS_SMALL)
     hp = dict(nx=32, ny=32, nz=32)
     U = initial.periodic_box(tab, 32, 32, 32, seed=5)
     ref, _ = _oracle_run(hp, U, 100)
-    g = gpumhd.MuramGPU(gpumhd.default_params(32, 32, 32, 3.2e6, precision=32), eos_path=H.EOS_SMALL)
+    g = gpumhd.MuramGPU(gpumhd.default_params(32, 32, 32, 3.2e6, precision=32, stage_kernel=kernel),
+                        eos_path=H.EOS_SMALL)
     g.upload_state(U)
     g.run_steps(100)
     e = H.rel_l2(H.interior(g.download_state()), H.interior(ref))
     print("FP32 vs FP64 oracle rel L2 per field:", np.array2string(e, precision=2))
+    assert np.all(e <= TOL32_L2), e
+
+
+def test_fp32_stage_kernels_agree_on_stratified_box(gpu_lib):
+    """Closed x with gravity, partial tiles in every direction (36 x 20 x 12):
+    the TMA / tensor-memory and the plain-load stage kernels give the same
+    FP32 state after 10 steps, to float rounding."""
+    tab = initial.EosTable(H.EOS_SMALL)
+    U = initial.stratified_box(tab, 36, 20, 12, seed=3)
+    out = []
+    for kernel in KERNELS:
+        p = gpumhd.default_params(36, 20, 12, 1.6e6, precision=32, periodic_x=0, grav=2.74e4, stage_kernel=kernel)
+        g = gpumhd.MuramGPU(p, eos_path=H.EOS_SMALL)
+        g.upload_state(U)
+        g.run_steps(10)
+        out.append(g.download_state())
+        g.close()
+    e = H.rel_linf(out[0], out[1])
+    print("TMA vs plain-load stage kernel, FP32, rel Linf:", np.array2string(e, precision=2))
+    assert np.all(e <= 1e-5), e
+
+
+def test_fp32_shape_without_tma_rows(gpu_lib):
+    """nx = 30: rows of 34 floats are not 16-byte multiples, so the context
+    takes the plain-load kernel; it still meets the FP32 bar (20 steps)."""
+    tab = initial.EosTable(H.EOS_SMALL)
+    hp = dict(nx=30, ny=16, nz=12)
+    U = initial.periodic_box(tab, 30, 16, 12, seed=8)
+    ref, _ = _oracle_run(hp, U, 20)
+    g = gpumhd.MuramGPU(gpumhd.default_params(30, 16, 12, 3.2e6, precision=32), eos_path=H.EOS_SMALL)
+    g.upload_state(U)
+    g.run_steps(20)
+    e = H.rel_l2(H.interior(g.download_state()), H.interior(ref))
     assert np.all(e <= TOL32_L2), e
