@@ -137,6 +137,11 @@ __host__ __device__ inline void derive_one(const Dyn& d, const double dx[3], con
 // std::max / std::min semantics: the first argument wins ties and NaNs.
 template <class R> __device__ __forceinline__ R smax(R a, R b) { return (a < b) ? b : a; }
 template <class R> __device__ __forceinline__ R smin(R a, R b) { return (b < a) ? b : a; }
+// FP32 mode: one min/max instruction instead of a compare and a select; it
+// differs from std::max/min only in which operand a NaN or a signed zero
+// yields, which the FP32 mode does not reproduce anyway.
+template <> __device__ __forceinline__ float smax<float>(float a, float b) { return fmaxf(a, b); }
+template <> __device__ __forceinline__ float smin<float>(float a, float b) { return fminf(a, b); }
 
 // The reference's 1e-100 floors; float cannot hold 1e-100, so FP32 uses 1e-30.
 template <class R> __device__ __forceinline__ R tiny100();

@@ -116,6 +116,14 @@ __device__ __forceinline__ void load_raw(const Geom& g, const R* __restrict__ U,
   r.v[8] = P[id];
 }
 
+template <class R>
+__device__ __forceinline__ void load_raw64(const Geom& g, const R* __restrict__ U, const R* __restrict__ P, long long id,
+                                           Raw9<R>& r) {
+#pragma unroll
+  for (int q = 0; q < NV; q++) r.v[q] = U[(long long)q * g.N + id];
+  r.v[8] = P[id];
+}
+
 __device__ __forceinline__ void fill_raw_one(Raw9<float>& r) {
 #pragma unroll
   for (int q = 0; q < 9; q++) r.v[q] = 1.0f;
@@ -526,18 +534,19 @@ struct TvdArgs {
   int n1;                // interior cells along the sweep
 };
 
+// Per-cell quantities from the cell's stored values r (state and pressure)
+// and its vertical boundary profiles hb, ht, qt.
 template <class R>
-__device__ __forceinline__ void tvd_load(const Consts& c, const R* __restrict__ U, const R* __restrict__ P, long long id,
-                                         int xi, R cmax_t, R fac0, bool hyper, R inv_va2max, TCell<R>& t) {
-  const Geom& g = c.g;
+__device__ __forceinline__ void tvd_cell(const Consts& c, const Raw9<R>& r, R hb, R ht, R qt, R cmax_t, R fac0,
+                                         bool hyper, R inv_va2max, TCell<R>& t) {
   const KC<R>& k = kc<R>(c);
   const R rho_min = k.rho_min;
-  R d = smax(rho_min, U[id]);
-  R v1 = U[g.N + id], v2 = U[2 * g.N + id], v3 = U[3 * g.N + id], e = U[4 * g.N + id];
-  R b5 = U[5 * g.N + id], b6 = U[6 * g.N + id], b7 = U[7 * g.N + id];
-  t.hb = k.hfb[xi];
-  t.ht = k.hft[xi];
-  t.qt = k.qft[xi];
+  R d = smax(rho_min, r.v[0]);
+  R v1 = r.v[1], v2 = r.v[2], v3 = r.v[3], e = r.v[4];
+  R b5 = r.v[5], b6 = r.v[6], b7 = r.v[7];
+  t.hb = hb;
+  t.ht = ht;
+  t.qt = qt;
   R dn = (R)1.0 / d;
   v1 = v1 * dn;
   v2 = v2 * dn;
@@ -551,7 +560,7 @@ __device__ __forceinline__ void tvd_load(const Consts& c, const R* __restrict__ 
   R va2 = bb * dn;
   R x2 = va2 * inv_va2max, x4 = x2 * x2, s = (R)1.0 + x2;
   R lf = s / (s + x4);
-  R cs2 = (R)(5.0 / 3.0) * P[id] * dn;
+  R cs2 = (R)(5.0 / 3.0) * r.v[8] * dn;
   R cfast = d_sqrt(va2 + cs2);
   const R CZ = k.CZ;
   R CME = ((R)1.0 - CZ) * ((R)(vv >= k.CME_thresh * cfast));
@@ -579,6 +588,18 @@ __device__ __forceinline__ void tvd_load(const Consts& c, const R* __restrict__ 
     e = d_log(e);
   }
   t.q[0] = d; t.q[1] = v1; t.q[2] = v2; t.q[3] = v3; t.q[4] = e; t.q[5] = b5; t.q[6] = b6; t.q[7] = b7;
+}
+
+template <class R>
+__device__ __forceinline__ void tvd_load(const Consts& c, const R* __restrict__ U, const R* __restrict__ P, long long id,
+                                         int xi, R cmax_t, R fac0, bool hyper, R inv_va2max, TCell<R>& t) {
+  const Geom& g = c.g;
+  const KC<R>& k = kc<R>(c);
+  Raw9<R> r;
+#pragma unroll
+  for (int q = 0; q < NV; q++) r.v[q] = U[(long long)q * g.N + id];
+  r.v[8] = P[id];
+  tvd_cell<R>(c, r, k.hfb[xi], k.hft[xi], k.qft[xi], cmax_t, fac0, hyper, inv_va2max, t);
 }
 
 // Limited slope at the middle cell b (src/tvdlimit_SR.C:388-434)
@@ -675,16 +696,16 @@ __global__ void __launch_bounds__(128) k_tvd_sweep(Consts c, const R* __restrict
   const Geom& g = c.g;
   if (dyn->err) return;
   if (ta.only_two_half && !dyn->two_half) return;   // second half pass not taken this step
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const int nch = (ta.n1 + ta.td - 1) / ta.td;
-  const long long total = (long long)ta.na * ta.nb * nch;
+  const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+  const unsigned nch = (unsigned)((ta.n1 + ta.td - 1) / ta.td);
+  const unsigned total = (unsigned)ta.na * (unsigned)ta.nb * nch;
   bool live = t < total;
   int a = 0, b = 0, ch = 0;
   if (live) {
-    a = (int)(t % ta.na);
-    long long r = t / ta.na;
-    b = (int)(r % ta.nb);
-    ch = (int)(r / ta.nb);
+    a = (int)(t % (unsigned)ta.na);
+    const unsigned r = t / (unsigned)ta.na;
+    b = (int)(r % (unsigned)ta.nb);
+    ch = (int)(r / (unsigned)ta.nb);
   }
   const int aa = ta.a0 + a, bb = ta.b0 + b;
   const long long base = (long long)aa * ta.sa + (long long)bb * ta.sb;
@@ -726,8 +747,22 @@ __global__ void __launch_bounds__(128) k_tvd_sweep(Consts c, const R* __restrict
       tvd_slope<R>(c, cm1, c0, c1, vsqr_diff, s0);
       tvd_flux<R, DIR>(c, cmm, cm1, c0, c1, sm, s0, p0 - 1, sz, fac0, cmax_t, hyper, istart, Fm, qm);
     }
+    // the boundary profiles depend on x only: fixed along a y or z pencil
+    R hb_f = (R)0, ht_f = (R)0, qt_f = (R)0;
+    if (DIR != 0) { hb_f = kk_.hfb[aa]; ht_f = kk_.hft[aa]; qt_f = kk_.qft[aa]; }
+    // the next cell's stored values are loaded one step ahead of their use
+    Raw9<R> nxt;
+    load_raw64<R>(g, Uin, Pst, base + (long long)(p0 + 2) * ta.sd, nxt);
     for (int pos = p0; pos < p1; pos++) {
-      tvd_load<R>(c, Uin, Pst, base + (long long)(pos + 2) * ta.sd, xi_of(pos + 2), cmax_t, fac0, hyper, inv_va2max, c2);
+      const long long id = base + (long long)pos * ta.sd;
+      R uc[NV];
+#pragma unroll
+      for (int v = 0; v < NV; v++) uc[v] = Uin[(long long)v * g.N + id];
+      if (DIR == 0)
+        tvd_cell<R>(c, nxt, kk_.hfb[pos + 2], kk_.hft[pos + 2], kk_.qft[pos + 2], cmax_t, fac0, hyper, inv_va2max, c2);
+      else
+        tvd_cell<R>(c, nxt, hb_f, ht_f, qt_f, cmax_t, fac0, hyper, inv_va2max, c2);
+      if (pos + 1 < p1) load_raw64<R>(g, Uin, Pst, base + (long long)(pos + 3) * ta.sd, nxt);
       tvd_slope<R>(c, c0, c1, c2, vsqr_diff, s1);
       tvd_flux<R, DIR>(c, cm1, c0, c1, c2, s0, s1, pos, sz, fac0, cmax_t, hyper, istart, F0, q0);
       // update of cell pos (src/tvdlimit_SR.C:565-657)
@@ -747,10 +782,9 @@ __global__ void __launch_bounds__(128) k_tvd_sweep(Consts c, const R* __restrict
         R qres = (R)0.5 * (q0 + qm) * c0.qt;
         res[4] += dtt * qres;
       }
-      const long long id = base + (long long)pos * ta.sd;
       R u[NV];
 #pragma unroll
-      for (int v = 0; v < NV; v++) u[v] = Uin[(long long)v * g.N + id] + res[v];
+      for (int v = 0; v < NV; v++) u[v] = uc[v] + res[v];
       u[0] = smax(kk_.rho_min, u[0]);
       u[4] = smax(u[4], kk_.eps_min * u[0] + (R)0.5 * (u[1] * u[1] + u[2] * u[2] + u[3] * u[3]) / u[0]);
       if (ta.mode == 0) {
@@ -818,15 +852,6 @@ template <class R>
 __device__ __forceinline__ R shfl(R v, int src) { return __shfl_sync(0xffffffffu, v, src); }
 
 template <class R>
-__device__ __forceinline__ void shfl_cell(const TCell<R>& in, TCell<R>& out, int src) {
-#pragma unroll
-  for (int v = 0; v < NV; v++) out.q[v] = shfl(in.q[v], src);
-  out.cm = shfl(in.cm, src); out.he = shfl(in.he, src); out.hv = shfl(in.hv, src); out.hB = shfl(in.hB, src);
-  out.BC2 = shfl(in.BC2, src); out.bsqr = shfl(in.bsqr, src); out.vsqr = shfl(in.vsqr, src);
-  out.hd = shfl(in.hd, src); out.hb = shfl(in.hb, src); out.ht = shfl(in.ht, src); out.qt = shfl(in.qt, src);
-}
-
-template <class R>
 __global__ void __launch_bounds__(128) k_tvd_sweep_xlanes(Consts c, const R* __restrict__ Uin, const R* __restrict__ Pst,
                                                           R* __restrict__ Uout, Dyn* __restrict__ dyn, int only_two_half) {
   const Geom& g = c.g;
@@ -834,9 +859,9 @@ __global__ void __launch_bounds__(128) k_tvd_sweep_xlanes(Consts c, const R* __r
   if (only_two_half && !dyn->two_half) return;
   constexpr int OUT = 28;
   const int lane = threadIdx.x & 31;
-  const int nseg = (g.nx + OUT - 1) / OUT;
-  const long long total = (long long)g.sy * g.sz * nseg;
-  const long long nwarps = ((long long)gridDim.x * blockDim.x) >> 5;
+  const unsigned nseg = (unsigned)((g.nx + OUT - 1) / OUT);
+  const unsigned total = (unsigned)g.sy * (unsigned)g.sz * nseg;
+  const unsigned nwarps = (gridDim.x * blockDim.x) >> 5;
   const DynR<R>& dr = dynr<R>(dyn);
   const R dtt = dr.dt_tvd;
   const R cmax_t = dr.cmax_t[0];
@@ -847,28 +872,40 @@ __global__ void __launch_bounds__(128) k_tvd_sweep_xlanes(Consts c, const R* __r
   const KC<R>& kk_ = kc<R>(c);
   const int istart = 1 + (g.periodic_x ? 0 : GH);
   const int sz = g.nx + 2 * GH;
+  const int lm = max(lane - 1, 0), lp = min(lane + 1, 31), lpp = min(lane + 2, 31);
   // whole warps stride over (pencil, segment) pairs together
-  for (long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; warp < total; warp += nwarps) {
-    const int seg = (int)(warp % nseg);
-    const long long pen = warp / nseg;
-    const int j = (int)(pen % g.sy), k = (int)(pen / g.sy);
-    const long long base = cidx(g, 0, j, k);
-    const int pos = GH + OUT * seg - 2 + lane;          // this lane's cell along x
+  for (unsigned warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; warp < total; warp += nwarps) {
+    const unsigned seg = warp % nseg;
+    const unsigned pen = warp / nseg;
+    const unsigned j = pen % (unsigned)g.sy, k = pen / (unsigned)g.sy;
+    const long long base = (long long)g.sx * ((long long)j + (long long)g.sy * (long long)k);
+    const int pos = GH + OUT * (int)seg - 2 + lane;     // this lane's cell along x
     const int posc = min(pos, g.sx - 1);                 // clamped for the tail of the last segment
     TCell<R> c0, cl, cr, crr;
     tvd_load<R>(c, Uin, Pst, base + posc, posc, cmax_t, fac0, hyper, inv_va2max, c0);
-    shfl_cell(c0, cl, max(lane - 1, 0));
-    shfl_cell(c0, cr, min(lane + 1, 31));
-    shfl_cell(c0, crr, min(lane + 2, 31));
+    // from the neighbours only what the slope and the interface flux read:
+    // q of both, cm and hd of the right one, q[0,1,4] two to the right (hyperdiffusion)
+#pragma unroll
+    for (int v = 0; v < NV; v++) {
+      cl.q[v] = shfl(c0.q[v], lm);
+      cr.q[v] = shfl(c0.q[v], lp);
+    }
+    cr.cm = shfl(c0.cm, lp);
+    cr.hd = shfl(c0.hd, lp);
+    if (hyper) {
+      crr.q[0] = shfl(c0.q[0], lpp);
+      crr.q[1] = shfl(c0.q[1], lpp);
+      crr.q[4] = shfl(c0.q[4], lpp);
+    }
     R s0[NV], s1[NV], F[NV], Fm[NV];
     tvd_slope<R>(c, cl, c0, cr, vsqr_diff, s0);
 #pragma unroll
-    for (int v = 0; v < NV; v++) s1[v] = shfl(s0[v], min(lane + 1, 31));
+    for (int v = 0; v < NV; v++) s1[v] = shfl(s0[v], lp);
     R qr;
     tvd_flux<R, 0>(c, cl, c0, cr, crr, s0, s1, pos, sz, fac0, cmax_t, hyper, istart, F, qr);
 #pragma unroll
-    for (int v = 0; v < NV; v++) Fm[v] = shfl(F[v], max(lane - 1, 0));
-    const R qm = shfl(qr, max(lane - 1, 0));
+    for (int v = 0; v < NV; v++) Fm[v] = shfl(F[v], lm);
+    const R qm = shfl(qr, lm);
     if (lane < 2 || lane >= 30 || pos >= GH + g.nx) continue;
     R res[NV];
 #pragma unroll
