@@ -278,7 +278,7 @@ static EncodeTiledFn encode_tiled_fn() {
 // row stride to be a multiple of 16 bytes: (nx+4)*sizeof(real) % 16 == 0.
 template <class R>
 static bool make_tensor_maps(gpumhd_ctx* ctx) {
-  constexpr int TX = StageTile<R>::TX, TY = StageTile<R>::TY;
+  constexpr int TX = StageTileTm<R>::TX, TY = StageTileTm<R>::TY;
   const Geom& g = ctx->c.g;
   const cuuint64_t esz = sizeof(R);
   if (((cuuint64_t)g.sx * esz) % 16 != 0) return false;

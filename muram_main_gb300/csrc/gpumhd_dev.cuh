@@ -326,6 +326,54 @@ __device__ __forceinline__ float eos_pres(const Consts& c, float d, float ei, fl
   return q.x * exp_small(fe * q.y + fr * q.z + fe * fr * q.w);
 }
 
+// The pressure lookup split in two, so that a kernel can issue the table
+// loads of one cell and finish the value later (after other work): begin()
+// computes the cell index and starts the loads, end() returns eos_pres's
+// value.  Outside the fast path (and in FP64) begin() computes it at once.
+template <class R>
+struct PresLookup {
+  float4 q;
+  float ix, id, eps, d;
+  R done;
+  int ready;
+};
+
+__device__ __forceinline__ void eos_pres_begin(const Consts& c, double d, double ei, double dn, PresLookup<double>& L) {
+  L.done = eos_pres(c, d, ei, dn);
+  L.ready = 1;
+}
+__device__ __forceinline__ double eos_pres_end(const PresLookup<double>& L) { return L.done; }
+
+__device__ __forceinline__ void eos_pres_begin(const Consts& c, float d, float ei, float dn, PresLookup<float>& L) {
+  constexpr float LN2 = 0.69314718f;
+  const KC<float>& k = c.kf;
+  const float eps = ei * dn + k.eps_off;
+  const float lgr = __log2f(d) * LN2;
+  const float ep = __log2f(eps) * LN2;
+  if (!(lgr >= k.xlr0 + 0.01f && lgr < k.xlrN + 1.0f && ep > k.xeps0 - 1.0f && ep < k.xepsN + 1.0f &&
+        !(eps > 0.8f * k.eps_max))) {
+    L.done = (float)c2p_eos_full(c, (double)d, (double)ei, 1.0 / (double)d).pres;
+    L.ready = 1;
+    return;
+  }
+  int i_d = (int)((lgr - k.xlr0) * k.inv_del_lr);
+  i_d = max(0, min(c.N_lr - 2, i_d));
+  int i_e = (int)((ep - k.xeps0) * k.inv_del_eps);
+  i_e = max(0, min(c.N_eps - 2, i_e));
+  L.ix = __ldg(c.inv_exp_xeps + i_e);
+  L.id = __ldg(c.inv_exp_xlr + i_d);
+  L.q = __ldg(c.pquad + (long long)i_e * c.N_lr + i_d);
+  L.eps = eps;
+  L.d = d;
+  L.ready = 0;
+}
+__device__ __forceinline__ float eos_pres_end(const PresLookup<float>& L) {
+  if (L.ready) return L.done;
+  const float fe = log1p_small(L.eps * L.ix - 1.0f);
+  const float fr = log1p_small(L.d * L.id - 1.0f);
+  return L.q.x * exp_small(fe * L.q.y + fr * L.q.z + fe * fr * L.q.w);
+}
+
 // ------------------------------------------------------------ Tcheck cell
 // src/Add_Sources_Integrate_SR.C:444-465 and :600-617
 template <class R>

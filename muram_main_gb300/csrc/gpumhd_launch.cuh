@@ -38,6 +38,10 @@ struct Launch {
 template <class R> struct StageTile;
 template <> struct StageTile<double> { static constexpr int TX = 16, TY = 8; };
 template <> struct StageTile<float> { static constexpr int TX = 16, TY = 16; };
+// Tile shapes of the TMA / tensor-memory stage kernel.
+template <class R> struct StageTileTm;
+template <> struct StageTileTm<double> { static constexpr int TX = 16, TY = 8; };
+template <> struct StageTileTm<float> { static constexpr int TX = 32, TY = 8; };
 
 inline int grid_for(long long n, int block) {
   long long b = (n + block - 1) / block;
@@ -71,12 +75,13 @@ cudaError_t Launch<R>::setup() {
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_stage<R, TX, TY, false>, TX * TY, bytes);
   if (e != cudaSuccess) return e;
   resident_stage_blocks = (per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
-  const int tb = (int)StageTm<R, TX, TY>::BYTES;
-  e = cudaFuncSetAttribute(k_stage_tm<R, TX, TY, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, tb);
+  constexpr int MX = StageTileTm<R>::TX, MY = StageTileTm<R>::TY;
+  const int tb = (int)StageTm<R, MX, MY>::BYTES;
+  e = cudaFuncSetAttribute(k_stage_tm<R, MX, MY, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, tb);
   if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(k_stage_tm<R, TX, TY, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, tb);
+  e = cudaFuncSetAttribute(k_stage_tm<R, MX, MY, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, tb);
   if (e != cudaSuccess) return e;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_stage_tm<R, TX, TY, false>, TX * TY, tb);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_stage_tm<R, MX, MY, false>, MX * MY, tb);
   if (e != cudaSuccess) return e;
   resident_tm_blocks = (per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
   return cudaSuccess;
@@ -86,9 +91,9 @@ template <class R>
 void Launch<R>::stage(const Consts& c, const R* Uin, const R* Pin, const R* U0, R* Uout, R* Pout, R* Res, Dyn* dyn,
                       int stage, bool resid, int write_pres, cudaStream_t s, const CUtensorMap* mu,
                       const CUtensorMap* mp) {
-  constexpr int TX = StageTile<R>::TX, TY = StageTile<R>::TY;
-  const Geom& g = c.g;
   const bool tma = mu && mp;
+  const int TX = tma ? StageTileTm<R>::TX : StageTile<R>::TX, TY = tma ? StageTileTm<R>::TY : StageTile<R>::TY;
+  const Geom& g = c.g;
   const int bx = (g.nx + TX - 1) / TX, by = (g.ny + TY - 1) / TY;
   // z chunk length: each block computes 4 extra z-flux planes before its
   // first output plane, and a partly filled last wave idles the GPU; pick the
@@ -109,20 +114,22 @@ void Launch<R>::stage(const Consts& c, const R* Uin, const R* Pin, const R* U0, 
   const int bz = (g.nz + zc - 1) / zc;
   dim3 grid(bx, by, bz);
   if (tma) {
-    const int bytes = (int)StageTm<R, TX, TY>::BYTES;
+    constexpr int MX = StageTileTm<R>::TX, MY = StageTileTm<R>::TY;
+    const int bytes = (int)StageTm<R, MX, MY>::BYTES;
     if (resid)
-      k_stage_tm<R, TX, TY, true><<<grid, TX * TY, bytes, s>>>(*mu, *mp, c, U0, Uout, Pout, Res, dyn, stage, zc,
+      k_stage_tm<R, MX, MY, true><<<grid, MX * MY, bytes, s>>>(*mu, *mp, c, U0, Uout, Pout, Res, dyn, stage, zc,
                                                                write_pres);
     else
-      k_stage_tm<R, TX, TY, false><<<grid, TX * TY, bytes, s>>>(*mu, *mp, c, U0, Uout, Pout, Res, dyn, stage, zc,
+      k_stage_tm<R, MX, MY, false><<<grid, MX * MY, bytes, s>>>(*mu, *mp, c, U0, Uout, Pout, Res, dyn, stage, zc,
                                                                 write_pres);
     return;
   }
+  constexpr int PX = StageTile<R>::TX, PY = StageTile<R>::TY;
   const int bytes = stage_smem_bytes();
   if (resid)
-    k_stage<R, TX, TY, true><<<grid, TX * TY, bytes, s>>>(c, Uin, Pin, U0, Uout, Pout, Res, dyn, stage, zc, write_pres);
+    k_stage<R, PX, PY, true><<<grid, PX * PY, bytes, s>>>(c, Uin, Pin, U0, Uout, Pout, Res, dyn, stage, zc, write_pres);
   else
-    k_stage<R, TX, TY, false><<<grid, TX * TY, bytes, s>>>(c, Uin, Pin, U0, Uout, Pout, Res, dyn, stage, zc, write_pres);
+    k_stage<R, PX, PY, false><<<grid, PX * PY, bytes, s>>>(c, Uin, Pin, U0, Uout, Pout, Res, dyn, stage, zc, write_pres);
 }
 
 template <class R>

@@ -355,6 +355,15 @@ __global__ void __launch_bounds__(TX* TY, 2)
 
   const unsigned plane = (unsigned)g.sx * (unsigned)g.sy;
   const unsigned own0 = cidx32(g, i, j, 0);
+  // The new state's pressure of plane k is looked up at the end of plane k
+  // and stored during plane k+1, so the table loads overlap that plane's work.
+  PresLookup<R> plook;
+  bool pend = false;
+  auto finish_pressure = [&](int kp) {
+    const R pr = eos_pres_end(plook);
+    store_scalar<R, true>(g, Pout, i, j, kp, images_of(g, i, j, kp, true), pr);
+    pend = false;
+  };
   int s0 = 2;  // ring slot of plane k
   for (int k = zb; k < ze; k++, s0 = slot_add(s0, 1)) {
     if (tid == 0 && k + 1 < ze) issue(k + 3);
@@ -399,6 +408,7 @@ __global__ void __launch_bounds__(TX* TY, 2)
 #pragma unroll
       for (int q = 0; q < NV; q++) base[q] = src[id + (unsigned)q * g.N32];
     }
+    if (pend) finish_pressure(k - 1);
     tm::tmem_wait_st();
     __syncthreads();
     // z derivative (all lanes), then the cell's residual and update
@@ -478,13 +488,14 @@ __global__ void __launch_bounds__(TX* TY, 2)
         if (write_pres) {
           R v1, v2, v3, ei;
           prim_from_cons(un[0], un[1], un[2], un[3], un[4], v1, v2, v3, ei);
-          const R pr = eos_pres(c, un[0], ei, (R)1.0 / un[0]);
-          store_scalar<R, true>(g, Pout, i, j, k, im, pr);
+          eos_pres_begin(c, un[0], ei, (R)1.0 / un[0], plook);
+          pend = true;
         }
       }
     }
     __syncthreads();
   }
+  if (pend) finish_pressure(ze - 1);
 
   // teardown: report an expired wait, let issued copies land, free tensor memory
   if (timed_out) atomicExch(&misc[2], 1u);
