@@ -309,6 +309,128 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+def run_ensemble(args):
+    """Batched ensemble: 64 independent periodic FP32 boxes, sides drawn from
+    {32, 48, 64, 96, 128} per axis, each with its own seed, velocity rms
+    log-uniform in [0.2, 2] km/s and field rms log-uniform in [10, 500] G.
+    Each box is autotuned, then all advance together in one graph launch
+    (while-loop body = one step of every box).  Reported against the same
+    boxes advanced one box per launch (each box's own per-step graph, box
+    after box)."""
+    import numpy as np
+    import torch
+    from muram_main_gb300 import eos_table, gpumhd, initial
+    eos_table.ensure_table(EOS_BENCH, "bench")
+    tab = initial.EosTable(EOS_BENCH)
+    rng = np.random.default_rng(2024)
+    sides = [32, 48, 64, 96, 128]
+    nbox = args.boxes
+    boxes, states, cells = [], [], 0
+    for b in range(nbox):
+        nx, ny, nz = (int(x) for x in rng.choice(sides, 3))
+        v_rms = float(np.exp(rng.uniform(np.log(0.2e5), np.log(2.0e5))))
+        b_rms = float(np.exp(rng.uniform(np.log(10.0), np.log(500.0))))
+        U = initial.periodic_box(tab, nx, ny, nz, dx=3.2e6, v_rms=v_rms, b_rms_gauss=b_rms, seed=1000 + b)
+        p = gpumhd.default_params(nx, ny, nz, 3.2e6, precision=32)
+        g = gpumhd.MuramGPU(p, eos_path=EOS_BENCH)
+        g.upload_state(U)
+        boxes.append(g)
+        states.append(U)
+        cells += nx * ny * nz
+    steps = args.steps
+    tune = [g.autotune(trial_steps=2) for g in boxes]
+    kernels = [g.tuning() for g in boxes]
+
+    def reset():
+        for g, U in zip(boxes, states):
+            g.upload_state(U)
+        torch.cuda.synchronize()
+
+    # one box per launch: each box's own per-step graph, box after box
+    reset()
+    for g in boxes:
+        g.run_steps(1)
+    reset()
+    t0 = time.perf_counter()
+    for g in boxes:
+        g.enqueue_steps(steps)
+        g.synchronize()
+    t_single = time.perf_counter() - t0
+    # the ensemble: one launch of the while-loop graph for all boxes and steps
+    reset()
+    ens = gpumhd.MuramEnsemble(boxes)
+    ens.run_steps(args.warmup)
+    reset()
+    stream = torch.cuda.ExternalStream(ens.stream)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    n0 = ens.launch_count
+    e0.record(stream)
+    ens.enqueue_steps(steps)
+    e1.record(stream)
+    ens.synchronize()
+    ms = e0.elapsed_time(e1)
+    launches = ens.launch_count - n0
+    value = cells * steps / (ms / 1e3)
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": steps, "warmup": args.warmup,
+        "ms_per_step": ms / steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded periodic boxes, generated EOS table 3000x3000)",
+        "config": {"workload": f"ensemble of {nbox} periodic FP32 boxes, sides in {sides}", "cells": cells,
+                   "graph": "one launch: while-loop graph, body = one step of every box",
+                   "autotuned": True},
+        "one_box_per_launch": {"value": cells * steps / t_single, "unit": UNIT,
+                               "wall_s": round(t_single, 4)},
+        "ensemble_over_one_box_per_launch": value / (cells * steps / t_single),
+        "gpu_launches": launches,
+        "tuning": {"stage_kernel_tma": sum(1 for k in kernels if k["stage_kernel"] == 0),
+                   "best_ms_per_step_sum": round(sum(tune), 4)},
+    }
+    ens.close()
+    for g in boxes:
+        g.close()
+    print(json.dumps(line))
+
+
+def run_large(args):
+    """Large single box: 256 (MURaM dimension 0) x 1024 x 1024 = 2.7e8 cells in
+    FP32.  Its state is the periodic 4x4 tiling (in y and z) of a seeded
+    256^3 periodic box from the 64^3 configuration's generators, built on the
+    device, so that the host never holds the 17 GB float64 state."""
+    import torch
+    from muram_main_gb300 import eos_table, gpumhd, initial
+    eos_table.ensure_table(EOS_BENCH, "bench")
+    tab = initial.EosTable(EOS_BENCH)
+    nx, ny, nz = 256, 1024, 1024
+    seed_box = initial.periodic_box(tab, 256, 256, 256, dx=3.2e6, seed=99)
+    gs = gpumhd.MuramGPU(gpumhd.default_params(256, 256, 256, 3.2e6, precision=32), eos_path=EOS_BENCH)
+    gs.upload_state(seed_box)
+    del seed_box
+    p = gpumhd.default_params(nx, ny, nz, 3.2e6, precision=32)
+    g = gpumhd.MuramGPU(p, eos_path=EOS_BENCH)
+    g.tile_from(gs)
+    gs.close()
+    g.run_steps(1)
+    ms, launches = time_device(g, args.steps, args.warmup)
+    n_cells = nx * ny * nz
+    phases = g.profile_steps(2)
+    value = n_cells * args.steps / (ms / 1e3)
+    step_bytes = sum(words_per_cell(q) for q in ["stage1", "stage2", "stage3", "stage4", "tvd_x", "tvd_y",
+                                                 "tvd_z"]) * 4 * n_cells
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded periodic box, generated EOS table 3000x3000)",
+        "config": {"workload": "periodic 256(dim 0) x 1024 x 1024 FP32, 4x4 tiling of a seeded 256^3 box",
+                   "cells": n_cells, "l2": "inputs larger than L2 (state 8.8 GB per buffer)"},
+        "step_hbm_gbs": round(step_bytes / (ms / args.steps / 1e3) / 1e9, 1),
+        "phases_ms": {k: round(v, 4) for k, v in phases.items()},
+        "gpu_launches": launches,
+    }
+    g.close()
+    print(json.dumps(line))
+
+
 def run_reference(args):
     ws, rank, _ = world()
     if rank != 0:
@@ -342,11 +464,19 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 leg")
+    ap.add_argument("--workload", default="stratified", choices=["stratified", "ensemble", "large"],
+                    help="stratified: the headline box; ensemble: 64 uneven boxes in one launch; "
+                         "large: one 1024x1024x256 box")
+    ap.add_argument("--boxes", type=int, default=64, help="boxes of the ensemble workload")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "ensemble":
+        run_ensemble(args)
+    elif args.workload == "large":
+        run_large(args)
     else:
         run_ours(args)
 

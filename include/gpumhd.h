@@ -153,6 +153,43 @@ void* gpumhd_stream(gpumhd_ctx* ctx);
 /* Number of kernel launches the context has enqueued so far. */
 long long gpumhd_launch_count(gpumhd_ctx* ctx);
 
+/* Benchmark / test set-up, no counterpart in the reference: the state of ctx
+ * becomes the periodic tiling of src's state (same precision; ctx's interior
+ * sizes multiples of src's), ghosts filled by ctx's boundary rule. */
+int gpumhd_tile_from(gpumhd_ctx* ctx, gpumhd_ctx* src);
+
+/* ---- launch shapes (no counterpart in the reference: GPU tiling only) ----
+ * stage_zchunk: z planes per stage-kernel block (0: chosen from the GPU's
+ * occupancy); tvd_chunk: cells per thread of the y / z TVD sweeps (0: 32).
+ * Results do not depend on them. */
+int gpumhd_set_tuning(gpumhd_ctx* ctx, int stage_zchunk, int tvd_chunk);
+/* stage_kernel: 0 when the TMA / tensor-memory stage kernel runs, 1 for the
+ * plain-load kernel. */
+int gpumhd_get_tuning(gpumhd_ctx* ctx, int* stage_kernel, int* stage_zchunk, int* tvd_chunk);
+/* Autotuner: times the candidate stage kernels, z chunks and TVD chunks on
+ * the context's own state (trial_steps timed steps each; the state, its
+ * pressure and the step scalars are restored afterwards) and keeps the
+ * fastest; *best_ms receives its time per step. */
+int gpumhd_autotune(gpumhd_ctx* ctx, int trial_steps, double* best_ms);
+
+/* ---- ensembles of independent boxes (no counterpart in the reference) ----
+ * An ensemble advances several contexts (boxes of any sizes and precisions on
+ * one device) together: one CUDA graph whose while-loop body is one fused step
+ * of every box, the boxes running as parallel branches, so that a single graph
+ * launch runs all requested steps.  The boxes must have their EOS and state
+ * loaded; the ensemble does not own them (destroy it before them). */
+typedef struct gpumhd_ensemble gpumhd_ensemble;
+int gpumhd_ensemble_create(gpumhd_ctx* const* boxes, int n, gpumhd_ensemble** out);
+int gpumhd_ensemble_destroy(gpumhd_ensemble* e);
+/* nsteps steps of every box in one graph launch; ordered after the work
+ * already queued on the boxes' streams, and later calls on a box wait for it. */
+int gpumhd_ensemble_enqueue_steps(gpumhd_ensemble* e, int nsteps);
+/* Waits for the ensemble and returns the first box error (as gpumhd_synchronize). */
+int gpumhd_ensemble_synchronize(gpumhd_ensemble* e);
+const char* gpumhd_ensemble_last_error(gpumhd_ensemble* e);
+void* gpumhd_ensemble_stream(gpumhd_ensemble* e);
+long long gpumhd_ensemble_launch_count(gpumhd_ensemble* e);
+
 #ifdef __cplusplus
 }
 #endif

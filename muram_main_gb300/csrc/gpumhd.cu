@@ -54,6 +54,8 @@ struct gpumhd_ctx {
   bool tma = false;
   CUtensorMap mapS[3];
   CUtensorMap mapP[2];
+  // launch shapes of the fused step (0: defaults); set by gpumhd_set_tuning / gpumhd_autotune
+  int tune_zc = 0, tune_td = 0;
   char err[1024] = {0};
 };
 
@@ -568,6 +570,27 @@ extern "C" int gpumhd_upload(gpumhd_ctx* ctx, int which, const double* host) {
   return check_launch(ctx, 1);
 }
 
+// dst's state (U) = periodic tiling of src's state; same precision, and dst's
+// interior sizes multiples of src's.  Ghosts filled with dst's boundary rule.
+extern "C" int gpumhd_tile_from(gpumhd_ctx* ctx, gpumhd_ctx* src) {
+  if (!ctx || !src || ctx->device != src->device) return GPUMHD_E_INVALID;
+  const Geom& gd = ctx->c.g;
+  const Geom& gs = src->c.g;
+  if (ctx->f32 != src->f32 || gd.nx % gs.nx || gd.ny % gs.ny || gd.nz % gs.nz)
+    return fail(ctx, GPUMHD_E_INVALID, "tile_from: precision differs or sizes are not multiples");
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaStreamSynchronize(src->stream));
+  if (ctx->f32) {
+    Launch<float>::tile_state(gd, gs, (const float*)src->S[src->iU], (float*)ctx->S[ctx->iU], ctx->stream);
+    Launch<float>::fill_ghosts(ctx->c, (float*)ctx->S[ctx->iU], 8, 1, ctx->stream);
+  } else {
+    Launch<double>::tile_state(gd, gs, (const double*)src->S[src->iU], (double*)ctx->S[ctx->iU], ctx->stream);
+    Launch<double>::fill_ghosts(ctx->c, (double*)ctx->S[ctx->iU], 8, 1, ctx->stream);
+  }
+  ctx->fused_ready = false;
+  return check_launch(ctx, 2);
+}
+
 extern "C" int gpumhd_download(gpumhd_ctx* ctx, int which, double* host) {
   if (!ctx || !host) return GPUMHD_E_INVALID;
   CK(cudaSetDevice(ctx->device));
@@ -782,49 +805,57 @@ static int enqueue_one_step(gpumhd_ctx* ctx, cudaEvent_t* ev = nullptr) {
     float* const* S = (float* const*)ctx->S;
     float* const* P = (float* const*)ctx->P;
     mark();
-    L::stage(c, S[a], P[pa], S[a], S[b], P[pb], nullptr, ctx->dyn, 1, false, 1, s, map_u(ctx, a), map_p(ctx, pa));
+    L::stage(c, S[a], P[pa], S[a], S[b], P[pb], nullptr, ctx->dyn, 1, false, 1, s,
+              map_u(ctx, a), map_p(ctx, pa), ctx->tune_zc);
     mark();
-    L::stage(c, S[b], P[pb], S[a], S[d], P[pa], nullptr, ctx->dyn, 2, false, 1, s, map_u(ctx, b), map_p(ctx, pb));
+    L::stage(c, S[b], P[pb], S[a], S[d], P[pa], nullptr, ctx->dyn, 2, false, 1, s,
+              map_u(ctx, b), map_p(ctx, pb), ctx->tune_zc);
     mark();
-    L::stage(c, S[d], P[pa], S[a], S[b], P[pb], nullptr, ctx->dyn, 3, false, 1, s, map_u(ctx, d), map_p(ctx, pa));
+    L::stage(c, S[d], P[pa], S[a], S[b], P[pb], nullptr, ctx->dyn, 3, false, 1, s,
+              map_u(ctx, d), map_p(ctx, pa), ctx->tune_zc);
     mark();
-    L::stage(c, S[b], P[pb], S[a], S[a], nullptr, nullptr, ctx->dyn, 4, false, 0, s, map_u(ctx, b), map_p(ctx, pb));
+    L::stage(c, S[b], P[pb], S[a], S[a], nullptr, nullptr, ctx->dyn, 4, false, 0, s,
+              map_u(ctx, b), map_p(ctx, pb), ctx->tune_zc);
     mark();
-    L::tvd(c, 0, 0, 0, S[a], P[pb], S[d], nullptr, ctx->dyn, s);
+    L::tvd(c, 0, 0, 0, S[a], P[pb], S[d], nullptr, ctx->dyn, s, ctx->tune_td);
     mark();
-    L::tvd(c, 1, 0, 0, S[d], P[pb], S[b], nullptr, ctx->dyn, s);
+    L::tvd(c, 1, 0, 0, S[d], P[pb], S[b], nullptr, ctx->dyn, s, ctx->tune_td);
     mark();
-    L::tvd(c, 2, 1, 0, S[b], P[pb], S[a], P[pa], ctx->dyn, s);
+    L::tvd(c, 2, 1, 0, S[b], P[pb], S[a], P[pa], ctx->dyn, s, ctx->tune_td);
     mark();
-    L::tvd(c, 0, 0, 1, S[a], P[pb], S[d], nullptr, ctx->dyn, s);
+    L::tvd(c, 0, 0, 1, S[a], P[pb], S[d], nullptr, ctx->dyn, s, ctx->tune_td);
     mark();
-    L::tvd(c, 1, 0, 1, S[d], P[pb], S[b], nullptr, ctx->dyn, s);
+    L::tvd(c, 1, 0, 1, S[d], P[pb], S[b], nullptr, ctx->dyn, s, ctx->tune_td);
     mark();
-    L::tvd(c, 2, 2, 1, S[b], P[pb], S[a], P[pa], ctx->dyn, s);
+    L::tvd(c, 2, 2, 1, S[b], P[pb], S[a], P[pa], ctx->dyn, s, ctx->tune_td);
   } else {
     using L = Launch<double>;
     double* const* S = (double* const*)ctx->S;
     double* const* P = (double* const*)ctx->P;
     mark();
-    L::stage(c, S[a], P[pa], S[a], S[b], P[pb], nullptr, ctx->dyn, 1, false, 1, s, map_u(ctx, a), map_p(ctx, pa));
+    L::stage(c, S[a], P[pa], S[a], S[b], P[pb], nullptr, ctx->dyn, 1, false, 1, s,
+              map_u(ctx, a), map_p(ctx, pa), ctx->tune_zc);
     mark();
-    L::stage(c, S[b], P[pb], S[a], S[d], P[pa], nullptr, ctx->dyn, 2, false, 1, s, map_u(ctx, b), map_p(ctx, pb));
+    L::stage(c, S[b], P[pb], S[a], S[d], P[pa], nullptr, ctx->dyn, 2, false, 1, s,
+              map_u(ctx, b), map_p(ctx, pb), ctx->tune_zc);
     mark();
-    L::stage(c, S[d], P[pa], S[a], S[b], P[pb], nullptr, ctx->dyn, 3, false, 1, s, map_u(ctx, d), map_p(ctx, pa));
+    L::stage(c, S[d], P[pa], S[a], S[b], P[pb], nullptr, ctx->dyn, 3, false, 1, s,
+              map_u(ctx, d), map_p(ctx, pa), ctx->tune_zc);
     mark();
-    L::stage(c, S[b], P[pb], S[a], S[a], nullptr, nullptr, ctx->dyn, 4, false, 0, s, map_u(ctx, b), map_p(ctx, pb));
+    L::stage(c, S[b], P[pb], S[a], S[a], nullptr, nullptr, ctx->dyn, 4, false, 0, s,
+              map_u(ctx, b), map_p(ctx, pb), ctx->tune_zc);
     mark();
-    L::tvd(c, 0, 0, 0, S[a], P[pb], S[d], nullptr, ctx->dyn, s);
+    L::tvd(c, 0, 0, 0, S[a], P[pb], S[d], nullptr, ctx->dyn, s, ctx->tune_td);
     mark();
-    L::tvd(c, 1, 0, 0, S[d], P[pb], S[b], nullptr, ctx->dyn, s);
+    L::tvd(c, 1, 0, 0, S[d], P[pb], S[b], nullptr, ctx->dyn, s, ctx->tune_td);
     mark();
-    L::tvd(c, 2, 1, 0, S[b], P[pb], S[a], P[pa], ctx->dyn, s);
+    L::tvd(c, 2, 1, 0, S[b], P[pb], S[a], P[pa], ctx->dyn, s, ctx->tune_td);
     mark();
-    L::tvd(c, 0, 0, 1, S[a], P[pb], S[d], nullptr, ctx->dyn, s);
+    L::tvd(c, 0, 0, 1, S[a], P[pb], S[d], nullptr, ctx->dyn, s, ctx->tune_td);
     mark();
-    L::tvd(c, 1, 0, 1, S[d], P[pb], S[b], nullptr, ctx->dyn, s);
+    L::tvd(c, 1, 0, 1, S[d], P[pb], S[b], nullptr, ctx->dyn, s, ctx->tune_td);
     mark();
-    L::tvd(c, 2, 2, 1, S[b], P[pb], S[a], P[pa], ctx->dyn, s);
+    L::tvd(c, 2, 2, 1, S[b], P[pb], S[a], P[pa], ctx->dyn, s, ctx->tune_td);
   }
     mark();
   return check_launch(ctx, 11);
@@ -979,3 +1010,274 @@ extern "C" int gpumhd_step_info(gpumhd_ctx* ctx, double* dt, double* cfl, double
 
 extern "C" void* gpumhd_stream(gpumhd_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
 extern "C" long long gpumhd_launch_count(gpumhd_ctx* ctx) { return ctx ? ctx->launches : 0; }
+
+// ------------------------------------------------------------- launch shapes
+extern "C" int gpumhd_set_tuning(gpumhd_ctx* ctx, int stage_zchunk, int tvd_chunk) {
+  if (!ctx || stage_zchunk < 0 || tvd_chunk < 0 || tvd_chunk > 1024) return GPUMHD_E_INVALID;
+  ctx->tune_zc = stage_zchunk;
+  ctx->tune_td = tvd_chunk;
+  if (ctx->graph) { cudaGraphExecDestroy(ctx->graph); ctx->graph = nullptr; }
+  return GPUMHD_OK;
+}
+
+extern "C" int gpumhd_get_tuning(gpumhd_ctx* ctx, int* stage_kernel, int* stage_zchunk, int* tvd_chunk) {
+  if (!ctx) return GPUMHD_E_INVALID;
+  if (stage_kernel) *stage_kernel = (ctx->tma && ctx->p.stage_kernel == 0) ? 0 : 1;
+  if (stage_zchunk) *stage_zchunk = ctx->tune_zc;
+  if (tvd_chunk) *tvd_chunk = ctx->tune_td;
+  return GPUMHD_OK;
+}
+
+// Mean time of `steps` fused steps (after one untimed step), CUDA events on the
+// context's stream.
+static int time_steps(gpumhd_ctx* ctx, int steps, double* ms) {
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  int rc = enqueue_one_step(ctx);
+  cudaEventRecord(e0, ctx->stream);
+  for (int s = 0; s < steps && rc == 0; s++) rc = enqueue_one_step(ctx);
+  cudaEventRecord(e1, ctx->stream);
+  float t = 0.f;
+  if (rc == 0) {
+    if (cudaEventSynchronize(e1) != cudaSuccess) rc = fail(ctx, GPUMHD_E_CUDA, "autotune: event sync failed");
+    else cudaEventElapsedTime(&t, e0, e1);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  *ms = (double)t / (steps > 0 ? steps : 1);
+  return rc;
+}
+
+// Times candidate launch shapes -- stage kernel (TMA / plain loads), z planes
+// per stage block, cells per thread of the y / z TVD sweeps -- on the
+// context's own state, and keeps the fastest.  The state, its pressure and the
+// step-control block are restored afterwards, so the run is unchanged.
+extern "C" int gpumhd_autotune(gpumhd_ctx* ctx, int trial_steps, double* best_ms) {
+  if (!ctx || trial_steps < 1) return GPUMHD_E_INVALID;
+  CK(cudaSetDevice(ctx->device));
+  int rc = fused_prepare(ctx, trial_steps + 1);
+  if (rc) return rc;
+  const long long N = ctx->c.g.N;
+  void* saveP = nullptr;
+  if (!ctx->T) CK(cudaMalloc(&ctx->T, 8 * N * ctx->rsz));
+  CK(cudaMalloc(&saveP, N * ctx->rsz));
+  CK(cudaMemcpyAsync(ctx->T, ctx->S[ctx->iU], 8 * N * ctx->rsz, cudaMemcpyDeviceToDevice, ctx->stream));
+  CK(cudaMemcpyAsync(saveP, ctx->P[ctx->iP], N * ctx->rsz, cudaMemcpyDeviceToDevice, ctx->stream));
+  rc = pull_dyn(ctx);
+  const Dyn saved = ctx->hdyn;
+  auto restore = [&]() {
+    cudaMemcpyAsync(ctx->S[ctx->iU], ctx->T, 8 * N * ctx->rsz, cudaMemcpyDeviceToDevice, ctx->stream);
+    cudaMemcpyAsync(ctx->P[ctx->iP], saveP, N * ctx->rsz, cudaMemcpyDeviceToDevice, ctx->stream);
+    ctx->hdyn = saved;
+    return push_dyn(ctx);
+  };
+  const int nz = ctx->c.g.nz;
+  std::vector<int> zcs = {0, nz};
+  for (int f = 2; f <= 16; f *= 2)
+    if ((nz + f - 1) / f >= 4) zcs.push_back((nz + f - 1) / f);
+  std::vector<int> kernels = {1};
+  if (ctx->tma) kernels.insert(kernels.begin(), 0);
+  const int keep_kernel = ctx->p.stage_kernel, keep_td = ctx->tune_td;
+  double best = 1e300;
+  int bk = keep_kernel, bz = 0, btd = keep_td;
+  for (int kern : kernels) {
+    for (int zc : zcs) {
+      if (rc) break;
+      ctx->p.stage_kernel = kern;
+      ctx->tune_zc = zc;
+      double ms = 0.0;
+      rc = restore();
+      if (!rc) rc = time_steps(ctx, trial_steps, &ms);
+      if (!rc && ms < best) { best = ms; bk = kern; bz = zc; }
+    }
+  }
+  ctx->p.stage_kernel = bk;
+  ctx->tune_zc = bz;
+  const int tds[] = {32, 16, 64};
+  for (int td : tds) {
+    if (rc) break;
+    ctx->tune_td = td;
+    double ms = 0.0;
+    rc = restore();
+    if (!rc) rc = time_steps(ctx, trial_steps, &ms);
+    if (!rc && ms < best) { best = ms; btd = td; }
+  }
+  ctx->tune_td = btd;
+  if (!rc) rc = restore();
+  cudaStreamSynchronize(ctx->stream);
+  cudaFree(saveP);
+  if (ctx->graph) { cudaGraphExecDestroy(ctx->graph); ctx->graph = nullptr; }
+  if (rc) return rc;
+  if (best_ms) *best_ms = best;
+  return gpumhd_synchronize(ctx);
+}
+
+// ------------------------------------------------------------------ ensemble
+// Independent boxes (contexts of any sizes on one device) advanced together:
+// one CUDA graph whose while-node body is one step of every box, the boxes as
+// parallel branches, so that a single graph launch runs all requested steps.
+struct gpumhd_ensemble {
+  std::vector<gpumhd_ctx*> box;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t fork = nullptr, done = nullptr;
+  std::vector<cudaEvent_t> join;
+  int* d_counter = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  long long launches = 0;
+  char err[1024] = {0};
+};
+
+static int efail(gpumhd_ensemble* e, int code, const char* msg) {
+  if (e) snprintf(e->err, sizeof e->err, "%s", msg);
+  snprintf(g_create_err, sizeof g_create_err, "%s", msg);
+  return code;
+}
+
+#define ECK(call)                                                  \
+  do {                                                             \
+    cudaError_t e_ = (call);                                       \
+    if (e_ != cudaSuccess) return efail(e, GPUMHD_E_CUDA, cudaGetErrorString(e_)); \
+  } while (0)
+
+static void ensemble_free(gpumhd_ensemble* e) {
+  if (!e) return;
+  if (e->exec) cudaGraphExecDestroy(e->exec);
+  for (cudaEvent_t ev : e->join) cudaEventDestroy(ev);
+  if (e->fork) cudaEventDestroy(e->fork);
+  if (e->done) cudaEventDestroy(e->done);
+  if (e->d_counter) cudaFree(e->d_counter);
+  if (e->stream) cudaStreamDestroy(e->stream);
+  delete e;
+}
+
+static int ensemble_build(gpumhd_ensemble* e) {
+  cudaGraph_t g = nullptr;
+  if (cudaGraphCreate(&g, 0) != cudaSuccess) return efail(e, GPUMHD_E_CUDA, "cudaGraphCreate failed");
+  cudaGraphConditionalHandle h;
+  if (cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault) != cudaSuccess) {
+    cudaGraphDestroy(g);
+    return efail(e, GPUMHD_E_CUDA, "cudaGraphConditionalHandleCreate failed");
+  }
+  cudaGraphNodeParams np = {};
+  np.type = cudaGraphNodeTypeConditional;
+  np.conditional.handle = h;
+  np.conditional.type = cudaGraphCondTypeWhile;
+  np.conditional.size = 1;
+  cudaGraphNode_t node;
+  if (cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np) != cudaSuccess) {
+    cudaGraphDestroy(g);
+    return efail(e, GPUMHD_E_CUDA, "adding the while node failed");
+  }
+  cudaGraph_t body = np.conditional.phGraph_out[0];
+  int rc = GPUMHD_OK;
+  if (cudaStreamBeginCaptureToGraph(e->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) !=
+      cudaSuccess) {
+    cudaGraphDestroy(g);
+    return efail(e, GPUMHD_E_CUDA, "capture into the loop body failed");
+  }
+  cudaEventRecord(e->fork, e->stream);
+  for (size_t b = 0; b < e->box.size() && rc == 0; b++) {
+    gpumhd_ctx* x = e->box[b];
+    cudaStreamWaitEvent(x->stream, e->fork, 0);
+    rc = enqueue_one_step(x);
+    x->launches -= 11;  // recorded into the graph, not launched
+    cudaEventRecord(e->join[b], x->stream);
+    cudaStreamWaitEvent(e->stream, e->join[b], 0);
+  }
+  k_loop_tick<<<1, 32, 0, e->stream>>>(e->d_counter, h);
+  cudaGraph_t out = nullptr;
+  const cudaError_t ce = cudaStreamEndCapture(e->stream, &out);
+  if (rc == 0 && ce != cudaSuccess) rc = efail(e, GPUMHD_E_CUDA, cudaGetErrorString(ce));
+  if (rc == 0 && cudaGraphInstantiate(&e->exec, g, 0) != cudaSuccess) {
+    e->exec = nullptr;
+    rc = efail(e, GPUMHD_E_CUDA, "instantiating the ensemble graph failed");
+  }
+  cudaGraphDestroy(g);
+  return rc;
+}
+
+extern "C" int gpumhd_ensemble_create(gpumhd_ctx* const* boxes, int n, gpumhd_ensemble** out) {
+  if (!boxes || n < 1 || !out) return efail(nullptr, GPUMHD_E_INVALID, "ensemble: no boxes");
+  *out = nullptr;
+  gpumhd_ensemble* e = new gpumhd_ensemble();
+  e->device = boxes[0] ? boxes[0]->device : 0;
+  for (int b = 0; b < n; b++) {
+    gpumhd_ctx* x = boxes[b];
+    if (!x || x->device != e->device) { ensemble_free(e); return efail(nullptr, GPUMHD_E_INVALID, "ensemble: null box or boxes on different devices"); }
+    for (int a = 0; a < b; a++)
+      if (boxes[a] == x) { ensemble_free(e); return efail(nullptr, GPUMHD_E_INVALID, "ensemble: a box appears twice"); }
+    e->box.push_back(x);
+  }
+  int rc = GPUMHD_OK;
+  if (cudaSetDevice(e->device) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&e->fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&e->done, cudaEventDisableTiming) != cudaSuccess ||
+      cudaMalloc(&e->d_counter, sizeof(int)) != cudaSuccess)
+    rc = efail(e, GPUMHD_E_CUDA, "ensemble: stream/event/counter setup failed");
+  for (int b = 0; b < n && rc == 0; b++) {
+    cudaEvent_t ev;
+    if (cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) != cudaSuccess) { rc = efail(e, GPUMHD_E_CUDA, "ensemble: event"); break; }
+    e->join.push_back(ev);
+    rc = fused_prepare(e->box[b], 1024);
+    if (rc) efail(e, rc, e->box[b]->err);
+  }
+  for (int b = 0; b < n && rc == 0; b++)
+    if (cudaStreamSynchronize(e->box[b]->stream) != cudaSuccess) rc = efail(e, GPUMHD_E_CUDA, "ensemble: box stream");
+  if (rc == 0) rc = ensemble_build(e);
+  if (rc) { ensemble_free(e); return rc; }
+  *out = e;
+  return GPUMHD_OK;
+}
+
+extern "C" int gpumhd_ensemble_destroy(gpumhd_ensemble* e) {
+  if (!e) return GPUMHD_E_INVALID;
+  cudaSetDevice(e->device);
+  if (e->stream) cudaStreamSynchronize(e->stream);
+  ensemble_free(e);
+  return GPUMHD_OK;
+}
+
+// nsteps steps of every box in one graph launch (stream-ordered after work
+// already queued on the boxes' own streams; later calls on a box wait for it).
+extern "C" int gpumhd_ensemble_enqueue_steps(gpumhd_ensemble* e, int nsteps) {
+  if (!e || nsteps < 0) return GPUMHD_E_INVALID;
+  if (nsteps == 0) return GPUMHD_OK;
+  ECK(cudaSetDevice(e->device));
+  for (size_t b = 0; b < e->box.size(); b++) {
+    ECK(cudaEventRecord(e->join[b], e->box[b]->stream));
+    ECK(cudaStreamWaitEvent(e->stream, e->join[b], 0));
+  }
+  k_set_counter<<<1, 32, 0, e->stream>>>(e->d_counter, nsteps);
+  ECK(cudaGraphLaunch(e->exec, e->stream));
+  for (gpumhd_ctx* x : e->box) {
+    ECK(cudaMemsetAsync(x->S[x->iRes], 0, 8 * x->c.g.N * x->rsz, e->stream));
+    x->have_pres = true;
+    x->launches += 11LL * nsteps;
+  }
+  e->launches += (11LL * (long long)e->box.size() + 1) * nsteps + 1;
+  ECK(cudaEventRecord(e->done, e->stream));
+  for (gpumhd_ctx* x : e->box) ECK(cudaStreamWaitEvent(x->stream, e->done, 0));
+  return GPUMHD_OK;
+}
+
+extern "C" int gpumhd_ensemble_synchronize(gpumhd_ensemble* e) {
+  if (!e) return GPUMHD_E_INVALID;
+  ECK(cudaSetDevice(e->device));
+  if (cudaStreamSynchronize(e->stream) != cudaSuccess) return efail(e, GPUMHD_E_CUDA, "ensemble stream failed");
+  for (size_t b = 0; b < e->box.size(); b++) {
+    const int rc = gpumhd_synchronize(e->box[b]);
+    if (rc) {
+      char msg[1024];
+      snprintf(msg, sizeof msg, "box %zu: %.900s", b, e->box[b]->err);
+      return efail(e, rc, msg);
+    }
+  }
+  return GPUMHD_OK;
+}
+
+extern "C" const char* gpumhd_ensemble_last_error(gpumhd_ensemble* e) { return e ? e->err : g_create_err; }
+extern "C" void* gpumhd_ensemble_stream(gpumhd_ensemble* e) { return e ? (void*)e->stream : nullptr; }
+extern "C" long long gpumhd_ensemble_launch_count(gpumhd_ensemble* e) { return e ? e->launches : 0; }

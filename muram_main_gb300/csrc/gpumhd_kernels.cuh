@@ -1142,6 +1142,23 @@ __global__ void k_tcheck(Consts c, R* __restrict__ U, const Dyn* __restrict__ dy
 // (periodic wrap; for closed x with with_bc, mirror with M_x, B_y, B_z flipped).
 // Without with_bc a closed x leaves the x ghosts and the y/z ghosts outside the
 // interior x range untouched, like exchange_grid_acc without the boundary call.
+// Interior of a box filled by periodic tiling of a smaller box's interior
+// (benchmark and test set-up): cell (i, j, k) takes the source cell
+// (i mod nx_s, j mod ny_s, k mod nz_s).  Ghosts are filled afterwards.
+template <class R>
+__global__ void k_tile_state(Geom gd, Geom gs, const R* __restrict__ Us, R* __restrict__ Ud) {
+  const long long n = (long long)gd.nx * gd.ny * gd.nz;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(t % gd.nx);
+    const long long r = t / gd.nx;
+    const int j = (int)(r % gd.ny), k = (int)(r / gd.ny);
+    const long long d = cidx(gd, GH + i, GH + j, GH + k);
+    const long long sidx = cidx(gs, GH + i % gs.nx, GH + j % gs.ny, GH + k % gs.nz);
+#pragma unroll
+    for (int q = 0; q < NV; q++) Ud[(long long)q * gd.N + d] = Us[(long long)q * gs.N + sidx];
+  }
+}
+
 template <class R>
 __global__ void k_fill_ghosts(Geom g, R* __restrict__ U, int nfield, int with_bc) {
   for (long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x; id < g.N; id += (long long)gridDim.x * blockDim.x) {

@@ -9,6 +9,10 @@ namespace gpumhd {
 // Sync_timestep (src/solver.C:487-548) on the CFL speed accumulated by the
 // previous pass, the TVD branch (src/solver.C:325-339) and Run.Advance.
 __global__ void k_step_begin(Consts c, Dyn* dyn, double* dt_hist, int dt_hist_cap);
+// Step counter of a graph's while loop: k_set_counter before the launch,
+// k_loop_tick at the end of each pass (sets the loop condition).
+__global__ void k_loop_tick(int* counter, cudaGraphConditionalHandle h);
+__global__ void k_set_counter(int* counter, int n);
 
 template <class R>
 struct Launch {
@@ -17,11 +21,13 @@ struct Launch {
   static int stage_smem_bytes();
   static cudaError_t setup();
   // mu / mp: tensor maps of Uin / Pin for the TMA kernel (both null: k_stage)
+  // zc: z planes per block (0: chosen from the occupancy, see stage())
   static void stage(const Consts& c, const R* Uin, const R* Pin, const R* U0, R* Uout, R* Pout, R* Res, Dyn* dyn,
                     int stage, bool resid, int write_pres, cudaStream_t s, const CUtensorMap* mu = nullptr,
-                    const CUtensorMap* mp = nullptr);
+                    const CUtensorMap* mp = nullptr, int zc = 0);
+  // td: cells per thread along the y / z sweeps (0: 32)
   static void tvd(const Consts& c, int dir, int mode, int only_two_half, const R* Uin, const R* Pst, R* Uout, R* Pout,
-                  Dyn* dyn, cudaStream_t s);
+                  Dyn* dyn, cudaStream_t s, int td = 0);
   static void cons_to_prim(const Consts& c, R* U, R* P, R* T, R* Ne, R* Ri, R* Am, cudaStream_t s);
   static void init_pass(const Consts& c, const R* U, R* P, Dyn* dyn, cudaStream_t s);
   static void adjust_stats(const Consts& c, const R* U, const R* P, Dyn* dyn, cudaStream_t s);
@@ -30,6 +36,7 @@ struct Launch {
   static void save_cons(const Consts& c, const R* U, R* U0, cudaStream_t s);
   static void tcheck(const Consts& c, R* U, const Dyn* dyn, cudaStream_t s);
   static void fill_ghosts(const Consts& c, R* U, int nfield, int with_bc, cudaStream_t s);
+  static void tile_state(const Geom& gd, const Geom& gs, const R* Us, R* Ud, cudaStream_t s);
   static void aos_to_soa(long long N, int nf, const double* A, R* S, cudaStream_t s);
   static void soa_to_aos(long long N, int nf, const R* S, double* A, cudaStream_t s);
 };
@@ -90,7 +97,7 @@ cudaError_t Launch<R>::setup() {
 template <class R>
 void Launch<R>::stage(const Consts& c, const R* Uin, const R* Pin, const R* U0, R* Uout, R* Pout, R* Res, Dyn* dyn,
                       int stage, bool resid, int write_pres, cudaStream_t s, const CUtensorMap* mu,
-                      const CUtensorMap* mp) {
+                      const CUtensorMap* mp, int zc_force) {
   const bool tma = mu && mp;
   const int TX = tma ? StageTileTm<R>::TX : StageTile<R>::TX, TY = tma ? StageTileTm<R>::TY : StageTile<R>::TY;
   const Geom& g = c.g;
@@ -111,6 +118,7 @@ void Launch<R>::stage(const Consts& c, const R* Uin, const R* Pin, const R* U0, 
     const double eff = ((double)blocks / (double)(waves * res)) / (1.0 + 4.0 / zcc);
     if (eff > best + 1e-9) { best = eff; zc = zcc; }
   }
+  if (zc_force > 0) zc = zc_force < g.nz ? zc_force : g.nz;
   const int bz = (g.nz + zc - 1) / zc;
   dim3 grid(bx, by, bz);
   if (tma) {
@@ -134,13 +142,13 @@ void Launch<R>::stage(const Consts& c, const R* Uin, const R* Pin, const R* U0, 
 
 template <class R>
 void Launch<R>::tvd(const Consts& c, int dir, int mode, int only_two_half, const R* Uin, const R* Pst, R* Uout,
-                    R* Pout, Dyn* dyn, cudaStream_t s) {
+                    R* Pout, Dyn* dyn, cudaStream_t s, int td) {
   const Geom& g = c.g;
   TvdArgs ta;
   ta.dir = dir;
   ta.mode = mode;
   ta.only_two_half = only_two_half;
-  ta.td = 32;
+  ta.td = td > 0 ? td : 32;
   const long long sx = 1, sy = g.sx, sz = (long long)g.sx * g.sy;
   // pencil ranges of TVDlimit's three sweeps (src/tvdlimit_SR.C:199-205, 671-672)
   if (dir == 0) {
@@ -203,6 +211,11 @@ template <class R>
 void Launch<R>::tcheck(const Consts& c, R* U, const Dyn* dyn, cudaStream_t s) {
   k_tcheck<R><<<grid_for((long long)c.g.nx * c.g.ny * c.g.nz, 256), 256, 0, s>>>(c, U, dyn);
 }
+template <class R>
+void Launch<R>::tile_state(const Geom& gd, const Geom& gs, const R* Us, R* Ud, cudaStream_t s) {
+  k_tile_state<R><<<grid_for((long long)gd.nx * gd.ny * gd.nz, 256), 256, 0, s>>>(gd, gs, Us, Ud);
+}
+
 template <class R>
 void Launch<R>::fill_ghosts(const Consts& c, R* U, int nfield, int with_bc, cudaStream_t s) {
   k_fill_ghosts<R><<<grid_for(c.g.N, 256), 256, 0, s>>>(c.g, U, nfield, with_bc);

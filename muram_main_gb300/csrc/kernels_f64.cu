@@ -50,3 +50,19 @@ __global__ void k_step_begin(Consts c, Dyn* dyn, double* dt_hist, int dt_hist_ca
 }
 
 }  // namespace gpumhd
+
+namespace gpumhd {
+
+// Loop control of the ensemble's while-graph: one tick per step.
+__global__ void k_loop_tick(int* counter, cudaGraphConditionalHandle h) {
+  if (threadIdx.x == 0) {
+    const int left = --(*counter);
+    cudaGraphSetConditional(h, left > 0 ? 1u : 0u);
+  }
+}
+
+__global__ void k_set_counter(int* counter, int n) {
+  if (threadIdx.x == 0) *counter = n;
+}
+
+}  // namespace gpumhd

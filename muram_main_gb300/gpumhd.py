@@ -61,6 +61,9 @@ EXPORTS = [
     "gpumhd_sync_timestep", "gpumhd_source_integrate_tcheck", "gpumhd_tvdlimit", "gpumhd_tcheck",
     "gpumhd_exchange", "gpumhd_run_steps", "gpumhd_enqueue_steps", "gpumhd_synchronize", "gpumhd_step_info",
     "gpumhd_stream", "gpumhd_launch_count", "gpumhd_profile_steps", "gpumhd_cfl_dt_noalloc",
+    "gpumhd_tile_from", "gpumhd_set_tuning", "gpumhd_get_tuning", "gpumhd_autotune", "gpumhd_ensemble_create",
+    "gpumhd_ensemble_destroy", "gpumhd_ensemble_enqueue_steps", "gpumhd_ensemble_synchronize",
+    "gpumhd_ensemble_last_error", "gpumhd_ensemble_stream", "gpumhd_ensemble_launch_count",
 ]
 
 _lib = None
@@ -111,6 +114,17 @@ def load(build_if_missing=True):
         "gpumhd_cfl_dt_noalloc": (C.c_int, [vp, vp, C.c_int, C.c_int, C.c_int, dp, C.c_double, vp, vp]),
         "gpumhd_stream": (vp, [vp]),
         "gpumhd_launch_count": (C.c_longlong, [vp]),
+        "gpumhd_tile_from": (C.c_int, [vp, vp]),
+        "gpumhd_set_tuning": (C.c_int, [vp, C.c_int, C.c_int]),
+        "gpumhd_get_tuning": (C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+        "gpumhd_autotune": (C.c_int, [vp, C.c_int, dp]),
+        "gpumhd_ensemble_create": (C.c_int, [C.POINTER(vp), C.c_int, C.POINTER(vp)]),
+        "gpumhd_ensemble_destroy": (C.c_int, [vp]),
+        "gpumhd_ensemble_enqueue_steps": (C.c_int, [vp, C.c_int]),
+        "gpumhd_ensemble_synchronize": (C.c_int, [vp]),
+        "gpumhd_ensemble_last_error": (C.c_char_p, [vp]),
+        "gpumhd_ensemble_stream": (vp, [vp]),
+        "gpumhd_ensemble_launch_count": (C.c_longlong, [vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -327,6 +341,26 @@ class MuramGPU:
     def download_ptr(self, which, ptr):
         self._chk(self._L.gpumhd_download(self._h, which, C.cast(ptr, C.POINTER(C.c_double))))
 
+    def tile_from(self, src):
+        """This box's state becomes the periodic tiling of src's (set-up of large boxes)."""
+        self._chk(self._L.gpumhd_tile_from(self._h, src._h))
+
+    # -- launch shapes
+    def set_tuning(self, stage_zchunk=0, tvd_chunk=0):
+        self._chk(self._L.gpumhd_set_tuning(self._h, stage_zchunk, tvd_chunk))
+
+    def tuning(self):
+        k, z, t = C.c_int(), C.c_int(), C.c_int()
+        self._chk(self._L.gpumhd_get_tuning(self._h, C.byref(k), C.byref(z), C.byref(t)))
+        return dict(stage_kernel=k.value, stage_zchunk=z.value, tvd_chunk=t.value)
+
+    def autotune(self, trial_steps=3):
+        """Pick the fastest launch shapes for this box (state left unchanged);
+        returns the best time per step in ms."""
+        ms = C.c_double()
+        self._chk(self._L.gpumhd_autotune(self._h, trial_steps, C.byref(ms)))
+        return ms.value
+
     @property
     def stream(self):
         return self._L.gpumhd_stream(self._h)
@@ -334,3 +368,51 @@ class MuramGPU:
     @property
     def launch_count(self):
         return self._L.gpumhd_launch_count(self._h)
+
+
+class MuramEnsemble:
+    """Several MuramGPU boxes advanced together by one graph launch per call."""
+
+    def __init__(self, boxes):
+        L = load()
+        self._L = L
+        self.boxes = list(boxes)
+        arr = (C.c_void_p * len(self.boxes))(*[b._h.value for b in self.boxes])
+        h = C.c_void_p()
+        rc = L.gpumhd_ensemble_create(arr, len(self.boxes), C.byref(h))
+        if rc != OK:
+            raise GpumhdError(rc, L.gpumhd_ensemble_last_error(None).decode())
+        self._h = h
+
+    def _chk(self, rc):
+        if rc != OK:
+            raise GpumhdError(rc, self._L.gpumhd_ensemble_last_error(self._h).decode())
+
+    def enqueue_steps(self, nsteps):
+        self._chk(self._L.gpumhd_ensemble_enqueue_steps(self._h, nsteps))
+
+    def synchronize(self):
+        self._chk(self._L.gpumhd_ensemble_synchronize(self._h))
+
+    def run_steps(self, nsteps):
+        self.enqueue_steps(nsteps)
+        self.synchronize()
+
+    @property
+    def stream(self):
+        return self._L.gpumhd_ensemble_stream(self._h)
+
+    @property
+    def launch_count(self):
+        return self._L.gpumhd_ensemble_launch_count(self._h)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.gpumhd_ensemble_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

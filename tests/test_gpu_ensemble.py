@@ -1,0 +1,110 @@
+"""Ensembles of boxes in one graph launch, and the launch-shape autotuner.
+
+Both change only how work is launched, so the results must equal those of
+the boxes run one by one (bit for bit: the per-cell arithmetic is the same).
+"""
+import numpy as np
+import pytest
+
+import helpers as H
+from muram_main_gb300 import gpumhd, initial
+
+pytestmark = pytest.mark.gpu
+
+
+def _box(nx, ny, nz, precision, seed, closed=False):
+    tab = initial.EosTable(H.EOS_SMALL)
+    if closed:
+        U = initial.stratified_box(tab, nx, ny, nz, seed=seed)
+        p = gpumhd.default_params(nx, ny, nz, 1.6e6, precision=precision, periodic_x=0, grav=2.74e4)
+    else:
+        U = initial.periodic_box(tab, nx, ny, nz, seed=seed)
+        p = gpumhd.default_params(nx, ny, nz, 3.2e6, precision=precision)
+    g = gpumhd.MuramGPU(p, eos_path=H.EOS_SMALL)
+    g.upload_state(U)
+    return g
+
+
+SHAPES = [(16, 12, 8, 64, 1, False), (24, 20, 12, 64, 2, True), (32, 16, 20, 32, 3, False), (18, 14, 10, 32, 4, True)]
+
+
+def test_ensemble_equals_boxes_run_one_by_one(gpu_lib):
+    steps = 6
+    alone = []
+    for nx, ny, nz, prec, seed, closed in SHAPES:
+        g = _box(nx, ny, nz, prec, seed, closed)
+        g.run_steps(steps)
+        alone.append((g.download_state(), g.step_info()))
+        g.close()
+    boxes = [_box(*s) for s in SHAPES]
+    ens = gpumhd.MuramEnsemble(boxes)
+    ens.run_steps(steps // 2)
+    ens.run_steps(steps - steps // 2)  # a second launch continues the loop
+    assert ens.launch_count == (11 * len(boxes) + 1) * steps + 2
+    for (ref, info), g in zip(alone, boxes):
+        got = g.download_state()
+        assert np.array_equal(got, ref), np.max(np.abs(got - ref))
+        assert g.step_info()[2] == info[2]  # same simulated time
+    ens.close()
+    for g in boxes:
+        g.close()
+
+
+def test_box_calls_after_an_ensemble_launch(gpu_lib):
+    """Per-box calls queued after an ensemble launch see its result."""
+    g1 = _box(16, 12, 8, 64, 11)
+    g2 = _box(16, 12, 8, 64, 11)
+    ens = gpumhd.MuramEnsemble([g1])
+    ens.enqueue_steps(3)
+    g1.run_steps(2)           # ordered after the ensemble's steps
+    g2.run_steps(5)
+    assert np.array_equal(g1.download_state(), g2.download_state())
+    ens.close()
+    g1.close()
+    g2.close()
+
+
+@pytest.mark.parametrize("precision", [64, 32])
+def test_autotune_keeps_state_and_results(gpu_lib, precision):
+    a = _box(40, 24, 20, precision, 21, closed=True)
+    b = _box(40, 24, 20, precision, 21, closed=True)
+    U0 = a.download_state()
+    ms = a.autotune(trial_steps=2)
+    assert ms > 0
+    t = a.tuning()
+    assert t["stage_kernel"] in (0, 1) and t["stage_zchunk"] >= 0 and t["tvd_chunk"] in (16, 32, 64)
+    assert np.array_equal(a.download_state(), U0)
+    assert a.step_info()[2] == b.step_info()[2]
+    a.run_steps(5)
+    b.run_steps(5)
+    assert np.array_equal(a.download_state(), b.download_state())
+    a.close()
+    b.close()
+
+
+def test_explicit_tuning_gives_same_results(gpu_lib):
+    ref = _box(24, 20, 36, 64, 5)
+    ref.run_steps(4)
+    for zc, td in [(36, 16), (5, 64), (9, 32)]:
+        g = _box(24, 20, 36, 64, 5)
+        g.set_tuning(zc, td)
+        g.run_steps(4)
+        assert np.array_equal(g.download_state(), ref.download_state()), (zc, td)
+        g.close()
+    ref.close()
+
+
+def test_tile_from_commutes_with_the_step(gpu_lib):
+    """A periodic box tiled 2 x 3 x 2 and advanced equals the advanced small
+    box tiled the same way (the periodic step treats every copy alike)."""
+    small = _box(16, 12, 8, 64, 31)
+    big = gpumhd.MuramGPU(gpumhd.default_params(32, 36, 16, 3.2e6), eos_path=H.EOS_SMALL)
+    big.tile_from(small)
+    U0 = small.download_state()[:, 2:-2, 2:-2, 2:-2]
+    assert np.array_equal(big.download_state()[:, 2:-2, 2:-2, 2:-2], np.tile(U0, (1, 2, 3, 2)))
+    small.run_steps(4)
+    big.run_steps(4)
+    U1 = small.download_state()[:, 2:-2, 2:-2, 2:-2]
+    assert np.array_equal(big.download_state()[:, 2:-2, 2:-2, 2:-2], np.tile(U1, (1, 2, 3, 2)))
+    small.close()
+    big.close()
