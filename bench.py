@@ -269,17 +269,42 @@ def run_ours(args):
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
     g.close()
     del g
-    # FP64 mode of the same box
+    # FP64 mode of the same box: throughput over --err-steps steps from the
+    # initial state, and the per-field error of the FP32 runs (plain and
+    # compensated) against it after the same steps.  The FP64 GPU mode matches
+    # the reference CPU build to 1e-12 (tests), so it stands for the oracle here.
     fp64 = None
+    fp32_err = None
     if not args.no_fp64:
+        import numpy as np
+        nerr = args.err_steps
         g64 = context(64)
         g64.run_steps(1)
-        n64 = max(2, args.steps // 4)
-        ms64, _ = time_device(g64, n64, 3)
-        value64 = ws * n_cells * n64 / (ms64 / 1e3)
-        fp64 = {"value": value64, "unit": UNIT, "ms_per_step": ms64 / n64, "fp32_over_fp64": value / value64}
+        g64.upload_state(U)
+        ms64, _ = time_device(g64, nerr, 0)
+        value64 = ws * n_cells * nerr / (ms64 / 1e3)
+        fp64 = {"value": value64, "unit": UNIT, "ms_per_step": ms64 / nerr, "steps": nerr,
+                "fp32_over_fp64": value / value64}
+        ref = g64.download_state()[:, 2:-2, 2:-2, 2:-2]
         g64.close()
         del g64
+        fp32_err = {"steps": nerr, "against": "FP64 GPU mode (= reference CPU build to 1e-12)",
+                    "fields": ["rho", "Mx", "My", "Mz", "e", "Bx", "By", "Bz"]}
+        for comp in (0, 1):
+            p32 = gpumhd.default_params(wl["nx"], wl["ny"], wl["nz"], wl["dx"], precision=32,
+                                        periodic_x=wl["periodic_x"], grav=wl["grav"], compensated=comp)
+            g32 = gpumhd.MuramGPU(p32, device=lrank, eos_path=EOS_BENCH)
+            g32.upload_state(U)
+            g32.run_steps(nerr)
+            got = g32.download_state()[:, 2:-2, 2:-2, 2:-2]
+            g32.close()
+            d = got - ref
+            l2 = [float(np.sqrt(np.sum(d[f] ** 2) / np.sum(ref[f] ** 2))) for f in range(8)]
+            linf = [float(np.max(np.abs(d[f])) / np.max(np.abs(ref[f]))) for f in range(8)]
+            key = "compensated" if comp else "plain"
+            fp32_err[key] = {"rel_l2": [float(f"{x:.3e}") for x in l2], "rel_linf": [float(f"{x:.3e}") for x in linf],
+                             "max_rel_l2": float(f"{max(l2):.3e}")}
+        del ref
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -296,6 +321,7 @@ def run_ours(args):
         "gpu_launches": launches,
         "clocks": clocks.summary(),
         "fp64": fp64,
+        "fp32_error": fp32_err,
     }
     if rank == 0 and ws == 1 and not args.no_cpu:
         cores = min(os.cpu_count() or 1, 16)
@@ -463,7 +489,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg")
-    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 leg")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 leg (and the FP32 error report)")
+    ap.add_argument("--err-steps", type=int, default=100, help="steps of the FP64 leg and the FP32 error report")
     ap.add_argument("--workload", default="stratified", choices=["stratified", "ensemble", "large"],
                     help="stratified: the headline box; ensemble: 64 uneven boxes in one launch; "
                          "large: one 1024x1024x256 box")

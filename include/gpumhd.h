@@ -52,7 +52,9 @@ typedef struct gpumhd_params {
   /* RunData */
   double CFL, CFL_tvd, dt, time, outcad;
   int autostep;          /* RunData::autostep (dt computed from the CFL condition) */
-  int pad1;
+  int compensated;       /* FP32 only: 1 = compensated (Kahan) RK updates -- a per-cell FP32
+                            remainder carries what rounding the state dropped at each step's
+                            last stage (8 more words per cell); 0 = plain updates */
   /* PhysicsData::params */
   double grav, va_max, va_adjust, max_fill;
   /* PhysicsData TVD settings */

@@ -56,6 +56,7 @@ struct gpumhd_ctx {
   CUtensorMap mapP[2];
   // launch shapes of the fused step (0: defaults); set by gpumhd_set_tuning / gpumhd_autotune
   int tune_zc = 0, tune_td = 0;
+  void* comp = nullptr;  // FP32 compensated mode: per-cell remainders of the RK update (8N floats)
   char err[1024] = {0};
 };
 
@@ -386,6 +387,7 @@ extern "C" int gpumhd_destroy(gpumhd_ctx* ctx) {
   for (void* q : ctx->aux) cudaFree(q);
   cudaFree(ctx->T);
   cudaFree(ctx->staging);
+  cudaFree(ctx->comp);
   cudaFree(ctx->dyn);
   cudaFree(ctx->dt_hist);
   cudaFree(ctx->d_xeps);
@@ -565,7 +567,10 @@ extern "C" int gpumhd_upload(gpumhd_ctx* ctx, int which, const double* host) {
   CK(cudaMemcpyAsync(ctx->staging, host, sizeof(double) * nf * N, cudaMemcpyHostToDevice, ctx->stream));
   if (ctx->f32) Launch<float>::aos_to_soa(N, nf, ctx->staging, (float*)dst, ctx->stream);
   else Launch<double>::aos_to_soa(N, nf, ctx->staging, (double*)dst, ctx->stream);
-  if (which == 0) ctx->fused_ready = false;
+  if (which == 0) {
+    ctx->fused_ready = false;
+    if (ctx->comp) CK(cudaMemsetAsync(ctx->comp, 0, sizeof(float) * 8 * N, ctx->stream));
+  }
   if (which == 3) ctx->have_pres = true;
   return check_launch(ctx, 1);
 }
@@ -587,6 +592,7 @@ extern "C" int gpumhd_tile_from(gpumhd_ctx* ctx, gpumhd_ctx* src) {
     Launch<double>::tile_state(gd, gs, (const double*)src->S[src->iU], (double*)ctx->S[ctx->iU], ctx->stream);
     Launch<double>::fill_ghosts(ctx->c, (double*)ctx->S[ctx->iU], 8, 1, ctx->stream);
   }
+  if (ctx->comp) CK(cudaMemsetAsync(ctx->comp, 0, sizeof(float) * 8 * gd.N, ctx->stream));
   ctx->fused_ready = false;
   return check_launch(ctx, 2);
 }
@@ -802,20 +808,21 @@ static int enqueue_one_step(gpumhd_ctx* ctx, cudaEvent_t* ev = nullptr) {
   k_step_begin<<<1, 32, 0, s>>>(c, ctx->dyn, ctx->dt_hist, ctx->dt_hist_cap);
   if (ctx->f32) {
     using L = Launch<float>;
+    float* const comp = (ctx->p.compensated && ctx->comp) ? (float*)ctx->comp : nullptr;
     float* const* S = (float* const*)ctx->S;
     float* const* P = (float* const*)ctx->P;
     mark();
     L::stage(c, S[a], P[pa], S[a], S[b], P[pb], nullptr, ctx->dyn, 1, false, 1, s,
-              map_u(ctx, a), map_p(ctx, pa), ctx->tune_zc);
+              map_u(ctx, a), map_p(ctx, pa), ctx->tune_zc, comp);
     mark();
     L::stage(c, S[b], P[pb], S[a], S[d], P[pa], nullptr, ctx->dyn, 2, false, 1, s,
-              map_u(ctx, b), map_p(ctx, pb), ctx->tune_zc);
+              map_u(ctx, b), map_p(ctx, pb), ctx->tune_zc, comp);
     mark();
     L::stage(c, S[d], P[pa], S[a], S[b], P[pb], nullptr, ctx->dyn, 3, false, 1, s,
-              map_u(ctx, d), map_p(ctx, pa), ctx->tune_zc);
+              map_u(ctx, d), map_p(ctx, pa), ctx->tune_zc, comp);
     mark();
     L::stage(c, S[b], P[pb], S[a], S[a], nullptr, nullptr, ctx->dyn, 4, false, 0, s,
-              map_u(ctx, b), map_p(ctx, pb), ctx->tune_zc);
+              map_u(ctx, b), map_p(ctx, pb), ctx->tune_zc, comp);
     mark();
     L::tvd(c, 0, 0, 0, S[a], P[pb], S[d], nullptr, ctx->dyn, s, ctx->tune_td);
     mark();
@@ -872,6 +879,10 @@ static int fused_prepare(gpumhd_ctx* ctx, int nsteps) {
     int cap = nsteps < 1024 ? 1024 : nsteps;
     CK(cudaMalloc(&ctx->dt_hist, sizeof(double) * cap));
     ctx->dt_hist_cap = cap;
+  }
+  if (ctx->f32 && ctx->p.compensated && !ctx->comp) {
+    CK(cudaMalloc(&ctx->comp, sizeof(float) * 8 * ctx->c.g.N));
+    CK(cudaMemsetAsync(ctx->comp, 0, sizeof(float) * 8 * ctx->c.g.N, ctx->stream));
   }
   if (!ctx->fused_ready) {
     // exchange + boundaries before the loop (src/solver.C:80-81), then the
@@ -1078,7 +1089,8 @@ extern "C" int gpumhd_autotune(gpumhd_ctx* ctx, int trial_steps, double* best_ms
     if ((nz + f - 1) / f >= 4) zcs.push_back((nz + f - 1) / f);
   std::vector<int> kernels = {1};
   if (ctx->tma) kernels.insert(kernels.begin(), 0);
-  const int keep_kernel = ctx->p.stage_kernel, keep_td = ctx->tune_td;
+  const int keep_kernel = ctx->p.stage_kernel, keep_td = ctx->tune_td, keep_comp = ctx->p.compensated;
+  ctx->p.compensated = 0;  // trial steps leave the compensation remainders alone
   double best = 1e300;
   int bk = keep_kernel, bz = 0, btd = keep_td;
   for (int kern : kernels) {
@@ -1104,6 +1116,7 @@ extern "C" int gpumhd_autotune(gpumhd_ctx* ctx, int trial_steps, double* best_ms
     if (!rc && ms < best) { best = ms; btd = td; }
   }
   ctx->tune_td = btd;
+  ctx->p.compensated = keep_comp;
   if (!rc) rc = restore();
   cudaStreamSynchronize(ctx->stream);
   cudaFree(saveP);

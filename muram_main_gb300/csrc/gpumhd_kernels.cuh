@@ -280,6 +280,35 @@ __device__ __forceinline__ void store_cell(double* p, const double v[12]) {
   for (int a = 0; a < 6; a++) q[a] = make_double2(v[2 * a], v[2 * a + 1]);
 }
 
+// RK update of one cell, un = base + wdt * R, then Tcheck.  With Cc (FP32
+// compensated mode) Cc holds, per interior cell, what rounding the state to
+// FP32 dropped at the last stage 4: every stage adds it back
+// (un = base + (wdt * R + C)) and stage 4 stores the new remainder -- zero
+// where Tcheck changed the value.
+template <class R>
+__device__ __forceinline__ void rk_update(const Consts& c, R* __restrict__ Cc, unsigned id, int stage, R wdt,
+                                          const R* base, const R* Racc, R vmax, R emax, R* un) {
+  if (Cc == nullptr) {
+#pragma unroll
+    for (int v = 0; v < NV; v++) un[v] = base[v] + wdt * Racc[v];
+    tcheck_cell<R>(c, vmax, emax, un[0], un[1], un[2], un[3], un[4]);
+    return;
+  }
+  const unsigned N32 = c.g.N32;
+  R y[NV], t[NV];
+#pragma unroll
+  for (int v = 0; v < NV; v++) {
+    y[v] = wdt * Racc[v] + Cc[id + (unsigned)v * N32];
+    t[v] = base[v] + y[v];
+    un[v] = t[v];
+  }
+  tcheck_cell<R>(c, vmax, emax, un[0], un[1], un[2], un[3], un[4]);
+  if (stage == 4) {
+#pragma unroll
+    for (int v = 0; v < NV; v++) Cc[id + (unsigned)v * N32] = (un[v] == t[v]) ? y[v] - (t[v] - base[v]) : (R)0;
+  }
+}
+
 // Shared memory of one stage block: the x fluxes of (TX+4) x TY cells, the y
 // fluxes of TX x (TY+4) cells (12 quantities each) and each thread's ring of
 // five z-flux planes.
@@ -313,7 +342,7 @@ template <class R, int TX, int TY, bool RESID>
 __global__ void __launch_bounds__(TX* TY, 2) k_stage(Consts c, const R* __restrict__ Uin, const R* __restrict__ Pin,
                                                      const R* __restrict__ U0, R* __restrict__ Uout,
                                                      R* __restrict__ Pout, R* __restrict__ Res, Dyn* __restrict__ dyn,
-                                                     int stage, int zc, int write_pres) {
+                                                     int stage, int zc, int write_pres, R* __restrict__ Cc) {
   using S = StageSmem<TX, TY>;
   constexpr int CW = CellW<R>::W;
   constexpr int NT = TX * TY;
@@ -499,9 +528,7 @@ __global__ void __launch_bounds__(TX* TY, 2) k_stage(Consts c, const R* __restri
         Racc[3] += b2;
         Racc[4] += b3;
         R un[NV];
-#pragma unroll
-        for (int v = 0; v < NV; v++) un[v] = base[v] + wdt * Racc[v];
-        tcheck_cell<R>(c, vmax, emax, un[0], un[1], un[2], un[3], un[4]);
+        rk_update<R>(c, Cc, id, stage, wdt, base, Racc, vmax, emax, un);
         const Images im = images_of(g, i, j, k, true);
         store_state<R, true>(g, Uout, i, j, k, im, un);
         if (write_pres) {

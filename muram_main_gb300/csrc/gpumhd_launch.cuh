@@ -24,7 +24,7 @@ struct Launch {
   // zc: z planes per block (0: chosen from the occupancy, see stage())
   static void stage(const Consts& c, const R* Uin, const R* Pin, const R* U0, R* Uout, R* Pout, R* Res, Dyn* dyn,
                     int stage, bool resid, int write_pres, cudaStream_t s, const CUtensorMap* mu = nullptr,
-                    const CUtensorMap* mp = nullptr, int zc = 0);
+                    const CUtensorMap* mp = nullptr, int zc = 0, R* Cc = nullptr);
   // td: cells per thread along the y / z sweeps (0: 32)
   static void tvd(const Consts& c, int dir, int mode, int only_two_half, const R* Uin, const R* Pst, R* Uout, R* Pout,
                   Dyn* dyn, cudaStream_t s, int td = 0);
@@ -97,7 +97,7 @@ cudaError_t Launch<R>::setup() {
 template <class R>
 void Launch<R>::stage(const Consts& c, const R* Uin, const R* Pin, const R* U0, R* Uout, R* Pout, R* Res, Dyn* dyn,
                       int stage, bool resid, int write_pres, cudaStream_t s, const CUtensorMap* mu,
-                      const CUtensorMap* mp, int zc_force) {
+                      const CUtensorMap* mp, int zc_force, R* Cc) {
   const bool tma = mu && mp;
   const int TX = tma ? StageTileTm<R>::TX : StageTile<R>::TX, TY = tma ? StageTileTm<R>::TY : StageTile<R>::TY;
   const Geom& g = c.g;
@@ -126,18 +126,20 @@ void Launch<R>::stage(const Consts& c, const R* Uin, const R* Pin, const R* U0, 
     const int bytes = (int)StageTm<R, MX, MY>::BYTES;
     if (resid)
       k_stage_tm<R, MX, MY, true><<<grid, MX * MY, bytes, s>>>(*mu, *mp, c, U0, Uout, Pout, Res, dyn, stage, zc,
-                                                               write_pres);
+                                                               write_pres, nullptr);
     else
       k_stage_tm<R, MX, MY, false><<<grid, MX * MY, bytes, s>>>(*mu, *mp, c, U0, Uout, Pout, Res, dyn, stage, zc,
-                                                                write_pres);
+                                                                write_pres, Cc);
     return;
   }
   constexpr int PX = StageTile<R>::TX, PY = StageTile<R>::TY;
   const int bytes = stage_smem_bytes();
   if (resid)
-    k_stage<R, PX, PY, true><<<grid, PX * PY, bytes, s>>>(c, Uin, Pin, U0, Uout, Pout, Res, dyn, stage, zc, write_pres);
+    k_stage<R, PX, PY, true><<<grid, PX * PY, bytes, s>>>(c, Uin, Pin, U0, Uout, Pout, Res, dyn, stage, zc, write_pres,
+                                                          nullptr);
   else
-    k_stage<R, PX, PY, false><<<grid, PX * PY, bytes, s>>>(c, Uin, Pin, U0, Uout, Pout, Res, dyn, stage, zc, write_pres);
+    k_stage<R, PX, PY, false><<<grid, PX * PY, bytes, s>>>(c, Uin, Pin, U0, Uout, Pout, Res, dyn, stage, zc, write_pres,
+                                                           Cc);
 }
 
 template <class R>

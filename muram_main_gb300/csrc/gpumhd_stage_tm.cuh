@@ -243,7 +243,7 @@ template <class R, int TX, int TY, bool RESID>
 __global__ void __launch_bounds__(TX* TY, 2)
     k_stage_tm(const __grid_constant__ CUtensorMap mapU, const __grid_constant__ CUtensorMap mapP, Consts c,
                const R* __restrict__ U0, R* __restrict__ Uout, R* __restrict__ Pout, R* __restrict__ Res,
-               Dyn* __restrict__ dyn, int stage, int zc, int write_pres) {
+               Dyn* __restrict__ dyn, int stage, int zc, int write_pres, R* __restrict__ Cc) {
   using L = StageTm<R, TX, TY>;
   constexpr int CW = CellW<R>::W;
   constexpr int NT = TX * TY;
@@ -480,9 +480,7 @@ __global__ void __launch_bounds__(TX* TY, 2)
         Racc[3] += b2;
         Racc[4] += b3;
         R un[NV];
-#pragma unroll
-        for (int v = 0; v < NV; v++) un[v] = base[v] + wdt * Racc[v];
-        tcheck_cell<R>(c, vmax, emax, un[0], un[1], un[2], un[3], un[4]);
+        rk_update<R>(c, Cc, id, stage, wdt, base, Racc, vmax, emax, un);
         const Images im = images_of(g, i, j, k, true);
         store_state<R, true>(g, Uout, i, j, k, im, un);
         if (write_pres) {

@@ -44,7 +44,7 @@ class Params(C.Structure):
         ("precision", C.c_int), ("stage_kernel", C.c_int),
         ("dx", C.c_double * 3),
         ("CFL", C.c_double), ("CFL_tvd", C.c_double), ("dt", C.c_double), ("time", C.c_double),
-        ("outcad", C.c_double), ("autostep", C.c_int), ("pad1", C.c_int),
+        ("outcad", C.c_double), ("autostep", C.c_int), ("compensated", C.c_int),
         ("grav", C.c_double), ("va_max", C.c_double), ("va_adjust", C.c_double), ("max_fill", C.c_double),
         ("tvd_h", C.c_double * 4), ("tvd_cs", C.c_double * 4), ("tvd", C.c_double * 10),
         ("tvd_h_bnd", C.c_double * 2), ("tvd_visc_bnd", C.c_double * 2), ("tvd_eta_bnd", C.c_double * 2),

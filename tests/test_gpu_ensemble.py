@@ -77,7 +77,11 @@ def test_autotune_keeps_state_and_results(gpu_lib, precision):
     assert a.step_info()[2] == b.step_info()[2]
     a.run_steps(5)
     b.run_steps(5)
-    assert np.array_equal(a.download_state(), b.download_state())
+    if precision == 64:
+        assert np.array_equal(a.download_state(), b.download_state())
+    else:
+        # FP32: the two stage kernels contract different products into FMAs
+        assert np.all(H.rel_linf(a.download_state(), b.download_state()) <= 1e-5)
     a.close()
     b.close()
 

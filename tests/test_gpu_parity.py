@@ -204,3 +204,27 @@ def test_fp32_shape_without_tma_rows(gpu_lib):
     g.run_steps(20)
     e = H.rel_l2(H.interior(g.download_state()), H.interior(ref))
     assert np.all(e <= TOL32_L2), e
+
+
+def test_fp32_compensated_rk_updates(gpu_lib):
+    """FP32 with compensated (Kahan) RK updates: meets the FP32 bar after 100
+    steps, and its state differs from the plain FP32 run (the remainders are
+    carried)."""
+    tab = initial.EosTable(H.EOS_SMALL)
+    hp = dict(nx=32, ny=32, nz=32)
+    U = initial.periodic_box(tab, 32, 32, 32, seed=5)
+    ref, _ = _oracle_run(hp, U, 100)
+    errs = {}
+    states = {}
+    for comp in (0, 1):
+        g = gpumhd.MuramGPU(gpumhd.default_params(32, 32, 32, 3.2e6, precision=32, compensated=comp),
+                            eos_path=H.EOS_SMALL)
+        g.upload_state(U)
+        g.run_steps(100)
+        states[comp] = H.interior(g.download_state())
+        errs[comp] = H.rel_l2(states[comp], H.interior(ref))
+        g.close()
+    print("FP32 rel L2 per field, plain:", np.array2string(errs[0], precision=2))
+    print("FP32 rel L2 per field, compensated:", np.array2string(errs[1], precision=2))
+    assert np.all(errs[1] <= TOL32_L2), errs[1]
+    assert not np.array_equal(states[0], states[1])
