@@ -174,6 +174,20 @@ int gpumhd_get_tuning(gpumhd_ctx* ctx, int* stage_kernel, int* stage_zchunk, int
  * fastest; *best_ms receives its time per step. */
 int gpumhd_autotune(gpumhd_ctx* ctx, int trial_steps, double* best_ms);
 
+/* ---- adjoint (no counterpart in the reference) ----
+ * Gradient of an objective J(U_T) with respect to the initial state U_0, where
+ * U_0 is the context's current state and U_T the state after nsteps fused
+ * steps of fixed dt (FP64 context, periodic box, autostep = 0, dt > 0, one TVD
+ * pass per step).  dJ_dUT: dJ/dU_T in the host cState layout (8 doubles per
+ * cell, ghosts included and ignored); dJ_dU0 receives dJ/dU_0 in the same
+ * layout (ghost records zero).  The hand-written adjoint of the step (stages
+ * with MHD_Residual, sources, Boris correction and Tcheck, ConsToPrim's
+ * pressure, the three TVD sweeps) runs backwards in time; forward states are
+ * kept every checkpoint_every steps and recomputed in between.  Limiter kinks
+ * and clamps take the derivative of the branch the forward step took.  The
+ * context's state is left unchanged. */
+int gpumhd_adjoint(gpumhd_ctx* ctx, int nsteps, int checkpoint_every, const double* dJ_dUT, double* dJ_dU0);
+
 /* ---- ensembles of independent boxes (no counterpart in the reference) ----
  * An ensemble advances several contexts (boxes of any sizes and precisions on
  * one device) together: one CUDA graph whose while-loop body is one fused step

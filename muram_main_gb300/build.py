@@ -1,12 +1,14 @@
 """Compile the gpumhd CUDA library in-tree for sm_103a.
 
-Three translation units are compiled in parallel and linked into
+Five translation units are compiled in parallel and linked into
 ``muram_main_gb300/_build/libgpumhd.so``:
 
 * ``kernels_f64.cu`` with ``--fmad=false`` (every product and sum rounds
   separately, like the reference's no-FMA builds);
 * ``kernels_f32.cu`` with FMA contraction;
-* ``gpumhd.cu`` (host side of the C ABI), host code with -ffp-contract=off.
+* ``gpumhd.cu`` (host side of the C ABI), host code with -ffp-contract=off;
+* ``adjoint.cu`` (the FP64 adjoint kernels) and ``noalloc.cu`` (the
+  allocation-free CFL entry point), both with ``--fmad=false``.
 """
 from __future__ import annotations
 
@@ -55,6 +57,7 @@ def build(force=False, verbose=False):
     units = [("kernels_f64.cu", ["--fmad=false"]),
              ("kernels_f32.cu", ["--fmad=true", "-prec-div=false", "-prec-sqrt=false"]),
              ("gpumhd.cu", ["--fmad=false"]),
+             ("adjoint.cu", ["--fmad=false"]),
              ("noalloc.cu", ["--fmad=false"])]
     procs = []
     objs = []

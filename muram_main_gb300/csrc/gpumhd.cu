@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "../../include/gpumhd.h"
+#include "gpumhd_adjoint.cuh"
 #include "gpumhd_launch.cuh"
 
 using namespace gpumhd;
@@ -1294,3 +1295,149 @@ extern "C" int gpumhd_ensemble_synchronize(gpumhd_ensemble* e) {
 extern "C" const char* gpumhd_ensemble_last_error(gpumhd_ensemble* e) { return e ? e->err : g_create_err; }
 extern "C" void* gpumhd_ensemble_stream(gpumhd_ensemble* e) { return e ? (void*)e->stream : nullptr; }
 extern "C" long long gpumhd_ensemble_launch_count(gpumhd_ensemble* e) { return e ? e->launches : 0; }
+
+// ------------------------------------------------------------------- adjoint
+// Gradient of an objective J(U_T) with respect to the initial state U_0 over
+// nsteps fused FP64 steps of fixed dt, by the hand-written adjoint step
+// (adjoint.cu) run backwards in time.  Forward states are kept only every
+// checkpoint_every steps; the steps in between are recomputed from the
+// nearest checkpoint when the reverse sweep reaches them (memory: one
+// checkpoint per segment plus one step's intermediates).
+namespace {
+
+struct AdjMem {
+  std::vector<void*> all;
+  double* get(gpumhd_ctx* ctx, size_t count, int* rc) {
+    void* p = nullptr;
+    if (*rc) return nullptr;
+    if (cudaMalloc(&p, count * sizeof(double)) != cudaSuccess) {
+      *rc = fail(ctx, GPUMHD_E_NOMEM, "adjoint: device allocation of %zu doubles failed", count);
+      return nullptr;
+    }
+    all.push_back(p);
+    return (double*)p;
+  }
+  ~AdjMem() {
+    for (void* p : all) cudaFree(p);
+  }
+};
+
+}  // namespace
+
+extern "C" int gpumhd_adjoint(gpumhd_ctx* ctx, int nsteps, int checkpoint_every, const double* dJ_dUT,
+                              double* dJ_dU0) {
+  if (!ctx || nsteps < 1 || checkpoint_every < 1 || !dJ_dUT || !dJ_dU0) return GPUMHD_E_INVALID;
+  if (ctx->f32) return fail(ctx, GPUMHD_E_INVALID, "adjoint: FP64 contexts only");
+  if (!ctx->p.periodic_x) return fail(ctx, GPUMHD_E_INVALID, "adjoint: periodic boxes only");
+  if (ctx->p.autostep) return fail(ctx, GPUMHD_E_INVALID, "adjoint: needs a fixed time step (autostep = 0, dt > 0)");
+  if (!(ctx->p.dt > 0.0)) return fail(ctx, GPUMHD_E_INVALID, "adjoint: dt must be positive");
+  CK(cudaSetDevice(ctx->device));
+  int rc = fused_prepare(ctx, nsteps);
+  if (rc) return rc;
+  cudaStream_t s = ctx->stream;
+  const Consts& c = ctx->c;
+  const size_t N = (size_t)c.g.N;
+  const size_t n = (size_t)c.g.nx * c.g.ny * c.g.nz;
+  const int ncp = (nsteps + checkpoint_every - 1) / checkpoint_every;
+  AdjMem m;
+  double *A = m.get(ctx, 8 * N, &rc), *An = m.get(ctx, 8 * N, &rc), *B1 = m.get(ctx, 8 * N, &rc);
+  double *B2 = m.get(ctx, 8 * N, &rc), *B3 = m.get(ctx, 8 * N, &rc), *B4 = m.get(ctx, 8 * N, &rc);
+  double *V1 = m.get(ctx, 8 * N, &rc), *V2 = m.get(ctx, 8 * N, &rc);
+  double *Q0 = m.get(ctx, N, &rc), *Qn = m.get(ctx, N, &rc), *Q1 = m.get(ctx, N, &rc);
+  double *Q2 = m.get(ctx, N, &rc), *Q3 = m.get(ctx, N, &rc);
+  double* cpU = m.get(ctx, 8 * N * ncp, &rc);
+  double* cpP = m.get(ctx, N * ncp, &rc);
+  double *lA = m.get(ctx, 8 * n, &rc), *lB = m.get(ctx, 8 * n, &rc), *lC = m.get(ctx, 8 * n, &rc);
+  double *lU0 = m.get(ctx, 8 * n, &rc), *lP3 = m.get(ctx, n, &rc), *lP = m.get(ctx, n, &rc);
+  double *bdq = m.get(ctx, 36 * n, &rc), *bwc = m.get(ctx, 11 * n, &rc);
+  double* tv = m.get(ctx, (size_t)ADJ_TVD_DOUBLES * n, &rc);
+  Dyn* adyn = nullptr;
+  if (!rc && cudaMalloc(&adyn, sizeof(Dyn)) != cudaSuccess) rc = fail(ctx, GPUMHD_E_NOMEM, "adjoint: Dyn");
+  if (rc) { cudaFree(adyn); return rc; }
+  m.all.push_back(adyn);
+  rc = ensure_staging(ctx);
+  if (rc) return rc;
+  AdjTvdScratch w;
+  w.in = tv;
+  w.cell = w.in + 8 * n;
+  w.fp = w.cell + 19 * n;
+  w.fm = w.fp + 9 * n;
+  w.iface = w.fm + 9 * n;
+  w.slope = w.iface + 92 * n;
+  using L = Launch<double>;
+  // one recorded forward step: (A, Q0) -> (An, Qn), intermediates kept
+  auto record = [&]() {
+    k_step_begin<<<1, 32, 0, s>>>(c, adyn, nullptr, 0);
+    L::stage(c, A, Q0, A, B1, Q1, nullptr, adyn, 1, false, 1, s);
+    L::stage(c, B1, Q1, A, B2, Q2, nullptr, adyn, 2, false, 1, s);
+    L::stage(c, B2, Q2, A, B3, Q3, nullptr, adyn, 3, false, 1, s);
+    L::stage(c, B3, Q3, A, B4, nullptr, nullptr, adyn, 4, false, 0, s);
+    L::tvd(c, 0, 0, 0, B4, Q3, V1, nullptr, adyn, s);
+    L::tvd(c, 1, 0, 0, V1, Q3, V2, nullptr, adyn, s);
+    L::tvd(c, 2, 1, 0, V2, Q3, An, Qn, adyn, s);
+    std::swap(A, An);
+    std::swap(Q0, Qn);
+  };
+  // forward pass: checkpoints every checkpoint_every steps
+  CK(cudaMemcpyAsync(adyn, ctx->dyn, sizeof(Dyn), cudaMemcpyDeviceToDevice, s));
+  CK(cudaMemcpyAsync(A, ctx->S[ctx->iU], 8 * N * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  CK(cudaMemcpyAsync(Q0, ctx->P[ctx->iP], N * sizeof(double), cudaMemcpyDeviceToDevice, s));
+  std::vector<Dyn> cpd(ncp);  // step-control block at each checkpoint
+  for (int t = 0; t < nsteps; t++) {
+    if (t % checkpoint_every == 0) {
+      const int q = t / checkpoint_every;
+      CK(cudaMemcpyAsync(cpU + 8 * N * q, A, 8 * N * sizeof(double), cudaMemcpyDeviceToDevice, s));
+      CK(cudaMemcpyAsync(cpP + N * q, Q0, N * sizeof(double), cudaMemcpyDeviceToDevice, s));
+      CK(cudaMemcpyAsync(&cpd[q], adyn, sizeof(Dyn), cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+    }
+    record();
+  }
+  ctx->launches += 8LL * nsteps;
+  Dyn dchk;
+  CK(cudaMemcpyAsync(&dchk, adyn, sizeof(Dyn), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (dchk.err) return fail(ctx, GPUMHD_E_BAD_DT, "adjoint: the forward run failed (device error %d)", dchk.err);
+  if (dchk.two_half)
+    return fail(ctx, GPUMHD_E_INVALID, "adjoint: the fixed dt needs two TVD half steps (cfl > CFL_tvd); use a smaller dt");
+  // reverse pass
+  CK(cudaMemcpyAsync(ctx->staging, dJ_dUT, 8 * N * sizeof(double), cudaMemcpyHostToDevice, s));
+  adjoint_from_cstate(c, ctx->staging, lA, s);
+  for (int t = nsteps - 1; t >= 0; t--) {
+    const int q = t / checkpoint_every;
+    CK(cudaMemcpyAsync(A, cpU + 8 * N * q, 8 * N * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(Q0, cpP + N * q, N * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    CK(cudaMemcpyAsync(adyn, &cpd[q], sizeof(Dyn), cudaMemcpyHostToDevice, s));
+    for (int u = q * checkpoint_every; u < t; u++) record();
+    // step t's intermediates: recorded by the last call; inputs back in A, Q0
+    record();
+    std::swap(A, An);
+    std::swap(Q0, Qn);
+    ctx->launches += 8LL * (t - q * checkpoint_every + 1);
+    CK(cudaMemsetAsync(lP3, 0, n * sizeof(double), s));
+    CK(cudaMemsetAsync(lU0, 0, 8 * n * sizeof(double), s));
+    adjoint_tvd(c, adyn, 2, V2, Q3, lA, 1, lB, lP3, w, s);
+    adjoint_tvd(c, adyn, 1, V1, Q3, lB, 0, lC, lP3, w, s);
+    adjoint_tvd(c, adyn, 0, B4, Q3, lC, 0, lB, lP3, w, s);
+    adjoint_stage(c, adyn, B3, Q3, A, lB, lU0, lC, lP3, bdq, bwc, 4, s);
+    adjoint_eos(c, B3, lP3, lC, s);
+    CK(cudaMemsetAsync(lP, 0, n * sizeof(double), s));
+    adjoint_stage(c, adyn, B2, Q2, A, lC, lU0, lB, lP, bdq, bwc, 3, s);
+    adjoint_eos(c, B2, lP, lB, s);
+    CK(cudaMemsetAsync(lP, 0, n * sizeof(double), s));
+    adjoint_stage(c, adyn, B1, Q1, A, lB, lU0, lC, lP, bdq, bwc, 2, s);
+    adjoint_eos(c, B1, lP, lC, s);
+    CK(cudaMemsetAsync(lP, 0, n * sizeof(double), s));
+    adjoint_stage(c, adyn, A, Q0, A, lC, lU0, lB, lP, bdq, bwc, 1, s);
+    adjoint_eos(c, A, lP, lB, s);
+    adjoint_add(c, lB, lU0, lA, s);
+    ctx->launches += 12 + 8 + 5;
+    rc = check_launch(ctx, 0);
+    if (rc) return rc;
+  }
+  CK(cudaMemsetAsync(ctx->staging, 0, 8 * N * sizeof(double), s));
+  adjoint_to_cstate(c, lA, ctx->staging, s);
+  CK(cudaMemcpyAsync(dJ_dU0, ctx->staging, 8 * N * sizeof(double), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  return check_launch(ctx, 0);
+}

@@ -78,9 +78,20 @@ struct Consts {
   KC<double> kd;
 };
 
-template <class R> __device__ __forceinline__ const KC<R>& kc(const Consts& c);
-template <> __device__ __forceinline__ const KC<float>& kc<float>(const Consts& c) { return c.kf; }
-template <> __device__ __forceinline__ const KC<double>& kc<double>(const Consts& c) { return c.kd; }
+// Run constants for arithmetic type R (a trait, so that other arithmetic
+// types -- the adjoint's dual numbers -- can map to one of the two sets).
+template <class R> struct KCSel;
+template <> struct KCSel<float> {
+  using T = KC<float>;
+  static __device__ __forceinline__ const T& get(const Consts& c) { return c.kf; }
+};
+template <> struct KCSel<double> {
+  using T = KC<double>;
+  static __device__ __forceinline__ const T& get(const Consts& c) { return c.kd; }
+};
+template <class R> __device__ __forceinline__ const typename KCSel<R>::T& kc(const Consts& c) {
+  return KCSel<R>::get(c);
+}
 
 // Per-step scalars in a kernel's type, derived from the double values once
 // per step (host for the per-routine calls, k_step_begin on the device).
@@ -144,9 +155,9 @@ template <> __device__ __forceinline__ float smax<float>(float a, float b) { ret
 template <> __device__ __forceinline__ float smin<float>(float a, float b) { return fminf(a, b); }
 
 // The reference's 1e-100 floors; float cannot hold 1e-100, so FP32 uses 1e-30.
-template <class R> __device__ __forceinline__ R tiny100();
-template <> __device__ __forceinline__ double tiny100<double>() { return 1e-100; }
-template <> __device__ __forceinline__ float tiny100<float>() { return 1e-30f; }
+template <class R> struct Tiny100 { static __device__ __forceinline__ double get() { return 1e-100; } };
+template <> struct Tiny100<float> { static __device__ __forceinline__ float get() { return 1e-30f; } };
+template <class R> __device__ __forceinline__ R tiny100() { return (R)Tiny100<R>::get(); }
 
 __device__ __forceinline__ double d_log(double x) { return log(x); }
 __device__ __forceinline__ float d_log(float x) { return logf(x); }

@@ -309,6 +309,47 @@ __device__ __forceinline__ void rk_update(const Consts& c, R* __restrict__ Cc, u
   }
 }
 
+// Boris factor of MHD_Residual's Lorentz-force blend at a cell (src/mhdres_SR.C:310-323).
+template <class R>
+__device__ __forceinline__ R boris_lf(const R* cen, R inv_va2max) {
+  const R dn = (R)1.0 / cen[P_D];
+  const R bb = cen[P_B1] * cen[P_B1] + cen[P_B2] * cen[P_B2] + cen[P_B3] * cen[P_B3];
+  const R va2 = bb * dn;
+  const R x2 = va2 * inv_va2max, x4 = x2 * x2, s = (R)1.0 + x2;
+  return s / (s + x4);
+}
+
+// Sources and semi-relativistic (Boris) correction added to the residual Racc
+// of a cell with primitives cen (src/Add_Sources_Integrate_SR.C:331-392):
+// gravity along x, the radiative term (zero here), then the correction.
+template <class R>
+__device__ __forceinline__ void stage_sources(R* Racc, const R* cen, R gx, R inv_va2max, R invRdt) {
+  const R rh = cen[P_D], vx = cen[P_V1], vy = cen[P_V2], vz = cen[P_V3];
+  const R bx = cen[P_B1], by = cen[P_B2], bz = cen[P_B3];
+  R dn = invRdt * cen[P_EI];
+  R efaci = (dn > (R)0 && dn < (R)INFINITY) ? (R)1.0 : dn / d_fmax(dn, (R)0.0);
+  dn = gx * rh - (R)0.0;
+  const R edmp = dn * vx;
+  Racc[1] += dn;
+  Racc[4] += edmp + (R)0.0 * efaci;
+  const R rd = Racc[0];
+  R fx = Racc[1], fy = Racc[2], fz = Racc[3];
+  const R bb = bx * bx + by * by + bz * bz;
+  const R va2 = bb / rh;
+  const R x2 = va2 * inv_va2max, x4 = x2 * x2;
+  const R bf = x4 / ((R)1 + x2 + x4);
+  fx -= vx * rd;
+  fy -= vy * rd;
+  fz -= vz * rd;
+  const R q = (fx * bx + fy * by + fz * bz) / d_fmax(tiny100<R>(), bb);
+  const R b0 = -bf * (fx - q * bx), b1 = -bf * (fy - q * by), b2 = -bf * (fz - q * bz);
+  const R b3 = b0 * vx + b1 * vy + b2 * vz;
+  Racc[1] += b0;
+  Racc[2] += b1;
+  Racc[3] += b2;
+  Racc[4] += b3;
+}
+
 // Shared memory of one stage block: the x fluxes of (TX+4) x TY cells, the y
 // fluxes of TX x (TY+4) cells (12 quantities each) and each thread's ring of
 // five z-flux planes.
@@ -465,14 +506,7 @@ __global__ void __launch_bounds__(TX* TY, 2) k_stage(Consts c, const R* __restri
         for (int q = 0; q < NV; q++) Racc[q] = (R)0.0;
       }
       // Boris factor at the cell (src/mhdres_SR.C:310-323)
-      R lf;
-      {
-        const R dn = (R)1.0 / cen[P_D];
-        const R bb = cen[P_B1] * cen[P_B1] + cen[P_B2] * cen[P_B2] + cen[P_B3] * cen[P_B3];
-        const R va2 = bb * dn;
-        const R x2 = va2 * inv_va2max, x4 = x2 * x2, s = (R)1.0 + x2;
-        lf = s / (s + x4);
-      }
+      const R lf = boris_lf<R>(cen, inv_va2max);
       R n0[NF], n1[NF], n2[NF], n3[NF];
       {
         const R* fb = FX + (ty * S::PW + tx + 2) * CW;
@@ -503,30 +537,7 @@ __global__ void __launch_bounds__(TX* TY, 2) k_stage(Consts c, const R* __restri
         atomic_max_nonneg(&dyn->cmax_bits, (double)cm);
       } else {
         // sources, Boris correction, update, Tcheck (src/Add_Sources_Integrate_SR.C:331-465)
-        const R rh = cen[P_D], vx = cen[P_V1], vy = cen[P_V2], vz = cen[P_V3];
-        const R bx = cen[P_B1], by = cen[P_B2], bz = cen[P_B3];
-        R dn = invRdt * cen[P_EI];
-        R efaci = (dn > (R)0 && dn < (R)INFINITY) ? (R)1.0 : dn / d_fmax(dn, (R)0.0);
-        dn = kk_.gx * rh - (R)0.0;
-        const R edmp = dn * vx;
-        Racc[1] += dn;
-        Racc[4] += edmp + (R)0.0 * efaci;
-        const R rd = Racc[0];
-        R fx = Racc[1], fy = Racc[2], fz = Racc[3];
-        const R bb = bx * bx + by * by + bz * bz;
-        const R va2 = bb / rh;
-        const R x2 = va2 * inv_va2max, x4 = x2 * x2;
-        const R bf = x4 / ((R)1 + x2 + x4);
-        fx -= vx * rd;
-        fy -= vy * rd;
-        fz -= vz * rd;
-        const R q = (fx * bx + fy * by + fz * bz) / d_fmax(tiny100<R>(), bb);
-        const R b0 = -bf * (fx - q * bx), b1 = -bf * (fy - q * by), b2 = -bf * (fz - q * bz);
-        const R b3 = b0 * vx + b1 * vy + b2 * vz;
-        Racc[1] += b0;
-        Racc[2] += b1;
-        Racc[3] += b2;
-        Racc[4] += b3;
+        stage_sources<R>(Racc, cen, kk_.gx, inv_va2max, invRdt);
         R un[NV];
         rk_update<R>(c, Cc, id, stage, wdt, base, Racc, vmax, emax, un);
         const Images im = images_of(g, i, j, k, true);
@@ -566,7 +577,7 @@ struct TvdArgs {
 template <class R>
 __device__ __forceinline__ void tvd_cell(const Consts& c, const Raw9<R>& r, R hb, R ht, R qt, R cmax_t, R fac0,
                                          bool hyper, R inv_va2max, TCell<R>& t) {
-  const KC<R>& k = kc<R>(c);
+  const auto& k = kc<R>(c);
   const R rho_min = k.rho_min;
   R d = smax(rho_min, r.v[0]);
   R v1 = r.v[1], v2 = r.v[2], v3 = r.v[3], e = r.v[4];
@@ -621,7 +632,7 @@ template <class R>
 __device__ __forceinline__ void tvd_load(const Consts& c, const R* __restrict__ U, const R* __restrict__ P, long long id,
                                          int xi, R cmax_t, R fac0, bool hyper, R inv_va2max, TCell<R>& t) {
   const Geom& g = c.g;
-  const KC<R>& k = kc<R>(c);
+  const auto& k = kc<R>(c);
   Raw9<R> r;
 #pragma unroll
   for (int q = 0; q < NV; q++) r.v[q] = U[(long long)q * g.N + id];
@@ -642,7 +653,7 @@ __device__ __forceinline__ void tvd_slope(const Consts& c, const TCell<R>& a, co
     R upper = smax(smax(sl, sr), slm);
     slp[v] = smax((R)0.0, lower) + smin((R)0.0, upper);
   }
-  const KC<R>& k = kc<R>(c);
+  const auto& k = kc<R>(c);
   if (k.has_visc_slope) {
     R cf = ((R)1.0 - k.visc_slope_bot * b.hb) * ((R)1.0 - k.visc_slope_top * b.ht);
     slp[1] *= cf; slp[2] *= cf; slp[3] *= cf;
@@ -675,7 +686,7 @@ __device__ __forceinline__ void tvd_flux(const Consts& c, const TCell<R>& am, co
   R fac = fac0 * smin(cmax_t, smax(a.cm, b.cm));
 #pragma unroll
   for (int v = 0; v < NV; v++) F[v] *= fac;
-  const KC<R>& k = kc<R>(c);
+  const auto& k = kc<R>(c);
   F[5 + DIR] *= k.B_par_diff;
   if (c.need_coeff) {
     F[0] *= k.tvd_coeff[0];
@@ -714,6 +725,36 @@ __device__ __forceinline__ void tvd_flux(const Consts& c, const TCell<R>& am, co
     if (ia == GH - 1) F[5] = (R)0.0;
   }
   qres = (b.q[5] - a.q[5]) * F[5] + (b.q[6] - a.q[6]) * F[6] + (b.q[7] - a.q[7]) * F[7];
+}
+
+// Update of one cell by a TVD sweep (src/tvdlimit_SR.C:565-657): the flux
+// difference, its kinetic-energy and Boris parts, the resistive heating, and
+// the density and energy floors.  u_in: the cell's stored state; Fp / Fm: the
+// fluxes at its right / left interfaces, qp / qm their heating terms.
+template <class R>
+__device__ __forceinline__ void tvd_update(const Consts& c, R dtt, const R* Fp, const R* Fm, R qp, R qm,
+                                           const TCell<R>& c0, const R* u_in, R* u) {
+  const auto& kk_ = kc<R>(c);
+  R res[NV];
+#pragma unroll
+  for (int v = 0; v < NV; v++) res[v] = dtt * (Fp[v] - Fm[v]);
+  res[4] += ((R)1.0 - c0.qt) * (res[1] * c0.q[1] + res[2] * c0.q[2] + res[3] * c0.q[3]);
+  {
+    R dn = (res[1] * c0.q[5] + res[2] * c0.q[6] + res[3] * c0.q[7]) / smax(tiny100<R>(), c0.bsqr);
+    R b0 = -c0.BC2 * (res[1] - dn * c0.q[5]);
+    R b1 = -c0.BC2 * (res[2] - dn * c0.q[6]);
+    R b2 = -c0.BC2 * (res[3] - dn * c0.q[7]);
+    R b3 = b0 * c0.q[1] + b1 * c0.q[2] + b2 * c0.q[3];
+    res[1] += b0; res[2] += b1; res[3] += b2; res[4] += b3;
+  }
+  {
+    R qres = (R)0.5 * (qp + qm) * c0.qt;
+    res[4] += dtt * qres;
+  }
+#pragma unroll
+  for (int v = 0; v < NV; v++) u[v] = u_in[v] + res[v];
+  u[0] = smax((R)kk_.rho_min, u[0]);
+  u[4] = smax(u[4], kk_.eps_min * u[0] + (R)0.5 * (u[1] * u[1] + u[2] * u[2] + u[3] * u[3]) / u[0]);
 }
 
 template <class R, int DIR>
@@ -793,27 +834,8 @@ __global__ void __launch_bounds__(128) k_tvd_sweep(Consts c, const R* __restrict
       tvd_slope<R>(c, c0, c1, c2, vsqr_diff, s1);
       tvd_flux<R, DIR>(c, cm1, c0, c1, c2, s0, s1, pos, sz, fac0, cmax_t, hyper, istart, F0, q0);
       // update of cell pos (src/tvdlimit_SR.C:565-657)
-      R res[NV];
-#pragma unroll
-      for (int v = 0; v < NV; v++) res[v] = dtt * (F0[v] - Fm[v]);
-      res[4] += ((R)1.0 - c0.qt) * (res[1] * c0.q[1] + res[2] * c0.q[2] + res[3] * c0.q[3]);
-      {
-        R dn = (res[1] * c0.q[5] + res[2] * c0.q[6] + res[3] * c0.q[7]) / smax(tiny100<R>(), c0.bsqr);
-        R b0 = -c0.BC2 * (res[1] - dn * c0.q[5]);
-        R b1 = -c0.BC2 * (res[2] - dn * c0.q[6]);
-        R b2 = -c0.BC2 * (res[3] - dn * c0.q[7]);
-        R b3 = b0 * c0.q[1] + b1 * c0.q[2] + b2 * c0.q[3];
-        res[1] += b0; res[2] += b1; res[3] += b2; res[4] += b3;
-      }
-      {
-        R qres = (R)0.5 * (q0 + qm) * c0.qt;
-        res[4] += dtt * qres;
-      }
       R u[NV];
-#pragma unroll
-      for (int v = 0; v < NV; v++) u[v] = uc[v] + res[v];
-      u[0] = smax(kk_.rho_min, u[0]);
-      u[4] = smax(u[4], kk_.eps_min * u[0] + (R)0.5 * (u[1] * u[1] + u[2] * u[2] + u[3] * u[3]) / u[0]);
+      tvd_update<R>(c, dtt, F0, Fm, q0, qm, c0, uc, u);
       if (ta.mode == 0) {
 #pragma unroll
         for (int v = 0; v < NV; v++) Uout[(long long)v * g.N + id] = u[v];
@@ -934,28 +956,11 @@ __global__ void __launch_bounds__(128) k_tvd_sweep_xlanes(Consts c, const R* __r
     for (int v = 0; v < NV; v++) Fm[v] = shfl(F[v], lm);
     const R qm = shfl(qr, lm);
     if (lane < 2 || lane >= 30 || pos >= GH + g.nx) continue;
-    R res[NV];
-#pragma unroll
-    for (int v = 0; v < NV; v++) res[v] = dtt * (F[v] - Fm[v]);
-    res[4] += ((R)1.0 - c0.qt) * (res[1] * c0.q[1] + res[2] * c0.q[2] + res[3] * c0.q[3]);
-    {
-      R dn = (res[1] * c0.q[5] + res[2] * c0.q[6] + res[3] * c0.q[7]) / smax(tiny100<R>(), c0.bsqr);
-      R b0 = -c0.BC2 * (res[1] - dn * c0.q[5]);
-      R b1 = -c0.BC2 * (res[2] - dn * c0.q[6]);
-      R b2 = -c0.BC2 * (res[3] - dn * c0.q[7]);
-      R b3 = b0 * c0.q[1] + b1 * c0.q[2] + b2 * c0.q[3];
-      res[1] += b0; res[2] += b1; res[3] += b2; res[4] += b3;
-    }
-    {
-      R qres = (R)0.5 * (qr + qm) * c0.qt;
-      res[4] += dtt * qres;
-    }
     const long long id = base + pos;
-    R u[NV];
+    R uc[NV], u[NV];
 #pragma unroll
-    for (int v = 0; v < NV; v++) u[v] = Uin[(long long)v * g.N + id] + res[v];
-    u[0] = smax(kk_.rho_min, u[0]);
-    u[4] = smax(u[4], kk_.eps_min * u[0] + (R)0.5 * (u[1] * u[1] + u[2] * u[2] + u[3] * u[3]) / u[0]);
+    for (int v = 0; v < NV; v++) uc[v] = Uin[(long long)v * g.N + id];
+    tvd_update<R>(c, dtt, F, Fm, qr, qm, c0, uc, u);
 #pragma unroll
     for (int v = 0; v < NV; v++) Uout[(long long)v * g.N + id] = u[v];
   }

@@ -426,14 +426,7 @@ __global__ void __launch_bounds__(TX* TY, 2)
         for (int q = 0; q < NV; q++) Racc[q] = (R)0.0;
       }
       // Boris factor at the cell (src/mhdres_SR.C:310-323)
-      R lf;
-      {
-        const R dn = (R)1.0 / cen[P_D];
-        const R bb = cen[P_B1] * cen[P_B1] + cen[P_B2] * cen[P_B2] + cen[P_B3] * cen[P_B3];
-        const R va2 = bb * dn;
-        const R x2 = va2 * inv_va2max, x4 = x2 * x2, s = (R)1.0 + x2;
-        lf = s / (s + x4);
-      }
+      const R lf = boris_lf<R>(cen, inv_va2max);
       {
         R Dq[NF];
         const R* fb = FX + (ty * L::BX + tx + 2) * CW;
@@ -455,30 +448,7 @@ __global__ void __launch_bounds__(TX* TY, 2)
         atomic_max_nonneg(&dyn->cmax_bits, (double)cm);
       } else {
         // sources, Boris correction, update, Tcheck (src/Add_Sources_Integrate_SR.C:331-465)
-        const R rh = cen[P_D], vx = cen[P_V1], vy = cen[P_V2], vz = cen[P_V3];
-        const R bx = cen[P_B1], by = cen[P_B2], bz = cen[P_B3];
-        R dn = invRdt * cen[P_EI];
-        R efaci = (dn > (R)0 && dn < (R)INFINITY) ? (R)1.0 : dn / d_fmax(dn, (R)0.0);
-        dn = kk_.gx * rh - (R)0.0;
-        const R edmp = dn * vx;
-        Racc[1] += dn;
-        Racc[4] += edmp + (R)0.0 * efaci;
-        const R rd = Racc[0];
-        R fx = Racc[1], fy = Racc[2], fz = Racc[3];
-        const R bb = bx * bx + by * by + bz * bz;
-        const R va2 = bb / rh;
-        const R x2 = va2 * inv_va2max, x4 = x2 * x2;
-        const R bf = x4 / ((R)1 + x2 + x4);
-        fx -= vx * rd;
-        fy -= vy * rd;
-        fz -= vz * rd;
-        const R q = (fx * bx + fy * by + fz * bz) / d_fmax(tiny100<R>(), bb);
-        const R b0 = -bf * (fx - q * bx), b1 = -bf * (fy - q * by), b2 = -bf * (fz - q * bz);
-        const R b3 = b0 * vx + b1 * vy + b2 * vz;
-        Racc[1] += b0;
-        Racc[2] += b1;
-        Racc[3] += b2;
-        Racc[4] += b3;
+        stage_sources<R>(Racc, cen, kk_.gx, inv_va2max, invRdt);
         R un[NV];
         rk_update<R>(c, Cc, id, stage, wdt, base, Racc, vmax, emax, un);
         const Images im = images_of(g, i, j, k, true);

@@ -160,9 +160,44 @@ def generate(n_eps=3000, n_lr=3000, n_lp3=400, n_s3=300,
     return header, tabs, inv
 
 
-def write_table(path, **kw):
+def generate_ideal(n_eps=256, n_lr=256, n_lp3=64, n_s3=64, e_min=1.0e11, e_max=2.0e15, rho_min=1.0e-16,
+                   rho_max=1.0e-3, gamma=5.0 / 3.0, mu=0.62):
+    """An ideal-gas table (fixed mean molecular weight mu, eps_off = 0):
+    p = (gamma-1) rho eps and T = (gamma-1) mu m_H eps / k_B, so ln p and ln T
+    are linear in (ln eps, ln rho) and the bilinear lookup is exact and
+    smooth -- no kinks at table nodes (used to check derivatives)."""
+    eps_off = 0.0
+    eps0 = float(np.float32(np.log(e_min)))
+    eps1 = float(np.float32(np.log(e_max)))
+    lr0 = float(np.float32(np.log(rho_min)))
+    lr1 = float(np.float32(np.log(rho_max)))
+    xeps = np.linspace(eps0, eps1, n_eps)
+    xlr = np.linspace(lr0, lr1, n_lr)
+    LE, LR = np.meshgrid(xeps, xlr, indexing="xy")
+    lnp = np.log(gamma - 1.0) + LR + LE
+    lnT = np.log((gamma - 1.0) * mu * M_H / K_B) + LE
+    s_phys = K_B / (mu * M_H) * (1.5 * lnT - LR)  # Sackur-Tetrode up to a constant
+    ss_off = float(np.float32(-np.median(s_phys)))
+    tabs = {"p": lnp, "T": lnT, "s": s_phys + ss_off, "ne": LR - np.log(1.2 * M_H),
+            "rhoi": LR, "amb": np.zeros_like(LR)}
+    lp0, lp1 = float(np.float32(np.percentile(lnp, 5))), float(np.float32(np.percentile(lnp, 95)))
+    s0, s1 = float(np.float32(np.percentile(tabs["s"], 5))), float(np.float32(np.percentile(tabs["s"], 95)))
+    LP, S = np.meshgrid(np.linspace(lp0, lp1, n_lp3), np.linspace(s0, s1, n_s3), indexing="xy")
+    # invert: ln p = c1 + ln rho + ln eps, s' = a (1.5 (c2 + ln eps) - ln rho)
+    a = K_B / (mu * M_H)
+    c1 = np.log(gamma - 1.0)
+    c2 = np.log((gamma - 1.0) * mu * M_H / K_B)
+    q = (S - ss_off) / a  # 1.5 (c2 + le) - lr
+    le = (q + (LP - c1) - 1.5 * c2) / 2.5
+    lr = LP - c1 - le
+    inv = {"eps3": le, "d3": lr}
+    header = [n_eps, n_lr, n_lp3, n_s3, eps0, eps1, lr0, lr1, lp0, lp1, s0, s1, eps_off, ss_off]
+    return header, tabs, inv
+
+
+def write_table(path, ideal=False, **kw):
     """Generate a table and write it in the eos_init binary layout; returns SHA-256."""
-    header, tabs, inv = generate(**kw)
+    header, tabs, inv = generate_ideal(**kw) if ideal else generate(**kw)
     blob = bytearray(struct.pack("<14f", *[float(h) for h in header]))
     for name in ("p", "T", "s", "ne", "rhoi", "amb"):
         blob += np.ascontiguousarray(tabs[name], dtype="<f4").tobytes()
@@ -187,11 +222,14 @@ def bench_table_kwargs():
 
 
 def ensure_table(path, kind="bench"):
-    """Create the table at ``path`` if it does not exist yet."""
+    """Create the table at ``path`` if it does not exist yet (kind: "bench",
+    "small" or "ideal")."""
     if not os.path.exists(path):
-        kw = bench_table_kwargs() if kind == "bench" else small_table_kwargs()
         os.makedirs(os.path.dirname(os.path.abspath(path)), exist_ok=True)
-        write_table(path, **kw)
+        if kind == "ideal":
+            write_table(path, ideal=True)
+        else:
+            write_table(path, **(bench_table_kwargs() if kind == "bench" else small_table_kwargs()))
     return path
 
 

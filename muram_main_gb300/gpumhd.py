@@ -61,7 +61,7 @@ EXPORTS = [
     "gpumhd_sync_timestep", "gpumhd_source_integrate_tcheck", "gpumhd_tvdlimit", "gpumhd_tcheck",
     "gpumhd_exchange", "gpumhd_run_steps", "gpumhd_enqueue_steps", "gpumhd_synchronize", "gpumhd_step_info",
     "gpumhd_stream", "gpumhd_launch_count", "gpumhd_profile_steps", "gpumhd_cfl_dt_noalloc",
-    "gpumhd_tile_from", "gpumhd_set_tuning", "gpumhd_get_tuning", "gpumhd_autotune", "gpumhd_ensemble_create",
+    "gpumhd_adjoint", "gpumhd_tile_from", "gpumhd_set_tuning", "gpumhd_get_tuning", "gpumhd_autotune", "gpumhd_ensemble_create",
     "gpumhd_ensemble_destroy", "gpumhd_ensemble_enqueue_steps", "gpumhd_ensemble_synchronize",
     "gpumhd_ensemble_last_error", "gpumhd_ensemble_stream", "gpumhd_ensemble_launch_count",
 ]
@@ -115,6 +115,7 @@ def load(build_if_missing=True):
         "gpumhd_stream": (vp, [vp]),
         "gpumhd_launch_count": (C.c_longlong, [vp]),
         "gpumhd_tile_from": (C.c_int, [vp, vp]),
+        "gpumhd_adjoint": (C.c_int, [vp, C.c_int, C.c_int, dp, dp]),
         "gpumhd_set_tuning": (C.c_int, [vp, C.c_int, C.c_int]),
         "gpumhd_get_tuning": (C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
         "gpumhd_autotune": (C.c_int, [vp, C.c_int, dp]),
@@ -340,6 +341,14 @@ class MuramGPU:
 
     def download_ptr(self, which, ptr):
         self._chk(self._L.gpumhd_download(self._h, which, C.cast(ptr, C.POINTER(C.c_double))))
+
+    def adjoint(self, nsteps, dJ_dUT, checkpoint_every=5):
+        """dJ/dU_0 for J(U_T) over nsteps fixed-dt FP64 steps from the current
+        state; dJ_dUT and the result are (8, sz, sy, sx) arrays (ghosts ignored / zero)."""
+        lam = np.ascontiguousarray(np.moveaxis(np.asarray(dJ_dUT, dtype=np.float64), 0, -1))
+        out = np.empty_like(lam)
+        self._chk(self._L.gpumhd_adjoint(self._h, nsteps, checkpoint_every, _dptr(lam), _dptr(out)))
+        return np.ascontiguousarray(np.moveaxis(out, -1, 0))
 
     def tile_from(self, src):
         """This box's state becomes the periodic tiling of src's (set-up of large boxes)."""
