@@ -64,6 +64,11 @@ typedef struct gpumhd_params {
   /* radiative transfer stays outside the path: constant optical depth,
    * zero radiative heating, constant radiative time step */
   double tau0, dt_rad;
+  /* PhysicsData::params[i_param_eta]: resistivity in cm^2/s (0: ideal MHD).
+   * MHD_Residual then adds eta times the fourth-order Laplacian of B, the ohmic
+   * heating eta*|curl B|^2, and the resistive time-step limit
+   * (src/mhdres_SR.C:58-61, 422-450, 741-765, 815-819). */
+  double eta;
 } gpumhd_params;
 
 typedef struct gpumhd_ctx gpumhd_ctx;

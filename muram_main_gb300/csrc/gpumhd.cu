@@ -125,6 +125,12 @@ static void fill_kc(const Consts& c, KC<R>& k, const R* prof) {
   for (int i = 0; i < 4; i++) { k.tvd_h[i] = (R)c.tvd_h[i]; k.tvd_cs[i] = (R)c.tvd_cs[i]; k.tvd_coeff[i] = (R)c.tvd_coeff[i]; }
   k.CZ = (R)c.CZ; k.tchk_vmax = (R)c.tchk_vmax; k.tchk_eps_max = (R)c.tchk_eps_max; k.gx = (R)c.gx;
   for (int d = 0; d < 3; d++) { k.w1[d] = (R)c.w1[d]; k.w2[d] = (R)c.w2[d]; }
+  k.eta = (R)c.eta;
+  for (int d = 0; d < 3; d++) {
+    k.ww0[d] = (R)(-30. / (12. * c.dx[d] * c.dx[d]));
+    k.ww1[d] = (R)(16. / (12. * c.dx[d] * c.dx[d]));
+    k.ww2[d] = (R)(-1. / (12. * c.dx[d] * c.dx[d]));
+  }
   k.hfb = prof; k.hft = prof + c.g.sx; k.qft = prof + 2 * c.g.sx;
   k.has_visc_slope = (c.visc_slope_bot > 0.0 || c.visc_slope_top > 0.0);
   k.has_eta_slope = (c.eta_slope_bot > 0.0 || c.eta_slope_top > 0.0);
@@ -177,6 +183,15 @@ static int fill_consts(gpumhd_ctx* ctx) {
   c.tchk_vmax = p.tchk[3];
   c.tchk_eps_max = p.tchk[2];
   c.gx = -p.grav;
+  // resistivity: time-step limit dt_diff_fac / eta, halved for CFL > 1 (src/mhdres_SR.C:47-62, 815-819)
+  c.eta = p.eta;
+  c.has_eta = p.eta > 0.0 ? 1 : 0;
+  c.dt_res = 0.0;
+  if (c.has_eta) {
+    const double dt_diff_fac = 0.5 / (1. / (p.dx[0] * p.dx[0]) + 1. / (p.dx[1] * p.dx[1]) + 1. / (p.dx[2] * p.dx[2]));
+    c.dt_res = dt_diff_fac / p.eta;
+    if (p.CFL > 1) c.dt_res *= 0.5;
+  }
   c.rt_cfl = p.rt_cfl;
   c.CFL = p.CFL; c.CFL_tvd = p.CFL_tvd; c.dt_rad = p.dt_rad; c.rt_tstep = p.rt_tstep; c.outcad = p.outcad;
   c.va_max = p.va_max; c.va_adjust = p.va_adjust; c.max_fill = p.max_fill;
@@ -322,6 +337,7 @@ extern "C" int gpumhd_create(const gpumhd_params* p, int device, gpumhd_ctx** ou
   if (p->nx < 4 || p->ny < 4 || p->nz < 4) return fail(nullptr, GPUMHD_E_INVALID, "grid must have >= 4 interior cells per dimension");
   if (p->precision != 64 && p->precision != 32) return fail(nullptr, GPUMHD_E_INVALID, "precision must be 32 or 64");
   if (p->stage_kernel != 0 && p->stage_kernel != 1) return fail(nullptr, GPUMHD_E_INVALID, "stage_kernel must be 0 or 1");
+  if (!(p->eta >= 0.0)) return fail(nullptr, GPUMHD_E_INVALID, "eta must be >= 0");
   if ((long long)(p->nx + 4) * (p->ny + 4) * (p->nz + 4) > GPUMHD_MAX_CELLS)
     return fail(nullptr, GPUMHD_E_INVALID, "grid too large: (nx+4)(ny+4)(nz+4) must not exceed %lld cells",
                 (long long)GPUMHD_MAX_CELLS);
@@ -710,7 +726,11 @@ extern "C" int gpumhd_mhd_residual(gpumhd_ctx* ctx, double* dt_mhd) {
   rc = pull_dyn(ctx);
   if (rc) return rc;
   const double cmax = bits_to_double(ctx->hdyn.cmax_bits);
-  if (dt_mhd) *dt_mhd = ctx->c.dxmin / cmax;
+  if (dt_mhd) {
+    double dt = ctx->c.dxmin / cmax;
+    if (ctx->c.has_eta) dt = stdmin(dt, ctx->c.dt_res);
+    *dt_mhd = dt;
+  }
   return GPUMHD_OK;
 }
 
@@ -1331,6 +1351,7 @@ extern "C" int gpumhd_adjoint(gpumhd_ctx* ctx, int nsteps, int checkpoint_every,
   if (!ctx->p.periodic_x) return fail(ctx, GPUMHD_E_INVALID, "adjoint: periodic boxes only");
   if (ctx->p.autostep) return fail(ctx, GPUMHD_E_INVALID, "adjoint: needs a fixed time step (autostep = 0, dt > 0)");
   if (!(ctx->p.dt > 0.0)) return fail(ctx, GPUMHD_E_INVALID, "adjoint: dt must be positive");
+  if (ctx->c.has_eta) return fail(ctx, GPUMHD_E_INVALID, "adjoint: ideal MHD only (eta = 0)");
   CK(cudaSetDevice(ctx->device));
   int rc = fused_prepare(ctx, nsteps);
   if (rc) return rc;

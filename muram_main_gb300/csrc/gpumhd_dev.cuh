@@ -35,6 +35,7 @@ struct KC {
   R tvd_h[4], tvd_cs[4], tvd_coeff[4];
   R CZ, tchk_vmax, tchk_eps_max, gx;
   R w1[3], w2[3];
+  R eta, ww0[3], ww1[3], ww2[3];  // resistivity and the second-derivative stencil
   const R* hfb;   // vertical boundary profiles, length sx
   const R* hft;
   const R* qft;
@@ -69,6 +70,8 @@ struct Consts {
   // Tcheck and sources
   double tchk_vmax, tchk_eps_max;
   double gx;                   // PhysicsData::g[0] = -grav
+  double eta, dt_res;          // resistivity and its time-step limit (eta > 0 only)
+  int has_eta, pad3;
   double rt_cfl;
   double CFL, CFL_tvd, dt_rad, rt_tstep, outcad;
   double va_max, va_adjust, max_fill;

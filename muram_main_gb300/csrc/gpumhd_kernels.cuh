@@ -10,6 +10,8 @@
 //  small kernels: ConsToPrim, Adjust_Valf_Max statistics, Source_Integrate,
 //               SaveCons, TCheck, ghost fill, layout conversion, step control.
 #pragma once
+#include <type_traits>
+
 #include "gpumhd_dev.cuh"
 
 namespace gpumhd {
@@ -211,11 +213,15 @@ __device__ __forceinline__ void deriv12(float* Dq, const float* fm2, const float
   }
 }
 
-template <class R, int D1>
-__device__ __forceinline__ void add_direction(R* Racc, const R* fm2, const R* fm1, const R* fp1, const R* fp2, R w1,
-                                              R w2, const R* cen, R lf) {
-  R Dq[NF];
-  deriv12(Dq, fm2, fm1, fp1, fp2, w1, w2);
+// Residual terms of one direction from its derivatives Dq (src/mhdres_SR.C:
+// 373-412), added to Racc: res = 0 - D(F); res[1..3] += Lorentz; res[4] +=
+// v . Lorentz; Racc += res.  ETA (resistivity, src/mhdres_SR.C:422-450,
+// 741-765): the direction's curl B parts accumulate in cb; the last direction
+// (z) adds the ohmic heating eta*|cb|^2 to Racc[4] before its residual; lap3
+// is eta times the fourth-order second derivative of B along the direction.
+template <class R, int D1, bool ETA = false>
+__device__ __forceinline__ void apply_direction(R* Racc, const R* Dq, const R* cen, R lf, R eta = (R)0,
+                                                R* cb = nullptr, const R* lap3 = nullptr) {
   R res[NV];
   res[0] = (R)0.0 - Dq[0];
   res[1] = (R)0.0 - Dq[1];
@@ -241,8 +247,41 @@ __device__ __forceinline__ void add_direction(R* Racc, const R* fm2, const R* fm
   res[2] += lrt1;
   res[3] += lrt2;
   res[4] += cen[P_V1] * lrt0 + cen[P_V2] * lrt1 + cen[P_V3] * lrt2;
+  if (ETA) {
+    const R signd1 = D1 == 1 ? (R)1.0 : (R)-1.0;
+    cb[Dirs<D1>::d2] += signd1 * dB3;
+    cb[Dirs<D1>::d3] += -signd1 * dB2;
+    if (D1 == 2) Racc[4] += eta * (cb[0] * cb[0] + cb[1] * cb[1] + cb[2] * cb[2]);
+    res[5] += lap3[0];
+    res[6] += lap3[1];
+    res[7] += lap3[2];
+  }
 #pragma unroll
   for (int q = 0; q < NV; q++) Racc[q] += res[q];
+}
+
+// eta times the fourth-order second derivative of B along a direction of
+// stride sd at cell id (src/mhdres_SR.C:441-450); cen: the cell's primitives.
+template <class R>
+__device__ __forceinline__ void eta_lap(const Consts& c, const R* __restrict__ U, unsigned id, unsigned sd, int d,
+                                        const R* cen, R* lap3) {
+  const auto& k = kc<R>(c);
+#pragma unroll
+  for (int q = 0; q < 3; q++) {
+    const R* B = U + (unsigned)(5 + q) * c.g.N32;
+    const R bp1 = B[id + sd], bm1 = B[id - sd], bp2 = B[id + 2 * sd], bm2 = B[id - 2 * sd];
+    lap3[q] = k.eta * (k.ww0[d] * cen[P_B1 + q] + k.ww1[d] * (bp1 + bm1) + k.ww2[d] * (bp2 + bm2));
+  }
+}
+
+template <class R, int D1, bool ETA = false>
+__device__ __forceinline__ void add_direction(R* Racc, const R* __restrict__ fm2, const R* __restrict__ fm1,
+                                              const R* __restrict__ fp1, const R* __restrict__ fp2, R w1,
+                                              R w2, const R* cen, R lf, R eta = (R)0, R* cb = nullptr,
+                                              const R* lap3 = nullptr) {
+  R Dq[NF];
+  deriv12(Dq, fm2, fm1, fp1, fp2, w1, w2);
+  apply_direction<R, D1, ETA>(Racc, Dq, cen, lf, eta, cb, lap3);
 }
 
 // ------------------------------------------------------------ stage kernel
@@ -507,28 +546,39 @@ __global__ void __launch_bounds__(TX* TY, 2) k_stage(Consts c, const R* __restri
       }
       // Boris factor at the cell (src/mhdres_SR.C:310-323)
       const R lf = boris_lf<R>(cen, inv_va2max);
-      R n0[NF], n1[NF], n2[NF], n3[NF];
-      {
-        const R* fb = FX + (ty * S::PW + tx + 2) * CW;
-        load_cell(fb - 2 * CW, n0);
-        load_cell(fb - CW, n1);
-        load_cell(fb + CW, n2);
-        load_cell(fb + 2 * CW, n3);
-        add_direction<R, 0>(Racc, n0, n1, n2, n3, w1x, w2x, cen, lf);
-      }
-      {
-        const R* fb = FY + ((ty + 2) * TX + tx) * CW;
-        load_cell(fb - 2 * TX * CW, n0);
-        load_cell(fb - TX * CW, n1);
-        load_cell(fb + TX * CW, n2);
-        load_cell(fb + 2 * TX * CW, n3);
-        add_direction<R, 1>(Racc, n0, n1, n2, n3, w1y, w2y, cen, lf);
-      }
-      load_cell(zcell(slot_add(s0, 3)), n0);
-      load_cell(zcell(slot_add(s0, 4)), n1);
-      load_cell(zcell(slot_add(s0, 1)), n2);
-      load_cell(zcell(slot_add(s0, 2)), n3);
-      add_direction<R, 2>(Racc, n0, n1, n2, n3, w1z, w2z, cen, lf);
+      // the three directions, with the resistive terms when eta > 0
+      auto directions = [&](auto eta_on) {
+        constexpr bool ETA = decltype(eta_on)::value;
+        R cb[3] = {(R)0, (R)0, (R)0};
+        R lap[3];
+        R n0[NF], n1[NF], n2[NF], n3[NF];
+        {
+          const R* fb = FX + (ty * S::PW + tx + 2) * CW;
+          load_cell(fb - 2 * CW, n0);
+          load_cell(fb - CW, n1);
+          load_cell(fb + CW, n2);
+          load_cell(fb + 2 * CW, n3);
+          if (ETA) eta_lap<R>(c, Uin, id, 1u, 0, cen, lap);
+          add_direction<R, 0, ETA>(Racc, n0, n1, n2, n3, w1x, w2x, cen, lf, kk_.eta, cb, lap);
+        }
+        {
+          const R* fb = FY + ((ty + 2) * TX + tx) * CW;
+          load_cell(fb - 2 * TX * CW, n0);
+          load_cell(fb - TX * CW, n1);
+          load_cell(fb + TX * CW, n2);
+          load_cell(fb + 2 * TX * CW, n3);
+          if (ETA) eta_lap<R>(c, Uin, id, (unsigned)g.sx, 1, cen, lap);
+          add_direction<R, 1, ETA>(Racc, n0, n1, n2, n3, w1y, w2y, cen, lf, kk_.eta, cb, lap);
+        }
+        load_cell(zcell(slot_add(s0, 3)), n0);
+        load_cell(zcell(slot_add(s0, 4)), n1);
+        load_cell(zcell(slot_add(s0, 1)), n2);
+        load_cell(zcell(slot_add(s0, 2)), n3);
+        if (ETA) eta_lap<R>(c, Uin, id, plane, 2, cen, lap);
+        add_direction<R, 2, ETA>(Racc, n0, n1, n2, n3, w1z, w2z, cen, lf, kk_.eta, cb, lap);
+      };
+      if (c.has_eta) directions(std::true_type());
+      else directions(std::false_type());
       if (RESID) {
 #pragma unroll
         for (int q = 0; q < NV; q++) Res[id + (unsigned)q * g.N32] = Racc[q];

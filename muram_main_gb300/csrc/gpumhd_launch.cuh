@@ -125,11 +125,11 @@ void Launch<R>::stage(const Consts& c, const R* Uin, const R* Pin, const R* U0, 
     constexpr int MX = StageTileTm<R>::TX, MY = StageTileTm<R>::TY;
     const int bytes = (int)StageTm<R, MX, MY>::BYTES;
     if (resid)
-      k_stage_tm<R, MX, MY, true><<<grid, MX * MY, bytes, s>>>(*mu, *mp, c, U0, Uout, Pout, Res, dyn, stage, zc,
-                                                               write_pres, nullptr);
+      k_stage_tm<R, MX, MY, true><<<grid, MX * MY, bytes, s>>>(*mu, *mp, c, Uin, U0, Uout, Pout, Res, dyn, stage,
+                                                               zc, write_pres, nullptr);
     else
-      k_stage_tm<R, MX, MY, false><<<grid, MX * MY, bytes, s>>>(*mu, *mp, c, U0, Uout, Pout, Res, dyn, stage, zc,
-                                                                write_pres, Cc);
+      k_stage_tm<R, MX, MY, false><<<grid, MX * MY, bytes, s>>>(*mu, *mp, c, Uin, U0, Uout, Pout, Res, dyn, stage,
+                                                                zc, write_pres, Cc);
     return;
   }
   constexpr int PX = StageTile<R>::TX, PY = StageTile<R>::TY;

@@ -202,47 +202,16 @@ __device__ __forceinline__ void tm_deriv12(double* Dq, unsigned m2, unsigned m1,
   }
 }
 
-// Residual terms of one direction from its derivatives Dq (the part of
-// add_direction after the differences, src/mhdres_SR.C:373-412).
-template <class R, int D1>
-__device__ __forceinline__ void apply_direction(R* Racc, const R* Dq, const R* cen, R lf) {
-  R res[NV];
-  res[0] = (R)0.0 - Dq[0];
-  res[1] = (R)0.0 - Dq[1];
-  res[2] = (R)0.0 - Dq[2];
-  res[3] = (R)0.0 - Dq[3];
-  res[4] = (R)0.0 - Dq[4];
-  res[5] = (R)0.0;
-  res[6] = (R)0.0;
-  res[7] = (R)0.0;
-  res[Dirs<D1>::fa] = (R)0.0 - Dq[5];
-  res[Dirs<D1>::fb] = (R)0.0 - Dq[6];
-  const R dB2 = Dq[10], dB3 = Dq[11];
-  const R Bd1 = cen[P_B1 + D1];
-  const R Bd2 = cen[P_B1 + Dirs<D1>::d2], Bd3 = cen[P_B1 + Dirs<D1>::d3];
-  R cbb[3];
-  cbb[D1] = -Bd2 * dB2 - Bd3 * dB3;
-  cbb[Dirs<D1>::d2] = Bd1 * dB2;
-  cbb[Dirs<D1>::d3] = Bd1 * dB3;
-  const R lrt0 = lf * Dq[7] + ((R)1.0 - lf) * cbb[0];
-  const R lrt1 = lf * Dq[8] + ((R)1.0 - lf) * cbb[1];
-  const R lrt2 = lf * Dq[9] + ((R)1.0 - lf) * cbb[2];
-  res[1] += lrt0;
-  res[2] += lrt1;
-  res[3] += lrt2;
-  res[4] += cen[P_V1] * lrt0 + cen[P_V2] * lrt1 + cen[P_V3] * lrt2;
-#pragma unroll
-  for (int q = 0; q < NV; q++) Racc[q] += res[q];
-}
-
 // Launch: grid (ceil(nx/TX), ceil(ny/TY), z chunks), TX*TY threads,
 // StageTm::BYTES of dynamic shared memory.  mapU: the input state as a 4-D
 // tensor (x, y, z, variable), box (TX+4, TY+4, 1, 8); mapP: its pressure,
-// box (TX+4, TY+4, 1).  Other arguments as k_stage.
+// box (TX+4, TY+4, 1); Ug: the same state as a pointer (read for the
+// resistive terms only).  Other arguments as k_stage.
 template <class R, int TX, int TY, bool RESID>
 __global__ void __launch_bounds__(TX* TY, 2)
     k_stage_tm(const __grid_constant__ CUtensorMap mapU, const __grid_constant__ CUtensorMap mapP, Consts c,
-               const R* __restrict__ U0, R* __restrict__ Uout, R* __restrict__ Pout, R* __restrict__ Res,
+               const R* __restrict__ Ug, const R* __restrict__ U0, R* __restrict__ Uout, R* __restrict__ Pout,
+               R* __restrict__ Res,
                Dyn* __restrict__ dyn, int stage, int zc, int write_pres, R* __restrict__ Cc) {
   using L = StageTm<R, TX, TY>;
   constexpr int CW = CellW<R>::W;
@@ -427,19 +396,30 @@ __global__ void __launch_bounds__(TX* TY, 2)
       }
       // Boris factor at the cell (src/mhdres_SR.C:310-323)
       const R lf = boris_lf<R>(cen, inv_va2max);
-      {
-        R Dq[NF];
-        const R* fb = FX + (ty * L::BX + tx + 2) * CW;
-        deriv12(Dq, fb - 2 * CW, fb - CW, fb + CW, fb + 2 * CW, kk_.w1[0], kk_.w2[0]);
-        apply_direction<R, 0>(Racc, Dq, cen, lf);
-      }
-      {
-        R Dq[NF];
-        const R* fb = FY + ((ty + 2) * TX + tx) * CW;
-        deriv12(Dq, fb - 2 * TX * CW, fb - TX * CW, fb + TX * CW, fb + 2 * TX * CW, kk_.w1[1], kk_.w2[1]);
-        apply_direction<R, 1>(Racc, Dq, cen, lf);
-      }
-      apply_direction<R, 2>(Racc, Dz, cen, lf);
+      // the three directions, with the resistive terms when eta > 0
+      auto directions = [&](auto eta_on) {
+        constexpr bool ETA = decltype(eta_on)::value;
+        R cb[3] = {(R)0, (R)0, (R)0};
+        R lap[3];
+        {
+          R Dq[NF];
+          const R* fb = FX + (ty * L::BX + tx + 2) * CW;
+          deriv12(Dq, fb - 2 * CW, fb - CW, fb + CW, fb + 2 * CW, kk_.w1[0], kk_.w2[0]);
+          if (ETA) eta_lap<R>(c, Ug, id, 1u, 0, cen, lap);
+          apply_direction<R, 0, ETA>(Racc, Dq, cen, lf, kk_.eta, cb, lap);
+        }
+        {
+          R Dq[NF];
+          const R* fb = FY + ((ty + 2) * TX + tx) * CW;
+          deriv12(Dq, fb - 2 * TX * CW, fb - TX * CW, fb + TX * CW, fb + 2 * TX * CW, kk_.w1[1], kk_.w2[1]);
+          if (ETA) eta_lap<R>(c, Ug, id, (unsigned)g.sx, 1, cen, lap);
+          apply_direction<R, 1, ETA>(Racc, Dq, cen, lf, kk_.eta, cb, lap);
+        }
+        if (ETA) eta_lap<R>(c, Ug, id, plane, 2, cen, lap);
+        apply_direction<R, 2, ETA>(Racc, Dz, cen, lf, kk_.eta, cb, lap);
+      };
+      if (c.has_eta) directions(std::true_type());
+      else directions(std::false_type());
       if (RESID) {
 #pragma unroll
         for (int q = 0; q < NV; q++) Res[id + (unsigned)q * g.N32] = Racc[q];

@@ -15,7 +15,8 @@ __global__ void k_step_begin(Consts c, Dyn* dyn, double* dt_hist, int dt_hist_ca
   dyn->v_lim = c.tchk_vmax;
   dyn->e_lim = c.tchk_eps_max;
   const double cmax = __longlong_as_double((long long)dyn->cmax_bits);
-  const double dt_mhd = c.dxmin / cmax;
+  double dt_mhd = c.dxmin / cmax;
+  if (c.has_eta) dt_mhd = smin(dt_mhd, c.dt_res);  // resistive limit (src/mhdres_SR.C:815-819)
   dyn->dt_mhd = dt_mhd;
   // Sync_timestep (src/solver.C:487-548) on one rank
   double r0 = c.dt_rad, r1 = dt_mhd;

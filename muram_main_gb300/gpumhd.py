@@ -50,7 +50,7 @@ class Params(C.Structure):
         ("tvd_h_bnd", C.c_double * 2), ("tvd_visc_bnd", C.c_double * 2), ("tvd_eta_bnd", C.c_double * 2),
         ("tvd_coeff", C.c_double * 4), ("tchk", C.c_double * 4),
         ("rt_cfl", C.c_double), ("rt_tstep", C.c_double), ("rt_update", C.c_double),
-        ("tau0", C.c_double), ("dt_rad", C.c_double),
+        ("tau0", C.c_double), ("dt_rad", C.c_double), ("eta", C.c_double),
     ]
 
 

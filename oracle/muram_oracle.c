@@ -274,10 +274,21 @@ double mo_mhd_residual(const mo_params* p, const double* U, const double* pres, 
   double* flx = (double*)malloc(sizeof(double) * NV * L);
   double* ms = (double*)malloc(sizeof(double) * 3 * L);
   double* lf1 = (double*)malloc(sizeof(double) * L);
+  /* resistivity (src/mhdres_SR.C:58-61, 112-118, 422-450, 741-765, 815-819):
+   * Grid.curlB starts at zero and accumulates the curl over the direction
+   * passes; in the last pass R.e gets the ohmic heating eta*|curlB|^2 before
+   * that pass's residual, and in every pass B gets eta times the fourth-order
+   * second derivative along the pass direction */
+  const double eta = p->eta;
+  const int needs_curlB = eta > 0.0;
+  double* curlB = needs_curlB ? (double*)calloc((size_t)3 * g.N, sizeof(double)) : NULL;
+  static const double sgn[3] = {-1., 1., -1.};
   for (int d = 0; d < 3; d++) {
     const int d1 = order[d][0], d2 = order[d][1], d3 = order[d][2];
     const double dx = p->dx[d1];
     const double w1 = 8. / (12. * dx), w2 = -1. / (12. * dx);
+    const double ww0 = -30. / (12. * dx * dx), ww1 = 16. / (12. * dx * dx), ww2 = -1. / (12. * dx * dx);
+    const double signd1 = sgn[d1];
     const double pd[3] = {d1 == 0 ? 1. : 0., d1 == 1 ? 1. : 0., d1 == 2 ? 1. : 0.};
     const int sz = n[d1] + 2 * GH;
     for (int b = GH; b < GH + n[d3]; b++)
@@ -340,12 +351,34 @@ double mo_mhd_residual(const mo_params* p, const double* U, const double* pres, 
           res[3] += lrt[2];
           res[4] += var[L + i] * lrt[0] + var[2 * L + i] * lrt[1] + var[3 * L + i] * lrt[2];
           long c = off + i * st[d1];
+          if (needs_curlB) {
+            double cb[3];
+            cb[d1] = 0;
+            cb[d2] = signd1 * dB3;
+            cb[d3] = -signd1 * dB2;
+            for (int q = 0; q < 3; q++) curlB[q * g.N + c] += cb[q];
+            if (d == 2) {  /* the last pass has the whole curl: ohmic heating */
+              const double cx = curlB[c], cy = curlB[g.N + c], cz = curlB[2 * g.N + c];
+              R[4 * g.N + c] += eta * (cx * cx + cy * cy + cz * cz);
+            }
+            for (int v = 5; v <= 7; v++) {
+              const double* b = var + v * L;
+              res[v] += eta * (ww0 * b[i] + ww1 * (b[i + 1] + b[i - 1]) + ww2 * (b[i + 2] + b[i - 2]));
+            }
+          }
           for (int v = 0; v < NV; v++) R[v * g.N + c] += res[v];
         }
       }
   }
-  free(var); free(flx); free(ms); free(lf1);
-  return dxmin / cmax;
+  free(var); free(flx); free(ms); free(lf1); free(curlB);
+  double dt_cfl = dxmin / cmax;
+  if (needs_curlB) {
+    const double dt_diff_fac = 0.5 / (1. / (p->dx[0] * p->dx[0]) + 1. / (p->dx[1] * p->dx[1]) + 1. / (p->dx[2] * p->dx[2]));
+    double dt_res = dt_diff_fac / eta;
+    if (p->CFL > 1) dt_res *= 0.5;
+    dt_cfl = smin(dt_cfl, dt_res);
+  }
+  return dt_cfl;
 }
 
 /* ----------------------------------------------------------- Sync_timestep */

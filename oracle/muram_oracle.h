@@ -34,6 +34,8 @@ typedef struct {
   int va_ini_flag;
   double last_cfl;
   int tvd_two_half_steps;
+  /* PhysicsData::params[i_param_eta]: resistivity (cm^2/s); 0 = ideal MHD */
+  double eta;
 } mo_params;
 
 typedef struct mo_eos mo_eos;

@@ -31,6 +31,7 @@ class MoParams(C.Structure):
         ("tau0", C.c_double), ("dt_rad", C.c_double),
         ("inv_va2max", C.c_double), ("v_lim", C.c_double), ("e_lim", C.c_double), ("va_max_old", C.c_double),
         ("va_ini_flag", C.c_int), ("last_cfl", C.c_double), ("tvd_two_half_steps", C.c_int),
+        ("eta", C.c_double),
     ]
 
 
@@ -104,7 +105,7 @@ def params_from_harness(hp):
     """Build MoParams from the harness key/value dict used by oracle.refrun."""
     kw = {}
     simple = {"CFL": "CFL", "CFL_tvd": "CFL_tvd", "grav": "grav", "va_max": "va_max",
-              "va_adjust": "va_adjust", "max_fill": "max_fill", "tau0": "tau0", "dt_rad": "dt_rad"}
+              "va_adjust": "va_adjust", "max_fill": "max_fill", "tau0": "tau0", "dt_rad": "dt_rad", "eta": "eta"}
     for k, a in simple.items():
         if k in hp:
             kw[a] = float(hp[k])

@@ -174,7 +174,7 @@ int main(int argc, char** argv) {
   Physics.params[i_param_va_adjust] = par_d("va_adjust", 0.0);
   Physics.params[i_param_max_fill] = par_d("max_fill", 1000.);
   Physics.params[i_param_spitzer] = 0.0;
-  Physics.params[i_param_eta] = 0.0;
+  Physics.params[i_param_eta] = par_d("eta", 0.0);
   Physics.params[i_param_ambipolar] = 0.0;
   par_arr("tvd_h", Physics.tvd_h, 4);
   par_arr("tvd_cs", Physics.tvd_cs, 4);

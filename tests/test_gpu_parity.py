@@ -228,3 +228,62 @@ def test_fp32_compensated_rk_updates(gpu_lib):
     print("FP32 rel L2 per field, compensated:", np.array2string(errs[1], precision=2))
     assert np.all(errs[1] <= TOL32_L2), errs[1]
     assert not np.array_equal(states[0], states[1])
+
+
+def _oracle_run_p(p, U, steps):
+    from oracle import oracle as O
+    eos = O.Eos(H.EOS_SMALL)
+    st = O.State(p, U)
+    dts = st.step(eos, steps)
+    return st.U, dts
+
+
+@pytest.mark.parametrize("kernel", KERNELS)
+@pytest.mark.parametrize("case", ["periodic", "closed"])
+def test_resistivity_vs_oracle(gpu_lib, kernel, case):
+    """MHD_Residual with resistivity: B diffusion, ohmic heating, and (closed
+    case, large eta) the resistive time-step limit; fused and per-routine
+    steps against the oracle (bit-pinned to the reference with eta > 0)."""
+    from oracle import oracle as O
+    tab = initial.EosTable(H.EOS_SMALL)
+    if case == "periodic":
+        nx, ny, nz, eta = 20, 16, 12, 3e10
+        U = initial.periodic_box(tab, nx, ny, nz, seed=23)
+        kw = dict(periodic_x=1, grav=0.0)
+        dx = 3.2e6
+    else:
+        nx, ny, nz, eta = 16, 12, 10, 2e12
+        U = initial.stratified_box(tab, nx, ny, nz, seed=29)
+        kw = dict(periodic_x=0, grav=2.74e4)
+        dx = 1.6e6
+    ref, dts_ref = _oracle_run_p(O.make_params(nx, ny, nz, dx, periodic_x=bool(kw["periodic_x"]), grav=kw["grav"],
+                                               eta=eta), U, 5)
+    p = gpumhd.default_params(nx, ny, nz, dx, stage_kernel=kernel, eta=eta, **kw)
+    g = gpumhd.MuramGPU(p, eos_path=H.EOS_SMALL)
+    g.upload_state(U)
+    dts = g.run_steps(5)
+    assert np.allclose(dts, [d[0] for d in dts_ref], rtol=TOL64, atol=0)
+    check(f"resistivity fused [{case}, kernel={kernel}]", g.download_state(), ref)
+    g.close()
+    g = gpumhd.MuramGPU(gpumhd.default_params(nx, ny, nz, dx, stage_kernel=kernel, eta=eta, **kw),
+                        eos_path=H.EOS_SMALL)
+    g.upload_state(U)
+    g.exchange_grid(True)
+    for _ in range(5):
+        g.step_reference_order()
+    check(f"resistivity per-routine [{case}, kernel={kernel}]", g.download_state(), ref)
+    g.close()
+
+
+def test_resistivity_fp32(gpu_lib):
+    from oracle import oracle as O
+    tab = initial.EosTable(H.EOS_SMALL)
+    U = initial.periodic_box(tab, 32, 32, 32, seed=5)
+    ref, _ = _oracle_run_p(O.make_params(32, 32, 32, 3.2e6, eta=3e10), U, 50)
+    g = gpumhd.MuramGPU(gpumhd.default_params(32, 32, 32, 3.2e6, precision=32, eta=3e10), eos_path=H.EOS_SMALL)
+    g.upload_state(U)
+    g.run_steps(50)
+    e = H.rel_l2(H.interior(g.download_state()), H.interior(ref))
+    print("FP32 with resistivity vs FP64 oracle, rel L2:", np.array2string(e, precision=2))
+    assert np.all(e <= TOL32_L2), e
+    g.close()

@@ -112,3 +112,23 @@ def test_live_reference_random_boxes(seed, eos):
     st = O.State(H.oracle_params(hp), U)
     st.step(eos, 4)
     assert np.array_equal(st.U, ref["final_U"])
+
+
+@pytest.mark.skipif(not refrun.available(), reason="reference harness not built here")
+@pytest.mark.parametrize("eta", [3e10, 2e12])
+def test_live_reference_resistivity(eta, eos):
+    """MHD_Residual with resistivity (Physics.params[i_param_eta] > 0): ohmic
+    heating from the running curl B, the B diffusion term, and the resistive
+    time-step limit (the larger eta sets dt) -- reference and oracle agree bit
+    for bit over several steps, closed x with gravity included."""
+    tab = initial.EosTable(H.EOS_SMALL)
+    U = initial.stratified_box(tab, 10, 8, 6, seed=17)
+    hp = dict(nx=10, ny=8, nz=6, dx=1.6e6, periodic_x=0, grav=2.74e4, eta=eta, eos=H.EOS_SMALL)
+    ref = refrun.run(U, hp, steps=3)
+    st = O.State(H.oracle_params(hp), U)
+    dts = st.step(eos, 3)
+    assert np.array_equal(st.U, ref["final_U"])
+    assert np.array_equal(np.array([d[0] for d in dts]), ref["dts"].reshape(-1, 3)[:, 0])
+    if eta > 1e12:  # dt set by the resistive limit dt_diff_fac / eta
+        dxmin = 1.6e6
+        assert ref["dts"].reshape(-1, 3)[0, 0] <= 0.8 * (dxmin * dxmin / 6.0) / eta * 1.0000001
