@@ -65,6 +65,7 @@ void mo_default_params(mo_params* p, int nx, int ny, int nz, double dx) {
   p->rt_cfl = 0.5; p->rt_tstep = 0.0; p->rt_update = 1;
   p->tau0 = 1.0; p->dt_rad = 1e9;
   p->v_lim = 0.0; p->e_lim = 0.0; p->va_ini_flag = 1;
+  p->divB_next_iter = 3;
 }
 
 /* ---------------------------------------------------------------- EOS load */
@@ -472,10 +473,10 @@ void mo_source_integrate_tcheck(const mo_params* p, double* U, const double* U0,
 /* --------------------------------------------------- ghost fill / boundary */
 /* Periodic fill of the periodic dimensions, in the dimension order and with
  * the growing face ranges of exchange_grid_acc (src/exchange.C:532-783). */
-static void fill_dim(const mo_params* p, const geom* g, double* U, int d, int lo[3], int hi[3]) {
+static void fill_dim_fields(const mo_params* p, const geom* g, double* U, int v0, int v1, int d, int lo[3], int hi[3]) {
   const int n[3] = {p->nx, p->ny, p->nz};
   int idx[3];
-  for (int v = 0; v < NV; v++) {
+  for (int v = v0; v < v1; v++) {
     double* F = U + v * g->N;
     int a0 = d == 0 ? 1 : 0, a1 = d == 2 ? 1 : 2;
     for (idx[a1] = lo[a1]; idx[a1] <= hi[a1]; idx[a1]++)
@@ -487,6 +488,25 @@ static void fill_dim(const mo_params* p, const geom* g, double* U, int d, int lo
           dst[d] = gg; src[d] = n[d] + gg;
           F[at(g, dst[0], dst[1], dst[2])] = F[at(g, src[0], src[1], src[2])];
         }
+  }
+}
+
+static void fill_dim(const mo_params* p, const geom* g, double* U, int d, int lo[3], int hi[3]) {
+  fill_dim_fields(p, g, U, 0, NV, d, lo, hi);
+}
+
+/* exchange of fields v0..v1-1 only (exchange_B_acc, exchange_single_acc:
+ * src/exchange.C:785-983, 985-1150) */
+static void exchange_fields(const mo_params* p, double* U, int v0, int v1) {
+  geom g = geom_of(p);
+  const int n[3] = {p->nx, p->ny, p->nz};
+  int lo[3], hi[3];
+  for (int d = 0; d < 3; d++) { lo[d] = GH; hi[d] = GH + n[d] - 1; }
+  for (int d = 0; d < 3; d++) {
+    if (d == 0 && !p->periodic_x) continue;
+    fill_dim_fields(p, &g, U, v0, v1, d, lo, hi);
+    lo[d] -= GH;
+    hi[d] += GH;
   }
 }
 
@@ -777,8 +797,111 @@ void mo_tcheck(const mo_params* p, double* U) {
       for (int i = GH; i < GH + p->nx; i++) tcheck_cell(p, U, g.N, at(&g, i, j, k));
 }
 
+/* ------------------------------------------------------------- Clean_divB */
+/* Fourth-order divergence of B at interior cell (i, j, k), summed over the
+ * dimensions from zero as src/clean_divB.C:136-156 does. */
+static double divb_cell(const geom* g, const double* U, const double w1[3], const double w2[3], int i, int j, int k) {
+  const long c = at(g, i, j, k);
+  const long st[3] = {1, g->sx, (long)g->sx * g->sy};
+  double d = 0.0;
+  for (int v = 0; v < 3; v++) {
+    const double* B = U + (5 + v) * g->N;
+    const long s = st[v];
+    d += (w1[v] * (B[c + s] - B[c - s]) + w2[v] * (B[c + 2 * s] - B[c - 2 * s]));
+  }
+  return d;
+}
+
+static double divb_pass(const mo_params* p, const geom* g, const double* U, const double w1[3], const double w2[3],
+                        double* divB) {
+  double err = 0.0;
+  for (int k = GH; k < GH + p->nz; k++)
+    for (int j = GH; j < GH + p->ny; j++)
+      for (int i = GH; i < GH + p->nx; i++) {
+        const double d = divb_cell(g, U, w1, w2, i, j, k);
+        divB[at(g, i, j, k)] = d;
+        err = smax(err, fabs(d));
+      }
+  return err;
+}
+
+/* src/clean_divB.C:35-369 on one rank: damped iterations phi += fac*divB -
+ * damp*phi, B += grad(phi), e += phi*divB, with the iteration count adapted
+ * from call to call (next_iter, a function static there, lives in p).  phi
+ * persists between calls; divB receives the last divergence.  A closed x
+ * dimension keeps B's x ghosts as the caller left them (exchange_B_acc does
+ * not fill physical boundaries) and makes phi antisymmetric across it. */
+void mo_clean_divB(mo_params* p, double* U, double* phi, double* divB) {
+  geom g = geom_of(p);
+  const long N = g.N;
+  const int it_max = (int)p->divB_itmax;
+  const double divB_coeff = 1.0, divB_damp = 0.65;
+  double w1[3], w2[3], err_unit = 0.0;
+  for (int v = 0; v < 3; v++) {
+    err_unit += 1.0 / p->dx[v];
+    w1[v] = 8. / (12. * p->dx[v]);
+    w2[v] = -1. / (12. * p->dx[v]);
+  }
+  err_unit = 0.5 / err_unit * 3.5449;
+  double dxmin = smin(p->dx[0], p->dx[1]);
+  double dxmax = smax(p->dx[0], p->dx[1]);
+  dxmin = smin(dxmin, p->dx[2]);
+  dxmax = smax(dxmin, p->dx[2]);  /* as written there: the new dxmin, not dxmax */
+  const double divB_fac = divB_coeff * smin(dxmin, 0.4 * dxmax) * dxmin;
+
+  exchange_fields(p, U, 5, 8);
+  double err0 = divb_pass(p, &g, U, w1, w2, divB), err1 = 0.0;
+  const int n = p->divB_next_iter;
+  const long st[3] = {1, g.sx, (long)g.sx * g.sy};
+  int iter;
+  for (iter = 0; iter < n; iter++) {
+    for (int k = GH; k < GH + p->nz; k++)
+      for (int j = GH; j < GH + p->ny; j++)
+        for (int i = GH; i < GH + p->nx; i++) {
+          const long c = at(&g, i, j, k);
+          phi[c] += divB_fac * divB[c] - divB_damp * phi[c];
+        }
+    exchange_fields(p, phi, 0, 1);
+    if (!p->periodic_x) {
+      const int lb = GH, le = GH + p->nx - 1;
+      for (int k = GH; k < GH + p->nz; k++)
+        for (int j = GH; j < GH + p->ny; j++) {
+          phi[at(&g, lb - 1, j, k)] = -phi[at(&g, lb, j, k)];
+          phi[at(&g, lb - 2, j, k)] = -phi[at(&g, lb + 1, j, k)];
+          phi[at(&g, le + 1, j, k)] = -phi[at(&g, le, j, k)];
+          phi[at(&g, le + 2, j, k)] = -phi[at(&g, le - 1, j, k)];
+        }
+    }
+    for (int k = GH; k < GH + p->nz; k++)
+      for (int j = GH; j < GH + p->ny; j++)
+        for (int i = GH; i < GH + p->nx; i++) {
+          const long c = at(&g, i, j, k);
+          for (int v = 0; v < 3; v++) {
+            const long s = st[v];
+            U[(5 + v) * N + c] += (w1[v] * (phi[c + s] - phi[c - s]) + w2[v] * (phi[c + 2 * s] - phi[c - 2 * s]));
+          }
+          U[4 * N + c] += phi[c] * divB[c];
+        }
+    exchange_fields(p, U, 5, 8);
+    err1 = divb_pass(p, &g, U, w1, w2, divB);
+  }
+  err0 *= err_unit;
+  err1 *= err_unit;
+  const double err = err1 / err0;
+  int next = n;
+  if (err > p->divB_err) next += 1;
+  else next -= 1;
+  next = next < it_max ? next : it_max;
+  next = next > 1 ? next : 1;
+  p->divB_next_iter = next;
+  p->divB_last_iters = iter;
+  p->divB_err0 = err0;
+  p->divB_err1 = err1;
+}
+
 /* --------------------------------------------------------------- full step */
-int mo_step(mo_params* p, const mo_eos* eos, double* U, double* U0, double* R, double* aux5) {
+int mo_step_divb(mo_params* p, const mo_eos* eos, double* U, double* U0, double* R, double* aux5, double* phi,
+                 double* divB) {
   geom g = geom_of(p);
   const long N = g.N;
   double* pres = aux5;
@@ -805,8 +928,16 @@ int mo_step(mo_params* p, const mo_eos* eos, double* U, double* U0, double* R, d
     mo_exchange_only(p, U);
     mo_tvdlimit(p, U, pres, 0.5 * p->dt);
   }
+  if (p->divB_switch > 0) {
+    if (!phi || !divB) return -10;
+    mo_clean_divB(p, U, phi, divB);
+  }
   mo_tcheck(p, U);
   mo_boundaries(p, U);
   p->time += p->dt;
   return 0;
+}
+
+int mo_step(mo_params* p, const mo_eos* eos, double* U, double* U0, double* R, double* aux5) {
+  return mo_step_divb(p, eos, U, U0, R, aux5, NULL, NULL);
 }

@@ -36,6 +36,13 @@ typedef struct {
   int tvd_two_half_steps;
   /* PhysicsData::params[i_param_eta]: resistivity (cm^2/s); 0 = ideal MHD */
   double eta;
+  /* PhysicsData::divB: cleaning on (> 0), iteration cap, target error ratio */
+  int divB_switch, divB_itmax;
+  double divB_err;
+  /* Clean_divB's adaptive iteration count (a function static there, starts
+   * at 3) and the last call's iterations and max|divB| before / after (G) */
+  int divB_next_iter, divB_last_iters;
+  double divB_err0, divB_err1;
 } mo_params;
 
 typedef struct mo_eos mo_eos;
@@ -65,9 +72,15 @@ void mo_exchange_only(const mo_params* p, double* U);
 void mo_tvdlimit(const mo_params* p, double* U, const double* pres, double dt_tvd);
 /* src/Add_Sources_Integrate_SR.C:534-625 */
 void mo_tcheck(const mo_params* p, double* U);
+/* src/clean_divB.C:35-369; phi (N, persists between calls), divB (N) */
+void mo_clean_divB(mo_params* p, double* U, double* phi, double* divB);
 /* One full step in the order of src/solver.C:109-365; returns 0 or a negative error code.
  * Scratch: U0, R (8N each) and pres, temp, ne, rhoi, amb (N each). */
 int mo_step(mo_params* p, const mo_eos* eos, double* U, double* U0, double* R, double* aux5);
+/* The same with divB cleaning after the TVD pass (src/solver.C:341-345) when
+ * p->divB_switch > 0; phi and divB as for mo_clean_divB. */
+int mo_step_divb(mo_params* p, const mo_eos* eos, double* U, double* U0, double* R, double* aux5, double* phi,
+                 double* divB);
 
 #ifdef __cplusplus
 }

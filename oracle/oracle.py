@@ -32,6 +32,9 @@ class MoParams(C.Structure):
         ("inv_va2max", C.c_double), ("v_lim", C.c_double), ("e_lim", C.c_double), ("va_max_old", C.c_double),
         ("va_ini_flag", C.c_int), ("last_cfl", C.c_double), ("tvd_two_half_steps", C.c_int),
         ("eta", C.c_double),
+        ("divB_switch", C.c_int), ("divB_itmax", C.c_int), ("divB_err", C.c_double),
+        ("divB_next_iter", C.c_int), ("divB_last_iters", C.c_int),
+        ("divB_err0", C.c_double), ("divB_err1", C.c_double),
     ]
 
 
@@ -69,6 +72,9 @@ def lib():
         L.mo_tcheck.argtypes = [P, dp]
         L.mo_step.restype = C.c_int
         L.mo_step.argtypes = [P, C.c_void_p, dp, dp, dp, dp]
+        L.mo_clean_divB.argtypes = [P, dp, dp, dp]
+        L.mo_step_divb.restype = C.c_int
+        L.mo_step_divb.argtypes = [P, C.c_void_p, dp, dp, dp, dp, dp, dp]
         _lib = L
     return _lib
 
@@ -105,10 +111,14 @@ def params_from_harness(hp):
     """Build MoParams from the harness key/value dict used by oracle.refrun."""
     kw = {}
     simple = {"CFL": "CFL", "CFL_tvd": "CFL_tvd", "grav": "grav", "va_max": "va_max",
-              "va_adjust": "va_adjust", "max_fill": "max_fill", "tau0": "tau0", "dt_rad": "dt_rad", "eta": "eta"}
+              "va_adjust": "va_adjust", "max_fill": "max_fill", "tau0": "tau0", "dt_rad": "dt_rad", "eta": "eta",
+              "divB_err": "divB_err"}
     for k, a in simple.items():
         if k in hp:
             kw[a] = float(hp[k])
+    for k in ("divB_switch", "divB_itmax"):
+        if k in hp:
+            kw[k] = int(float(hp[k]))
     for k in ("tvd_h", "tvd_cs", "tvd_coeff", "tvd_h_bnd", "tvd_visc_bnd", "tvd_eta_bnd"):
         if k in hp:
             kw[k] = [float(x) for x in hp[k]]
@@ -128,7 +138,10 @@ def params_from_harness(hp):
 
 
 class State:
-    """Scratch buffers for full steps on the oracle."""
+    """Scratch buffers for full steps on the oracle.  With divB cleaning on
+    (p.divB_switch > 0), ``phi`` carries the cleaning potential from step to
+    step, ``divB`` holds the last divergence and ``divb_log`` one entry
+    (iterations, max|divB| before, after) per step."""
 
     def __init__(self, p, U):
         self.p = p
@@ -136,13 +149,18 @@ class State:
         self.U0 = np.zeros_like(self.U)
         self.R = np.zeros_like(self.U)
         self.aux = np.zeros((5,) + self.U.shape[1:])
+        self.phi = np.zeros(self.U.shape[1:])
+        self.divB = np.zeros(self.U.shape[1:])
+        self.divb_log = []
         lib().mo_boundaries(C.byref(p), self.U)
 
     def step(self, eos, n=1):
         dts = []
         for _ in range(n):
-            rc = lib().mo_step(C.byref(self.p), eos.ptr, self.U, self.U0, self.R, self.aux)
+            rc = lib().mo_step_divb(C.byref(self.p), eos.ptr, self.U, self.U0, self.R, self.aux, self.phi, self.divB)
             if rc:
                 raise RuntimeError(f"oracle step failed: {rc}")
             dts.append((self.p.dt, self.p.last_cfl))
+            if self.p.divB_switch > 0:
+                self.divb_log.append((self.p.divB_last_iters, self.p.divB_err0, self.p.divB_err1))
         return dts

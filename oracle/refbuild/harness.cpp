@@ -4,6 +4,9 @@
 // the arrays the GPU path is compared against.  Only tests and the CPU
 // baseline run this program; the product never links it.
 //
+// With divB_switch > 0 the reference's Clean_divB runs after the TVD pass, as
+// in src/solver.C:341-345; phi starts at zero.
+//
 // What the harness supplies around the reference functions:
 //  * RT stub: Qtot = 0, Tau = tau0 everywhere, dt_rad = a large constant
 //    (replaces rts->wrapper, src/solver.C:141);
@@ -37,6 +40,7 @@
 #include "mhd_tvd.H"
 #include "src_int_tck.H"
 #include "exchange.H"
+#include "divB.H"
 
 MPI_Comm cart_comm;  // defined in comm_split.C, which the harness does not need
 
@@ -195,7 +199,9 @@ int main(int argc, char** argv) {
   Physics.tvd[i_tvd_pm_B] = par_d("tvd_pm_B", Physics.tvd[i_tvd_pm_B]);
   Physics.tvd[i_tvd_vmax_lim] = par_d("tvd_vmax_lim", Physics.tvd[i_tvd_vmax_lim]);
   Physics.tvd[i_tvd_CME_thresh] = par_d("tvd_CME_thresh", Physics.tvd[i_tvd_CME_thresh]);
-  Physics.divB[i_divB_switch] = 0;
+  Physics.divB[i_divB_switch] = par_d("divB_switch", 0.0);
+  Physics.divB[i_divB_itmax] = par_d("divB_itmax", 5.0);
+  Physics.divB[i_divB_err] = par_d("divB_err", 0.2);
   Physics.tchk[i_tchk_eps_min] = par_d("tchk_eps_min", Physics.tchk[i_tchk_eps_min]);
   Physics.tchk[i_tchk_rho_min] = par_d("tchk_rho_min", Physics.tchk[i_tchk_rho_min]);
   Physics.tchk[i_tchk_eps_max] = par_d("tchk_eps_max", Physics.tchk[i_tchk_eps_max]);
@@ -208,6 +214,7 @@ int main(int argc, char** argv) {
   Physics.bnd[i_bnd_top] = 0;
 
   Run.Init(0);
+  Run.verbose = par_i("verbose", 0);
   Physics.Init();
   Grid.Init(Run, Physics);
   if (Grid.periods[0]) {  // truly periodic x: no physical x boundary inside the TVD
@@ -223,6 +230,7 @@ int main(int argc, char** argv) {
     Grid.Res[i].zero();
     Grid.U0[i].zero();
     Grid.pres[i] = Grid.temp[i] = Grid.ne[i] = Grid.rhoi[i] = Grid.amb[i] = 0.0;
+    Grid.phi[i] = Grid.divB[i] = 0.0;  // Grid.C:284-285 leaves them unset; the cleaning starts from phi = 0
   }
 
   eos_init(Grid, Run, Physics);
@@ -293,6 +301,11 @@ int main(int argc, char** argv) {
       TVDlimit(Run, Grid, Physics, 0.5 * Run.dt);
     }
     if (tr) dump("tvd_U", Grid.U, ubytes);
+    if (Physics.divB[i_divB_switch] > 0) {  // src/solver.C:341-345
+      if (tr) dump("divb_phi_in", Grid.phi, Grid.bufsize * sizeof(double));
+      Clean_divB(Run, Grid, Physics);
+      if (tr) dump("divb_U", Grid.U, ubytes);
+    }
     TCheck(Run, Grid, Physics);
     if (tr) dump("tck_U", Grid.U, ubytes);
     boundaries(Grid, Physics, 0);
@@ -300,6 +313,10 @@ int main(int argc, char** argv) {
     Run.Advance();
   }
   dump("final_U", Grid.U, ubytes);
+  if (Physics.divB[i_divB_switch] > 0) {
+    dump("final_phi", Grid.phi, Grid.bufsize * sizeof(double));
+    dump("final_divB", Grid.divB, Grid.bufsize * sizeof(double));
+  }
   dump("dts", dts.data(), dts.size() * sizeof(double));
   dump("limits", limits.data(), limits.size() * sizeof(double));
   {

@@ -45,8 +45,9 @@ def run(U, params, steps=1, trace_step=0, keep=None):
 
     ``params`` is a dict of harness keys (nx, ny, nz, dx, dy, dz, eos, CFL, ...).
     Returns a dict of numpy arrays: final_U, dts (per step: dt, cfl, dt_mhd),
-    limits (per step: inv_va2max, v_lim, e_lim) and, for the traced step, the
-    PCAST-style snapshots keyed by name.
+    limits (per step: inv_va2max, v_lim, e_lim), with divB cleaning on
+    final_phi and final_divB, the harness's stdout and, for the traced step,
+    the PCAST-style snapshots keyed by name.
     """
     sz, sy, sx = U.shape[1:]
     p = dict(params)
@@ -67,6 +68,7 @@ def run(U, params, steps=1, trace_step=0, keep=None):
         res = subprocess.run([REF_BIN, pf, sf, od], capture_output=True, text=True)
         if res.returncode != 0:
             raise RuntimeError(f"reference harness failed ({res.returncode}): {res.stderr[-2000:]}")
+        out["stdout"] = res.stdout
         for fn in os.listdir(od):
             path = os.path.join(od, fn)
             if fn.endswith(".txt"):
@@ -78,5 +80,7 @@ def run(U, params, steps=1, trace_step=0, keep=None):
                 a = np.ascontiguousarray(np.moveaxis(a.reshape(sz, sy, sx, 8), -1, 0))
             elif name.endswith("_aux"):
                 a = a.reshape(5, sz, sy, sx)
+            elif name in ("final_phi", "final_divB", "divb_phi_in"):
+                a = a.reshape(sz, sy, sx)
             out[name] = a
     return out

@@ -6,13 +6,18 @@ stores, per case, the initial state and the PCAST-style snapshots around each
 routine of one traced step, the state after several steps, and the per-step
 dt.  The EOS table is the committed ``eos_small.dat``.
 
+The divb_cleaning case also runs the reference's Clean_divB after each TVD
+pass and keeps the cleaning potential phi, the last divergence and the
+iteration count of every step (parsed from the reference's own log line).
+
 Usage (in a checkout with the reference sources available):
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [case ...]     (default: every case)
 """
 from __future__ import annotations
 
 import hashlib
 import os
+import re
 import sys
 
 import numpy as np
@@ -35,37 +40,52 @@ def cases():
         initial.stratified_box(eos, 16, 8, 6, dx=1.6e6, seed=12), dict(steps=3, trace_step=2)
     yield "two_half_tvd", dict(nx=8, ny=8, nz=6, dx=3.2e6, periodic_x=1, CFL=1.2, CFL_tvd=1.0), \
         initial.periodic_box(eos, 8, 8, 6, seed=13, v_rms=3.0e5, b_rms_gauss=400.0), dict(steps=3, trace_step=1)
+    yield "divb_cleaning", dict(nx=10, ny=8, nz=6, dx=1.6e6, dy=1.2e6, dz=1.4e6, periodic_x=0, grav=2.74e4,
+                                divB_switch=1, divB_itmax=4, divB_err=0.15, verbose=1), \
+        initial.stratified_box(eos, 10, 8, 6, dx=1.6e6, seed=14), dict(steps=5, trace_step=2)
 
 
 KEEP = ["init_U", "s1_c2p_U", "s1_c2p_aux", "s1_res_R", "s1_res_dt", "s1_si_U", "s1_bc_U", "s2_c2p_U",
-        "s4_bc_U", "s4_c2p_aux", "tvd_U", "tck_U", "end_U", "final_U", "dts", "limits"]
+        "s4_bc_U", "s4_c2p_aux", "tvd_U", "divb_U", "tck_U", "end_U", "final_U", "dts", "limits",
+        "final_phi", "final_divB"]
+KEEP_DIVB = ["init_U", "tvd_U", "divb_phi_in", "divb_U", "tck_U", "final_U", "dts", "limits", "final_phi",
+             "final_divB"]
 
 
-def main():
+def main(only=()):
     if not refrun.available():
         refrun.build()
-    manifest = []
+    mpath = os.path.join(HERE, "MANIFEST.txt")
+    manifest = {}
+    if os.path.exists(mpath):
+        for line in open(mpath).read().splitlines()[2:]:
+            manifest[line.split(".npz")[0]] = line
     for name, hp, U, run in cases():
+        if only and name not in only:
+            continue
         hp = dict(hp)
         hp["eos"] = EOS
         out = refrun.run(U, hp, **run)
-        arrays = {k: out[k] for k in KEEP if k in out}
+        keep = KEEP_DIVB if hp.get("divB_switch", 0) else KEEP
+        arrays = {k: out[k] for k in keep if k in out}
         arrays["input_U"] = U
         arrays["trace_step"] = np.array(run["trace_step"])
         arrays["steps"] = np.array(run["steps"])
+        if hp.get("divB_switch", 0):
+            arrays["divb_iters"] = np.array([int(m) for m in re.findall(r"divB_max \[(\d+)\]", out["stdout"])])
         meta = {k: v for k, v in hp.items() if k != "eos"}
         for k, v in meta.items():
             arrays["param_" + k] = np.array(v)
         path = os.path.join(HERE, f"{name}.npz")
         np.savez_compressed(path, **arrays)
         h = hashlib.sha256(open(path, "rb").read()).hexdigest()[:16]
-        manifest.append(f"{name}.npz {h} {out['summary'].strip().replace(chr(10), ' ')}")
-        print(manifest[-1])
-    with open(os.path.join(HERE, "MANIFEST.txt"), "w") as fh:
+        manifest[name] = f"{name}.npz {h} {out['summary'].strip().replace(chr(10), ' ')}"
+        print(manifest[name])
+    with open(mpath, "w") as fh:
         fh.write("# golden fixtures from the reference harness (make_golden.py)\n")
         fh.write(f"eos_small.dat {hashlib.sha256(open(EOS, 'rb').read()).hexdigest()}\n")
-        fh.write("\n".join(manifest) + "\n")
+        fh.write("\n".join(manifest.values()) + "\n")
 
 
 if __name__ == "__main__":
-    main()
+    main(tuple(sys.argv[1:]))

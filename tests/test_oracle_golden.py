@@ -67,6 +67,37 @@ def test_routines_bitexact_periodic(eos):
     assert np.array_equal(U, d["end_U"])
 
 
+def test_divb_cleaning_bitexact(eos):
+    """Clean_divB after each TVD pass (closed x, gravity, unequal dx/dy/dz):
+    the state, the cleaning potential phi carried between steps, the last
+    divergence and the adaptive iteration count of every step match the
+    reference bit for bit; and the cleaning alone on the traced step's
+    post-TVD state and incoming phi reproduces the reference's output."""
+    d, hp = H.load_case("divb_cleaning")
+    p = H.oracle_params(hp)
+    st = O.State(p, d["input_U"])
+    dts = st.step(eos, int(d["steps"]))
+    assert [x[0] for x in dts] == list(d["dts"].reshape(-1, 3)[:, 0])
+    assert np.array_equal(st.U, d["final_U"])
+    assert np.array_equal(st.phi, d["final_phi"])
+    assert np.array_equal(st.divB, d["final_divB"])
+    assert [x[0] for x in st.divb_log] == list(d["divb_iters"])
+    assert len(set(d["divb_iters"])) > 1  # the iteration count adapts
+    # one call on the traced step's post-TVD state
+    t = int(d["trace_step"])
+    p2 = H.oracle_params(hp)
+    p2.divB_next_iter = int(d["divb_iters"][t - 1])
+    U = d["tvd_U"].copy()
+    phi = d["divb_phi_in"].copy()
+    divB = np.zeros_like(phi)
+    O.lib().mo_clean_divB(C.byref(p2), U, phi, divB)
+    assert p2.divB_last_iters == d["divb_iters"][t - 1]
+    assert p2.divB_next_iter == d["divb_iters"][t]
+    assert np.array_equal(U, d["divb_U"])
+    O.lib().mo_tcheck(C.byref(p2), U)
+    assert np.array_equal(U, d["tck_U"])
+
+
 def test_eos_interpolation_exact_at_nodes(eos):
     """Known answer: at a table node the bilinear lookup returns exp of the node value."""
     t = initial.EosTable(H.EOS_SMALL)
@@ -112,6 +143,29 @@ def test_live_reference_random_boxes(seed, eos):
     st = O.State(H.oracle_params(hp), U)
     st.step(eos, 4)
     assert np.array_equal(st.U, ref["final_U"])
+
+
+@pytest.mark.skipif(not refrun.available(), reason="reference harness not built here")
+@pytest.mark.parametrize("periodic_x,itmax,err", [(1, 5, 0.2), (0, 1, 0.5), (1, 3, 0.01)])
+def test_live_reference_divb_cleaning(periodic_x, itmax, err, eos):
+    """Clean_divB on periodic and closed boxes, with iteration caps below and
+    above the starting count of 3, against the reference run live."""
+    import re
+    tab = initial.EosTable(H.EOS_SMALL)
+    if periodic_x:
+        U = initial.periodic_box(tab, 12, 8, 10, seed=3)
+        hp = dict(nx=12, ny=8, nz=10, dx=3.2e6, dy=2.4e6, dz=2.0e6)
+    else:
+        U = initial.stratified_box(tab, 10, 8, 6, seed=17)
+        hp = dict(nx=10, ny=8, nz=6, dx=1.6e6, periodic_x=0, grav=2.74e4)
+    hp.update(eos=H.EOS_SMALL, divB_switch=1, divB_itmax=itmax, divB_err=err, verbose=1)
+    ref = refrun.run(U, hp, steps=5)
+    st = O.State(H.oracle_params(hp), U)
+    st.step(eos, 5)
+    assert np.array_equal(st.U, ref["final_U"])
+    assert np.array_equal(st.phi, ref["final_phi"])
+    iters = [int(m) for m in re.findall(r"divB_max \[(\d+)\]", ref["stdout"])]
+    assert [x[0] for x in st.divb_log] == iters
 
 
 @pytest.mark.skipif(not refrun.available(), reason="reference harness not built here")
