@@ -69,6 +69,12 @@ typedef struct gpumhd_params {
    * heating eta*|curl B|^2, and the resistive time-step limit
    * (src/mhdres_SR.C:58-61, 422-450, 741-765, 815-819). */
   double eta;
+  /* PhysicsData::divB (include/physics.H:43-45): divB_switch > 0 runs Clean_divB
+   * after the TVD pass of every fused step (src/solver.C:341-345); divB_itmax caps
+   * its adaptive iteration count, divB_err is the target ratio of max|divB|
+   * after / before the iterations (src/clean_divB.C:35-369). */
+  int divB_switch, divB_itmax;
+  double divB_err;
 } gpumhd_params;
 
 typedef struct gpumhd_ctx gpumhd_ctx;
@@ -92,9 +98,19 @@ int gpumhd_eos_init(gpumhd_ctx* ctx, const char* path);
 
 /* ACCH::UpdateGPU / ACCH::UpdateCPU of the GridData arrays (src/ACCH.C:114-158):
  * which = 0: U, 1: U0, 2: Res (cState arrays, 8 doubles per node);
- * which = 3..7: pres, temp, ne, rhoi, amb (one double per node). */
+ * which = 3..7: pres, temp, ne, rhoi, amb; 8: phi, 9: divB (the divB cleaning's
+ * potential and last divergence, GridData::phi / divB; one double per node). */
 int gpumhd_upload(gpumhd_ctx* ctx, int which, const double* host);
 int gpumhd_download(gpumhd_ctx* ctx, int which, double* host);
+
+/* Clean_divB (include/divB.H:5, src/clean_divB.C:35-369): damped iterations
+ * phi += fac*divB - 0.65*phi, B += grad phi, e += phi*divB on U, their count
+ * adapted from call to call as the reference's function static does (starts
+ * at 3).  phi persists in the context (zero at creation; which = 8 above).
+ * gpumhd_divb_info: the last call's iteration count, the next call's, and
+ * max|divB| before / after it in G (the reference's verbose log line). */
+int gpumhd_clean_divB(gpumhd_ctx* ctx);
+int gpumhd_divb_info(gpumhd_ctx* ctx, int* last_iters, int* next_iters, double* err_before, double* err_after);
 
 /* SaveCons (include/src_int_tck.H:10, src/Add_Sources_Integrate_SR.C:475-531). */
 int gpumhd_save_cons(gpumhd_ctx* ctx);
@@ -136,8 +152,9 @@ int gpumhd_synchronize(gpumhd_ctx* ctx);
 int gpumhd_step_info(gpumhd_ctx* ctx, double* dt, double* cfl, double* time, int* tvd_two_half);
 
 /* Run `nsteps` fused steps without graph capture, timing each launch with CUDA
- * events on the context's stream; ms_phase[11] receives the mean duration of:
- * step control, RK stages 1-4, TVD x/y/z sweeps, second-half TVD x/y/z sweeps. */
+ * events on the context's stream; ms_phase[12] receives the mean duration of:
+ * step control, RK stages 1-4, TVD x/y/z sweeps, second-half TVD x/y/z sweeps,
+ * divB cleaning with the end-of-step pass (0 when divB_switch = 0). */
 int gpumhd_profile_steps(gpumhd_ctx* ctx, int nsteps, double* ms_phase);
 /* MHD_Residual's CFL time step, dt_mhd = dxmin / cmax, computed with no device
  * allocation at all.  No counterpart in the reference: it exists for callers

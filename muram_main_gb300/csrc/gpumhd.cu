@@ -58,6 +58,8 @@ struct gpumhd_ctx {
   // launch shapes of the fused step (0: defaults); set by gpumhd_set_tuning / gpumhd_autotune
   int tune_zc = 0, tune_td = 0;
   void* comp = nullptr;  // FP32 compensated mode: per-cell remainders of the RK update (8N floats)
+  void* phi = nullptr;   // divB cleaning potential (GridData::phi, N), persists between calls
+  void* divb = nullptr;  // last divergence of B (GridData::divB, N)
   char err[1024] = {0};
 };
 
@@ -103,6 +105,7 @@ extern "C" int gpumhd_default_params(gpumhd_params* p, int nx, int ny, int nz, d
   p->tchk[0] = 1.0e11; p->tchk[1] = 1.0e-16; p->tchk[2] = 4.0e15; p->tchk[3] = 100.0e5;
   p->rt_cfl = 0.5; p->rt_tstep = 0.0; p->rt_update = 1;
   p->tau0 = 1.0; p->dt_rad = 1e9;
+  p->divB_switch = 0; p->divB_itmax = 5; p->divB_err = 0.2;  // off; the reference's test settings when on
   return GPUMHD_OK;
 }
 
@@ -131,6 +134,8 @@ static void fill_kc(const Consts& c, KC<R>& k, const R* prof) {
     k.ww1[d] = (R)(16. / (12. * c.dx[d] * c.dx[d]));
     k.ww2[d] = (R)(-1. / (12. * c.dx[d] * c.dx[d]));
   }
+  k.divb_fac = (R)c.divb_fac_d;
+  k.divb_damp = (R)0.65;
   k.hfb = prof; k.hft = prof + c.g.sx; k.qft = prof + 2 * c.g.sx;
   k.has_visc_slope = (c.visc_slope_bot > 0.0 || c.visc_slope_top > 0.0);
   k.has_eta_slope = (c.eta_slope_bot > 0.0 || c.eta_slope_top > 0.0);
@@ -191,6 +196,21 @@ static int fill_consts(gpumhd_ctx* ctx) {
     const double dt_diff_fac = 0.5 / (1. / (p.dx[0] * p.dx[0]) + 1. / (p.dx[1] * p.dx[1]) + 1. / (p.dx[2] * p.dx[2]));
     c.dt_res = dt_diff_fac / p.eta;
     if (p.CFL > 1) c.dt_res *= 0.5;
+  }
+  // divB cleaning constants (src/clean_divB.C:47-101): error unit 0.5/sum(1/dx)*3.5449 and
+  // fac = coeff*min(dxmin, 0.4*dxmax)*dxmin, where dxmax is formed from the updated dxmin
+  c.divb_on = p.divB_switch > 0 ? 1 : 0;
+  c.divb_itmax = p.divB_itmax;
+  c.divb_err = p.divB_err;
+  {
+    double eu = 0.0;
+    for (int d = 0; d < 3; d++) eu += 1.0 / p.dx[d];
+    c.divb_err_unit = 0.5 / eu * 3.5449;
+    double dxmin = stdmin(p.dx[0], p.dx[1]);
+    double dxmax = stdmax(p.dx[0], p.dx[1]);
+    dxmin = stdmin(dxmin, p.dx[2]);
+    dxmax = stdmax(dxmin, p.dx[2]);
+    c.divb_fac_d = 1.0 * stdmin(dxmin, 0.4 * dxmax) * dxmin;
   }
   c.rt_cfl = p.rt_cfl;
   c.CFL = p.CFL; c.CFL_tvd = p.CFL_tvd; c.dt_rad = p.dt_rad; c.rt_tstep = p.rt_tstep; c.outcad = p.outcad;
@@ -338,6 +358,7 @@ extern "C" int gpumhd_create(const gpumhd_params* p, int device, gpumhd_ctx** ou
   if (p->precision != 64 && p->precision != 32) return fail(nullptr, GPUMHD_E_INVALID, "precision must be 32 or 64");
   if (p->stage_kernel != 0 && p->stage_kernel != 1) return fail(nullptr, GPUMHD_E_INVALID, "stage_kernel must be 0 or 1");
   if (!(p->eta >= 0.0)) return fail(nullptr, GPUMHD_E_INVALID, "eta must be >= 0");
+  if (p->divB_switch > 0 && !(p->divB_err >= 0.0)) return fail(nullptr, GPUMHD_E_INVALID, "divB_err must be >= 0");
   if ((long long)(p->nx + 4) * (p->ny + 4) * (p->nz + 4) > GPUMHD_MAX_CELLS)
     return fail(nullptr, GPUMHD_E_INVALID, "grid too large: (nx+4)(ny+4)(nz+4) must not exceed %lld cells",
                 (long long)GPUMHD_MAX_CELLS);
@@ -375,6 +396,7 @@ extern "C" int gpumhd_create(const gpumhd_params* p, int device, gpumhd_ctx** ou
     ctx->hdyn.dt = p->dt;
     ctx->hdyn.time = p->time;
     ctx->hdyn.va_ini_flag = 1;
+    ctx->hdyn.divb_next = 3;  // Clean_divB's static next_iter starts at 3 (src/clean_divB.C:51)
     ctx->hdyn.inv_va2max = 1.0 / pow(p->va_max, 2);
     ctx->hdyn.v_lim = 0.0;
     ctx->hdyn.e_lim = 0.0;
@@ -405,6 +427,8 @@ extern "C" int gpumhd_destroy(gpumhd_ctx* ctx) {
   cudaFree(ctx->T);
   cudaFree(ctx->staging);
   cudaFree(ctx->comp);
+  cudaFree(ctx->phi);
+  cudaFree(ctx->divb);
   cudaFree(ctx->dyn);
   cudaFree(ctx->dt_hist);
   cudaFree(ctx->d_xeps);
@@ -435,8 +459,13 @@ extern "C" int gpumhd_set_params(gpumhd_ctx* ctx, const gpumhd_params* p) {
   if (p->nx != ctx->p.nx || p->ny != ctx->p.ny || p->nz != ctx->p.nz || p->precision != ctx->p.precision ||
       (p->periodic_x != 0) != (ctx->p.periodic_x != 0))
     return fail(ctx, GPUMHD_E_INVALID, "grid shape, boundaries and precision are fixed at creation");
+  if (p->divB_switch > 0 && !(p->divB_err >= 0.0)) return fail(ctx, GPUMHD_E_INVALID, "divB_err must be >= 0");
   CK(cudaSetDevice(ctx->device));
   CK(cudaStreamSynchronize(ctx->stream));
+  {
+    int rc0 = pull_dyn(ctx);  // the device's copy is current (the cleaning's count lives there)
+    if (rc0) return rc0;
+  }
   const Consts keep = ctx->c;
   ctx->p = *p;
   int rc = fill_consts(ctx);
@@ -555,6 +584,14 @@ static void* field_ptr(gpumhd_ctx* ctx, int which, int* nf, int* rc) {
   }
   *nf = 1;
   if (which == 3) return ctx->P[ctx->iP];
+  if (which == 8 || which == 9) {
+    void*& a = which == 8 ? ctx->phi : ctx->divb;
+    if (!a) {
+      if (cudaMalloc(&a, ctx->c.g.N * ctx->rsz) != cudaSuccess) { *rc = GPUMHD_E_NOMEM; return nullptr; }
+      cudaMemsetAsync(a, 0, ctx->c.g.N * ctx->rsz, ctx->stream);
+    }
+    return a;
+  }
   if (which >= 4 && which <= 7) {
     void*& a = ctx->aux[which - 4];
     if (!a) {
@@ -565,6 +602,16 @@ static void* field_ptr(gpumhd_ctx* ctx, int which, int* nf, int* rc) {
   }
   *rc = GPUMHD_E_INVALID;
   return nullptr;
+}
+
+// phi and divB exist (zero-initialised) before the first cleaning.
+static int ensure_divb(gpumhd_ctx* ctx) {
+  int nf, rc;
+  field_ptr(ctx, 8, &nf, &rc);
+  if (rc) return fail(ctx, rc, "allocation of the divB cleaning fields failed");
+  field_ptr(ctx, 9, &nf, &rc);
+  if (rc) return fail(ctx, rc, "allocation of the divB cleaning fields failed");
+  return GPUMHD_OK;
 }
 
 static int ensure_staging(gpumhd_ctx* ctx) {
@@ -790,6 +837,43 @@ extern "C" int gpumhd_tcheck(gpumhd_ctx* ctx) {
 
 // TVDlimit: three in-place sweeps; each sweep reads a copy of the state so that
 // pencil chunks never see a neighbour's partial update.
+// Clean_divB (src/clean_divB.C:35-369): the damped iterations on the
+// context's state with its persistent phi; B's ghosts of the periodic
+// dimensions are refreshed at the end as exchange_B_acc leaves them.
+extern "C" int gpumhd_clean_divB(gpumhd_ctx* ctx) {
+  if (!ctx) return GPUMHD_E_INVALID;
+  CK(cudaSetDevice(ctx->device));
+  int rc = ensure_divb(ctx);
+  if (rc) return rc;
+  Consts c = ctx->c;
+  c.divb_on = 1;
+  int n;
+  if (ctx->f32) {
+    float* U = (float*)ctx->S[ctx->iU];
+    n = Launch<float>::divb_clean(c, U, (float*)ctx->phi, (float*)ctx->divb, ctx->dyn, ctx->stream);
+    Launch<float>::fill_ghosts(c, U + 5 * c.g.N, 3, 0, ctx->stream);
+  } else {
+    double* U = (double*)ctx->S[ctx->iU];
+    n = Launch<double>::divb_clean(c, U, (double*)ctx->phi, (double*)ctx->divb, ctx->dyn, ctx->stream);
+    Launch<double>::fill_ghosts(c, U + 5 * c.g.N, 3, 0, ctx->stream);
+  }
+  rc = check_launch(ctx, n + 1);
+  if (rc) return rc;
+  // the adaptive count lives on the device: bring the host copy up to date
+  CK(cudaStreamSynchronize(ctx->stream));
+  return pull_dyn(ctx);
+}
+
+extern "C" int gpumhd_divb_info(gpumhd_ctx* ctx, int* last_iters, int* next_iters, double* err_before,
+                                double* err_after) {
+  if (!ctx) return GPUMHD_E_INVALID;
+  if (last_iters) *last_iters = ctx->hdyn.divb_last;
+  if (next_iters) *next_iters = ctx->hdyn.divb_next;
+  if (err_before) *err_before = ctx->hdyn.divb_err0;
+  if (err_after) *err_after = ctx->hdyn.divb_err1;
+  return GPUMHD_OK;
+}
+
 extern "C" int gpumhd_tvdlimit(gpumhd_ctx* ctx, double dt_tvd) {
   if (!ctx) return GPUMHD_E_INVALID;
   if (!ctx->have_pres) return fail(ctx, GPUMHD_E_ORDER, "TVDlimit needs the pressure of a ConsToPrim call");
@@ -815,9 +899,20 @@ extern "C" int gpumhd_tvdlimit(gpumhd_ctx* ctx, double dt_tvd) {
 }
 
 // ------------------------------------------------------------- fused path
+// Launches of one fused step: step control, four RK stages, six TVD sweeps;
+// with divB cleaning also the cleaning passes and the end-of-step pass.
+static int step_launches(const gpumhd_ctx* ctx) {
+  int n = 11;
+  if (ctx->c.divb_on) n += 3 + 2 * (ctx->c.divb_itmax > 3 ? ctx->c.divb_itmax : 3) + 1;
+  return n;
+}
+
 // One fused step: step control, four RK stages, two TVD passes (the second
-// returns at once unless the step takes two half passes).  With ev != NULL an
-// event is recorded before each of the 11 launches and after the last.
+// returns at once unless the step takes two half passes), and with divB
+// cleaning on, Clean_divB and the end-of-step pass (TCheck, ghosts, next
+// pressure) that the last TVD sweep leaves to it (src/solver.C:324-350).
+// With ev != NULL an event is recorded before each of the 11 launches, before
+// the cleaning and after the last launch (13 events).
 static int enqueue_one_step(gpumhd_ctx* ctx, cudaEvent_t* ev = nullptr) {
   const Consts& c = ctx->c;
   cudaStream_t s = ctx->stream;
@@ -825,6 +920,7 @@ static int enqueue_one_step(gpumhd_ctx* ctx, cudaEvent_t* ev = nullptr) {
   auto mark = [&]() { if (ev) cudaEventRecord(ev[k++], s); };
   const int a = ctx->iU, b = ctx->iU0, d = ctx->iRes;  // a: state, b and d: work buffers
   const int pa = ctx->iP, pb = 1 - ctx->iP;
+  const int defer = c.divb_on;
   mark();
   k_step_begin<<<1, 32, 0, s>>>(c, ctx->dyn, ctx->dt_hist, ctx->dt_hist_cap);
   if (ctx->f32) {
@@ -849,13 +945,18 @@ static int enqueue_one_step(gpumhd_ctx* ctx, cudaEvent_t* ev = nullptr) {
     mark();
     L::tvd(c, 1, 0, 0, S[d], P[pb], S[b], nullptr, ctx->dyn, s, ctx->tune_td);
     mark();
-    L::tvd(c, 2, 1, 0, S[b], P[pb], S[a], P[pa], ctx->dyn, s, ctx->tune_td);
+    L::tvd(c, 2, 1, 0, S[b], P[pb], S[a], P[pa], ctx->dyn, s, ctx->tune_td, defer);
     mark();
     L::tvd(c, 0, 0, 1, S[a], P[pb], S[d], nullptr, ctx->dyn, s, ctx->tune_td);
     mark();
     L::tvd(c, 1, 0, 1, S[d], P[pb], S[b], nullptr, ctx->dyn, s, ctx->tune_td);
     mark();
-    L::tvd(c, 2, 2, 1, S[b], P[pb], S[a], P[pa], ctx->dyn, s, ctx->tune_td);
+    L::tvd(c, 2, 2, 1, S[b], P[pb], S[a], P[pa], ctx->dyn, s, ctx->tune_td, defer);
+    mark();
+    if (defer) {
+      L::divb_clean(c, S[a], (float*)ctx->phi, (float*)ctx->divb, ctx->dyn, s);
+      L::step_finish(c, S[a], P[pa], ctx->dyn, s);
+    }
   } else {
     using L = Launch<double>;
     double* const* S = (double* const*)ctx->S;
@@ -877,16 +978,21 @@ static int enqueue_one_step(gpumhd_ctx* ctx, cudaEvent_t* ev = nullptr) {
     mark();
     L::tvd(c, 1, 0, 0, S[d], P[pb], S[b], nullptr, ctx->dyn, s, ctx->tune_td);
     mark();
-    L::tvd(c, 2, 1, 0, S[b], P[pb], S[a], P[pa], ctx->dyn, s, ctx->tune_td);
+    L::tvd(c, 2, 1, 0, S[b], P[pb], S[a], P[pa], ctx->dyn, s, ctx->tune_td, defer);
     mark();
     L::tvd(c, 0, 0, 1, S[a], P[pb], S[d], nullptr, ctx->dyn, s, ctx->tune_td);
     mark();
     L::tvd(c, 1, 0, 1, S[d], P[pb], S[b], nullptr, ctx->dyn, s, ctx->tune_td);
     mark();
-    L::tvd(c, 2, 2, 1, S[b], P[pb], S[a], P[pa], ctx->dyn, s, ctx->tune_td);
-  }
+    L::tvd(c, 2, 2, 1, S[b], P[pb], S[a], P[pa], ctx->dyn, s, ctx->tune_td, defer);
     mark();
-  return check_launch(ctx, 11);
+    if (defer) {
+      L::divb_clean(c, S[a], (double*)ctx->phi, (double*)ctx->divb, ctx->dyn, s);
+      L::step_finish(c, S[a], P[pa], ctx->dyn, s);
+    }
+  }
+  mark();
+  return check_launch(ctx, step_launches(ctx));
 }
 
 static int fused_prepare(gpumhd_ctx* ctx, int nsteps) {
@@ -900,6 +1006,10 @@ static int fused_prepare(gpumhd_ctx* ctx, int nsteps) {
     int cap = nsteps < 1024 ? 1024 : nsteps;
     CK(cudaMalloc(&ctx->dt_hist, sizeof(double) * cap));
     ctx->dt_hist_cap = cap;
+  }
+  if (ctx->c.divb_on) {
+    int rc1 = ensure_divb(ctx);
+    if (rc1) return rc1;
   }
   if (ctx->f32 && ctx->p.compensated && !ctx->comp) {
     CK(cudaMalloc(&ctx->comp, sizeof(float) * 8 * ctx->c.g.N));
@@ -942,7 +1052,7 @@ extern "C" int gpumhd_enqueue_steps(gpumhd_ctx* ctx, int nsteps) {
   for (int s = 0; s < nsteps; s++) {
     if (ctx->graph) {
       CK(cudaGraphLaunch(ctx->graph, ctx->stream));
-      ctx->launches += 11;
+      ctx->launches += step_launches(ctx);
     } else {
       rc = enqueue_one_step(ctx);
       if (rc) return rc;
@@ -963,7 +1073,7 @@ static int capture_graph(gpumhd_ctx* ctx) {
   cudaError_t e = cudaStreamEndCapture(ctx->stream, &g);
   if (rc) { if (g) cudaGraphDestroy(g); return rc; }
   if (e != cudaSuccess) return fail(ctx, GPUMHD_E_CUDA, "graph capture: %s", cudaGetErrorString(e));
-  ctx->launches -= 11;  // capture records, it does not launch
+  ctx->launches -= step_launches(ctx);  // capture records, it does not launch
   e = cudaGraphInstantiate(&ctx->graph, g, 0);
   cudaGraphDestroy(g);
   if (e != cudaSuccess) { ctx->graph = nullptr; return fail(ctx, GPUMHD_E_CUDA, "graph instantiate: %s", cudaGetErrorString(e)); }
@@ -1012,20 +1122,20 @@ extern "C" int gpumhd_profile_steps(gpumhd_ctx* ctx, int nsteps, double* ms_phas
   CK(cudaSetDevice(ctx->device));
   int rc = fused_prepare(ctx, nsteps);
   if (rc) return rc;
-  cudaEvent_t ev[12];
-  for (int q = 0; q < 12; q++) CK(cudaEventCreate(&ev[q]));
-  for (int q = 0; q < 11; q++) ms_phase[q] = 0.0;
+  cudaEvent_t ev[13];
+  for (int q = 0; q < 13; q++) CK(cudaEventCreate(&ev[q]));
+  for (int q = 0; q < 12; q++) ms_phase[q] = 0.0;
   for (int st = 0; st < nsteps && rc == 0; st++) {
     rc = enqueue_one_step(ctx, ev);
     if (rc) break;
-    if (cudaEventSynchronize(ev[11]) != cudaSuccess) { rc = fail(ctx, GPUMHD_E_CUDA, "event sync failed"); break; }
-    for (int q = 0; q < 11; q++) {
+    if (cudaEventSynchronize(ev[12]) != cudaSuccess) { rc = fail(ctx, GPUMHD_E_CUDA, "event sync failed"); break; }
+    for (int q = 0; q < 12; q++) {
       float ms = 0.f;
       cudaEventElapsedTime(&ms, ev[q], ev[q + 1]);
       ms_phase[q] += ms / nsteps;
     }
   }
-  for (int q = 0; q < 12; q++) cudaEventDestroy(ev[q]);
+  for (int q = 0; q < 13; q++) cudaEventDestroy(ev[q]);
   if (rc) return rc;
   CK(cudaMemsetAsync(ctx->S[ctx->iRes], 0, 8 * ctx->c.g.N * ctx->rsz, ctx->stream));
   return gpumhd_synchronize(ctx);
@@ -1216,7 +1326,7 @@ static int ensemble_build(gpumhd_ensemble* e) {
     gpumhd_ctx* x = e->box[b];
     cudaStreamWaitEvent(x->stream, e->fork, 0);
     rc = enqueue_one_step(x);
-    x->launches -= 11;  // recorded into the graph, not launched
+    x->launches -= step_launches(x);  // recorded into the graph, not launched
     cudaEventRecord(e->join[b], x->stream);
     cudaStreamWaitEvent(e->stream, e->join[b], 0);
   }
@@ -1289,9 +1399,11 @@ extern "C" int gpumhd_ensemble_enqueue_steps(gpumhd_ensemble* e, int nsteps) {
   for (gpumhd_ctx* x : e->box) {
     ECK(cudaMemsetAsync(x->S[x->iRes], 0, 8 * x->c.g.N * x->rsz, e->stream));
     x->have_pres = true;
-    x->launches += 11LL * nsteps;
+    x->launches += (long long)step_launches(x) * nsteps;
   }
-  e->launches += (11LL * (long long)e->box.size() + 1) * nsteps + 1;
+  long long per_step = 1;
+  for (gpumhd_ctx* x : e->box) per_step += step_launches(x);
+  e->launches += per_step * nsteps + 1;
   ECK(cudaEventRecord(e->done, e->stream));
   for (gpumhd_ctx* x : e->box) ECK(cudaStreamWaitEvent(x->stream, e->done, 0));
   return GPUMHD_OK;
@@ -1352,6 +1464,7 @@ extern "C" int gpumhd_adjoint(gpumhd_ctx* ctx, int nsteps, int checkpoint_every,
   if (ctx->p.autostep) return fail(ctx, GPUMHD_E_INVALID, "adjoint: needs a fixed time step (autostep = 0, dt > 0)");
   if (!(ctx->p.dt > 0.0)) return fail(ctx, GPUMHD_E_INVALID, "adjoint: dt must be positive");
   if (ctx->c.has_eta) return fail(ctx, GPUMHD_E_INVALID, "adjoint: ideal MHD only (eta = 0)");
+  if (ctx->c.divb_on) return fail(ctx, GPUMHD_E_INVALID, "adjoint: without divB cleaning (divB_switch = 0)");
   CK(cudaSetDevice(ctx->device));
   int rc = fused_prepare(ctx, nsteps);
   if (rc) return rc;

@@ -36,6 +36,7 @@ struct KC {
   R CZ, tchk_vmax, tchk_eps_max, gx;
   R w1[3], w2[3];
   R eta, ww0[3], ww1[3], ww2[3];  // resistivity and the second-derivative stencil
+  R divb_fac, divb_damp;          // divB cleaning: phi += fac*divB - damp*phi
   const R* hfb;   // vertical boundary profiles, length sx
   const R* hft;
   const R* qft;
@@ -72,6 +73,9 @@ struct Consts {
   double gx;                   // PhysicsData::g[0] = -grav
   double eta, dt_res;          // resistivity and its time-step limit (eta > 0 only)
   int has_eta, pad3;
+  // divB cleaning (src/clean_divB.C:43-101): on, iteration cap, target ratio, error unit
+  int divb_on, divb_itmax;
+  double divb_err, divb_err_unit, divb_fac_d;
   double rt_cfl;
   double CFL, CFL_tvd, dt_rad, rt_tstep, outcad;
   double va_max, va_adjust, max_fill;
@@ -120,6 +124,14 @@ struct Dyn {
   double dt_mhd;
   DynR<float> rf;
   DynR<double> rd;
+  // divB cleaning: the adaptive iteration count (a function static of
+  // Clean_divB, starts at 3), this call's count, max|divB| before the
+  // iterations and after the latest one (bit patterns, reduced by atomics),
+  // and the last call's errors in G
+  int divb_next, divb_iters;
+  unsigned long long divb_err_bits[2];
+  double divb_err0, divb_err1;
+  int divb_last, divb_pad;
 };
 
 template <class R> __device__ __forceinline__ const DynR<R>& dynr(const Dyn* d);

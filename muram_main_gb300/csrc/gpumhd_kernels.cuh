@@ -620,6 +620,7 @@ struct TvdArgs {
   int na, nb, a0, b0;    // pencil ranges: a fastest (coalesced), b second
   long long sa, sb, sd;  // strides of a, b and along the sweep
   int n1;                // interior cells along the sweep
+  int defer;             // the last pass stores the interior only (k_step_finish ends the step)
 };
 
 // Per-cell quantities from the cell's stored values r (state and pressure)
@@ -807,6 +808,56 @@ __device__ __forceinline__ void tvd_update(const Consts& c, R dtt, const R* Fp, 
   u[4] = smax(u[4], kk_.eps_min * u[0] + (R)0.5 * (u[1] * u[1] + u[2] * u[2] + u[3] * u[3]) / u[0]);
 }
 
+// The end of a step for one interior cell with its updated state u: TCheck,
+// the state's ghost images (closed-x mirror included), and the next step's
+// stage-1 pressure, CFL speed and Adjust_Valf_Max statistics, accumulated in
+// FinishAcc and reduced once per warp by flush().
+template <class R>
+struct FinishAcc {
+  R cmax = (R)0, v = (R)0, cs = (R)0, e = (R)0;
+  unsigned long long nv = 0, ne = 0;
+  __device__ __forceinline__ void flush(Dyn* dyn) {
+    R m = warp_max_nonnan(cmax);
+    R a1 = warp_max_nonnan(v), a2 = warp_max_nonnan(cs), a3 = warp_max_nonnan(e);
+    for (int o = 16; o > 0; o >>= 1) {
+      nv += __shfl_xor_sync(0xffffffffu, nv, o);
+      ne += __shfl_xor_sync(0xffffffffu, ne, o);
+    }
+    if ((threadIdx.x & 31) == 0) {
+      atomic_max_nonneg(&dyn->cmax_bits, (double)m);
+      atomic_max_nonneg(&dyn->stat_max_bits[0], (double)a1);
+      atomic_max_nonneg(&dyn->stat_max_bits[1], (double)a2);
+      atomic_max_nonneg(&dyn->stat_max_bits[2], (double)a3);
+      if (nv) atomicAdd(&dyn->stat_cnt[0], nv);
+      if (ne) atomicAdd(&dyn->stat_cnt[1], ne);
+    }
+  }
+};
+
+template <class R>
+__device__ __forceinline__ void finish_cell(const Consts& c, R* __restrict__ Uout, R* __restrict__ Pout, int ci, int cj,
+                                            int ck, R* u, R vmax, R emax, R inv_va2max, R vlim95, R elim95,
+                                            FinishAcc<R>& acc) {
+  const Geom& g = c.g;
+  tcheck_cell<R>(c, vmax, emax, u[0], u[1], u[2], u[3], u[4]);
+  const Images im = images_of(g, ci, cj, ck, true);
+  store_state<R>(g, Uout, ci, cj, ck, im, u);
+  R v1, v2, v3, ei;
+  prim_from_cons(u[0], u[1], u[2], u[3], u[4], v1, v2, v3, ei);
+  const R pr = eos_pres(c, u[0], ei, (R)1.0 / u[0]);
+  store_scalar<R>(g, Pout, ci, cj, ck, im, pr);
+  R cmv = cmax_cell<R>(u[0], v1, v2, v3, u[5], u[6], u[7], pr, inv_va2max);
+  acc.cmax = smax(acc.cmax, cmv);
+  R vabs = d_sqrt(v1 * v1 + v2 * v2 + v3 * v3);
+  R cs = (R)(5 / 3.) * pr / u[0];
+  R ee = ei / u[0];
+  acc.v = d_fmax(acc.v, vabs);
+  acc.cs = d_fmax(acc.cs, cs);
+  acc.e = d_fmax(acc.e, ee);
+  if (vabs >= vlim95) acc.nv++;
+  if (ee >= elim95) acc.ne++;
+}
+
 template <class R, int DIR>
 __global__ void __launch_bounds__(128) k_tvd_sweep(Consts c, const R* __restrict__ Uin, const R* __restrict__ Pst,
                                                    R* __restrict__ Uout, R* __restrict__ Pout, Dyn* __restrict__ dyn,
@@ -842,10 +893,12 @@ __global__ void __launch_bounds__(128) k_tvd_sweep(Consts c, const R* __restrict
   const R emax = dr.emax;
   const R vlim95 = dr.vlim95, elim95 = dr.elim95;
   const int istart = 1 + (c.g.periodic_x ? 0 : GH);
-  // final pass: TCheck, full ghost images, next step's pressure and statistics;
+  // final pass: TCheck, full ghost images, next step's pressure and statistics
+  // (unless deferred to k_step_finish: then only the interior is stored);
   // half_images: after the first of two half passes only the periodic exchange
-  const bool final_pass = (ta.mode == 2) || (ta.mode == 1 && !dyn->two_half);
+  const bool final_pass = !ta.defer && ((ta.mode == 2) || (ta.mode == 1 && !dyn->two_half));
   const bool half_images = (ta.mode == 1) && dyn->two_half;
+  const bool plain = !final_pass && !half_images;
   R cmax_loc = (R)0;
   R st_v = (R)0, st_c = (R)0, st_e = (R)0;
   unsigned long long cnt_v = 0, cnt_e = 0;
@@ -886,7 +939,7 @@ __global__ void __launch_bounds__(128) k_tvd_sweep(Consts c, const R* __restrict
       // update of cell pos (src/tvdlimit_SR.C:565-657)
       R u[NV];
       tvd_update<R>(c, dtt, F0, Fm, q0, qm, c0, uc, u);
-      if (ta.mode == 0) {
+      if (plain) {
 #pragma unroll
         for (int v = 0; v < NV; v++) Uout[(long long)v * g.N + id] = u[v];
       } else if (half_images) {
@@ -894,6 +947,7 @@ __global__ void __launch_bounds__(128) k_tvd_sweep(Consts c, const R* __restrict
         int ci = DIR == 0 ? pos : aa, cj = DIR == 1 ? pos : (DIR == 0 ? aa : bb), ck = DIR == 2 ? pos : bb;
         store_state<R>(g, Uout, ci, cj, ck, images_of(g, ci, cj, ck, false), u);
       } else if (final_pass) {
+        // finish_cell's work, written out: as a call the FP64 sweep spills more
         tcheck_cell<R>(c, vmax, emax, u[0], u[1], u[2], u[3], u[4]);
         int ci = DIR == 0 ? pos : aa, cj = DIR == 1 ? pos : (DIR == 0 ? aa : bb), ck = DIR == 2 ? pos : bb;
         const Images im = images_of(g, ci, cj, ck, true);
@@ -922,22 +976,9 @@ __global__ void __launch_bounds__(128) k_tvd_sweep(Consts c, const R* __restrict
     }
   }
   if (final_pass) {
-    {
-      R m = warp_max_nonnan(cmax_loc);
-      R a1 = warp_max_nonnan(st_v), a2 = warp_max_nonnan(st_c), a3 = warp_max_nonnan(st_e);
-      for (int o = 16; o > 0; o >>= 1) {
-        cnt_v += __shfl_xor_sync(0xffffffffu, cnt_v, o);
-        cnt_e += __shfl_xor_sync(0xffffffffu, cnt_e, o);
-      }
-      if ((threadIdx.x & 31) == 0) {
-        atomic_max_nonneg(&dyn->cmax_bits, (double)m);
-        atomic_max_nonneg(&dyn->stat_max_bits[0], (double)a1);
-        atomic_max_nonneg(&dyn->stat_max_bits[1], (double)a2);
-        atomic_max_nonneg(&dyn->stat_max_bits[2], (double)a3);
-        if (cnt_v) atomicAdd(&dyn->stat_cnt[0], cnt_v);
-        if (cnt_e) atomicAdd(&dyn->stat_cnt[1], cnt_e);
-      }
-    }
+    FinishAcc<R> acc;
+    acc.cmax = cmax_loc; acc.v = st_v; acc.cs = st_c; acc.e = st_e; acc.nv = cnt_v; acc.ne = cnt_e;
+    acc.flush(dyn);
   }
 }
 

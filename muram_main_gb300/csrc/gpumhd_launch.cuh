@@ -2,6 +2,7 @@
 // unit (FP64 without FMA contraction, FP32 with it).
 #pragma once
 #include "gpumhd_stage_tm.cuh"
+#include "gpumhd_divb.cuh"
 
 namespace gpumhd {
 
@@ -13,6 +14,8 @@ __global__ void k_step_begin(Consts c, Dyn* dyn, double* dt_hist, int dt_hist_ca
 // k_loop_tick at the end of each pass (sets the loop condition).
 __global__ void k_loop_tick(int* counter, cudaGraphConditionalHandle h);
 __global__ void k_set_counter(int* counter, int n);
+__global__ void k_divb_begin(Dyn* dyn);
+__global__ void k_divb_end(Consts c, Dyn* dyn);
 
 template <class R>
 struct Launch {
@@ -25,9 +28,13 @@ struct Launch {
   static void stage(const Consts& c, const R* Uin, const R* Pin, const R* U0, R* Uout, R* Pout, R* Res, Dyn* dyn,
                     int stage, bool resid, int write_pres, cudaStream_t s, const CUtensorMap* mu = nullptr,
                     const CUtensorMap* mp = nullptr, int zc = 0, R* Cc = nullptr);
-  // td: cells per thread along the y / z sweeps (0: 32)
+  // td: cells per thread along the y / z sweeps (0: 32); defer: the last pass
+  // stores the interior only and step_finish ends the step
   static void tvd(const Consts& c, int dir, int mode, int only_two_half, const R* Uin, const R* Pst, R* Uout, R* Pout,
-                  Dyn* dyn, cudaStream_t s, int td = 0);
+                  Dyn* dyn, cudaStream_t s, int td = 0, int defer = 0);
+  // Clean_divB on U (phi, divb: N each); returns the number of launches
+  static int divb_clean(const Consts& c, R* U, R* phi, R* divb, Dyn* dyn, cudaStream_t s);
+  static void step_finish(const Consts& c, R* U, R* P, Dyn* dyn, cudaStream_t s);
   static void cons_to_prim(const Consts& c, R* U, R* P, R* T, R* Ne, R* Ri, R* Am, cudaStream_t s);
   static void init_pass(const Consts& c, const R* U, R* P, Dyn* dyn, cudaStream_t s);
   static void adjust_stats(const Consts& c, const R* U, const R* P, Dyn* dyn, cudaStream_t s);
@@ -144,13 +151,14 @@ void Launch<R>::stage(const Consts& c, const R* Uin, const R* Pin, const R* U0, 
 
 template <class R>
 void Launch<R>::tvd(const Consts& c, int dir, int mode, int only_two_half, const R* Uin, const R* Pst, R* Uout,
-                    R* Pout, Dyn* dyn, cudaStream_t s, int td) {
+                    R* Pout, Dyn* dyn, cudaStream_t s, int td, int defer) {
   const Geom& g = c.g;
   TvdArgs ta;
   ta.dir = dir;
   ta.mode = mode;
   ta.only_two_half = only_two_half;
   ta.td = td > 0 ? td : 32;
+  ta.defer = defer;
   const long long sx = 1, sy = g.sx, sz = (long long)g.sx * g.sy;
   // pencil ranges of TVDlimit's three sweeps (src/tvdlimit_SR.C:199-205, 671-672)
   if (dir == 0) {
@@ -183,6 +191,30 @@ void Launch<R>::tvd(const Consts& c, int dir, int mode, int only_two_half, const
   else k_tvd_sweep<R, 2><<<(unsigned)blocks, block, 0, s>>>(c, Uin, Pst, Uout, Pout, dyn, ta);
 }
 
+template <class R>
+int Launch<R>::divb_clean(const Consts& c, R* U, R* phi, R* divb, Dyn* dyn, cudaStream_t s) {
+  const Geom& g = c.g;
+  const dim3 block(DIVB_BX, DIVB_BY);
+  const int bx = (g.nx + DIVB_BX - 1) / DIVB_BX, by = (g.ny + DIVB_BY - 1) / DIVB_BY;
+  // z chunks: enough blocks for ~16 per SM
+  int nzch = (152 * 16 + bx * by - 1) / (bx * by);
+  nzch = nzch < 1 ? 1 : (nzch > g.nz ? g.nz : nzch);
+  const int zc = (g.nz + nzch - 1) / nzch;
+  const dim3 grid(bx, by, (g.nz + zc - 1) / zc);
+  const int maxit = c.divb_itmax > 3 ? c.divb_itmax : 3;
+  k_divb_begin<<<1, 32, 0, s>>>(dyn);
+  k_divb_div<R><<<grid, block, 0, s>>>(c, U, phi, divb, dyn, 0, zc);
+  for (int it = 0; it < maxit; it++) {
+    k_divb_grad<R><<<grid, block, 0, s>>>(c, U, phi, divb, dyn, it, zc);
+    k_divb_div<R><<<grid, block, 0, s>>>(c, U, phi, divb, dyn, it + 1, zc);
+  }
+  k_divb_end<<<1, 32, 0, s>>>(c, dyn);
+  return 3 + 2 * maxit;
+}
+template <class R>
+void Launch<R>::step_finish(const Consts& c, R* U, R* P, Dyn* dyn, cudaStream_t s) {
+  k_step_finish<R><<<grid_for((long long)c.g.nx * c.g.ny * c.g.nz, 256), 256, 0, s>>>(c, U, P, dyn);
+}
 template <class R>
 void Launch<R>::cons_to_prim(const Consts& c, R* U, R* P, R* T, R* Ne, R* Ri, R* Am, cudaStream_t s) {
   k_cons_to_prim<R><<<grid_for(c.g.N, 256), 256, 0, s>>>(c, U, P, T, Ne, Ri, Am);

@@ -66,4 +66,32 @@ __global__ void k_set_counter(int* counter, int n) {
   if (threadIdx.x == 0) *counter = n;
 }
 
+__global__ void k_divb_begin(Dyn* dyn) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  if (dyn->err) return;
+  dyn->divb_iters = dyn->divb_next;
+  dyn->divb_err_bits[0] = 0ULL;
+  dyn->divb_err_bits[1] = 0ULL;
+}
+
+// Clean_divB: error ratio and the next call's iteration count (src/clean_divB.C:335-354).
+__global__ void k_divb_end(Consts c, Dyn* dyn) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  if (dyn->err) return;
+  const int n = dyn->divb_iters;
+  const double e0 = __longlong_as_double((long long)dyn->divb_err_bits[0]) * c.divb_err_unit;
+  const double e1 = __longlong_as_double((long long)dyn->divb_err_bits[1]) * c.divb_err_unit;
+  const double err = e1 / e0;
+  int next = n;
+  if (err > c.divb_err) next += 1;
+  else next -= 1;
+  next = min(next, c.divb_itmax);
+  next = max(1, next);
+  dyn->divb_next = next;
+  dyn->divb_last = n;
+  dyn->divb_err0 = e0;
+  dyn->divb_err1 = e1;
+}
+
+
 }  // namespace gpumhd

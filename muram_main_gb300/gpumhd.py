@@ -28,7 +28,7 @@ E_CFL = -5
 E_ORDER = -6
 E_NOMEM = -7
 
-FIELD_U, FIELD_U0, FIELD_RES, FIELD_PRES, FIELD_TEMP, FIELD_NE, FIELD_RHOI, FIELD_AMB = range(8)
+FIELD_U, FIELD_U0, FIELD_RES, FIELD_PRES, FIELD_TEMP, FIELD_NE, FIELD_RHOI, FIELD_AMB, FIELD_PHI, FIELD_DIVB = range(10)
 
 
 class GpumhdError(RuntimeError):
@@ -51,6 +51,7 @@ class Params(C.Structure):
         ("tvd_coeff", C.c_double * 4), ("tchk", C.c_double * 4),
         ("rt_cfl", C.c_double), ("rt_tstep", C.c_double), ("rt_update", C.c_double),
         ("tau0", C.c_double), ("dt_rad", C.c_double), ("eta", C.c_double),
+        ("divB_switch", C.c_int), ("divB_itmax", C.c_int), ("divB_err", C.c_double),
     ]
 
 
@@ -64,6 +65,7 @@ EXPORTS = [
     "gpumhd_adjoint", "gpumhd_tile_from", "gpumhd_set_tuning", "gpumhd_get_tuning", "gpumhd_autotune", "gpumhd_ensemble_create",
     "gpumhd_ensemble_destroy", "gpumhd_ensemble_enqueue_steps", "gpumhd_ensemble_synchronize",
     "gpumhd_ensemble_last_error", "gpumhd_ensemble_stream", "gpumhd_ensemble_launch_count",
+    "gpumhd_clean_divB", "gpumhd_divb_info",
 ]
 
 _lib = None
@@ -126,6 +128,8 @@ def load(build_if_missing=True):
         "gpumhd_ensemble_last_error": (C.c_char_p, [vp]),
         "gpumhd_ensemble_stream": (vp, [vp]),
         "gpumhd_ensemble_launch_count": (C.c_longlong, [vp]),
+        "gpumhd_clean_divB": (C.c_int, [vp]),
+        "gpumhd_divb_info": (C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), dp, dp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -252,6 +256,17 @@ class MuramGPU:
     def exchange_grid(self, with_bc=True):
         self._chk(self._L.gpumhd_exchange(self._h, 1 if with_bc else 0))
 
+    def Clean_divB(self):
+        self._chk(self._L.gpumhd_clean_divB(self._h))
+
+    def divb_info(self):
+        """(iterations of the last cleaning, iterations of the next, max|divB|
+        before and after the last cleaning in G)."""
+        a, b = C.c_int(), C.c_int()
+        e0, e1 = C.c_double(), C.c_double()
+        self._chk(self._L.gpumhd_divb_info(self._h, C.byref(a), C.byref(b), C.byref(e0), C.byref(e1)))
+        return a.value, b.value, e0.value, e1.value
+
     def step_reference_order(self, dt_rad=None):
         """One step through the per-routine entry points in ComputeSolution's
         order (src/solver.C:109-365); returns (dt, cfl)."""
@@ -275,6 +290,8 @@ class MuramGPU:
             self.TVDlimit(0.5 * dt)
             self.exchange_grid(False)
             self.TVDlimit(0.5 * dt)
+        if p.divB_switch > 0:
+            self.Clean_divB()
         self.TCheck()
         self.exchange_grid(True)
         return dt, cfl
@@ -327,11 +344,12 @@ class MuramGPU:
         return dt.value, cfl.value, t.value, two.value
 
     PHASES = ["step_control", "stage1", "stage2", "stage3", "stage4", "tvd_x", "tvd_y", "tvd_z",
-              "tvd2_x", "tvd2_y", "tvd2_z"]
+              "tvd2_x", "tvd2_y", "tvd2_z", "divb_clean"]
 
     def profile_steps(self, nsteps=2):
-        """Mean duration (ms) of each launch of a fused step, timed with CUDA events."""
-        ms = np.zeros(11)
+        """Mean duration (ms) of each launch of a fused step, timed with CUDA events
+        (divb_clean: the cleaning passes and the end-of-step pass together)."""
+        ms = np.zeros(12)
         self._chk(self._L.gpumhd_profile_steps(self._h, nsteps, _dptr(ms)))
         return dict(zip(self.PHASES, ms.tolist()))
 

@@ -4,8 +4,8 @@
 // objects of the hot-path routines it defines (src/Makefile:10-42):
 //   cons_to_prim.o (ConsToPrim only; keep eos_init.o for the host EOS tables),
 //   mhdres_SR.o, tvdlimit_SR.o, Add_Sources_Integrate_SR.o, Adjust_Valf_Max.o,
-//   boundary_pdmp_1_fftw3.o (SetBoundaryConditions), the exchange_grid_acc of
-//   exchange.o, and ACCH::UpdateCPU/UpdateGPU of ACCH.o.
+//   boundary_pdmp_1_fftw3.o (SetBoundaryConditions), clean_divB.o (Clean_divB),
+//   the exchange_grid_acc of exchange.o, and ACCH::UpdateCPU/UpdateGPU of ACCH.o.
 // Link with -Wl,--wrap=_Z8eos_initR8GridDataR7RunDataRK11PhysicsData (that is,
 // eos_init): the reference's eos_init still builds the host EOS tables (other
 // host code reads them), and the wrapper then creates the GPU context.  ComputeSolution (src/solver.C) is unchanged: each routine it
@@ -14,10 +14,10 @@
 // Host arrays are refreshed only at ACCH::UpdateCPU, and the device copy
 // only at ACCH::UpdateGPU, as with the reference's OpenACC build.
 //
-// Scope: ideal MHD with the Boris correction, gravity, periodic y/z, periodic
-// or closed x (the OPEN_TOP = 0 mirror rule), constant Tau and Qtot = 0
-// (radiation outside the path).  Every other setting reports an error and
-// aborts, as the reference does on invalid input.
+// Scope: MHD with the Boris correction, gravity, constant resistivity eta,
+// divB cleaning, periodic y/z, periodic or closed x (the OPEN_TOP = 0 mirror
+// rule), constant Tau and Qtot = 0 (radiation outside the path).  Every other
+// setting reports an error and aborts, as the reference does on invalid input.
 #include <mpi.h>
 
 #include <cmath>
@@ -34,6 +34,7 @@
 #include "exchange.H"
 #include "ACCH.h"
 #include "icbc.H"
+#include "divB.H"
 #include "gpumhd.h"
 
 // include/limit_va.H:5 -- defined by Adjust_Valf_Max.C in the reference
@@ -86,6 +87,10 @@ void fill_params(gpumhd_params& p, const RunData& Run, const GridData& Grid, con
   p.rt_tstep = Physics.rt[i_rt_tstep];
   p.rt_update = Physics.rt[i_rt_update];
   p.tau0 = Grid.Tau ? Grid.Tau[0] : 1.0;
+  p.eta = Physics.params[i_param_eta];
+  p.divB_switch = (int)Physics.divB[i_divB_switch];
+  p.divB_itmax = (int)Physics.divB[i_divB_itmax];
+  p.divB_err = Physics.divB[i_divB_err];
 }
 
 const RunData* g_run = nullptr;
@@ -122,8 +127,7 @@ extern "C" void GPUMHD_CAT(__real_, GPUMHD_EOS_INIT_MANGLED)(GridData&, RunData&
 extern "C" void GPUMHD_CAT(__wrap_, GPUMHD_EOS_INIT_MANGLED)(GridData& Grid, RunData& Run,
                                                             const PhysicsData& Physics) {
   GPUMHD_CAT(__real_, GPUMHD_EOS_INIT_MANGLED)(Grid, Run, Physics);
-  if (Physics.params[i_param_spitzer] > 0 || Physics.params[i_param_eta] > 0 ||
-      Physics.params[i_param_ambipolar] > 0 || Run.diagnostics || Physics.dmp[i_dmp_switch] > 0 ||
+  if (Physics.params[i_param_spitzer] > 0 || Physics.params[i_param_ambipolar] > 0 || Run.diagnostics || Physics.dmp[i_dmp_switch] > 0 ||
       Physics.rt_ext[i_ext_cor] > 0 || Grid.procs[0] * Grid.procs[1] * Grid.procs[2] != 1) {
     fprintf(stderr, "gpumhd: configuration outside the GPU path\n");
     MPI_Abort(MPI_COMM_WORLD, 1);
@@ -179,6 +183,10 @@ void TCheck(const RunData& Run, GridData& Grid, const PhysicsData& Physics) {  /
   check("TCheck", gpumhd_tcheck(ctx()));
 }
 
+void Clean_divB(const RunData& Run, GridData& Grid, const PhysicsData& Physics) {  // include/divB.H:5
+  check("Clean_divB", gpumhd_clean_divB(ctx()));
+}
+
 void exchange_grid_acc(GridData& Grid, const PhysicsData& Physics, const int) {  // include/exchange.H:8
   if (!g_ctx) return;  // before eos_init the host state is still authoritative
   check("exchange", gpumhd_exchange(g_ctx, 0));
@@ -205,10 +213,13 @@ void UpdateCPU(void* ptr, std::size_t) {
   else if (ptr == g_grid->ne) check("download ne", gpumhd_download(g_ctx, 5, (double*)ptr));
   else if (ptr == g_grid->rhoi) check("download rhoi", gpumhd_download(g_ctx, 6, (double*)ptr));
   else if (ptr == g_grid->amb) check("download amb", gpumhd_download(g_ctx, 7, (double*)ptr));
+  else if (ptr == g_grid->phi) check("download phi", gpumhd_download(g_ctx, 8, (double*)ptr));
+  else if (ptr == g_grid->divB) check("download divB", gpumhd_download(g_ctx, 9, (double*)ptr));
 }
 void UpdateGPU(void* ptr, std::size_t) {
   if (!g_ctx || !g_grid) return;
   if (ptr == g_grid->U) check("upload U", gpumhd_upload(g_ctx, 0, (const double*)ptr));
   else if (ptr == g_grid->U0) check("upload U0", gpumhd_upload(g_ctx, 1, (const double*)ptr));
+  else if (ptr == g_grid->divB) check("upload divB", gpumhd_upload(g_ctx, 9, (const double*)ptr));
 }
 }  // namespace ACCH

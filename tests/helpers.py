@@ -31,10 +31,15 @@ def oracle_params(hp):
 def gpu_params(hp, precision=64):
     from muram_main_gb300 import gpumhd
     kw = {}
-    for k in ("CFL", "CFL_tvd", "grav"):
+    for k in ("CFL", "CFL_tvd", "grav", "eta", "divB_err"):
         if k in hp:
             kw[k] = float(hp[k])
+    for k in ("divB_switch", "divB_itmax"):
+        if k in hp:
+            kw[k] = int(hp[k])
     dx = float(hp.get("dx", 3.2e6))
+    kw["dy"] = float(hp.get("dy", dx))
+    kw["dz"] = float(hp.get("dz", dx))
     p = gpumhd.default_params(int(hp["nx"]), int(hp["ny"]), int(hp["nz"]), dx, precision=precision,
                               periodic_x=int(hp.get("periodic_x", 1)), **kw)
     return p

@@ -17,7 +17,7 @@ HEADER = os.path.join(H.ROOT, "include", "gpumhd.h")
 
 def header_functions():
     txt = open(HEADER).read()
-    return sorted(set(re.findall(r"\b(gpumhd_[a-z_0-9]+)\s*\(", txt)))
+    return sorted(set(re.findall(r"\b(gpumhd_[A-Za-z_0-9]+)\s*\(", txt)))
 
 
 def test_library_builds_and_exports_header():
