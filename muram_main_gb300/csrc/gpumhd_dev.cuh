@@ -220,6 +220,20 @@ __device__ __forceinline__ R warp_max_nonnan(R v) {
   return v;
 }
 
+// NaN-ignoring maximum over the block (values >= 0), valid in thread 0;
+// every thread of the block calls it.
+template <class R>
+__device__ __forceinline__ R block_max_nonnan(R v) {
+  __shared__ R sw[32];
+  v = warp_max_nonnan(v);
+  const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+  const int nw = (blockDim.x * blockDim.y * blockDim.z + 31) >> 5;
+  if ((tid & 31) == 0) sw[tid >> 5] = v;
+  __syncthreads();
+  if (tid < 32) v = warp_max_nonnan(tid < nw ? sw[tid] : (R)0);
+  return v;
+}
+
 // ------------------------------------------------------------------- EOS
 struct C2POut {
   double pres, temp, ne, rhoi, amb;

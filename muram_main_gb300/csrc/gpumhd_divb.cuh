@@ -84,30 +84,41 @@ __global__ void __launch_bounds__(DIVB_BX* DIVB_BY) k_divb_div(Consts c, const R
     const R* By = U + 6u * g.N32;
     const R* Bz = U + 7u * g.N32;
     const unsigned col = (unsigned)i + (unsigned)j * sy;
+    // one plane's loads (B_x along the row, B_y along the column, the next
+    // B_z of the z window, phi) are issued a plane ahead of their use
+    struct In { R x[4], y[4], z, ph; };
+    auto load = [&](int k, In& v) {
+      const unsigned pl = (unsigned)k * sz;
+      const unsigned row = pl + (unsigned)j * sy;
+      v.x[0] = Bx[row + xm2]; v.x[1] = Bx[row + xm1]; v.x[2] = Bx[row + xp1]; v.x[3] = Bx[row + xp2];
+      v.y[0] = By[pl + ym2 + i]; v.y[1] = By[pl + ym1 + i]; v.y[2] = By[pl + yp1 + i]; v.y[3] = By[pl + yp2 + i];
+      v.z = Bz[col + (unsigned)wrap_i(k, 2, g.nz) * sz];
+      v.ph = upd ? phi[row + (unsigned)i] : (R)0;
+    };
     R zm2 = Bz[col + (unsigned)wrap_i(k0, -2, g.nz) * sz];
     R zm1 = Bz[col + (unsigned)wrap_i(k0, -1, g.nz) * sz];
     R z0 = Bz[col + (unsigned)k0 * sz];
     R zp1 = Bz[col + (unsigned)wrap_i(k0, 1, g.nz) * sz];
+    In cur;
+    load(k0, cur);
     for (int k = k0; k < k1; k++) {
-      const R zp2 = Bz[col + (unsigned)wrap_i(k, 2, g.nz) * sz];
-      const unsigned pl = (unsigned)k * sz;
-      const unsigned row = pl + (unsigned)j * sy;
+      In nxt;
+      if (k + 1 < k1) load(k + 1, nxt);
+      const R zp2 = cur.z;
       R d = (R)0;
-      d += (w1x * (Bx[row + xp1] - Bx[row + xm1]) + w2x * (Bx[row + xp2] - Bx[row + xm2]));
-      d += (w1y * (By[pl + yp1 + i] - By[pl + ym1 + i]) + w2y * (By[pl + yp2 + i] - By[pl + ym2 + i]));
+      d += (w1x * (cur.x[2] - cur.x[1]) + w2x * (cur.x[3] - cur.x[0]));
+      d += (w1y * (cur.y[2] - cur.y[1]) + w2y * (cur.y[3] - cur.y[0]));
       d += (w1z * (zp1 - zm1) + w2z * (zp2 - zm2));
-      const unsigned id = row + (unsigned)i;
+      const unsigned id = (unsigned)k * sz + col;
       divb[id] = d;
-      if (upd) {
-        const R ph = phi[id];
-        phi[id] = ph + (fac * d - damp * ph);
-      }
+      if (upd) phi[id] = cur.ph + (fac * d - damp * cur.ph);
       err = smax(err, d_fabs(d));  // std::max semantics: a NaN divergence is skipped
       zm2 = zm1; zm1 = z0; z0 = zp1; zp1 = zp2;
+      cur = nxt;
     }
   }
-  const R m = warp_max_nonnan(err);
-  if (((threadIdx.y * DIVB_BX + threadIdx.x) & 31) == 0) atomic_max_nonneg(&dyn->divb_err_bits[q == 0 ? 0 : 1], (double)m);
+  const R m = block_max_nonnan(err);  // one atomic per block
+  if (threadIdx.x == 0 && threadIdx.y == 0) atomic_max_nonneg(&dyn->divb_err_bits[q == 0 ? 0 : 1], (double)m);
 }
 
 // Gradient pass of iteration it: B_v += w1*(phi[+1]-phi[-1]) + w2*(phi[+2]-phi[-2])
@@ -140,25 +151,39 @@ __global__ void __launch_bounds__(DIVB_BX* DIVB_BY) k_divb_grad(Consts c, R* __r
   R* By = U + 6u * g.N32;
   R* Bz = U + 7u * g.N32;
   const unsigned col = (unsigned)i + (unsigned)j * sy;
+  // one plane's loads issued a plane ahead of their use
+  struct In { R x[4], y[4], pz, bx, by, bz, e, dv; };
+  auto load = [&](int k, In& v) {
+    const unsigned pl = (unsigned)k * sz;
+    const unsigned row = pl + (unsigned)j * sy;
+    const unsigned id = row + (unsigned)i;
+    v.x[0] = phi[row + xm2]; v.x[1] = phi[row + xm1]; v.x[2] = phi[row + xp1]; v.x[3] = phi[row + xp2];
+    v.y[0] = phi[pl + ym2 + i]; v.y[1] = phi[pl + ym1 + i]; v.y[2] = phi[pl + yp1 + i]; v.y[3] = phi[pl + yp2 + i];
+    v.pz = phi[col + (unsigned)wrap_i(k, 2, g.nz) * sz];
+    v.bx = Bx[id]; v.by = By[id]; v.bz = Bz[id]; v.e = E[id]; v.dv = divb[id];
+  };
   R pm2 = phi[col + (unsigned)wrap_i(k0, -2, g.nz) * sz];
   R pm1 = phi[col + (unsigned)wrap_i(k0, -1, g.nz) * sz];
   R p0 = phi[col + (unsigned)k0 * sz];
   R pp1 = phi[col + (unsigned)wrap_i(k0, 1, g.nz) * sz];
+  In cur;
+  load(k0, cur);
   for (int k = k0; k < k1; k++) {
-    const R pp2 = phi[col + (unsigned)wrap_i(k, 2, g.nz) * sz];
-    const unsigned pl = (unsigned)k * sz;
-    const unsigned row = pl + (unsigned)j * sy;
-    const unsigned id = row + (unsigned)i;
-    R a2 = phi[row + xm2], a1 = phi[row + xm1], b1 = phi[row + xp1], b2 = phi[row + xp2];
+    In nxt;
+    if (k + 1 < k1) load(k + 1, nxt);
+    const R pp2 = cur.pz;
+    const unsigned id = (unsigned)k * sz + col;
+    R a2 = cur.x[0], a1 = cur.x[1], b1 = cur.x[2], b2 = cur.x[3];
     if (nm2) a2 = -a2;
     if (nm1) a1 = -a1;
     if (np1) b1 = -b1;
     if (np2) b2 = -b2;
-    Bx[id] = Bx[id] + (w1x * (b1 - a1) + w2x * (b2 - a2));
-    By[id] = By[id] + (w1y * (phi[pl + yp1 + i] - phi[pl + ym1 + i]) + w2y * (phi[pl + yp2 + i] - phi[pl + ym2 + i]));
-    Bz[id] = Bz[id] + (w1z * (pp1 - pm1) + w2z * (pp2 - pm2));
-    E[id] = E[id] + p0 * divb[id];
+    Bx[id] = cur.bx + (w1x * (b1 - a1) + w2x * (b2 - a2));
+    By[id] = cur.by + (w1y * (cur.y[2] - cur.y[1]) + w2y * (cur.y[3] - cur.y[0]));
+    Bz[id] = cur.bz + (w1z * (pp1 - pm1) + w2z * (pp2 - pm2));
+    E[id] = cur.e + p0 * cur.dv;
     pm2 = pm1; pm1 = p0; p0 = pp1; pp1 = pp2;
+    cur = nxt;
   }
 }
 

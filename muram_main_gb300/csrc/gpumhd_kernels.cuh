@@ -816,20 +816,46 @@ template <class R>
 struct FinishAcc {
   R cmax = (R)0, v = (R)0, cs = (R)0, e = (R)0;
   unsigned long long nv = 0, ne = 0;
+  // Warp reductions, then lane 0 of each warp parks its values in shared
+  // memory and warp 0 combines them: one atomic per statistic and block
+  // (same-address atomics from every warp serialise in L2).  Every thread of
+  // the block calls this.
   __device__ __forceinline__ void flush(Dyn* dyn) {
-    R m = warp_max_nonnan(cmax);
+    __shared__ R sr[32][4];
+    __shared__ unsigned long long sn[32][2];
+    R a0 = warp_max_nonnan(cmax);
     R a1 = warp_max_nonnan(v), a2 = warp_max_nonnan(cs), a3 = warp_max_nonnan(e);
     for (int o = 16; o > 0; o >>= 1) {
       nv += __shfl_xor_sync(0xffffffffu, nv, o);
       ne += __shfl_xor_sync(0xffffffffu, ne, o);
     }
-    if ((threadIdx.x & 31) == 0) {
-      atomic_max_nonneg(&dyn->cmax_bits, (double)m);
-      atomic_max_nonneg(&dyn->stat_max_bits[0], (double)a1);
-      atomic_max_nonneg(&dyn->stat_max_bits[1], (double)a2);
-      atomic_max_nonneg(&dyn->stat_max_bits[2], (double)a3);
-      if (nv) atomicAdd(&dyn->stat_cnt[0], nv);
-      if (ne) atomicAdd(&dyn->stat_cnt[1], ne);
+    const int tid = threadIdx.x + blockDim.x * (threadIdx.y + blockDim.y * threadIdx.z);
+    const int nw = (blockDim.x * blockDim.y * blockDim.z + 31) >> 5;
+    const int w = tid >> 5, lane = tid & 31;
+    if (lane == 0) {
+      sr[w][0] = a0; sr[w][1] = a1; sr[w][2] = a2; sr[w][3] = a3;
+      sn[w][0] = nv; sn[w][1] = ne;
+    }
+    __syncthreads();
+    if (w == 0) {
+      const bool h = lane < nw;
+      a0 = warp_max_nonnan(h ? sr[lane][0] : (R)0);
+      a1 = warp_max_nonnan(h ? sr[lane][1] : (R)0);
+      a2 = warp_max_nonnan(h ? sr[lane][2] : (R)0);
+      a3 = warp_max_nonnan(h ? sr[lane][3] : (R)0);
+      unsigned long long c0 = h ? sn[lane][0] : 0ULL, c1 = h ? sn[lane][1] : 0ULL;
+      for (int o = 16; o > 0; o >>= 1) {
+        c0 += __shfl_xor_sync(0xffffffffu, c0, o);
+        c1 += __shfl_xor_sync(0xffffffffu, c1, o);
+      }
+      if (lane == 0) {
+        atomic_max_nonneg(&dyn->cmax_bits, (double)a0);
+        atomic_max_nonneg(&dyn->stat_max_bits[0], (double)a1);
+        atomic_max_nonneg(&dyn->stat_max_bits[1], (double)a2);
+        atomic_max_nonneg(&dyn->stat_max_bits[2], (double)a3);
+        if (c0) atomicAdd(&dyn->stat_cnt[0], c0);
+        if (c1) atomicAdd(&dyn->stat_cnt[1], c1);
+      }
     }
   }
 };
