@@ -39,6 +39,9 @@
 
 // include/limit_va.H:5 -- defined by Adjust_Valf_Max.C in the reference
 double inv_va2max, v_lim = 0.0, e_lim = 0.0;
+// the open bottom's pressure and entropy (src/boundary_pdmp_1_fftw3.C:31; read
+// from backup.dat by ReadBackupFile, negative: set from the first boundary call)
+double p_bc, s_bc;
 
 namespace {
 

@@ -34,6 +34,10 @@ struct mo_eos {
   double del_eps, del_lr, inv_del_eps, inv_del_lr, eps_off, ss_off;
   double *xeps, *xlr;
   float* tab[6]; /* [i_eps*N_lr + j_rho]: ln p, ln T, s, ln ne, ln rhoi, ln amb (pre-divided) */
+  /* inverse tables over (ln p, s): [i_lp*N_s3 + j_s], ln eps and ln rho (pre-divided) */
+  double del_lp3, del_s3, inv_del_lp3, inv_del_s3;
+  double *xlp3, *xs3;
+  float *eps3, *d3;
 };
 
 /* Geometry helpers */
@@ -66,6 +70,9 @@ void mo_default_params(mo_params* p, int nx, int ny, int nz, double dx) {
   p->tau0 = 1.0; p->dt_rad = 1e9;
   p->v_lim = 0.0; p->e_lim = 0.0; p->va_ini_flag = 1;
   p->divB_next_iter = 3;
+  p->bnd_bcrit = 1.0e10;
+  p->p_bc = -1.0; p->s_bc = -1.0;
+  p->bnd_ini = 1;
 }
 
 /* ---------------------------------------------------------------- EOS load */
@@ -94,7 +101,6 @@ mo_eos* mo_eos_load(const char* path) {
   if (fread(buf, sizeof(float), 6 * n, f) != (size_t)(6 * n)) {
     free(buf); fclose(f); mo_eos_free(e); return NULL;
   }
-  fclose(f);
   const double scale = e->del_eps * e->del_lr;
   for (int t = 0; t < 6; t++) {
     e->tab[t] = (float*)malloc(sizeof(float) * n);
@@ -103,6 +109,32 @@ mo_eos* mo_eos_load(const char* path) {
         e->tab[t][(long)i * e->N_lr + j] = (float)(((double)buf[t * n + (long)j * e->N_eps + i]) / scale);
   }
   free(buf);
+  /* inverse tables (src/eos_init.C:120-136, 181-198); missing ones leave them unset */
+  const double lp0 = (double)h[8], lp1 = (double)h[9], s0 = (double)h[10], s1 = (double)h[11];
+  e->del_lp3 = (lp1 - lp0) / ((double)(e->N_lp3 - 1));
+  e->del_s3 = (s1 - s0) / ((double)(e->N_s3 - 1));
+  e->inv_del_lp3 = 1.0 / e->del_lp3;
+  e->inv_del_s3 = 1.0 / e->del_s3;
+  const long n3 = (long)e->N_lp3 * e->N_s3;
+  if (n3 > 0) {
+    float* b3 = (float*)malloc(sizeof(float) * 2 * n3);
+    if (fread(b3, sizeof(float), 2 * n3, f) == (size_t)(2 * n3)) {
+      e->xlp3 = (double*)malloc(sizeof(double) * e->N_lp3);
+      e->xs3 = (double*)malloc(sizeof(double) * e->N_s3);
+      for (int i = 0; i < e->N_lp3; i++) e->xlp3[i] = lp0 + e->del_lp3 * ((double)i);
+      for (int i = 0; i < e->N_s3; i++) e->xs3[i] = s0 + e->del_s3 * ((double)i);
+      e->eps3 = (float*)malloc(sizeof(float) * n3);
+      e->d3 = (float*)malloc(sizeof(float) * n3);
+      const double sc3 = e->del_lp3 * e->del_s3;
+      for (int i = 0; i < e->N_lp3; i++)
+        for (int j = 0; j < e->N_s3; j++) {
+          e->eps3[(long)i * e->N_s3 + j] = (float)(((double)b3[(long)j * e->N_lp3 + i]) / sc3);
+          e->d3[(long)i * e->N_s3 + j] = (float)(((double)b3[n3 + (long)j * e->N_lp3 + i]) / sc3);
+        }
+    }
+    free(b3);
+  }
+  fclose(f);
   return e;
 }
 
@@ -110,6 +142,7 @@ void mo_eos_free(mo_eos* e) {
   if (!e) return;
   free(e->xeps); free(e->xlr);
   for (int t = 0; t < 6; t++) free(e->tab[t]);
+  free(e->xlp3); free(e->xs3); free(e->eps3); free(e->d3);
   free(e);
 }
 
@@ -797,6 +830,181 @@ void mo_tcheck(const mo_params* p, double* U) {
       for (int i = GH; i < GH + p->nx; i++) tcheck_cell(p, U, g.N, at(&g, i, j, k));
 }
 
+/* ------------------------------------------------- physical x boundaries */
+/* Scalar EOS lookups of src/eos_init.C (their bilinear terms are summed in
+ * another order than ConsToPrim's): p_interp :319-343, s_interp :268-292,
+ * d3_interp :216-240, eps3_interp :242-266. */
+static double eos_fwd(const mo_eos* e, int t, double ee, double dd) {
+  const double ee1 = log(ee + e->eps_off);
+  const double logr = log(dd);
+  int i = (int)((ee1 - e->xeps[0]) * e->inv_del_eps);
+  if (i < 0) i = 0;
+  if (i > e->N_eps - 2) i = e->N_eps - 2;
+  int j = (int)((logr - e->xlr[0]) * e->inv_del_lr);
+  if (j < 0) j = 0;
+  if (j > e->N_lr - 2) j = e->N_lr - 2;
+  const float* T = e->tab[t];
+  const long L = e->N_lr;
+  return (logr - e->xlr[j]) * (ee1 - e->xeps[i]) * (double)T[(i + 1) * L + j + 1] +
+         (logr - e->xlr[j]) * (e->xeps[i + 1] - ee1) * (double)T[i * L + j + 1] +
+         (e->xlr[j + 1] - logr) * (ee1 - e->xeps[i]) * (double)T[(i + 1) * L + j] +
+         (e->xlr[j + 1] - logr) * (e->xeps[i + 1] - ee1) * (double)T[i * L + j];
+}
+static double eos_p_interp(const mo_eos* e, double ee, double dd) { return exp(eos_fwd(e, 0, ee, dd)); }
+static double eos_s_interp(const mo_eos* e, double ee, double dd) { return eos_fwd(e, 2, ee, dd) - e->ss_off; }
+static double eos_inv(const mo_eos* e, const float* T, double pp, double ss) {
+  const double ss1 = ss + e->ss_off;
+  const double logp = log(pp);
+  int i = (int)((logp - e->xlp3[0]) * e->inv_del_lp3);
+  if (i < 0) i = 0;
+  if (i > e->N_lp3 - 2) i = e->N_lp3 - 2;
+  int j = (int)((ss1 - e->xs3[0]) * e->inv_del_s3);
+  if (j < 0) j = 0;
+  if (j > e->N_s3 - 2) j = e->N_s3 - 2;
+  const long L = e->N_s3;
+  return (logp - e->xlp3[i]) * (ss1 - e->xs3[j]) * (double)T[(i + 1) * L + j + 1] +
+         (logp - e->xlp3[i]) * (e->xs3[j + 1] - ss1) * (double)T[(i + 1) * L + j] +
+         (e->xlp3[i + 1] - logp) * (ss1 - e->xs3[j]) * (double)T[i * L + j + 1] +
+         (e->xlp3[i + 1] - logp) * (e->xs3[j + 1] - ss1) * (double)T[i * L + j];
+}
+static double eos_d3_interp(const mo_eos* e, double pp, double ss) { return exp(eos_inv(e, e->d3, pp, ss)); }
+static double eos_eps3_interp(const mo_eos* e, double pp, double ss) {
+  return exp(eos_inv(e, e->eps3, pp, ss)) - e->eps_off;
+}
+
+/* set_p_s_bc (src/boundary_pdmp_1_fftw3.C:496-565): p_bc from the mean
+ * pressures of the two bottom layers, s_bc from the mean entropy of the
+ * upflows (or of all cells) of the first one; only the negative ones are set. */
+static void set_p_s_bc(mo_params* p, const mo_eos* e, const double* U) {
+  geom g = geom_of(p);
+  const long N = g.N;
+  double b0 = 0, b1 = 0, b2 = 0, b3 = 0, b4 = 0;
+  for (int k = GH; k < GH + p->nz; k++)
+    for (int j = GH; j < GH + p->ny; j++) {
+      const long c1 = at(&g, GH, j, k), c2 = at(&g, GH + 1, j, k);
+      const double d1 = U[c1], d2 = U[c2];
+      const double m1 = U[N + c1], m2 = U[2 * N + c1], m3 = U[3 * N + c1];
+      const double q1 = U[N + c2], q2 = U[2 * N + c2], q3 = U[3 * N + c2];
+      const double e1 = U[4 * N + c1] - 0.5 * (m1 * m1 + m2 * m2 + m3 * m3) / d1;
+      const double e2 = U[4 * N + c2] - 0.5 * (q1 * q1 + q2 * q2 + q3 * q3) / d2;
+      const double eps1 = e1 / d1, eps2 = e2 / d2;
+      b0 += eos_p_interp(e, eps1, d1);
+      b1 += eos_p_interp(e, eps2, d2);
+      if (m1 > 0.0) {
+        b2 += 1.0;
+        b3 += eos_s_interp(e, eps1, d1);
+      }
+      b4 += eos_s_interp(e, eps1, d1);
+    }
+  const double n = (double)(p->ny * p->nz);
+  b0 /= n;
+  b1 /= n;
+  if (p->p_bc < 0.0) p->p_bc = b0 * sqrt(b0 / b1);
+  if (p->s_bc < 0.0) p->s_bc = (b2 > 0.0) ? b3 / b2 : b4 / n;
+}
+
+/* SetBoundaryConditions (src/boundary_pdmp_1_fftw3.C:81-493) without the
+ * potential-field top: at the bottom, ghost pressures extrapolated
+ * exponentially from the mean pressure of the two first layers to p_bc with
+ * their fluctuations damped (p1_dmp = 0.8), entropy s_bc in upflows and the
+ * cell's own entropy in downflows, density and energy from the inverse EOS,
+ * momentum scaled down where |B_x| nears B_crit; at the top, M_x mirrored
+ * (always, or only in downflows with bnd_top = 1), B_y and B_z mirrored, and
+ * the internal energy fixed at eps_top when it is positive.  Covers the y and
+ * z ghost columns too; the caller has exchanged the periodic dimensions. */
+static void set_boundary_conditions(mo_params* p, const mo_eos* e, double* U) {
+  geom g = geom_of(p);
+  const long N = g.N;
+  const int lb = GH, le = GH + p->nx - 1;
+  const double p1_dmp = 0.8;
+  const double B_crit = p->bnd_bcrit / sqrt(8.0 * asin(1.0));
+  if (p->bnd_ini) {
+    if ((p->p_bc < 0.0) || (p->s_bc < 0.0)) set_p_s_bc(p, e, U);
+    p->bnd_ini = 0;
+  }
+  double l5 = 0, l6 = 0;
+  for (int k = GH; k < GH + p->nz; k++)
+    for (int j = GH; j < GH + p->ny; j++) {
+      const long c1 = at(&g, lb, j, k), c2 = at(&g, lb + 1, j, k);
+      const double d1 = U[c1], d2 = U[c2];
+      const double m1 = U[N + c1], m2 = U[2 * N + c1], m3 = U[3 * N + c1];
+      const double q1 = U[N + c2], q2 = U[2 * N + c2], q3 = U[3 * N + c2];
+      const double e1 = U[4 * N + c1] - 0.5 * ((m1 * m1 + m2 * m2 + m3 * m3) / d1);
+      const double e2 = U[4 * N + c2] - 0.5 * ((q1 * q1 + q2 * q2 + q3 * q3) / d2);
+      l5 += eos_p_interp(e, e1 / d1, d1);
+      l6 += eos_p_interp(e, e2 / d2, d2);
+    }
+  const double cn = 1.0 / ((double)(p->ny * p->nz));
+  const double pmean1 = l5 * cn, pmean2 = l6 * cn;
+  for (int k = 0; k < g.sz; k++)
+    for (int j = 0; j < g.sy; j++) {
+      const long c1 = at(&g, lb, j, k), c2 = at(&g, lb + 1, j, k);
+      double u1[NV], u2[NV];
+      for (int v = 0; v < NV; v++) { u1[v] = U[v * N + c1]; u2[v] = U[v * N + c2]; }
+      u1[4] -= 0.5 * (u1[1] * u1[1] + u1[2] * u1[2] + u1[3] * u1[3]) / u1[0];
+      u2[4] -= 0.5 * (u2[1] * u2[1] + u2[2] * u2[2] + u2[3] * u2[3]) / u2[0];
+      double eps1 = u1[4] / u1[0], eps2 = u2[4] / u2[0];
+      const double pmag = 0.5 * u1[5] * u1[5];
+      const double pmin1 = eos_p_interp(e, eps1, u1[0]) - pmean1;
+      const double pmin2 = eos_p_interp(e, eps2, u2[0]) - pmean2;
+      const double smin1 = eos_s_interp(e, eps1, u1[0]);
+      const double smin2 = eos_s_interp(e, eps2, u2[0]);
+      double s1, s2;
+      if (u1[1] >= 0.e0) { s1 = p->s_bc; s2 = p->s_bc; }
+      else { s1 = smin1; s2 = smin2; }
+      double c = p->p_bc / sqrt(pmean1 * pmean2);
+      double p1 = pmean1 * c;
+      double p2 = pmean1 * c * c;
+      p1 += pmin1 * p1_dmp;
+      p2 += pmin1 * p1_dmp * p1_dmp;
+      p1 -= pmag * (1.0 - p1_dmp);
+      p2 -= pmag * (1.0 - p1_dmp * p1_dmp);
+      (void)pmin2;
+      c = u1[5] / B_crit;
+      c = pow(c, 4);
+      c = (1.0 - c) / (1.0 + c);
+      for (int v = 1; v <= 3; v++) { u1[v] *= c; u2[v] *= c; }
+      const double rho1 = eos_d3_interp(e, p1, s1), rho2 = eos_d3_interp(e, p2, s2);
+      eps1 = eos_eps3_interp(e, p1, s1);
+      eps2 = eos_eps3_interp(e, p2, s2);
+      u1[0] = rho1;
+      u2[0] = rho2;
+      u1[4] = eps1 * rho1 + 0.5 * (u1[1] * u1[1] + u1[2] * u1[2] + u1[3] * u1[3]) / u1[0];
+      u2[4] = eps2 * rho2 + 0.5 * (u2[1] * u2[1] + u2[2] * u2[2] + u2[3] * u2[3]) / u2[0];
+      const long g1 = at(&g, lb - 1, j, k), g2 = at(&g, lb - 2, j, k);
+      for (int v = 0; v < NV; v++) { U[v * N + g1] = u1[v]; U[v * N + g2] = u2[v]; }
+    }
+  for (int k = 0; k < g.sz; k++)
+    for (int j = 0; j < g.sy; j++) {
+      const long c1 = at(&g, le, j, k), c2 = at(&g, le - 1, j, k);
+      double u1[NV], u2[NV];
+      for (int v = 0; v < NV; v++) { u1[v] = U[v * N + c1]; u2[v] = U[v * N + c2]; }
+      if (p->bnd_top == 1) {
+        if (u1[1] < 0.0) { u1[1] *= -1; u2[1] *= -1; }
+      } else {
+        u1[1] *= -1;
+        u2[1] *= -1;
+      }
+      if (p->bnd_eps_top > 0.0) {
+        u1[4] = p->bnd_eps_top * u1[0] + 0.5 * (u1[1] * u1[1] + u1[2] * u1[2] + u1[3] * u1[3]) / u1[0];
+        u2[4] = p->bnd_eps_top * u2[0] + 0.5 * (u2[1] * u2[1] + u2[2] * u2[2] + u2[3] * u2[3]) / u2[0];
+      }
+      u1[6] *= -1; u2[6] *= -1;
+      u1[7] *= -1; u2[7] *= -1;
+      const long g1 = at(&g, le + 1, j, k), g2 = at(&g, le + 2, j, k);
+      for (int v = 0; v < NV; v++) { U[v * N + g1] = u1[v]; U[v * N + g2] = u2[v]; }
+    }
+}
+
+void mo_boundaries_eos(mo_params* p, const mo_eos* e, double* U) {
+  if (p->xbnd == 1 && !p->periodic_x) {
+    mo_exchange_only(p, U);
+    set_boundary_conditions(p, e, U);
+  } else {
+    mo_boundaries(p, U);
+  }
+}
+
 /* ------------------------------------------------------------- Clean_divB */
 /* Fourth-order divergence of B at interior cell (i, j, k), summed over the
  * dimensions from zero as src/clean_divB.C:136-156 does. */
@@ -917,7 +1125,7 @@ int mo_step_divb(mo_params* p, const mo_eos* eos, double* U, double* U0, double*
       p->last_cfl = cfl;
     }
     mo_source_integrate_tcheck(p, U, U0, R, stage);
-    mo_boundaries(p, U);
+    mo_boundaries_eos(p, eos, U);
   }
   if (cfl <= p->CFL_tvd) {
     p->tvd_two_half_steps = 0;
@@ -933,7 +1141,7 @@ int mo_step_divb(mo_params* p, const mo_eos* eos, double* U, double* U0, double*
     mo_clean_divB(p, U, phi, divB);
   }
   mo_tcheck(p, U);
-  mo_boundaries(p, U);
+  mo_boundaries_eos(p, eos, U);
   p->time += p->dt;
   return 0;
 }

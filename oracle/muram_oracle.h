@@ -43,6 +43,13 @@ typedef struct {
    * at 3) and the last call's iterations and max|divB| before / after (G) */
   int divB_next_iter, divB_last_iters;
   double divB_err0, divB_err1;
+  /* x boundaries of a closed box: 0 = mirror at both ends; 1 = MURaM's physical
+   * boundaries (open bottom, closed or half-open top).  PhysicsData::bnd: top
+   * mode (0 closed, 1 open to outflows), B_crit (G), eps_top; p_bc and s_bc
+   * (negative: set from the first call's bottom layers); bnd_ini: first call pending */
+  int xbnd, bnd_top;
+  double bnd_bcrit, bnd_eps_top, p_bc, s_bc;
+  int bnd_ini;
 } mo_params;
 
 typedef struct mo_eos mo_eos;
@@ -68,6 +75,9 @@ void mo_source_integrate_tcheck(const mo_params* p, double* U, const double* U0,
 /* src/exchange.C:532-783 on one rank plus the closed-x mirror rule */
 void mo_boundaries(const mo_params* p, double* U);
 void mo_exchange_only(const mo_params* p, double* U);
+/* exchange, then the x boundaries p->xbnd selects (src/boundary_pdmp_1_fftw3.C:81-565
+ * for xbnd = 1, which needs the EOS's inverse tables) */
+void mo_boundaries_eos(mo_params* p, const mo_eos* eos, double* U);
 /* src/tvdlimit_SR.C:33-695 */
 void mo_tvdlimit(const mo_params* p, double* U, const double* pres, double dt_tvd);
 /* src/Add_Sources_Integrate_SR.C:534-625 */

@@ -35,6 +35,9 @@ class MoParams(C.Structure):
         ("divB_switch", C.c_int), ("divB_itmax", C.c_int), ("divB_err", C.c_double),
         ("divB_next_iter", C.c_int), ("divB_last_iters", C.c_int),
         ("divB_err0", C.c_double), ("divB_err1", C.c_double),
+        ("xbnd", C.c_int), ("bnd_top", C.c_int),
+        ("bnd_bcrit", C.c_double), ("bnd_eps_top", C.c_double), ("p_bc", C.c_double), ("s_bc", C.c_double),
+        ("bnd_ini", C.c_int),
     ]
 
 
@@ -73,6 +76,7 @@ def lib():
         L.mo_step.restype = C.c_int
         L.mo_step.argtypes = [P, C.c_void_p, dp, dp, dp, dp]
         L.mo_clean_divB.argtypes = [P, dp, dp, dp]
+        L.mo_boundaries_eos.argtypes = [P, C.c_void_p, dp]
         L.mo_step_divb.restype = C.c_int
         L.mo_step_divb.argtypes = [P, C.c_void_p, dp, dp, dp, dp, dp, dp]
         _lib = L
@@ -112,11 +116,12 @@ def params_from_harness(hp):
     kw = {}
     simple = {"CFL": "CFL", "CFL_tvd": "CFL_tvd", "grav": "grav", "va_max": "va_max",
               "va_adjust": "va_adjust", "max_fill": "max_fill", "tau0": "tau0", "dt_rad": "dt_rad", "eta": "eta",
-              "divB_err": "divB_err"}
+              "divB_err": "divB_err", "bnd_bcrit": "bnd_bcrit", "bnd_eps_top": "bnd_eps_top",
+              "p_bc": "p_bc", "s_bc": "s_bc"}
     for k, a in simple.items():
         if k in hp:
             kw[a] = float(hp[k])
-    for k in ("divB_switch", "divB_itmax"):
+    for k in ("divB_switch", "divB_itmax", "xbnd", "bnd_top"):
         if k in hp:
             kw[k] = int(float(hp[k]))
     for k in ("tvd_h", "tvd_cs", "tvd_coeff", "tvd_h_bnd", "tvd_visc_bnd", "tvd_eta_bnd"):
@@ -143,7 +148,7 @@ class State:
     step, ``divB`` holds the last divergence and ``divb_log`` one entry
     (iterations, max|divB| before, after) per step."""
 
-    def __init__(self, p, U):
+    def __init__(self, p, U, eos=None):
         self.p = p
         self.U = np.ascontiguousarray(U, dtype=np.float64).copy()
         self.U0 = np.zeros_like(self.U)
@@ -152,7 +157,12 @@ class State:
         self.phi = np.zeros(self.U.shape[1:])
         self.divB = np.zeros(self.U.shape[1:])
         self.divb_log = []
-        lib().mo_boundaries(C.byref(p), self.U)
+        if p.xbnd == 1 and not p.periodic_x:
+            if eos is None:
+                raise ValueError("the physical x boundaries need the EOS (State(p, U, eos))")
+            lib().mo_boundaries_eos(C.byref(p), eos.ptr, self.U)
+        else:
+            lib().mo_boundaries(C.byref(p), self.U)
 
     def step(self, eos, n=1):
         dts = []

@@ -4,6 +4,9 @@
 // the arrays the GPU path is compared against.  Only tests and the CPU
 // baseline run this program; the product never links it.
 //
+// With xbnd = 1 a closed x dimension gets the reference's own physical
+// boundaries (SetBoundaryConditions, src/boundary_pdmp_1_fftw3.C:81-493:
+// open bottom, top per bnd_top; no potential field) instead of the mirror.
 // With divB_switch > 0 the reference's Clean_divB runs after the TVD pass, as
 // in src/solver.C:341-345; phi starts at zero.
 //
@@ -41,8 +44,21 @@
 #include "src_int_tck.H"
 #include "exchange.H"
 #include "divB.H"
+#include "icbc.H"
+#include "comm_split.H"
 
 MPI_Comm cart_comm;  // defined in comm_split.C, which the harness does not need
+// the rest of comm_split.C's globals: one rank, every sub-communicator is the world
+MPI_Comm XY_COMM = 0, XZ_COMM = 0, YZ_COMM = 0, XCOL_COMM = 0, YCOL_COMM = 0, ZCOL_COMM = 0;
+MPI_Datatype xy_subarray, xz_subarray, yz_subarray;
+int xy_rank = 0, xz_rank = 0, yz_rank = 0, xcol_rank = 0, ycol_rank = 0, zcol_rank = 0;
+// the potential-field top needs FFTs; the harness runs with bnd_pot = 0
+void potential_ext_heffte(const GridData&, double*, double*) {
+  fprintf(stderr, "potential-field boundary not available in the harness\n");
+  exit(6);
+}
+extern double p_bc, s_bc;  // src/boundary_pdmp_1_fftw3.C:31
+static int g_xbnd = 0;
 
 static std::map<std::string, std::string> g_par;
 
@@ -122,9 +138,14 @@ static void closed_x_bc(GridData& G) {
     }
 }
 
+// xbnd = 1: the reference's own SetBoundaryConditions (open bottom, top per
+// bnd_top); its stage argument only selects logging, so 0 is passed.
+static RunData* g_run = nullptr;
 static void boundaries(GridData& G, const PhysicsData& P, int needs_sflx) {
   exchange_grid_acc(G, P, needs_sflx);
-  if (!G.periods[0]) closed_x_bc(G);
+  if (G.periods[0]) return;
+  if (g_xbnd == 1) SetBoundaryConditions(*g_run, G, P, 0, 0, nullptr);
+  else closed_x_bc(G);
 }
 
 int main(int argc, char** argv) {
@@ -211,10 +232,16 @@ int main(int argc, char** argv) {
   Physics.rt[i_rt_tstep] = 0.0;
   Physics.rt_ext[i_ext_cor] = 0;
   Physics.bnd[i_bnd_pot] = 0;
-  Physics.bnd[i_bnd_top] = 0;
+  Physics.bnd[i_bnd_top] = par_d("bnd_top", 0.0);
+  Physics.bnd[i_bnd_bcrit] = par_d("bnd_bcrit", 1.0e10);
+  Physics.bnd[i_bnd_eps_top] = par_d("bnd_eps_top", 0.0);
+  g_xbnd = par_i("xbnd", 0);
+  p_bc = par_d("p_bc", -1.0);
+  s_bc = par_d("s_bc", -1.0);
 
   Run.Init(0);
   Run.verbose = par_i("verbose", 0);
+  g_run = &Run;
   Physics.Init();
   Grid.Init(Run, Physics);
   if (Grid.periods[0]) {  // truly periodic x: no physical x boundary inside the TVD
@@ -324,6 +351,7 @@ int main(int argc, char** argv) {
     FILE* f = fopen(fn.c_str(), "w");
     fprintf(f, "steps=%d\ntime=%.17g\ndt=%.17g\ncfl=%.17g\ntvd_two_half_steps=%d\n", steps, Run.time,
             Run.dt, cfl, tvd_two);
+    if (g_xbnd == 1) fprintf(f, "p_bc=%.17g\ns_bc=%.17g\n", p_bc, s_bc);
     fclose(f);
   }
   return 0;

@@ -6,6 +6,8 @@ stores, per case, the initial state and the PCAST-style snapshots around each
 routine of one traced step, the state after several steps, and the per-step
 dt.  The EOS table is the committed ``eos_small.dat``.
 
+The open_bottom case uses the reference's own physical x boundaries (open
+bottom, top open to outflows) and keeps the p_bc and s_bc they set.
 The divb_cleaning case also runs the reference's Clean_divB after each TVD
 pass and keeps the cleaning potential phi, the last divergence and the
 iteration count of every step (parsed from the reference's own log line).
@@ -43,11 +45,15 @@ def cases():
     yield "divb_cleaning", dict(nx=10, ny=8, nz=6, dx=1.6e6, dy=1.2e6, dz=1.4e6, periodic_x=0, grav=2.74e4,
                                 divB_switch=1, divB_itmax=4, divB_err=0.15, verbose=1), \
         initial.stratified_box(eos, 10, 8, 6, dx=1.6e6, seed=14), dict(steps=5, trace_step=2)
+    yield "open_bottom", dict(nx=12, ny=8, nz=6, dx=1.6e6, periodic_x=0, grav=2.74e4, xbnd=1, bnd_top=1), \
+        initial.stratified_box(eos, 12, 8, 6, dx=1.6e6, seed=15), dict(steps=4, trace_step=2)
 
 
 KEEP = ["init_U", "s1_c2p_U", "s1_c2p_aux", "s1_res_R", "s1_res_dt", "s1_si_U", "s1_bc_U", "s2_c2p_U",
         "s4_bc_U", "s4_c2p_aux", "tvd_U", "divb_U", "tck_U", "end_U", "final_U", "dts", "limits",
         "final_phi", "final_divB"]
+KEEP_BND = ["init_U", "s1_si_U", "s1_bc_U", "s4_bc_U", "s4_c2p_aux", "tvd_U", "tck_U", "end_U", "final_U", "dts",
+            "limits"]
 KEEP_DIVB = ["init_U", "tvd_U", "divb_phi_in", "divb_U", "tck_U", "final_U", "dts", "limits", "final_phi",
              "final_divB"]
 
@@ -66,11 +72,15 @@ def main(only=()):
         hp = dict(hp)
         hp["eos"] = EOS
         out = refrun.run(U, hp, **run)
-        keep = KEEP_DIVB if hp.get("divB_switch", 0) else KEEP
+        keep = KEEP_DIVB if hp.get("divB_switch", 0) else (KEEP_BND if hp.get("xbnd", 0) else KEEP)
         arrays = {k: out[k] for k in keep if k in out}
         arrays["input_U"] = U
         arrays["trace_step"] = np.array(run["trace_step"])
         arrays["steps"] = np.array(run["steps"])
+        if hp.get("xbnd", 0):
+            summ = dict(x.split("=") for x in out["summary"].split())
+            arrays["p_bc"] = np.array(float(summ["p_bc"]))
+            arrays["s_bc"] = np.array(float(summ["s_bc"]))
         if hp.get("divB_switch", 0):
             arrays["divb_iters"] = np.array([int(m) for m in re.findall(r"divB_max \[(\d+)\]", out["stdout"])])
         meta = {k: v for k, v in hp.items() if k != "eos"}

@@ -98,6 +98,24 @@ def test_divb_cleaning_bitexact(eos):
     assert np.array_equal(U, d["tck_U"])
 
 
+def test_open_bottom_bitexact(eos):
+    """MURaM's physical x boundaries (open bottom through the inverse EOS,
+    top open to outflows) after every stage and step: the reference's state,
+    dt and the p_bc / s_bc its first call sets, bit for bit; and the stage-1
+    boundary call alone on the traced step."""
+    d, hp = H.load_case("open_bottom")
+    p = H.oracle_params(hp)
+    st = O.State(p, d["input_U"], eos)
+    assert np.array_equal(st.U, d["init_U"])
+    assert p.p_bc == float(d["p_bc"]) and p.s_bc == float(d["s_bc"])
+    dts = st.step(eos, int(d["steps"]))
+    assert [x[0] for x in dts] == list(d["dts"].reshape(-1, 3)[:, 0])
+    assert np.array_equal(st.U, d["final_U"])
+    U = d["s1_si_U"].copy()
+    O.lib().mo_boundaries_eos(C.byref(p), eos.ptr, U)
+    assert np.array_equal(U, d["s1_bc_U"])
+
+
 def test_eos_interpolation_exact_at_nodes(eos):
     """Known answer: at a table node the bilinear lookup returns exp of the node value."""
     t = initial.EosTable(H.EOS_SMALL)
@@ -141,6 +159,22 @@ def test_live_reference_random_boxes(seed, eos):
     hp = dict(nx=nx, ny=ny, nz=nz, dx=2.4e6, dy=3.2e6, dz=4.0e6, eos=H.EOS_SMALL)
     ref = refrun.run(U, hp, steps=4)
     st = O.State(H.oracle_params(hp), U)
+    st.step(eos, 4)
+    assert np.array_equal(st.U, ref["final_U"])
+
+
+@pytest.mark.skipif(not refrun.available(), reason="reference harness not built here")
+@pytest.mark.parametrize("top,eps_top,bcrit,seed", [(0, 0.0, 1e10, 17), (1, 0.0, 1e10, 18), (1, 3e12, 40.0, 19)])
+def test_live_reference_open_bottom(top, eps_top, bcrit, seed, eos):
+    """The physical x boundaries against the reference run live: closed and
+    half-open top, a fixed top internal energy, and a B_crit low enough that
+    the footpoint factor changes the bottom momenta."""
+    tab = initial.EosTable(H.EOS_SMALL)
+    U = initial.stratified_box(tab, 12, 8, 6, dx=1.6e6, seed=seed)
+    hp = dict(nx=12, ny=8, nz=6, dx=1.6e6, periodic_x=0, grav=2.74e4, eos=H.EOS_SMALL, xbnd=1, bnd_top=top,
+              bnd_eps_top=eps_top, bnd_bcrit=bcrit)
+    ref = refrun.run(U, hp, steps=4)
+    st = O.State(H.oracle_params(hp), U, eos)
     st.step(eos, 4)
     assert np.array_equal(st.U, ref["final_U"])
 
