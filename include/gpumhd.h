@@ -75,6 +75,18 @@ typedef struct gpumhd_params {
    * after / before the iterations (src/clean_divB.C:35-369). */
   int divB_switch, divB_itmax;
   double divB_err;
+  /* x boundaries of a closed box (periodic_x = 0).  xbnd = 0: mirror rule at
+   * both ends (M_x, B_y, B_z change sign).  xbnd = 1: MURaM's physical
+   * boundaries, SetBoundaryConditions of src/boundary_pdmp_1_fftw3.C:81-565
+   * without the potential-field top: open bottom (mean pressure extrapolated
+   * to p_bc, entropy s_bc in upflows, density and energy from the EOS's
+   * inverse tables), top closed (bnd_top = 0) or open to outflows (1), top
+   * internal energy fixed at bnd_eps_top when positive; bnd_bcrit is
+   * PhysicsData::bnd[i_bnd_bcrit] in G.  p_bc, s_bc: the values backup.dat
+   * carries; negative ones are set from the bottom layers by the first
+   * boundary call (set_p_s_bc), gpumhd_boundary_info reads them back. */
+  int xbnd, bnd_top;
+  double bnd_bcrit, bnd_eps_top, p_bc, s_bc;
 } gpumhd_params;
 
 typedef struct gpumhd_ctx gpumhd_ctx;
@@ -110,6 +122,9 @@ int gpumhd_download(gpumhd_ctx* ctx, int which, double* host);
  * gpumhd_divb_info: the last call's iteration count, the next call's, and
  * max|divB| before / after it in G (the reference's verbose log line). */
 int gpumhd_clean_divB(gpumhd_ctx* ctx);
+/* The open bottom's current p_bc and s_bc (WriteBackupFile,
+ * src/boundary_pdmp_1_fftw3.C:44-50, writes them to backup.dat). */
+int gpumhd_boundary_info(gpumhd_ctx* ctx, double* p_bc, double* s_bc);
 int gpumhd_divb_info(gpumhd_ctx* ctx, int* last_iters, int* next_iters, double* err_before, double* err_after);
 
 /* SaveCons (include/src_int_tck.H:10, src/Add_Sources_Integrate_SR.C:475-531). */

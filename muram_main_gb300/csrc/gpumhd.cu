@@ -60,6 +60,9 @@ struct gpumhd_ctx {
   void* comp = nullptr;  // FP32 compensated mode: per-cell remainders of the RK update (8N floats)
   void* phi = nullptr;   // divB cleaning potential (GridData::phi, N), persists between calls
   void* divb = nullptr;  // last divergence of B (GridData::divB, N)
+  double* bnd_part = nullptr;  // per-plane sums of the physical x boundaries (nz * BND_NQ)
+  double *d_xlp3 = nullptr, *d_xs3 = nullptr;  // inverse EOS axes and tables
+  float *d_d3 = nullptr, *d_eps3 = nullptr;
   char err[1024] = {0};
 };
 
@@ -106,6 +109,8 @@ extern "C" int gpumhd_default_params(gpumhd_params* p, int nx, int ny, int nz, d
   p->rt_cfl = 0.5; p->rt_tstep = 0.0; p->rt_update = 1;
   p->tau0 = 1.0; p->dt_rad = 1e9;
   p->divB_switch = 0; p->divB_itmax = 5; p->divB_err = 0.2;  // off; the reference's test settings when on
+  p->xbnd = 0; p->bnd_top = 0; p->bnd_bcrit = 1.0e10; p->bnd_eps_top = 0.0;  // include/physics.H defaults
+  p->p_bc = -1.0; p->s_bc = -1.0;
   return GPUMHD_OK;
 }
 
@@ -159,6 +164,11 @@ static int fill_consts(gpumhd_ctx* ctx) {
   g.N = (long long)g.sx * g.sy * g.sz;
   g.N32 = (unsigned)g.N;
   g.periodic_x = p.periodic_x ? 1 : 0;
+  g.xmirror = (!p.periodic_x && p.xbnd == 0) ? 1 : 0;
+  c.xbnd = (!p.periodic_x && p.xbnd == 1) ? 1 : 0;
+  c.bnd_top = p.bnd_top;
+  c.bnd_bcrit = p.bnd_bcrit / sqrt(8.0 * asin(1.0));  // G to code units (src/boundary_pdmp_1_fftw3.C:90)
+  c.bnd_eps_top = p.bnd_eps_top;
   for (int d = 0; d < 3; d++) {
     c.dx[d] = p.dx[d];
     c.w1[d] = 8. / (12. * p.dx[d]);
@@ -359,6 +369,7 @@ extern "C" int gpumhd_create(const gpumhd_params* p, int device, gpumhd_ctx** ou
   if (p->stage_kernel != 0 && p->stage_kernel != 1) return fail(nullptr, GPUMHD_E_INVALID, "stage_kernel must be 0 or 1");
   if (!(p->eta >= 0.0)) return fail(nullptr, GPUMHD_E_INVALID, "eta must be >= 0");
   if (p->divB_switch > 0 && !(p->divB_err >= 0.0)) return fail(nullptr, GPUMHD_E_INVALID, "divB_err must be >= 0");
+  if (p->xbnd != 0 && p->xbnd != 1) return fail(nullptr, GPUMHD_E_INVALID, "xbnd must be 0 or 1");
   if ((long long)(p->nx + 4) * (p->ny + 4) * (p->nz + 4) > GPUMHD_MAX_CELLS)
     return fail(nullptr, GPUMHD_E_INVALID, "grid too large: (nx+4)(ny+4)(nz+4) must not exceed %lld cells",
                 (long long)GPUMHD_MAX_CELLS);
@@ -397,6 +408,9 @@ extern "C" int gpumhd_create(const gpumhd_params* p, int device, gpumhd_ctx** ou
     ctx->hdyn.time = p->time;
     ctx->hdyn.va_ini_flag = 1;
     ctx->hdyn.divb_next = 3;  // Clean_divB's static next_iter starts at 3 (src/clean_divB.C:51)
+    ctx->hdyn.p_bc = p->p_bc;
+    ctx->hdyn.s_bc = p->s_bc;
+    ctx->hdyn.bnd_ini = 1;
     ctx->hdyn.inv_va2max = 1.0 / pow(p->va_max, 2);
     ctx->hdyn.v_lim = 0.0;
     ctx->hdyn.e_lim = 0.0;
@@ -429,6 +443,8 @@ extern "C" int gpumhd_destroy(gpumhd_ctx* ctx) {
   cudaFree(ctx->comp);
   cudaFree(ctx->phi);
   cudaFree(ctx->divb);
+  cudaFree(ctx->bnd_part);
+  cudaFree(ctx->d_xlp3); cudaFree(ctx->d_xs3); cudaFree(ctx->d_d3); cudaFree(ctx->d_eps3);
   cudaFree(ctx->dyn);
   cudaFree(ctx->dt_hist);
   cudaFree(ctx->d_xeps);
@@ -467,6 +483,11 @@ extern "C" int gpumhd_set_params(gpumhd_ctx* ctx, const gpumhd_params* p) {
     if (rc0) return rc0;
   }
   const Consts keep = ctx->c;
+  if (p->p_bc != ctx->p.p_bc || p->s_bc != ctx->p.s_bc) {
+    ctx->hdyn.p_bc = p->p_bc;
+    ctx->hdyn.s_bc = p->s_bc;
+    ctx->hdyn.bnd_ini = 1;
+  }
   ctx->p = *p;
   int rc = fill_consts(ctx);
   if (rc) return rc;
@@ -478,6 +499,9 @@ extern "C" int gpumhd_set_params(gpumhd_ctx* ctx, const gpumhd_params* p) {
   for (int t = 0; t < 6; t++) c.tab[t] = keep.tab[t];
   c.pquad = keep.pquad; c.inv_exp_xeps = keep.inv_exp_xeps; c.inv_exp_xlr = keep.inv_exp_xlr;
   c.c_pres = keep.c_pres; c.c_temp = keep.c_temp; c.kb = keep.kb; c.mun_mh = keep.mun_mh;
+  c.ss_off = keep.ss_off; c.N_lp3 = keep.N_lp3; c.N_s3 = keep.N_s3;
+  c.inv_del_lp3 = keep.inv_del_lp3; c.inv_del_s3 = keep.inv_del_s3;
+  c.xlp3 = keep.xlp3; c.xs3 = keep.xs3; c.d3 = keep.d3; c.eps3 = keep.eps3;
   fill_kcs(ctx);
   ctx->hdyn.dt = p->dt;
   ctx->hdyn.time = p->time;
@@ -494,7 +518,8 @@ extern "C" int gpumhd_eos_init(gpumhd_ctx* ctx, const char* path) {
   float h[14];
   if (fread(h, sizeof(float), 14, f) != 14) { fclose(f); return fail(ctx, GPUMHD_E_EOS, "eos_init: short header in %s", path); }
   const int N_eps = (int)h[0], N_lr = (int)h[1], N_lp3 = (int)h[2], N_s3 = (int)h[3];
-  if (N_eps < 2 || N_lr < 2 || N_eps > 100000 || N_lr > 100000 || N_lp3 < 0 || N_s3 < 0)
+  if (N_eps < 2 || N_lr < 2 || N_eps > 100000 || N_lr > 100000 || N_lp3 < 0 || N_s3 < 0 || N_lp3 > 100000 ||
+      N_s3 > 100000)
     { fclose(f); return fail(ctx, GPUMHD_E_EOS, "eos_init: bad table sizes in %s", path); }
   const double eps0 = (double)h[4], eps1 = (double)h[5], lr0 = (double)h[6], lr1 = (double)h[7];
   const double eps_off = (double)h[12];
@@ -506,6 +531,12 @@ extern "C" int gpumhd_eos_init(gpumhd_ctx* ctx, const char* path) {
   const size_t n = (size_t)N_eps * N_lr;
   std::vector<float> buf(6 * n);
   if (fread(buf.data(), sizeof(float), 6 * n, f) != 6 * n) { fclose(f); return fail(ctx, GPUMHD_E_EOS, "eos_init: truncated tables in %s", path); }
+  // inverse tables eps(p, s), rho(p, s) (src/eos_init.C:120-136, 181-198); a file
+  // without them serves every boundary but the open bottom
+  const double lp0 = (double)h[8], lp1 = (double)h[9], s0 = (double)h[10], s1 = (double)h[11];
+  const size_t n3 = (size_t)N_lp3 * N_s3;
+  std::vector<float> b3(2 * n3);
+  const bool have_inv = N_lp3 >= 2 && N_s3 >= 2 && fread(b3.data(), sizeof(float), 2 * n3, f) == 2 * n3;
   fclose(f);
   std::vector<float> tab(6 * n);
   const double scale = del_eps * del_lr;
@@ -553,7 +584,39 @@ extern "C" int gpumhd_eos_init(gpumhd_ctx* ctx, const char* path) {
     CK(cudaMemcpy(ctx->d_inv_xeps, ie.data(), sizeof(float) * N_eps, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(ctx->d_inv_xlr, ir.data(), sizeof(float) * N_lr, cudaMemcpyHostToDevice));
   }
+  cudaFree(ctx->d_xlp3); cudaFree(ctx->d_xs3); cudaFree(ctx->d_d3); cudaFree(ctx->d_eps3);
+  ctx->d_xlp3 = ctx->d_xs3 = nullptr;
+  ctx->d_d3 = ctx->d_eps3 = nullptr;
+  double del_lp3 = 0.0, del_s3 = 0.0;
+  if (have_inv) {
+    del_lp3 = (lp1 - lp0) / (double(N_lp3 - 1));
+    del_s3 = (s1 - s0) / (double(N_s3 - 1));
+    std::vector<double> xlp3(N_lp3), xs3(N_s3);
+    for (int i = 0; i < N_lp3; i++) xlp3[i] = lp0 + del_lp3 * ((double)i);
+    for (int i = 0; i < N_s3; i++) xs3[i] = s0 + del_s3 * ((double)i);
+    std::vector<float> eps3(n3), d3(n3);
+    const double sc3 = del_lp3 * del_s3;
+    for (int i = 0; i < N_lp3; i++)
+      for (int j = 0; j < N_s3; j++) {
+        eps3[(size_t)i * N_s3 + j] = (float)(((double)b3[(size_t)j * N_lp3 + i]) / sc3);
+        d3[(size_t)i * N_s3 + j] = (float)(((double)b3[n3 + (size_t)j * N_lp3 + i]) / sc3);
+      }
+    CK(cudaMalloc(&ctx->d_xlp3, sizeof(double) * N_lp3));
+    CK(cudaMalloc(&ctx->d_xs3, sizeof(double) * N_s3));
+    CK(cudaMalloc(&ctx->d_eps3, sizeof(float) * n3));
+    CK(cudaMalloc(&ctx->d_d3, sizeof(float) * n3));
+    CK(cudaMemcpy(ctx->d_xlp3, xlp3.data(), sizeof(double) * N_lp3, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->d_xs3, xs3.data(), sizeof(double) * N_s3, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->d_eps3, eps3.data(), sizeof(float) * n3, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ctx->d_d3, d3.data(), sizeof(float) * n3, cudaMemcpyHostToDevice));
+  }
   Consts& c = ctx->c;
+  c.N_lp3 = have_inv ? N_lp3 : 0;
+  c.N_s3 = have_inv ? N_s3 : 0;
+  c.inv_del_lp3 = have_inv ? 1.0 / del_lp3 : 0.0;
+  c.inv_del_s3 = have_inv ? 1.0 / del_s3 : 0.0;
+  c.xlp3 = ctx->d_xlp3; c.xs3 = ctx->d_xs3; c.d3 = ctx->d_d3; c.eps3 = ctx->d_eps3;
+  c.ss_off = (double)h[13];
   c.N_eps = N_eps; c.N_lr = N_lr;
   c.eps_off = eps_off;
   c.xeps0 = xeps[0]; c.xlr0 = xlr[0]; c.xepsN = xeps[N_eps - 1]; c.xlrN = xlr[N_lr - 1];
@@ -612,6 +675,22 @@ static int ensure_divb(gpumhd_ctx* ctx) {
   field_ptr(ctx, 9, &nf, &rc);
   if (rc) return fail(ctx, rc, "allocation of the divB cleaning fields failed");
   return GPUMHD_OK;
+}
+
+// The physical x boundaries need the EOS's inverse tables and a plane-sum buffer.
+static int ensure_bnd(gpumhd_ctx* ctx) {
+  if (!ctx->c.xbnd) return GPUMHD_OK;
+  if (!ctx->eos_loaded) return fail(ctx, GPUMHD_E_ORDER, "physical x boundaries before eos_init");
+  if (!ctx->c.d3) return fail(ctx, GPUMHD_E_EOS, "the open bottom needs the EOS file's inverse tables");
+  if (!ctx->bnd_part) CK(cudaMalloc(&ctx->bnd_part, sizeof(double) * BND_NQ * ctx->c.g.nz));
+  return GPUMHD_OK;
+}
+
+// MURaM's physical x boundaries on state buffer U (P, cmax: see Launch::bc).
+static int enqueue_bc(gpumhd_ctx* ctx, void* U, void* P, int with_cmax) {
+  if (ctx->f32)
+    return Launch<float>::bc(ctx->c, (float*)U, (float*)P, ctx->dyn, ctx->bnd_part, with_cmax, ctx->stream);
+  return Launch<double>::bc(ctx->c, (double*)U, (double*)P, ctx->dyn, ctx->bnd_part, with_cmax, ctx->stream);
 }
 
 static int ensure_staging(gpumhd_ctx* ctx) {
@@ -822,9 +901,34 @@ extern "C" int gpumhd_source_integrate_tcheck(gpumhd_ctx* ctx, int stage) {
 extern "C" int gpumhd_exchange(gpumhd_ctx* ctx, int with_bc) {
   if (!ctx) return GPUMHD_E_INVALID;
   CK(cudaSetDevice(ctx->device));
-  if (ctx->f32) Launch<float>::fill_ghosts(ctx->c, (float*)ctx->S[ctx->iU], 8, with_bc, ctx->stream);
-  else Launch<double>::fill_ghosts(ctx->c, (double*)ctx->S[ctx->iU], 8, with_bc, ctx->stream);
-  return check_launch(ctx, 1);
+  const bool phys = with_bc && ctx->c.xbnd;
+  if (phys) {
+    int rc = ensure_bnd(ctx);
+    if (rc) return rc;
+  }
+  // exchange (periodic images; the mirror rule too when it is the x boundary)
+  const int mirror = (with_bc && ctx->c.g.xmirror) ? 1 : 0;
+  if (ctx->f32) Launch<float>::fill_ghosts(ctx->c, (float*)ctx->S[ctx->iU], 8, mirror, ctx->stream);
+  else Launch<double>::fill_ghosts(ctx->c, (double*)ctx->S[ctx->iU], 8, mirror, ctx->stream);
+  int n = 1;
+  if (phys) n += enqueue_bc(ctx, ctx->S[ctx->iU], nullptr, 0);
+  int rc = check_launch(ctx, n);
+  if (rc || !phys || !ctx->hdyn.bnd_ini) return rc;
+  // the first call sets p_bc and s_bc on the device: bring the host copy up to
+  // date before a later push of the per-step scalars could overwrite them
+  CK(cudaStreamSynchronize(ctx->stream));
+  return pull_dyn(ctx);
+}
+
+extern "C" int gpumhd_boundary_info(gpumhd_ctx* ctx, double* p_bc, double* s_bc) {
+  if (!ctx) return GPUMHD_E_INVALID;
+  CK(cudaSetDevice(ctx->device));
+  CK(cudaStreamSynchronize(ctx->stream));
+  int rc = pull_dyn(ctx);
+  if (rc) return rc;
+  if (p_bc) *p_bc = ctx->hdyn.p_bc;
+  if (s_bc) *s_bc = ctx->hdyn.s_bc;
+  return GPUMHD_OK;
 }
 
 extern "C" int gpumhd_tcheck(gpumhd_ctx* ctx) {
@@ -904,6 +1008,7 @@ extern "C" int gpumhd_tvdlimit(gpumhd_ctx* ctx, double dt_tvd) {
 static int step_launches(const gpumhd_ctx* ctx) {
   int n = 11;
   if (ctx->c.divb_on) n += 3 + 2 * (ctx->c.divb_itmax > 3 ? ctx->c.divb_itmax : 3) + 1;
+  if (ctx->c.xbnd) n += 5 * 3;  // the boundaries after each stage and at the end of the step
   return n;
 }
 
@@ -921,6 +1026,7 @@ static int enqueue_one_step(gpumhd_ctx* ctx, cudaEvent_t* ev = nullptr) {
   const int a = ctx->iU, b = ctx->iU0, d = ctx->iRes;  // a: state, b and d: work buffers
   const int pa = ctx->iP, pb = 1 - ctx->iP;
   const int defer = c.divb_on;
+  const bool xb = c.xbnd != 0;
   mark();
   k_step_begin<<<1, 32, 0, s>>>(c, ctx->dyn, ctx->dt_hist, ctx->dt_hist_cap);
   if (ctx->f32) {
@@ -931,15 +1037,19 @@ static int enqueue_one_step(gpumhd_ctx* ctx, cudaEvent_t* ev = nullptr) {
     mark();
     L::stage(c, S[a], P[pa], S[a], S[b], P[pb], nullptr, ctx->dyn, 1, false, 1, s,
               map_u(ctx, a), map_p(ctx, pa), ctx->tune_zc, comp);
+    if (xb) L::bc(c, S[b], P[pb], ctx->dyn, ctx->bnd_part, 0, s);
     mark();
     L::stage(c, S[b], P[pb], S[a], S[d], P[pa], nullptr, ctx->dyn, 2, false, 1, s,
               map_u(ctx, b), map_p(ctx, pb), ctx->tune_zc, comp);
+    if (xb) L::bc(c, S[d], P[pa], ctx->dyn, ctx->bnd_part, 0, s);
     mark();
     L::stage(c, S[d], P[pa], S[a], S[b], P[pb], nullptr, ctx->dyn, 3, false, 1, s,
               map_u(ctx, d), map_p(ctx, pa), ctx->tune_zc, comp);
+    if (xb) L::bc(c, S[b], P[pb], ctx->dyn, ctx->bnd_part, 0, s);
     mark();
     L::stage(c, S[b], P[pb], S[a], S[a], nullptr, nullptr, ctx->dyn, 4, false, 0, s,
               map_u(ctx, b), map_p(ctx, pb), ctx->tune_zc, comp);
+    if (xb) L::bc(c, S[a], (float*)nullptr, ctx->dyn, ctx->bnd_part, 0, s);  // TVD keeps the stale pressure
     mark();
     L::tvd(c, 0, 0, 0, S[a], P[pb], S[d], nullptr, ctx->dyn, s, ctx->tune_td);
     mark();
@@ -957,6 +1067,9 @@ static int enqueue_one_step(gpumhd_ctx* ctx, cudaEvent_t* ev = nullptr) {
       L::divb_clean(c, S[a], (float*)ctx->phi, (float*)ctx->divb, ctx->dyn, s);
       L::step_finish(c, S[a], P[pa], ctx->dyn, s);
     }
+    if (xb) {
+      L::bc(c, S[a], P[pa], ctx->dyn, ctx->bnd_part, 1, s);  // the next step's ghosts, pressure and CFL speed
+    }
   } else {
     using L = Launch<double>;
     double* const* S = (double* const*)ctx->S;
@@ -964,15 +1077,19 @@ static int enqueue_one_step(gpumhd_ctx* ctx, cudaEvent_t* ev = nullptr) {
     mark();
     L::stage(c, S[a], P[pa], S[a], S[b], P[pb], nullptr, ctx->dyn, 1, false, 1, s,
               map_u(ctx, a), map_p(ctx, pa), ctx->tune_zc);
+    if (xb) L::bc(c, S[b], P[pb], ctx->dyn, ctx->bnd_part, 0, s);
     mark();
     L::stage(c, S[b], P[pb], S[a], S[d], P[pa], nullptr, ctx->dyn, 2, false, 1, s,
               map_u(ctx, b), map_p(ctx, pb), ctx->tune_zc);
+    if (xb) L::bc(c, S[d], P[pa], ctx->dyn, ctx->bnd_part, 0, s);
     mark();
     L::stage(c, S[d], P[pa], S[a], S[b], P[pb], nullptr, ctx->dyn, 3, false, 1, s,
               map_u(ctx, d), map_p(ctx, pa), ctx->tune_zc);
+    if (xb) L::bc(c, S[b], P[pb], ctx->dyn, ctx->bnd_part, 0, s);
     mark();
     L::stage(c, S[b], P[pb], S[a], S[a], nullptr, nullptr, ctx->dyn, 4, false, 0, s,
               map_u(ctx, b), map_p(ctx, pb), ctx->tune_zc);
+    if (xb) L::bc(c, S[a], (double*)nullptr, ctx->dyn, ctx->bnd_part, 0, s);  // TVD keeps the stale pressure
     mark();
     L::tvd(c, 0, 0, 0, S[a], P[pb], S[d], nullptr, ctx->dyn, s, ctx->tune_td);
     mark();
@@ -989,6 +1106,9 @@ static int enqueue_one_step(gpumhd_ctx* ctx, cudaEvent_t* ev = nullptr) {
     if (defer) {
       L::divb_clean(c, S[a], (double*)ctx->phi, (double*)ctx->divb, ctx->dyn, s);
       L::step_finish(c, S[a], P[pa], ctx->dyn, s);
+    }
+    if (xb) {
+      L::bc(c, S[a], P[pa], ctx->dyn, ctx->bnd_part, 1, s);  // the next step's ghosts, pressure and CFL speed
     }
   }
   mark();
@@ -1011,6 +1131,10 @@ static int fused_prepare(gpumhd_ctx* ctx, int nsteps) {
     int rc1 = ensure_divb(ctx);
     if (rc1) return rc1;
   }
+  {
+    int rc1 = ensure_bnd(ctx);
+    if (rc1) return rc1;
+  }
   if (ctx->f32 && ctx->p.compensated && !ctx->comp) {
     CK(cudaMalloc(&ctx->comp, sizeof(float) * 8 * ctx->c.g.N));
     CK(cudaMemsetAsync(ctx->comp, 0, sizeof(float) * 8 * ctx->c.g.N, ctx->stream));
@@ -1030,14 +1154,19 @@ static int fused_prepare(gpumhd_ctx* ctx, int nsteps) {
     d.err = 0;
     int rc = reset_accumulators(ctx);
     if (rc) return rc;
+    // physical x boundaries: their ghosts, with the CFL speed of the x ghosts
+    // (no longer images of interior cells), before the pressures and statistics
+    int n = 2;
     if (ctx->f32) {
       Launch<float>::fill_ghosts(ctx->c, (float*)ctx->S[ctx->iU], 8, 1, ctx->stream);
+      if (ctx->c.xbnd) n += enqueue_bc(ctx, ctx->S[ctx->iU], ctx->P[ctx->iP], 1);
       Launch<float>::init_pass(ctx->c, (const float*)ctx->S[ctx->iU], (float*)ctx->P[ctx->iP], ctx->dyn, ctx->stream);
     } else {
       Launch<double>::fill_ghosts(ctx->c, (double*)ctx->S[ctx->iU], 8, 1, ctx->stream);
+      if (ctx->c.xbnd) n += enqueue_bc(ctx, ctx->S[ctx->iU], ctx->P[ctx->iP], 1);
       Launch<double>::init_pass(ctx->c, (const double*)ctx->S[ctx->iU], (double*)ctx->P[ctx->iP], ctx->dyn, ctx->stream);
     }
-    rc = check_launch(ctx, 2);
+    rc = check_launch(ctx, n);
     if (rc) return rc;
     ctx->fused_ready = true;
   }

@@ -20,6 +20,8 @@ struct Geom {
   long long N;          // sx*sy*sz
   int periodic_x;
   unsigned N32;         // N as 32-bit: every offset q*N + cell of the 8 state arrays is below 2^32
+  int xmirror;          // closed x with the mirror rule at both ends (0: periodic, or MURaM's physical boundaries)
+  int pad_g;
 };
 
 // Run constants in the kernel's own type, converted once on the host: the
@@ -76,6 +78,16 @@ struct Consts {
   // divB cleaning (src/clean_divB.C:43-101): on, iteration cap, target ratio, error unit
   int divb_on, divb_itmax;
   double divb_err, divb_err_unit, divb_fac_d;
+  // physical x boundaries (src/boundary_pdmp_1_fftw3.C:81-565): on, top mode,
+  // B_crit in code units, eps_top; the EOS's entropy offset and inverse tables
+  int xbnd, bnd_top;
+  double bnd_bcrit, bnd_eps_top, ss_off;
+  int N_lp3, N_s3;
+  double inv_del_lp3, inv_del_s3;
+  const double* xlp3;
+  const double* xs3;
+  const float* d3;     // ln rho (p, s), [i_lp*N_s3 + j_s], pre-divided
+  const float* eps3;   // ln eps (p, s)
   double rt_cfl;
   double CFL, CFL_tvd, dt_rad, rt_tstep, outcad;
   double va_max, va_adjust, max_fill;
@@ -132,6 +144,10 @@ struct Dyn {
   unsigned long long divb_err_bits[2];
   double divb_err0, divb_err1;
   int divb_last, divb_pad;
+  // physical x boundaries: the bottom's pressure and entropy (negative: set
+  // by the first call), the first call still pending, the latest mean pressures
+  double p_bc, s_bc, pmean1, pmean2;
+  int bnd_ini, bnd_pad;
 };
 
 template <class R> __device__ __forceinline__ const DynR<R>& dynr(const Dyn* d);

@@ -33,7 +33,7 @@ __device__ __forceinline__ Images images_of(const Geom& g, int i, int j, int k, 
   if (g.periodic_x) {
     if (I < GH) im.xa = i + g.nx;
     else if (I >= g.nx - GH) im.xa = i - g.nx;
-  } else if (xmirror) {
+  } else if (xmirror && g.xmirror) {
     if (I < GH) { im.xa = 2 * GH - 1 - i; im.xf = 1; }
     else if (I >= g.nx - GH) { im.xa = 2 * GH + 2 * g.nx - 1 - i; im.xf = 1; }
   }
@@ -1317,7 +1317,7 @@ __global__ void k_fill_ghosts(Geom g, R* __restrict__ U, int nfield, int with_bc
     bool flip = false;
     if (gx) {
       if (g.periodic_x) i = i < GH ? i + g.nx : i - g.nx;
-      else if (with_bc) { i = i < GH ? 2 * GH - 1 - i : 2 * GH + 2 * g.nx - 1 - i; flip = true; }
+      else if (with_bc && g.xmirror) { i = i < GH ? 2 * GH - 1 - i : 2 * GH + 2 * g.nx - 1 - i; flip = true; }
       else continue;
     }
     if (gy) j = j < GH ? j + g.ny : j - g.ny;

@@ -3,6 +3,7 @@
 #pragma once
 #include "gpumhd_stage_tm.cuh"
 #include "gpumhd_divb.cuh"
+#include "gpumhd_bnd.cuh"
 
 namespace gpumhd {
 
@@ -35,6 +36,10 @@ struct Launch {
   // Clean_divB on U (phi, divb: N each); returns the number of launches
   static int divb_clean(const Consts& c, R* U, R* phi, R* divb, Dyn* dyn, cudaStream_t s);
   static void step_finish(const Consts& c, R* U, R* P, Dyn* dyn, cudaStream_t s);
+  // MURaM's physical x boundaries on U (P: ghost pressures, may be null;
+  // with_cmax: ghost CFL speeds join the step maximum); part: nz*BND_NQ doubles.
+  // Returns the number of launches.
+  static int bc(const Consts& c, R* U, R* P, Dyn* dyn, double* part, int with_cmax, cudaStream_t s);
   static void cons_to_prim(const Consts& c, R* U, R* P, R* T, R* Ne, R* Ri, R* Am, cudaStream_t s);
   static void init_pass(const Consts& c, const R* U, R* P, Dyn* dyn, cudaStream_t s);
   static void adjust_stats(const Consts& c, const R* U, const R* P, Dyn* dyn, cudaStream_t s);
@@ -196,8 +201,8 @@ int Launch<R>::divb_clean(const Consts& c, R* U, R* phi, R* divb, Dyn* dyn, cuda
   const Geom& g = c.g;
   const dim3 block(DIVB_BX, DIVB_BY);
   const int bx = (g.nx + DIVB_BX - 1) / DIVB_BX, by = (g.ny + DIVB_BY - 1) / DIVB_BY;
-  // z chunks: enough blocks for ~16 per SM
-  int nzch = (152 * 16 + bx * by - 1) / (bx * by);
+  // z chunks: about 64 blocks per SM (short z marches keep more loads in flight)
+  int nzch = (152 * 64 + bx * by - 1) / (bx * by);
   nzch = nzch < 1 ? 1 : (nzch > g.nz ? g.nz : nzch);
   const int zc = (g.nz + nzch - 1) / nzch;
   const dim3 grid(bx, by, (g.nz + zc - 1) / zc);
@@ -210,6 +215,15 @@ int Launch<R>::divb_clean(const Consts& c, R* U, R* phi, R* divb, Dyn* dyn, cuda
   }
   k_divb_end<<<1, 32, 0, s>>>(c, dyn);
   return 3 + 2 * maxit;
+}
+template <class R>
+int Launch<R>::bc(const Consts& c, R* U, R* P, Dyn* dyn, double* part, int with_cmax, cudaStream_t s) {
+  const Geom& g = c.g;
+  k_bc_sums<R><<<g.nz, BND_THREADS, 0, s>>>(c, U, dyn, part);
+  k_bc_setup<<<1, 32, 0, s>>>(c, dyn, part);
+  const long long cols = (long long)g.sy * g.sz;
+  k_bc_ghosts<R><<<(unsigned)((cols + BND_THREADS - 1) / BND_THREADS), BND_THREADS, 0, s>>>(c, U, P, dyn, with_cmax);
+  return 3;
 }
 template <class R>
 void Launch<R>::step_finish(const Consts& c, R* U, R* P, Dyn* dyn, cudaStream_t s) {

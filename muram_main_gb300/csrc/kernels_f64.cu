@@ -94,4 +94,26 @@ __global__ void k_divb_end(Consts c, Dyn* dyn) {
 }
 
 
+__global__ void k_bc_setup(Consts c, Dyn* dyn, const double* __restrict__ part) {
+  if (dyn->err) return;
+  const int lane = threadIdx.x;
+  double t[BND_NQ];
+  for (int q = 0; q < BND_NQ; q++) t[q] = 0.0;
+  for (int k = lane; k < c.g.nz; k += 32)
+    for (int q = 0; q < BND_NQ; q++) t[q] += part[(long long)k * BND_NQ + q];
+  for (int o = 16; o > 0; o >>= 1)
+    for (int q = 0; q < BND_NQ; q++) t[q] += __shfl_xor_sync(0xffffffffu, t[q], o);
+  if (lane != 0) return;
+  const double n = (double)(c.g.ny * c.g.nz);
+  if (dyn->bnd_ini) {
+    const double b0 = t[2] / n, b1 = t[3] / n;
+    if (dyn->p_bc < 0.0) dyn->p_bc = b0 * sqrt(b0 / b1);
+    if (dyn->s_bc < 0.0) dyn->s_bc = (t[4] > 0.0) ? t[5] / t[4] : t[6] / n;
+    dyn->bnd_ini = 0;
+  }
+  const double cn = 1.0 / n;
+  dyn->pmean1 = t[0] * cn;
+  dyn->pmean2 = t[1] * cn;
+}
+
 }  // namespace gpumhd

@@ -52,6 +52,8 @@ class Params(C.Structure):
         ("rt_cfl", C.c_double), ("rt_tstep", C.c_double), ("rt_update", C.c_double),
         ("tau0", C.c_double), ("dt_rad", C.c_double), ("eta", C.c_double),
         ("divB_switch", C.c_int), ("divB_itmax", C.c_int), ("divB_err", C.c_double),
+        ("xbnd", C.c_int), ("bnd_top", C.c_int),
+        ("bnd_bcrit", C.c_double), ("bnd_eps_top", C.c_double), ("p_bc", C.c_double), ("s_bc", C.c_double),
     ]
 
 
@@ -65,7 +67,7 @@ EXPORTS = [
     "gpumhd_adjoint", "gpumhd_tile_from", "gpumhd_set_tuning", "gpumhd_get_tuning", "gpumhd_autotune", "gpumhd_ensemble_create",
     "gpumhd_ensemble_destroy", "gpumhd_ensemble_enqueue_steps", "gpumhd_ensemble_synchronize",
     "gpumhd_ensemble_last_error", "gpumhd_ensemble_stream", "gpumhd_ensemble_launch_count",
-    "gpumhd_clean_divB", "gpumhd_divb_info",
+    "gpumhd_clean_divB", "gpumhd_divb_info", "gpumhd_boundary_info",
 ]
 
 _lib = None
@@ -130,6 +132,7 @@ def load(build_if_missing=True):
         "gpumhd_ensemble_launch_count": (C.c_longlong, [vp]),
         "gpumhd_clean_divB": (C.c_int, [vp]),
         "gpumhd_divb_info": (C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), dp, dp]),
+        "gpumhd_boundary_info": (C.c_int, [vp, dp, dp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -255,6 +258,12 @@ class MuramGPU:
 
     def exchange_grid(self, with_bc=True):
         self._chk(self._L.gpumhd_exchange(self._h, 1 if with_bc else 0))
+
+    def boundary_info(self):
+        """(p_bc, s_bc) of the open bottom (negative until the first boundary call sets them)."""
+        a, b = C.c_double(), C.c_double()
+        self._chk(self._L.gpumhd_boundary_info(self._h, C.byref(a), C.byref(b)))
+        return a.value, b.value
 
     def Clean_divB(self):
         self._chk(self._L.gpumhd_clean_divB(self._h))

@@ -94,6 +94,13 @@ void fill_params(gpumhd_params& p, const RunData& Run, const GridData& Grid, con
   p.divB_switch = (int)Physics.divB[i_divB_switch];
   p.divB_itmax = (int)Physics.divB[i_divB_itmax];
   p.divB_err = Physics.divB[i_divB_err];
+  // a closed x gets MURaM's physical boundaries (src/boundary_pdmp_1_fftw3.C:81-493)
+  p.xbnd = Grid.periods[0] ? 0 : 1;
+  p.bnd_top = (int)Physics.bnd[i_bnd_top];
+  p.bnd_bcrit = Physics.bnd[i_bnd_bcrit];
+  p.bnd_eps_top = Physics.bnd[i_bnd_eps_top];
+  p.p_bc = p_bc;
+  p.s_bc = s_bc;
 }
 
 const RunData* g_run = nullptr;
@@ -130,7 +137,7 @@ extern "C" void GPUMHD_CAT(__real_, GPUMHD_EOS_INIT_MANGLED)(GridData&, RunData&
 extern "C" void GPUMHD_CAT(__wrap_, GPUMHD_EOS_INIT_MANGLED)(GridData& Grid, RunData& Run,
                                                             const PhysicsData& Physics) {
   GPUMHD_CAT(__real_, GPUMHD_EOS_INIT_MANGLED)(Grid, Run, Physics);
-  if (Physics.params[i_param_spitzer] > 0 || Physics.params[i_param_ambipolar] > 0 || Run.diagnostics || Physics.dmp[i_dmp_switch] > 0 ||
+  if (Physics.params[i_param_spitzer] > 0 || Physics.params[i_param_ambipolar] > 0 || Physics.bnd[i_bnd_pot] > 0 || Run.diagnostics || Physics.dmp[i_dmp_switch] > 0 ||
       Physics.rt_ext[i_ext_cor] > 0 || Grid.procs[0] * Grid.procs[1] * Grid.procs[2] != 1) {
     fprintf(stderr, "gpumhd: configuration outside the GPU path\n");
     MPI_Abort(MPI_COMM_WORLD, 1);
@@ -195,14 +202,16 @@ void exchange_grid_acc(GridData& Grid, const PhysicsData& Physics, const int) { 
   check("exchange", gpumhd_exchange(g_ctx, 0));
 }
 
-// SetBoundaryConditions (include/icbc.H:10-12) for the boundaries the library
-// implements: periodic x needs nothing beyond the exchange; a closed x gets
-// the OPEN_TOP = 0 mirror rule (src/boundary_pdmp_1_fftw3.C:415-447) at both
-// ends.  The open bottom and potential-field top are outside the GPU path.
+// SetBoundaryConditions (include/icbc.H:10-12): periodic x needs nothing
+// beyond the exchange; a closed x gets MURaM's physical boundaries (open
+// bottom, top per bnd_top; src/boundary_pdmp_1_fftw3.C:81-565), and p_bc /
+// s_bc, which the first call may set, return to the globals for backup.dat.
+// The potential-field top is outside the GPU path.
 void SetBoundaryConditions(const RunData& Run, GridData& Grid, const PhysicsData& Physics, const int,
                            const int, RTS*) {
   if (!g_ctx || Grid.periods[0]) return;
   check("boundaries", gpumhd_exchange(ctx(), 1));
+  check("boundary info", gpumhd_boundary_info(g_ctx, &p_bc, &s_bc));
 }
 
 // ACCH::UpdateCPU / UpdateGPU (src/ACCH.C:114-158) for the arrays the library owns.

@@ -31,10 +31,10 @@ def oracle_params(hp):
 def gpu_params(hp, precision=64):
     from muram_main_gb300 import gpumhd
     kw = {}
-    for k in ("CFL", "CFL_tvd", "grav", "eta", "divB_err"):
+    for k in ("CFL", "CFL_tvd", "grav", "eta", "divB_err", "bnd_bcrit", "bnd_eps_top", "p_bc", "s_bc"):
         if k in hp:
             kw[k] = float(hp[k])
-    for k in ("divB_switch", "divB_itmax"):
+    for k in ("divB_switch", "divB_itmax", "xbnd", "bnd_top"):
         if k in hp:
             kw[k] = int(hp[k])
     dx = float(hp.get("dx", 3.2e6))

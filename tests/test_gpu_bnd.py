@@ -1,0 +1,133 @@
+"""MURaM's physical x boundaries (SetBoundaryConditions without the
+potential-field top, src/boundary_pdmp_1_fftw3.C:81-565) on the GPU.
+
+Against the reference's own fixture (open bottom, top open to outflows) and
+against the oracle, whose restatement is bit-pinned to the reference on the
+closed and half-open tops, a fixed top energy and a low B_crit.  The two mean
+pressures of the bottom layers are summed in another order on the GPU than in
+the reference (an ulp), so FP64 is held to the same 1e-12 relative
+L-infinity bar as the other fused paths; FP32 to 1e-5 relative L2.
+"""
+import numpy as np
+import pytest
+
+import helpers as H
+from muram_main_gb300 import gpumhd, initial
+
+pytestmark = pytest.mark.gpu
+
+TOL64 = 1e-12
+KERNELS = [0, 1]
+
+
+def ctx_for(hp, precision=64, stage_kernel=0):
+    p = H.gpu_params(hp, precision)
+    p.stage_kernel = stage_kernel
+    return gpumhd.MuramGPU(p, eos_path=H.EOS_SMALL)
+
+
+def check(name, got, ref, tol=TOL64):
+    e = H.rel_linf(got, ref)
+    print(f"{name}: rel Linf per field {np.array2string(e, precision=2)}")
+    assert np.all(e <= tol), (name, e)
+
+
+@pytest.mark.parametrize("capture", [0, 1])
+@pytest.mark.parametrize("kernel", KERNELS)
+def test_fused_steps_vs_reference_fixture(gpu_lib, kernel, capture):
+    d, hp = H.load_case("open_bottom")
+    g = ctx_for(hp, stage_kernel=kernel)
+    g.upload_state(d["input_U"])
+    dts = g.run_steps(int(d["steps"]), capture=bool(capture))
+    assert np.allclose(dts, d["dts"].reshape(-1, 3)[:, 0], rtol=TOL64, atol=0)
+    check(f"open bottom fused [kernel={kernel}, graph={capture}]", g.download_state(), d["final_U"])
+    p_bc, s_bc = g.boundary_info()
+    assert abs(p_bc - float(d["p_bc"])) <= TOL64 * float(d["p_bc"])
+    assert abs(s_bc - float(d["s_bc"])) <= TOL64 * abs(float(d["s_bc"]))
+    g.close()
+
+
+def test_reference_order_steps_vs_reference_fixture(gpu_lib):
+    d, hp = H.load_case("open_bottom")
+    g = ctx_for(hp)
+    g.upload_state(d["input_U"])
+    g.exchange_grid(True)
+    check("open bottom initial boundaries", g.download_state(), d["init_U"])
+    for _ in range(int(d["steps"])):
+        g.step_reference_order()
+    check("open bottom per-routine steps", g.download_state(), d["final_U"])
+    g.close()
+
+
+def test_boundary_call_vs_reference_fixture(gpu_lib):
+    """One exchange + SetBoundaryConditions on the traced step's stage-1
+    state, with the p_bc / s_bc the run set at its start."""
+    d, hp = H.load_case("open_bottom")
+    hp = dict(hp, p_bc=float(d["p_bc"]), s_bc=float(d["s_bc"]))
+    g = ctx_for(hp)
+    g.upload_state(d["s1_si_U"])
+    g.exchange_grid(True)
+    check("SetBoundaryConditions", g.download_state(), d["s1_bc_U"])
+    assert g.boundary_info() == (float(d["p_bc"]), float(d["s_bc"]))
+    g.close()
+
+
+@pytest.mark.parametrize("kernel", KERNELS)
+@pytest.mark.parametrize("top,eps_top,bcrit", [(0, 0.0, 1e10), (1, 3e12, 40.0)])
+def test_fused_vs_oracle(gpu_lib, kernel, top, eps_top, bcrit):
+    from oracle import oracle as O
+    tab = initial.EosTable(H.EOS_SMALL)
+    U = initial.stratified_box(tab, 24, 16, 12, dx=1.6e6, seed=31)
+    hp = dict(nx=24, ny=16, nz=12, dx=1.6e6, periodic_x=0, grav=2.74e4, xbnd=1, bnd_top=top,
+              bnd_eps_top=eps_top, bnd_bcrit=bcrit)
+    eos = O.Eos(H.EOS_SMALL)
+    st = O.State(H.oracle_params(hp), U, eos)
+    dts = st.step(eos, 6)
+    g = ctx_for(hp, stage_kernel=kernel)
+    g.upload_state(U)
+    got = g.run_steps(6)
+    assert np.allclose(got, [x[0] for x in dts], rtol=TOL64, atol=0)
+    check(f"open bottom vs oracle [top={top}, eps_top={eps_top}, kernel={kernel}]", g.download_state(), st.U)
+    g.close()
+
+
+def test_fp32_open_bottom_vs_fp64_oracle(gpu_lib):
+    from oracle import oracle as O
+    tab = initial.EosTable(H.EOS_SMALL)
+    U = initial.stratified_box(tab, 32, 24, 24, dx=1.6e6, seed=33)
+    hp = dict(nx=32, ny=24, nz=24, dx=1.6e6, periodic_x=0, grav=2.74e4, xbnd=1, bnd_top=1)
+    eos = O.Eos(H.EOS_SMALL)
+    st = O.State(H.oracle_params(hp), U, eos)
+    st.step(eos, 40)
+    g = ctx_for(hp, precision=32)
+    g.upload_state(U)
+    g.run_steps(40)
+    e = H.rel_l2(H.interior(g.download_state()), H.interior(st.U))
+    print("FP32 open bottom vs FP64 oracle, rel L2:", np.array2string(e, precision=2))
+    assert np.all(e <= 1e-5), e
+    g.close()
+
+
+def test_ensemble_with_open_bottom(gpu_lib):
+    tab = initial.EosTable(H.EOS_SMALL)
+    shapes = [(16, 12, 8, 1), (20, 12, 12, 0)]
+
+    def box(nx, ny, nz, xb, seed):
+        g = ctx_for(dict(nx=nx, ny=ny, nz=nz, dx=1.6e6, periodic_x=0, grav=2.74e4, xbnd=xb, bnd_top=1))
+        g.upload_state(initial.stratified_box(tab, nx, ny, nz, dx=1.6e6, seed=seed))
+        return g
+
+    alone = []
+    for q, (nx, ny, nz, xb) in enumerate(shapes):
+        g = box(nx, ny, nz, xb, 70 + q)
+        g.run_steps(4)
+        alone.append(g.download_state())
+        g.close()
+    boxes = [box(nx, ny, nz, xb, 70 + q) for q, (nx, ny, nz, xb) in enumerate(shapes)]
+    ens = gpumhd.MuramEnsemble(boxes)
+    ens.run_steps(4)
+    for ref, g in zip(alone, boxes):
+        assert np.array_equal(g.download_state(), ref)
+    ens.close()
+    for g in boxes:
+        g.close()
