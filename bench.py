@@ -184,7 +184,9 @@ def words_per_cell(phase):
     if phase in ("tvd_x", "tvd_y"):
         return 8 + 1 + 8              # read U, stale p; write U
     if phase == "tvd_z":
-        return 8 + 1 + 8 + 1          # + next step's pressure
+        return 8 + 1 + 8              # the interior only; the end-of-step pass follows
+    if phase == "finish":
+        return 8 + 1                  # read U (TCheck stores only what it changes); write p
     return 0
 
 
@@ -250,8 +252,8 @@ def run_ours(args):
         last, nxt, e0, e1 = g.divb_info()
     phases = g.profile_steps(2)
     if args.divb:
-        # words per cell: divergence passes 6 (the last 4), gradient passes 10, end-of-step pass 17
-        words = 6 + 16 * last - 2 + 17
+        # words per cell: divergence passes 6 (the last 4), gradient passes 10
+        words = 6 + 16 * last - 2
         divb = {"iterations_last_step": last, "max_divB_before_after_G": [e0, e1],
                 "ms_per_step": round(phases["divb_clean"], 4),
                 "algorithmic_bytes_per_step": words * 4 * n_cells,
@@ -273,7 +275,7 @@ def run_ours(args):
                 "algorithmic_bytes_per_launch": bytes_per_launch, "mean_launch_ms": round(mean_ms, 4),
                 "peak_source": f"{peak_src} hbm_gbs"}
     # whole-step bytes against HBM
-    step_bytes = sum(words_per_cell(p) for p in fam["stage"] + fam["tvd"]) * 4 * n_cells
+    step_bytes = sum(words_per_cell(p) for p in fam["stage"] + fam["tvd"] + ["finish"]) * 4 * n_cells
     step_ms = ms / args.steps
     # end to end through the C ABI with host buffers
     e2e = None

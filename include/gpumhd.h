@@ -167,9 +167,10 @@ int gpumhd_synchronize(gpumhd_ctx* ctx);
 int gpumhd_step_info(gpumhd_ctx* ctx, double* dt, double* cfl, double* time, int* tvd_two_half);
 
 /* Run `nsteps` fused steps without graph capture, timing each launch with CUDA
- * events on the context's stream; ms_phase[12] receives the mean duration of:
+ * events on the context's stream; ms_phase[13] receives the mean duration of:
  * step control, RK stages 1-4, TVD x/y/z sweeps, second-half TVD x/y/z sweeps,
- * divB cleaning with the end-of-step pass (0 when divB_switch = 0). */
+ * divB cleaning (0 when divB_switch = 0), the end-of-step pass (TCheck, ghost
+ * images, next pressure and statistics). */
 int gpumhd_profile_steps(gpumhd_ctx* ctx, int nsteps, double* ms_phase);
 /* MHD_Residual's CFL time step, dt_mhd = dxmin / cmax, computed with no device
  * allocation at all.  No counterpart in the reference: it exists for callers

@@ -992,10 +992,10 @@ extern "C" int gpumhd_tvdlimit(gpumhd_ctx* ctx, double dt_tvd) {
     CK(cudaMemcpyAsync(ctx->T, ctx->S[ctx->iU], 8 * N * ctx->rsz, cudaMemcpyDeviceToDevice, ctx->stream));
     if (ctx->f32)
       Launch<float>::tvd(ctx->c, d, 0, 0, (const float*)ctx->T, (const float*)ctx->P[ctx->iP], (float*)ctx->S[ctx->iU],
-                         nullptr, ctx->dyn, ctx->stream);
+                         ctx->dyn, ctx->stream);
     else
       Launch<double>::tvd(ctx->c, d, 0, 0, (const double*)ctx->T, (const double*)ctx->P[ctx->iP],
-                          (double*)ctx->S[ctx->iU], nullptr, ctx->dyn, ctx->stream);
+                          (double*)ctx->S[ctx->iU], ctx->dyn, ctx->stream);
     rc = check_launch(ctx, 1);
     if (rc) return rc;
   }
@@ -1003,21 +1003,22 @@ extern "C" int gpumhd_tvdlimit(gpumhd_ctx* ctx, double dt_tvd) {
 }
 
 // ------------------------------------------------------------- fused path
-// Launches of one fused step: step control, four RK stages, six TVD sweeps;
-// with divB cleaning also the cleaning passes and the end-of-step pass.
+// Launches of one fused step: step control, four RK stages, six TVD sweeps,
+// the end-of-step pass; with divB cleaning also the cleaning passes, with the
+// physical x boundaries their three launches after each stage and the step.
 static int step_launches(const gpumhd_ctx* ctx) {
-  int n = 11;
-  if (ctx->c.divb_on) n += 3 + 2 * (ctx->c.divb_itmax > 3 ? ctx->c.divb_itmax : 3) + 1;
+  int n = 12;
+  if (ctx->c.divb_on) n += 3 + 2 * (ctx->c.divb_itmax > 3 ? ctx->c.divb_itmax : 3);
   if (ctx->c.xbnd) n += 5 * 3;  // the boundaries after each stage and at the end of the step
   return n;
 }
 
 // One fused step: step control, four RK stages, two TVD passes (the second
-// returns at once unless the step takes two half passes), and with divB
-// cleaning on, Clean_divB and the end-of-step pass (TCheck, ghosts, next
-// pressure) that the last TVD sweep leaves to it (src/solver.C:324-350).
-// With ev != NULL an event is recorded before each of the 11 launches, before
-// the cleaning and after the last launch (13 events).
+// returns at once unless the step takes two half passes), Clean_divB when it
+// is on, and the end-of-step pass (TCheck, ghost images, the next step's
+// pressure, CFL speed and statistics; src/solver.C:324-365).  With ev != NULL
+// an event is recorded before each of the 11 launches up to the TVD passes,
+// before the cleaning, before the end-of-step pass and after it (14 events).
 static int enqueue_one_step(gpumhd_ctx* ctx, cudaEvent_t* ev = nullptr) {
   const Consts& c = ctx->c;
   cudaStream_t s = ctx->stream;
@@ -1025,7 +1026,6 @@ static int enqueue_one_step(gpumhd_ctx* ctx, cudaEvent_t* ev = nullptr) {
   auto mark = [&]() { if (ev) cudaEventRecord(ev[k++], s); };
   const int a = ctx->iU, b = ctx->iU0, d = ctx->iRes;  // a: state, b and d: work buffers
   const int pa = ctx->iP, pb = 1 - ctx->iP;
-  const int defer = c.divb_on;
   const bool xb = c.xbnd != 0;
   mark();
   k_step_begin<<<1, 32, 0, s>>>(c, ctx->dyn, ctx->dt_hist, ctx->dt_hist_cap);
@@ -1051,20 +1051,21 @@ static int enqueue_one_step(gpumhd_ctx* ctx, cudaEvent_t* ev = nullptr) {
               map_u(ctx, b), map_p(ctx, pb), ctx->tune_zc, comp);
     if (xb) L::bc(c, S[a], (float*)nullptr, ctx->dyn, ctx->bnd_part, 0, s);  // TVD keeps the stale pressure
     mark();
-    L::tvd(c, 0, 0, 0, S[a], P[pb], S[d], nullptr, ctx->dyn, s, ctx->tune_td);
+    L::tvd(c, 0, 0, 0, S[a], P[pb], S[d], ctx->dyn, s, ctx->tune_td);
     mark();
-    L::tvd(c, 1, 0, 0, S[d], P[pb], S[b], nullptr, ctx->dyn, s, ctx->tune_td);
+    L::tvd(c, 1, 0, 0, S[d], P[pb], S[b], ctx->dyn, s, ctx->tune_td);
     mark();
-    L::tvd(c, 2, 1, 0, S[b], P[pb], S[a], P[pa], ctx->dyn, s, ctx->tune_td, defer);
+    L::tvd(c, 2, 1, 0, S[b], P[pb], S[a], ctx->dyn, s, ctx->tune_td);
     mark();
-    L::tvd(c, 0, 0, 1, S[a], P[pb], S[d], nullptr, ctx->dyn, s, ctx->tune_td);
+    L::tvd(c, 0, 0, 1, S[a], P[pb], S[d], ctx->dyn, s, ctx->tune_td);
     mark();
-    L::tvd(c, 1, 0, 1, S[d], P[pb], S[b], nullptr, ctx->dyn, s, ctx->tune_td);
+    L::tvd(c, 1, 0, 1, S[d], P[pb], S[b], ctx->dyn, s, ctx->tune_td);
     mark();
-    L::tvd(c, 2, 2, 1, S[b], P[pb], S[a], P[pa], ctx->dyn, s, ctx->tune_td, defer);
+    L::tvd(c, 2, 2, 1, S[b], P[pb], S[a], ctx->dyn, s, ctx->tune_td);
     mark();
-    if (defer) {
-      L::divb_clean(c, S[a], (float*)ctx->phi, (float*)ctx->divb, ctx->dyn, s);
+    if (c.divb_on) L::divb_clean(c, S[a], (float*)ctx->phi, (float*)ctx->divb, ctx->dyn, s);
+    mark();
+    {
       L::step_finish(c, S[a], P[pa], ctx->dyn, s);
     }
     if (xb) {
@@ -1091,20 +1092,21 @@ static int enqueue_one_step(gpumhd_ctx* ctx, cudaEvent_t* ev = nullptr) {
               map_u(ctx, b), map_p(ctx, pb), ctx->tune_zc);
     if (xb) L::bc(c, S[a], (double*)nullptr, ctx->dyn, ctx->bnd_part, 0, s);  // TVD keeps the stale pressure
     mark();
-    L::tvd(c, 0, 0, 0, S[a], P[pb], S[d], nullptr, ctx->dyn, s, ctx->tune_td);
+    L::tvd(c, 0, 0, 0, S[a], P[pb], S[d], ctx->dyn, s, ctx->tune_td);
     mark();
-    L::tvd(c, 1, 0, 0, S[d], P[pb], S[b], nullptr, ctx->dyn, s, ctx->tune_td);
+    L::tvd(c, 1, 0, 0, S[d], P[pb], S[b], ctx->dyn, s, ctx->tune_td);
     mark();
-    L::tvd(c, 2, 1, 0, S[b], P[pb], S[a], P[pa], ctx->dyn, s, ctx->tune_td, defer);
+    L::tvd(c, 2, 1, 0, S[b], P[pb], S[a], ctx->dyn, s, ctx->tune_td);
     mark();
-    L::tvd(c, 0, 0, 1, S[a], P[pb], S[d], nullptr, ctx->dyn, s, ctx->tune_td);
+    L::tvd(c, 0, 0, 1, S[a], P[pb], S[d], ctx->dyn, s, ctx->tune_td);
     mark();
-    L::tvd(c, 1, 0, 1, S[d], P[pb], S[b], nullptr, ctx->dyn, s, ctx->tune_td);
+    L::tvd(c, 1, 0, 1, S[d], P[pb], S[b], ctx->dyn, s, ctx->tune_td);
     mark();
-    L::tvd(c, 2, 2, 1, S[b], P[pb], S[a], P[pa], ctx->dyn, s, ctx->tune_td, defer);
+    L::tvd(c, 2, 2, 1, S[b], P[pb], S[a], ctx->dyn, s, ctx->tune_td);
     mark();
-    if (defer) {
-      L::divb_clean(c, S[a], (double*)ctx->phi, (double*)ctx->divb, ctx->dyn, s);
+    if (c.divb_on) L::divb_clean(c, S[a], (double*)ctx->phi, (double*)ctx->divb, ctx->dyn, s);
+    mark();
+    {
       L::step_finish(c, S[a], P[pa], ctx->dyn, s);
     }
     if (xb) {
@@ -1251,20 +1253,20 @@ extern "C" int gpumhd_profile_steps(gpumhd_ctx* ctx, int nsteps, double* ms_phas
   CK(cudaSetDevice(ctx->device));
   int rc = fused_prepare(ctx, nsteps);
   if (rc) return rc;
-  cudaEvent_t ev[13];
-  for (int q = 0; q < 13; q++) CK(cudaEventCreate(&ev[q]));
-  for (int q = 0; q < 12; q++) ms_phase[q] = 0.0;
+  cudaEvent_t ev[14];
+  for (int q = 0; q < 14; q++) CK(cudaEventCreate(&ev[q]));
+  for (int q = 0; q < 13; q++) ms_phase[q] = 0.0;
   for (int st = 0; st < nsteps && rc == 0; st++) {
     rc = enqueue_one_step(ctx, ev);
     if (rc) break;
-    if (cudaEventSynchronize(ev[12]) != cudaSuccess) { rc = fail(ctx, GPUMHD_E_CUDA, "event sync failed"); break; }
-    for (int q = 0; q < 12; q++) {
+    if (cudaEventSynchronize(ev[13]) != cudaSuccess) { rc = fail(ctx, GPUMHD_E_CUDA, "event sync failed"); break; }
+    for (int q = 0; q < 13; q++) {
       float ms = 0.f;
       cudaEventElapsedTime(&ms, ev[q], ev[q + 1]);
       ms_phase[q] += ms / nsteps;
     }
   }
-  for (int q = 0; q < 13; q++) cudaEventDestroy(ev[q]);
+  for (int q = 0; q < 14; q++) cudaEventDestroy(ev[q]);
   if (rc) return rc;
   CK(cudaMemsetAsync(ctx->S[ctx->iRes], 0, 8 * ctx->c.g.N * ctx->rsz, ctx->stream));
   return gpumhd_synchronize(ctx);
@@ -1635,9 +1637,10 @@ extern "C" int gpumhd_adjoint(gpumhd_ctx* ctx, int nsteps, int checkpoint_every,
     L::stage(c, B1, Q1, A, B2, Q2, nullptr, adyn, 2, false, 1, s);
     L::stage(c, B2, Q2, A, B3, Q3, nullptr, adyn, 3, false, 1, s);
     L::stage(c, B3, Q3, A, B4, nullptr, nullptr, adyn, 4, false, 0, s);
-    L::tvd(c, 0, 0, 0, B4, Q3, V1, nullptr, adyn, s);
-    L::tvd(c, 1, 0, 0, V1, Q3, V2, nullptr, adyn, s);
-    L::tvd(c, 2, 1, 0, V2, Q3, An, Qn, adyn, s);
+    L::tvd(c, 0, 0, 0, B4, Q3, V1, adyn, s);
+    L::tvd(c, 1, 0, 0, V1, Q3, V2, adyn, s);
+    L::tvd(c, 2, 1, 0, V2, Q3, An, adyn, s);
+    L::step_finish(c, An, Qn, adyn, s);
     std::swap(A, An);
     std::swap(Q0, Qn);
   };
@@ -1656,7 +1659,7 @@ extern "C" int gpumhd_adjoint(gpumhd_ctx* ctx, int nsteps, int checkpoint_every,
     }
     record();
   }
-  ctx->launches += 8LL * nsteps;
+  ctx->launches += 9LL * nsteps;
   Dyn dchk;
   CK(cudaMemcpyAsync(&dchk, adyn, sizeof(Dyn), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
@@ -1676,7 +1679,7 @@ extern "C" int gpumhd_adjoint(gpumhd_ctx* ctx, int nsteps, int checkpoint_every,
     record();
     std::swap(A, An);
     std::swap(Q0, Qn);
-    ctx->launches += 8LL * (t - q * checkpoint_every + 1);
+    ctx->launches += 9LL * (t - q * checkpoint_every + 1);
     CK(cudaMemsetAsync(lP3, 0, n * sizeof(double), s));
     CK(cudaMemsetAsync(lU0, 0, 8 * n * sizeof(double), s));
     adjoint_tvd(c, adyn, 2, V2, Q3, lA, 1, lB, lP3, w, s);

@@ -1,5 +1,4 @@
-// divB cleaning (Clean_divB, src/clean_divB.C:35-369) and the end-of-step
-// pass that runs after it.
+// divB cleaning (Clean_divB, src/clean_divB.C:35-369).
 //
 // One call: the divergence pass (k_divb_div, pass 0) gives divB and its
 // maximum; then each of n iterations is a gradient pass (k_divb_grad:
@@ -185,33 +184,6 @@ __global__ void __launch_bounds__(DIVB_BX* DIVB_BY) k_divb_grad(Consts c, R* __r
     pm2 = pm1; pm1 = p0; p0 = pp1; pp1 = pp2;
     cur = nxt;
   }
-}
-
-// End of a step whose TVD pass left TCheck to a later kernel: per interior
-// cell TCheck (src/Add_Sources_Integrate_SR.C:534-625), the ghost images with
-// the closed-x mirror, and the next step's pressure, CFL speed and
-// Adjust_Valf_Max statistics -- what the last TVD sweep does otherwise.
-template <class R>
-__global__ void __launch_bounds__(256) k_step_finish(Consts c, R* __restrict__ U, R* __restrict__ Pout,
-                                                     Dyn* __restrict__ dyn) {
-  if (dyn->err) return;
-  const Geom& g = c.g;
-  const DynR<R>& dr = dynr<R>(dyn);
-  const R vmax = dr.vmax, emax = dr.emax, inv_va2max = dr.inv_va2max, vlim95 = dr.vlim95, elim95 = dr.elim95;
-  FinishAcc<R> acc;
-  const long long ncell = (long long)g.nx * g.ny * g.nz;
-  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < ncell; t += (long long)gridDim.x * blockDim.x) {
-    const int i = GH + (int)(t % g.nx);
-    const long long r = t / g.nx;
-    const int j = GH + (int)(r % g.ny);
-    const int k = GH + (int)(r / g.ny);
-    const unsigned id = cidx32(g, i, j, k);
-    R u[NV];
-#pragma unroll
-    for (int v = 0; v < NV; v++) u[v] = U[(unsigned)v * g.N32 + id];
-    finish_cell<R>(c, U, Pout, i, j, k, u, vmax, emax, inv_va2max, vlim95, elim95, acc);
-  }
-  acc.flush(dyn);
 }
 
 }  // namespace gpumhd

@@ -620,7 +620,6 @@ struct TvdArgs {
   int na, nb, a0, b0;    // pencil ranges: a fastest (coalesced), b second
   long long sa, sb, sd;  // strides of a, b and along the sweep
   int n1;                // interior cells along the sweep
-  int defer;             // the last pass stores the interior only (k_step_finish ends the step)
 };
 
 // Per-cell quantities from the cell's stored values r (state and pressure)
@@ -860,34 +859,88 @@ struct FinishAcc {
   }
 };
 
+// End of a fused step, after the TVD sweeps (and Clean_divB): per interior
+// cell TCheck (src/Add_Sources_Integrate_SR.C:534-625) in place -- a field is
+// stored only where TCheck changed its bits, so most cells cost reads only --,
+// the cell's ghost images (closed-x mirror included), and the next step's
+// stage-1 pressure, CFL speed and Adjust_Valf_Max statistics.  Block 32 x 8
+// over (x, y), z planes by the grid's third dimension.
+constexpr int FIN_BX = 32, FIN_BY = 8;
+
 template <class R>
-__device__ __forceinline__ void finish_cell(const Consts& c, R* __restrict__ Uout, R* __restrict__ Pout, int ci, int cj,
-                                            int ck, R* u, R vmax, R emax, R inv_va2max, R vlim95, R elim95,
-                                            FinishAcc<R>& acc) {
+__device__ __forceinline__ bool same_bits(R a, R b);
+template <>
+__device__ __forceinline__ bool same_bits<float>(float a, float b) { return __float_as_uint(a) == __float_as_uint(b); }
+template <>
+__device__ __forceinline__ bool same_bits<double>(double a, double b) {
+  return __double_as_longlong(a) == __double_as_longlong(b);
+}
+
+// resident blocks per SM the register budget is set for (FP32: 64 registers)
+template <class R> struct FinBlocks { static constexpr int v = sizeof(R) == 4 ? 4 : 2; };
+
+template <class R>
+__global__ void __launch_bounds__(FIN_BX* FIN_BY, FinBlocks<R>::v) k_step_finish(Consts c, R* __restrict__ U, R* __restrict__ Pout,
+                                                               Dyn* __restrict__ dyn) {
+  if (dyn->err) return;
   const Geom& g = c.g;
-  tcheck_cell<R>(c, vmax, emax, u[0], u[1], u[2], u[3], u[4]);
-  const Images im = images_of(g, ci, cj, ck, true);
-  store_state<R>(g, Uout, ci, cj, ck, im, u);
-  R v1, v2, v3, ei;
-  prim_from_cons(u[0], u[1], u[2], u[3], u[4], v1, v2, v3, ei);
-  const R pr = eos_pres(c, u[0], ei, (R)1.0 / u[0]);
-  store_scalar<R>(g, Pout, ci, cj, ck, im, pr);
-  R cmv = cmax_cell<R>(u[0], v1, v2, v3, u[5], u[6], u[7], pr, inv_va2max);
-  acc.cmax = smax(acc.cmax, cmv);
-  R vabs = d_sqrt(v1 * v1 + v2 * v2 + v3 * v3);
-  R cs = (R)(5 / 3.) * pr / u[0];
-  R ee = ei / u[0];
-  acc.v = d_fmax(acc.v, vabs);
-  acc.cs = d_fmax(acc.cs, cs);
-  acc.e = d_fmax(acc.e, ee);
-  if (vabs >= vlim95) acc.nv++;
-  if (ee >= elim95) acc.ne++;
+  const DynR<R>& dr = dynr<R>(dyn);
+  const R vmax = dr.vmax, emax = dr.emax, inv_va2max = dr.inv_va2max, vlim95 = dr.vlim95, elim95 = dr.elim95;
+  FinishAcc<R> acc;
+  const int i = GH + blockIdx.x * FIN_BX + threadIdx.x;
+  const int j = GH + blockIdx.y * FIN_BY + threadIdx.y;
+  if (i < GH + g.nx && j < GH + g.ny) {
+#pragma unroll 2
+    for (int k = GH + blockIdx.z; k < GH + g.nz; k += gridDim.z) {
+      const unsigned id = cidx32(g, i, j, k);
+      R u[NV], u0[5];
+#pragma unroll
+      for (int v = 0; v < NV; v++) u[v] = U[(unsigned)v * g.N32 + id];
+#pragma unroll
+      for (int v = 0; v < 5; v++) u0[v] = u[v];
+      tcheck_cell<R>(c, vmax, emax, u[0], u[1], u[2], u[3], u[4]);
+#pragma unroll
+      for (int v = 0; v < 5; v++)
+        if (!same_bits(u[v], u0[v])) U[(unsigned)v * g.N32 + id] = u[v];
+      R v1, v2, v3, ei;
+      prim_from_cons(u[0], u[1], u[2], u[3], u[4], v1, v2, v3, ei);
+      const R pr = eos_pres(c, u[0], ei, (R)1.0 / u[0]);
+      Pout[id] = pr;
+      const Images im = images_of(g, i, j, k, true);
+      if (im.xa >= 0 || im.ya >= 0 || im.za >= 0) {
+        // the ghost images (every combination but the cell itself)
+        for (int q = 1; q < 8; q++) {
+          const int ii = (q & 1) ? im.xa : i, jj = (q & 2) ? im.ya : j, kk = (q & 4) ? im.za : k;
+          if (ii < 0 || jj < 0 || kk < 0) continue;
+          const unsigned gid = cidx32(g, ii, jj, kk);
+          const bool f = (q & 1) && im.xf;
+#pragma unroll
+          for (int v = 0; v < NV; v++) {
+            R x = u[v];
+            if (f && (v == 1 || v == 6 || v == 7)) x = -x;
+            U[(unsigned)v * g.N32 + gid] = x;
+          }
+          Pout[gid] = pr;
+        }
+      }
+      R cmv = cmax_cell<R>(u[0], v1, v2, v3, u[5], u[6], u[7], pr, inv_va2max);
+      acc.cmax = smax(acc.cmax, cmv);
+      R vabs = d_sqrt(v1 * v1 + v2 * v2 + v3 * v3);
+      R cs = (R)(5 / 3.) * pr / u[0];
+      R ee = ei / u[0];
+      acc.v = d_fmax(acc.v, vabs);
+      acc.cs = d_fmax(acc.cs, cs);
+      acc.e = d_fmax(acc.e, ee);
+      if (vabs >= vlim95) acc.nv++;
+      if (ee >= elim95) acc.ne++;
+    }
+  }
+  acc.flush(dyn);
 }
 
 template <class R, int DIR>
 __global__ void __launch_bounds__(128) k_tvd_sweep(Consts c, const R* __restrict__ Uin, const R* __restrict__ Pst,
-                                                   R* __restrict__ Uout, R* __restrict__ Pout, Dyn* __restrict__ dyn,
-                                                   TvdArgs ta) {
+                                                   R* __restrict__ Uout, Dyn* __restrict__ dyn, TvdArgs ta) {
   const Geom& g = c.g;
   if (dyn->err) return;
   if (ta.only_two_half && !dyn->two_half) return;   // second half pass not taken this step
@@ -915,19 +968,11 @@ __global__ void __launch_bounds__(128) k_tvd_sweep(Consts c, const R* __restrict
   const R vsqr_diff = dr.vsqr_diff;
   const bool hyper = (DIR == 0) && kc<R>(c).has_vhyp;
   const KC<R>& kk_ = kc<R>(c);
-  const R vmax = dr.vmax;
-  const R emax = dr.emax;
-  const R vlim95 = dr.vlim95, elim95 = dr.elim95;
   const int istart = 1 + (c.g.periodic_x ? 0 : GH);
-  // final pass: TCheck, full ghost images, next step's pressure and statistics
-  // (unless deferred to k_step_finish: then only the interior is stored);
-  // half_images: after the first of two half passes only the periodic exchange
-  const bool final_pass = !ta.defer && ((ta.mode == 2) || (ta.mode == 1 && !dyn->two_half));
+  // after the first of two half passes the z sweep also writes the periodic
+  // images (the exchange between the halves); otherwise the interior only --
+  // k_step_finish ends the step (TCheck, images, next pressure, statistics)
   const bool half_images = (ta.mode == 1) && dyn->two_half;
-  const bool plain = !final_pass && !half_images;
-  R cmax_loc = (R)0;
-  R st_v = (R)0, st_c = (R)0, st_e = (R)0;
-  unsigned long long cnt_v = 0, cnt_e = 0;
   if (live) {
     auto xi_of = [&](int pos) { return DIR == 0 ? pos : aa; };
     TCell<R> cm1, c0, c1, c2;
@@ -965,34 +1010,13 @@ __global__ void __launch_bounds__(128) k_tvd_sweep(Consts c, const R* __restrict
       // update of cell pos (src/tvdlimit_SR.C:565-657)
       R u[NV];
       tvd_update<R>(c, dtt, F0, Fm, q0, qm, c0, uc, u);
-      if (plain) {
+      if (!half_images) {
 #pragma unroll
         for (int v = 0; v < NV; v++) Uout[(long long)v * g.N + id] = u[v];
-      } else if (half_images) {
+      } else {
         // first of two half steps: exchange (periodic dimensions) only
         int ci = DIR == 0 ? pos : aa, cj = DIR == 1 ? pos : (DIR == 0 ? aa : bb), ck = DIR == 2 ? pos : bb;
         store_state<R>(g, Uout, ci, cj, ck, images_of(g, ci, cj, ck, false), u);
-      } else if (final_pass) {
-        // finish_cell's work, written out: as a call the FP64 sweep spills more
-        tcheck_cell<R>(c, vmax, emax, u[0], u[1], u[2], u[3], u[4]);
-        int ci = DIR == 0 ? pos : aa, cj = DIR == 1 ? pos : (DIR == 0 ? aa : bb), ck = DIR == 2 ? pos : bb;
-        const Images im = images_of(g, ci, cj, ck, true);
-        store_state<R>(g, Uout, ci, cj, ck, im, u);
-        // next step's stage-1 pressure, CFL speed and Adjust_Valf_Max statistics
-        R v1, v2, v3, ei;
-        prim_from_cons(u[0], u[1], u[2], u[3], u[4], v1, v2, v3, ei);
-        const R pr = eos_pres(c, u[0], ei, (R)1.0 / u[0]);
-        store_scalar<R>(g, Pout, ci, cj, ck, im, pr);
-        R cmv = cmax_cell<R>(u[0], v1, v2, v3, u[5], u[6], u[7], pr, inv_va2max);
-        cmax_loc = smax(cmax_loc, cmv);
-        R vabs = d_sqrt(v1 * v1 + v2 * v2 + v3 * v3);
-        R cs = (R)(5 / 3.) * pr / u[0];
-        R ee = ei / u[0];
-        st_v = d_fmax(st_v, vabs);
-        st_c = d_fmax(st_c, cs);
-        st_e = d_fmax(st_e, ee);
-        if (vabs >= vlim95) cnt_v++;
-        if (ee >= elim95) cnt_e++;
       }
       // shift the window
       cm1 = c0; c0 = c1; c1 = c2;
@@ -1000,11 +1024,6 @@ __global__ void __launch_bounds__(128) k_tvd_sweep(Consts c, const R* __restrict
       for (int v = 0; v < NV; v++) { s0[v] = s1[v]; Fm[v] = F0[v]; }
       qm = q0;
     }
-  }
-  if (final_pass) {
-    FinishAcc<R> acc;
-    acc.cmax = cmax_loc; acc.v = st_v; acc.cs = st_c; acc.e = st_e; acc.nv = cnt_v; acc.ne = cnt_e;
-    acc.flush(dyn);
   }
 }
 

@@ -29,10 +29,11 @@ struct Launch {
   static void stage(const Consts& c, const R* Uin, const R* Pin, const R* U0, R* Uout, R* Pout, R* Res, Dyn* dyn,
                     int stage, bool resid, int write_pres, cudaStream_t s, const CUtensorMap* mu = nullptr,
                     const CUtensorMap* mp = nullptr, int zc = 0, R* Cc = nullptr);
-  // td: cells per thread along the y / z sweeps (0: 32); defer: the last pass
-  // stores the interior only and step_finish ends the step
-  static void tvd(const Consts& c, int dir, int mode, int only_two_half, const R* Uin, const R* Pst, R* Uout, R* Pout,
-                  Dyn* dyn, cudaStream_t s, int td = 0, int defer = 0);
+  // td: cells per thread along the y / z sweeps (0: 32); the sweeps store the
+  // interior (and after a first half pass the periodic images), step_finish
+  // then ends the step
+  static void tvd(const Consts& c, int dir, int mode, int only_two_half, const R* Uin, const R* Pst, R* Uout,
+                  Dyn* dyn, cudaStream_t s, int td = 0);
   // Clean_divB on U (phi, divb: N each); returns the number of launches
   static int divb_clean(const Consts& c, R* U, R* phi, R* divb, Dyn* dyn, cudaStream_t s);
   static void step_finish(const Consts& c, R* U, R* P, Dyn* dyn, cudaStream_t s);
@@ -156,14 +157,13 @@ void Launch<R>::stage(const Consts& c, const R* Uin, const R* Pin, const R* U0, 
 
 template <class R>
 void Launch<R>::tvd(const Consts& c, int dir, int mode, int only_two_half, const R* Uin, const R* Pst, R* Uout,
-                    R* Pout, Dyn* dyn, cudaStream_t s, int td, int defer) {
+                    Dyn* dyn, cudaStream_t s, int td) {
   const Geom& g = c.g;
   TvdArgs ta;
   ta.dir = dir;
   ta.mode = mode;
   ta.only_two_half = only_two_half;
   ta.td = td > 0 ? td : 32;
-  ta.defer = defer;
   const long long sx = 1, sy = g.sx, sz = (long long)g.sx * g.sy;
   // pencil ranges of TVDlimit's three sweeps (src/tvdlimit_SR.C:199-205, 671-672)
   if (dir == 0) {
@@ -191,9 +191,9 @@ void Launch<R>::tvd(const Consts& c, int dir, int mode, int only_two_half, const
     k_tvd_sweep_xlanes<R><<<(unsigned)nb, block, 0, s>>>(c, Uin, Pst, Uout, dyn, only_two_half);
     return;
   }
-  if (dir == 0) k_tvd_sweep<R, 0><<<(unsigned)blocks, block, 0, s>>>(c, Uin, Pst, Uout, Pout, dyn, ta);
-  else if (dir == 1) k_tvd_sweep<R, 1><<<(unsigned)blocks, block, 0, s>>>(c, Uin, Pst, Uout, Pout, dyn, ta);
-  else k_tvd_sweep<R, 2><<<(unsigned)blocks, block, 0, s>>>(c, Uin, Pst, Uout, Pout, dyn, ta);
+  if (dir == 0) k_tvd_sweep<R, 0><<<(unsigned)blocks, block, 0, s>>>(c, Uin, Pst, Uout, dyn, ta);
+  else if (dir == 1) k_tvd_sweep<R, 1><<<(unsigned)blocks, block, 0, s>>>(c, Uin, Pst, Uout, dyn, ta);
+  else k_tvd_sweep<R, 2><<<(unsigned)blocks, block, 0, s>>>(c, Uin, Pst, Uout, dyn, ta);
 }
 
 template <class R>
@@ -227,7 +227,16 @@ int Launch<R>::bc(const Consts& c, R* U, R* P, Dyn* dyn, double* part, int with_
 }
 template <class R>
 void Launch<R>::step_finish(const Consts& c, R* U, R* P, Dyn* dyn, cudaStream_t s) {
-  k_step_finish<R><<<grid_for((long long)c.g.nx * c.g.ny * c.g.nz, 256), 256, 0, s>>>(c, U, P, dyn);
+  const Geom& g = c.g;
+  const dim3 block(FIN_BX, FIN_BY);
+  // z planes per block: one wave of resident blocks (each block marches
+  // through its share of the planes), so that the statistics atomics (one per
+  // statistic and block) stay few
+  const int bxy = ((g.nx + FIN_BX - 1) / FIN_BX) * ((g.ny + FIN_BY - 1) / FIN_BY);
+  int gz = (152 * FinBlocks<R>::v) / bxy;
+  gz = gz < 1 ? 1 : (gz > g.nz ? g.nz : gz);
+  const dim3 grid((g.nx + FIN_BX - 1) / FIN_BX, (g.ny + FIN_BY - 1) / FIN_BY, gz);
+  k_step_finish<R><<<grid, block, 0, s>>>(c, U, P, dyn);
 }
 template <class R>
 void Launch<R>::cons_to_prim(const Consts& c, R* U, R* P, R* T, R* Ne, R* Ri, R* Am, cudaStream_t s) {

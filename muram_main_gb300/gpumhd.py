@@ -353,12 +353,12 @@ class MuramGPU:
         return dt.value, cfl.value, t.value, two.value
 
     PHASES = ["step_control", "stage1", "stage2", "stage3", "stage4", "tvd_x", "tvd_y", "tvd_z",
-              "tvd2_x", "tvd2_y", "tvd2_z", "divb_clean"]
+              "tvd2_x", "tvd2_y", "tvd2_z", "divb_clean", "finish"]
 
     def profile_steps(self, nsteps=2):
         """Mean duration (ms) of each launch of a fused step, timed with CUDA events
-        (divb_clean: the cleaning passes and the end-of-step pass together)."""
-        ms = np.zeros(12)
+        (divb_clean: all cleaning passes; finish: the end-of-step pass)."""
+        ms = np.zeros(13)
         self._chk(self._L.gpumhd_profile_steps(self._h, nsteps, _dptr(ms)))
         return dict(zip(self.PHASES, ms.tolist()))
 
