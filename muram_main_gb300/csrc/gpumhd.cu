@@ -61,8 +61,8 @@ struct gpumhd_ctx {
   void* phi = nullptr;   // divB cleaning potential (GridData::phi, N), persists between calls
   void* divb = nullptr;  // last divergence of B (GridData::divB, N)
   double* bnd_part = nullptr;  // per-plane sums of the physical x boundaries (nz * BND_NQ)
-  double *d_xlp3 = nullptr, *d_xs3 = nullptr;  // inverse EOS axes and tables
-  float *d_d3 = nullptr, *d_eps3 = nullptr;
+  float *d_d3 = nullptr, *d_eps3 = nullptr;  // inverse EOS tables
+  float eos_hdr[14] = {0};                    // the EOS file's header (axes of the boundary lookups)
   char err[1024] = {0};
 };
 
@@ -153,6 +153,30 @@ static void fill_kcs(gpumhd_ctx* ctx) {
   fill_kc<float>(ctx->c, ctx->c.kf, ctx->d_prof_f);
 }
 
+// The physical boundaries' lookup constants from the EOS header, as
+// eos_init forms its axes (src/eos_init.C:92-146), and B_crit, eps_top.
+template <class R>
+static void fill_bndk1(const float* h, const gpumhd_params& p, BndK<R>& b) {
+  const int N_eps = (int)h[0], N_lr = (int)h[1], N_lp3 = (int)h[2], N_s3 = (int)h[3];
+  const double eps0 = (double)h[4], eps1 = (double)h[5], lr0 = (double)h[6], lr1 = (double)h[7];
+  const double lp0 = (double)h[8], lp1 = (double)h[9], s0 = (double)h[10], s1 = (double)h[11];
+  const double del_eps = N_eps > 1 ? (eps1 - eps0) / (double(N_eps - 1)) : 1.0;
+  const double del_lr = N_lr > 1 ? (lr1 - lr0) / (double(N_lr - 1)) : 1.0;
+  const double del_lp3 = N_lp3 > 1 ? (lp1 - lp0) / (double(N_lp3 - 1)) : 1.0;
+  const double del_s3 = N_s3 > 1 ? (s1 - s0) / (double(N_s3 - 1)) : 1.0;
+  b.eps0 = (R)eps0; b.del_eps = (R)del_eps; b.inv_del_eps = (R)(1.0 / del_eps);
+  b.lr0 = (R)lr0; b.del_lr = (R)del_lr; b.inv_del_lr = (R)(1.0 / del_lr);
+  b.lp30 = (R)lp0; b.del_lp3 = (R)del_lp3; b.inv_del_lp3 = (R)(1.0 / del_lp3);
+  b.s30 = (R)s0; b.del_s3 = (R)del_s3; b.inv_del_s3 = (R)(1.0 / del_s3);
+  b.eps_off = (R)(double)h[12];
+  b.ss_off = (R)(double)h[13];
+  b.bcrit = (R)(p.bnd_bcrit / sqrt(8.0 * asin(1.0)));  // G to code units (src/boundary_pdmp_1_fftw3.C:90)
+  b.eps_top = (R)p.bnd_eps_top;
+}
+static void fill_bndk(gpumhd_ctx* ctx) {
+  fill_bndk1<double>(ctx->eos_hdr, ctx->p, ctx->c.bndd);
+}
+
 // Run constants derived from the parameters, computed with the host math
 // library exactly as the reference computes them.
 static int fill_consts(gpumhd_ctx* ctx) {
@@ -167,8 +191,6 @@ static int fill_consts(gpumhd_ctx* ctx) {
   g.xmirror = (!p.periodic_x && p.xbnd == 0) ? 1 : 0;
   c.xbnd = (!p.periodic_x && p.xbnd == 1) ? 1 : 0;
   c.bnd_top = p.bnd_top;
-  c.bnd_bcrit = p.bnd_bcrit / sqrt(8.0 * asin(1.0));  // G to code units (src/boundary_pdmp_1_fftw3.C:90)
-  c.bnd_eps_top = p.bnd_eps_top;
   for (int d = 0; d < 3; d++) {
     c.dx[d] = p.dx[d];
     c.w1[d] = 8. / (12. * p.dx[d]);
@@ -248,6 +270,7 @@ static int fill_consts(gpumhd_ctx* ctx) {
   c.hft = ctx->d_prof + g.sx;
   c.qft = ctx->d_prof + 2 * g.sx;
   fill_kcs(ctx);
+  fill_bndk(ctx);
   return GPUMHD_OK;
 }
 
@@ -444,7 +467,7 @@ extern "C" int gpumhd_destroy(gpumhd_ctx* ctx) {
   cudaFree(ctx->phi);
   cudaFree(ctx->divb);
   cudaFree(ctx->bnd_part);
-  cudaFree(ctx->d_xlp3); cudaFree(ctx->d_xs3); cudaFree(ctx->d_d3); cudaFree(ctx->d_eps3);
+  cudaFree(ctx->d_d3); cudaFree(ctx->d_eps3);
   cudaFree(ctx->dyn);
   cudaFree(ctx->dt_hist);
   cudaFree(ctx->d_xeps);
@@ -499,10 +522,10 @@ extern "C" int gpumhd_set_params(gpumhd_ctx* ctx, const gpumhd_params* p) {
   for (int t = 0; t < 6; t++) c.tab[t] = keep.tab[t];
   c.pquad = keep.pquad; c.inv_exp_xeps = keep.inv_exp_xeps; c.inv_exp_xlr = keep.inv_exp_xlr;
   c.c_pres = keep.c_pres; c.c_temp = keep.c_temp; c.kb = keep.kb; c.mun_mh = keep.mun_mh;
-  c.ss_off = keep.ss_off; c.N_lp3 = keep.N_lp3; c.N_s3 = keep.N_s3;
-  c.inv_del_lp3 = keep.inv_del_lp3; c.inv_del_s3 = keep.inv_del_s3;
-  c.xlp3 = keep.xlp3; c.xs3 = keep.xs3; c.d3 = keep.d3; c.eps3 = keep.eps3;
+  c.N_lp3 = keep.N_lp3; c.N_s3 = keep.N_s3;
+  c.d3 = keep.d3; c.eps3 = keep.eps3;
   fill_kcs(ctx);
+  fill_bndk(ctx);
   ctx->hdyn.dt = p->dt;
   ctx->hdyn.time = p->time;
   if (ctx->graph) { cudaGraphExecDestroy(ctx->graph); ctx->graph = nullptr; }
@@ -584,16 +607,11 @@ extern "C" int gpumhd_eos_init(gpumhd_ctx* ctx, const char* path) {
     CK(cudaMemcpy(ctx->d_inv_xeps, ie.data(), sizeof(float) * N_eps, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(ctx->d_inv_xlr, ir.data(), sizeof(float) * N_lr, cudaMemcpyHostToDevice));
   }
-  cudaFree(ctx->d_xlp3); cudaFree(ctx->d_xs3); cudaFree(ctx->d_d3); cudaFree(ctx->d_eps3);
-  ctx->d_xlp3 = ctx->d_xs3 = nullptr;
+  cudaFree(ctx->d_d3); cudaFree(ctx->d_eps3);
   ctx->d_d3 = ctx->d_eps3 = nullptr;
-  double del_lp3 = 0.0, del_s3 = 0.0;
   if (have_inv) {
-    del_lp3 = (lp1 - lp0) / (double(N_lp3 - 1));
-    del_s3 = (s1 - s0) / (double(N_s3 - 1));
-    std::vector<double> xlp3(N_lp3), xs3(N_s3);
-    for (int i = 0; i < N_lp3; i++) xlp3[i] = lp0 + del_lp3 * ((double)i);
-    for (int i = 0; i < N_s3; i++) xs3[i] = s0 + del_s3 * ((double)i);
+    const double del_lp3 = (lp1 - lp0) / (double(N_lp3 - 1));
+    const double del_s3 = (s1 - s0) / (double(N_s3 - 1));
     std::vector<float> eps3(n3), d3(n3);
     const double sc3 = del_lp3 * del_s3;
     for (int i = 0; i < N_lp3; i++)
@@ -601,22 +619,17 @@ extern "C" int gpumhd_eos_init(gpumhd_ctx* ctx, const char* path) {
         eps3[(size_t)i * N_s3 + j] = (float)(((double)b3[(size_t)j * N_lp3 + i]) / sc3);
         d3[(size_t)i * N_s3 + j] = (float)(((double)b3[n3 + (size_t)j * N_lp3 + i]) / sc3);
       }
-    CK(cudaMalloc(&ctx->d_xlp3, sizeof(double) * N_lp3));
-    CK(cudaMalloc(&ctx->d_xs3, sizeof(double) * N_s3));
     CK(cudaMalloc(&ctx->d_eps3, sizeof(float) * n3));
     CK(cudaMalloc(&ctx->d_d3, sizeof(float) * n3));
-    CK(cudaMemcpy(ctx->d_xlp3, xlp3.data(), sizeof(double) * N_lp3, cudaMemcpyHostToDevice));
-    CK(cudaMemcpy(ctx->d_xs3, xs3.data(), sizeof(double) * N_s3, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(ctx->d_eps3, eps3.data(), sizeof(float) * n3, cudaMemcpyHostToDevice));
     CK(cudaMemcpy(ctx->d_d3, d3.data(), sizeof(float) * n3, cudaMemcpyHostToDevice));
   }
   Consts& c = ctx->c;
   c.N_lp3 = have_inv ? N_lp3 : 0;
   c.N_s3 = have_inv ? N_s3 : 0;
-  c.inv_del_lp3 = have_inv ? 1.0 / del_lp3 : 0.0;
-  c.inv_del_s3 = have_inv ? 1.0 / del_s3 : 0.0;
-  c.xlp3 = ctx->d_xlp3; c.xs3 = ctx->d_xs3; c.d3 = ctx->d_d3; c.eps3 = ctx->d_eps3;
-  c.ss_off = (double)h[13];
+  c.d3 = ctx->d_d3; c.eps3 = ctx->d_eps3;
+  memcpy(ctx->eos_hdr, h, sizeof(h));
+  fill_bndk(ctx);
   c.N_eps = N_eps; c.N_lr = N_lr;
   c.eps_off = eps_off;
   c.xeps0 = xeps[0]; c.xlr0 = xlr[0]; c.xepsN = xeps[N_eps - 1]; c.xlrN = xlr[N_lr - 1];
@@ -682,7 +695,10 @@ static int ensure_bnd(gpumhd_ctx* ctx) {
   if (!ctx->c.xbnd) return GPUMHD_OK;
   if (!ctx->eos_loaded) return fail(ctx, GPUMHD_E_ORDER, "physical x boundaries before eos_init");
   if (!ctx->c.d3) return fail(ctx, GPUMHD_E_EOS, "the open bottom needs the EOS file's inverse tables");
-  if (!ctx->bnd_part) CK(cudaMalloc(&ctx->bnd_part, sizeof(double) * BND_NQ * ctx->c.g.nz));
+  if (!ctx->bnd_part) {
+    const long long nb = (long long)((ctx->c.g.ny + BND_BX - 1) / BND_BX) * ((ctx->c.g.nz + BND_BY - 1) / BND_BY);
+    CK(cudaMalloc(&ctx->bnd_part, sizeof(double) * BND_NQ * nb));
+  }
   return GPUMHD_OK;
 }
 

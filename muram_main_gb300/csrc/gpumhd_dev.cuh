@@ -45,6 +45,16 @@ struct KC {
   int has_visc_slope, has_eta_slope, has_vmax_lim, has_vhyp;
 };
 
+// Constants of the physical x boundaries' EOS lookups and formulas: table
+// axes as x0 + del*i (src/eos_init.C:125-146), offsets, B_crit (code units)
+// and eps_top.
+template <class R>
+struct BndK {
+  R eps0, del_eps, inv_del_eps, lr0, del_lr, inv_del_lr;
+  R lp30, del_lp3, inv_del_lp3, s30, del_s3, inv_del_s3;
+  R eps_off, ss_off, bcrit, eps_top;
+};
+
 // Constants of a run (copied by value into every kernel).
 struct Consts {
   Geom g;
@@ -79,15 +89,12 @@ struct Consts {
   int divb_on, divb_itmax;
   double divb_err, divb_err_unit, divb_fac_d;
   // physical x boundaries (src/boundary_pdmp_1_fftw3.C:81-565): on, top mode,
-  // B_crit in code units, eps_top; the EOS's entropy offset and inverse tables
+  // the EOS's inverse tables and the lookup constants per precision
   int xbnd, bnd_top;
-  double bnd_bcrit, bnd_eps_top, ss_off;
   int N_lp3, N_s3;
-  double inv_del_lp3, inv_del_s3;
-  const double* xlp3;
-  const double* xs3;
   const float* d3;     // ln rho (p, s), [i_lp*N_s3 + j_s], pre-divided
   const float* eps3;   // ln eps (p, s)
+  BndK<double> bndd;
   double rt_cfl;
   double CFL, CFL_tvd, dt_rad, rt_tstep, outcad;
   double va_max, va_adjust, max_fill;

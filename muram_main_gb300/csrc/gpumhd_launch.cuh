@@ -219,10 +219,11 @@ int Launch<R>::divb_clean(const Consts& c, R* U, R* phi, R* divb, Dyn* dyn, cuda
 template <class R>
 int Launch<R>::bc(const Consts& c, R* U, R* P, Dyn* dyn, double* part, int with_cmax, cudaStream_t s) {
   const Geom& g = c.g;
-  k_bc_sums<R><<<g.nz, BND_THREADS, 0, s>>>(c, U, dyn, part);
-  k_bc_setup<<<1, 32, 0, s>>>(c, dyn, part);
+  const dim3 gs((g.ny + BND_BX - 1) / BND_BX, (g.nz + BND_BY - 1) / BND_BY);
+  k_bc_sums<R><<<gs, dim3(BND_BX, BND_BY), 0, s>>>(c, U, dyn, part);
+  k_bc_setup<<<1, BND_SETUP_THREADS, 0, s>>>(c, dyn, part, (int)(gs.x * gs.y));
   const long long cols = (long long)g.sy * g.sz;
-  k_bc_ghosts<R><<<(unsigned)((cols + BND_THREADS - 1) / BND_THREADS), BND_THREADS, 0, s>>>(c, U, P, dyn, with_cmax);
+  k_bc_ghosts<R><<<(unsigned)((2 * cols + BND_THREADS - 1) / BND_THREADS), BND_THREADS, 0, s>>>(c, U, P, dyn, with_cmax);
   return 3;
 }
 template <class R>

@@ -94,16 +94,23 @@ __global__ void k_divb_end(Consts c, Dyn* dyn) {
 }
 
 
-__global__ void k_bc_setup(Consts c, Dyn* dyn, const double* __restrict__ part) {
+__global__ void k_bc_setup(Consts c, Dyn* dyn, const double* __restrict__ part, int nb) {
   if (dyn->err) return;
-  const int lane = threadIdx.x;
+  __shared__ double sh[BND_NQ][BND_SETUP_THREADS];
+  const int tid = threadIdx.x;
   double t[BND_NQ];
   for (int q = 0; q < BND_NQ; q++) t[q] = 0.0;
-  for (int k = lane; k < c.g.nz; k += 32)
+  for (int k = tid; k < nb; k += BND_SETUP_THREADS)
     for (int q = 0; q < BND_NQ; q++) t[q] += part[(long long)k * BND_NQ + q];
-  for (int o = 16; o > 0; o >>= 1)
-    for (int q = 0; q < BND_NQ; q++) t[q] += __shfl_xor_sync(0xffffffffu, t[q], o);
-  if (lane != 0) return;
+  for (int q = 0; q < BND_NQ; q++) sh[q][tid] = t[q];
+  __syncthreads();
+  for (int st = BND_SETUP_THREADS / 2; st > 0; st >>= 1) {
+    if (tid < st)
+      for (int q = 0; q < BND_NQ; q++) sh[q][tid] += sh[q][tid + st];
+    __syncthreads();
+  }
+  if (tid != 0) return;
+  for (int q = 0; q < BND_NQ; q++) t[q] = sh[q][0];
   const double n = (double)(c.g.ny * c.g.nz);
   if (dyn->bnd_ini) {
     const double b0 = t[2] / n, b1 = t[3] / n;

@@ -6,7 +6,8 @@ against the oracle, whose restatement is bit-pinned to the reference on the
 closed and half-open tops, a fixed top energy and a low B_crit.  The two mean
 pressures of the bottom layers are summed in another order on the GPU than in
 the reference (an ulp), so FP64 is held to the same 1e-12 relative
-L-infinity bar as the other fused paths; FP32 to 1e-5 relative L2.
+L-infinity bar as the other fused paths; FP32 to 1e-5 relative L2 (its
+boundary arithmetic is FP64, like the reference's).
 """
 import numpy as np
 import pytest
