@@ -293,7 +293,8 @@ void mo_adjust_valf_max(mo_params* p, const double* U, const double* pres, doubl
  * of the two other dimensions: fluxes at every pencil point, 4th-order central
  * derivative, Lorentz force blended between Maxwell stress and curl B x B by
  * the Boris factor, accumulated into R.  cmax covers every pencil point. */
-double mo_mhd_residual(const mo_params* p, const double* U, const double* pres, double* R) {
+double mo_mhd_residual_ex(const mo_params* p, const double* U, const double* pres, const double* temp, double* R,
+                          mo_fields* f) {
   geom g = geom_of(p);
   const int n[3] = {p->nx, p->ny, p->nz};
   const long st[3] = {1, g.sx, (long)g.sx * g.sy};
@@ -317,6 +318,31 @@ double mo_mhd_residual(const mo_params* p, const double* U, const double* pres, 
   const int needs_curlB = eta > 0.0;
   double* curlB = needs_curlB ? (double*)calloc((size_t)3 * g.N, sizeof(double)) : NULL;
   static const double sgn[3] = {-1., 1., -1.};
+  /* hyperbolic Spitzer conduction (src/mhdres_SR.C:33-46, 121-145, 251-253,
+   * 355-358, 492-521, 668-692): the heat flux sflx along B enters the energy
+   * flux; BgradT accumulates B.grad(T) over the passes, Rflx a hyperdiffusion
+   * of sflx per pass and, in the last pass, the relaxation towards the
+   * saturated Spitzer flux.  cmax_hyp and friends come from the previous dt. */
+  const int spitzer = p->spitzer > 0.0 && f && f->sflx;
+  const double CFL_hyp = 1.8, avr_max = 0.25, eps_hyp = 0.02;
+  const double k0_spt = p->spitzer;
+  const double Rgas = 8.314e7, X_H = 0.7;
+  const double sat_flx = (1.0 + X_H) * pow(Rgas, 1.5) * sqrt(1836.) / 8.0;
+  double cmax_hyp, nu_hyp_max, hyp_diff;
+  if (p->dt > 0.0) {
+    cmax_hyp = smin(p->CFL, CFL_hyp) * dxmin / p->dt;
+    nu_hyp_max = avr_max / p->dt;
+    hyp_diff = eps_hyp / p->dt;
+  } else {
+    cmax_hyp = 0.0;
+    nu_hyp_max = avr_max * cmax_hyp / (smin(p->CFL, CFL_hyp) * dxmin);
+    hyp_diff = eps_hyp * cmax_hyp / (smin(p->CFL, CFL_hyp) * dxmin);
+  }
+  double* sfl = (double*)malloc(sizeof(double) * L);
+  double* vvl = (double*)malloc(sizeof(double) * L);
+  double* bbl = (double*)malloc(sizeof(double) * L);
+  if (spitzer)
+    for (long c = 0; c < g.N; c++) f->BgradT[c] = 0.0;
   for (int d = 0; d < 3; d++) {
     const int d1 = order[d][0], d2 = order[d][1], d3 = order[d][2];
     const double dx = p->dx[d1];
@@ -344,7 +370,9 @@ double mo_mhd_residual(const mo_params* p, const double* U, const double* pres, 
           lf1[i] = s / (s + x4);
           double pr = pres[c];
           double cs2 = 5.0 / 3.0 * pr * dn;
+          bbl[i] = bb;
           vv = sqrt(vv);
+          vvl[i] = vv;
           cmax = smax(cmax, vv + 0.0 + sqrt(smax(cs2, lf1[i] * (cs2 + va2))));
           double mflx = vel * r0;
           flx[0 * L + i] = mflx;
@@ -352,6 +380,10 @@ double mo_mhd_residual(const mo_params* p, const double* U, const double* pres, 
           flx[2 * L + i] = mflx * r2 + pd[1] * pr;
           flx[3 * L + i] = mflx * r3 + pd[2] * pr;
           flx[4 * L + i] = vel * (r4 + ekin + pr);
+          if (spitzer) {
+            sfl[i] = f->sflx[c];
+            flx[4 * L + i] += sfl[i] * var[(5 + d1) * L + i];
+          }
           flx[5 * L + i] = vel * b5 - r1 * mag;
           flx[6 * L + i] = vel * b6 - r2 * mag;
           flx[7 * L + i] = vel * b7 - r3 * mag;
@@ -401,10 +433,30 @@ double mo_mhd_residual(const mo_params* p, const double* U, const double* pres, 
             }
           }
           for (int v = 0; v < NV; v++) R[v * g.N + c] += res[v];
+          if (spitzer) {
+            const long np1 = c + st[d1], np2 = c + 2 * st[d1], nm1 = c - st[d1], nm2 = c - 2 * st[d1];
+            const double* T = temp;
+            f->BgradT[c] += (var[(5 + d1) * L + i] * (w1 * (T[np1] - T[nm1]) + w2 * (T[np2] - T[nm2])));
+            f->Rflx[c] -= hyp_diff * ((sfl[i + 2] + sfl[i - 2]) - 4. * (sfl[i + 1] + sfl[i - 1]) + 6. * sfl[i]);
+            if (d == 2) {  /* the last pass: relaxation to the limited Spitzer flux */
+              const double tempi = T[c];
+              const double c_lim = cmax_hyp - vvl[i];
+              const double tt32 = tempi * sqrt(tempi);
+              double kap_spt = k0_spt * tempi * tt32;
+              const double F_sat = sat_flx * var[i] * tt32;
+              const double invBB = 1.0 / smax(1e-100, bbl[i]);
+              double F_spt = -kap_spt * f->BgradT[c];
+              const double f_lim = F_sat / (F_sat + fabs(F_spt * sqrt(invBB)));
+              F_spt *= invBB * f_lim;
+              kap_spt *= f_lim;
+              const double nu_hyp = smin(c_lim * c_lim * var[4 * L + i] / (tempi * kap_spt), nu_hyp_max);
+              f->Rflx[c] += nu_hyp * (F_spt - sfl[i]);
+            }
+          }
         }
       }
   }
-  free(var); free(flx); free(ms); free(lf1); free(curlB);
+  free(var); free(flx); free(ms); free(lf1); free(curlB); free(sfl); free(vvl); free(bbl);
   double dt_cfl = dxmin / cmax;
   if (needs_curlB) {
     const double dt_diff_fac = 0.5 / (1. / (p->dx[0] * p->dx[0]) + 1. / (p->dx[1] * p->dx[1]) + 1. / (p->dx[2] * p->dx[2]));
@@ -413,6 +465,10 @@ double mo_mhd_residual(const mo_params* p, const double* U, const double* pres, 
     dt_cfl = smin(dt_cfl, dt_res);
   }
   return dt_cfl;
+}
+
+double mo_mhd_residual(const mo_params* p, const double* U, const double* pres, double* R) {
+  return mo_mhd_residual_ex(p, U, pres, NULL, R, NULL);
 }
 
 /* ----------------------------------------------------------- Sync_timestep */
@@ -456,7 +512,7 @@ static void tcheck_cell(const mo_params* p, double* U, long N, long c) {
   U[3 * N + c] = mz * s;
 }
 
-void mo_source_integrate_tcheck(const mo_params* p, double* U, const double* U0, double* R, int stage) {
+void mo_source_integrate_ex(const mo_params* p, double* U, const double* U0, double* R, int stage, mo_fields* f) {
   geom g = geom_of(p);
   const long N = g.N;
   const double wdt = p->dt / ((double)(4 + 1 - stage));
@@ -500,7 +556,16 @@ void mo_source_integrate_tcheck(const mo_params* p, double* U, const double* U0,
         }
         /* Tcheck (:444-465) */
         tcheck_cell(p, U, N, c);
+        /* hyperbolic conduction (:410-419) */
+        if (p->spitzer > 0.0 && f && f->sflx) {
+          f->sflx[c] = f->sflx0[c] + wdt * f->Rflx[c];
+          f->Rflx[c] = 0;
+        }
       }
+}
+
+void mo_source_integrate_tcheck(const mo_params* p, double* U, const double* U0, double* R, int stage) {
+  mo_source_integrate_ex(p, U, U0, R, stage, NULL);
 }
 
 /* --------------------------------------------------- ghost fill / boundary */
@@ -996,14 +1061,42 @@ static void set_boundary_conditions(mo_params* p, const mo_eos* e, double* U) {
     }
 }
 
-void mo_boundaries_eos(mo_params* p, const mo_eos* e, double* U) {
+/* the heat flux's boundary values (src/boundary_pdmp_1_fftw3.C:302-306, 426-438):
+ * zero in the bottom ghosts; at the top symmetric with eps_top > 0, else zero
+ * in the two top layers and their ghosts */
+static void sflx_boundaries(const mo_params* p, double* sflx) {
+  geom g = geom_of(p);
+  const int lb = GH, le = GH + p->nx - 1;
+  for (int k = 0; k < g.sz; k++)
+    for (int j = 0; j < g.sy; j++) {
+      sflx[at(&g, lb - 1, j, k)] = 0.0;
+      sflx[at(&g, lb - 2, j, k)] = 0.0;
+      if (p->bnd_eps_top > 0.0) {
+        sflx[at(&g, le + 1, j, k)] = sflx[at(&g, le, j, k)];
+        sflx[at(&g, le + 2, j, k)] = sflx[at(&g, le - 1, j, k)];
+      } else {
+        sflx[at(&g, le - 1, j, k)] = 0.0;
+        sflx[at(&g, le, j, k)] = 0.0;
+        sflx[at(&g, le + 1, j, k)] = 0.0;
+        sflx[at(&g, le + 2, j, k)] = 0.0;
+      }
+    }
+}
+
+void mo_boundaries_ex(mo_params* p, const mo_eos* e, double* U, mo_fields* f, int needs_sflx) {
+  const int spitzer = p->spitzer > 0.0 && f && f->sflx;
   if (p->xbnd == 1 && !p->periodic_x) {
     mo_exchange_only(p, U);
+    if (spitzer && needs_sflx) exchange_fields(p, f->sflx, 0, 1);
     set_boundary_conditions(p, e, U);
+    if (spitzer) sflx_boundaries(p, f->sflx);
   } else {
     mo_boundaries(p, U);
+    if (spitzer && needs_sflx) exchange_fields(p, f->sflx, 0, 1);
   }
 }
+
+void mo_boundaries_eos(mo_params* p, const mo_eos* e, double* U) { mo_boundaries_ex(p, e, U, NULL, 1); }
 
 /* ------------------------------------------------------------- Clean_divB */
 /* Fourth-order divergence of B at interior cell (i, j, k), summed over the
@@ -1108,24 +1201,29 @@ void mo_clean_divB(mo_params* p, double* U, double* phi, double* divB) {
 }
 
 /* --------------------------------------------------------------- full step */
-int mo_step_divb(mo_params* p, const mo_eos* eos, double* U, double* U0, double* R, double* aux5, double* phi,
-                 double* divB) {
+int mo_step_ex(mo_params* p, const mo_eos* eos, double* U, double* U0, double* R, double* aux5, mo_fields* f) {
   geom g = geom_of(p);
   const long N = g.N;
   double* pres = aux5;
   double cfl = 0.0;
+  const int spitzer = p->spitzer > 0.0;
+  if (spitzer && !(f && f->sflx && f->sflx0 && f->Rflx && f->BgradT)) return -11;
   mo_save_cons(p, U, U0);
+  if (spitzer)  /* SaveCons's heat-flux copy (src/Add_Sources_Integrate_SR.C:503-516) */
+    for (int k = GH; k < GH + p->nz; k++)
+      for (int j = GH; j < GH + p->ny; j++)
+        for (int i = GH; i < GH + p->nx; i++) f->sflx0[at(&g, i, j, k)] = f->sflx[at(&g, i, j, k)];
   for (int stage = 1; stage <= 4; stage++) {
     mo_cons_to_prim(p, eos, U, pres, aux5 + N, aux5 + 2 * N, aux5 + 3 * N, aux5 + 4 * N);
     if (stage == 1) mo_adjust_valf_max(p, U, pres, NULL);
-    double dt_mhd = mo_mhd_residual(p, U, pres, R);
+    double dt_mhd = mo_mhd_residual_ex(p, U, pres, aux5 + N, R, f);
     if (stage == 1) {
       int rc = mo_sync_timestep(p, p->dt_rad, dt_mhd, &cfl);
       if (rc) return rc;
       p->last_cfl = cfl;
     }
-    mo_source_integrate_tcheck(p, U, U0, R, stage);
-    mo_boundaries_eos(p, eos, U);
+    mo_source_integrate_ex(p, U, U0, R, stage, f);
+    mo_boundaries_ex(p, eos, U, f, 1);
   }
   if (cfl <= p->CFL_tvd) {
     p->tvd_two_half_steps = 0;
@@ -1137,13 +1235,19 @@ int mo_step_divb(mo_params* p, const mo_eos* eos, double* U, double* U0, double*
     mo_tvdlimit(p, U, pres, 0.5 * p->dt);
   }
   if (p->divB_switch > 0) {
-    if (!phi || !divB) return -10;
-    mo_clean_divB(p, U, phi, divB);
+    if (!(f && f->phi && f->divB)) return -10;
+    mo_clean_divB(p, U, f->phi, f->divB);
   }
   mo_tcheck(p, U);
-  mo_boundaries_eos(p, eos, U);
+  mo_boundaries_ex(p, eos, U, f, 0);
   p->time += p->dt;
   return 0;
+}
+
+int mo_step_divb(mo_params* p, const mo_eos* eos, double* U, double* U0, double* R, double* aux5, double* phi,
+                 double* divB) {
+  mo_fields f = {phi, divB, NULL, NULL, NULL, NULL};
+  return mo_step_ex(p, eos, U, U0, R, aux5, &f);
 }
 
 int mo_step(mo_params* p, const mo_eos* eos, double* U, double* U0, double* R, double* aux5) {

@@ -50,9 +50,19 @@ typedef struct {
   int xbnd, bnd_top;
   double bnd_bcrit, bnd_eps_top, p_bc, s_bc;
   int bnd_ini;
+  /* PhysicsData::params[i_param_spitzer]: Spitzer coefficient of the hyperbolic
+   * heat conduction (0: off) */
+  double spitzer;
 } mo_params;
 
 typedef struct mo_eos mo_eos;
+
+/* Fields beyond the state that some settings evolve (NULL where unused):
+ * divB cleaning's phi and last divergence; Spitzer conduction's heat flux
+ * sflx, its stage-start copy sflx0, its residual Rflx and B.grad(T). N each. */
+typedef struct {
+  double *phi, *divB, *sflx, *sflx0, *Rflx, *BgradT;
+} mo_fields;
 
 void mo_default_params(mo_params* p, int nx, int ny, int nz, double dx);
 mo_eos* mo_eos_load(const char* path);
@@ -68,16 +78,23 @@ void mo_cons_to_prim(const mo_params* p, const mo_eos* eos, double* U, double* p
 void mo_adjust_valf_max(mo_params* p, const double* U, const double* pres, double* stats);
 /* src/mhdres_SR.C:27-854 (ideal MHD branch); returns dt_mhd */
 double mo_mhd_residual(const mo_params* p, const double* U, const double* pres, double* R);
+/* the same with the Spitzer terms when p->spitzer > 0 (temp: ConsToPrim's T) */
+double mo_mhd_residual_ex(const mo_params* p, const double* U, const double* pres, const double* temp, double* R,
+                          mo_fields* f);
 /* src/solver.C:487-548; returns 0 or a negative error code */
 int mo_sync_timestep(mo_params* p, double dt_rad, double dt_mhd, double* cfl);
 /* src/Add_Sources_Integrate_SR.C:38-472 (no-diagnostics branch) */
 void mo_source_integrate_tcheck(const mo_params* p, double* U, const double* U0, double* R, int stage);
+void mo_source_integrate_ex(const mo_params* p, double* U, const double* U0, double* R, int stage, mo_fields* f);
 /* src/exchange.C:532-783 on one rank plus the closed-x mirror rule */
 void mo_boundaries(const mo_params* p, double* U);
 void mo_exchange_only(const mo_params* p, double* U);
 /* exchange, then the x boundaries p->xbnd selects (src/boundary_pdmp_1_fftw3.C:81-565
  * for xbnd = 1, which needs the EOS's inverse tables) */
 void mo_boundaries_eos(mo_params* p, const mo_eos* eos, double* U);
+/* the same with the heat flux: exchanged when needs_sflx (src/exchange.C:590-760),
+ * and its boundary values with the physical x boundaries */
+void mo_boundaries_ex(mo_params* p, const mo_eos* eos, double* U, mo_fields* f, int needs_sflx);
 /* src/tvdlimit_SR.C:33-695 */
 void mo_tvdlimit(const mo_params* p, double* U, const double* pres, double dt_tvd);
 /* src/Add_Sources_Integrate_SR.C:534-625 */
@@ -91,6 +108,8 @@ int mo_step(mo_params* p, const mo_eos* eos, double* U, double* U0, double* R, d
  * p->divB_switch > 0; phi and divB as for mo_clean_divB. */
 int mo_step_divb(mo_params* p, const mo_eos* eos, double* U, double* U0, double* R, double* aux5, double* phi,
                  double* divB);
+/* One step with every optional field (divB cleaning, Spitzer conduction) */
+int mo_step_ex(mo_params* p, const mo_eos* eos, double* U, double* U0, double* R, double* aux5, mo_fields* f);
 
 #ifdef __cplusplus
 }

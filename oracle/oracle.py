@@ -38,7 +38,12 @@ class MoParams(C.Structure):
         ("xbnd", C.c_int), ("bnd_top", C.c_int),
         ("bnd_bcrit", C.c_double), ("bnd_eps_top", C.c_double), ("p_bc", C.c_double), ("s_bc", C.c_double),
         ("bnd_ini", C.c_int),
+        ("spitzer", C.c_double),
     ]
+
+
+class MoFields(C.Structure):
+    _fields_ = [(n, C.POINTER(C.c_double)) for n in ("phi", "divB", "sflx", "sflx0", "Rflx", "BgradT")]
 
 
 _lib = None
@@ -77,6 +82,8 @@ def lib():
         L.mo_step.argtypes = [P, C.c_void_p, dp, dp, dp, dp]
         L.mo_clean_divB.argtypes = [P, dp, dp, dp]
         L.mo_boundaries_eos.argtypes = [P, C.c_void_p, dp]
+        L.mo_step_ex.restype = C.c_int
+        L.mo_step_ex.argtypes = [P, C.c_void_p, dp, dp, dp, dp, C.POINTER(MoFields)]
         L.mo_step_divb.restype = C.c_int
         L.mo_step_divb.argtypes = [P, C.c_void_p, dp, dp, dp, dp, dp, dp]
         _lib = L
@@ -117,7 +124,7 @@ def params_from_harness(hp):
     simple = {"CFL": "CFL", "CFL_tvd": "CFL_tvd", "grav": "grav", "va_max": "va_max",
               "va_adjust": "va_adjust", "max_fill": "max_fill", "tau0": "tau0", "dt_rad": "dt_rad", "eta": "eta",
               "divB_err": "divB_err", "bnd_bcrit": "bnd_bcrit", "bnd_eps_top": "bnd_eps_top",
-              "p_bc": "p_bc", "s_bc": "s_bc"}
+              "p_bc": "p_bc", "s_bc": "s_bc", "spitzer": "spitzer"}
     for k, a in simple.items():
         if k in hp:
             kw[a] = float(hp[k])
@@ -156,6 +163,13 @@ class State:
         self.aux = np.zeros((5,) + self.U.shape[1:])
         self.phi = np.zeros(self.U.shape[1:])
         self.divB = np.zeros(self.U.shape[1:])
+        self.sflx = np.zeros(self.U.shape[1:])
+        self.sflx0 = np.zeros(self.U.shape[1:])
+        self.Rflx = np.zeros(self.U.shape[1:])
+        self.BgradT = np.zeros(self.U.shape[1:])
+        ptr = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+        self._f = MoFields(ptr(self.phi), ptr(self.divB), ptr(self.sflx), ptr(self.sflx0), ptr(self.Rflx),
+                           ptr(self.BgradT))
         self.divb_log = []
         if p.xbnd == 1 and not p.periodic_x:
             if eos is None:
@@ -167,7 +181,7 @@ class State:
     def step(self, eos, n=1):
         dts = []
         for _ in range(n):
-            rc = lib().mo_step_divb(C.byref(self.p), eos.ptr, self.U, self.U0, self.R, self.aux, self.phi, self.divB)
+            rc = lib().mo_step_ex(C.byref(self.p), eos.ptr, self.U, self.U0, self.R, self.aux, C.byref(self._f))
             if rc:
                 raise RuntimeError(f"oracle step failed: {rc}")
             dts.append((self.p.dt, self.p.last_cfl))

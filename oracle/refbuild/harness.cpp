@@ -7,6 +7,7 @@
 // With xbnd = 1 a closed x dimension gets the reference's own physical
 // boundaries (SetBoundaryConditions, src/boundary_pdmp_1_fftw3.C:81-493:
 // open bottom, top per bnd_top; no potential field) instead of the mirror.
+// With spitzer > 0 the hyperbolic heat conduction runs (heat flux sflx from zero).
 // With divB_switch > 0 the reference's Clean_divB runs after the TVD pass, as
 // in src/solver.C:341-345; phi starts at zero.
 //
@@ -198,7 +199,7 @@ int main(int argc, char** argv) {
   Physics.params[i_param_va_max] = par_d("va_max", 1e7);
   Physics.params[i_param_va_adjust] = par_d("va_adjust", 0.0);
   Physics.params[i_param_max_fill] = par_d("max_fill", 1000.);
-  Physics.params[i_param_spitzer] = 0.0;
+  Physics.params[i_param_spitzer] = par_d("spitzer", 0.0);
   Physics.params[i_param_eta] = par_d("eta", 0.0);
   Physics.params[i_param_ambipolar] = 0.0;
   par_arr("tvd_h", Physics.tvd_h, 4);
@@ -258,6 +259,7 @@ int main(int argc, char** argv) {
     Grid.U0[i].zero();
     Grid.pres[i] = Grid.temp[i] = Grid.ne[i] = Grid.rhoi[i] = Grid.amb[i] = 0.0;
     Grid.phi[i] = Grid.divB[i] = 0.0;  // Grid.C:284-285 leaves them unset; the cleaning starts from phi = 0
+    if (Grid.sflx) Grid.sflx[i] = Grid.sflx0[i] = Grid.Rflx[i] = Grid.BgradT[i] = 0.0;  // heat flux starts at zero
   }
 
   eos_init(Grid, Run, Physics);
@@ -340,6 +342,7 @@ int main(int argc, char** argv) {
     Run.Advance();
   }
   dump("final_U", Grid.U, ubytes);
+  if (Grid.sflx) dump("final_sflx", Grid.sflx, Grid.bufsize * sizeof(double));
   if (Physics.divB[i_divB_switch] > 0) {
     dump("final_phi", Grid.phi, Grid.bufsize * sizeof(double));
     dump("final_divB", Grid.divB, Grid.bufsize * sizeof(double));

@@ -80,7 +80,7 @@ def run(U, params, steps=1, trace_step=0, keep=None):
                 a = np.ascontiguousarray(np.moveaxis(a.reshape(sz, sy, sx, 8), -1, 0))
             elif name.endswith("_aux"):
                 a = a.reshape(5, sz, sy, sx)
-            elif name in ("final_phi", "final_divB", "divb_phi_in"):
+            elif name in ("final_phi", "final_divB", "divb_phi_in", "final_sflx"):
                 a = a.reshape(sz, sy, sx)
             out[name] = a
     return out

@@ -6,6 +6,8 @@ stores, per case, the initial state and the PCAST-style snapshots around each
 routine of one traced step, the state after several steps, and the per-step
 dt.  The EOS table is the committed ``eos_small.dat``.
 
+The spitzer case adds the hyperbolic heat conduction (heat flux from zero,
+hot top) and keeps the final heat flux.
 The open_bottom case uses the reference's own physical x boundaries (open
 bottom, top open to outflows) and keeps the p_bc and s_bc they set.
 The divb_cleaning case also runs the reference's Clean_divB after each TVD
@@ -45,6 +47,9 @@ def cases():
     yield "divb_cleaning", dict(nx=10, ny=8, nz=6, dx=1.6e6, dy=1.2e6, dz=1.4e6, periodic_x=0, grav=2.74e4,
                                 divB_switch=1, divB_itmax=4, divB_err=0.15, verbose=1), \
         initial.stratified_box(eos, 10, 8, 6, dx=1.6e6, seed=14), dict(steps=5, trace_step=2)
+    yield "spitzer", dict(nx=12, ny=8, nz=6, dx=1.6e6, periodic_x=0, grav=2.74e4, xbnd=1, bnd_top=1,
+                          bnd_eps_top=3e12, spitzer=1.0), \
+        initial.stratified_box(eos, 12, 8, 6, dx=1.6e6, seed=16), dict(steps=6, trace_step=3)
     yield "open_bottom", dict(nx=12, ny=8, nz=6, dx=1.6e6, periodic_x=0, grav=2.74e4, xbnd=1, bnd_top=1), \
         initial.stratified_box(eos, 12, 8, 6, dx=1.6e6, seed=15), dict(steps=4, trace_step=2)
 
@@ -73,6 +78,8 @@ def main(only=()):
         hp["eos"] = EOS
         out = refrun.run(U, hp, **run)
         keep = KEEP_DIVB if hp.get("divB_switch", 0) else (KEEP_BND if hp.get("xbnd", 0) else KEEP)
+        if hp.get("spitzer", 0):
+            keep = ["init_U", "final_U", "final_sflx", "dts", "limits"]
         arrays = {k: out[k] for k in keep if k in out}
         arrays["input_U"] = U
         arrays["trace_step"] = np.array(run["trace_step"])

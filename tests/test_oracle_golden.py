@@ -116,6 +116,24 @@ def test_open_bottom_bitexact(eos):
     assert np.array_equal(U, d["s1_bc_U"])
 
 
+def test_spitzer_bitexact(eos):
+    """Hyperbolic Spitzer conduction (heat flux along B with its hyperdiffusion
+    and relaxation to the saturation-limited Spitzer flux; physical x
+    boundaries with a hot top): state and heat flux match the reference bit
+    for bit, and the conduction changes the energy well above rounding."""
+    d, hp = H.load_case("spitzer")
+    st = O.State(H.oracle_params(hp), d["input_U"], eos)
+    dts = st.step(eos, int(d["steps"]))
+    assert [x[0] for x in dts] == list(d["dts"].reshape(-1, 3)[:, 0])
+    assert np.array_equal(st.U, d["final_U"])
+    assert np.array_equal(st.sflx, d["final_sflx"])
+    assert np.abs(st.sflx).max() > 0
+    hp0 = dict(hp, spitzer=0.0)
+    st0 = O.State(H.oracle_params(hp0), d["input_U"], eos)
+    st0.step(eos, int(d["steps"]))
+    assert np.max(np.abs(st0.U[4] - st.U[4])) > 1e-8 * np.max(np.abs(st.U[4]))
+
+
 def test_eos_interpolation_exact_at_nodes(eos):
     """Known answer: at a table node the bilinear lookup returns exp of the node value."""
     t = initial.EosTable(H.EOS_SMALL)
@@ -161,6 +179,28 @@ def test_live_reference_random_boxes(seed, eos):
     st = O.State(H.oracle_params(hp), U)
     st.step(eos, 4)
     assert np.array_equal(st.U, ref["final_U"])
+
+
+@pytest.mark.skipif(not refrun.available(), reason="reference harness not built here")
+@pytest.mark.parametrize("case", ["periodic", "closed", "open_cold_top"])
+def test_live_reference_spitzer(case, eos):
+    """The conduction on a periodic box, with the mirror rule, and with the
+    physical boundaries and no hot top (its top layers' heat flux zeroed)."""
+    tab = initial.EosTable(H.EOS_SMALL)
+    if case == "periodic":
+        U = initial.periodic_box(tab, 12, 8, 10, seed=3)
+        hp = dict(nx=12, ny=8, nz=10, dx=3.2e6, dy=2.4e6, dz=2.0e6)
+    else:
+        U = initial.stratified_box(tab, 12, 8, 6, dx=1.6e6, seed=17)
+        hp = dict(nx=12, ny=8, nz=6, dx=1.6e6, periodic_x=0, grav=2.74e4)
+        if case == "open_cold_top":
+            hp.update(xbnd=1, bnd_top=0)
+    hp.update(eos=H.EOS_SMALL, spitzer=0.5)
+    ref = refrun.run(U, hp, steps=5)
+    st = O.State(H.oracle_params(hp), U, eos)
+    st.step(eos, 5)
+    assert np.array_equal(st.U, ref["final_U"])
+    assert np.array_equal(st.sflx, ref["final_sflx"])
 
 
 @pytest.mark.skipif(not refrun.available(), reason="reference harness not built here")
