@@ -87,6 +87,12 @@ typedef struct gpumhd_params {
    * boundary call (set_p_s_bc), gpumhd_boundary_info reads them back. */
   int xbnd, bnd_top;
   double bnd_bcrit, bnd_eps_top, p_bc, s_bc;
+  /* PhysicsData::params[i_param_spitzer]: hyperbolic Spitzer heat conduction
+   * (0: off).  A ninth field, the heat flux along B (which = 10 in
+   * upload/download, zero at creation), evolves with the RK stages
+   * (src/mhdres_SR.C:33-46, 121-145, 355-358, 492-521, 668-692;
+   * src/Add_Sources_Integrate_SR.C:410-419). */
+  double spitzer;
 } gpumhd_params;
 
 typedef struct gpumhd_ctx gpumhd_ctx;
@@ -111,7 +117,8 @@ int gpumhd_eos_init(gpumhd_ctx* ctx, const char* path);
 /* ACCH::UpdateGPU / ACCH::UpdateCPU of the GridData arrays (src/ACCH.C:114-158):
  * which = 0: U, 1: U0, 2: Res (cState arrays, 8 doubles per node);
  * which = 3..7: pres, temp, ne, rhoi, amb; 8: phi, 9: divB (the divB cleaning's
- * potential and last divergence, GridData::phi / divB; one double per node). */
+ * potential and last divergence, GridData::phi / divB); 10: sflx (the Spitzer
+ * heat flux, GridData::sflx); one double per node. */
 int gpumhd_upload(gpumhd_ctx* ctx, int which, const double* host);
 int gpumhd_download(gpumhd_ctx* ctx, int which, double* host);
 

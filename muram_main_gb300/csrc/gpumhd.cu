@@ -61,6 +61,10 @@ struct gpumhd_ctx {
   void* phi = nullptr;   // divB cleaning potential (GridData::phi, N), persists between calls
   void* divb = nullptr;  // last divergence of B (GridData::divB, N)
   double* bnd_part = nullptr;  // per-plane sums of the physical x boundaries (nz * BND_NQ)
+  // Spitzer conduction (N each): spt[0] the heat flux (step start = sflx0 of
+  // the fused step), spt[1], spt[2] the stages' outputs (per routine: sflx0 and
+  // Rflx), spt[3] the temperature, spt[4] the energy residual's share
+  void* spt[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   float *d_d3 = nullptr, *d_eps3 = nullptr;  // inverse EOS tables
   float eos_hdr[14] = {0};                    // the EOS file's header (axes of the boundary lookups)
   char err[1024] = {0};
@@ -111,6 +115,7 @@ extern "C" int gpumhd_default_params(gpumhd_params* p, int nx, int ny, int nz, d
   p->divB_switch = 0; p->divB_itmax = 5; p->divB_err = 0.2;  // off; the reference's test settings when on
   p->xbnd = 0; p->bnd_top = 0; p->bnd_bcrit = 1.0e10; p->bnd_eps_top = 0.0;  // include/physics.H defaults
   p->p_bc = -1.0; p->s_bc = -1.0;
+  p->spitzer = 0.0;
   return GPUMHD_OK;
 }
 
@@ -191,6 +196,10 @@ static int fill_consts(gpumhd_ctx* ctx) {
   g.xmirror = (!p.periodic_x && p.xbnd == 0) ? 1 : 0;
   c.xbnd = (!p.periodic_x && p.xbnd == 1) ? 1 : 0;
   c.bnd_top = p.bnd_top;
+  c.spitzer = p.spitzer;
+  c.has_spitzer = p.spitzer > 0.0 ? 1 : 0;
+  c.spt_sat_flx = (1.0 + 0.7) * pow(8.314e7, 1.5) * sqrt(1836.) / 8.0;  // src/mhdres_SR.C:42-46
+  c.spt_rsp = ctx->spt[4];
   for (int d = 0; d < 3; d++) {
     c.dx[d] = p.dx[d];
     c.w1[d] = 8. / (12. * p.dx[d]);
@@ -393,6 +402,7 @@ extern "C" int gpumhd_create(const gpumhd_params* p, int device, gpumhd_ctx** ou
   if (!(p->eta >= 0.0)) return fail(nullptr, GPUMHD_E_INVALID, "eta must be >= 0");
   if (p->divB_switch > 0 && !(p->divB_err >= 0.0)) return fail(nullptr, GPUMHD_E_INVALID, "divB_err must be >= 0");
   if (p->xbnd != 0 && p->xbnd != 1) return fail(nullptr, GPUMHD_E_INVALID, "xbnd must be 0 or 1");
+  if (!(p->spitzer >= 0.0)) return fail(nullptr, GPUMHD_E_INVALID, "spitzer must be >= 0");
   if ((long long)(p->nx + 4) * (p->ny + 4) * (p->nz + 4) > GPUMHD_MAX_CELLS)
     return fail(nullptr, GPUMHD_E_INVALID, "grid too large: (nx+4)(ny+4)(nz+4) must not exceed %lld cells",
                 (long long)GPUMHD_MAX_CELLS);
@@ -467,6 +477,7 @@ extern "C" int gpumhd_destroy(gpumhd_ctx* ctx) {
   cudaFree(ctx->phi);
   cudaFree(ctx->divb);
   cudaFree(ctx->bnd_part);
+  for (void* q : ctx->spt) cudaFree(q);
   cudaFree(ctx->d_d3); cudaFree(ctx->d_eps3);
   cudaFree(ctx->dyn);
   cudaFree(ctx->dt_hist);
@@ -524,6 +535,7 @@ extern "C" int gpumhd_set_params(gpumhd_ctx* ctx, const gpumhd_params* p) {
   c.c_pres = keep.c_pres; c.c_temp = keep.c_temp; c.kb = keep.kb; c.mun_mh = keep.mun_mh;
   c.N_lp3 = keep.N_lp3; c.N_s3 = keep.N_s3;
   c.d3 = keep.d3; c.eps3 = keep.eps3;
+  c.spt_rsp = ctx->spt[4];
   fill_kcs(ctx);
   fill_bndk(ctx);
   ctx->hdyn.dt = p->dt;
@@ -660,6 +672,14 @@ static void* field_ptr(gpumhd_ctx* ctx, int which, int* nf, int* rc) {
   }
   *nf = 1;
   if (which == 3) return ctx->P[ctx->iP];
+  if (which == 10) {
+    void*& a = ctx->spt[0];
+    if (!a) {
+      if (cudaMalloc(&a, ctx->c.g.N * ctx->rsz) != cudaSuccess) { *rc = GPUMHD_E_NOMEM; return nullptr; }
+      cudaMemsetAsync(a, 0, ctx->c.g.N * ctx->rsz, ctx->stream);
+    }
+    return a;
+  }
   if (which == 8 || which == 9) {
     void*& a = which == 8 ? ctx->phi : ctx->divb;
     if (!a) {
@@ -690,6 +710,19 @@ static int ensure_divb(gpumhd_ctx* ctx) {
   return GPUMHD_OK;
 }
 
+// Spitzer conduction's buffers (zero-initialised).
+static int ensure_spitzer(gpumhd_ctx* ctx) {
+  if (!ctx->c.has_spitzer) return GPUMHD_OK;
+  if (!ctx->eos_loaded) return fail(ctx, GPUMHD_E_ORDER, "Spitzer conduction before eos_init");
+  for (int b = 0; b < 5; b++)
+    if (!ctx->spt[b]) {
+      CK(cudaMalloc(&ctx->spt[b], ctx->c.g.N * ctx->rsz));
+      CK(cudaMemsetAsync(ctx->spt[b], 0, ctx->c.g.N * ctx->rsz, ctx->stream));
+    }
+  ctx->c.spt_rsp = ctx->spt[4];
+  return GPUMHD_OK;
+}
+
 // The physical x boundaries need the EOS's inverse tables and a plane-sum buffer.
 static int ensure_bnd(gpumhd_ctx* ctx) {
   if (!ctx->c.xbnd) return GPUMHD_OK;
@@ -704,9 +737,11 @@ static int ensure_bnd(gpumhd_ctx* ctx) {
 
 // MURaM's physical x boundaries on state buffer U (P, cmax: see Launch::bc).
 static int enqueue_bc(gpumhd_ctx* ctx, void* U, void* P, int with_cmax) {
+  void* sf = ctx->c.has_spitzer ? ctx->spt[0] : nullptr;  // the heat flux's boundary values too
   if (ctx->f32)
-    return Launch<float>::bc(ctx->c, (float*)U, (float*)P, ctx->dyn, ctx->bnd_part, with_cmax, ctx->stream);
-  return Launch<double>::bc(ctx->c, (double*)U, (double*)P, ctx->dyn, ctx->bnd_part, with_cmax, ctx->stream);
+    return Launch<float>::bc(ctx->c, (float*)U, (float*)P, ctx->dyn, ctx->bnd_part, with_cmax, ctx->stream, (float*)sf);
+  return Launch<double>::bc(ctx->c, (double*)U, (double*)P, ctx->dyn, ctx->bnd_part, with_cmax, ctx->stream,
+                            (double*)sf);
 }
 
 static int ensure_staging(gpumhd_ctx* ctx) {
@@ -781,6 +816,11 @@ extern "C" int gpumhd_save_cons(gpumhd_ctx* ctx) {
   CK(cudaSetDevice(ctx->device));
   if (ctx->f32) Launch<float>::save_cons(ctx->c, (const float*)ctx->S[ctx->iU], (float*)ctx->S[ctx->iU0], ctx->stream);
   else Launch<double>::save_cons(ctx->c, (const double*)ctx->S[ctx->iU], (double*)ctx->S[ctx->iU0], ctx->stream);
+  if (ctx->c.has_spitzer) {  // sflx0 = sflx (src/Add_Sources_Integrate_SR.C:503-516)
+    int rc = ensure_spitzer(ctx);
+    if (rc) return rc;
+    CK(cudaMemcpyAsync(ctx->spt[1], ctx->spt[0], ctx->c.g.N * ctx->rsz, cudaMemcpyDeviceToDevice, ctx->stream));
+  }
   return check_launch(ctx, 1);
 }
 
@@ -852,6 +892,24 @@ extern "C" int gpumhd_mhd_residual(gpumhd_ctx* ctx, double* dt_mhd) {
   CK(cudaSetDevice(ctx->device));
   int rc = reset_accumulators(ctx);
   if (rc) return rc;
+  int nl = 2;
+  if (ctx->c.has_spitzer) {
+    // heat flux residual into Rflx (spt[2]) and the energy share, from the
+    // primitive state and ConsToPrim's temperature
+    rc = ensure_spitzer(ctx);
+    if (rc) return rc;
+    int nf;
+    void* Tm = field_ptr(ctx, 4, &nf, &rc);
+    if (rc) return fail(ctx, rc, "temperature field allocation failed");
+    if (ctx->f32)
+      Launch<float>::spitzer(ctx->c, (const float*)ctx->S[ctx->iU], true, (const float*)Tm, (const float*)ctx->spt[0],
+                             nullptr, nullptr, (float*)ctx->spt[2], (float*)ctx->spt[4], ctx->dyn, 0, ctx->stream);
+    else
+      Launch<double>::spitzer(ctx->c, (const double*)ctx->S[ctx->iU], true, (const double*)Tm,
+                              (const double*)ctx->spt[0], nullptr, nullptr, (double*)ctx->spt[2],
+                              (double*)ctx->spt[4], ctx->dyn, 0, ctx->stream);
+    nl += 1;
+  }
   if (ctx->f32) {
     Launch<float>::stage(ctx->c, (const float*)ctx->S[ctx->iU], (const float*)ctx->P[ctx->iP], nullptr, nullptr, nullptr,
                          (float*)ctx->S[ctx->iRes], ctx->dyn, 0, true, 0, ctx->stream, map_u(ctx, ctx->iU),
@@ -863,7 +921,7 @@ extern "C" int gpumhd_mhd_residual(gpumhd_ctx* ctx, double* dt_mhd) {
                           map_u(ctx, ctx->iU), map_p(ctx, ctx->iP));
     Launch<double>::cmax_faces(ctx->c, (const double*)ctx->S[ctx->iU], (const double*)ctx->P[ctx->iP], ctx->dyn, ctx->stream);
   }
-  rc = check_launch(ctx, 2);
+  rc = check_launch(ctx, nl);
   if (rc) return rc;
   rc = pull_dyn(ctx);
   if (rc) return rc;
@@ -911,7 +969,19 @@ extern "C" int gpumhd_source_integrate_tcheck(gpumhd_ctx* ctx, int stage) {
   else
     Launch<double>::source_integrate(ctx->c, (double*)ctx->S[ctx->iU], (const double*)ctx->S[ctx->iU0],
                                      (double*)ctx->S[ctx->iRes], ctx->dyn, stage, ctx->stream);
-  return check_launch(ctx, 1);
+  int nl = 1;
+  if (ctx->c.has_spitzer) {  // sflx = sflx0 + wdt*Rflx, Rflx = 0 (src/Add_Sources_Integrate_SR.C:410-419)
+    int rc = ensure_spitzer(ctx);
+    if (rc) return rc;
+    if (ctx->f32)
+      Launch<float>::sflx_update(ctx->c, (float*)ctx->spt[0], (const float*)ctx->spt[1], (float*)ctx->spt[2], ctx->dyn,
+                                 stage, ctx->stream);
+    else
+      Launch<double>::sflx_update(ctx->c, (double*)ctx->spt[0], (const double*)ctx->spt[1], (double*)ctx->spt[2],
+                                  ctx->dyn, stage, ctx->stream);
+    nl += 1;
+  }
+  return check_launch(ctx, nl);
 }
 
 extern "C" int gpumhd_exchange(gpumhd_ctx* ctx, int with_bc) {
@@ -927,6 +997,13 @@ extern "C" int gpumhd_exchange(gpumhd_ctx* ctx, int with_bc) {
   if (ctx->f32) Launch<float>::fill_ghosts(ctx->c, (float*)ctx->S[ctx->iU], 8, mirror, ctx->stream);
   else Launch<double>::fill_ghosts(ctx->c, (double*)ctx->S[ctx->iU], 8, mirror, ctx->stream);
   int n = 1;
+  if (ctx->c.has_spitzer) {  // the heat flux's periodic images (src/exchange.C:590-760)
+    int rc = ensure_spitzer(ctx);
+    if (rc) return rc;
+    if (ctx->f32) Launch<float>::fill_ghosts(ctx->c, (float*)ctx->spt[0], 1, 0, ctx->stream);
+    else Launch<double>::fill_ghosts(ctx->c, (double*)ctx->spt[0], 1, 0, ctx->stream);
+    n += 1;
+  }
   if (phys) n += enqueue_bc(ctx, ctx->S[ctx->iU], nullptr, 0);
   int rc = check_launch(ctx, n);
   if (rc || !phys || !ctx->hdyn.bnd_ini) return rc;
@@ -1026,6 +1103,7 @@ static int step_launches(const gpumhd_ctx* ctx) {
   int n = 12;
   if (ctx->c.divb_on) n += 3 + 2 * (ctx->c.divb_itmax > 3 ? ctx->c.divb_itmax : 3);
   if (ctx->c.xbnd) n += 5 * 3;  // the boundaries after each stage and at the end of the step
+  if (ctx->c.has_spitzer) n += 4 * 2;  // temperature and heat flux before each stage
   return n;
 }
 
@@ -1043,29 +1121,46 @@ static int enqueue_one_step(gpumhd_ctx* ctx, cudaEvent_t* ev = nullptr) {
   const int a = ctx->iU, b = ctx->iU0, d = ctx->iRes;  // a: state, b and d: work buffers
   const int pa = ctx->iP, pb = 1 - ctx->iP;
   const bool xb = c.xbnd != 0;
+  const bool sp = c.has_spitzer != 0;
   mark();
   k_step_begin<<<1, 32, 0, s>>>(c, ctx->dyn, ctx->dt_hist, ctx->dt_hist_cap);
   if (ctx->f32) {
     using L = Launch<float>;
+    // Spitzer conduction before each stage: temperature, then the heat flux's
+    // residual (the energy share for the stage kernel) and its update
+    float* const* SF = (float* const*)ctx->spt;
+    static const int sf_in[5] = {0, 0, 1, 2, 1}, sf_out[5] = {0, 1, 2, 1, 0};
+    auto spz = [&](const float* Uin, int st) {
+      if (!sp) return;
+      L::temp(c, Uin, SF[3], s);
+      L::spitzer(c, Uin, false, SF[3], SF[sf_in[st]], SF[0], SF[sf_out[st]], nullptr, SF[4], ctx->dyn, st, s);
+    };
+    float* const sf1 = sp ? SF[1] : nullptr;
+    float* const sf2 = sp ? SF[2] : nullptr;
+    float* const sf0 = sp ? SF[0] : nullptr;
     float* const comp = (ctx->p.compensated && ctx->comp) ? (float*)ctx->comp : nullptr;
     float* const* S = (float* const*)ctx->S;
     float* const* P = (float* const*)ctx->P;
     mark();
+    spz(S[a], 1);
     L::stage(c, S[a], P[pa], S[a], S[b], P[pb], nullptr, ctx->dyn, 1, false, 1, s,
               map_u(ctx, a), map_p(ctx, pa), ctx->tune_zc, comp);
-    if (xb) L::bc(c, S[b], P[pb], ctx->dyn, ctx->bnd_part, 0, s);
+    if (xb) L::bc(c, S[b], P[pb], ctx->dyn, ctx->bnd_part, 0, s, sf1);
     mark();
+    spz(S[b], 2);
     L::stage(c, S[b], P[pb], S[a], S[d], P[pa], nullptr, ctx->dyn, 2, false, 1, s,
               map_u(ctx, b), map_p(ctx, pb), ctx->tune_zc, comp);
-    if (xb) L::bc(c, S[d], P[pa], ctx->dyn, ctx->bnd_part, 0, s);
+    if (xb) L::bc(c, S[d], P[pa], ctx->dyn, ctx->bnd_part, 0, s, sf2);
     mark();
+    spz(S[d], 3);
     L::stage(c, S[d], P[pa], S[a], S[b], P[pb], nullptr, ctx->dyn, 3, false, 1, s,
               map_u(ctx, d), map_p(ctx, pa), ctx->tune_zc, comp);
-    if (xb) L::bc(c, S[b], P[pb], ctx->dyn, ctx->bnd_part, 0, s);
+    if (xb) L::bc(c, S[b], P[pb], ctx->dyn, ctx->bnd_part, 0, s, sf1);
     mark();
+    spz(S[b], 4);
     L::stage(c, S[b], P[pb], S[a], S[a], nullptr, nullptr, ctx->dyn, 4, false, 0, s,
               map_u(ctx, b), map_p(ctx, pb), ctx->tune_zc, comp);
-    if (xb) L::bc(c, S[a], (float*)nullptr, ctx->dyn, ctx->bnd_part, 0, s);  // TVD keeps the stale pressure
+    if (xb) L::bc(c, S[a], (float*)nullptr, ctx->dyn, ctx->bnd_part, 0, s, sf0);  // TVD keeps the stale pressure
     mark();
     L::tvd(c, 0, 0, 0, S[a], P[pb], S[d], ctx->dyn, s, ctx->tune_td);
     mark();
@@ -1085,28 +1180,44 @@ static int enqueue_one_step(gpumhd_ctx* ctx, cudaEvent_t* ev = nullptr) {
       L::step_finish(c, S[a], P[pa], ctx->dyn, s);
     }
     if (xb) {
-      L::bc(c, S[a], P[pa], ctx->dyn, ctx->bnd_part, 1, s);  // the next step's ghosts, pressure and CFL speed
+      L::bc(c, S[a], P[pa], ctx->dyn, ctx->bnd_part, 1, s, sf0);  // the next step's ghosts, pressure and CFL speed
     }
   } else {
     using L = Launch<double>;
+    // Spitzer conduction before each stage: temperature, then the heat flux's
+    // residual (the energy share for the stage kernel) and its update
+    double* const* SF = (double* const*)ctx->spt;
+    static const int sf_in[5] = {0, 0, 1, 2, 1}, sf_out[5] = {0, 1, 2, 1, 0};
+    auto spz = [&](const double* Uin, int st) {
+      if (!sp) return;
+      L::temp(c, Uin, SF[3], s);
+      L::spitzer(c, Uin, false, SF[3], SF[sf_in[st]], SF[0], SF[sf_out[st]], nullptr, SF[4], ctx->dyn, st, s);
+    };
+    double* const sf1 = sp ? SF[1] : nullptr;
+    double* const sf2 = sp ? SF[2] : nullptr;
+    double* const sf0 = sp ? SF[0] : nullptr;
     double* const* S = (double* const*)ctx->S;
     double* const* P = (double* const*)ctx->P;
     mark();
+    spz(S[a], 1);
     L::stage(c, S[a], P[pa], S[a], S[b], P[pb], nullptr, ctx->dyn, 1, false, 1, s,
               map_u(ctx, a), map_p(ctx, pa), ctx->tune_zc);
-    if (xb) L::bc(c, S[b], P[pb], ctx->dyn, ctx->bnd_part, 0, s);
+    if (xb) L::bc(c, S[b], P[pb], ctx->dyn, ctx->bnd_part, 0, s, sf1);
     mark();
+    spz(S[b], 2);
     L::stage(c, S[b], P[pb], S[a], S[d], P[pa], nullptr, ctx->dyn, 2, false, 1, s,
               map_u(ctx, b), map_p(ctx, pb), ctx->tune_zc);
-    if (xb) L::bc(c, S[d], P[pa], ctx->dyn, ctx->bnd_part, 0, s);
+    if (xb) L::bc(c, S[d], P[pa], ctx->dyn, ctx->bnd_part, 0, s, sf2);
     mark();
+    spz(S[d], 3);
     L::stage(c, S[d], P[pa], S[a], S[b], P[pb], nullptr, ctx->dyn, 3, false, 1, s,
               map_u(ctx, d), map_p(ctx, pa), ctx->tune_zc);
-    if (xb) L::bc(c, S[b], P[pb], ctx->dyn, ctx->bnd_part, 0, s);
+    if (xb) L::bc(c, S[b], P[pb], ctx->dyn, ctx->bnd_part, 0, s, sf1);
     mark();
+    spz(S[b], 4);
     L::stage(c, S[b], P[pb], S[a], S[a], nullptr, nullptr, ctx->dyn, 4, false, 0, s,
               map_u(ctx, b), map_p(ctx, pb), ctx->tune_zc);
-    if (xb) L::bc(c, S[a], (double*)nullptr, ctx->dyn, ctx->bnd_part, 0, s);  // TVD keeps the stale pressure
+    if (xb) L::bc(c, S[a], (double*)nullptr, ctx->dyn, ctx->bnd_part, 0, s, sf0);  // TVD keeps the stale pressure
     mark();
     L::tvd(c, 0, 0, 0, S[a], P[pb], S[d], ctx->dyn, s, ctx->tune_td);
     mark();
@@ -1126,7 +1237,7 @@ static int enqueue_one_step(gpumhd_ctx* ctx, cudaEvent_t* ev = nullptr) {
       L::step_finish(c, S[a], P[pa], ctx->dyn, s);
     }
     if (xb) {
-      L::bc(c, S[a], P[pa], ctx->dyn, ctx->bnd_part, 1, s);  // the next step's ghosts, pressure and CFL speed
+      L::bc(c, S[a], P[pa], ctx->dyn, ctx->bnd_part, 1, s, sf0);  // the next step's ghosts, pressure and CFL speed
     }
   }
   mark();
@@ -1152,6 +1263,8 @@ static int fused_prepare(gpumhd_ctx* ctx, int nsteps) {
   {
     int rc1 = ensure_bnd(ctx);
     if (rc1) return rc1;
+    rc1 = ensure_spitzer(ctx);
+    if (rc1) return rc1;
   }
   if (ctx->f32 && ctx->p.compensated && !ctx->comp) {
     CK(cudaMalloc(&ctx->comp, sizeof(float) * 8 * ctx->c.g.N));
@@ -1175,6 +1288,11 @@ static int fused_prepare(gpumhd_ctx* ctx, int nsteps) {
     // physical x boundaries: their ghosts, with the CFL speed of the x ghosts
     // (no longer images of interior cells), before the pressures and statistics
     int n = 2;
+    if (ctx->c.has_spitzer) {  // the heat flux's periodic images
+      if (ctx->f32) Launch<float>::fill_ghosts(ctx->c, (float*)ctx->spt[0], 1, 0, ctx->stream);
+      else Launch<double>::fill_ghosts(ctx->c, (double*)ctx->spt[0], 1, 0, ctx->stream);
+      n += 1;
+    }
     if (ctx->f32) {
       Launch<float>::fill_ghosts(ctx->c, (float*)ctx->S[ctx->iU], 8, 1, ctx->stream);
       if (ctx->c.xbnd) n += enqueue_bc(ctx, ctx->S[ctx->iU], ctx->P[ctx->iP], 1);
@@ -1612,6 +1730,7 @@ extern "C" int gpumhd_adjoint(gpumhd_ctx* ctx, int nsteps, int checkpoint_every,
   if (!(ctx->p.dt > 0.0)) return fail(ctx, GPUMHD_E_INVALID, "adjoint: dt must be positive");
   if (ctx->c.has_eta) return fail(ctx, GPUMHD_E_INVALID, "adjoint: ideal MHD only (eta = 0)");
   if (ctx->c.divb_on) return fail(ctx, GPUMHD_E_INVALID, "adjoint: without divB cleaning (divB_switch = 0)");
+  if (ctx->c.has_spitzer) return fail(ctx, GPUMHD_E_INVALID, "adjoint: without Spitzer conduction (spitzer = 0)");
   CK(cudaSetDevice(ctx->device));
   int rc = fused_prepare(ctx, nsteps);
   if (rc) return rc;

@@ -139,7 +139,8 @@ __global__ void k_bc_setup(Consts c, Dyn* dyn, const double* __restrict__ part, 
 // cells MHD_Residual's x pencils reach -- join the step's maximum.
 template <class R>
 __global__ void __launch_bounds__(BND_THREADS) k_bc_ghosts(Consts c, R* __restrict__ U, R* __restrict__ P,
-                                                          Dyn* __restrict__ dyn, int with_cmax) {
+                                                          Dyn* __restrict__ dyn, int with_cmax,
+                                                          R* __restrict__ sflx) {
   if (dyn->err) return;
   const Geom& g = c.g;
   const long long ncol = (long long)g.sy * g.sz;
@@ -216,6 +217,10 @@ __global__ void __launch_bounds__(BND_THREADS) k_bc_ghosts(Consts c, R* __restri
       u2[4] = eps2 * rho2 + 0.5 * (u2[1] * u2[1] + u2[2] * u2[2] + u2[3] * u2[3]) / u2[0];
       out(lb - 1, u1);
       out(lb - 2, u2);
+      if (sflx) {  // heat flux: zero in the bottom ghosts (src/boundary_pdmp_1_fftw3.C:302-306)
+        sflx[cidx(g, lb - 1, j, k)] = (R)0;
+        sflx[cidx(g, lb - 2, j, k)] = (R)0;
+      }
     } else {
       // top (src/boundary_pdmp_1_fftw3.C:398-450)
       if (c.bnd_top == 1) {
@@ -237,6 +242,17 @@ __global__ void __launch_bounds__(BND_THREADS) k_bc_ghosts(Consts c, R* __restri
       u2[7] *= -1;
       out(le + 1, u1);
       out(le + 2, u2);
+      if (sflx) {  // heat flux: symmetric under a hot top, else zero in the top layers (:426-438)
+        if (b.eps_top > 0.0) {
+          sflx[cidx(g, le + 1, j, k)] = sflx[cidx(g, le, j, k)];
+          sflx[cidx(g, le + 2, j, k)] = sflx[cidx(g, le - 1, j, k)];
+        } else {
+          sflx[cidx(g, le - 1, j, k)] = (R)0;
+          sflx[cidx(g, le, j, k)] = (R)0;
+          sflx[cidx(g, le + 1, j, k)] = (R)0;
+          sflx[cidx(g, le + 2, j, k)] = (R)0;
+        }
+      }
     }
   }
   if (with_cmax) {

@@ -95,6 +95,11 @@ struct Consts {
   const float* d3;     // ln rho (p, s), [i_lp*N_s3 + j_s], pre-divided
   const float* eps3;   // ln eps (p, s)
   BndK<double> bndd;
+  // hyperbolic Spitzer conduction: coefficient (0: off), saturation flux
+  // factor (1+X_H) Rgas^1.5 sqrt(1836)/8 (src/mhdres_SR.C:40-46)
+  double spitzer, spt_sat_flx;
+  int has_spitzer, pad_spt;
+  const void* spt_rsp;  // the energy residual's Spitzer share for this stage (N, state precision)
   double rt_cfl;
   double CFL, CFL_tvd, dt_rad, rt_tstep, outcad;
   double va_max, va_adjust, max_fill;
@@ -155,6 +160,7 @@ struct Dyn {
   // by the first call), the first call still pending, the latest mean pressures
   double p_bc, s_bc, pmean1, pmean2;
   int bnd_ini, bnd_pad;
+  double dt_prev;       // the previous step's dt (Spitzer relaxation caps at stage 1)
 };
 
 template <class R> __device__ __forceinline__ const DynR<R>& dynr(const Dyn* d);

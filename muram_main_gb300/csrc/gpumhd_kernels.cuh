@@ -579,6 +579,8 @@ __global__ void __launch_bounds__(TX* TY, 2) k_stage(Consts c, const R* __restri
       };
       if (c.has_eta) directions(std::true_type());
       else directions(std::false_type());
+      // Spitzer conduction's share of the energy residual (-sum_d D_d(sflx B_d))
+      if (c.has_spitzer) Racc[4] += ((const R*)c.spt_rsp)[id];
       if (RESID) {
 #pragma unroll
         for (int q = 0; q < NV; q++) Res[id + (unsigned)q * g.N32] = Racc[q];

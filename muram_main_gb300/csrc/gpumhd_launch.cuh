@@ -4,6 +4,7 @@
 #include "gpumhd_stage_tm.cuh"
 #include "gpumhd_divb.cuh"
 #include "gpumhd_bnd.cuh"
+#include "gpumhd_spitzer.cuh"
 
 namespace gpumhd {
 
@@ -40,7 +41,15 @@ struct Launch {
   // MURaM's physical x boundaries on U (P: ghost pressures, may be null;
   // with_cmax: ghost CFL speeds join the step maximum); part: nz*BND_NQ doubles.
   // Returns the number of launches.
-  static int bc(const Consts& c, R* U, R* P, Dyn* dyn, double* part, int with_cmax, cudaStream_t s);
+  static int bc(const Consts& c, R* U, R* P, Dyn* dyn, double* part, int with_cmax, cudaStream_t s,
+                R* sflx = nullptr);
+  // Spitzer conduction: the temperature of a conserved state; the per-stage
+  // residual of the heat flux (prim: U after ConsToPrim; Sout: the fused
+  // step's update of sflx, else Rflx receives the residual)
+  static void temp(const Consts& c, const R* U, R* T, cudaStream_t s);
+  static void spitzer(const Consts& c, const R* U, bool prim, const R* T, const R* S, const R* S0, R* Sout, R* Rflx,
+                      R* Rsp, const Dyn* dyn, int stage, cudaStream_t s);
+  static void sflx_update(const Consts& c, R* S, const R* S0, R* Rflx, const Dyn* dyn, int stage, cudaStream_t s);
   static void cons_to_prim(const Consts& c, R* U, R* P, R* T, R* Ne, R* Ri, R* Am, cudaStream_t s);
   static void init_pass(const Consts& c, const R* U, R* P, Dyn* dyn, cudaStream_t s);
   static void adjust_stats(const Consts& c, const R* U, const R* P, Dyn* dyn, cudaStream_t s);
@@ -217,14 +226,34 @@ int Launch<R>::divb_clean(const Consts& c, R* U, R* phi, R* divb, Dyn* dyn, cuda
   return 3 + 2 * maxit;
 }
 template <class R>
-int Launch<R>::bc(const Consts& c, R* U, R* P, Dyn* dyn, double* part, int with_cmax, cudaStream_t s) {
+int Launch<R>::bc(const Consts& c, R* U, R* P, Dyn* dyn, double* part, int with_cmax, cudaStream_t s, R* sflx) {
   const Geom& g = c.g;
   const dim3 gs((g.ny + BND_BX - 1) / BND_BX, (g.nz + BND_BY - 1) / BND_BY);
   k_bc_sums<R><<<gs, dim3(BND_BX, BND_BY), 0, s>>>(c, U, dyn, part);
   k_bc_setup<<<1, BND_SETUP_THREADS, 0, s>>>(c, dyn, part, (int)(gs.x * gs.y));
   const long long cols = (long long)g.sy * g.sz;
-  k_bc_ghosts<R><<<(unsigned)((2 * cols + BND_THREADS - 1) / BND_THREADS), BND_THREADS, 0, s>>>(c, U, P, dyn, with_cmax);
+  k_bc_ghosts<R><<<(unsigned)((2 * cols + BND_THREADS - 1) / BND_THREADS), BND_THREADS, 0, s>>>(c, U, P, dyn, with_cmax,
+                                                                                              sflx);
   return 3;
+}
+template <class R>
+void Launch<R>::temp(const Consts& c, const R* U, R* T, cudaStream_t s) {
+  k_temp<R><<<grid_for(c.g.N, 256), 256, 0, s>>>(c, U, T);
+}
+template <class R>
+void Launch<R>::spitzer(const Consts& c, const R* U, bool prim, const R* T, const R* S, const R* S0, R* Sout, R* Rflx,
+                        R* Rsp, const Dyn* dyn, int stage, cudaStream_t s) {
+  const Geom& g = c.g;
+  const int bx = (g.nx + SPT_BX - 1) / SPT_BX, by = (g.ny + SPT_BY - 1) / SPT_BY;
+  int gz = (152 * 8 + bx * by - 1) / (bx * by);
+  gz = gz < 1 ? 1 : (gz > g.nz ? g.nz : gz);
+  const dim3 grid(bx, by, gz), block(SPT_BX, SPT_BY);
+  if (prim) k_spitzer<R, true><<<grid, block, 0, s>>>(c, U, T, S, S0, Sout, Rflx, Rsp, dyn, stage);
+  else k_spitzer<R, false><<<grid, block, 0, s>>>(c, U, T, S, S0, Sout, Rflx, Rsp, dyn, stage);
+}
+template <class R>
+void Launch<R>::sflx_update(const Consts& c, R* S, const R* S0, R* Rflx, const Dyn* dyn, int stage, cudaStream_t s) {
+  k_sflx_update<R><<<grid_for((long long)c.g.nx * c.g.ny * c.g.nz, 256), 256, 0, s>>>(c, S, S0, Rflx, dyn, stage);
 }
 template <class R>
 void Launch<R>::step_finish(const Consts& c, R* U, R* P, Dyn* dyn, cudaStream_t s) {

@@ -14,6 +14,7 @@ __global__ void k_step_begin(Consts c, Dyn* dyn, double* dt_hist, int dt_hist_ca
   // fused path runs only in that mode, so the limits are the run constants.
   dyn->v_lim = c.tchk_vmax;
   dyn->e_lim = c.tchk_eps_max;
+  dyn->dt_prev = dyn->dt;  // Run.dt as MHD_Residual sees it at stage 1
   const double cmax = __longlong_as_double((long long)dyn->cmax_bits);
   double dt_mhd = c.dxmin / cmax;
   if (c.has_eta) dt_mhd = smin(dt_mhd, c.dt_res);  // resistive limit (src/mhdres_SR.C:815-819)

@@ -28,7 +28,8 @@ E_CFL = -5
 E_ORDER = -6
 E_NOMEM = -7
 
-FIELD_U, FIELD_U0, FIELD_RES, FIELD_PRES, FIELD_TEMP, FIELD_NE, FIELD_RHOI, FIELD_AMB, FIELD_PHI, FIELD_DIVB = range(10)
+(FIELD_U, FIELD_U0, FIELD_RES, FIELD_PRES, FIELD_TEMP, FIELD_NE, FIELD_RHOI, FIELD_AMB, FIELD_PHI, FIELD_DIVB,
+ FIELD_SFLX) = range(11)
 
 
 class GpumhdError(RuntimeError):
@@ -54,6 +55,7 @@ class Params(C.Structure):
         ("divB_switch", C.c_int), ("divB_itmax", C.c_int), ("divB_err", C.c_double),
         ("xbnd", C.c_int), ("bnd_top", C.c_int),
         ("bnd_bcrit", C.c_double), ("bnd_eps_top", C.c_double), ("p_bc", C.c_double), ("s_bc", C.c_double),
+        ("spitzer", C.c_double),
     ]
 
 
