@@ -228,6 +228,9 @@ def run_ours(args):
     # bnd_pot 0, bnd_bcrit 2.5e30)
     if args.xbnd:
         divb_kw.update(xbnd=1, bnd_top=0, bnd_bcrit=2.5e30)
+    # --spitzer K: hyperbolic Spitzer conduction with coefficient K (the reference's test run: 1e-6)
+    if args.spitzer > 0:
+        divb_kw.update(spitzer=args.spitzer)
 
     def context(prec):
         p = gpumhd.default_params(wl["nx"], wl["ny"], wl["nz"], wl["dx"], precision=prec,
@@ -333,7 +336,8 @@ def run_ours(args):
         "dtype": "f32", "data": "synthetic (seeded stratified box, generated EOS table 3000x3000)",
         "config": {"workload": "stratified 128(vertical) x 384 x 384 at 16 km, closed top/bottom, gravity 2.74e4"
                                + (", divB cleaning after every TVD pass" if args.divb else "")
-                               + (", open bottom / closed top (MURaM's physical x boundaries)" if args.xbnd else ""),
+                               + (", open bottom / closed top (MURaM's physical x boundaries)" if args.xbnd else "")
+                               + (f", Spitzer conduction (coefficient {args.spitzer:g})" if args.spitzer > 0 else ""),
                    "cells": n_cells, "precision": "fp32 storage+arithmetic",
                    "l2": "inputs larger than L2 (state 0.64 GB per buffer)",
                    "tvd_branch": "two half steps" if two_half else "single", "dt_s": dt, "cfl": cfl,
@@ -611,6 +615,8 @@ def main():
                     help="stratified: the headline box; ensemble: 64 uneven boxes in one launch; "
                          "large: one 1024x1024x256 box; adjoint: gradient of a 20-step objective")
     ap.add_argument("--boxes", type=int, default=64, help="boxes of the ensemble workload")
+    ap.add_argument("--spitzer", type=float, default=0.0,
+                    help="stratified workload with hyperbolic Spitzer conduction of this coefficient")
     ap.add_argument("--xbnd", action="store_true",
                     help="stratified workload with MURaM's physical x boundaries (open bottom) instead of the mirror")
     ap.add_argument("--divb", action="store_true",

@@ -15,8 +15,9 @@
 // only at ACCH::UpdateGPU, as with the reference's OpenACC build.
 //
 // Scope: MHD with the Boris correction, gravity, constant resistivity eta,
-// divB cleaning, periodic y/z, periodic or closed x (the OPEN_TOP = 0 mirror
-// rule), constant Tau and Qtot = 0 (radiation outside the path).  Every other
+// hyperbolic Spitzer conduction, divB cleaning, periodic y/z, periodic x or
+// MURaM's physical x boundaries without the potential-field top, constant Tau
+// and Qtot = 0 (radiation outside the path).  Every other
 // setting reports an error and aborts, as the reference does on invalid input.
 #include <mpi.h>
 
@@ -101,6 +102,7 @@ void fill_params(gpumhd_params& p, const RunData& Run, const GridData& Grid, con
   p.bnd_eps_top = Physics.bnd[i_bnd_eps_top];
   p.p_bc = p_bc;
   p.s_bc = s_bc;
+  p.spitzer = Physics.params[i_param_spitzer];
 }
 
 const RunData* g_run = nullptr;
@@ -137,7 +139,7 @@ extern "C" void GPUMHD_CAT(__real_, GPUMHD_EOS_INIT_MANGLED)(GridData&, RunData&
 extern "C" void GPUMHD_CAT(__wrap_, GPUMHD_EOS_INIT_MANGLED)(GridData& Grid, RunData& Run,
                                                             const PhysicsData& Physics) {
   GPUMHD_CAT(__real_, GPUMHD_EOS_INIT_MANGLED)(Grid, Run, Physics);
-  if (Physics.params[i_param_spitzer] > 0 || Physics.params[i_param_ambipolar] > 0 || Physics.bnd[i_bnd_pot] > 0 || Run.diagnostics || Physics.dmp[i_dmp_switch] > 0 ||
+  if (Physics.params[i_param_ambipolar] > 0 || Physics.bnd[i_bnd_pot] > 0 || Run.diagnostics || Physics.dmp[i_dmp_switch] > 0 ||
       Physics.rt_ext[i_ext_cor] > 0 || Grid.procs[0] * Grid.procs[1] * Grid.procs[2] != 1) {
     fprintf(stderr, "gpumhd: configuration outside the GPU path\n");
     MPI_Abort(MPI_COMM_WORLD, 1);
@@ -227,11 +229,13 @@ void UpdateCPU(void* ptr, std::size_t) {
   else if (ptr == g_grid->amb) check("download amb", gpumhd_download(g_ctx, 7, (double*)ptr));
   else if (ptr == g_grid->phi) check("download phi", gpumhd_download(g_ctx, 8, (double*)ptr));
   else if (ptr == g_grid->divB) check("download divB", gpumhd_download(g_ctx, 9, (double*)ptr));
+  else if (g_grid->sflx && ptr == g_grid->sflx) check("download sflx", gpumhd_download(g_ctx, 10, (double*)ptr));
 }
 void UpdateGPU(void* ptr, std::size_t) {
   if (!g_ctx || !g_grid) return;
   if (ptr == g_grid->U) check("upload U", gpumhd_upload(g_ctx, 0, (const double*)ptr));
   else if (ptr == g_grid->U0) check("upload U0", gpumhd_upload(g_ctx, 1, (const double*)ptr));
   else if (ptr == g_grid->divB) check("upload divB", gpumhd_upload(g_ctx, 9, (const double*)ptr));
+  else if (g_grid->sflx && ptr == g_grid->sflx) check("upload sflx", gpumhd_upload(g_ctx, 10, (const double*)ptr));
 }
 }  // namespace ACCH
