@@ -145,6 +145,8 @@ static void fill_kc(const Consts& c, KC<R>& k, const R* prof) {
     k.ww2[d] = (R)(-1. / (12. * c.dx[d] * c.dx[d]));
   }
   k.divb_fac = (R)c.divb_fac_d;
+  k.del_eps = (R)(c.inv_del_eps > 0.0 ? 1.0 / c.inv_del_eps : 0.0);
+  k.del_lr = (R)(c.inv_del_lr > 0.0 ? 1.0 / c.inv_del_lr : 0.0);
   k.divb_damp = (R)0.65;
   k.hfb = prof; k.hft = prof + c.g.sx; k.qft = prof + 2 * c.g.sx;
   k.has_visc_slope = (c.visc_slope_bot > 0.0 || c.visc_slope_top > 0.0);

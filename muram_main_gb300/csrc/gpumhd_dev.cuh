@@ -39,6 +39,7 @@ struct KC {
   R w1[3], w2[3];
   R eta, ww0[3], ww1[3], ww2[3];  // resistivity and the second-derivative stencil
   R divb_fac, divb_damp;          // divB cleaning: phi += fac*divB - damp*phi
+  R del_eps, del_lr;              // EOS cell widths (FP32 temperature lookup)
   const R* hfb;   // vertical boundary profiles, length sx
   const R* hft;
   const R* qft;

@@ -245,11 +245,13 @@ void Launch<R>::spitzer(const Consts& c, const R* U, bool prim, const R* T, cons
                         R* Rsp, const Dyn* dyn, int stage, cudaStream_t s) {
   const Geom& g = c.g;
   const int bx = (g.nx + SPT_BX - 1) / SPT_BX, by = (g.ny + SPT_BY - 1) / SPT_BY;
-  int gz = (152 * 8 + bx * by - 1) / (bx * by);
-  gz = gz < 1 ? 1 : (gz > g.nz ? g.nz : gz);
-  const dim3 grid(bx, by, gz), block(SPT_BX, SPT_BY);
-  if (prim) k_spitzer<R, true><<<grid, block, 0, s>>>(c, U, T, S, S0, Sout, Rflx, Rsp, dyn, stage);
-  else k_spitzer<R, false><<<grid, block, 0, s>>>(c, U, T, S, S0, Sout, Rflx, Rsp, dyn, stage);
+  // z chunks: about 16 blocks per SM
+  int nzch = (152 * 16 + bx * by - 1) / (bx * by);
+  nzch = nzch < 1 ? 1 : (nzch > g.nz ? g.nz : nzch);
+  const int zc = (g.nz + nzch - 1) / nzch;
+  const dim3 grid(bx, by, (g.nz + zc - 1) / zc), block(SPT_BX, SPT_BY);
+  if (prim) k_spitzer<R, true><<<grid, block, 0, s>>>(c, U, T, S, S0, Sout, Rflx, Rsp, dyn, stage, zc);
+  else k_spitzer<R, false><<<grid, block, 0, s>>>(c, U, T, S, S0, Sout, Rflx, Rsp, dyn, stage, zc);
 }
 template <class R>
 void Launch<R>::sflx_update(const Consts& c, R* S, const R* S0, R* Rflx, const Dyn* dyn, int stage, cudaStream_t s) {

@@ -74,6 +74,37 @@ __device__ inline double c2p_temp(const Consts& c, double d, double ei, double d
   return tm;
 }
 
+// Temperature in FP32, as eos_pres's FP32 path does the pressure: inside the
+// table (and away from the high-eps blend) the offsets from the cell's lower
+// corner come from ln of ratios near one, and the bilinear weights are the
+// offsets and the cell width minus them (so that they sum to the cell area the
+// table values are divided by); elsewhere the FP64 routine decides.
+__device__ __forceinline__ float eos_temp(const Consts& c, float d, float ei, float dn) {
+  constexpr float LN2 = 0.69314718f;
+  const KC<float>& k = c.kf;
+  const float eps = ei * dn + k.eps_off;
+  const float lgr = __log2f(d) * LN2;
+  const float ep = __log2f(eps) * LN2;
+  if (!(lgr >= k.xlr0 + 0.01f && lgr < k.xlrN + 1.0f && ep > k.xeps0 - 1.0f && ep < k.xepsN + 1.0f &&
+        !(eps > 0.8f * k.eps_max)))
+    return (float)c2p_temp(c, (double)d, (double)ei, 1.0 / (double)d);
+  int i_d = (int)((lgr - k.xlr0) * k.inv_del_lr);
+  i_d = max(0, min(c.N_lr - 2, i_d));
+  int i_e = (int)((ep - k.xeps0) * k.inv_del_eps);
+  i_e = max(0, min(c.N_eps - 2, i_e));
+  const float fe = log1p_small(eps * __ldg(c.inv_exp_xeps + i_e) - 1.0f);
+  const float fr = log1p_small(d * __ldg(c.inv_exp_xlr + i_d) - 1.0f);
+  const float ge = k.del_eps - fe, gr = k.del_lr - fr;
+  const float* T = c.tab[1];
+  const long long r1 = (long long)(i_e + 1) * c.N_lr + i_d;
+  const long long r0 = (long long)i_e * c.N_lr + i_d;
+  const float s = fe * fr * __ldg(T + r1 + 1) + fe * gr * __ldg(T + r1) + ge * fr * __ldg(T + r0 + 1) +
+                  ge * gr * __ldg(T + r0);
+  return expf(s);
+}
+__device__ __forceinline__ float temp_of(const Consts& c, float d, float ei) { return eos_temp(c, d, ei, 1.0f / d); }
+__device__ __forceinline__ double temp_of(const Consts& c, double d, double ei) { return c2p_temp(c, d, ei, 1.0 / d); }
+
 // Temperature of every cell, ghosts included, of a conserved state.
 template <class R>
 __global__ void __launch_bounds__(256) k_temp(Consts c, const R* __restrict__ U, R* __restrict__ T) {
@@ -82,29 +113,32 @@ __global__ void __launch_bounds__(256) k_temp(Consts c, const R* __restrict__ U,
     R v1, v2, v3, ei;
     const R d = U[id];
     prim_from_cons(d, U[g.N + id], U[2 * g.N + id], U[3 * g.N + id], U[4 * g.N + id], v1, v2, v3, ei);
-    T[id] = (R)c2p_temp(c, (double)d, (double)ei, 1.0 / (double)d);
+    T[id] = temp_of(c, d, ei);
   }
 }
 
-// One interior cell per thread (block 32 x 8 over x, y; z planes by the
-// grid's third dimension).  U: conserved (fused step) or primitive (after
-// ConsToPrim, PRIM).  T: temperature; S: sflx with its ghosts; stage: 1-4
-// in the fused step (stage 1 takes the previous step's dt for the relaxation
-// caps, as MHD_Residual runs before Sync_timestep there), 0 per routine
-// (the context's dt).  Outputs: Rsp (the energy residual's share), and
-// either Sout = S0 + wdt*Rflx with its periodic images (fused; Sout may be
-// S0 itself, each cell reading its own value before writing it) or Rflx.
+// One thread per (x, y) column of a chunk of zc interior z planes (block
+// 32 x 8); the z stencils of the heat flux, the temperature and B_z move
+// through five-value register windows, so a plane costs three new z loads.
+// U: conserved (fused step) or primitive (after ConsToPrim, PRIM).  T:
+// temperature; S: sflx with its ghosts; stage: 1-4 in the fused step (stage
+// 1 takes the previous step's dt for the relaxation caps, as MHD_Residual
+// runs before Sync_timestep there), 0 per routine (the context's dt).
+// Outputs: Rsp (the energy residual's share), and either Sout = S0 + wdt*Rflx
+// with its periodic images (fused; Sout may be S0 itself, each cell reading
+// its own value before writing it) or Rflx.
 template <class R, bool PRIM>
 __global__ void __launch_bounds__(SPT_BX* SPT_BY) k_spitzer(Consts c, const R* __restrict__ U, const R* __restrict__ T,
                                                            const R* __restrict__ S, const R* S0, R* Sout,
-                                                           R* __restrict__ Rflx,
-                                                           R* __restrict__ Rsp, const Dyn* __restrict__ dyn,
-                                                           int stage) {
+                                                           R* __restrict__ Rflx, R* __restrict__ Rsp,
+                                                           const Dyn* __restrict__ dyn, int stage, int zc) {
   if (dyn->err) return;
   const Geom& g = c.g;
   const int i = GH + blockIdx.x * SPT_BX + threadIdx.x;
   const int j = GH + blockIdx.y * SPT_BY + threadIdx.y;
   if (i >= GH + g.nx || j >= GH + g.ny) return;
+  const int k0 = GH + blockIdx.z * zc;
+  const int k1 = min(k0 + zc, GH + g.nz);
   // the relaxation's caps from the time step (src/mhdres_SR.C:137-145)
   const double dt_h = (stage == 1) ? dyn->dt_prev : dyn->dt;
   const double CFL_hyp = 1.8, avr_max = 0.25, eps_hyp = 0.02;
@@ -119,25 +153,41 @@ __global__ void __launch_bounds__(SPT_BX* SPT_BY) k_spitzer(Consts c, const R* _
     hyp_diff_d = eps_hyp * cmax_hyp_d / (smin(c.CFL, CFL_hyp) * c.dxmin);
   }
   const R cmax_hyp = (R)cmax_hyp_d, nu_hyp_max = (R)nu_hyp_max_d, hyp_diff = (R)hyp_diff_d;
-  const R k0 = (R)c.spitzer, sat_flx = (R)c.spt_sat_flx;
+  const R k0s = (R)c.spitzer, sat_flx = (R)c.spt_sat_flx;
   const R wdt = dynr<R>(dyn).wdt[stage > 0 ? stage : 0];
   const auto& kk = kc<R>(c);
-  const unsigned st[3] = {1u, (unsigned)g.sx, (unsigned)g.sx * (unsigned)g.sy};
-  for (int k = GH + blockIdx.z; k < GH + g.nz; k += gridDim.z) {
-    const unsigned id = cidx32(g, i, j, k);
-    R rsp = (R)0, bgt = (R)0, rfl = (R)0;
-    const R s0 = S[id];
+  const unsigned sy = (unsigned)g.sx, sz = (unsigned)g.sx * (unsigned)g.sy;
+  const R* Bx = U + 5u * g.N32;
+  const R* By = U + 6u * g.N32;
+  const R* Bz = U + 7u * g.N32;
+  const unsigned col = (unsigned)i + (unsigned)j * sy;
+  // z windows at k-2 .. k+2
+  R sw[5], tw[5], bw[5];
 #pragma unroll
-    for (int d = 0; d < 3; d++) {
-      const R* Bd = U + (unsigned)(5 + d) * g.N32;
-      const unsigned sd = st[d];
-      const R w1 = kk.w1[d], w2 = kk.w2[d];
-      const R sp1 = S[id + sd], sm1 = S[id - sd], sp2 = S[id + 2 * sd], sm2 = S[id - 2 * sd];
-      const R bp1 = Bd[id + sd], bm1 = Bd[id - sd], bp2 = Bd[id + 2 * sd], bm2 = Bd[id - 2 * sd];
-      rsp += (R)0 - (w1 * (sp1 * bp1 - sm1 * bm1) + w2 * (sp2 * bp2 - sm2 * bm2));
-      bgt += (Bd[id] * (w1 * (T[id + sd] - T[id - sd]) + w2 * (T[id + 2 * sd] - T[id - 2 * sd])));
-      rfl -= hyp_diff * ((sp2 + sm2) - (R)4. * (sp1 + sm1) + (R)6. * s0);
+  for (int o = 0; o < 4; o++) {
+    const unsigned id = col + (unsigned)(k0 - 2 + o) * sz;
+    sw[o] = S[id]; tw[o] = T[id]; bw[o] = Bz[id];
+  }
+  for (int k = k0; k < k1; k++) {
+    const unsigned id = col + (unsigned)k * sz;
+    {
+      const unsigned id2 = id + 2 * sz;
+      sw[4] = S[id2]; tw[4] = T[id2]; bw[4] = Bz[id2];
     }
+    const R s0 = sw[2];
+    R rsp = (R)0, bgt = (R)0, rfl = (R)0;
+    auto dir = [&](R w1, R w2, R sp1, R sm1, R sp2, R sm2, R bp1, R bm1, R bp2, R bm2, R b0, R tp1, R tm1, R tp2,
+                   R tm2) {
+      rsp += (R)0 - (w1 * (sp1 * bp1 - sm1 * bm1) + w2 * (sp2 * bp2 - sm2 * bm2));
+      bgt += (b0 * (w1 * (tp1 - tm1) + w2 * (tp2 - tm2)));
+      rfl -= hyp_diff * ((sp2 + sm2) - (R)4. * (sp1 + sm1) + (R)6. * s0);
+    };
+    dir(kk.w1[0], kk.w2[0], S[id + 1], S[id - 1], S[id + 2], S[id - 2], Bx[id + 1], Bx[id - 1], Bx[id + 2],
+        Bx[id - 2], Bx[id], T[id + 1], T[id - 1], T[id + 2], T[id - 2]);
+    dir(kk.w1[1], kk.w2[1], S[id + sy], S[id - sy], S[id + 2 * sy], S[id - 2 * sy], By[id + sy], By[id - sy],
+        By[id + 2 * sy], By[id - 2 * sy], By[id], T[id + sy], T[id - sy], T[id + 2 * sy], T[id - 2 * sy]);
+    dir(kk.w1[2], kk.w2[2], sw[3], sw[1], sw[4], sw[0], bw[3], bw[1], bw[4], bw[0], bw[2], tw[3], tw[1], tw[4],
+        tw[0]);
     // relaxation to the limited Spitzer flux (src/mhdres_SR.C:503-519)
     const R d = U[id];
     R v1, v2, v3, ei;
@@ -146,13 +196,13 @@ __global__ void __launch_bounds__(SPT_BX* SPT_BY) k_spitzer(Consts c, const R* _
     } else {
       prim_from_cons(d, U[g.N32 + id], U[2u * g.N32 + id], U[3u * g.N32 + id], U[4u * g.N32 + id], v1, v2, v3, ei);
     }
-    const R b5 = U[5u * g.N32 + id], b6 = U[6u * g.N32 + id], b7 = U[7u * g.N32 + id];
+    const R b5 = Bx[id], b6 = By[id], b7 = bw[2];
     const R vv = d_sqrt(v1 * v1 + v2 * v2 + v3 * v3);
     const R bb = b5 * b5 + b6 * b6 + b7 * b7;
-    const R tempi = T[id];
+    const R tempi = tw[2];
     const R c_lim = cmax_hyp - vv;
     const R tt32 = tempi * d_sqrt(tempi);
-    R kap_spt = k0 * tempi * tt32;
+    R kap_spt = k0s * tempi * tt32;
     const R F_sat = sat_flx * d * tt32;
     const R invBB = (R)1.0 / smax(spt_bbmin<R>(), bb);
     R F_spt = -kap_spt * bgt;
@@ -169,6 +219,8 @@ __global__ void __launch_bounds__(SPT_BX* SPT_BY) k_spitzer(Consts c, const R* _
       const Images im = images_of(g, i, j, k, false);
       for_images<true>(g, i, j, k, im, [&](unsigned long long gid, bool) { Sout[(unsigned)gid] = sn; });
     }
+#pragma unroll
+    for (int o = 0; o < 4; o++) { sw[o] = sw[o + 1]; tw[o] = tw[o + 1]; bw[o] = bw[o + 1]; }
   }
 }
 

@@ -91,10 +91,7 @@ def test_fused_vs_oracle(gpu_lib, kernel, case):
 def test_fp32_spitzer_vs_fp64_oracle(gpu_lib, xbnd):
     """FP32 state and arithmetic against the FP64 oracle after 30 steps of a
     stratified box with conduction (coefficient 0.5), mirrored or open x.
-    Mirrored: the 1e-5 bar (measured 4.8e-6).  Open bottom: its pressure
-    extrapolation from the layers' fluctuations feeds FP32 rounding back into
-    the box (6e-6 in the momenta without conduction, 1.03e-5 with it), so the
-    bar there is 2e-5."""
+    The 1e-5 bar (measured 4.8e-6 mirrored, 5.4e-6 open)."""
     from oracle import oracle as O
     tab = initial.EosTable(H.EOS_SMALL)
     U = initial.stratified_box(tab, 32, 24, 24, dx=1.6e6, seed=53)
@@ -107,7 +104,7 @@ def test_fp32_spitzer_vs_fp64_oracle(gpu_lib, xbnd):
     g.run_steps(30)
     e = H.rel_l2(H.interior(g.download_state()), H.interior(st.U))
     print(f"FP32 Spitzer vs FP64 oracle [xbnd={xbnd}], rel L2:", np.array2string(e, precision=2))
-    assert np.all(e <= (2e-5 if xbnd else 1e-5)), e
+    assert np.all(e <= 1e-5), e
     g.close()
 
 
