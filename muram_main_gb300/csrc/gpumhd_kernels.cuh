@@ -68,6 +68,65 @@ __device__ __forceinline__ void for_images(const Geom& g, int i, int j, int k, c
   }
 }
 
+// The ghost images of the cells of one (i, j) column as 32-bit index offsets:
+// the x and y parts (0: none) are fixed along the column, the z part depends
+// on the plane only (uniform over a block that shares k).  Writes the same
+// (index, mirrored) set as images_of / for_images.
+struct ColImg {
+  int ox, oy;  // offsets of the x and y images
+  int xf;      // the x image is a mirror (sign flips)
+};
+__device__ __forceinline__ ColImg col_images(const Geom& g, int i, int j, bool xmirror) {
+  ColImg ci;
+  ci.ox = 0; ci.oy = 0; ci.xf = 0;
+  const int I = i - GH, J = j - GH;
+  if (g.periodic_x) {
+    if (I < GH) ci.ox = g.nx;
+    else if (I >= g.nx - GH) ci.ox = -g.nx;
+  } else if (xmirror && g.xmirror) {
+    if (I < GH) { ci.ox = 2 * GH - 1 - 2 * i; ci.xf = 1; }
+    else if (I >= g.nx - GH) { ci.ox = 2 * GH + 2 * g.nx - 1 - 2 * i; ci.xf = 1; }
+  }
+  if (J < GH) ci.oy = g.ny * g.sx;
+  else if (J >= g.ny - GH) ci.oy = -g.ny * g.sx;
+  return ci;
+}
+__device__ __forceinline__ int z_image_off(const Geom& g, int k) {
+  const int K = k - GH;
+  const int pl = g.sx * g.sy;
+  return K < GH ? g.nz * pl : (K >= g.nz - GH ? -g.nz * pl : 0);
+}
+// f(index, mirrored) for the cell id and each of its images.
+template <class F>
+__device__ __forceinline__ void for_col_images(unsigned id, const ColImg& ci, int oz, F f) {
+  f(id, false);
+  if (ci.ox) f(id + (unsigned)ci.ox, ci.xf != 0);
+  if (ci.oy) {
+    f(id + (unsigned)ci.oy, false);
+    if (ci.ox) f(id + (unsigned)(ci.oy + ci.ox), ci.xf != 0);
+  }
+  if (oz) {
+    f(id + (unsigned)oz, false);
+    if (ci.ox) f(id + (unsigned)(oz + ci.ox), ci.xf != 0);
+    if (ci.oy) {
+      f(id + (unsigned)(oz + ci.oy), false);
+      if (ci.ox) f(id + (unsigned)(oz + ci.oy + ci.ox), ci.xf != 0);
+    }
+  }
+}
+template <class R>
+__device__ __forceinline__ void store_state_col(const Geom& g, R* __restrict__ U, unsigned id, const ColImg& ci, int oz,
+                                                const R v[NV]) {
+  for_col_images(id, ci, oz, [&](unsigned t, bool f) {
+#pragma unroll
+    for (int q = 0; q < NV; q++) {
+      R x = v[q];
+      if (f && (q == 1 || q == 6 || q == 7)) x = -x;
+      U[t + (unsigned)q * g.N32] = x;
+    }
+  });
+}
+
 template <class R, bool IDX32 = false>
 __device__ __forceinline__ void store_state(const Geom& g, R* __restrict__ U, int i, int j, int k, const Images& im,
                                             const R v[NV]) {

@@ -330,7 +330,8 @@ __global__ void __launch_bounds__(TX* TY, 2)
   bool pend = false;
   auto finish_pressure = [&](int kp) {
     const R pr = eos_pres_end(plook);
-    store_scalar<R, true>(g, Pout, i, j, kp, images_of(g, i, j, kp, true), pr);
+    for_col_images(own0 + (unsigned)kp * plane, col_images(g, i, j, true), z_image_off(g, kp),
+                   [&](unsigned t, bool) { Pout[t] = pr; });
     pend = false;
   };
   int s0 = 2;  // ring slot of plane k
@@ -433,8 +434,7 @@ __global__ void __launch_bounds__(TX* TY, 2)
         stage_sources<R>(Racc, cen, kk_.gx, inv_va2max, invRdt);
         R un[NV];
         rk_update<R>(c, Cc, id, stage, wdt, base, Racc, vmax, emax, un);
-        const Images im = images_of(g, i, j, k, true);
-        store_state<R, true>(g, Uout, i, j, k, im, un);
+        store_state_col<R>(g, Uout, id, col_images(g, i, j, true), z_image_off(g, k), un);
         if (write_pres) {
           R v1, v2, v3, ei;
           prim_from_cons(un[0], un[1], un[2], un[3], un[4], v1, v2, v3, ei);
