@@ -121,6 +121,18 @@ int gpumhd_eos_init(gpumhd_ctx* ctx, const char* path);
  * heat flux, GridData::sflx); one double per node. */
 int gpumhd_upload(gpumhd_ctx* ctx, int which, const double* host);
 int gpumhd_download(gpumhd_ctx* ctx, int which, double* host);
+/* The same transfers without waiting (no reference counterpart): each one
+ * is ordered with the context's steps as the synchronous call is, but its
+ * host copy runs on a copy stream of its own, so that the upload of one
+ * step's input and the download of another step's result overlap the steps
+ * in between.  The host buffer must stay valid (and, for an upload,
+ * unchanged) until gpumhd_synchronize, which also waits for these copies;
+ * pinned host memory makes the copies asynchronous.  Each direction has two
+ * device-side buffers used in turn (2 x 8 doubles per node, allocated on the
+ * first asynchronous call); a third transfer waits for the first one's
+ * buffer, so any number may be queued. */
+int gpumhd_upload_async(gpumhd_ctx* ctx, int which, const double* host);
+int gpumhd_download_async(gpumhd_ctx* ctx, int which, double* host);
 
 /* Clean_divB (include/divB.H:5, src/clean_divB.C:35-369): damped iterations
  * phi += fac*divB - 0.65*phi, B += grad phi, e += phi*divB on U, their count

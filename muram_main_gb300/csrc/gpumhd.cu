@@ -30,6 +30,14 @@ struct gpumhd_ctx {
   void* aux[4] = {nullptr, nullptr, nullptr, nullptr};  // temp, ne, rhoi, amb
   void* T = nullptr;                          // TVD scratch of the per-routine path (8N)
   double* staging = nullptr;                  // host-layout transfer buffer (8N doubles)
+  // asynchronous transfers: their own copy streams and two host-layout
+  // buffers per direction (used in turn), ordered against the context's
+  // stream by events (created on first use)
+  cudaStream_t s_in = nullptr, s_out = nullptr;
+  double* astage_in[2] = {nullptr, nullptr};  // 8N doubles each
+  double* astage_out[2] = {nullptr, nullptr};
+  cudaEvent_t ev_in_ready[2] = {}, ev_in_free[2] = {}, ev_out_ready[2] = {}, ev_out_free[2] = {};
+  unsigned n_up = 0, n_down = 0;              // asynchronous transfers so far (buffer turn)
   Dyn* dyn = nullptr;
   double* dt_hist = nullptr;
   int dt_hist_cap = 0;
@@ -475,6 +483,16 @@ extern "C" int gpumhd_destroy(gpumhd_ctx* ctx) {
   for (void* q : ctx->aux) cudaFree(q);
   cudaFree(ctx->T);
   cudaFree(ctx->staging);
+  if (ctx->s_in) cudaStreamSynchronize(ctx->s_in);
+  if (ctx->s_out) cudaStreamSynchronize(ctx->s_out);
+  for (int b = 0; b < 2; b++) {
+    cudaFree(ctx->astage_in[b]);
+    cudaFree(ctx->astage_out[b]);
+    for (cudaEvent_t e : {ctx->ev_in_ready[b], ctx->ev_in_free[b], ctx->ev_out_ready[b], ctx->ev_out_free[b]})
+      if (e) cudaEventDestroy(e);
+  }
+  if (ctx->s_in) cudaStreamDestroy(ctx->s_in);
+  if (ctx->s_out) cudaStreamDestroy(ctx->s_out);
   cudaFree(ctx->comp);
   cudaFree(ctx->phi);
   cudaFree(ctx->divb);
@@ -791,6 +809,75 @@ extern "C" int gpumhd_tile_from(gpumhd_ctx* ctx, gpumhd_ctx* src) {
   if (ctx->comp) CK(cudaMemsetAsync(ctx->comp, 0, sizeof(float) * 8 * gd.N, ctx->stream));
   ctx->fused_ready = false;
   return check_launch(ctx, 2);
+}
+
+// The asynchronous transfers' streams, events and buffers.
+static int ensure_async(gpumhd_ctx* ctx) {
+  if (ctx->s_in) return GPUMHD_OK;
+  const size_t B = sizeof(double) * 8 * (size_t)ctx->c.g.N;
+  for (int b = 0; b < 2; b++) {
+    CK(cudaMalloc(&ctx->astage_in[b], B));
+    CK(cudaMalloc(&ctx->astage_out[b], B));
+    for (cudaEvent_t* e : {&ctx->ev_in_ready[b], &ctx->ev_in_free[b], &ctx->ev_out_ready[b], &ctx->ev_out_free[b]})
+      CK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+  }
+  CK(cudaStreamCreateWithFlags(&ctx->s_out, cudaStreamNonBlocking));
+  CK(cudaStreamCreateWithFlags(&ctx->s_in, cudaStreamNonBlocking));
+  return GPUMHD_OK;
+}
+
+// Upload through the copy-in stream: the host-to-device copy waits only for
+// the conversion of the upload before last (two buffers in turn), so it
+// overlaps the steps enqueued before it; the conversion into the field runs
+// in stream order.
+extern "C" int gpumhd_upload_async(gpumhd_ctx* ctx, int which, const double* host) {
+  if (!ctx || !host) return GPUMHD_E_INVALID;
+  CK(cudaSetDevice(ctx->device));
+  int nf, rc;
+  void* dst = field_ptr(ctx, which, &nf, &rc);
+  if (rc) return fail(ctx, rc, "upload_async: bad field %d", which);
+  rc = ensure_async(ctx);
+  if (rc) return rc;
+  const long long N = ctx->c.g.N;
+  const int b = (int)(ctx->n_up++ & 1u);
+  CK(cudaStreamWaitEvent(ctx->s_in, ctx->ev_in_free[b], 0));
+  CK(cudaMemcpyAsync(ctx->astage_in[b], host, sizeof(double) * nf * N, cudaMemcpyHostToDevice, ctx->s_in));
+  CK(cudaEventRecord(ctx->ev_in_ready[b], ctx->s_in));
+  CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_in_ready[b], 0));
+  if (ctx->f32) Launch<float>::aos_to_soa(N, nf, ctx->astage_in[b], (float*)dst, ctx->stream);
+  else Launch<double>::aos_to_soa(N, nf, ctx->astage_in[b], (double*)dst, ctx->stream);
+  CK(cudaEventRecord(ctx->ev_in_free[b], ctx->stream));
+  if (which == 0) {
+    ctx->fused_ready = false;
+    if (ctx->comp) CK(cudaMemsetAsync(ctx->comp, 0, sizeof(float) * 8 * N, ctx->stream));
+  }
+  if (which == 3) ctx->have_pres = true;
+  return check_launch(ctx, 1);
+}
+
+// Download through the copy-out stream: the field is converted in stream
+// order into a copy-out buffer (once the download before last has left it)
+// and copied to the host while later steps run.
+extern "C" int gpumhd_download_async(gpumhd_ctx* ctx, int which, double* host) {
+  if (!ctx || !host) return GPUMHD_E_INVALID;
+  CK(cudaSetDevice(ctx->device));
+  int nf, rc;
+  void* src = field_ptr(ctx, which, &nf, &rc);
+  if (rc) return fail(ctx, rc, "download_async: bad field %d", which);
+  rc = ensure_async(ctx);
+  if (rc) return rc;
+  const long long N = ctx->c.g.N;
+  const int b = (int)(ctx->n_down++ & 1u);
+  CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_out_free[b], 0));
+  if (ctx->f32) Launch<float>::soa_to_aos(N, nf, (const float*)src, ctx->astage_out[b], ctx->stream);
+  else Launch<double>::soa_to_aos(N, nf, (const double*)src, ctx->astage_out[b], ctx->stream);
+  rc = check_launch(ctx, 1);
+  if (rc) return rc;
+  CK(cudaEventRecord(ctx->ev_out_ready[b], ctx->stream));
+  CK(cudaStreamWaitEvent(ctx->s_out, ctx->ev_out_ready[b], 0));
+  CK(cudaMemcpyAsync(host, ctx->astage_out[b], sizeof(double) * nf * N, cudaMemcpyDeviceToHost, ctx->s_out));
+  CK(cudaEventRecord(ctx->ev_out_free[b], ctx->s_out));
+  return GPUMHD_OK;
 }
 
 extern "C" int gpumhd_download(gpumhd_ctx* ctx, int which, double* host) {
@@ -1275,8 +1362,10 @@ static int fused_prepare(gpumhd_ctx* ctx, int nsteps) {
   if (!ctx->fused_ready) {
     // exchange + boundaries before the loop (src/solver.C:80-81), then the
     // pressure, CFL speed and statistics of the initial state
-    int rc0 = pull_dyn(ctx);
-    if (rc0) return rc0;
+    // The limits, error flag and accumulators are reset by a kernel rather
+    // than a host round trip of Dyn: no host synchronisation and no small
+    // copy queued behind large asynchronous transfers.  The host mirror gets
+    // the same values (its other fields are refreshed by the next pull).
     Dyn& d = ctx->hdyn;
     d.va_ini_flag = 0;
     d.inv_va2max = 1.0 / pow(ctx->p.va_max, 2);
@@ -1285,11 +1374,14 @@ static int fused_prepare(gpumhd_ctx* ctx, int nsteps) {
     const double vml = ctx->p.tvd[8];
     d.vsqr_diff = vml < 1.0 ? pow(vml * d.v_lim, 2.0) : pow(vml, 2.0);
     d.err = 0;
-    int rc = reset_accumulators(ctx);
-    if (rc) return rc;
+    d.cmax_bits = 0;
+    d.stat_max_bits[0] = d.stat_max_bits[1] = d.stat_max_bits[2] = 0;
+    d.stat_cnt[0] = d.stat_cnt[1] = 0;
+    k_fused_reinit<<<1, 32, 0, ctx->stream>>>(ctx->c, ctx->dyn, d.inv_va2max, d.v_lim, d.e_lim, d.vsqr_diff);
+    int rc = GPUMHD_OK;
     // physical x boundaries: their ghosts, with the CFL speed of the x ghosts
     // (no longer images of interior cells), before the pressures and statistics
-    int n = 2;
+    int n = 3;
     if (ctx->c.has_spitzer) {  // the heat flux's periodic images
       if (ctx->f32) Launch<float>::fill_ghosts(ctx->c, (float*)ctx->spt[0], 1, 0, ctx->stream);
       else Launch<double>::fill_ghosts(ctx->c, (double*)ctx->spt[0], 1, 0, ctx->stream);
@@ -1351,6 +1443,8 @@ extern "C" int gpumhd_synchronize(gpumhd_ctx* ctx) {
   if (!ctx) return GPUMHD_E_INVALID;
   CK(cudaSetDevice(ctx->device));
   CK(cudaStreamSynchronize(ctx->stream));
+  if (ctx->s_out) CK(cudaStreamSynchronize(ctx->s_out));
+  if (ctx->s_in) CK(cudaStreamSynchronize(ctx->s_in));
   int rc = pull_dyn(ctx);
   if (rc) return rc;
   switch (ctx->hdyn.err) {

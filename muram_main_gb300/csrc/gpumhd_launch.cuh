@@ -17,6 +17,10 @@ __global__ void k_step_begin(Consts c, Dyn* dyn, double* dt_hist, int dt_hist_ca
 __global__ void k_loop_tick(int* counter, cudaGraphConditionalHandle h);
 __global__ void k_set_counter(int* counter, int n);
 __global__ void k_divb_begin(Dyn* dyn);
+// Start of a fused run on a new state (one thread): the step limits, the
+// error flag, the reduction accumulators and the per-precision derived
+// scalars, set on the device so that no host copy sits in the stream.
+__global__ void k_fused_reinit(Consts c, Dyn* dyn, double inv_va2max, double v_lim, double e_lim, double vsqr_diff);
 __global__ void k_divb_end(Consts c, Dyn* dyn);
 
 template <class R>

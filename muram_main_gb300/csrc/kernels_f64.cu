@@ -67,6 +67,21 @@ __global__ void k_set_counter(int* counter, int n) {
   if (threadIdx.x == 0) *counter = n;
 }
 
+__global__ void k_fused_reinit(Consts c, Dyn* dyn, double inv_va2max, double v_lim, double e_lim, double vsqr_diff) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  dyn->va_ini_flag = 0;
+  dyn->inv_va2max = inv_va2max;
+  dyn->v_lim = v_lim;
+  dyn->e_lim = e_lim;
+  dyn->vsqr_diff = vsqr_diff;
+  dyn->err = 0;
+  dyn->cmax_bits = 0ULL;
+  dyn->stat_max_bits[0] = dyn->stat_max_bits[1] = dyn->stat_max_bits[2] = 0ULL;
+  dyn->stat_cnt[0] = dyn->stat_cnt[1] = 0ULL;
+  derive_one<float>(*dyn, c.dx, c.idx, c.rt_cfl, c.tchk_vmax, c.tchk_eps_max, dyn->rf);
+  derive_one<double>(*dyn, c.dx, c.idx, c.rt_cfl, c.tchk_vmax, c.tchk_eps_max, dyn->rd);
+}
+
 __global__ void k_divb_begin(Dyn* dyn) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   if (dyn->err) return;

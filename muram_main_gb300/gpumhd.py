@@ -61,7 +61,8 @@ class Params(C.Structure):
 
 EXPORTS = [
     "gpumhd_default_params", "gpumhd_create", "gpumhd_destroy", "gpumhd_set_params", "gpumhd_get_params",
-    "gpumhd_last_error", "gpumhd_eos_init", "gpumhd_upload", "gpumhd_download", "gpumhd_save_cons",
+    "gpumhd_last_error", "gpumhd_eos_init", "gpumhd_upload", "gpumhd_download", "gpumhd_upload_async",
+    "gpumhd_download_async", "gpumhd_save_cons",
     "gpumhd_cons_to_prim", "gpumhd_adjust_valf_max", "gpumhd_get_limits", "gpumhd_mhd_residual",
     "gpumhd_sync_timestep", "gpumhd_source_integrate_tcheck", "gpumhd_tvdlimit", "gpumhd_tcheck",
     "gpumhd_exchange", "gpumhd_run_steps", "gpumhd_enqueue_steps", "gpumhd_synchronize", "gpumhd_step_info",
@@ -101,6 +102,8 @@ def load(build_if_missing=True):
         "gpumhd_last_error": (C.c_char_p, [vp]),
         "gpumhd_eos_init": (C.c_int, [vp, C.c_char_p]),
         "gpumhd_upload": (C.c_int, [vp, C.c_int, dp]),
+        "gpumhd_upload_async": (C.c_int, [vp, C.c_int, dp]),
+        "gpumhd_download_async": (C.c_int, [vp, C.c_int, dp]),
         "gpumhd_download": (C.c_int, [vp, C.c_int, dp]),
         "gpumhd_save_cons": (C.c_int, [vp]),
         "gpumhd_cons_to_prim": (C.c_int, [vp]),
@@ -370,6 +373,16 @@ class MuramGPU:
 
     def download_ptr(self, which, ptr):
         self._chk(self._L.gpumhd_download(self._h, which, C.cast(ptr, C.POINTER(C.c_double))))
+
+    def upload_ptr_async(self, which, ptr):
+        """Upload from a host pointer without waiting: the copy overlaps the
+        steps enqueued before it; the buffer must stay valid and unchanged
+        until synchronize()."""
+        self._chk(self._L.gpumhd_upload_async(self._h, which, C.cast(ptr, C.POINTER(C.c_double))))
+
+    def download_ptr_async(self, which, ptr):
+        """Download to a host pointer without waiting; the data are there after synchronize()."""
+        self._chk(self._L.gpumhd_download_async(self._h, which, C.cast(ptr, C.POINTER(C.c_double))))
 
     def adjoint(self, nsteps, dJ_dUT, checkpoint_every=5):
         """dJ/dU_0 for J(U_T) over nsteps fixed-dt FP64 steps from the current
