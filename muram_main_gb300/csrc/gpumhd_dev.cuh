@@ -234,6 +234,26 @@ __device__ __forceinline__ unsigned cidx32(const Geom& g, int i, int j, int k) {
   return (unsigned)i + (unsigned)g.sx * ((unsigned)j + (unsigned)g.sy * (unsigned)k);
 }
 
+// (i, j, k) of interior cell t (x fastest) and of box node id, in 32-bit
+// arithmetic (8 N < 2^32 for every context, so both fit).
+__device__ __forceinline__ void interior_ijk(const Geom& g, unsigned t, int& i, int& j, int& k) {
+  const unsigned nx = (unsigned)g.nx, ny = (unsigned)g.ny;
+  const unsigned q = t / nx;
+  i = GH + (int)(t - q * nx);
+  j = GH + (int)(q % ny);
+  k = GH + (int)(q / ny);
+}
+__device__ __forceinline__ void node_ijk(const Geom& g, unsigned id, int& i, int& j, int& k) {
+  const unsigned sx = (unsigned)g.sx, sy = (unsigned)g.sy;
+  const unsigned q = id / sx;
+  i = (int)(id - q * sx);
+  j = (int)(q % sy);
+  k = (int)(q / sy);
+}
+// Grid-stride loop bounds in 32 bits.
+__device__ __forceinline__ unsigned gs_first() { return blockIdx.x * blockDim.x + threadIdx.x; }
+__device__ __forceinline__ unsigned gs_step() { return gridDim.x * blockDim.x; }
+
 // Order-preserving bits for non-negative doubles (cmax, maxima); NaN never stored.
 __device__ __forceinline__ void atomic_max_nonneg(unsigned long long* dst, double v) {
   if (v == v && v > 0.0) atomicMax(dst, (unsigned long long)__double_as_longlong(v));
@@ -394,6 +414,57 @@ __device__ __forceinline__ float eos_pres(const Consts& c, float d, float ei, fl
   const float fr = log1p_small(d * __ldg(c.inv_exp_xlr + i_d) - 1.0f);
   const float4 q = __ldg(c.pquad + (long long)i_e * c.N_lr + i_d);
   return q.x * exp_small(fe * q.y + fr * q.z + fe * fr * q.w);
+}
+
+// All ConsToPrim outputs in FP32 (src/cons_to_prim.C:148-243): the pressure
+// from eos_pres; temperature, n_e, rho_i and the ambipolar coefficient as
+// exp of float bilinear sums whose weights are the offsets from the cell's
+// corners taken as ln of ratios near one (table values are pre-divided by
+// the cell area, so the weights must be formed to float accuracy); outside
+// the table or in the high-eps blend the FP64 routine decides.
+__device__ inline void c2p_outputs(const Consts& c, float d, float ei, float dn, float& pr, float& tm, float& ne,
+                                   float& ri, float& am) {
+  constexpr float LN2 = 0.69314718f;
+  const KC<float>& k = c.kf;
+  const float eps = ei * dn + k.eps_off;
+  const float lgr = __log2f(d) * LN2;
+  const float ep = __log2f(eps) * LN2;
+  if (!(lgr >= k.xlr0 + 0.01f && lgr < k.xlrN + 1.0f && ep > k.xeps0 - 1.0f && ep < k.xepsN + 1.0f &&
+        !(eps > 0.8f * k.eps_max))) {
+    const C2POut o = c2p_eos_full(c, (double)d, (double)ei, 1.0 / (double)d);
+    pr = (float)o.pres; tm = (float)o.temp; ne = (float)o.ne; ri = (float)o.rhoi; am = (float)o.amb;
+    return;
+  }
+  int i_d = (int)((lgr - k.xlr0) * k.inv_del_lr);
+  i_d = max(0, min(c.N_lr - 2, i_d));
+  int i_e = (int)((ep - k.xeps0) * k.inv_del_eps);
+  i_e = max(0, min(c.N_eps - 2, i_e));
+  const float fe = log1p_small(eps * __ldg(c.inv_exp_xeps + i_e) - 1.0f);
+  const float fr = log1p_small(d * __ldg(c.inv_exp_xlr + i_d) - 1.0f);
+  const float ge = k.del_eps - fe, gr = k.del_lr - fr;
+  const long long r1 = (long long)(i_e + 1) * c.N_lr + i_d;
+  const long long r0 = (long long)i_e * c.N_lr + i_d;
+  auto look = [&](int t) {
+    const float* T = c.tab[t];
+    return expf(fe * fr * __ldg(T + r1 + 1) + fe * gr * __ldg(T + r1) + ge * fr * __ldg(T + r0 + 1) +
+                ge * gr * __ldg(T + r0));
+  };
+  pr = eos_pres(c, d, ei, dn);
+  tm = look(1);
+  ne = look(3);
+  ri = look(4);
+  am = look(5);
+  const float inf = __int_as_float(0x7f800000);
+  if (!(pr > 0.0f && pr < inf) || !(tm > 0.0f && tm < inf)) {
+    pr = (float)(c.c_pres * (double)ei);
+    tm = (float)(c.c_temp * (double)eps);
+  }
+  if (!(ne >= 1.0f) || ne == inf) ne = 1.0f;
+}
+__device__ inline void c2p_outputs(const Consts& c, double d, double ei, double dn, double& pr, double& tm, double& ne,
+                                   double& ri, double& am) {
+  const C2POut o = c2p_eos_full(c, d, ei, dn);
+  pr = o.pres; tm = o.temp; ne = o.ne; ri = o.rhoi; am = o.amb;
 }
 
 // The pressure lookup split in two, so that a kernel can issue the table

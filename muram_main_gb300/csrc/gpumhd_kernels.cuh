@@ -527,6 +527,7 @@ __global__ void __launch_bounds__(TX* TY, 2) k_stage(Consts c, const R* __restri
   const R invRdt = dr.invRdt;
   const R vmax = dr.vmax;
   const R emax = dr.emax;
+  R cm_acc = (R)0;  // residual mode: this thread's largest CFL speed
   R prim[NF];
   R fl[NF];
   prim[NPRIM] = (R)0;
@@ -643,9 +644,9 @@ __global__ void __launch_bounds__(TX* TY, 2) k_stage(Consts c, const R* __restri
       if (RESID) {
 #pragma unroll
         for (int q = 0; q < NV; q++) Res[id + (unsigned)q * g.N32] = Racc[q];
-        R cm = cmax_cell<R>(cen[P_D], cen[P_V1], cen[P_V2], cen[P_V3], cen[P_B1], cen[P_B2], cen[P_B3], cen[P_P],
-                            inv_va2max);
-        atomic_max_nonneg(&dyn->cmax_bits, (double)cm);
+        const R cm = cmax_cell<R>(cen[P_D], cen[P_V1], cen[P_V2], cen[P_V3], cen[P_B1], cen[P_B2], cen[P_B3],
+                                  cen[P_P], inv_va2max);
+        if (cm > cm_acc) cm_acc = cm;  // a NaN speed is skipped, as the atomic maximum skips it
       } else {
         // sources, Boris correction, update, Tcheck (src/Add_Sources_Integrate_SR.C:331-465)
         stage_sources<R>(Racc, cen, kk_.gx, inv_va2max, invRdt);
@@ -662,6 +663,10 @@ __global__ void __launch_bounds__(TX* TY, 2) k_stage(Consts c, const R* __restri
       }
     }
     __syncthreads();
+  }
+  if (RESID) {  // one atomic per block
+    const R m = block_max_nonnan(cm_acc);
+    if (threadIdx.x == 0 && threadIdx.y == 0) atomic_max_nonneg(&dyn->cmax_bits, (double)m);
   }
 }
 
@@ -1169,19 +1174,20 @@ template <class R>
 __global__ void k_cons_to_prim(Consts c, R* __restrict__ U, R* __restrict__ P, R* __restrict__ T, R* __restrict__ Ne,
                                R* __restrict__ Ri, R* __restrict__ Am) {
   const Geom& g = c.g;
-  for (long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x; id < g.N; id += (long long)gridDim.x * blockDim.x) {
+  const unsigned N = g.N32;
+  for (unsigned id = gs_first(); id < N; id += gs_step()) {
     R d = U[id];
     R v1, v2, v3, ei;
-    prim_from_cons(d, U[g.N + id], U[2 * g.N + id], U[3 * g.N + id], U[4 * g.N + id], v1, v2, v3, ei);
+    prim_from_cons(d, U[N + id], U[2 * N + id], U[3 * N + id], U[4 * N + id], v1, v2, v3, ei);
     const R dn = (R)1.0 / d;
-    C2POut o = c2p_eos_full(c, (double)d, (double)ei, (double)dn);
-    if (sizeof(R) == 4) o.pres = (double)eos_pres(c, d, ei, dn);
-    U[g.N + id] = v1;
-    U[2 * g.N + id] = v2;
-    U[3 * g.N + id] = v3;
-    U[4 * g.N + id] = ei;
-    P[id] = (R)o.pres;
-    if (T) { T[id] = (R)o.temp; Ne[id] = (R)o.ne; Ri[id] = (R)o.rhoi; Am[id] = (R)o.amb; }
+    R pr, tm, ne, ri, am;
+    c2p_outputs(c, d, ei, dn, pr, tm, ne, ri, am);
+    U[N + id] = v1;
+    U[2 * N + id] = v2;
+    U[3 * N + id] = v3;
+    U[4 * N + id] = ei;
+    P[id] = pr;
+    if (T) { T[id] = tm; Ne[id] = ne; Ri[id] = ri; Am[id] = am; }
   }
 }
 
@@ -1194,15 +1200,17 @@ __global__ void k_init_pass(Consts c, const R* __restrict__ U, R* __restrict__ P
   unsigned long long nv = 0, ne = 0;
   const R inv_va2max = dynr<R>(dyn).inv_va2max;
   const R vlim95 = dynr<R>(dyn).vlim95, elim95 = dynr<R>(dyn).elim95;
-  for (long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x; id < g.N; id += (long long)gridDim.x * blockDim.x) {
+  const unsigned N = g.N32;
+  for (unsigned id = gs_first(); id < N; id += gs_step()) {
     R d = U[id];
     R v1, v2, v3, ei;
-    prim_from_cons(d, U[g.N + id], U[2 * g.N + id], U[3 * g.N + id], U[4 * g.N + id], v1, v2, v3, ei);
+    prim_from_cons(d, U[N + id], U[2 * N + id], U[3 * N + id], U[4 * N + id], v1, v2, v3, ei);
     R pr = eos_pres(c, d, ei, (R)1.0 / d);
     P[id] = pr;
-    const int i = (int)(id % g.sx), j = (int)((id / g.sx) % g.sy), k = (int)(id / ((long long)g.sx * g.sy));
+    int i, j, k;
+    node_ijk(g, id, i, j, k);
     if (i >= GH && i < GH + g.nx && j >= GH && j < GH + g.ny && k >= GH && k < GH + g.nz) {
-      cm_loc = smax(cm_loc, cmax_cell<R>(d, v1, v2, v3, U[5 * g.N + id], U[6 * g.N + id], U[7 * g.N + id], pr, inv_va2max));
+      cm_loc = smax(cm_loc, cmax_cell<R>(d, v1, v2, v3, U[5 * N + id], U[6 * N + id], U[7 * N + id], pr, inv_va2max));
       R vabs = d_sqrt(v1 * v1 + v2 * v2 + v3 * v3);
       R cs = (R)(5 / 3.) * pr / d;
       R ee = ei / d;
@@ -1234,14 +1242,15 @@ __global__ void k_init_pass(Consts c, const R* __restrict__ U, R* __restrict__ P
 template <class R>
 __global__ void k_adjust_stats(Consts c, const R* __restrict__ U, const R* __restrict__ P, Dyn* __restrict__ dyn) {
   const Geom& g = c.g;
-  const long long n = (long long)g.nx * g.ny * g.nz;
+  const unsigned n = (unsigned)g.nx * (unsigned)g.ny * (unsigned)g.nz, N = g.N32;
   R sv = 0, sc = 0, se = 0;
   unsigned long long nv = 0, ne = 0;
   const R vlim95 = dynr<R>(dyn).vlim95, elim95 = dynr<R>(dyn).elim95;
-  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
-    const int i = GH + (int)(t % g.nx), j = GH + (int)((t / g.nx) % g.ny), k = GH + (int)(t / ((long long)g.nx * g.ny));
-    const long long id = cidx(g, i, j, k);
-    R d = U[id], v1 = U[g.N + id], v2 = U[2 * g.N + id], v3 = U[3 * g.N + id], ei = U[4 * g.N + id];
+  for (unsigned t = gs_first(); t < n; t += gs_step()) {
+    int i, j, k;
+    interior_ijk(g, t, i, j, k);
+    const unsigned id = cidx32(g, i, j, k);
+    R d = U[id], v1 = U[N + id], v2 = U[2 * N + id], v3 = U[3 * N + id], ei = U[4 * N + id];
     R vabs = d_sqrt(v1 * v1 + v2 * v2 + v3 * v3);
     R ee = ei / d;
     sv = d_fmax(sv, vabs);
@@ -1297,19 +1306,20 @@ template <class R>
 __global__ void k_source_integrate(Consts c, R* __restrict__ U, const R* __restrict__ U0, R* __restrict__ Res,
                                    const Dyn* __restrict__ dyn, int stage) {
   const Geom& g = c.g;
-  const long long n = (long long)g.nx * g.ny * g.nz;
+  const unsigned n = (unsigned)g.nx * (unsigned)g.ny * (unsigned)g.nz, N = g.N32;
   const DynR<R>& dr = dynr<R>(dyn);
   const R wdt = dr.wdt[stage];
   const R invRdt = dr.invRdt;
   const R inv_va2max = dr.inv_va2max;
   const R vmax = dr.vmax;
   const R emax = dr.emax;
-  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
-    const int i = GH + (int)(t % g.nx), j = GH + (int)((t / g.nx) % g.ny), k = GH + (int)(t / ((long long)g.nx * g.ny));
-    const long long id = cidx(g, i, j, k);
+  for (unsigned t = gs_first(); t < n; t += gs_step()) {
+    int i, j, k;
+    interior_ijk(g, t, i, j, k);
+    const unsigned id = cidx32(g, i, j, k);
     R r[NV], u[NV];
 #pragma unroll
-    for (int v = 0; v < NV; v++) { r[v] = Res[(long long)v * g.N + id]; u[v] = U[(long long)v * g.N + id]; }
+    for (int v = 0; v < NV; v++) { r[v] = Res[(unsigned)v * N + id]; u[v] = U[(unsigned)v * N + id]; }
     R dn = invRdt * u[4];
     R efaci = dn / d_fmax(dn, (R)0.0);
     dn = kc<R>(c).gx * u[0] - (R)0.0;
@@ -1332,38 +1342,40 @@ __global__ void k_source_integrate(Consts c, R* __restrict__ U, const R* __restr
     R un[NV];
 #pragma unroll
     for (int v = 0; v < NV; v++) {
-      un[v] = U0[(long long)v * g.N + id] + wdt * r[v];
-      Res[(long long)v * g.N + id] = (R)0;
+      un[v] = U0[(unsigned)v * N + id] + wdt * r[v];
+      Res[(unsigned)v * N + id] = (R)0;
     }
     tcheck_cell<R>(c, vmax, emax, un[0], un[1], un[2], un[3], un[4]);
 #pragma unroll
-    for (int v = 0; v < NV; v++) U[(long long)v * g.N + id] = un[v];
+    for (int v = 0; v < NV; v++) U[(unsigned)v * N + id] = un[v];
   }
 }
 
 template <class R>
 __global__ void k_save_cons(Geom g, const R* __restrict__ U, R* __restrict__ U0) {
-  const long long n = (long long)g.nx * g.ny * g.nz;
-  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
-    const int i = GH + (int)(t % g.nx), j = GH + (int)((t / g.nx) % g.ny), k = GH + (int)(t / ((long long)g.nx * g.ny));
-    const long long id = cidx(g, i, j, k);
+  const unsigned n = (unsigned)g.nx * (unsigned)g.ny * (unsigned)g.nz, N = g.N32;
+  for (unsigned t = gs_first(); t < n; t += gs_step()) {
+    int i, j, k;
+    interior_ijk(g, t, i, j, k);
+    const unsigned id = cidx32(g, i, j, k);
 #pragma unroll
-    for (int v = 0; v < NV; v++) U0[(long long)v * g.N + id] = U[(long long)v * g.N + id];
+    for (int v = 0; v < NV; v++) U0[(unsigned)v * N + id] = U[(unsigned)v * N + id];
   }
 }
 
 template <class R>
 __global__ void k_tcheck(Consts c, R* __restrict__ U, const Dyn* __restrict__ dyn) {
   const Geom& g = c.g;
-  const long long n = (long long)g.nx * g.ny * g.nz;
+  const unsigned n = (unsigned)g.nx * (unsigned)g.ny * (unsigned)g.nz, N = g.N32;
   const R vmax = dynr<R>(dyn).vmax;
   const R emax = dynr<R>(dyn).emax;
-  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
-    const int i = GH + (int)(t % g.nx), j = GH + (int)((t / g.nx) % g.ny), k = GH + (int)(t / ((long long)g.nx * g.ny));
-    const long long id = cidx(g, i, j, k);
-    R d = U[id], m1 = U[g.N + id], m2 = U[2 * g.N + id], m3 = U[3 * g.N + id], e = U[4 * g.N + id];
+  for (unsigned t = gs_first(); t < n; t += gs_step()) {
+    int i, j, k;
+    interior_ijk(g, t, i, j, k);
+    const unsigned id = cidx32(g, i, j, k);
+    R d = U[id], m1 = U[N + id], m2 = U[2 * N + id], m3 = U[3 * N + id], e = U[4 * N + id];
     tcheck_cell<R>(c, vmax, emax, d, m1, m2, m3, e);
-    U[id] = d; U[g.N + id] = m1; U[2 * g.N + id] = m2; U[3 * g.N + id] = m3; U[4 * g.N + id] = e;
+    U[id] = d; U[N + id] = m1; U[2 * N + id] = m2; U[3 * N + id] = m3; U[4 * N + id] = e;
   }
 }
 
@@ -1390,8 +1402,10 @@ __global__ void k_tile_state(Geom gd, Geom gs, const R* __restrict__ Us, R* __re
 
 template <class R>
 __global__ void k_fill_ghosts(Geom g, R* __restrict__ U, int nfield, int with_bc) {
-  for (long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x; id < g.N; id += (long long)gridDim.x * blockDim.x) {
-    int i = (int)(id % g.sx), j = (int)((id / g.sx) % g.sy), k = (int)(id / ((long long)g.sx * g.sy));
+  const unsigned N = g.N32;
+  for (unsigned id = gs_first(); id < N; id += gs_step()) {
+    int i, j, k;
+    node_ijk(g, id, i, j, k);
     const bool gx = (i < GH || i >= GH + g.nx), gy = (j < GH || j >= GH + g.ny), gz = (k < GH || k >= GH + g.nz);
     if (!gx && !gy && !gz) continue;
     bool flip = false;
@@ -1402,11 +1416,11 @@ __global__ void k_fill_ghosts(Geom g, R* __restrict__ U, int nfield, int with_bc
     }
     if (gy) j = j < GH ? j + g.ny : j - g.ny;
     if (gz) k = k < GH ? k + g.nz : k - g.nz;
-    const long long src = cidx(g, i, j, k);
+    const unsigned src = cidx32(g, i, j, k);
     for (int v = 0; v < nfield; v++) {
-      R x = U[(long long)v * g.N + src];
+      R x = U[(unsigned)v * N + src];
       if (flip && (v == 1 || v == 6 || v == 7)) x = -x;
-      U[(long long)v * g.N + id] = x;
+      U[(unsigned)v * N + id] = x;
     }
   }
 }

@@ -109,10 +109,11 @@ __device__ __forceinline__ double temp_of(const Consts& c, double d, double ei) 
 template <class R>
 __global__ void __launch_bounds__(256) k_temp(Consts c, const R* __restrict__ U, R* __restrict__ T) {
   const Geom& g = c.g;
-  for (long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x; id < g.N; id += (long long)gridDim.x * blockDim.x) {
+  const unsigned N = g.N32;
+  for (unsigned id = gs_first(); id < N; id += gs_step()) {
     R v1, v2, v3, ei;
     const R d = U[id];
-    prim_from_cons(d, U[g.N + id], U[2 * g.N + id], U[3 * g.N + id], U[4 * g.N + id], v1, v2, v3, ei);
+    prim_from_cons(d, U[N + id], U[2 * N + id], U[3 * N + id], U[4 * N + id], v1, v2, v3, ei);
     T[id] = temp_of(c, d, ei);
   }
 }
@@ -232,9 +233,10 @@ __global__ void k_sflx_update(Consts c, R* __restrict__ S, const R* __restrict__
   const Geom& g = c.g;
   const R wdt = dynr<R>(dyn).wdt[stage];
   const long long n = (long long)g.nx * g.ny * g.nz;
-  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (long long)gridDim.x * blockDim.x) {
-    const int i = GH + (int)(t % g.nx), j = GH + (int)((t / g.nx) % g.ny), k = GH + (int)(t / ((long long)g.nx * g.ny));
-    const long long id = cidx(g, i, j, k);
+  for (unsigned t = gs_first(); t < (unsigned)n; t += gs_step()) {
+    int i, j, k;
+    interior_ijk(g, t, i, j, k);
+    const unsigned id = cidx32(g, i, j, k);
     S[id] = S0[id] + wdt * Rflx[id];
     Rflx[id] = (R)0;
   }

@@ -275,6 +275,7 @@ __global__ void __launch_bounds__(TX* TY, 2)
   const R invRdt = dr.invRdt;
   const R vmax = dr.vmax;
   const R emax = dr.emax;
+  R cm_acc = (R)0;  // residual mode: this thread's largest CFL speed
   R prim[NF];
   R fl[NF];
   prim[NPRIM] = (R)0;
@@ -426,9 +427,9 @@ __global__ void __launch_bounds__(TX* TY, 2)
       if (RESID) {
 #pragma unroll
         for (int q = 0; q < NV; q++) Res[id + (unsigned)q * g.N32] = Racc[q];
-        R cm = cmax_cell<R>(cen[P_D], cen[P_V1], cen[P_V2], cen[P_V3], cen[P_B1], cen[P_B2], cen[P_B3], cen[P_P],
-                            inv_va2max);
-        atomic_max_nonneg(&dyn->cmax_bits, (double)cm);
+        const R cm = cmax_cell<R>(cen[P_D], cen[P_V1], cen[P_V2], cen[P_V3], cen[P_B1], cen[P_B2], cen[P_B3],
+                                  cen[P_P], inv_va2max);
+        if (cm > cm_acc) cm_acc = cm;  // a NaN speed is skipped, as the atomic maximum skips it
       } else {
         // sources, Boris correction, update, Tcheck (src/Add_Sources_Integrate_SR.C:331-465)
         stage_sources<R>(Racc, cen, kk_.gx, inv_va2max, invRdt);
@@ -446,6 +447,10 @@ __global__ void __launch_bounds__(TX* TY, 2)
     __syncthreads();
   }
   if (pend) finish_pressure(ze - 1);
+  if (RESID) {  // one atomic per block
+    const R m = block_max_nonnan(cm_acc);
+    if (tid == 0) atomic_max_nonneg(&dyn->cmax_bits, (double)m);
+  }
 
   // teardown: report an expired wait, let issued copies land, free tensor memory
   if (timed_out) atomicExch(&misc[2], 1u);

@@ -173,6 +173,42 @@ def test_fused_fp32_error_vs_fp64_oracle(gpu_lib, kernel):
     assert np.all(e <= TOL32_L2), e
 
 
+def test_fp32_reference_order_steps_vs_fp64_oracle(gpu_lib):
+    """FP32 through the per-routine entry points (MURaM's drop-in use: ConsToPrim,
+    MHD_Residual, Source_Integrate_Tcheck, TVDlimit, ... in ComputeSolution's
+    order): relative L2 per field after 40 steps, the FP32 bar."""
+    tab = initial.EosTable(H.EOS_SMALL)
+    U = initial.periodic_box(tab, 32, 32, 32, seed=5)
+    ref, _ = _oracle_run(dict(nx=32, ny=32, nz=32), U, 40)
+    g = gpumhd.MuramGPU(gpumhd.default_params(32, 32, 32, 3.2e6, precision=32), eos_path=H.EOS_SMALL)
+    g.upload_state(U)
+    g.exchange_grid(True)
+    for _ in range(40):
+        g.step_reference_order()
+    e = H.rel_l2(H.interior(g.download_state()), H.interior(ref))
+    print("FP32 per-routine vs FP64 oracle rel L2 per field:", np.array2string(e, precision=2))
+    assert np.all(e <= TOL32_L2), e
+    g.close()
+
+
+def test_fp32_cons_to_prim_outputs(gpu_lib):
+    """ConsToPrim's five EOS outputs in FP32 (float table lookups) against the
+    FP64 routine on the reference fixture's state: the FP32 bar, relative L2
+    per field <= 1e-5 (measured 3.5e-8 for the pressure, 2.3e-6 for n_e,
+    whose logarithm varies fastest across the table cells)."""
+    d, hp = H.load_case("periodic")
+    out = {}
+    for prec in (64, 32):
+        g = ctx_for(hp, precision=prec)
+        g.upload_state(d["init_U"])
+        g.ConsToPrim()
+        out[prec] = np.stack([g.download_field(w) for w in range(gpumhd.FIELD_PRES, gpumhd.FIELD_AMB + 1)])
+        g.close()
+    e = H.rel_l2(out[32], out[64])
+    print("FP32 ConsToPrim pres/temp/ne/rhoi/amb rel L2:", np.array2string(e, precision=2))
+    assert np.all(e <= TOL32_L2), e
+
+
 def test_fp32_stage_kernels_agree_on_stratified_box(gpu_lib):
     """Closed x with gravity, partial tiles in every direction (36 x 20 x 12):
     the TMA / tensor-memory and the plain-load stage kernels give the same
