@@ -307,6 +307,23 @@ def run_ours(args):
                "ms_per_step": round(e2e_ms / e2e_steps, 3),
                "transfers": "asynchronous upload / download on copy streams, overlapping the neighbouring steps",
                "result_equals_synchronous_path": same}
+    # the per-routine entry points in ComputeSolution's order (how MURaM itself
+    # calls the library through the drop-in shim), device-resident
+    per_routine = None
+    if not args.no_e2e:
+        g.upload_state(U)
+        g.exchange_grid(True)
+        g.step_reference_order()
+        g.synchronize()
+        t0 = time.perf_counter()
+        pr_steps = 3
+        for _ in range(pr_steps):
+            g.step_reference_order()
+        g.synchronize()
+        pr_ms = (time.perf_counter() - t0) * 1e3 / pr_steps
+        per_routine = {"value": ws * n_cells / (pr_ms / 1e3), "unit": UNIT, "ms_per_step": round(pr_ms, 3),
+                       "steps": pr_steps, "calls": "SaveCons, 4 x (ConsToPrim, MHD_Residual, Source_Integrate_Tcheck, "
+                       "exchange), TVDlimit, TCheck, exchange; host-timed, one host round trip per MHD_Residual"}
     g.close()
     del g
     # FP64 mode of the same box: throughput over --err-steps steps from the
@@ -361,6 +378,7 @@ def run_ours(args):
         "step_hbm_gbs": round(step_bytes / (step_ms / 1e3) / 1e9, 1),
         "phases_ms": {k: round(v, 4) for k, v in phases.items()},
         "e2e": e2e,
+        "per_routine": per_routine,
         "gpu_launches": launches,
         "clocks": clocks.summary(),
         "fp64": fp64,
