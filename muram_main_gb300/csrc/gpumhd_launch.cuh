@@ -109,13 +109,25 @@ cudaError_t Launch<R>::setup() {
   if (e != cudaSuccess) return e;
   resident_stage_blocks = (per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
   constexpr int MX = StageTileTm<R>::TX, MY = StageTileTm<R>::TY;
-  const int tb = (int)StageTm<R, MX, MY>::BYTES;
-  e = cudaFuncSetAttribute(k_stage_tm<R, MX, MY, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, tb);
+  const int tb = (int)StageTm<R, MX, MY, false>::BYTES;
+  e = cudaFuncSetAttribute(k_stage_tm<R, MX, MY, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, tb);
   if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(k_stage_tm<R, MX, MY, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, tb);
+  e = cudaFuncSetAttribute(k_stage_tm<R, MX, MY, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, tb);
   if (e != cudaSuccess) return e;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_stage_tm<R, MX, MY, false>, MX * MY, tb);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_stage_tm<R, MX, MY, false, false>, MX * MY, tb);
   if (e != cudaSuccess) return e;
+  int per_sm_db = per_sm;
+  if constexpr (sizeof(R) == 4) {
+    const int tdb = (int)StageTm<R, MX, MY, true>::BYTES;
+    e = cudaFuncSetAttribute(k_stage_tm<R, MX, MY, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, tdb);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(k_stage_tm<R, MX, MY, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, tdb);
+    if (e != cudaSuccess) return e;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_db, k_stage_tm<R, MX, MY, false, true>, MX * MY, tdb);
+    if (e != cudaSuccess) return e;
+  }
+  // the z chunking assumes the smaller residency of the two layouts
+  per_sm = per_sm_db < per_sm ? per_sm_db : per_sm;
   resident_tm_blocks = (per_sm > 0 ? per_sm : 1) * (sms > 0 ? sms : 1);
   return cudaSuccess;
 }
@@ -149,13 +161,26 @@ void Launch<R>::stage(const Consts& c, const R* Uin, const R* Pin, const R* U0, 
   dim3 grid(bx, by, bz);
   if (tma) {
     constexpr int MX = StageTileTm<R>::TX, MY = StageTileTm<R>::TY;
-    const int bytes = (int)StageTm<R, MX, MY>::BYTES;
-    if (resid)
-      k_stage_tm<R, MX, MY, true><<<grid, MX * MY, bytes, s>>>(*mu, *mp, c, Uin, U0, Uout, Pout, Res, dyn, stage,
-                                                               zc, write_pres, nullptr);
-    else
-      k_stage_tm<R, MX, MY, false><<<grid, MX * MY, bytes, s>>>(*mu, *mp, c, Uin, U0, Uout, Pout, Res, dyn, stage,
-                                                                zc, write_pres, Cc);
+    // FP32: the double-buffered layout for the residual and for stages 1
+    // and 4 (no separate U0 stream), the four-slot one for stages 2 and 3
+    bool db = false;
+    if constexpr (sizeof(R) == 4) db = resid || stage == 1 || stage == 4;
+    auto go = [&](auto dbt) {
+      constexpr bool DB = decltype(dbt)::value;
+      const int bytes = (int)StageTm<R, MX, MY, DB>::BYTES;
+      if (resid)
+        k_stage_tm<R, MX, MY, true, DB><<<grid, MX * MY, bytes, s>>>(*mu, *mp, c, Uin, U0, Uout, Pout, Res, dyn,
+                                                                     stage, zc, write_pres, nullptr);
+      else
+        k_stage_tm<R, MX, MY, false, DB><<<grid, MX * MY, bytes, s>>>(*mu, *mp, c, Uin, U0, Uout, Pout, Res, dyn,
+                                                                      stage, zc, write_pres, Cc);
+    };
+    if constexpr (sizeof(R) == 4) {
+      if (db) go(std::true_type());
+      else go(std::false_type());
+    } else {
+      go(std::false_type());
+    }
     return;
   }
   constexpr int PX = StageTile<R>::TX, PY = StageTile<R>::TY;

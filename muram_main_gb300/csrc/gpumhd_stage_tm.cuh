@@ -115,18 +115,30 @@ __device__ __forceinline__ void tmem_wait_ld16(unsigned* r) {
 }  // namespace tm
 
 // Shared-memory layout of one k_stage_tm block.
-template <class R, int TX, int TY>
+template <class R, int TX, int TY, bool DB_>
 struct StageTm {
   static constexpr int BX = TX + 4, BY = TY + 4;  // TMA box of one plane (x, y)
   static constexpr int BOXN = BX * BY;
   static constexpr unsigned UB = (unsigned)(sizeof(R) * BOXN * NV);  // state box bytes ([v][y][x])
   static constexpr unsigned PB = (unsigned)(sizeof(R) * BOXN);       // pressure box bytes, right after
   static constexpr size_t TILE = ((size_t)UB + PB + 127) / 128 * 128;
-  static constexpr int NSLOT = 4;
+  // DB: three plane slots and two x / y flux buffers used in turn, so that
+  // one barrier per plane suffices (the next plane's fluxes go to the other
+  // buffer; a slot is refilled right after the barrier of the plane that
+  // last reads it).  Otherwise four slots and one flux buffer, two barriers
+  // per plane.  Two blocks per SM fit either way in FP32; FP64 uses the
+  // latter only.  Measured at 128 x 384 x 384 (FP32): DB is faster for the
+  // stages that read no separate U0 (stage 1: 0.76 against 0.79 ms; stage 4,
+  // whose U0 is its output, 0.62 against 0.67 ms; the residual), slower for
+  // stages 2 and 3 (0.80 against 0.78 ms), whose U0 loads and EOS gathers
+  // then have less L1 beside the larger shared memory.
+  static constexpr bool DB = DB_;
+  static constexpr int NSLOT = DB ? 3 : 4;
+  static constexpr int NFB = DB ? 2 : 1;
   static constexpr int FXN = BX * TY, FYN = TX * BY;
-  static constexpr size_t OFF_FX = NSLOT * TILE;
-  static constexpr size_t OFF_FY = OFF_FX + sizeof(R) * 12 * FXN;
-  static constexpr size_t OFF_BAR = OFF_FY + sizeof(R) * 12 * FYN;
+  static constexpr size_t FSET = sizeof(R) * 12 * (FXN + FYN);  // one x + y flux buffer pair
+  static constexpr size_t OFF_FX = NSLOT * TILE;                  // set b: x at OFF_FX + b * FSET, y after it
+  static constexpr size_t OFF_BAR = OFF_FX + NFB * FSET;
   static constexpr size_t OFF_MISC = OFF_BAR + 8 * NSLOT;  // TMEM address, flags
   static constexpr size_t BYTES = OFF_MISC + 16 + 128;     // + alignment slack
   // tensor memory: per thread 5 slots x 12 quantities (32-bit columns)
@@ -207,21 +219,21 @@ __device__ __forceinline__ void tm_deriv12(double* Dq, unsigned m2, unsigned m1,
 // tensor (x, y, z, variable), box (TX+4, TY+4, 1, 8); mapP: its pressure,
 // box (TX+4, TY+4, 1); Ug: the same state as a pointer (read for the
 // resistive terms only).  Other arguments as k_stage.
-template <class R, int TX, int TY, bool RESID>
+template <class R, int TX, int TY, bool RESID, bool DB>
 __global__ void __launch_bounds__(TX* TY, 2)
     k_stage_tm(const __grid_constant__ CUtensorMap mapU, const __grid_constant__ CUtensorMap mapP, Consts c,
                const R* __restrict__ Ug, const R* __restrict__ U0, R* __restrict__ Uout, R* __restrict__ Pout,
                R* __restrict__ Res,
                Dyn* __restrict__ dyn, int stage, int zc, int write_pres, R* __restrict__ Cc) {
-  using L = StageTm<R, TX, TY>;
+  using L = StageTm<R, TX, TY, DB>;
+  static_assert(!DB || sizeof(R) == 4, "the double-buffered layout is for FP32");
   constexpr int CW = CellW<R>::W;
   constexpr int NT = TX * TY;
   constexpr int NH = 4 * TY + 4 * TX;
   static_assert(NH <= NT, "every halo cell needs a thread");
   extern __shared__ unsigned char smem_raw[];
   unsigned char* sm = smem_raw + ((128u - (tm::su32(smem_raw) & 127u)) & 127u);
-  R* FX = reinterpret_cast<R*>(sm + L::OFF_FX);
-  R* FY = reinterpret_cast<R*>(sm + L::OFF_FY);
+  auto fx_of = [&](int b) { return reinterpret_cast<R*>(sm + L::OFF_FX + (size_t)b * L::FSET); };
   unsigned long long* bar = reinterpret_cast<unsigned long long*>(sm + L::OFF_BAR);
   unsigned* misc = reinterpret_cast<unsigned*>(sm + L::OFF_MISC);  // [0] TMEM base, [1] skip, [2] timeout
   const Geom& g = c.g;
@@ -281,11 +293,11 @@ __global__ void __launch_bounds__(TX* TY, 2)
   prim[NPRIM] = (R)0;
   fl[NPRIM] = (R)0;
 
-  // plane tiles: plane p is tile t = p - (zb - 2), slot t % 4, phase (t / 4) % 2
+  // plane tiles: plane p is tile t = p - (zb - 2), slot t % NSLOT, phase (t / NSLOT) % 2
   const int p_first = zb - 2;
-  auto tile = [&](int p) { return reinterpret_cast<const R*>(sm + (size_t)((p - p_first) & 3) * L::TILE); };
+  auto tile = [&](int p) { return reinterpret_cast<const R*>(sm + (size_t)((p - p_first) % L::NSLOT) * L::TILE); };
   auto issue = [&](int p) {  // one thread
-    const int t = p - p_first, sl = t & 3;
+    const int t = p - p_first, sl = t % L::NSLOT;
     unsigned char* dst = sm + (size_t)sl * L::TILE;
     tm::fence_proxy_async();
     tm::mbar_arrive_expect_tx(&bar[sl], L::UB + L::PB);
@@ -295,7 +307,7 @@ __global__ void __launch_bounds__(TX* TY, 2)
   bool timed_out = false;
   auto wait_tile = [&](int p) {
     const int t = p - p_first;
-    if (!tm::mbar_wait(&bar[t & 3], (unsigned)((t >> 2) & 1))) timed_out = true;
+    if (!tm::mbar_wait(&bar[t % L::NSLOT], (unsigned)((t / L::NSLOT) & 1))) timed_out = true;
   };
   // cell offsets inside a tile: own cell and halo cell
   const int o_own = (ty + 2) * L::BX + (tx + 2);
@@ -309,8 +321,13 @@ __global__ void __launch_bounds__(TX* TY, 2)
   auto slot_add = [](int sl, int d) { return sl + d >= 5 ? sl + d - 5 : sl + d; };
 
   if (tid == 0)
-    for (int p = zb - 2; p < zb + 2; p++) issue(p);
+    for (int p = zb - 2; p < zb - 2 + L::NSLOT; p++) issue(p);
   for (int p = zb - 2; p < zb + 2; p++) {
+    if (L::DB && p == zb + 1) {  // the fourth prologue plane takes the first plane's slot
+      tm::tmem_wait_st();
+      __syncthreads();
+      if (tid == 0) issue(p);
+    }
     wait_tile(p);
     __syncwarp();
     Raw9<R> r;
@@ -337,7 +354,9 @@ __global__ void __launch_bounds__(TX* TY, 2)
   };
   int s0 = 2;  // ring slot of plane k
   for (int k = zb; k < ze; k++, s0 = slot_add(s0, 1)) {
-    if (tid == 0 && k + 1 < ze) issue(k + 3);
+    if (!L::DB && tid == 0 && k + 1 < ze) issue(k + 3);
+    R* const FX = fx_of(L::DB ? ((k - zb) & 1) : 0);
+    R* const FY = FX + 12 * L::FXN;
     // z flux of plane k+2 (all lanes: tensor-memory stores are warp-wide)
     wait_tile(k + 2);
     __syncwarp();
@@ -382,6 +401,9 @@ __global__ void __launch_bounds__(TX* TY, 2)
     if (pend) finish_pressure(k - 1);
     tm::tmem_wait_st();
     __syncthreads();
+    // FP32: plane k's slot is free (its last reads were this plane's own and
+    // halo cells), refill it with plane k+3, read in the next plane
+    if (L::DB && tid == 0 && k + 1 < ze) issue(k + 3);
     // z derivative (all lanes), then the cell's residual and update
     R Dz[NF];
     __syncwarp();
@@ -444,7 +466,7 @@ __global__ void __launch_bounds__(TX* TY, 2)
         }
       }
     }
-    __syncthreads();
+    if (!L::DB) __syncthreads();  // FP64: the flux buffer is rewritten by the next plane
   }
   if (pend) finish_pressure(ze - 1);
   if (RESID) {  // one atomic per block
@@ -459,11 +481,11 @@ __global__ void __launch_bounds__(TX* TY, 2)
   if (misc[2]) {
     if (tid == 0) {
       atomicExch(&dyn->err, (int)ERR_WAIT_TIMEOUT);
-      // the last four tiles issued are the only ones that can be in flight
+      // the last NSLOT tiles issued are the only ones that can be in flight
       const int p_last = max(ze + 1, zb + 2);
-      for (int p = max(p_first, p_last - 3); p <= p_last; p++) {
+      for (int p = max(p_first, p_last - (L::NSLOT - 1)); p <= p_last; p++) {
         const int t = p - p_first;
-        tm::mbar_wait(&bar[t & 3], (unsigned)((t >> 2) & 1));
+        tm::mbar_wait(&bar[t % L::NSLOT], (unsigned)((t / L::NSLOT) & 1));
       }
     }
     __syncthreads();
