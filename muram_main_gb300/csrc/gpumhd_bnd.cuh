@@ -56,12 +56,35 @@ __device__ __forceinline__ double bnd_fwd(const Consts& c, const float* T, doubl
   return wr0 * we0 * (double)T[(i + 1) * L + j + 1] + wr0 * we1 * (double)T[i * L + j + 1] +
          wr1 * we0 * (double)T[(i + 1) * L + j] + wr1 * we1 * (double)T[i * L + j];
 }
+// The same two lookups as bnd_fwd on two tables (ln p and s + ss_off) at one
+// (ee, dd): logs, cell and weights formed once, each sum as bnd_fwd's.
+__device__ __forceinline__ void bnd_fwd2(const Consts& c, const float* T1, const float* T2, double ee, double dd,
+                                         double& o1, double& o2) {
+  const BndK<double>& b = c.bndd;
+  const double ee1 = log(ee + b.eps_off);
+  const double logr = log(dd);
+  int i = cvt_x86((ee1 - b.eps0) * b.inv_del_eps);
+  if (i < 0) i = 0;
+  if (i > c.N_eps - 2) i = c.N_eps - 2;
+  int j = cvt_x86((logr - b.lr0) * b.inv_del_lr);
+  if (j < 0) j = 0;
+  if (j > c.N_lr - 2) j = c.N_lr - 2;
+  double we0, we1, wr0, wr1;
+  bnd_w(ee1, b.eps0, b.del_eps, i, we0, we1);
+  bnd_w(logr, b.lr0, b.del_lr, j, wr0, wr1);
+  const long long L = c.N_lr;
+  o1 = wr0 * we0 * (double)T1[(i + 1) * L + j + 1] + wr0 * we1 * (double)T1[i * L + j + 1] +
+       wr1 * we0 * (double)T1[(i + 1) * L + j] + wr1 * we1 * (double)T1[i * L + j];
+  o2 = wr0 * we0 * (double)T2[(i + 1) * L + j + 1] + wr0 * we1 * (double)T2[i * L + j + 1] +
+       wr1 * we0 * (double)T2[(i + 1) * L + j] + wr1 * we1 * (double)T2[i * L + j];
+}
 __device__ __forceinline__ double bnd_p(const Consts& c, double ee, double dd) { return exp(bnd_fwd(c, c.tab[0], ee, dd)); }
 __device__ __forceinline__ double bnd_s(const Consts& c, double ee, double dd) {
   return bnd_fwd(c, c.tab[2], ee, dd) - c.bndd.ss_off;
 }
-// d3_interp / eps3_interp (src/eos_init.C:216-266): ln rho or ln(eps + eps_off)
-__device__ __forceinline__ double bnd_inv(const Consts& c, const float* T, double pp, double ss) {
+// d3_interp and eps3_interp (src/eos_init.C:216-266) at one (pp, ss): ln rho
+// and ln(eps + eps_off), the log, cell and weights formed once for both.
+__device__ __forceinline__ void bnd_inv2(const Consts& c, double pp, double ss, double& lrho, double& leps) {
   const BndK<double>& b = c.bndd;
   const double ss1 = ss + b.ss_off;
   const double logp = log(pp);
@@ -75,8 +98,12 @@ __device__ __forceinline__ double bnd_inv(const Consts& c, const float* T, doubl
   bnd_w(logp, b.lp30, b.del_lp3, i, wp0, wp1);
   bnd_w(ss1, b.s30, b.del_s3, j, ws0, ws1);
   const long long L = c.N_s3;
-  return wp0 * ws0 * (double)T[(i + 1) * L + j + 1] + wp0 * ws1 * (double)T[(i + 1) * L + j] +
-         wp1 * ws0 * (double)T[i * L + j + 1] + wp1 * ws1 * (double)T[i * L + j];
+  const float* D = c.d3;
+  const float* E = c.eps3;
+  lrho = wp0 * ws0 * (double)D[(i + 1) * L + j + 1] + wp0 * ws1 * (double)D[(i + 1) * L + j] +
+         wp1 * ws0 * (double)D[i * L + j + 1] + wp1 * ws1 * (double)D[i * L + j];
+  leps = wp0 * ws0 * (double)E[(i + 1) * L + j + 1] + wp0 * ws1 * (double)E[(i + 1) * L + j] +
+         wp1 * ws0 * (double)E[i * L + j + 1] + wp1 * ws1 * (double)E[i * L + j];
 }
 
 // Per block of 32 (y) x 4 (z) interior columns: sums over the first two
@@ -184,13 +211,16 @@ __global__ void __launch_bounds__(BND_THREADS) k_bc_ghosts(Consts c, R* __restri
       u2[4] -= 0.5 * (u2[1] * u2[1] + u2[2] * u2[2] + u2[3] * u2[3]) / u2[0];
       double eps1 = u1[4] / u1[0], eps2 = u2[4] / u2[0];
       const double pmag = 0.5 * u1[5] * u1[5];
-      const double pmin1 = bnd_p(c, eps1, u1[0]) - pmean1;
+      // p_interp and s_interp of the first layer share their logs and weights
+      double lnp1, ss1;
+      bnd_fwd2(c, c.tab[0], c.tab[2], eps1, u1[0], lnp1, ss1);
+      const double pmin1 = exp(lnp1) - pmean1;
       double s1, s2;
       if (u1[1] >= 0.e0) {
         s1 = s_bc;
         s2 = s_bc;
       } else {
-        s1 = bnd_s(c, eps1, u1[0]);
+        s1 = ss1 - c.bndd.ss_off;
         s2 = bnd_s(c, eps2, u2[0]);
       }
       double cc = p_bc / sqrt(pmean1 * pmean2);
@@ -201,16 +231,19 @@ __global__ void __launch_bounds__(BND_THREADS) k_bc_ghosts(Consts c, R* __restri
       p1 -= pmag * (1.0 - p1_dmp);
       p2 -= pmag * (1.0 - p1_dmp * p1_dmp);
       cc = u1[5] / b.bcrit;
-      cc = pow(cc, 4);
+      cc = (cc * cc) * (cc * cc);  // pow(cc, 4) to the last bit or two
       cc = (1.0 - cc) / (1.0 + cc);
 #pragma unroll
       for (int v = 1; v <= 3; v++) {
         u1[v] *= cc;
         u2[v] *= cc;
       }
-      const double rho1 = exp(bnd_inv(c, c.d3, p1, s1)), rho2 = exp(bnd_inv(c, c.d3, p2, s2));
-      eps1 = exp(bnd_inv(c, c.eps3, p1, s1)) - b.eps_off;
-      eps2 = exp(bnd_inv(c, c.eps3, p2, s2)) - b.eps_off;
+      double lr1, le1, lr2, le2;
+      bnd_inv2(c, p1, s1, lr1, le1);
+      bnd_inv2(c, p2, s2, lr2, le2);
+      const double rho1 = exp(lr1), rho2 = exp(lr2);
+      eps1 = exp(le1) - b.eps_off;
+      eps2 = exp(le2) - b.eps_off;
       u1[0] = rho1;
       u2[0] = rho2;
       u1[4] = eps1 * rho1 + 0.5 * (u1[1] * u1[1] + u1[2] * u1[2] + u1[3] * u1[3]) / u1[0];
