@@ -1004,8 +1004,14 @@ __global__ void __launch_bounds__(FIN_BX* FIN_BY, FinBlocks<R>::v) k_step_finish
   acc.flush(dyn);
 }
 
+// Resident blocks of 128 threads the TVD sweeps are compiled for (FP32; FP64
+// keeps the compiler's register choice).  Measured at 128 x 384 x 384: y / z
+// sweeps 0.496 / 0.489 -> 0.490 / 0.482 ms with 4 blocks (128 registers, a
+// few spilled), the x sweep 0.623 -> 0.603 ms with 6 (85 registers).
+template <class R> struct TvdBlocks { static constexpr int pencil = sizeof(R) == 4 ? 4 : 1, lanes = sizeof(R) == 4 ? 6 : 1; };
+
 template <class R, int DIR>
-__global__ void __launch_bounds__(128) k_tvd_sweep(Consts c, const R* __restrict__ Uin, const R* __restrict__ Pst,
+__global__ void __launch_bounds__(128, TvdBlocks<R>::pencil) k_tvd_sweep(Consts c, const R* __restrict__ Uin, const R* __restrict__ Pst,
                                                    R* __restrict__ Uout, Dyn* __restrict__ dyn, TvdArgs ta) {
   const Geom& g = c.g;
   if (dyn->err) return;
@@ -1103,7 +1109,7 @@ template <class R>
 __device__ __forceinline__ R shfl(R v, int src) { return __shfl_sync(0xffffffffu, v, src); }
 
 template <class R>
-__global__ void __launch_bounds__(128) k_tvd_sweep_xlanes(Consts c, const R* __restrict__ Uin, const R* __restrict__ Pst,
+__global__ void __launch_bounds__(128, TvdBlocks<R>::lanes) k_tvd_sweep_xlanes(Consts c, const R* __restrict__ Uin, const R* __restrict__ Pst,
                                                           R* __restrict__ Uout, Dyn* __restrict__ dyn, int only_two_half) {
   const Geom& g = c.g;
   if (dyn->err) return;
