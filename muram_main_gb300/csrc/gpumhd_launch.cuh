@@ -162,9 +162,12 @@ void Launch<R>::stage(const Consts& c, const R* Uin, const R* Pin, const R* U0, 
   if (tma) {
     constexpr int MX = StageTileTm<R>::TX, MY = StageTileTm<R>::TY;
     // FP32: the double-buffered layout for the residual and for stages 1
-    // and 4 (no separate U0 stream), the four-slot one for stages 2 and 3
+    // and 4 (no separate U0 stream), the four-slot one for stages 2 and 3.
+    // With three slots a block's first planes wait for their tiles twice
+    // (the fourth prologue plane and the first output plane), so short z
+    // chunks (small boxes, ensembles) keep the four-slot layout.
     bool db = false;
-    if constexpr (sizeof(R) == 4) db = resid || stage == 1 || stage == 4;
+    if constexpr (sizeof(R) == 4) db = (resid || stage == 1 || stage == 4) && zc >= 16;
     auto go = [&](auto dbt) {
       constexpr bool DB = decltype(dbt)::value;
       const int bytes = (int)StageTm<R, MX, MY, DB>::BYTES;

@@ -98,6 +98,30 @@ def test_explicit_tuning_gives_same_results(gpu_lib):
     ref.close()
 
 
+@pytest.mark.parametrize("closed", [False, True])
+def test_fp32_stage_layouts_agree(gpu_lib, closed):
+    """FP32 stage kernel: on z chunks of 16 planes or more, stages 1 and 4 and
+    the residual take the three-slot, double-buffered layout (one barrier per
+    plane); on shorter chunks every stage takes the four-slot layout.  Same
+    per-cell arithmetic, so the states agree to the FMA contractions of the
+    two compiled instances; so do the per-routine residual and its dt."""
+    runs = []
+    for zc in (48, 8):
+        g = _box(64, 32, 48, 32, 7, closed=closed)
+        g.set_tuning(zc, 0)
+        g.run_steps(6)
+        U = g.download_state()
+        g.ConsToPrim()
+        g.Adjust_Valf_Max()
+        dt = g.MHD_Residual()
+        runs.append((U, dt, g.download_state(gpumhd.FIELD_RES)))
+        g.close()
+    (ua, dta, ra), (ub, dtb, rb) = runs
+    assert np.all(H.rel_linf(ua, ub) <= 1e-6), H.rel_linf(ua, ub)
+    assert abs(dta / dtb - 1) <= 1e-6
+    assert np.all(H.rel_linf(ra, rb) <= 1e-5), H.rel_linf(ra, rb)
+
+
 def test_tile_from_commutes_with_the_step(gpu_lib):
     """A periodic box tiled 2 x 3 x 2 and advanced equals the advanced small
     box tiled the same way (the periodic step treats every copy alike)."""
