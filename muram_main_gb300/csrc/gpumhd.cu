@@ -34,6 +34,8 @@ struct gpumhd_ctx {
   // buffers per direction (used in turn), ordered against the context's
   // stream by events (created on first use)
   cudaStream_t s_in = nullptr, s_out = nullptr;
+  cudaStream_t s_cond = nullptr;              // captures the bodies of conditional graph nodes
+  bool cond_tvd2 = false;                     // the captured step holds the second TVD pass in a conditional node
   double* astage_in[2] = {nullptr, nullptr};  // 8N doubles each
   double* astage_out[2] = {nullptr, nullptr};
   cudaEvent_t ev_in_ready[2] = {}, ev_in_free[2] = {}, ev_out_ready[2] = {}, ev_out_free[2] = {};
@@ -431,6 +433,7 @@ extern "C" int gpumhd_create(const gpumhd_params* p, int device, gpumhd_ctx** ou
   int rc = GPUMHD_OK;
   do {
     if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) { rc = GPUMHD_E_CUDA; break; }
+    if (cudaStreamCreateWithFlags(&ctx->s_cond, cudaStreamNonBlocking) != cudaSuccess) { rc = GPUMHD_E_CUDA; break; }
     e = ctx->f32 ? Launch<float>::setup() : Launch<double>::setup();
     if (e != cudaSuccess) { rc = fail(ctx, GPUMHD_E_CUDA, "kernel setup: %s", cudaGetErrorString(e)); break; }
     rc = fill_consts(ctx);
@@ -493,6 +496,7 @@ extern "C" int gpumhd_destroy(gpumhd_ctx* ctx) {
   }
   if (ctx->s_in) cudaStreamDestroy(ctx->s_in);
   if (ctx->s_out) cudaStreamDestroy(ctx->s_out);
+  if (ctx->s_cond) cudaStreamDestroy(ctx->s_cond);
   cudaFree(ctx->comp);
   cudaFree(ctx->phi);
   cudaFree(ctx->divb);
@@ -1195,6 +1199,36 @@ static int step_launches(const gpumhd_ctx* ctx) {
   if (ctx->c.has_spitzer) n += 4 * 2;  // temperature and heat flux before each stage
   return n;
 }
+// Kernels one replay of the captured step always launches: the second TVD
+// half pass sits in a conditional node (k_step_begin counts it when taken).
+static int graph_step_launches(const gpumhd_ctx* ctx) { return step_launches(ctx) - (ctx->cond_tvd2 ? 3 : 0); }
+
+// During a capture on the context's stream: an IF node, controlled by handle
+// h, after the work captured so far; body(q) enqueues its contents on stream q.
+template <class F>
+static int capture_if(gpumhd_ctx* ctx, cudaGraphConditionalHandle h, F body) {
+  cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+  cudaGraph_t cg = nullptr;
+  const cudaGraphNode_t* deps = nullptr;
+  const cudaGraphEdgeData* ed = nullptr;
+  size_t nd = 0;
+  CK(cudaStreamGetCaptureInfo(ctx->stream, &st, nullptr, &cg, &deps, &ed, &nd));
+  if (st != cudaStreamCaptureStatusActive || !cg) return fail(ctx, GPUMHD_E_CUDA, "conditional node outside a capture");
+  cudaGraphNodeParams np = {};
+  np.type = cudaGraphNodeTypeConditional;
+  np.conditional.handle = h;
+  np.conditional.type = cudaGraphCondTypeIf;
+  np.conditional.size = 1;
+  cudaGraphNode_t node;
+  CK(cudaGraphAddNode(&node, cg, deps, ed, nd, &np));
+  CK(cudaStreamBeginCaptureToGraph(ctx->s_cond, np.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                   cudaStreamCaptureModeThreadLocal));
+  body(ctx->s_cond);
+  cudaGraph_t bg = nullptr;
+  CK(cudaStreamEndCapture(ctx->s_cond, &bg));
+  CK(cudaStreamUpdateCaptureDependencies(ctx->stream, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+  return GPUMHD_OK;
+}
 
 // One fused step: step control, four RK stages, two TVD passes (the second
 // returns at once unless the step takes two half passes), Clean_divB when it
@@ -1211,8 +1245,23 @@ static int enqueue_one_step(gpumhd_ctx* ctx, cudaEvent_t* ev = nullptr) {
   const int pa = ctx->iP, pb = 1 - ctx->iP;
   const bool xb = c.xbnd != 0;
   const bool sp = c.has_spitzer != 0;
+  // Under stream capture the second TVD half pass (which most steps skip)
+  // becomes an IF node that k_step_begin switches on only for steps that take
+  // it; launched directly, its kernels return at once when not taken.
+  cudaGraphConditionalHandle tvd2 = 0;
+  bool cond = false;
+  {
+    cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+    cudaGraph_t cg = nullptr;
+    if (cudaStreamGetCaptureInfo(s, &st, nullptr, &cg, nullptr, nullptr, nullptr) == cudaSuccess &&
+        st == cudaStreamCaptureStatusActive && cg) {
+      if (cudaGraphConditionalHandleCreate(&tvd2, cg, 0, cudaGraphCondAssignDefault) == cudaSuccess) cond = true;
+      else cudaGetLastError();
+    }
+  }
+  ctx->cond_tvd2 = cond;
   mark();
-  k_step_begin<<<1, 32, 0, s>>>(c, ctx->dyn, ctx->dt_hist, ctx->dt_hist_cap);
+  k_step_begin<<<1, 32, 0, s>>>(c, ctx->dyn, ctx->dt_hist, ctx->dt_hist_cap, tvd2, cond ? 1 : 0);
   if (ctx->f32) {
     using L = Launch<float>;
     // Spitzer conduction before each stage: temperature, then the heat flux's
@@ -1256,12 +1305,21 @@ static int enqueue_one_step(gpumhd_ctx* ctx, cudaEvent_t* ev = nullptr) {
     L::tvd(c, 1, 0, 0, S[d], P[pb], S[b], ctx->dyn, s, ctx->tune_td);
     mark();
     L::tvd(c, 2, 1, 0, S[b], P[pb], S[a], ctx->dyn, s, ctx->tune_td);
-    mark();
-    L::tvd(c, 0, 0, 1, S[a], P[pb], S[d], ctx->dyn, s, ctx->tune_td);
-    mark();
-    L::tvd(c, 1, 0, 1, S[d], P[pb], S[b], ctx->dyn, s, ctx->tune_td);
-    mark();
-    L::tvd(c, 2, 2, 1, S[b], P[pb], S[a], ctx->dyn, s, ctx->tune_td);
+    if (cond) {
+      const int rc2 = capture_if(ctx, tvd2, [&](cudaStream_t q) {
+        L::tvd(c, 0, 0, 1, S[a], P[pb], S[d], ctx->dyn, q, ctx->tune_td);
+        L::tvd(c, 1, 0, 1, S[d], P[pb], S[b], ctx->dyn, q, ctx->tune_td);
+        L::tvd(c, 2, 2, 1, S[b], P[pb], S[a], ctx->dyn, q, ctx->tune_td);
+      });
+      if (rc2) return rc2;
+    } else {
+      mark();
+      L::tvd(c, 0, 0, 1, S[a], P[pb], S[d], ctx->dyn, s, ctx->tune_td);
+      mark();
+      L::tvd(c, 1, 0, 1, S[d], P[pb], S[b], ctx->dyn, s, ctx->tune_td);
+      mark();
+      L::tvd(c, 2, 2, 1, S[b], P[pb], S[a], ctx->dyn, s, ctx->tune_td);
+    }
     mark();
     if (c.divb_on) L::divb_clean(c, S[a], (float*)ctx->phi, (float*)ctx->divb, ctx->dyn, s);
     mark();
@@ -1313,12 +1371,21 @@ static int enqueue_one_step(gpumhd_ctx* ctx, cudaEvent_t* ev = nullptr) {
     L::tvd(c, 1, 0, 0, S[d], P[pb], S[b], ctx->dyn, s, ctx->tune_td);
     mark();
     L::tvd(c, 2, 1, 0, S[b], P[pb], S[a], ctx->dyn, s, ctx->tune_td);
-    mark();
-    L::tvd(c, 0, 0, 1, S[a], P[pb], S[d], ctx->dyn, s, ctx->tune_td);
-    mark();
-    L::tvd(c, 1, 0, 1, S[d], P[pb], S[b], ctx->dyn, s, ctx->tune_td);
-    mark();
-    L::tvd(c, 2, 2, 1, S[b], P[pb], S[a], ctx->dyn, s, ctx->tune_td);
+    if (cond) {
+      const int rc2 = capture_if(ctx, tvd2, [&](cudaStream_t q) {
+        L::tvd(c, 0, 0, 1, S[a], P[pb], S[d], ctx->dyn, q, ctx->tune_td);
+        L::tvd(c, 1, 0, 1, S[d], P[pb], S[b], ctx->dyn, q, ctx->tune_td);
+        L::tvd(c, 2, 2, 1, S[b], P[pb], S[a], ctx->dyn, q, ctx->tune_td);
+      });
+      if (rc2) return rc2;
+    } else {
+      mark();
+      L::tvd(c, 0, 0, 1, S[a], P[pb], S[d], ctx->dyn, s, ctx->tune_td);
+      mark();
+      L::tvd(c, 1, 0, 1, S[d], P[pb], S[b], ctx->dyn, s, ctx->tune_td);
+      mark();
+      L::tvd(c, 2, 2, 1, S[b], P[pb], S[a], ctx->dyn, s, ctx->tune_td);
+    }
     mark();
     if (c.divb_on) L::divb_clean(c, S[a], (double*)ctx->phi, (double*)ctx->divb, ctx->dyn, s);
     mark();
@@ -1411,7 +1478,7 @@ extern "C" int gpumhd_enqueue_steps(gpumhd_ctx* ctx, int nsteps) {
   for (int s = 0; s < nsteps; s++) {
     if (ctx->graph) {
       CK(cudaGraphLaunch(ctx->graph, ctx->stream));
-      ctx->launches += step_launches(ctx);
+      ctx->launches += graph_step_launches(ctx);
     } else {
       rc = enqueue_one_step(ctx);
       if (rc) return rc;
@@ -1512,7 +1579,16 @@ extern "C" int gpumhd_step_info(gpumhd_ctx* ctx, double* dt, double* cfl, double
 }
 
 extern "C" void* gpumhd_stream(gpumhd_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
-extern "C" long long gpumhd_launch_count(gpumhd_ctx* ctx) { return ctx ? ctx->launches : 0; }
+// After gpumhd_synchronize: the host-counted launches plus those the device
+// enabled in captured steps' conditional nodes.
+extern "C" long long gpumhd_launch_count(gpumhd_ctx* ctx) {
+  if (!ctx) return 0;
+  unsigned long long cl = 0;
+  if (cudaSetDevice(ctx->device) != cudaSuccess ||
+      cudaMemcpy(&cl, &ctx->dyn->cond_launches, sizeof cl, cudaMemcpyDeviceToHost) != cudaSuccess)
+    cl = 0;
+  return ctx->launches + (long long)cl;
+}
 
 // ------------------------------------------------------------- launch shapes
 extern "C" int gpumhd_set_tuning(gpumhd_ctx* ctx, int stage_zchunk, int tvd_chunk) {
@@ -1760,10 +1836,10 @@ extern "C" int gpumhd_ensemble_enqueue_steps(gpumhd_ensemble* e, int nsteps) {
   for (gpumhd_ctx* x : e->box) {
     ECK(cudaMemsetAsync(x->S[x->iRes], 0, 8 * x->c.g.N * x->rsz, e->stream));
     x->have_pres = true;
-    x->launches += (long long)step_launches(x) * nsteps;
+    x->launches += (long long)graph_step_launches(x) * nsteps;
   }
   long long per_step = 1;
-  for (gpumhd_ctx* x : e->box) per_step += step_launches(x);
+  for (gpumhd_ctx* x : e->box) per_step += graph_step_launches(x);
   e->launches += per_step * nsteps + 1;
   ECK(cudaEventRecord(e->done, e->stream));
   for (gpumhd_ctx* x : e->box) ECK(cudaStreamWaitEvent(x->stream, e->done, 0));
@@ -1863,7 +1939,7 @@ extern "C" int gpumhd_adjoint(gpumhd_ctx* ctx, int nsteps, int checkpoint_every,
   using L = Launch<double>;
   // one recorded forward step: (A, Q0) -> (An, Qn), intermediates kept
   auto record = [&]() {
-    k_step_begin<<<1, 32, 0, s>>>(c, adyn, nullptr, 0);
+    k_step_begin<<<1, 32, 0, s>>>(c, adyn, nullptr, 0, 0, 0);
     L::stage(c, A, Q0, A, B1, Q1, nullptr, adyn, 1, false, 1, s);
     L::stage(c, B1, Q1, A, B2, Q2, nullptr, adyn, 2, false, 1, s);
     L::stage(c, B2, Q2, A, B3, Q3, nullptr, adyn, 3, false, 1, s);

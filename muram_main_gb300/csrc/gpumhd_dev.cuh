@@ -162,6 +162,9 @@ struct Dyn {
   double p_bc, s_bc, pmean1, pmean2;
   int bnd_ini, bnd_pad;
   double dt_prev;       // the previous step's dt (Spitzer relaxation caps at stage 1)
+  // kernels a captured step launched through its conditional nodes (the
+  // second TVD half pass), counted by k_step_begin when it enables them
+  unsigned long long cond_launches;
 };
 
 template <class R> __device__ __forceinline__ const DynR<R>& dynr(const Dyn* d);

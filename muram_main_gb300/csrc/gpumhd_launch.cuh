@@ -11,7 +11,10 @@ namespace gpumhd {
 // Step control for the fused path (one thread): the Adjust_Valf_Max limits,
 // Sync_timestep (src/solver.C:487-548) on the CFL speed accumulated by the
 // previous pass, the TVD branch (src/solver.C:325-339) and Run.Advance.
-__global__ void k_step_begin(Consts c, Dyn* dyn, double* dt_hist, int dt_hist_cap);
+// With use_cond (a captured step) it also sets the conditional node of the
+// second TVD half pass (tvd2) from the branch it chose.
+__global__ void k_step_begin(Consts c, Dyn* dyn, double* dt_hist, int dt_hist_cap, cudaGraphConditionalHandle tvd2,
+                             int use_cond);
 // Step counter of a graph's while loop: k_set_counter before the launch,
 // k_loop_tick at the end of each pass (sets the loop condition).
 __global__ void k_loop_tick(int* counter, cudaGraphConditionalHandle h);

@@ -7,8 +7,20 @@ namespace gpumhd {
 
 template struct Launch<double>;
 
-__global__ void k_step_begin(Consts c, Dyn* dyn, double* dt_hist, int dt_hist_cap) {
+__device__ __forceinline__ void step_begin(const Consts& c, Dyn* dyn, double* dt_hist, int dt_hist_cap);
+
+__global__ void k_step_begin(Consts c, Dyn* dyn, double* dt_hist, int dt_hist_cap, cudaGraphConditionalHandle tvd2,
+                             int use_cond) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  step_begin(c, dyn, dt_hist, dt_hist_cap);
+  if (use_cond) {  // the captured step's second TVD half pass runs only when this step takes it
+    const bool take = !dyn->err && dyn->two_half;
+    if (take) dyn->cond_launches += 3ULL;
+    cudaGraphSetConditional(tvd2, take ? 1u : 0u);
+  }
+}
+
+__device__ __forceinline__ void step_begin(const Consts& c, Dyn* dyn, double* dt_hist, int dt_hist_cap) {
   if (dyn->err) return;
   // Adjust_Valf_Max without va_adjust (src/Adjust_Valf_Max.C:136-142); the
   // fused path runs only in that mode, so the limits are the run constants.

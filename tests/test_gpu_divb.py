@@ -178,7 +178,7 @@ def test_ensemble_with_cleaning(gpu_lib):
     boxes = [box(nx, ny, nz, on, 60 + q) for q, (nx, ny, nz, on) in enumerate(shapes)]
     ens = gpumhd.MuramEnsemble(boxes)
     ens.run_steps(4)
-    per_step = 1 + sum(12 + (3 + 2 * 4 if on else 0) for *_, on in shapes)
+    per_step = 1 + sum(9 + (3 + 2 * 4 if on else 0) for *_, on in shapes)  # second TVD pass: conditional
     assert ens.launch_count == per_step * 4 + 1
     for ref, g in zip(alone, boxes):
         assert np.array_equal(g.download_state(), ref)

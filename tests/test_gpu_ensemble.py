@@ -40,7 +40,9 @@ def test_ensemble_equals_boxes_run_one_by_one(gpu_lib):
     ens = gpumhd.MuramEnsemble(boxes)
     ens.run_steps(steps // 2)
     ens.run_steps(steps - steps // 2)  # a second launch continues the loop
-    assert ens.launch_count == (12 * len(boxes) + 1) * steps + 2
+    # 9 kernels per box and step always run; the second TVD half pass (3 more)
+    # sits in a conditional node that these steps do not take
+    assert ens.launch_count == (9 * len(boxes) + 1) * steps + 2
     for (ref, info), g in zip(alone, boxes):
         got = g.download_state()
         assert np.array_equal(got, ref), np.max(np.abs(got - ref))
