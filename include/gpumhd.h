@@ -209,7 +209,9 @@ int gpumhd_cfl_dt_noalloc(const double* U_prim, const double* pres, int nx, int 
                           double inv_va2max, void* stream, double* dt_out);
 /* The CUDA stream the context enqueues on (a cudaStream_t). */
 void* gpumhd_stream(gpumhd_ctx* ctx);
-/* Number of kernel launches the context has enqueued so far. */
+/* Number of kernels the context has launched so far: those it enqueued plus
+ * those that captured steps ran through their conditional nodes (the second
+ * TVD half pass); exact after gpumhd_synchronize. */
 long long gpumhd_launch_count(gpumhd_ctx* ctx);
 
 /* Benchmark / test set-up, no counterpart in the reference: the state of ctx
