@@ -267,6 +267,7 @@ static int fill_consts(gpumhd_ctx* ctx) {
   }
   c.rt_cfl = p.rt_cfl;
   c.CFL = p.CFL; c.CFL_tvd = p.CFL_tvd; c.dt_rad = p.dt_rad; c.rt_tstep = p.rt_tstep; c.outcad = p.outcad;
+  c.spt_cfl_dx = (1.8 < c.CFL ? 1.8 : c.CFL) * c.dxmin;  // smin(CFL, CFL_hyp) * dxmin
   c.va_max = p.va_max; c.va_adjust = p.va_adjust; c.max_fill = p.max_fill;
   c.autostep = p.autostep;
   // vertical boundary profiles of TVDlimit (src/tvdlimit_SR.C:132-149)
@@ -337,8 +338,8 @@ static void adjust_limits(gpumhd_ctx* ctx, const double st[5]) {
 
 static int push_dyn(gpumhd_ctx* ctx) {
   const Consts& c = ctx->c;
-  derive_one<float>(ctx->hdyn, c.dx, c.idx, c.rt_cfl, c.tchk_vmax, c.tchk_eps_max, ctx->hdyn.rf);
-  derive_one<double>(ctx->hdyn, c.dx, c.idx, c.rt_cfl, c.tchk_vmax, c.tchk_eps_max, ctx->hdyn.rd);
+  derive_one<float>(ctx->hdyn, c.dx, c.idx, c.rt_cfl, c.tchk_vmax, c.tchk_eps_max, ctx->hdyn.rf, c.spt_cfl_dx);
+  derive_one<double>(ctx->hdyn, c.dx, c.idx, c.rt_cfl, c.tchk_vmax, c.tchk_eps_max, ctx->hdyn.rd, c.spt_cfl_dx);
   CK(cudaMemcpyAsync(ctx->dyn, &ctx->hdyn, sizeof(Dyn), cudaMemcpyHostToDevice, ctx->stream));
   return GPUMHD_OK;
 }

@@ -99,6 +99,7 @@ struct Consts {
   // hyperbolic Spitzer conduction: coefficient (0: off), saturation flux
   // factor (1+X_H) Rgas^1.5 sqrt(1836)/8 (src/mhdres_SR.C:40-46)
   double spitzer, spt_sat_flx;
+  double spt_cfl_dx;  // min(CFL, 1.8) * dxmin, the hyperbolic speed cap's numerator (src/mhdres_SR.C:137-145)
   int has_spitzer, pad_spt;
   const void* spt_rsp;  // the energy residual's Spitzer share for this stage (N, state precision)
   double rt_cfl;
@@ -133,6 +134,9 @@ struct DynR {
   R inv_va2max, vsqr_diff;
   R vmax, emax, vlim95, elim95;      // Tcheck limits, Adjust_Valf_Max thresholds
   R wdt[5], invRdt;                  // dt/(5-stage), rt_cfl/dt (src/Add_Sources_Integrate_SR.C:44, 85)
+  // Spitzer relaxation caps (src/mhdres_SR.C:137-145) for [0] the previous
+  // step's dt (stage 1 of a fused step) and [1] the current dt
+  R spt_cmax[2], spt_numax[2], spt_hyp[2];
 };
 
 // Values that change during a run; live in device memory.
@@ -175,7 +179,8 @@ enum { ERR_BAD_DT_RAD = 1, ERR_BAD_DT_MHD = 2, ERR_CFL = 3 };
 
 template <class R>
 __host__ __device__ inline void derive_one(const Dyn& d, const double dx[3], const double idx[3], double rt_cfl,
-                                           double tchk_vmax, double tchk_eps_max, DynR<R>& r) {
+                                           double tchk_vmax, double tchk_eps_max, DynR<R>& r,
+                                           double spt_cfl_dx = 0.0) {
   r.dt_tvd = (R)d.dt_tvd;
   for (int q = 0; q < 3; q++) {
     r.cmax_t[q] = (R)(0.975 * dx[q] / d.dt_tvd);
@@ -190,6 +195,23 @@ __host__ __device__ inline void derive_one(const Dyn& d, const double dx[3], con
   r.wdt[0] = (R)0;
   for (int st = 1; st <= 4; st++) r.wdt[st] = (R)(d.dt / (double)(4 + 1 - st));
   r.invRdt = (R)(rt_cfl / d.dt);
+  // spt_cfl_dx = min(CFL, CFL_hyp = 1.8) * dxmin
+  for (int q = 0; q < 2; q++) {
+    const double dth = q == 0 ? d.dt_prev : d.dt;
+    double cm, nu, hy;
+    if (dth > 0.0) {
+      cm = spt_cfl_dx / dth;
+      nu = 0.25 / dth;
+      hy = 0.02 / dth;
+    } else {
+      cm = 0.0;
+      nu = 0.25 * cm / spt_cfl_dx;
+      hy = 0.02 * cm / spt_cfl_dx;
+    }
+    r.spt_cmax[q] = (R)cm;
+    r.spt_numax[q] = (R)nu;
+    r.spt_hyp[q] = (R)hy;
+  }
 }
 
 // ---------------------------------------------------------------- helpers

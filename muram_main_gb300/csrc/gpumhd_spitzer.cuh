@@ -140,20 +140,12 @@ __global__ void __launch_bounds__(SPT_BX* SPT_BY) k_spitzer(Consts c, const R* _
   if (i >= GH + g.nx || j >= GH + g.ny) return;
   const int k0 = GH + blockIdx.z * zc;
   const int k1 = min(k0 + zc, GH + g.nz);
-  // the relaxation's caps from the time step (src/mhdres_SR.C:137-145)
-  const double dt_h = (stage == 1) ? dyn->dt_prev : dyn->dt;
-  const double CFL_hyp = 1.8, avr_max = 0.25, eps_hyp = 0.02;
-  double cmax_hyp_d, nu_hyp_max_d, hyp_diff_d;
-  if (dt_h > 0.0) {
-    cmax_hyp_d = smin(c.CFL, CFL_hyp) * c.dxmin / dt_h;
-    nu_hyp_max_d = avr_max / dt_h;
-    hyp_diff_d = eps_hyp / dt_h;
-  } else {
-    cmax_hyp_d = 0.0;
-    nu_hyp_max_d = avr_max * cmax_hyp_d / (smin(c.CFL, CFL_hyp) * c.dxmin);
-    hyp_diff_d = eps_hyp * cmax_hyp_d / (smin(c.CFL, CFL_hyp) * c.dxmin);
-  }
-  const R cmax_hyp = (R)cmax_hyp_d, nu_hyp_max = (R)nu_hyp_max_d, hyp_diff = (R)hyp_diff_d;
+  // the relaxation's caps from the time step (src/mhdres_SR.C:137-145),
+  // derived once per step with the step scalars: stage 1 of a fused step
+  // takes the previous step's dt, everything else the current one
+  const int qd = (stage == 1) ? 0 : 1;
+  const DynR<R>& drr = dynr<R>(dyn);
+  const R cmax_hyp = drr.spt_cmax[qd], nu_hyp_max = drr.spt_numax[qd], hyp_diff = drr.spt_hyp[qd];
   const R k0s = (R)c.spitzer, sat_flx = (R)c.spt_sat_flx;
   const R wdt = dynr<R>(dyn).wdt[stage > 0 ? stage : 0];
   const auto& kk = kc<R>(c);

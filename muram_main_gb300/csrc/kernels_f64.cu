@@ -55,8 +55,8 @@ __device__ __forceinline__ void step_begin(const Consts& c, Dyn* dyn, double* dt
   if (dt_hist && dyn->steps_done >= 0 && dyn->steps_done < dt_hist_cap) dt_hist[dyn->steps_done] = dyn->dt;
   dyn->steps_done += 1;
   dyn->time += dyn->dt;
-  derive_one<float>(*dyn, c.dx, c.idx, c.rt_cfl, c.tchk_vmax, c.tchk_eps_max, dyn->rf);
-  derive_one<double>(*dyn, c.dx, c.idx, c.rt_cfl, c.tchk_vmax, c.tchk_eps_max, dyn->rd);
+  derive_one<float>(*dyn, c.dx, c.idx, c.rt_cfl, c.tchk_vmax, c.tchk_eps_max, dyn->rf, c.spt_cfl_dx);
+  derive_one<double>(*dyn, c.dx, c.idx, c.rt_cfl, c.tchk_vmax, c.tchk_eps_max, dyn->rd, c.spt_cfl_dx);
   // the last TVD pass of this step accumulates the next step's values
   dyn->cmax_bits = 0ULL;
   dyn->stat_max_bits[0] = dyn->stat_max_bits[1] = dyn->stat_max_bits[2] = 0ULL;
@@ -90,8 +90,8 @@ __global__ void k_fused_reinit(Consts c, Dyn* dyn, double inv_va2max, double v_l
   dyn->cmax_bits = 0ULL;
   dyn->stat_max_bits[0] = dyn->stat_max_bits[1] = dyn->stat_max_bits[2] = 0ULL;
   dyn->stat_cnt[0] = dyn->stat_cnt[1] = 0ULL;
-  derive_one<float>(*dyn, c.dx, c.idx, c.rt_cfl, c.tchk_vmax, c.tchk_eps_max, dyn->rf);
-  derive_one<double>(*dyn, c.dx, c.idx, c.rt_cfl, c.tchk_vmax, c.tchk_eps_max, dyn->rd);
+  derive_one<float>(*dyn, c.dx, c.idx, c.rt_cfl, c.tchk_vmax, c.tchk_eps_max, dyn->rf, c.spt_cfl_dx);
+  derive_one<double>(*dyn, c.dx, c.idx, c.rt_cfl, c.tchk_vmax, c.tchk_eps_max, dyn->rd, c.spt_cfl_dx);
 }
 
 __global__ void k_divb_begin(Dyn* dyn) {
