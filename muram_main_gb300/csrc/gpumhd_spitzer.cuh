@@ -107,7 +107,7 @@ __device__ __forceinline__ double temp_of(const Consts& c, double d, double ei) 
 
 // Temperature of every cell, ghosts included, of a conserved state.
 template <class R>
-__global__ void __launch_bounds__(256) k_temp(Consts c, const R* __restrict__ U, R* __restrict__ T) {
+__global__ void __launch_bounds__(256, EwBlocks<R>::v) k_temp(Consts c, const R* __restrict__ U, R* __restrict__ T) {
   const Geom& g = c.g;
   const unsigned N = g.N32;
   for (unsigned id = gs_first(); id < N; id += gs_step()) {
