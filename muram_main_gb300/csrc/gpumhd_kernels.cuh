@@ -1176,8 +1176,10 @@ __global__ void __launch_bounds__(128, TvdBlocks<R>::lanes) k_tvd_sweep_xlanes(C
 
 // ---------------------------------------------------------- small kernels
 // ConsToPrim over the whole box (src/cons_to_prim.C:78-266).  FP32: compiled
-// for 6 resident blocks of 256 (at most 42 registers): 0.71 -> 0.52 ms at
-// 19.9 M nodes, the EOS gathers' latency hidden by more warps.
+// for 6 resident blocks of 256 (at most 42 registers; the spills are in the
+// FP64 fallback of cells outside the table): 0.71 -> 0.52 ms at 19.9 M nodes,
+// the EOS gathers' latency hidden by more warps.  The same bound serves the
+// temperature and Source_Integrate kernels (0.97 -> 0.75 ms).
 template <class R> struct EwBlocks { static constexpr int v = sizeof(R) == 4 ? 6 : 1; };
 template <class R>
 __global__ void __launch_bounds__(256, EwBlocks<R>::v) k_cons_to_prim(Consts c, R* __restrict__ U, R* __restrict__ P, R* __restrict__ T, R* __restrict__ Ne,
@@ -1312,7 +1314,7 @@ __global__ void k_cmax_faces(Consts c, const R* __restrict__ U, const R* __restr
 
 // Source_Integrate_Tcheck (src/Add_Sources_Integrate_SR.C:297-467) on a primitive U.
 template <class R>
-__global__ void k_source_integrate(Consts c, R* __restrict__ U, const R* __restrict__ U0, R* __restrict__ Res,
+__global__ void __launch_bounds__(256, EwBlocks<R>::v) k_source_integrate(Consts c, R* __restrict__ U, const R* __restrict__ U0, R* __restrict__ Res,
                                    const Dyn* __restrict__ dyn, int stage) {
   const Geom& g = c.g;
   const unsigned n = (unsigned)g.nx * (unsigned)g.ny * (unsigned)g.nz, N = g.N32;
