@@ -310,6 +310,9 @@ def run_ours(args):
                 "kernel": f"k_stage (FP32, RK stages 1-4)" if dom == "stage" else "k_tvd_sweep (FP32, x/y/z)",
                 "algorithmic_bytes_per_launch": bytes_per_launch, "mean_launch_ms": round(mean_ms, 4),
                 "peak_source": f"{peak_src} hbm_gbs"}
+    if dom == "stage":
+        roofline["limiter"] = ("instruction issue and dependency latency, not HBM (ncu: ~58 % issue active, "
+                               "24-39 % DRAM throughput; profiles/mhd_step_fp32_stratified_128x384x384.md)")
     # whole-step bytes against HBM
     step_bytes = sum(words_per_cell(p) for p in fam["stage"] + fam["tvd"] + ["finish"]) * 4 * n_cells
     step_ms = ms / args.steps
