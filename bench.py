@@ -312,7 +312,7 @@ def run_ours(args):
                 "peak_source": f"{peak_src} hbm_gbs"}
     if dom == "stage":
         roofline["limiter"] = ("instruction issue and dependency latency, not HBM (ncu: ~58 % issue active, "
-                               "24-39 % DRAM throughput; profiles/mhd_step_fp32_stratified_128x384x384.md)")
+                               "24-39 % DRAM throughput)")
     # whole-step bytes against HBM
     step_bytes = sum(words_per_cell(p) for p in fam["stage"] + fam["tvd"] + ["finish"]) * 4 * n_cells
     step_ms = ms / args.steps

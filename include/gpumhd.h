@@ -173,7 +173,11 @@ int gpumhd_exchange(gpumhd_ctx* ctx, int with_bc);
 /* Fused path: advance `nsteps` full time steps (SaveCons, 4 RK stages,
  * Sync_timestep, TVD, TCheck, boundaries; src/solver.C:109-365) entirely on
  * the device.  Equivalent to the per-routine calls above on U in conserved
- * form with filled ghosts.  dt_out (may be NULL) receives dt of each step.
+ * form with filled ghosts.  With adaptive limits (va_adjust > 0) each step
+ * also updates the limits on the device from the previous pass's statistics
+ * and takes the stage-1 CFL speed in one more pass; the limits' history (the
+ * reference's function statics) carries over between per-routine and fused
+ * calls.  dt_out (may be NULL) receives dt of each step.
  * With capture = 1 the step sequence is recorded once as a CUDA graph and
  * replayed. */
 int gpumhd_run_steps(gpumhd_ctx* ctx, int nsteps, double* dt_out, int capture);
@@ -200,11 +204,18 @@ int gpumhd_profile_steps(gpumhd_ctx* ctx, int nsteps, double* ms_phase);
  * ConsToPrim leaves them (8 fields of (nx+4)(ny+4)(nz+4) doubles, x fastest),
  * pres the pressure; dx[3] and inv_va2max are host values; dt_out is a device
  * double the result is written to, in stream order on `stream` (a
- * cudaStream_t, NULL for the default stream).  Scratch: a fixed 32 KiB
- * __device__ array, one partial per z plane, so nz + 4 must not exceed 4096
- * (GPUMHD_E_INVALID otherwise).  The first call on each device looks up that
- * array's device address; make it before any stream capture.  All calls share
- * the array: calls that overlap on the GPU race. */
+ * cudaStream_t, NULL for the default stream).  The result is the CFL term
+ * only: MHD_Residual also takes min(dt, dt_diff_fac/eta) when resistivity is
+ * on (src/mhdres_SR.C:815-819), so a resistive run takes that minimum itself.
+ * The speeds are those of MHD_Residual's pencils: interior cells and face
+ * ghosts (one index in a ghost layer), not edge or corner ghosts.
+ * Scratch: a fixed 32 KiB __device__ array, one partial per z plane, so
+ * nz + 4 must not exceed 4096 (GPUMHD_E_INVALID otherwise).  The first call
+ * on each device looks up that array's device address and keeps it for the
+ * life of the process; make it before any stream capture, and do not call
+ * the function again after a cudaDeviceReset (the library may then sit at
+ * another address).  All calls share the array: calls that overlap on the
+ * GPU race. */
 int gpumhd_cfl_dt_noalloc(const double* U_prim, const double* pres, int nx, int ny, int nz, const double dx[3],
                           double inv_va2max, void* stream, double* dt_out);
 /* The CUDA stream the context enqueues on (a cudaStream_t). */
@@ -224,6 +235,16 @@ int gpumhd_tile_from(gpumhd_ctx* ctx, gpumhd_ctx* src);
  * occupancy); tvd_chunk: cells per thread of the y / z TVD sweeps (0: 32).
  * Results do not depend on them. */
 int gpumhd_set_tuning(gpumhd_ctx* ctx, int stage_zchunk, int tvd_chunk);
+/* Test hook of the TMA stage kernel's bounded waits (no counterpart in the
+ * reference; for testing the error path only).  wait_cycles limits each wait
+ * for a plane's copy in SM clock cycles (0: the default, about one second);
+ * withhold_last = 1 makes every block of the kernel skip the copy of the last
+ * plane it needs, so that its wait for that plane runs out: the block records
+ * ERR_WAIT_TIMEOUT, waits for the copies it did issue, frees its tensor memory
+ * and returns; the rest of the step returns at once, and gpumhd_synchronize
+ * (or MHD_Residual) reports GPUMHD_E_CUDA.  Drops the captured step graph;
+ * ensembles built before keep their launch parameters. */
+int gpumhd_test_tma_wait(gpumhd_ctx* ctx, long long wait_cycles, int withhold_last);
 /* stage_kernel: 0 when the TMA / tensor-memory stage kernel runs, 1 for the
  * plain-load kernel. */
 int gpumhd_get_tuning(gpumhd_ctx* ctx, int* stage_kernel, int* stage_zchunk, int* tvd_chunk);
@@ -237,9 +258,9 @@ int gpumhd_autotune(gpumhd_ctx* ctx, int trial_steps, double* best_ms);
  * Gradient of an objective J(U_T) with respect to the initial state U_0, where
  * U_0 is the context's current state and U_T the state after nsteps fused
  * steps of fixed dt (FP64 context, periodic box, autostep = 0, dt > 0, one TVD
- * pass per step).  dJ_dUT: dJ/dU_T in the host cState layout (8 doubles per
- * cell, ghosts included and ignored); dJ_dU0 receives dJ/dU_0 in the same
- * layout (ghost records zero).  The hand-written adjoint of the step (stages
+ * pass per step, fixed limits: va_adjust = 0).  dJ_dUT: dJ/dU_T in the host
+ * cState layout (8 doubles per cell, ghosts included and ignored); dJ_dU0
+ * receives dJ/dU_0 in the same layout (ghost records zero).  The hand-written adjoint of the step (stages
  * with MHD_Residual, sources, Boris correction and Tcheck, ConsToPrim's
  * pressure, the three TVD sweeps) runs backwards in time; forward states are
  * kept every checkpoint_every steps and recomputed in between.  Limiter kinks

@@ -67,6 +67,9 @@ struct gpumhd_ctx {
   CUtensorMap mapP[2];
   // launch shapes of the fused step (0: defaults); set by gpumhd_set_tuning / gpumhd_autotune
   int tune_zc = 0, tune_td = 0;
+  // test hook of the TMA stage kernel's bounded waits (gpumhd_test_tma_wait)
+  int tm_withhold_last = 0;
+  long long tm_wait_cycles = 0;
   void* comp = nullptr;  // FP32 compensated mode: per-cell remainders of the RK update (8N floats)
   void* phi = nullptr;   // divB cleaning potential (GridData::phi, N), persists between calls
   void* divb = nullptr;  // last divergence of B (GridData::divB, N)
@@ -205,6 +208,8 @@ static int fill_consts(gpumhd_ctx* ctx) {
   g.N = (long long)g.sx * g.sy * g.sz;
   g.N32 = (unsigned)g.N;
   g.periodic_x = p.periodic_x ? 1 : 0;
+  c.tm_withhold_last = ctx->tm_withhold_last;
+  c.tm_wait_cycles = ctx->tm_wait_cycles;
   g.xmirror = (!p.periodic_x && p.xbnd == 0) ? 1 : 0;
   c.xbnd = (!p.periodic_x && p.xbnd == 1) ? 1 : 0;
   c.bnd_top = p.bnd_top;
@@ -1019,6 +1024,11 @@ extern "C" int gpumhd_mhd_residual(gpumhd_ctx* ctx, double* dt_mhd) {
   if (rc) return rc;
   rc = pull_dyn(ctx);
   if (rc) return rc;
+  if (ctx->hdyn.err == ERR_WAIT_TIMEOUT) {  // the residual is incomplete; report it once
+    ctx->hdyn.err = 0;
+    push_dyn(ctx);
+    return fail(ctx, GPUMHD_E_CUDA, "a device-side wait for a TMA copy timed out");
+  }
   const double cmax = bits_to_double(ctx->hdyn.cmax_bits);
   if (dt_mhd) {
     double dt = ctx->c.dxmin / cmax;
@@ -1198,6 +1208,7 @@ static int step_launches(const gpumhd_ctx* ctx) {
   if (ctx->c.divb_on) n += 3 + 2 * (ctx->c.divb_itmax > 3 ? ctx->c.divb_itmax : 3);
   if (ctx->c.xbnd) n += 5 * 3;  // the boundaries after each stage and at the end of the step
   if (ctx->c.has_spitzer) n += 4 * 2;  // temperature and heat flux before each stage
+  if (ctx->c.va_adjust > 0.0) n += ctx->c.xbnd ? 3 : 2;  // adaptive limits, then the CFL speed with them
   return n;
 }
 // Kernels one replay of the captured step always launches: the second TVD
@@ -1262,6 +1273,18 @@ static int enqueue_one_step(gpumhd_ctx* ctx, cudaEvent_t* ev = nullptr) {
   }
   ctx->cond_tvd2 = cond;
   mark();
+  if (c.va_adjust > 0.0) {
+    // Adjust_Valf_Max with adaptive limits, then the stage-1 CFL speed under
+    // the new inv_va2max (interior, and the physical boundaries' face ghosts)
+    k_step_limits<<<1, 32, 0, s>>>(c, ctx->dyn);
+    if (ctx->f32) {
+      Launch<float>::cfl_cons(c, (const float*)ctx->S[ctx->iU], (const float*)ctx->P[ctx->iP], ctx->dyn, s);
+      if (c.xbnd) Launch<float>::cmax_faces(c, (const float*)ctx->S[ctx->iU], (const float*)ctx->P[ctx->iP], ctx->dyn, s);
+    } else {
+      Launch<double>::cfl_cons(c, (const double*)ctx->S[ctx->iU], (const double*)ctx->P[ctx->iP], ctx->dyn, s);
+      if (c.xbnd) Launch<double>::cmax_faces(c, (const double*)ctx->S[ctx->iU], (const double*)ctx->P[ctx->iP], ctx->dyn, s);
+    }
+  }
   k_step_begin<<<1, 32, 0, s>>>(c, ctx->dyn, ctx->dt_hist, ctx->dt_hist_cap, tvd2, cond ? 1 : 0);
   if (ctx->f32) {
     using L = Launch<float>;
@@ -1403,8 +1426,6 @@ static int enqueue_one_step(gpumhd_ctx* ctx, cudaEvent_t* ev = nullptr) {
 
 static int fused_prepare(gpumhd_ctx* ctx, int nsteps) {
   if (!ctx->eos_loaded) return fail(ctx, GPUMHD_E_ORDER, "time steps before eos_init");
-  if (ctx->p.va_adjust > 0.0)
-    return fail(ctx, GPUMHD_E_INVALID, "the fused step supports va_adjust = 0; use the per-routine calls");
   if (nsteps > ctx->dt_hist_cap) {
     if (ctx->graph) { cudaGraphExecDestroy(ctx->graph); ctx->graph = nullptr; }
     cudaFree(ctx->dt_hist);
@@ -1434,13 +1455,17 @@ static int fused_prepare(gpumhd_ctx* ctx, int nsteps) {
     // than a host round trip of Dyn: no host synchronisation and no small
     // copy queued behind large asynchronous transfers.  The host mirror gets
     // the same values (its other fields are refreshed by the next pull).
+    // With adaptive limits (va_adjust > 0) the limits and their history stay
+    // as the device holds them: k_step_limits updates them at every step.
     Dyn& d = ctx->hdyn;
-    d.va_ini_flag = 0;
-    d.inv_va2max = 1.0 / pow(ctx->p.va_max, 2);
-    d.v_lim = ctx->p.tchk[3];
-    d.e_lim = ctx->p.tchk[2];
-    const double vml = ctx->p.tvd[8];
-    d.vsqr_diff = vml < 1.0 ? pow(vml * d.v_lim, 2.0) : pow(vml, 2.0);
+    if (!(ctx->p.va_adjust > 0.0)) {
+      d.va_ini_flag = 0;
+      d.inv_va2max = 1.0 / pow(ctx->p.va_max, 2);
+      d.v_lim = ctx->p.tchk[3];
+      d.e_lim = ctx->p.tchk[2];
+      const double vml = ctx->p.tvd[8];
+      d.vsqr_diff = vml < 1.0 ? pow(vml * d.v_lim, 2.0) : pow(vml, 2.0);
+    }
     d.err = 0;
     d.cmax_bits = 0;
     d.stat_max_bits[0] = d.stat_max_bits[1] = d.stat_max_bits[2] = 0;
@@ -1592,6 +1617,19 @@ extern "C" long long gpumhd_launch_count(gpumhd_ctx* ctx) {
 }
 
 // ------------------------------------------------------------- launch shapes
+extern "C" int gpumhd_test_tma_wait(gpumhd_ctx* ctx, long long wait_cycles, int withhold_last) {
+  if (!ctx || wait_cycles < 0) return GPUMHD_E_INVALID;
+  ctx->tm_wait_cycles = wait_cycles;
+  ctx->tm_withhold_last = withhold_last ? 1 : 0;
+  ctx->c.tm_wait_cycles = ctx->tm_wait_cycles;
+  ctx->c.tm_withhold_last = ctx->tm_withhold_last;
+  if (ctx->graph) {  // the captured step holds the old launch parameters
+    cudaGraphExecDestroy(ctx->graph);
+    ctx->graph = nullptr;
+  }
+  return GPUMHD_OK;
+}
+
 extern "C" int gpumhd_set_tuning(gpumhd_ctx* ctx, int stage_zchunk, int tvd_chunk) {
   if (!ctx || stage_zchunk < 0 || tvd_chunk < 0 || tvd_chunk > 1024) return GPUMHD_E_INVALID;
   ctx->tune_zc = stage_zchunk;
@@ -1904,6 +1942,7 @@ extern "C" int gpumhd_adjoint(gpumhd_ctx* ctx, int nsteps, int checkpoint_every,
   if (ctx->c.has_eta) return fail(ctx, GPUMHD_E_INVALID, "adjoint: ideal MHD only (eta = 0)");
   if (ctx->c.divb_on) return fail(ctx, GPUMHD_E_INVALID, "adjoint: without divB cleaning (divB_switch = 0)");
   if (ctx->c.has_spitzer) return fail(ctx, GPUMHD_E_INVALID, "adjoint: without Spitzer conduction (spitzer = 0)");
+  if (ctx->c.va_adjust > 0.0) return fail(ctx, GPUMHD_E_INVALID, "adjoint: with fixed limits (va_adjust = 0)");
   CK(cudaSetDevice(ctx->device));
   int rc = fused_prepare(ctx, nsteps);
   if (rc) return rc;

@@ -106,7 +106,11 @@ struct Consts {
   double CFL, CFL_tvd, dt_rad, rt_tstep, outcad;
   double va_max, va_adjust, max_fill;
   int autostep;
-  int pad2;
+  // test hook of the TMA stage kernel's bounded waits: withhold the copy of
+  // each block's last plane (its wait then runs out); the wait limit in clock
+  // cycles for the planes' copies
+  int tm_withhold_last;
+  long long tm_wait_cycles;
   KC<float> kf;
   KC<double> kd;
 };

@@ -1284,6 +1284,34 @@ __global__ void k_adjust_stats(Consts c, const R* __restrict__ U, const R* __res
   }
 }
 
+// Stage-1 CFL speed of a conserved state over the interior, with the limits
+// the step's Adjust_Valf_Max has just set (MHD_Residual's cmax from
+// ConsToPrim's velocities, src/cons_to_prim.C:148-159, src/mhdres_SR.C:
+// 310-327).  A fused step runs it only with adaptive limits (va_adjust > 0):
+// the end-of-step pass's speeds used the previous step's inv_va2max, and the
+// speed depends on it cell by cell.  Same expression as k_step_finish; one
+// atomic per block.
+template <class R>
+__global__ void __launch_bounds__(256) k_cfl_cons(Consts c, const R* __restrict__ U, const R* __restrict__ P,
+                                                  Dyn* __restrict__ dyn) {
+  if (dyn->err) return;
+  const Geom& g = c.g;
+  const unsigned n = (unsigned)g.nx * (unsigned)g.ny * (unsigned)g.nz, N = g.N32;
+  const R inv_va2max = dynr<R>(dyn).inv_va2max;
+  R cm = (R)0;
+  for (unsigned t = gs_first(); t < n; t += gs_step()) {
+    int i, j, k;
+    interior_ijk(g, t, i, j, k);
+    const unsigned id = cidx32(g, i, j, k);
+    const R d = U[id];
+    R v1, v2, v3, ei;
+    prim_from_cons(d, U[N + id], U[2 * N + id], U[3 * N + id], U[4 * N + id], v1, v2, v3, ei);
+    cm = smax(cm, cmax_cell<R>(d, v1, v2, v3, U[5 * N + id], U[6 * N + id], U[7 * N + id], P[id], inv_va2max));
+  }
+  const R m = block_max_nonnan(cm);
+  if (threadIdx.x == 0) atomic_max_nonneg(&dyn->cmax_bits, (double)m);
+}
+
 // CFL speed on the face ghost cells the residual's pencils include
 // (one coordinate in the ghost range, the other two interior).
 template <class R>

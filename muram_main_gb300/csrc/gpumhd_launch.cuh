@@ -25,6 +25,10 @@ __global__ void k_divb_begin(Dyn* dyn);
 // scalars, set on the device so that no host copy sits in the stream.
 __global__ void k_fused_reinit(Consts c, Dyn* dyn, double inv_va2max, double v_lim, double e_lim, double vsqr_diff);
 __global__ void k_divb_end(Consts c, Dyn* dyn);
+// Adjust_Valf_Max with adaptive limits (va_adjust > 0) at the start of a fused
+// step (one thread): the limits from the statistics the previous pass
+// reduced, and a cleared CFL accumulator for the pass that follows.
+__global__ void k_step_limits(Consts c, Dyn* dyn);
 
 template <class R>
 struct Launch {
@@ -61,6 +65,8 @@ struct Launch {
   static void init_pass(const Consts& c, const R* U, R* P, Dyn* dyn, cudaStream_t s);
   static void adjust_stats(const Consts& c, const R* U, const R* P, Dyn* dyn, cudaStream_t s);
   static void cmax_faces(const Consts& c, const R* U, const R* P, Dyn* dyn, cudaStream_t s);
+  // interior CFL speed of a conserved state with the step's limits (adaptive limits only)
+  static void cfl_cons(const Consts& c, const R* U, const R* P, Dyn* dyn, cudaStream_t s);
   static void source_integrate(const Consts& c, R* U, const R* U0, R* Res, const Dyn* dyn, int stage, cudaStream_t s);
   static void save_cons(const Consts& c, const R* U, R* U0, cudaStream_t s);
   static void tcheck(const Consts& c, R* U, const Dyn* dyn, cudaStream_t s);
@@ -322,6 +328,11 @@ void Launch<R>::cmax_faces(const Consts& c, const R* U, const R* P, Dyn* dyn, cu
   const Geom& g = c.g;
   long long n = 2LL * GH * ((long long)g.ny * g.nz + (long long)g.nx * g.nz + (long long)g.nx * g.ny);
   k_cmax_faces<R><<<grid_for(n, 256), 256, 0, s>>>(c, U, P, dyn);
+}
+template <class R>
+void Launch<R>::cfl_cons(const Consts& c, const R* U, const R* P, Dyn* dyn, cudaStream_t s) {
+  const long long n = (long long)c.g.nx * c.g.ny * c.g.nz;
+  k_cfl_cons<R><<<grid_for(n, 256), 256, 0, s>>>(c, U, P, dyn);
 }
 template <class R>
 void Launch<R>::source_integrate(const Consts& c, R* U, const R* U0, R* Res, const Dyn* dyn, int stage, cudaStream_t s) {

@@ -10,9 +10,10 @@
 //    memory (tcgen05.st / tcgen05.ld, one TMEM lane per thread), which leaves
 //    shared memory to the plane tiles and the x / y flux buffers.
 //
-// Every mbarrier wait is bounded (about one second); on expiry the kernel sets
-// ERR_WAIT_TIMEOUT in the step-control block, waits (bounded) for the copies it
-// issued, releases its tensor memory and returns.
+// Every mbarrier wait is bounded (about one second, or the test hook's limit);
+// on expiry the kernel sets ERR_WAIT_TIMEOUT in the step-control block, waits
+// (bounded, about one second) for the copies it issued, releases its tensor
+// memory and returns.
 #pragma once
 #include <cuda.h>
 
@@ -51,12 +52,12 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long* b, unsigned pa
       : "memory");
   return ok != 0;
 }
-// Wait for completion of phase `parity`; false after WAIT_CYCLES.
-__device__ __forceinline__ bool mbar_wait(unsigned long long* b, unsigned parity) {
+// Wait for completion of phase `parity`; false after `limit` clock cycles.
+__device__ __forceinline__ bool mbar_wait(unsigned long long* b, unsigned parity, long long limit = WAIT_CYCLES) {
   if (mbar_try_wait(b, parity)) return true;
   const long long t0 = clock64();
   while (!mbar_try_wait(b, parity))
-    if (clock64() - t0 > WAIT_CYCLES) return false;
+    if (clock64() - t0 > limit) return false;
   return true;
 }
 
@@ -296,7 +297,11 @@ __global__ void __launch_bounds__(TX* TY, 2)
   // plane tiles: plane p is tile t = p - (zb - 2), slot t % NSLOT, phase (t / NSLOT) % 2
   const int p_first = zb - 2;
   auto tile = [&](int p) { return reinterpret_cast<const R*>(sm + (size_t)((p - p_first) % L::NSLOT) * L::TILE); };
+  // test hook: the last plane's copy is never issued, so its wait runs out
+  const int withheld = c.tm_withhold_last ? ze + 1 : -1;
+  const long long wait_limit = c.tm_wait_cycles > 0 ? c.tm_wait_cycles : tm::WAIT_CYCLES;
   auto issue = [&](int p) {  // one thread
+    if (p == withheld) return;
     const int t = p - p_first, sl = t % L::NSLOT;
     unsigned char* dst = sm + (size_t)sl * L::TILE;
     tm::fence_proxy_async();
@@ -307,7 +312,7 @@ __global__ void __launch_bounds__(TX* TY, 2)
   bool timed_out = false;
   auto wait_tile = [&](int p) {
     const int t = p - p_first;
-    if (!tm::mbar_wait(&bar[t % L::NSLOT], (unsigned)((t / L::NSLOT) & 1))) timed_out = true;
+    if (!tm::mbar_wait(&bar[t % L::NSLOT], (unsigned)((t / L::NSLOT) & 1), wait_limit)) timed_out = true;
   };
   // cell offsets inside a tile: own cell and halo cell
   const int o_own = (ty + 2) * L::BX + (tx + 2);
@@ -484,6 +489,7 @@ __global__ void __launch_bounds__(TX* TY, 2)
       // the last NSLOT tiles issued are the only ones that can be in flight
       const int p_last = max(ze + 1, zb + 2);
       for (int p = max(p_first, p_last - (L::NSLOT - 1)); p <= p_last; p++) {
+        if (p == withheld) continue;  // never issued
         const int t = p - p_first;
         tm::mbar_wait(&bar[t % L::NSLOT], (unsigned)((t / L::NSLOT) & 1));
       }

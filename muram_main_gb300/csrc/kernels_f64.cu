@@ -20,12 +20,68 @@ __global__ void k_step_begin(Consts c, Dyn* dyn, double* dt_hist, int dt_hist_ca
   }
 }
 
+// Adjust_Valf_Max with adaptive limits (src/Adjust_Valf_Max.C:92-144) from the
+// maxima and near-limit counts the previous pass reduced over the step's
+// stage-1 state: the first call takes v_lim and e_lim from the maxima, later
+// calls scale them by 1.04 / 1.01 / 0.99 from the counts; va_max follows the
+// velocity and sound-speed maxima and decays by at most 1 % per call.  The
+// function statics of the reference (ini_flag, va_max_old) live in Dyn.
+// Where the reference squares with pow(x, 2.0), this squares with one
+// multiplication: the correctly rounded square, which glibc's pow misses by
+// one ulp for about 0.1 % of arguments.
+__global__ void k_step_limits(Consts c, Dyn* dyn) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  if (dyn->err) return;
+  const double g0 = __longlong_as_double((long long)dyn->stat_max_bits[0]);
+  const double g1 = sqrt(__longlong_as_double((long long)dyn->stat_max_bits[1]));
+  const double g2 = __longlong_as_double((long long)dyn->stat_max_bits[2]);
+  const double n0 = (double)dyn->stat_cnt[0], n1 = (double)dyn->stat_cnt[1];
+  const double cs_fac = 2.0, vv_fac = 3.0, eps_decay = 0.99, mf = c.max_fill;
+  double v_lim = dyn->v_lim, e_lim = dyn->e_lim;
+  if (dyn->va_ini_flag) {
+    v_lim = fmin(g0, c.tchk_vmax);
+    e_lim = fmin(g2, c.tchk_eps_max);
+    dyn->va_max_old = 0.0;
+    dyn->va_ini_flag = 0;
+  } else {
+    if (n0 >= 4 * mf) v_lim *= 1.04;
+    else if (n0 >= mf) v_lim *= 1.01;
+    else if (n0 < 0.5 * mf) v_lim *= 0.99;
+    if (n1 >= 4 * mf) e_lim *= 1.04;
+    else if (n1 >= mf) e_lim *= 1.01;
+    else if (n1 < 0.5 * mf) e_lim *= 0.99;
+  }
+  double va_max = fmax(c.va_max, c.va_adjust * vv_fac * g0);
+  va_max = fmax(va_max, c.va_adjust * cs_fac * g1);
+  va_max = fmax(va_max, dyn->va_max_old * eps_decay);
+  v_lim = fmax(v_lim, c.va_max / vv_fac);
+  v_lim = fmin(v_lim, c.tchk_vmax);
+  const double ef = c.va_max / cs_fac;
+  e_lim = fmax(e_lim, ef * ef);
+  e_lim = fmin(e_lim, c.tchk_eps_max);
+  dyn->v_lim = v_lim;
+  dyn->e_lim = e_lim;
+  dyn->inv_va2max = 1.0 / (va_max * va_max);
+  dyn->va_max_old = va_max;
+  // TVDlimit's velocity cap (src/tvdlimit_SR.C:194-197); with vmax_lim >= 1
+  // it does not depend on v_lim and keeps the host's value
+  if (c.vmax_lim < 1.0) {
+    const double vl = c.vmax_lim * v_lim;
+    dyn->vsqr_diff = vl * vl;
+  }
+  derive_one<float>(*dyn, c.dx, c.idx, c.rt_cfl, c.tchk_vmax, c.tchk_eps_max, dyn->rf, c.spt_cfl_dx);
+  derive_one<double>(*dyn, c.dx, c.idx, c.rt_cfl, c.tchk_vmax, c.tchk_eps_max, dyn->rd, c.spt_cfl_dx);
+  dyn->cmax_bits = 0ULL;  // the CFL pass that follows uses the new inv_va2max
+}
+
 __device__ __forceinline__ void step_begin(const Consts& c, Dyn* dyn, double* dt_hist, int dt_hist_cap) {
   if (dyn->err) return;
-  // Adjust_Valf_Max without va_adjust (src/Adjust_Valf_Max.C:136-142); the
-  // fused path runs only in that mode, so the limits are the run constants.
-  dyn->v_lim = c.tchk_vmax;
-  dyn->e_lim = c.tchk_eps_max;
+  // Adjust_Valf_Max (src/Adjust_Valf_Max.C:136-142): without va_adjust the
+  // limits are the run constants; with it k_step_limits has set them.
+  if (!(c.va_adjust > 0.0)) {
+    dyn->v_lim = c.tchk_vmax;
+    dyn->e_lim = c.tchk_eps_max;
+  }
   dyn->dt_prev = dyn->dt;  // Run.dt as MHD_Residual sees it at stage 1
   const double cmax = __longlong_as_double((long long)dyn->cmax_bits);
   double dt_mhd = c.dxmin / cmax;
@@ -81,11 +137,13 @@ __global__ void k_set_counter(int* counter, int n) {
 
 __global__ void k_fused_reinit(Consts c, Dyn* dyn, double inv_va2max, double v_lim, double e_lim, double vsqr_diff) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  dyn->va_ini_flag = 0;
-  dyn->inv_va2max = inv_va2max;
-  dyn->v_lim = v_lim;
-  dyn->e_lim = e_lim;
-  dyn->vsqr_diff = vsqr_diff;
+  if (!(c.va_adjust > 0.0)) {  // adaptive limits keep their history (the reference's function statics)
+    dyn->va_ini_flag = 0;
+    dyn->inv_va2max = inv_va2max;
+    dyn->v_lim = v_lim;
+    dyn->e_lim = e_lim;
+    dyn->vsqr_diff = vsqr_diff;
+  }
   dyn->err = 0;
   dyn->cmax_bits = 0ULL;
   dyn->stat_max_bits[0] = dyn->stat_max_bits[1] = dyn->stat_max_bits[2] = 0ULL;

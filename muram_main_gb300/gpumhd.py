@@ -70,7 +70,7 @@ EXPORTS = [
     "gpumhd_adjoint", "gpumhd_tile_from", "gpumhd_set_tuning", "gpumhd_get_tuning", "gpumhd_autotune", "gpumhd_ensemble_create",
     "gpumhd_ensemble_destroy", "gpumhd_ensemble_enqueue_steps", "gpumhd_ensemble_synchronize",
     "gpumhd_ensemble_last_error", "gpumhd_ensemble_stream", "gpumhd_ensemble_launch_count",
-    "gpumhd_clean_divB", "gpumhd_divb_info", "gpumhd_boundary_info",
+    "gpumhd_clean_divB", "gpumhd_divb_info", "gpumhd_boundary_info", "gpumhd_test_tma_wait",
 ]
 
 _lib = None
@@ -138,6 +138,7 @@ def load(build_if_missing=True):
         "gpumhd_clean_divB": (C.c_int, [vp]),
         "gpumhd_divb_info": (C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), dp, dp]),
         "gpumhd_boundary_info": (C.c_int, [vp, dp, dp]),
+        "gpumhd_test_tma_wait": (C.c_int, [vp, C.c_longlong, C.c_int]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -397,6 +398,10 @@ class MuramGPU:
         self._chk(self._L.gpumhd_tile_from(self._h, src._h))
 
     # -- launch shapes
+    def test_tma_wait(self, wait_cycles=0, withhold_last=False):
+        """Test hook of the TMA stage kernel's bounded waits (see gpumhd.h)."""
+        self._chk(self._L.gpumhd_test_tma_wait(self._h, int(wait_cycles), 1 if withhold_last else 0))
+
     def set_tuning(self, stage_zchunk=0, tvd_chunk=0):
         self._chk(self._L.gpumhd_set_tuning(self._h, stage_zchunk, tvd_chunk))
 

@@ -153,7 +153,8 @@ class State:
     """Scratch buffers for full steps on the oracle.  With divB cleaning on
     (p.divB_switch > 0), ``phi`` carries the cleaning potential from step to
     step, ``divB`` holds the last divergence and ``divb_log`` one entry
-    (iterations, max|divB| before, after) per step."""
+    (iterations, max|divB| before, after) per step.  ``limits_log`` holds
+    Adjust_Valf_Max's (inv_va2max, v_lim, e_lim) after each step."""
 
     def __init__(self, p, U, eos=None):
         self.p = p
@@ -171,6 +172,7 @@ class State:
         self._f = MoFields(ptr(self.phi), ptr(self.divB), ptr(self.sflx), ptr(self.sflx0), ptr(self.Rflx),
                            ptr(self.BgradT))
         self.divb_log = []
+        self.limits_log = []
         if p.xbnd == 1 and not p.periodic_x:
             if eos is None:
                 raise ValueError("the physical x boundaries need the EOS (State(p, U, eos))")
@@ -185,6 +187,7 @@ class State:
             if rc:
                 raise RuntimeError(f"oracle step failed: {rc}")
             dts.append((self.p.dt, self.p.last_cfl))
+            self.limits_log.append((self.p.inv_va2max, self.p.v_lim, self.p.e_lim))
             if self.p.divB_switch > 0:
                 self.divb_log.append((self.p.divB_last_iters, self.p.divB_err0, self.p.divB_err1))
         return dts

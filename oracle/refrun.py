@@ -15,8 +15,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 REF_BIN = os.path.join(HERE, "_ref", "muram_ref_harness")
 DROPIN_BIN = os.path.join(HERE, "_ref", "muram_gpu_dropin")
-# where the reference sources are mounted in the build container
-REF_ROOT = os.environ.get("MURAM_REF", "/root/reference")
+# the reference sources: $MURAM_REF, else a checkout named "reference" beside
+# this repository
+REF_ROOT = os.environ.get("MURAM_REF") or os.path.normpath(os.path.join(HERE, "..", "..", "reference"))
 
 
 def available():

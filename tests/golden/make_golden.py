@@ -10,6 +10,8 @@ The spitzer case adds the hyperbolic heat conduction (heat flux from zero,
 hot top) and keeps the final heat flux.
 The open_bottom case uses the reference's own physical x boundaries (open
 bottom, top open to outflows) and keeps the p_bc and s_bc they set.
+The va_adjust case runs the adaptive limits of Adjust_Valf_Max and keeps its
+per-step log line (maxima, va_max, the limits and the near-limit counts).
 The divb_cleaning case also runs the reference's Clean_divB after each TVD
 pass and keeps the cleaning potential phi, the last divergence and the
 iteration count of every step (parsed from the reference's own log line).
@@ -52,6 +54,12 @@ def cases():
         initial.stratified_box(eos, 12, 8, 6, dx=1.6e6, seed=16), dict(steps=6, trace_step=3)
     yield "open_bottom", dict(nx=12, ny=8, nz=6, dx=1.6e6, periodic_x=0, grav=2.74e4, xbnd=1, bnd_top=1), \
         initial.stratified_box(eos, 12, 8, 6, dx=1.6e6, seed=15), dict(steps=4, trace_step=2)
+    # the adaptive Alfven-speed, velocity and energy limits of the reference's
+    # 3-D test run (va_adjust 1, max_fill 100: TEST/Test_3D/parameters.dat:52-53)
+    # with va_max low enough that v_lim adapts instead of sitting at va_max/3
+    yield "va_adjust", dict(nx=16, ny=12, nz=8, dx=3.2e6, periodic_x=1, va_max=3.0e5, va_adjust=1.0,
+                            max_fill=100.0, verbose=1), \
+        initial.periodic_box(eos, 16, 12, 8, seed=17, v_rms=2.0e5, b_rms_gauss=800.0), dict(steps=8, trace_step=3)
 
 
 KEEP = ["init_U", "s1_c2p_U", "s1_c2p_aux", "s1_res_R", "s1_res_dt", "s1_si_U", "s1_bc_U", "s2_c2p_U",
@@ -88,6 +96,13 @@ def main(only=()):
             summ = dict(x.split("=") for x in out["summary"].split())
             arrays["p_bc"] = np.array(float(summ["p_bc"]))
             arrays["s_bc"] = np.array(float(summ["s_bc"]))
+        if hp.get("va_adjust", 0):
+            # per step: max|v|, max c_s, va_max, v_lim, cells near v_lim, e_lim,
+            # cells near e_lim (the reference's own log line)
+            num = r"([-+0-9.eE]+)"
+            pat = (r"Adjust_va_max \[\d+\]\s+" + num + r"\s+" + num + r"\s+" + num + r"\s+\|\s+" + num +
+                   r" \(" + num + r"\)\s+" + num + r" \(" + num + r"\)")
+            arrays["va_log"] = np.array([[float(x) for x in m] for m in re.findall(pat, out["stdout"])])
         if hp.get("divB_switch", 0):
             arrays["divb_iters"] = np.array([int(m) for m in re.findall(r"divB_max \[(\d+)\]", out["stdout"])])
         meta = {k: v for k, v in hp.items() if k != "eos"}

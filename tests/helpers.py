@@ -31,7 +31,8 @@ def oracle_params(hp):
 def gpu_params(hp, precision=64):
     from muram_main_gb300 import gpumhd
     kw = {}
-    for k in ("CFL", "CFL_tvd", "grav", "eta", "divB_err", "bnd_bcrit", "bnd_eps_top", "p_bc", "s_bc", "spitzer"):
+    for k in ("CFL", "CFL_tvd", "grav", "eta", "divB_err", "bnd_bcrit", "bnd_eps_top", "p_bc", "s_bc", "spitzer",
+              "va_max", "va_adjust", "max_fill"):
         if k in hp:
             kw[k] = float(hp[k])
     for k in ("divB_switch", "divB_itmax", "xbnd", "bnd_top"):

@@ -6,6 +6,8 @@ host C library by at most a few ulp, so exact equality is not expected where
 the EOS is involved; the observed errors are printed.
 FP32 tolerance: relative L2 per field of 1e-5 after the run.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -129,6 +131,29 @@ def _oracle_run(hp, U, steps):
     st = O.State(H.oracle_params(hp), U)
     dts = st.step(eos, steps)
     return st.U, dts
+
+
+def test_fused_fp64_64cubed_bench_table_100_steps(gpu_lib):
+    """The plain FP64 step at its stated size: a 64^3 fully periodic box at 32 km
+    on the full 3000 x 3000 EOS table (uniform rho = 3e-7 g/cm^3 at 6000 K,
+    1 km/s rms velocity and 100 G rms divergence-free field on wavenumbers
+    1-8), 100 fused steps at CFL 0.8 with TVD diffusion: dt equal to 1e-12 at
+    every step and relative L-infinity <= 1e-12 per field against the oracle."""
+    from muram_main_gb300 import eos_table
+    from oracle import oracle as O
+    path = os.path.join(H.ROOT, "muram_main_gb300", "_data", "eos_bench.dat")
+    eos_table.ensure_table(path, "bench")
+    tab = initial.EosTable(path)
+    U = initial.periodic_box(tab, 64, 64, 64, dx=3.2e6, seed=2024)
+    st = O.State(O.make_params(64, 64, 64, 3.2e6), U)
+    dts_ref = [x[0] for x in st.step(O.Eos(path), 100)]
+    g = gpumhd.MuramGPU(gpumhd.default_params(64, 64, 64, 3.2e6), eos_path=path)
+    g.upload_state(U)
+    dts = g.run_steps(100)
+    assert np.allclose(dts, dts_ref, rtol=TOL64, atol=0), np.max(np.abs(np.array(dts) / dts_ref - 1))
+    assert g.step_info()[3] == 0  # the single-sweep TVD branch (cfl = 0.8 <= CFL_tvd)
+    check("FP64 fused vs oracle, 64^3 at 32 km, 3000x3000 table, 100 steps", H.interior(g.download_state()),
+          H.interior(st.U))
 
 
 @pytest.mark.parametrize("kernel", KERNELS)

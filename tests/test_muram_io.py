@@ -8,8 +8,9 @@ import pytest
 from helpers import EOS_SMALL, rel_linf
 from muram_main_gb300 import muram_io
 from muram_main_gb300.initial import EosTable, periodic_box
+from oracle import refrun
 
-REF_TEST3D = os.path.join(os.environ.get("MURAM_REF", "/root/reference"), "TEST", "Test_3D")
+REF_TEST3D = os.path.join(refrun.REF_ROOT, "TEST", "Test_3D")
 
 
 def _box(nx=12, ny=10, nz=8, seed=5):

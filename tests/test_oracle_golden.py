@@ -260,3 +260,40 @@ def test_live_reference_resistivity(eta, eos):
     if eta > 1e12:  # dt set by the resistive limit dt_diff_fac / eta
         dxmin = 1.6e6
         assert ref["dts"].reshape(-1, 3)[0, 0] <= 0.8 * (dxmin * dxmin / 6.0) / eta * 1.0000001
+
+
+def test_va_adjust_bitexact(eos):
+    """Adjust_Valf_Max with adaptive limits at the reference's 3-D test settings
+    (va_adjust 1, max_fill 100): the first call sets v_lim and e_lim from the
+    maxima, later calls scale them by 1.04, 1.01 or 0.99 from the near-limit
+    counts and clamp them, va_max follows the maxima; the limits of every
+    step, dt and the state match the reference bit for bit."""
+    d, hp = H.load_case("va_adjust")
+    st = O.State(H.oracle_params(hp), d["input_U"])
+    dts = st.step(eos, int(d["steps"]))
+    assert [x[0] for x in dts] == list(d["dts"].reshape(-1, 3)[:, 0])
+    assert [list(x) for x in st.limits_log] == d["limits"].reshape(-1, 3).tolist()
+    assert np.array_equal(st.U, d["final_U"])
+    # the fixture exercises the adaptation: e_lim raised by 4 % and by 1 %, v_lim lowered by 1 %
+    lim = d["limits"].reshape(-1, 3)
+    ratios_e = set(np.round(lim[1:, 2] / lim[:-1, 2], 6))
+    assert {1.04, 1.01} <= ratios_e
+    assert np.allclose(lim[2:, 1] / lim[1:-1, 1], 0.99, rtol=1e-12)
+
+
+@pytest.mark.skipif(not refrun.available(), reason="reference harness not built here")
+@pytest.mark.parametrize("max_fill,va_max,v_rms,seed", [(2.0, 3.0e5, 3.0e5, 41), (30.0, 2.0e6, 1.0e5, 42),
+                                                        (1000.0, 1.0e5, 2.0e5, 43)])
+def test_live_reference_va_adjust(max_fill, va_max, v_rms, seed, eos):
+    """The adaptive limits against the reference run live, with near-limit
+    counts above 4 max_fill, between, and below max_fill / 2, and a va_max
+    floor (va_max / 3, (va_max / 2)^2) that binds or not."""
+    tab = initial.EosTable(H.EOS_SMALL)
+    U = initial.periodic_box(tab, 12, 10, 8, seed=seed, v_rms=v_rms, b_rms_gauss=600.0)
+    hp = dict(nx=12, ny=10, nz=8, dx=3.2e6, eos=H.EOS_SMALL, va_adjust=1.0, max_fill=max_fill, va_max=va_max)
+    ref = refrun.run(U, hp, steps=6)
+    st = O.State(H.oracle_params(hp), U)
+    dts = st.step(eos, 6)
+    assert np.array_equal(np.array([x[0] for x in dts]), ref["dts"].reshape(-1, 3)[:, 0])
+    assert np.array_equal(np.array(st.limits_log).reshape(-1), ref["limits"])
+    assert np.array_equal(st.U, ref["final_U"])
