@@ -69,7 +69,7 @@ def make_state(nx, ny, nz, seed):
 
 # ----------------------------------------------------------------- CPU side
 def _cpu_worker(args):
-    seed, steps = args
+    seed, steps, warmup = args
     import numpy as np  # noqa: F401
     from oracle import oracle as O
     U = make_state(SAMPLE["nx"], SAMPLE["ny"], SAMPLE["nz"], seed)
@@ -77,14 +77,14 @@ def _cpu_worker(args):
                       grav=WORKLOAD["grav"])
     st = O.State(p, U)
     eos = O.Eos(EOS_BENCH)
-    st.step(eos, 1)  # warm-up
+    st.step(eos, warmup)
     t0 = time.perf_counter()
     st.step(eos, steps)
     dt = time.perf_counter() - t0
     return SAMPLE["nx"] * SAMPLE["ny"] * SAMPLE["nz"] * steps, dt
 
 
-def cpu_baseline(cores, steps_per_core):
+def cpu_baseline(cores, steps_per_core, warmup=1):
     """Oracle (C restatement of the reference path) on `cores` spawned processes,
     each advancing its own 128x32x32 column of the workload; aggregate rate."""
     from oracle import oracle as O
@@ -93,7 +93,7 @@ def cpu_baseline(cores, steps_per_core):
     eos_table.ensure_table(EOS_BENCH, "bench")
     ctx = mp.get_context("spawn")
     with ctx.Pool(cores) as pool:
-        res = pool.map(_cpu_worker, [(1000 + i, steps_per_core) for i in range(cores)])
+        res = pool.map(_cpu_worker, [(1000 + i, steps_per_core, warmup) for i in range(cores)])
     cells = sum(r[0] for r in res)
     wall = max(r[1] for r in res)
     return cells / wall, wall
@@ -115,7 +115,7 @@ class ClockSampler:
         try:
             self._proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
         except OSError:
             self._proc = None
             return
@@ -221,6 +221,44 @@ def words_per_cell(phase):
     return 0
 
 
+# Algorithmic words per interior cell and step, the compulsory traffic of a
+# fused design (ghost reads as cache hits): each of the 4 RK stages reads and
+# writes the 8-word state, stages 2-4 also read U0, stage 4 stores the pressure
+# the TVD sweeps use, and 3 TVD sweeps read 8 + 1 and write 8.  The roofline
+# uses these counts; the kernels here also hand the pressure from stage to
+# stage (words_per_cell above), which the counts leave out.
+ALGO_STAGE_WORDS = 4 * 16 + 3 * 8 + 1      # 89 per 4 stage launches
+ALGO_TVD_WORDS = 3 * 17                    # 51 per 3 sweeps
+ALGO_STEP_WORDS = ALGO_STAGE_WORDS + ALGO_TVD_WORDS  # 140
+# Floating-point operations per cell-update (4 stages, 3 TVD sweeps), counted
+# from the reference's source to +-30 %: the FP64 mode's arithmetic roofline
+FLOPS_PER_CELL_UPDATE = 3700.0
+FLOPS_STAGE_PER_CELL = 2600.0 / 4          # per stage launch
+
+
+def fp64_peak_tflops():
+    """The GPU's FP64 rate as cuBLAS reaches it: a DGEMM of 8192^3 through
+    torch.matmul (best of 5 after a warm-up, CUDA events)."""
+    import torch
+    n = 8192
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    torch.matmul(a, b)
+    best = None
+    for _ in range(5):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        best = ms if best is None else min(best, ms)
+    del a, b
+    torch.cuda.empty_cache()
+    return 2.0 * n ** 3 / (best / 1e3) / 1e12
+
+
 def load_traffic():
     path = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(path):
@@ -301,7 +339,9 @@ def run_ours(args):
     dom = max(tot, key=tot.get)
     launches_dom = fam[dom]
     mean_ms = tot[dom] / len(launches_dom)
-    bytes_per_launch = sum(words_per_cell(p) for p in launches_dom) / len(launches_dom) * 4 * n_cells
+    algo_words = ALGO_STAGE_WORDS if dom == "stage" else ALGO_TVD_WORDS
+    bytes_per_launch = algo_words / len(launches_dom) * 4 * n_cells
+    design_bytes_per_launch = sum(words_per_cell(p) for p in launches_dom) / len(launches_dom) * 4 * n_cells
     achieved = bytes_per_launch / (mean_ms / 1e3) / 1e9
     traffic = load_traffic().get(f"{dom}_f32_bytes_per_cell")
     roofline = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak_gbs, "unit": "GB/s",
@@ -309,12 +349,14 @@ def run_ours(args):
                 "traffic": (traffic * n_cells if traffic else None),
                 "kernel": f"k_stage (FP32, RK stages 1-4)" if dom == "stage" else "k_tvd_sweep (FP32, x/y/z)",
                 "algorithmic_bytes_per_launch": bytes_per_launch, "mean_launch_ms": round(mean_ms, 4),
+                "algorithmic_words_per_cell": f"{algo_words} per {len(launches_dom)} launches",
+                "design_bytes_per_launch": design_bytes_per_launch,
                 "peak_source": f"{peak_src} hbm_gbs"}
     if dom == "stage":
         roofline["limiter"] = ("instruction issue and dependency latency, not HBM (ncu: ~58 % issue active, "
                                "24-39 % DRAM throughput)")
     # whole-step bytes against HBM
-    step_bytes = sum(words_per_cell(p) for p in fam["stage"] + fam["tvd"] + ["finish"]) * 4 * n_cells
+    step_bytes = ALGO_STEP_WORDS * 4 * n_cells
     step_ms = ms / args.steps
     # end to end through the C ABI with host buffers
     e2e = None
@@ -355,34 +397,56 @@ def run_ours(args):
     if not args.no_fp64:
         import numpy as np
         nerr = args.err_steps
+        checkpoints = sorted({nerr, 2 * nerr})  # the 100-step bar and the configuration's 200-step run
         g64 = context(64)
         g64.run_steps(1)
         g64.upload_state(U)
         ms64, _ = time_device(g64, nerr, 0)
         ms64 = replica_max(ms64)
         value64 = job_rate(ws, n_cells, nerr, ms64)
-        fp64 = {"value": value64, "unit": UNIT, "ms_per_step": ms64 / nerr, "steps": nerr,
-                "fp32_over_fp64": value / value64}
-        ref = g64.download_state()[:, 2:-2, 2:-2, 2:-2]
+        refs = {nerr: g64.download_state()[:, 2:-2, 2:-2, 2:-2]}
+        for cp in checkpoints[1:]:
+            g64.run_steps(cp - nerr)
+            refs[cp] = g64.download_state()[:, 2:-2, 2:-2, 2:-2]
+        ph64 = g64.profile_steps(2)
         g64.close()
         del g64
-        fp32_err = {"steps": nerr, "against": "FP64 GPU mode (= reference CPU build to 1e-12)",
+        stage64_ms = sum(ph64[f"stage{q}"] for q in range(1, 5)) / 4
+        peak64 = fp64_peak_tflops()
+        ach64 = FLOPS_STAGE_PER_CELL * n_cells / (stage64_ms / 1e3) / 1e12
+        fp64 = {"value": value64, "unit": UNIT, "ms_per_step": ms64 / nerr, "steps": nerr,
+                "fp32_over_fp64": value / value64,
+                "roofline": {"bound": "fp64", "kernel": "k_stage_tm (FP64, RK stages 1-4)",
+                             "achieved": round(ach64, 4), "peak": round(peak64, 4), "unit": "TFLOP/s",
+                             "frac": round(ach64 / peak64, 4), "mean_launch_ms": round(stage64_ms, 4),
+                             "flops_per_cell_per_launch": FLOPS_STAGE_PER_CELL,
+                             "peak_source": "measured: cuBLAS DGEMM 8192^3 via torch.matmul",
+                             "hbm_frac": round(ALGO_STAGE_WORDS / 4 * 8 * n_cells / (stage64_ms / 1e3) / 1e9
+                                               / peak_gbs, 4)},
+                "phases_ms": {k: round(v, 3) for k, v in ph64.items()}}
+        fp32_err = {"steps": checkpoints, "against": "FP64 GPU mode (= reference CPU build to 1e-12)",
                     "fields": ["rho", "Mx", "My", "Mz", "e", "Bx", "By", "Bz"]}
         for comp in (0, 1):
             p32 = gpumhd.default_params(wl["nx"], wl["ny"], wl["nz"], wl["dx"], precision=32,
                                         periodic_x=wl["periodic_x"], grav=wl["grav"], compensated=comp, **divb_kw)
             g32 = gpumhd.MuramGPU(p32, device=lrank, eos_path=EOS_BENCH)
             g32.upload_state(U)
-            g32.run_steps(nerr)
-            got = g32.download_state()[:, 2:-2, 2:-2, 2:-2]
-            g32.close()
-            d = got - ref
-            l2 = [float(np.sqrt(np.sum(d[f] ** 2) / np.sum(ref[f] ** 2))) for f in range(8)]
-            linf = [float(np.max(np.abs(d[f])) / np.max(np.abs(ref[f]))) for f in range(8)]
             key = "compensated" if comp else "plain"
-            fp32_err[key] = {"rel_l2": [float(f"{x:.3e}") for x in l2], "rel_linf": [float(f"{x:.3e}") for x in linf],
-                             "max_rel_l2": float(f"{max(l2):.3e}")}
-        del ref
+            fp32_err[key] = {}
+            done = 0
+            for cp in checkpoints:
+                g32.run_steps(cp - done)
+                done = cp
+                got = g32.download_state()[:, 2:-2, 2:-2, 2:-2]
+                ref = refs[cp]
+                d = got - ref
+                l2 = [float(np.sqrt(np.sum(d[f] ** 2) / np.sum(ref[f] ** 2))) for f in range(8)]
+                linf = [float(np.max(np.abs(d[f])) / np.max(np.abs(ref[f]))) for f in range(8)]
+                fp32_err[key][str(cp)] = {"rel_l2": [float(f"{x:.3e}") for x in l2],
+                                          "rel_linf": [float(f"{x:.3e}") for x in linf],
+                                          "max_rel_l2": float(f"{max(l2):.3e}")}
+            g32.close()
+        del refs
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -525,8 +589,7 @@ def run_large(args):
     n_cells = nx * ny * nz
     phases = g.profile_steps(2)
     value = n_cells * args.steps / (ms / 1e3)
-    step_bytes = sum(words_per_cell(q) for q in ["stage1", "stage2", "stage3", "stage4", "tvd_x", "tvd_y",
-                                                 "tvd_z"]) * 4 * n_cells
+    step_bytes = ALGO_STEP_WORDS * 4 * n_cells
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -636,11 +699,11 @@ def run_reference(args):
     if rank != 0:
         return
     cores = min(os.cpu_count() or 1, 16)
-    steps = max(1, min(args.steps, 3))
+    steps = args.steps
     t0 = time.perf_counter()
-    rate, wall = cpu_baseline(cores, steps)
+    rate, wall = cpu_baseline(cores, steps, args.warmup)
     line = {
-        "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": ws, "steps": steps, "warmup": 1,
+        "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": ws, "steps": steps, "warmup": args.warmup,
         "ms_per_step": SAMPLE["nx"] * SAMPLE["ny"] * SAMPLE["nz"] * cores / rate * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded stratified box, generated EOS table 3000x3000)",
@@ -648,7 +711,8 @@ def run_reference(args):
                    "sample": "128x32x32 columns, one per core"},
         "impl": "reference",
         "cpu_baseline": {"value": rate, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"{cores} processes x {steps} steps of a 128x32x32 column (FP64)"},
+                         "sample": f"{cores} processes x {steps} steps (after {args.warmup} warm-up steps) of a "
+                                   f"128x32x32 column of the workload (FP64), {wall:.1f} s wall"},
         "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "wall_s": round(time.perf_counter() - t0, 2),
     }
@@ -658,7 +722,7 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")

@@ -145,6 +145,13 @@ int gpumhd_clean_divB(gpumhd_ctx* ctx);
  * src/boundary_pdmp_1_fftw3.C:44-50, writes them to backup.dat). */
 int gpumhd_boundary_info(gpumhd_ctx* ctx, double* p_bc, double* s_bc);
 int gpumhd_divb_info(gpumhd_ctx* ctx, int* last_iters, int* next_iters, double* err_before, double* err_after);
+/* Set the iteration count the next Clean_divB call (per routine or inside a
+ * fused step) starts from: the function static next_iter of src/clean_divB.C
+ * (starts at 3), which MURaM keeps only in memory and restarts at 3.  For
+ * carrying it across a restart, or for running two contexts on one iteration
+ * sequence; 1 <= next_iters <= max(3, divB_itmax), else GPUMHD_E_INVALID.
+ * Stream-ordered with the context's other calls. */
+int gpumhd_set_divb_iters(gpumhd_ctx* ctx, int next_iters);
 
 /* SaveCons (include/src_int_tck.H:10, src/Add_Sources_Integrate_SR.C:475-531). */
 int gpumhd_save_cons(gpumhd_ctx* ctx);

@@ -1165,6 +1165,17 @@ extern "C" int gpumhd_clean_divB(gpumhd_ctx* ctx) {
   return pull_dyn(ctx);
 }
 
+extern "C" int gpumhd_set_divb_iters(gpumhd_ctx* ctx, int next_iters) {
+  if (!ctx) return GPUMHD_E_INVALID;
+  const int cap = ctx->p.divB_itmax > 3 ? ctx->p.divB_itmax : 3;  // the count starts at 3 whatever itmax is
+  if (next_iters < 1 || next_iters > cap)
+    return fail(ctx, GPUMHD_E_INVALID, "divB iteration count %d outside [1, %d]", next_iters, cap);
+  CK(cudaSetDevice(ctx->device));
+  k_set_counter<<<1, 32, 0, ctx->stream>>>(&ctx->dyn->divb_next, next_iters);  // stream-ordered
+  ctx->hdyn.divb_next = next_iters;
+  return check_launch(ctx, 1);
+}
+
 extern "C" int gpumhd_divb_info(gpumhd_ctx* ctx, int* last_iters, int* next_iters, double* err_before,
                                 double* err_after) {
   if (!ctx) return GPUMHD_E_INVALID;

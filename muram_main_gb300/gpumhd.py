@@ -71,6 +71,7 @@ EXPORTS = [
     "gpumhd_ensemble_destroy", "gpumhd_ensemble_enqueue_steps", "gpumhd_ensemble_synchronize",
     "gpumhd_ensemble_last_error", "gpumhd_ensemble_stream", "gpumhd_ensemble_launch_count",
     "gpumhd_clean_divB", "gpumhd_divb_info", "gpumhd_boundary_info", "gpumhd_test_tma_wait",
+    "gpumhd_set_divb_iters",
 ]
 
 _lib = None
@@ -139,6 +140,7 @@ def load(build_if_missing=True):
         "gpumhd_divb_info": (C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), dp, dp]),
         "gpumhd_boundary_info": (C.c_int, [vp, dp, dp]),
         "gpumhd_test_tma_wait": (C.c_int, [vp, C.c_longlong, C.c_int]),
+        "gpumhd_set_divb_iters": (C.c_int, [vp, C.c_int]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -273,6 +275,10 @@ class MuramGPU:
 
     def Clean_divB(self):
         self._chk(self._L.gpumhd_clean_divB(self._h))
+
+    def set_divb_iters(self, next_iters):
+        """Set Clean_divB's adaptive iteration count for the next call."""
+        self._chk(self._L.gpumhd_set_divb_iters(self._h, int(next_iters)))
 
     def divb_info(self):
         """(iterations of the last cleaning, iterations of the next, max|divB|

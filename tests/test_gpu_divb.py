@@ -128,19 +128,45 @@ def test_fused_vs_oracle(gpu_lib, kernel, case):
 
 
 def test_fp32_cleaning_vs_fp64_oracle(gpu_lib):
+    """FP32 with cleaning against the FP64 oracle after 100 steps.
+
+    Clean_divB's iteration count adapts from the ratio of max|divB| after and
+    before the iterations against divB_err.  Where that ratio lands close to
+    divB_err, the FP32 divergence (a small difference of float fluxes) can
+    fall on the other side of it: FP32 then takes one iteration more or fewer
+    on that step and departs from FP64 by far more than rounding (an earlier
+    build measured 5e-5 relative L2 in B on this machine).  Both runs are checked:
+    one on FP64's iteration sequence (set before each step through
+    gpumhd_set_divb_iters) and the free-running one; the steps whose counts
+    differ are printed."""
     from oracle import oracle as O
     tab = initial.EosTable(H.EOS_SMALL)
     U = initial.periodic_box(tab, 32, 32, 32, seed=5)
     hp = dict(nx=32, ny=32, nz=32, dx=3.2e6, divB_switch=1, divB_itmax=5, divB_err=0.2)
     st = O.State(H.oracle_params(hp), U)
-    st.step(O.Eos(H.EOS_SMALL), 50)
-    g = ctx_for(hp, precision=32)
-    g.upload_state(U)
-    g.run_steps(50)
-    e = H.rel_l2(H.interior(g.download_state()), H.interior(st.U))
-    print("FP32 with cleaning vs FP64 oracle, rel L2:", np.array2string(e, precision=2))
+    st.step(O.Eos(H.EOS_SMALL), 100)
+    iters64 = [x[0] for x in st.divb_log]
+    forced = ctx_for(hp, precision=32)
+    free = ctx_for(hp, precision=32)
+    forced.upload_state(U)
+    free.upload_state(U)
+    iters32 = []
+    for s in range(100):
+        forced.set_divb_iters(iters64[s])
+        forced.run_steps(1)
+        assert forced.divb_info()[0] == iters64[s]
+        free.run_steps(1)
+        iters32.append(free.divb_info()[0])
+    e_free = H.rel_l2(H.interior(free.download_state()), H.interior(st.U))
+    e = H.rel_l2(H.interior(forced.download_state()), H.interior(st.U))
+    flips = [s for s in range(100) if iters32[s] != iters64[s]]
+    print("FP32 with cleaning vs FP64 oracle after 100 steps, rel L2 -- on FP64's iteration counts:",
+          np.array2string(e, precision=2), "free-running:", np.array2string(e_free, precision=2),
+          "steps whose count differs:", flips[:10])
     assert np.all(e <= 1e-5), e
-    g.close()
+    assert np.all(e_free <= 1e-5), (e_free, flips)
+    forced.close()
+    free.close()
 
 
 def test_cleaning_reduces_divergence_and_is_timed(gpu_lib):
