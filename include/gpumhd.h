@@ -118,7 +118,8 @@ int gpumhd_eos_init(gpumhd_ctx* ctx, const char* path);
  * which = 0: U, 1: U0, 2: Res (cState arrays, 8 doubles per node);
  * which = 3..7: pres, temp, ne, rhoi, amb; 8: phi, 9: divB (the divB cleaning's
  * potential and last divergence, GridData::phi / divB); 10: sflx (the Spitzer
- * heat flux, GridData::sflx); one double per node. */
+ * heat flux, GridData::sflx); 11..20: the diagnostics tvar1..tvar8, Qres, Qvis
+ * (GridData, see gpumhd_set_need_diagnostics); one double per node. */
 int gpumhd_upload(gpumhd_ctx* ctx, int which, const double* host);
 int gpumhd_download(gpumhd_ctx* ctx, int which, double* host);
 /* The same transfers without waiting (no reference counterpart): each one
@@ -153,6 +154,20 @@ int gpumhd_divb_info(gpumhd_ctx* ctx, int* last_iters, int* next_iters, double* 
  * Stream-ordered with the context's other calls. */
 int gpumhd_set_divb_iters(gpumhd_ctx* ctx, int next_iters);
 
+/* RunData::need_diagnostics (include/run.H; set per stage by src/solver.C:
+ * 264-289): on = 1 zeroes the ten diagnostic arrays (which = 11..20) and makes
+ * the per-routine calls that follow fill them as the reference's do on an
+ * output step -- MHD_Residual: tvar1 the energy-flux divergence (tvar2 its
+ * conduction share), tvar3 the Lorentz force's work (src/mhdres_SR.C:
+ * 368-384, 434-435, 689-702, 751-752); Source_Integrate_Tcheck: tvar4 the
+ * radiation factor, tvar5 the gravity work, tvar6 the Boris energy, tvar7
+ * += Tcheck's energy change / dt (src/Add_Sources_Integrate_SR.C:122-296);
+ * TVDlimit: tvar8 its energy change, tvar6 its Boris part, Qres and Qvis the
+ * resistive and viscous heating, tvar7 its energy floor's change, per unit
+ * of Run.dt (src/tvdlimit_SR.C:577-667); TCheck: tvar7 (:618-620).  MURaM
+ * sets it at stage 4 of an output step and clears it at the next stage 1.
+ * Fused steps refuse to run while it is on. */
+int gpumhd_set_need_diagnostics(gpumhd_ctx* ctx, int on);
 /* SaveCons (include/src_int_tck.H:10, src/Add_Sources_Integrate_SR.C:475-531). */
 int gpumhd_save_cons(gpumhd_ctx* ctx);
 /* ConsToPrim (include/eos.H:39, src/cons_to_prim.C:78-266). */

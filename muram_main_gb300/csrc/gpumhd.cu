@@ -71,6 +71,10 @@ struct gpumhd_ctx {
   int tm_withhold_last = 0;
   long long tm_wait_cycles = 0;
   void* comp = nullptr;  // FP32 compensated mode: per-cell remainders of the RK update (8N floats)
+  // diagnostics of an output step (RunData::need_diagnostics): tvar1..tvar8,
+  // Qres, Qvis (GridData, 10 x N), allocated when first switched on
+  void* diag = nullptr;
+  bool need_diag = false;
   void* phi = nullptr;   // divB cleaning potential (GridData::phi, N), persists between calls
   void* divb = nullptr;  // last divergence of B (GridData::divB, N)
   double* bnd_part = nullptr;  // per-plane sums of the physical x boundaries (nz * BND_NQ)
@@ -504,6 +508,7 @@ extern "C" int gpumhd_destroy(gpumhd_ctx* ctx) {
   if (ctx->s_out) cudaStreamDestroy(ctx->s_out);
   if (ctx->s_cond) cudaStreamDestroy(ctx->s_cond);
   cudaFree(ctx->comp);
+  cudaFree(ctx->diag);
   cudaFree(ctx->phi);
   cudaFree(ctx->divb);
   cudaFree(ctx->bnd_part);
@@ -718,6 +723,13 @@ static void* field_ptr(gpumhd_ctx* ctx, int which, int* nf, int* rc) {
     }
     return a;
   }
+  if (which >= 11 && which <= 20) {  // diagnostics: tvar1..tvar8, Qres, Qvis
+    if (!ctx->diag) {
+      if (cudaMalloc(&ctx->diag, 10 * ctx->c.g.N * ctx->rsz) != cudaSuccess) { *rc = GPUMHD_E_NOMEM; return nullptr; }
+      cudaMemsetAsync(ctx->diag, 0, 10 * ctx->c.g.N * ctx->rsz, ctx->stream);
+    }
+    return (char*)ctx->diag + (size_t)(which - 11) * ctx->c.g.N * ctx->rsz;
+  }
   if (which >= 4 && which <= 7) {
     void*& a = ctx->aux[which - 4];
     if (!a) {
@@ -910,6 +922,19 @@ extern "C" int gpumhd_download(gpumhd_ctx* ctx, int which, double* host) {
 
 #define DISPATCH(call_f, call_d) (ctx->f32 ? (call_f) : (call_d))
 
+extern "C" int gpumhd_set_need_diagnostics(gpumhd_ctx* ctx, int on) {
+  if (!ctx) return GPUMHD_E_INVALID;
+  CK(cudaSetDevice(ctx->device));
+  if (on) {  // src/solver.C:271-289: the arrays start the output step at zero
+    int nf, rc;
+    field_ptr(ctx, 11, &nf, &rc);
+    if (rc) return fail(ctx, rc, "diagnostics allocation failed");
+    CK(cudaMemsetAsync(ctx->diag, 0, 10 * ctx->c.g.N * ctx->rsz, ctx->stream));
+  }
+  ctx->need_diag = on != 0;
+  return GPUMHD_OK;
+}
+
 extern "C" int gpumhd_save_cons(gpumhd_ctx* ctx) {
   if (!ctx) return GPUMHD_E_INVALID;
   CK(cudaSetDevice(ctx->device));
@@ -1020,6 +1045,17 @@ extern "C" int gpumhd_mhd_residual(gpumhd_ctx* ctx, double* dt_mhd) {
                           map_u(ctx, ctx->iU), map_p(ctx, ctx->iP));
     Launch<double>::cmax_faces(ctx->c, (const double*)ctx->S[ctx->iU], (const double*)ctx->P[ctx->iP], ctx->dyn, ctx->stream);
   }
+  if (ctx->need_diag) {  // tvar1..3 of the output step
+    if (ctx->f32)
+      Launch<float>::diag_residual(ctx->c, (const float*)ctx->S[ctx->iU], (const float*)ctx->P[ctx->iP],
+                                   ctx->c.has_spitzer ? (const float*)ctx->spt[0] : nullptr, (float*)ctx->diag,
+                                   ctx->dyn, ctx->stream);
+    else
+      Launch<double>::diag_residual(ctx->c, (const double*)ctx->S[ctx->iU], (const double*)ctx->P[ctx->iP],
+                                    ctx->c.has_spitzer ? (const double*)ctx->spt[0] : nullptr, (double*)ctx->diag,
+                                    ctx->dyn, ctx->stream);
+    nl += 1;
+  }
   rc = check_launch(ctx, nl);
   if (rc) return rc;
   rc = pull_dyn(ctx);
@@ -1067,12 +1103,15 @@ extern "C" int gpumhd_sync_timestep(gpumhd_ctx* ctx, double dt_rad, double dt_mh
 extern "C" int gpumhd_source_integrate_tcheck(gpumhd_ctx* ctx, int stage) {
   if (!ctx || stage < 1 || stage > 4) return GPUMHD_E_INVALID;
   CK(cudaSetDevice(ctx->device));
+  const double invdt = 1.0 / ctx->hdyn.dt;  // src/Add_Sources_Integrate_SR.C:84
   if (ctx->f32)
     Launch<float>::source_integrate(ctx->c, (float*)ctx->S[ctx->iU], (const float*)ctx->S[ctx->iU0],
-                                    (float*)ctx->S[ctx->iRes], ctx->dyn, stage, ctx->stream);
+                                    (float*)ctx->S[ctx->iRes], ctx->dyn, stage, ctx->stream,
+                                    ctx->need_diag ? (float*)ctx->diag : nullptr, (float)invdt);
   else
     Launch<double>::source_integrate(ctx->c, (double*)ctx->S[ctx->iU], (const double*)ctx->S[ctx->iU0],
-                                     (double*)ctx->S[ctx->iRes], ctx->dyn, stage, ctx->stream);
+                                     (double*)ctx->S[ctx->iRes], ctx->dyn, stage, ctx->stream,
+                                     ctx->need_diag ? (double*)ctx->diag : nullptr, invdt);
   int nl = 1;
   if (ctx->c.has_spitzer) {  // sflx = sflx0 + wdt*Rflx, Rflx = 0 (src/Add_Sources_Integrate_SR.C:410-419)
     int rc = ensure_spitzer(ctx);
@@ -1131,8 +1170,13 @@ extern "C" int gpumhd_boundary_info(gpumhd_ctx* ctx, double* p_bc, double* s_bc)
 extern "C" int gpumhd_tcheck(gpumhd_ctx* ctx) {
   if (!ctx) return GPUMHD_E_INVALID;
   CK(cudaSetDevice(ctx->device));
-  if (ctx->f32) Launch<float>::tcheck(ctx->c, (float*)ctx->S[ctx->iU], ctx->dyn, ctx->stream);
-  else Launch<double>::tcheck(ctx->c, (double*)ctx->S[ctx->iU], ctx->dyn, ctx->stream);
+  const double invdt = ctx->hdyn.dt > 0.0 ? 1.0 / ctx->hdyn.dt : 0.0;  // src/Add_Sources_Integrate_SR.C:560-564
+  if (ctx->f32)
+    Launch<float>::tcheck(ctx->c, (float*)ctx->S[ctx->iU], ctx->dyn, ctx->stream,
+                          ctx->need_diag ? (float*)ctx->diag : nullptr, (float)invdt);
+  else
+    Launch<double>::tcheck(ctx->c, (double*)ctx->S[ctx->iU], ctx->dyn, ctx->stream,
+                           ctx->need_diag ? (double*)ctx->diag : nullptr, invdt);
   return check_launch(ctx, 1);
 }
 
@@ -1198,12 +1242,16 @@ extern "C" int gpumhd_tvdlimit(gpumhd_ctx* ctx, double dt_tvd) {
   if (rc) return rc;
   for (int d = 0; d < 3; d++) {
     CK(cudaMemcpyAsync(ctx->T, ctx->S[ctx->iU], 8 * N * ctx->rsz, cudaMemcpyDeviceToDevice, ctx->stream));
+    // an output step's diagnostics (src/tvdlimit_SR.C:115-116): per unit of the full step's time
+    const double idt_full = 1.0 / ctx->hdyn.dt, dt_fac = dt_tvd / ctx->hdyn.dt;
+    const TvdDiag<float> dgf{(float*)ctx->diag, (float)idt_full, (float)dt_fac};
+    const TvdDiag<double> dgd{(double*)ctx->diag, idt_full, dt_fac};
     if (ctx->f32)
       Launch<float>::tvd(ctx->c, d, 0, 0, (const float*)ctx->T, (const float*)ctx->P[ctx->iP], (float*)ctx->S[ctx->iU],
-                         ctx->dyn, ctx->stream);
+                         ctx->dyn, ctx->stream, 0, ctx->need_diag ? &dgf : nullptr);
     else
       Launch<double>::tvd(ctx->c, d, 0, 0, (const double*)ctx->T, (const double*)ctx->P[ctx->iP],
-                          (double*)ctx->S[ctx->iU], ctx->dyn, ctx->stream);
+                          (double*)ctx->S[ctx->iU], ctx->dyn, ctx->stream, 0, ctx->need_diag ? &dgd : nullptr);
     rc = check_launch(ctx, 1);
     if (rc) return rc;
   }
@@ -1437,6 +1485,9 @@ static int enqueue_one_step(gpumhd_ctx* ctx, cudaEvent_t* ev = nullptr) {
 
 static int fused_prepare(gpumhd_ctx* ctx, int nsteps) {
   if (!ctx->eos_loaded) return fail(ctx, GPUMHD_E_ORDER, "time steps before eos_init");
+  if (ctx->need_diag)
+    return fail(ctx, GPUMHD_E_INVALID, "an output step's diagnostics come from the per-routine calls; "
+                "switch them off (gpumhd_set_need_diagnostics) before fused steps");
   if (nsteps > ctx->dt_hist_cap) {
     if (ctx->graph) { cudaGraphExecDestroy(ctx->graph); ctx->graph = nullptr; }
     cudaFree(ctx->dt_hist);

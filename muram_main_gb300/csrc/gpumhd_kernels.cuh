@@ -688,6 +688,15 @@ struct TvdArgs {
   int n1;                // interior cells along the sweep
 };
 
+// An output step's TVDlimit diagnostics (src/tvdlimit_SR.C:577-667): the ten
+// diagnostic arrays (tvar1..tvar8, Qres, Qvis; N each), 1 / Run.dt and
+// dt_tvd / Run.dt.
+template <class R>
+struct TvdDiag {
+  R* d;
+  R idt_full, dt_fac;
+};
+
 // Per-cell quantities from the cell's stored values r (state and pressure)
 // and its vertical boundary profiles hb, ht, qt.
 template <class R>
@@ -786,10 +795,10 @@ __device__ __forceinline__ void tvd_slope(const Consts& c, const TCell<R>& a, co
 // Interface flux between cells a (index ia) and b, plus its resistive-heating
 // term (src/tvdlimit_SR.C:436-557, 559-563, 608-614).  am = cell left of a,
 // bp = cell right of b (hyperdiffusion stencil).
-template <class R, int DIR>
+template <class R, int DIR, bool DIAG = false>
 __device__ __forceinline__ void tvd_flux(const Consts& c, const TCell<R>& am, const TCell<R>& a, const TCell<R>& b,
                                          const TCell<R>& bp, const R* sa, const R* sb, int ia, int sz, R fac0,
-                                         R cmax_t, bool hyper, int istart, R* F, R& qres) {
+                                         R cmax_t, bool hyper, int istart, R* F, R& qres, R* qvis = nullptr) {
 #pragma unroll
   for (int v = 0; v < NV; v++) {
     R sl = b.q[v] - a.q[v];
@@ -841,20 +850,28 @@ __device__ __forceinline__ void tvd_flux(const Consts& c, const TCell<R>& am, co
     if (ia == GH - 1) F[5] = (R)0.0;
   }
   qres = (b.q[5] - a.q[5]) * F[5] + (b.q[6] - a.q[6]) * F[6] + (b.q[7] - a.q[7]) * F[7];
+  // viscous heating at the interface, for the diagnostics (src/tvdlimit_SR.C:626-635)
+  if (DIAG) *qvis = (b.q[1] - a.q[1]) * F[1] + (b.q[2] - a.q[2]) * F[2] + (b.q[3] - a.q[3]) * F[3];
 }
 
 // Update of one cell by a TVD sweep (src/tvdlimit_SR.C:565-657): the flux
 // difference, its kinetic-energy and Boris parts, the resistive heating, and
 // the density and energy floors.  u_in: the cell's stored state; Fp / Fm: the
 // fluxes at its right / left interfaces, qp / qm their heating terms.
-template <class R>
+// DIAG (an output step): the sweep's diagnostics of cell id accumulate in
+// dg (src/tvdlimit_SR.C:577-584, 601-604, 617-624, 659-667); qvp / qvm: the
+// viscous heating terms of its right / left interfaces.
+template <class R, bool DIAG = false>
 __device__ __forceinline__ void tvd_update(const Consts& c, R dtt, const R* Fp, const R* Fm, R qp, R qm,
-                                           const TCell<R>& c0, const R* u_in, R* u) {
+                                           const TCell<R>& c0, const R* u_in, R* u, const TvdDiag<R>* dg = nullptr,
+                                           long long id = 0, R qvp = (R)0, R qvm = (R)0) {
   const auto& kk_ = kc<R>(c);
+  const long long N = c.g.N;
   R res[NV];
 #pragma unroll
   for (int v = 0; v < NV; v++) res[v] = dtt * (Fp[v] - Fm[v]);
   res[4] += ((R)1.0 - c0.qt) * (res[1] * c0.q[1] + res[2] * c0.q[2] + res[3] * c0.q[3]);
+  if (DIAG) dg->d[7 * N + id] += res[4] * dg->idt_full;
   {
     R dn = (res[1] * c0.q[5] + res[2] * c0.q[6] + res[3] * c0.q[7]) / smax(tiny100<R>(), c0.bsqr);
     R b0 = -c0.BC2 * (res[1] - dn * c0.q[5]);
@@ -862,15 +879,22 @@ __device__ __forceinline__ void tvd_update(const Consts& c, R dtt, const R* Fp, 
     R b2 = -c0.BC2 * (res[3] - dn * c0.q[7]);
     R b3 = b0 * c0.q[1] + b1 * c0.q[2] + b2 * c0.q[3];
     res[1] += b0; res[2] += b1; res[3] += b2; res[4] += b3;
+    if (DIAG) dg->d[5 * N + id] += b3 * dg->idt_full;
   }
   {
     R qres = (R)0.5 * (qp + qm) * c0.qt;
     res[4] += dtt * qres;
+    if (DIAG) dg->d[8 * N + id] += dg->dt_fac * qres;
   }
 #pragma unroll
   for (int v = 0; v < NV; v++) u[v] = u_in[v] + res[v];
   u[0] = smax((R)kk_.rho_min, u[0]);
+  const R eb = u[4];
   u[4] = smax(u[4], kk_.eps_min * u[0] + (R)0.5 * (u[1] * u[1] + u[2] * u[2] + u[3] * u[3]) / u[0]);
+  if (DIAG) {
+    dg->d[6 * N + id] += (u[4] - eb) * dg->idt_full;
+    dg->d[9 * N + id] += dg->dt_fac * ((R)0.5 * (qvp + qvm) * c0.qt);
+  }
 }
 
 // The end of a step for one interior cell with its updated state u: TCheck,
@@ -1010,9 +1034,10 @@ __global__ void __launch_bounds__(FIN_BX* FIN_BY, FinBlocks<R>::v) k_step_finish
 // few spilled), the x sweep 0.623 -> 0.603 ms with 6 (85 registers).
 template <class R> struct TvdBlocks { static constexpr int pencil = sizeof(R) == 4 ? 4 : 1, lanes = sizeof(R) == 4 ? 6 : 1; };
 
-template <class R, int DIR>
+template <class R, int DIR, bool DIAG = false>
 __global__ void __launch_bounds__(128, TvdBlocks<R>::pencil) k_tvd_sweep(Consts c, const R* __restrict__ Uin, const R* __restrict__ Pst,
-                                                   R* __restrict__ Uout, Dyn* __restrict__ dyn, TvdArgs ta) {
+                                                   R* __restrict__ Uout, Dyn* __restrict__ dyn, TvdArgs ta,
+                                                   TvdDiag<R> dg) {
   const Geom& g = c.g;
   if (dyn->err) return;
   if (ta.only_two_half && !dyn->two_half) return;   // second half pass not taken this step
@@ -1050,6 +1075,7 @@ __global__ void __launch_bounds__(128, TvdBlocks<R>::pencil) k_tvd_sweep(Consts 
     TCell<R> cm1, c0, c1, c2;
     R s0[NV], s1[NV], Fm[NV], F0[NV];
     R qm, q0;
+    R qvm = (R)0, qv0 = (R)0;  // viscous heating at the interfaces (diagnostics)
     {
       TCell<R> cmm;
       tvd_load<R>(c, Uin, Pst, base + (long long)(p0 - 2) * ta.sd, xi_of(p0 - 2), cmax_t, fac0, hyper, inv_va2max, cmm);
@@ -1059,7 +1085,7 @@ __global__ void __launch_bounds__(128, TvdBlocks<R>::pencil) k_tvd_sweep(Consts 
       R sm[NV];
       tvd_slope<R>(c, cmm, cm1, c0, vsqr_diff, sm);
       tvd_slope<R>(c, cm1, c0, c1, vsqr_diff, s0);
-      tvd_flux<R, DIR>(c, cmm, cm1, c0, c1, sm, s0, p0 - 1, sz, fac0, cmax_t, hyper, istart, Fm, qm);
+      tvd_flux<R, DIR, DIAG>(c, cmm, cm1, c0, c1, sm, s0, p0 - 1, sz, fac0, cmax_t, hyper, istart, Fm, qm, &qvm);
     }
     // the boundary profiles depend on x only: fixed along a y or z pencil
     R hb_f = (R)0, ht_f = (R)0, qt_f = (R)0;
@@ -1078,10 +1104,10 @@ __global__ void __launch_bounds__(128, TvdBlocks<R>::pencil) k_tvd_sweep(Consts 
         tvd_cell<R>(c, nxt, hb_f, ht_f, qt_f, cmax_t, fac0, hyper, inv_va2max, c2);
       if (pos + 1 < p1) load_raw64<R>(g, Uin, Pst, base + (long long)(pos + 3) * ta.sd, nxt);
       tvd_slope<R>(c, c0, c1, c2, vsqr_diff, s1);
-      tvd_flux<R, DIR>(c, cm1, c0, c1, c2, s0, s1, pos, sz, fac0, cmax_t, hyper, istart, F0, q0);
+      tvd_flux<R, DIR, DIAG>(c, cm1, c0, c1, c2, s0, s1, pos, sz, fac0, cmax_t, hyper, istart, F0, q0, &qv0);
       // update of cell pos (src/tvdlimit_SR.C:565-657)
       R u[NV];
-      tvd_update<R>(c, dtt, F0, Fm, q0, qm, c0, uc, u);
+      tvd_update<R, DIAG>(c, dtt, F0, Fm, q0, qm, c0, uc, u, &dg, id, qv0, qvm);
       if (!half_images) {
 #pragma unroll
         for (int v = 0; v < NV; v++) Uout[(long long)v * g.N + id] = u[v];
@@ -1095,6 +1121,7 @@ __global__ void __launch_bounds__(128, TvdBlocks<R>::pencil) k_tvd_sweep(Consts 
 #pragma unroll
       for (int v = 0; v < NV; v++) { s0[v] = s1[v]; Fm[v] = F0[v]; }
       qm = q0;
+      qvm = qv0;
     }
   }
 }
@@ -1284,6 +1311,81 @@ __global__ void k_adjust_stats(Consts c, const R* __restrict__ U, const R* __res
   }
 }
 
+// MHD_Residual's diagnostics on an output step (src/mhdres_SR.C:368-384,
+// 434-435, 689-702, 751-752), per interior cell and direction in the
+// residual's order x, y, z: tvar1 += the energy-flux divergence (without the
+// conduction share, which goes to tvar2) and tvar3 += the work of the
+// Boris-blended Lorentz force, each formed as the residual forms it (the same
+// flux, derivative and blend functions).  U: primitives as ConsToPrim leaves
+// them; P: the pressure; S: the heat flux (null without conduction); diag:
+// tvar1..3 at 0, N, 2N.
+template <class R>
+__global__ void __launch_bounds__(256) k_diag_residual(Consts c, const R* __restrict__ U, const R* __restrict__ P,
+                                                       const R* __restrict__ S, R* __restrict__ diag,
+                                                       const Dyn* __restrict__ dyn) {
+  const Geom& g = c.g;
+  const unsigned n = (unsigned)g.nx * (unsigned)g.ny * (unsigned)g.nz, N = g.N32;
+  const KC<R>& k = kc<R>(c);
+  const R inv_va2max = dynr<R>(dyn).inv_va2max;
+  for (unsigned t = gs_first(); t < n; t += gs_step()) {
+    int i, j, kk;
+    interior_ijk(g, t, i, j, kk);
+    const unsigned id = cidx32(g, i, j, kk);
+    Raw9<R> r;
+    load_raw(g, U, P, id, r);
+    R cen[NF];
+    prim_of_raw<R, true>(r, cen);
+    cen[NPRIM] = (R)0;
+    const R lf = boris_lf<R>(cen, inv_va2max);
+    R t1 = diag[id], t2 = diag[N + id], t3 = diag[2 * N + id];
+    auto direction = [&](auto dim) {
+      constexpr int D1 = decltype(dim)::value;
+      const unsigned sd = D1 == 0 ? 1u : (D1 == 1 ? (unsigned)g.sx : (unsigned)g.sx * (unsigned)g.sy);
+      const unsigned nb[4] = {id - 2 * sd, id - sd, id + sd, id + 2 * sd};  // c-2, c-1, c+1, c+2
+      R fl[4][NF], sb[4];
+#pragma unroll
+      for (int m = 0; m < 4; m++) {
+        Raw9<R> rm;
+        load_raw(g, U, P, nb[m], rm);
+        R pm[NF];
+        prim_of_raw<R, true>(rm, pm);
+        pm[NPRIM] = (R)0;
+        flux12<R, D1>(pm, 1, fl[m], 1);
+        sb[m] = S ? S[nb[m]] * pm[P_B1 + D1] : (R)0;
+      }
+      R Dq[NF];
+      deriv12(Dq, fl[0], fl[1], fl[2], fl[3], k.w1[D1], k.w2[D1]);
+      const R w1 = k.w1[D1], w2 = k.w2[D1];
+      if (S) {  // the reference's energy flux carries sflx * B_d
+        const R f0 = fl[0][4] + sb[0], f1 = fl[1][4] + sb[1], f2 = fl[2][4] + sb[2], f3 = fl[3][4] + sb[3];
+        const R r4 = (R)0.0 - (w1 * (f2 - f1) + w2 * (f3 - f0));
+        const R dn = -(w1 * (sb[2] - sb[1]) + w2 * (sb[3] - sb[0]));
+        t1 += r4 - dn;
+        t2 += dn;
+      } else {
+        t1 += (R)0.0 - Dq[4];
+      }
+      const R dB2 = Dq[10], dB3 = Dq[11];
+      const R Bd1 = cen[P_B1 + D1];
+      const R Bd2 = cen[P_B1 + Dirs<D1>::d2], Bd3 = cen[P_B1 + Dirs<D1>::d3];
+      R cbb[3];
+      cbb[D1] = -Bd2 * dB2 - Bd3 * dB3;
+      cbb[Dirs<D1>::d2] = Bd1 * dB2;
+      cbb[Dirs<D1>::d3] = Bd1 * dB3;
+      const R lrt0 = lf * Dq[7] + ((R)1.0 - lf) * cbb[0];
+      const R lrt1 = lf * Dq[8] + ((R)1.0 - lf) * cbb[1];
+      const R lrt2 = lf * Dq[9] + ((R)1.0 - lf) * cbb[2];
+      t3 += cen[P_V1] * lrt0 + cen[P_V2] * lrt1 + cen[P_V3] * lrt2;
+    };
+    direction(std::integral_constant<int, 0>());
+    direction(std::integral_constant<int, 1>());
+    direction(std::integral_constant<int, 2>());
+    diag[id] = t1;
+    diag[N + id] = t2;
+    diag[2 * N + id] = t3;
+  }
+}
+
 // Stage-1 CFL speed of a conserved state over the interior, with the limits
 // the step's Adjust_Valf_Max has just set (MHD_Residual's cmax from
 // ConsToPrim's velocities, src/cons_to_prim.C:148-159, src/mhdres_SR.C:
@@ -1341,9 +1443,12 @@ __global__ void k_cmax_faces(Consts c, const R* __restrict__ U, const R* __restr
 }
 
 // Source_Integrate_Tcheck (src/Add_Sources_Integrate_SR.C:297-467) on a primitive U.
+// diag (an output step, else null): tvar4 = the radiation factor, tvar5 = the
+// gravity work, tvar6 = the Boris correction's energy, tvar7 += Tcheck's
+// energy change * invdt (src/Add_Sources_Integrate_SR.C:122-296).
 template <class R>
 __global__ void __launch_bounds__(256, EwBlocks<R>::v) k_source_integrate(Consts c, R* __restrict__ U, const R* __restrict__ U0, R* __restrict__ Res,
-                                   const Dyn* __restrict__ dyn, int stage) {
+                                   const Dyn* __restrict__ dyn, int stage, R* __restrict__ diag, R invdt) {
   const Geom& g = c.g;
   const unsigned n = (unsigned)g.nx * (unsigned)g.ny * (unsigned)g.nz, N = g.N32;
   const DynR<R>& dr = dynr<R>(dyn);
@@ -1384,7 +1489,14 @@ __global__ void __launch_bounds__(256, EwBlocks<R>::v) k_source_integrate(Consts
       un[v] = U0[(unsigned)v * N + id] + wdt * r[v];
       Res[(unsigned)v * N + id] = (R)0;
     }
+    const R ee = un[4];
     tcheck_cell<R>(c, vmax, emax, un[0], un[1], un[2], un[3], un[4]);
+    if (diag) {
+      diag[3 * N + id] = efaci;
+      diag[4 * N + id] = edmp;
+      diag[5 * N + id] = b3;
+      diag[6 * N + id] += (un[4] - ee) * invdt;
+    }
 #pragma unroll
     for (int v = 0; v < NV; v++) U[(unsigned)v * N + id] = un[v];
   }
@@ -1402,8 +1514,10 @@ __global__ void k_save_cons(Geom g, const R* __restrict__ U, R* __restrict__ U0)
   }
 }
 
+// diag (an output step, else null): tvar7 += the energy change * invdt
+// (src/Add_Sources_Integrate_SR.C:560-564, 618-620).
 template <class R>
-__global__ void k_tcheck(Consts c, R* __restrict__ U, const Dyn* __restrict__ dyn) {
+__global__ void k_tcheck(Consts c, R* __restrict__ U, const Dyn* __restrict__ dyn, R* __restrict__ diag, R invdt) {
   const Geom& g = c.g;
   const unsigned n = (unsigned)g.nx * (unsigned)g.ny * (unsigned)g.nz, N = g.N32;
   const R vmax = dynr<R>(dyn).vmax;
@@ -1413,8 +1527,10 @@ __global__ void k_tcheck(Consts c, R* __restrict__ U, const Dyn* __restrict__ dy
     interior_ijk(g, t, i, j, k);
     const unsigned id = cidx32(g, i, j, k);
     R d = U[id], m1 = U[N + id], m2 = U[2 * N + id], m3 = U[3 * N + id], e = U[4 * N + id];
+    const R eei = e;
     tcheck_cell<R>(c, vmax, emax, d, m1, m2, m3, e);
     U[id] = d; U[N + id] = m1; U[2 * N + id] = m2; U[3 * N + id] = m3; U[4 * N + id] = e;
+    if (diag) diag[6 * N + id] += (e - eei) * invdt;
   }
 }
 

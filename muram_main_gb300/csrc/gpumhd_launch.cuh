@@ -44,8 +44,10 @@ struct Launch {
   // td: cells per thread along the y / z sweeps (0: 32); the sweeps store the
   // interior (and after a first half pass the periodic images), step_finish
   // then ends the step
+  // dg (per-routine TVDlimit on an output step): the diagnostics, through the
+  // pencil kernel in every direction
   static void tvd(const Consts& c, int dir, int mode, int only_two_half, const R* Uin, const R* Pst, R* Uout,
-                  Dyn* dyn, cudaStream_t s, int td = 0);
+                  Dyn* dyn, cudaStream_t s, int td = 0, const TvdDiag<R>* dg = nullptr);
   // Clean_divB on U (phi, divb: N each); returns the number of launches
   static int divb_clean(const Consts& c, R* U, R* phi, R* divb, Dyn* dyn, cudaStream_t s);
   static void step_finish(const Consts& c, R* U, R* P, Dyn* dyn, cudaStream_t s);
@@ -67,9 +69,14 @@ struct Launch {
   static void cmax_faces(const Consts& c, const R* U, const R* P, Dyn* dyn, cudaStream_t s);
   // interior CFL speed of a conserved state with the step's limits (adaptive limits only)
   static void cfl_cons(const Consts& c, const R* U, const R* P, Dyn* dyn, cudaStream_t s);
-  static void source_integrate(const Consts& c, R* U, const R* U0, R* Res, const Dyn* dyn, int stage, cudaStream_t s);
+  // diag (an output step, else null): tvar1..Qvis, N each; invdt = 1 / Run.dt
+  static void source_integrate(const Consts& c, R* U, const R* U0, R* Res, const Dyn* dyn, int stage, cudaStream_t s,
+                               R* diag = nullptr, R invdt = (R)0);
   static void save_cons(const Consts& c, const R* U, R* U0, cudaStream_t s);
-  static void tcheck(const Consts& c, R* U, const Dyn* dyn, cudaStream_t s);
+  static void tcheck(const Consts& c, R* U, const Dyn* dyn, cudaStream_t s, R* diag = nullptr, R invdt = (R)0);
+  // MHD_Residual's diagnostics (tvar1..3) of a primitive state
+  static void diag_residual(const Consts& c, const R* U, const R* P, const R* S, R* diag, const Dyn* dyn,
+                            cudaStream_t s);
   static void fill_ghosts(const Consts& c, R* U, int nfield, int with_bc, cudaStream_t s);
   static void tile_state(const Geom& gd, const Geom& gs, const R* Us, R* Ud, cudaStream_t s);
   static void aos_to_soa(long long N, int nf, const double* A, R* S, cudaStream_t s);
@@ -207,7 +214,7 @@ void Launch<R>::stage(const Consts& c, const R* Uin, const R* Pin, const R* U0, 
 
 template <class R>
 void Launch<R>::tvd(const Consts& c, int dir, int mode, int only_two_half, const R* Uin, const R* Pst, R* Uout,
-                    Dyn* dyn, cudaStream_t s, int td) {
+                    Dyn* dyn, cudaStream_t s, int td, const TvdDiag<R>* dg) {
   const Geom& g = c.g;
   TvdArgs ta;
   ta.dir = dir;
@@ -233,6 +240,13 @@ void Launch<R>::tvd(const Consts& c, int dir, int mode, int only_two_half, const
   const long long total = (long long)ta.na * ta.nb * nch;
   const int block = 128;
   const long long blocks = (total + block - 1) / block;
+  if (dg) {
+    if (dir == 0) k_tvd_sweep<R, 0, true><<<(unsigned)blocks, block, 0, s>>>(c, Uin, Pst, Uout, dyn, ta, *dg);
+    else if (dir == 1) k_tvd_sweep<R, 1, true><<<(unsigned)blocks, block, 0, s>>>(c, Uin, Pst, Uout, dyn, ta, *dg);
+    else k_tvd_sweep<R, 2, true><<<(unsigned)blocks, block, 0, s>>>(c, Uin, Pst, Uout, dyn, ta, *dg);
+    return;
+  }
+  const TvdDiag<R> nod{nullptr, (R)0, (R)0};
   if (dir == 0 && mode == 0) {
     // contiguous pencils: one cell per lane, 28 updates per warp
     const long long warps = (long long)g.sy * g.sz * ((g.nx + 27) / 28);
@@ -241,9 +255,9 @@ void Launch<R>::tvd(const Consts& c, int dir, int mode, int only_two_half, const
     k_tvd_sweep_xlanes<R><<<(unsigned)nb, block, 0, s>>>(c, Uin, Pst, Uout, dyn, only_two_half);
     return;
   }
-  if (dir == 0) k_tvd_sweep<R, 0><<<(unsigned)blocks, block, 0, s>>>(c, Uin, Pst, Uout, dyn, ta);
-  else if (dir == 1) k_tvd_sweep<R, 1><<<(unsigned)blocks, block, 0, s>>>(c, Uin, Pst, Uout, dyn, ta);
-  else k_tvd_sweep<R, 2><<<(unsigned)blocks, block, 0, s>>>(c, Uin, Pst, Uout, dyn, ta);
+  if (dir == 0) k_tvd_sweep<R, 0><<<(unsigned)blocks, block, 0, s>>>(c, Uin, Pst, Uout, dyn, ta, nod);
+  else if (dir == 1) k_tvd_sweep<R, 1><<<(unsigned)blocks, block, 0, s>>>(c, Uin, Pst, Uout, dyn, ta, nod);
+  else k_tvd_sweep<R, 2><<<(unsigned)blocks, block, 0, s>>>(c, Uin, Pst, Uout, dyn, ta, nod);
 }
 
 template <class R>
@@ -335,18 +349,24 @@ void Launch<R>::cfl_cons(const Consts& c, const R* U, const R* P, Dyn* dyn, cuda
   k_cfl_cons<R><<<grid_for(n, 256), 256, 0, s>>>(c, U, P, dyn);
 }
 template <class R>
-void Launch<R>::source_integrate(const Consts& c, R* U, const R* U0, R* Res, const Dyn* dyn, int stage, cudaStream_t s) {
+void Launch<R>::source_integrate(const Consts& c, R* U, const R* U0, R* Res, const Dyn* dyn, int stage, cudaStream_t s,
+                                 R* diag, R invdt) {
   // one cell per thread: more loads in flight than a capped grid-stride loop (0.93 against 1.14 ms at 18.9 M cells)
   const long long n = (long long)c.g.nx * c.g.ny * c.g.nz;
-  k_source_integrate<R><<<(int)((n + 255) / 256), 256, 0, s>>>(c, U, U0, Res, dyn, stage);
+  k_source_integrate<R><<<(int)((n + 255) / 256), 256, 0, s>>>(c, U, U0, Res, dyn, stage, diag, invdt);
 }
 template <class R>
 void Launch<R>::save_cons(const Consts& c, const R* U, R* U0, cudaStream_t s) {
   k_save_cons<R><<<grid_for((long long)c.g.nx * c.g.ny * c.g.nz, 256), 256, 0, s>>>(c.g, U, U0);
 }
 template <class R>
-void Launch<R>::tcheck(const Consts& c, R* U, const Dyn* dyn, cudaStream_t s) {
-  k_tcheck<R><<<grid_for((long long)c.g.nx * c.g.ny * c.g.nz, 256), 256, 0, s>>>(c, U, dyn);
+void Launch<R>::tcheck(const Consts& c, R* U, const Dyn* dyn, cudaStream_t s, R* diag, R invdt) {
+  k_tcheck<R><<<grid_for((long long)c.g.nx * c.g.ny * c.g.nz, 256), 256, 0, s>>>(c, U, dyn, diag, invdt);
+}
+template <class R>
+void Launch<R>::diag_residual(const Consts& c, const R* U, const R* P, const R* S, R* diag, const Dyn* dyn,
+                              cudaStream_t s) {
+  k_diag_residual<R><<<grid_for((long long)c.g.nx * c.g.ny * c.g.nz, 256), 256, 0, s>>>(c, U, P, S, diag, dyn);
 }
 template <class R>
 void Launch<R>::tile_state(const Geom& gd, const Geom& gs, const R* Us, R* Ud, cudaStream_t s) {

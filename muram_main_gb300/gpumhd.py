@@ -30,6 +30,9 @@ E_NOMEM = -7
 
 (FIELD_U, FIELD_U0, FIELD_RES, FIELD_PRES, FIELD_TEMP, FIELD_NE, FIELD_RHOI, FIELD_AMB, FIELD_PHI, FIELD_DIVB,
  FIELD_SFLX) = range(11)
+# an output step's diagnostics: tvar1..tvar8, Qres, Qvis
+FIELD_DIAG = 11
+DIAG_NAMES = ("tvar1", "tvar2", "tvar3", "tvar4", "tvar5", "tvar6", "tvar7", "tvar8", "Qres", "Qvis")
 
 
 class GpumhdError(RuntimeError):
@@ -71,7 +74,7 @@ EXPORTS = [
     "gpumhd_ensemble_destroy", "gpumhd_ensemble_enqueue_steps", "gpumhd_ensemble_synchronize",
     "gpumhd_ensemble_last_error", "gpumhd_ensemble_stream", "gpumhd_ensemble_launch_count",
     "gpumhd_clean_divB", "gpumhd_divb_info", "gpumhd_boundary_info", "gpumhd_test_tma_wait",
-    "gpumhd_set_divb_iters",
+    "gpumhd_set_divb_iters", "gpumhd_set_need_diagnostics",
 ]
 
 _lib = None
@@ -141,6 +144,7 @@ def load(build_if_missing=True):
         "gpumhd_boundary_info": (C.c_int, [vp, dp, dp]),
         "gpumhd_test_tma_wait": (C.c_int, [vp, C.c_longlong, C.c_int]),
         "gpumhd_set_divb_iters": (C.c_int, [vp, C.c_int]),
+        "gpumhd_set_need_diagnostics": (C.c_int, [vp, C.c_int]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -231,6 +235,15 @@ class MuramGPU:
     def eos_init(self, path):
         self._chk(self._L.gpumhd_eos_init(self._h, os.fsencode(path)))
 
+    def set_need_diagnostics(self, on):
+        """RunData::need_diagnostics: on zeroes the ten diagnostic arrays, which
+        the per-routine calls that follow fill (an output step)."""
+        self._chk(self._L.gpumhd_set_need_diagnostics(self._h, 1 if on else 0))
+
+    def download_diagnostics(self):
+        """tvar1..tvar8, Qres, Qvis as one (10, sz, sy, sx) array."""
+        return np.stack([self.download_field(FIELD_DIAG + q) for q in range(10)])
+
     def SaveCons(self):
         self._chk(self._L.gpumhd_save_cons(self._h))
 
@@ -288,9 +301,11 @@ class MuramGPU:
         self._chk(self._L.gpumhd_divb_info(self._h, C.byref(a), C.byref(b), C.byref(e0), C.byref(e1)))
         return a.value, b.value, e0.value, e1.value
 
-    def step_reference_order(self, dt_rad=None):
+    def step_reference_order(self, dt_rad=None, diagnostics=False):
         """One step through the per-routine entry points in ComputeSolution's
-        order (src/solver.C:109-365); returns (dt, cfl)."""
+        order (src/solver.C:109-365); returns (dt, cfl).  diagnostics: an
+        output step, whose diagnostics (need_diagnostics from stage 4 through
+        TCheck) are left in the diagnostic arrays."""
         p = self.params
         dt_rad = p.dt_rad if dt_rad is None else dt_rad
         cfl = 0.0
@@ -299,6 +314,8 @@ class MuramGPU:
             self.ConsToPrim()
             if stage == 1:
                 self.Adjust_Valf_Max()
+            if stage == 4 and diagnostics:
+                self.set_need_diagnostics(True)
             dt_mhd = self.MHD_Residual()
             if stage == 1:
                 cfl = self.Sync_timestep(dt_rad, dt_mhd)
@@ -314,6 +331,8 @@ class MuramGPU:
         if p.divB_switch > 0:
             self.Clean_divB()
         self.TCheck()
+        if diagnostics:
+            self.set_need_diagnostics(False)
         self.exchange_grid(True)
         return dt, cfl
 

@@ -108,6 +108,17 @@ void fill_params(gpumhd_params& p, const RunData& Run, const GridData& Grid, con
 const RunData* g_run = nullptr;
 const PhysicsData* g_phys = nullptr;
 double g_dt = -1.0, g_time = -1.0;
+int g_need_diag = 0;
+
+// Run.need_diagnostics (set by ComputeSolution per stage, src/solver.C:264-289):
+// switching it on zeroes the diagnostic arrays as the reference does there.
+void sync_diagnostics(gpumhd_ctx* c, const RunData& Run) {
+  const int on = Run.need_diagnostics ? 1 : 0;
+  if (on != g_need_diag) {
+    check("need_diagnostics", gpumhd_set_need_diagnostics(c, on));
+    g_need_diag = on;
+  }
+}
 
 // The run parameters the device needs change only through Run.dt / Run.time
 // (Sync_timestep, Run.Advance); push them when they did.
@@ -139,7 +150,7 @@ extern "C" void GPUMHD_CAT(__real_, GPUMHD_EOS_INIT_MANGLED)(GridData&, RunData&
 extern "C" void GPUMHD_CAT(__wrap_, GPUMHD_EOS_INIT_MANGLED)(GridData& Grid, RunData& Run,
                                                             const PhysicsData& Physics) {
   GPUMHD_CAT(__real_, GPUMHD_EOS_INIT_MANGLED)(Grid, Run, Physics);
-  if (Physics.params[i_param_ambipolar] > 0 || Physics.bnd[i_bnd_pot] > 0 || Run.diagnostics || Physics.dmp[i_dmp_switch] > 0 ||
+  if (Physics.params[i_param_ambipolar] > 0 || Physics.bnd[i_bnd_pot] > 0 || Physics.dmp[i_dmp_switch] > 0 ||
       Physics.rt_ext[i_ext_cor] > 0 || Grid.procs[0] * Grid.procs[1] * Grid.procs[2] != 1) {
     fprintf(stderr, "gpumhd: configuration outside the GPU path\n");
     MPI_Abort(MPI_COMM_WORLD, 1);
@@ -178,21 +189,29 @@ double lfac(double va2) {  // include/limit_va.H:9
 
 double MHD_Residual(const RunData& Run, GridData& Grid, const PhysicsData& Physics) {  // include/mhd_tvd.H:5
   double dt_mhd = 0.0;
-  check("MHD_Residual", gpumhd_mhd_residual(ctx(), &dt_mhd));
+  gpumhd_ctx* c = ctx();
+  sync_diagnostics(c, Run);
+  check("MHD_Residual", gpumhd_mhd_residual(c, &dt_mhd));
   return dt_mhd;
 }
 
 void Source_Integrate_Tcheck(const RunData& Run, GridData& Grid, const PhysicsData& Physics,
                              const int stage) {  // include/src_int_tck.H:8-9
-  check("Source_Integrate_Tcheck", gpumhd_source_integrate_tcheck(ctx(), stage));
+  gpumhd_ctx* c = ctx();
+  sync_diagnostics(c, Run);
+  check("Source_Integrate_Tcheck", gpumhd_source_integrate_tcheck(c, stage));
 }
 
 void TVDlimit(const RunData& Run, GridData& Grid, const PhysicsData& Physics, const double dt_tvd) {  // include/mhd_tvd.H:6
-  check("TVDlimit", gpumhd_tvdlimit(ctx(), dt_tvd));
+  gpumhd_ctx* c = ctx();
+  sync_diagnostics(c, Run);
+  check("TVDlimit", gpumhd_tvdlimit(c, dt_tvd));
 }
 
 void TCheck(const RunData& Run, GridData& Grid, const PhysicsData& Physics) {  // include/src_int_tck.H:7
-  check("TCheck", gpumhd_tcheck(ctx()));
+  gpumhd_ctx* c = ctx();
+  sync_diagnostics(c, Run);
+  check("TCheck", gpumhd_tcheck(c));
 }
 
 void Clean_divB(const RunData& Run, GridData& Grid, const PhysicsData& Physics) {  // include/divB.H:5
@@ -230,6 +249,12 @@ void UpdateCPU(void* ptr, std::size_t) {
   else if (ptr == g_grid->phi) check("download phi", gpumhd_download(g_ctx, 8, (double*)ptr));
   else if (ptr == g_grid->divB) check("download divB", gpumhd_download(g_ctx, 9, (double*)ptr));
   else if (g_grid->sflx && ptr == g_grid->sflx) check("download sflx", gpumhd_download(g_ctx, 10, (double*)ptr));
+  else {  // the diagnostics of an output step (solver.C:162-172): tvar1..tvar8, Qres, Qvis
+    double* const dg[10] = {g_grid->tvar1, g_grid->tvar2, g_grid->tvar3, g_grid->tvar4, g_grid->tvar5,
+                            g_grid->tvar6, g_grid->tvar7, g_grid->tvar8, g_grid->Qres, g_grid->Qvis};
+    for (int q = 0; q < 10; q++)
+      if (dg[q] && ptr == dg[q]) check("download diagnostics", gpumhd_download(g_ctx, 11 + q, (double*)ptr));
+  }
 }
 void UpdateGPU(void* ptr, std::size_t) {
   if (!g_ctx || !g_grid) return;

@@ -338,6 +338,7 @@ double mo_mhd_residual_ex(const mo_params* p, const double* U, const double* pre
     nu_hyp_max = avr_max * cmax_hyp / (smin(p->CFL, CFL_hyp) * dxmin);
     hyp_diff = eps_hyp * cmax_hyp / (smin(p->CFL, CFL_hyp) * dxmin);
   }
+  const int dg = p->need_diagnostics && p->diag;
   double* sfl = (double*)malloc(sizeof(double) * L);
   double* vvl = (double*)malloc(sizeof(double) * L);
   double* bbl = (double*)malloc(sizeof(double) * L);
@@ -397,6 +398,18 @@ double mo_mhd_residual_ex(const mo_params* p, const double* U, const double* pre
             const double* f = flx + v * L;
             res[v] = 0.0 - (w1 * (f[i + 1] - f[i - 1]) + w2 * (f[i + 2] - f[i - 2]));
           }
+          if (dg) {  /* energy-flux divergence, its conduction share (src/mhdres_SR.C:368-384, 689-702) */
+            const long cd = off + i * st[d1];
+            if (spitzer) {
+              const double* Bd = var + (5 + d1) * L;
+              const double dn = -(w1 * ((sfl[i + 1] * Bd[i + 1]) - (sfl[i - 1] * Bd[i - 1])) +
+                                  w2 * ((sfl[i + 2] * Bd[i + 2]) - (sfl[i - 2] * Bd[i - 2])));
+              p->diag[cd] += res[4] - dn;
+              p->diag[g.N + cd] += dn;
+            } else {
+              p->diag[cd] += res[4];
+            }
+          }
           const double* B2 = var + (5 + d2) * L;
           const double* B3 = var + (5 + d3) * L;
           double dB2 = w1 * (B2[i + 1] - B2[i - 1]) + w2 * (B2[i + 2] - B2[i - 2]);
@@ -412,6 +425,8 @@ double mo_mhd_residual_ex(const mo_params* p, const double* U, const double* pre
           }
           double lf = lf1[i];
           for (int q = 0; q < 3; q++) lrt[q] = lf * lrt[q] + (1.0 - lf) * cbb[q];
+          if (dg)  /* work of the Lorentz force (src/mhdres_SR.C:434-435, 751-752) */
+            p->diag[2 * g.N + off + i * st[d1]] += var[L + i] * lrt[0] + var[2 * L + i] * lrt[1] + var[3 * L + i] * lrt[2];
           res[1] += lrt[0];
           res[2] += lrt[1];
           res[3] += lrt[2];
@@ -519,6 +534,9 @@ void mo_source_integrate_ex(const mo_params* p, double* U, const double* U0, dou
   const double gx = -p->grav;
   const double invRdt = p->rt_cfl / p->dt;
   const double Qrad = 0.0, dmp = 0.0;
+  /* diagnostics (src/Add_Sources_Integrate_SR.C:122-296): tvar4..6 set, tvar7 += TCheck's energy change / dt */
+  const int dg = p->need_diagnostics && p->diag;
+  const double invdt = 1.0 / p->dt;
   for (int k = GH; k < GH + p->nz; k++)
     for (int j = GH; j < GH + p->ny; j++)
       for (int i = GH; i < GH + p->nx; i++) {
@@ -530,6 +548,10 @@ void mo_source_integrate_ex(const mo_params* p, double* U, const double* U0, dou
         double edmp = dn * U[N + c];
         R[N + c] += dn;
         R[4 * N + c] += edmp + Qrad * efaci;
+        if (dg) {
+          p->diag[3 * N + c] = efaci;
+          p->diag[4 * N + c] = edmp;
+        }
         /* Boris correction (:347-392) */
         double rh = U[c], rd = R[c];
         double vx = U[N + c], vy = U[2 * N + c], vz = U[3 * N + c];
@@ -549,13 +571,16 @@ void mo_source_integrate_ex(const mo_params* p, double* U, const double* U0, dou
         R[2 * N + c] += b1;
         R[3 * N + c] += b2;
         R[4 * N + c] += b3;
+        if (dg) p->diag[5 * N + c] = b3;
         /* time integration (:394-408) */
         for (int v = 0; v < NV; v++) {
           U[v * N + c] = U0[v * N + c] + wdt * R[v * N + c];
           R[v * N + c] = 0;
         }
         /* Tcheck (:444-465) */
+        const double ee = U[4 * N + c];
         tcheck_cell(p, U, N, c);
+        if (dg) p->diag[6 * N + c] += (U[4 * N + c] - ee) * invdt;
         /* hyperbolic conduction (:410-419) */
         if (p->spitzer > 0.0 && f && f->sflx) {
           f->sflx[c] = f->sflx0[c] + wdt * f->Rflx[c];
@@ -645,6 +670,9 @@ void mo_tvdlimit(const mo_params* p, double* U, const double* pres, double dt_tv
   const int n[3] = {p->nx, p->ny, p->nz};
   const long st[3] = {1, g.sx, (long)g.sx * g.sy};
   const double rho_min = p->tchk[1], eps_min = p->tchk[0];
+  /* diagnostics (src/tvdlimit_SR.C:115-116): per unit of the full step's time */
+  const int dg = p->need_diagnostics && p->diag;
+  const double idt_full = 1.0 / p->dt, dt_fac = dt_tvd / p->dt;
   const double rho_lev = pow(p->tvd[0], 2);
   const int rho_log = (int)p->tvd[1];
   const double q_rho_max = log(p->tvd[2]);
@@ -854,6 +882,8 @@ void mo_tvdlimit(const mo_params* p, double* U, const double* pres, double dt_tv
         for (int i = GH; i < sz - GH; i++)
           res[4 * L + i] += (1.0 - q_t[i]) * (res[L + i] * var[L + i] + res[2 * L + i] * var[2 * L + i] +
                                               res[3 * L + i] * var[3 * L + i]);
+        if (dg)  /* energy change of the sweep (src/tvdlimit_SR.C:577-584) */
+          for (int i = GH; i < sz - GH; i++) p->diag[7 * N + off + i * st[d1]] += res[4 * L + i] * idt_full;
         for (int i = GH; i < sz - GH; i++) {
           double dn = (res[L + i] * var[5 * L + i] + res[2 * L + i] * var[6 * L + i] + res[3 * L + i] * var[7 * L + i]) /
                       smax(1e-100, bsqr[i]);
@@ -862,6 +892,7 @@ void mo_tvdlimit(const mo_params* p, double* U, const double* pres, double dt_tv
           double b2 = -BC2[i] * (res[3 * L + i] - dn * var[7 * L + i]);
           double b3 = b0 * var[L + i] + b1 * var[2 * L + i] + b2 * var[3 * L + i];
           res[L + i] += b0; res[2 * L + i] += b1; res[3 * L + i] += b2; res[4 * L + i] += b3;
+          if (dg) p->diag[5 * N + off + i * st[d1]] += b3 * idt_full;  /* (:601-604) */
         }
         for (int i = 1; i < sz - 2; i++)
           qrho[i] = (var[5 * L + i + 1] - var[5 * L + i]) * flx[5 * L + i] +
@@ -870,13 +901,23 @@ void mo_tvdlimit(const mo_params* p, double* U, const double* pres, double dt_tv
         for (int i = GH; i < sz - GH; i++) {
           double qres = 0.5 * (qrho[i] + qrho[i - 1]) * q_t[i];
           res[4 * L + i] += dt_tvd * qres;
+          if (dg) p->diag[8 * N + off + i * st[d1]] += dt_fac * qres;  /* Qres (:617-624) */
         }
+        if (dg)  /* viscous heating, for the diagnostics only (:626-635) */
+          for (int i = 1; i < sz - 2; i++)
+            qrho[i] = (var[L + i + 1] - var[L + i]) * flx[L + i] + (var[2 * L + i + 1] - var[2 * L + i]) * flx[2 * L + i] +
+                      (var[3 * L + i + 1] - var[3 * L + i]) * flx[3 * L + i];
         for (int i = GH; i < sz - GH; i++) {
           long c = off + i * st[d1];
           for (int v = 0; v < NV; v++) U[v * N + c] += res[v * L + i];
           U[c] = smax(rho_min, U[c]);
           double mx = U[N + c], my = U[2 * N + c], mz = U[3 * N + c];
+          const double eb = U[4 * N + c];
           U[4 * N + c] = smax(U[4 * N + c], eps_min * U[c] + 0.5 * (mx * mx + my * my + mz * mz) / U[c]);
+          if (dg) {  /* the energy floor's change and Qvis (:659-667) */
+            p->diag[6 * N + c] += (U[4 * N + c] - eb) * idt_full;
+            p->diag[9 * N + c] += dt_fac * (0.5 * (qrho[i] + qrho[i - 1]) * q_t[i]);
+          }
         }
       }
     blo[d1] = GH;
@@ -890,9 +931,17 @@ void mo_tvdlimit(const mo_params* p, double* U, const double* pres, double dt_tv
 /* ------------------------------------------------------------------ TCheck */
 void mo_tcheck(const mo_params* p, double* U) {
   geom g = geom_of(p);
+  /* diagnostics: tvar7 += energy change / dt (src/Add_Sources_Integrate_SR.C:560-564, 618-620) */
+  const int dg = p->need_diagnostics && p->diag;
+  const double invdt = p->dt > 0.0 ? 1.0 / p->dt : 0.0;
   for (int k = GH; k < GH + p->nz; k++)
     for (int j = GH; j < GH + p->ny; j++)
-      for (int i = GH; i < GH + p->nx; i++) tcheck_cell(p, U, g.N, at(&g, i, j, k));
+      for (int i = GH; i < GH + p->nx; i++) {
+        const long c = at(&g, i, j, k);
+        const double eei = U[4 * g.N + c];
+        tcheck_cell(p, U, g.N, c);
+        if (dg) p->diag[6 * g.N + c] += (U[4 * g.N + c] - eei) * invdt;
+      }
 }
 
 /* ------------------------------------------------- physical x boundaries */
@@ -1213,9 +1262,15 @@ int mo_step_ex(mo_params* p, const mo_eos* eos, double* U, double* U0, double* R
     for (int k = GH; k < GH + p->nz; k++)
       for (int j = GH; j < GH + p->ny; j++)
         for (int i = GH; i < GH + p->nx; i++) f->sflx0[at(&g, i, j, k)] = f->sflx[at(&g, i, j, k)];
+  const int diag_step = p->diagnostics_next_step && p->diag;
+  p->need_diagnostics = 0;
   for (int stage = 1; stage <= 4; stage++) {
     mo_cons_to_prim(p, eos, U, pres, aux5 + N, aux5 + 2 * N, aux5 + 3 * N, aux5 + 4 * N);
     if (stage == 1) mo_adjust_valf_max(p, U, pres, NULL);
+    if (stage == 4 && diag_step) {  /* an output step's diagnostics (src/solver.C:264-289) */
+      p->need_diagnostics = 1;
+      for (long c = 0; c < 10 * N; c++) p->diag[c] = 0.0;
+    }
     double dt_mhd = mo_mhd_residual_ex(p, U, pres, aux5 + N, R, f);
     if (stage == 1) {
       int rc = mo_sync_timestep(p, p->dt_rad, dt_mhd, &cfl);
@@ -1239,6 +1294,8 @@ int mo_step_ex(mo_params* p, const mo_eos* eos, double* U, double* U0, double* R
     mo_clean_divB(p, U, f->phi, f->divB);
   }
   mo_tcheck(p, U);
+  p->need_diagnostics = 0;
+  p->diagnostics_next_step = 0;
   mo_boundaries_ex(p, eos, U, f, 0);
   p->time += p->dt;
   return 0;

@@ -53,6 +53,12 @@ typedef struct {
   /* PhysicsData::params[i_param_spitzer]: Spitzer coefficient of the hyperbolic
    * heat conduction (0: off) */
   double spitzer;
+  /* RunData::need_diagnostics (src/solver.C:264-289) and the ten diagnostic
+   * arrays tvar1..tvar8, Qres, Qvis (10 x N, NULL: none).  mo_step_ex sets
+   * need_diagnostics at stage 4 of a step requested by diagnostics_next_step,
+   * zeroes the arrays there, and clears both flags after that step's TCheck. */
+  int need_diagnostics, diagnostics_next_step;
+  double* diag;
 } mo_params;
 
 typedef struct mo_eos mo_eos;

@@ -39,6 +39,7 @@ class MoParams(C.Structure):
         ("bnd_bcrit", C.c_double), ("bnd_eps_top", C.c_double), ("p_bc", C.c_double), ("s_bc", C.c_double),
         ("bnd_ini", C.c_int),
         ("spitzer", C.c_double),
+        ("need_diagnostics", C.c_int), ("diagnostics_next_step", C.c_int), ("diag", C.c_void_p),
     ]
 
 
@@ -173,6 +174,9 @@ class State:
                            ptr(self.BgradT))
         self.divb_log = []
         self.limits_log = []
+        # tvar1..tvar8, Qres, Qvis of the last step run with diagnostics
+        self.diag = np.zeros((10,) + self.U.shape[1:])
+        self.p.diag = self.diag.ctypes.data
         if p.xbnd == 1 and not p.periodic_x:
             if eos is None:
                 raise ValueError("the physical x boundaries need the EOS (State(p, U, eos))")
@@ -180,9 +184,12 @@ class State:
         else:
             lib().mo_boundaries(C.byref(p), self.U)
 
-    def step(self, eos, n=1):
+    def step(self, eos, n=1, diagnostics_at=None):
+        """n steps; diagnostics_at: the 1-based step among them whose
+        diagnostics (an output step's) fill self.diag."""
         dts = []
-        for _ in range(n):
+        for s in range(n):
+            self.p.diagnostics_next_step = 1 if diagnostics_at == s + 1 else 0
             rc = lib().mo_step_ex(C.byref(self.p), eos.ptr, self.U, self.U0, self.R, self.aux, C.byref(self._f))
             if rc:
                 raise RuntimeError(f"oracle step failed: {rc}")

@@ -242,6 +242,11 @@ int main(int argc, char** argv) {
 
   Run.Init(0);
   Run.verbose = par_i("verbose", 0);
+  // diag_step > 0: the diagnostics of that (1-based) step, as ComputeSolution
+  // sets them on an output step (src/solver.C:264-289); GridData::Init
+  // allocates the arrays only with Run.diagnostics (src/grid.C:318-334)
+  const int diag_step = par_i("diag_step", 0);
+  Run.diagnostics = diag_step > 0 ? 1 : 0;
   g_run = &Run;
   Physics.Init();
   Grid.Init(Run, Physics);
@@ -304,7 +309,13 @@ int main(int argc, char** argv) {
         limits.push_back(e_lim);
         dt_rad = dt_rad_const;  // RT stub (Qtot = 0, Tau = tau0 set once above)
       }
-      Run.need_diagnostics = 0;
+      Run.need_diagnostics = (it == diag_step && stage == maxstage) ? 1 : 0;
+      if (Run.need_diagnostics) {
+        double* dg[10] = {Grid.tvar1, Grid.tvar2, Grid.tvar3, Grid.tvar4, Grid.tvar5,
+                          Grid.tvar6, Grid.tvar7, Grid.tvar8, Grid.Qres, Grid.Qvis};
+        for (int q = 0; q < 10; q++)
+          for (int i = 0; i < Grid.bufsize; i++) dg[q][i] = 0.0;
+      }
       dt_mhd = MHD_Residual(Run, Grid, Physics);
       if (tr) {
         snprintf(name, sizeof name, "s%d_res_R", stage); dump(name, Grid.Res, ubytes);
@@ -337,6 +348,15 @@ int main(int argc, char** argv) {
     }
     TCheck(Run, Grid, Physics);
     if (tr) dump("tck_U", Grid.U, ubytes);
+    if (it == diag_step) {
+      const double* dg[10] = {Grid.tvar1, Grid.tvar2, Grid.tvar3, Grid.tvar4, Grid.tvar5,
+                              Grid.tvar6, Grid.tvar7, Grid.tvar8, Grid.Qres, Grid.Qvis};
+      std::vector<double> all;
+      for (int q = 0; q < 10; q++) all.insert(all.end(), dg[q], dg[q] + Grid.bufsize);
+      dump("diag", all.data(), all.size() * sizeof(double));
+      dump("diag_U", Grid.U, ubytes);  // the state after TCheck of that step
+    }
+    Run.need_diagnostics = 0;
     boundaries(Grid, Physics, 0);
     if (tr) dump("end_U", Grid.U, ubytes);
     Run.Advance();

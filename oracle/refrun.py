@@ -83,5 +83,7 @@ def run(U, params, steps=1, trace_step=0, keep=None):
                 a = a.reshape(5, sz, sy, sx)
             elif name in ("final_phi", "final_divB", "divb_phi_in", "final_sflx"):
                 a = a.reshape(sz, sy, sx)
+            elif name == "diag":  # tvar1..8, Qres, Qvis of the diagnostics step
+                a = a.reshape(10, sz, sy, sx)
             out[name] = a
     return out

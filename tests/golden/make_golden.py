@@ -12,6 +12,8 @@ The open_bottom case uses the reference's own physical x boundaries (open
 bottom, top open to outflows) and keeps the p_bc and s_bc they set.
 The va_adjust case runs the adaptive limits of Adjust_Valf_Max and keeps its
 per-step log line (maxima, va_max, the limits and the near-limit counts).
+The diagnostics cases switch on the reference's diagnostics for one step
+(tvar1..8, Qres, Qvis after that step's TCheck) and keep them with the state.
 The divb_cleaning case also runs the reference's Clean_divB after each TVD
 pass and keeps the cleaning potential phi, the last divergence and the
 iteration count of every step (parsed from the reference's own log line).
@@ -60,6 +62,18 @@ def cases():
     yield "va_adjust", dict(nx=16, ny=12, nz=8, dx=3.2e6, periodic_x=1, va_max=3.0e5, va_adjust=1.0,
                             max_fill=100.0, verbose=1), \
         initial.periodic_box(eos, 16, 12, 8, seed=17, v_rms=2.0e5, b_rms_gauss=800.0), dict(steps=8, trace_step=3)
+    # the diagnostics of one output step (Run.need_diagnostics at stage 4 through
+    # TVDlimit and TCheck, src/solver.C:264-289): closed x with gravity, Boris
+    # corrections (va_max 3e5) and an energy ceiling that TCheck applies
+    yield "diagnostics", dict(nx=12, ny=8, nz=6, dx=1.6e6, periodic_x=0, grav=2.74e4, va_max=3.0e5,
+                              tchk_eps_max=1.686e12, diag_step=3), \
+        initial.stratified_box(eos, 12, 8, 6, dx=1.6e6, seed=21, v_rms=1.0e5), dict(steps=4, trace_step=0)
+    yield "diagnostics_spitzer", dict(nx=12, ny=8, nz=6, dx=1.6e6, periodic_x=0, grav=2.74e4, xbnd=1, bnd_top=1,
+                                      bnd_eps_top=3e12, spitzer=1.0, diag_step=4), \
+        initial.stratified_box(eos, 12, 8, 6, dx=1.6e6, seed=16), dict(steps=5, trace_step=0)
+    yield "diagnostics_two_half", dict(nx=8, ny=8, nz=6, dx=3.2e6, periodic_x=1, CFL=1.2, CFL_tvd=1.0,
+                                       diag_step=2), \
+        initial.periodic_box(eos, 8, 8, 6, seed=23, v_rms=3.0e5, b_rms_gauss=400.0), dict(steps=3, trace_step=0)
 
 
 KEEP = ["init_U", "s1_c2p_U", "s1_c2p_aux", "s1_res_R", "s1_res_dt", "s1_si_U", "s1_bc_U", "s2_c2p_U",
@@ -88,6 +102,8 @@ def main(only=()):
         keep = KEEP_DIVB if hp.get("divB_switch", 0) else (KEEP_BND if hp.get("xbnd", 0) else KEEP)
         if hp.get("spitzer", 0):
             keep = ["init_U", "final_U", "final_sflx", "dts", "limits"]
+        if hp.get("diag_step", 0):
+            keep = keep + ["diag", "diag_U"]
         arrays = {k: out[k] for k in keep if k in out}
         arrays["input_U"] = U
         arrays["trace_step"] = np.array(run["trace_step"])

@@ -43,6 +43,9 @@ def gpu_params(hp, precision=64):
     kw["dz"] = float(hp.get("dz", dx))
     p = gpumhd.default_params(int(hp["nx"]), int(hp["ny"]), int(hp["nz"]), dx, precision=precision,
                               periodic_x=int(hp.get("periodic_x", 1)), **kw)
+    for i, k in enumerate(("tchk_eps_min", "tchk_rho_min", "tchk_eps_max", "tchk_vmax")):
+        if k in hp:
+            p.tchk[i] = float(hp[k])
     return p
 
 

@@ -297,3 +297,26 @@ def test_live_reference_va_adjust(max_fill, va_max, v_rms, seed, eos):
     assert np.array_equal(np.array([x[0] for x in dts]), ref["dts"].reshape(-1, 3)[:, 0])
     assert np.array_equal(np.array(st.limits_log).reshape(-1), ref["limits"])
     assert np.array_equal(st.U, ref["final_U"])
+
+
+DIAG_NAMES = ["tvar1", "tvar2", "tvar3", "tvar4", "tvar5", "tvar6", "tvar7", "tvar8", "Qres", "Qvis"]
+
+
+@pytest.mark.parametrize("name", ["diagnostics", "diagnostics_spitzer", "diagnostics_two_half"])
+def test_diagnostics_bitexact(name, eos):
+    """An output step's diagnostics (Run.need_diagnostics from stage 4 through
+    TVDlimit and TCheck): the energy-flux divergence, its conduction share and
+    the Lorentz work of MHD_Residual, Source_Integrate's radiation factor,
+    gravity work, Boris energy and TCheck energy change, and TVDlimit's
+    energy change, Boris part, resistive and viscous heating and floor
+    change -- bit for bit against the reference, with the state."""
+    d, hp = H.load_case(name)
+    st = O.State(H.oracle_params(hp), d["input_U"], eos)
+    ds = int(hp["diag_step"])
+    st.step(eos, ds, diagnostics_at=ds)
+    assert np.array_equal(H.interior(st.U), H.interior(d["diag_U"]))
+    for q in range(10):
+        assert np.array_equal(st.diag[q], d["diag"][q]), DIAG_NAMES[q]
+    st.step(eos, int(d["steps"]) - ds)
+    assert np.array_equal(st.U, d["final_U"])
+    assert not st.p.need_diagnostics  # off again after the output step
