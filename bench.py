@@ -278,7 +278,9 @@ def run_ours(args):
     torch.cuda.set_device(lrank)
     build.build()
     eos_table.ensure_table(EOS_BENCH, "bench")
-    wl = WORKLOAD
+    wl = dict(WORKLOAD)
+    if args.ny:  # a smaller horizontal extent, for profiler captures (the headline is the default)
+        wl["ny"] = wl["nz"] = args.ny
     n_cells = wl["nx"] * wl["ny"] * wl["nz"]
     U = make_state(wl["nx"], wl["ny"], wl["nz"], seed=7 + rank)
     peaks = {}
@@ -451,7 +453,8 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": step_ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded stratified box, generated EOS table 3000x3000)",
-        "config": {"workload": "stratified 128(vertical) x 384 x 384 at 16 km, closed top/bottom, gravity 2.74e4"
+        "config": {"workload": f"stratified 128(vertical) x {wl['ny']} x {wl['nz']} at 16 km, closed top/bottom, "
+                               "gravity 2.74e4"
                                + (", divB cleaning after every TVD pass" if args.divb else "")
                                + (", open bottom / closed top (MURaM's physical x boundaries)" if args.xbnd else "")
                                + (f", Spitzer conduction (coefficient {args.spitzer:g})" if args.spitzer > 0 else ""),
@@ -577,13 +580,16 @@ def run_large(args):
     tab = initial.EosTable(EOS_BENCH)
     nx, ny, nz = 256, 1024, 1024
     seed_box = initial.periodic_box(tab, 256, 256, 256, dx=3.2e6, seed=99)
-    gs = gpumhd.MuramGPU(gpumhd.default_params(256, 256, 256, 3.2e6, precision=32), eos_path=EOS_BENCH)
-    gs.upload_state(seed_box)
-    del seed_box
-    p = gpumhd.default_params(nx, ny, nz, 3.2e6, precision=32)
-    g = gpumhd.MuramGPU(p, eos_path=EOS_BENCH)
-    g.tile_from(gs)
-    gs.close()
+
+    def large_box(prec):
+        gs = gpumhd.MuramGPU(gpumhd.default_params(256, 256, 256, 3.2e6, precision=prec), eos_path=EOS_BENCH)
+        gs.upload_state(seed_box)
+        gl = gpumhd.MuramGPU(gpumhd.default_params(nx, ny, nz, 3.2e6, precision=prec), eos_path=EOS_BENCH)
+        gl.tile_from(gs)
+        gs.close()
+        return gl
+
+    g = large_box(32)
     g.run_steps(1)
     ms, launches = time_device(g, args.steps, args.warmup)
     n_cells = nx * ny * nz
@@ -601,6 +607,27 @@ def run_large(args):
         "gpu_launches": launches,
     }
     g.close()
+    if not args.no_fp64:
+        # FP32 against the FP64 mode after the configuration's 50 steps from the
+        # same tiled state (the FP64 mode matches the reference CPU build to 1e-12)
+        import numpy as np
+        nerr = 50
+        res = {}
+        for prec in (64, 32):
+            gl = large_box(prec)
+            t0 = time.perf_counter()
+            gl.run_steps(nerr)
+            res[prec] = (gl.download_state()[:, 2:-2, 2:-2, 2:-2], time.perf_counter() - t0)
+            gl.close()
+        ref, got = res[64][0], res[32][0]
+        l2 = [float(f"{np.sqrt(np.sum((got[f] - ref[f]) ** 2) / np.sum(ref[f] ** 2)):.3e}") for f in range(8)]
+        line["fp32_error"] = {"steps": nerr, "against": "FP64 GPU mode (= reference CPU build to 1e-12)",
+                              "fields": ["rho", "Mx", "My", "Mz", "e", "Bx", "By", "Bz"], "rel_l2": l2,
+                              "max_rel_l2": max(l2)}
+        line["fp64"] = {"value": n_cells * nerr / res[64][1], "unit": UNIT, "steps": nerr,
+                        "note": "host-timed run_steps incl. graph capture"}
+        del res, ref, got
+    del seed_box
     print(json.dumps(line))
 
 
@@ -733,6 +760,8 @@ def main():
                     help="stratified: the headline box; ensemble: 64 uneven boxes in one launch; "
                          "large: one 1024x1024x256 box; adjoint: gradient of a 20-step objective")
     ap.add_argument("--boxes", type=int, default=64, help="boxes of the ensemble workload")
+    ap.add_argument("--ny", type=int, default=0,
+                    help="horizontal size (y = z) of the stratified box instead of 384, for profiler captures")
     ap.add_argument("--spitzer", type=float, default=0.0,
                     help="stratified workload with hyperbolic Spitzer conduction of this coefficient")
     ap.add_argument("--xbnd", action="store_true",
