@@ -653,15 +653,29 @@ def run_adjoint(args):
     def J(U):
         return float(np.sum(mask * U[5, 2:-2, 2:-2, -10:-2] ** 2))
 
-    def case(eos_path, ndir):
+    # TVD diffusion off: every TVD flux is multiplied by zero (tvd_coeff, the
+    # boundary viscosity / resistivity profiles and the x hyperdiffusion all
+    # 0), so the sweeps are the identity and the limiter's kinks drop out of
+    # both the forward step and its adjoint
+    no_tvd = dict(tvd_coeff=[0.0] * 4, tvd_visc_bnd=[0.0, 0.0], tvd_eta_bnd=[0.0, 0.0])
+
+    def case(eos_path, ndir, tvd_off=False):
         tab = initial.EosTable(eos_path)
         U0 = initial.periodic_box(tab, n, n, n, seed=4)
-        g = gpumhd.MuramGPU(gpumhd.default_params(n, n, n, 3.2e6), eos_path=eos_path)
+        kw = dict(no_tvd) if tvd_off else {}
+
+        def params(**more):
+            p = gpumhd.default_params(n, n, n, 3.2e6, **kw, **more)
+            if tvd_off:
+                p.tvd[4] = 0.0  # tvd_vhyp
+            return p
+
+        g = gpumhd.MuramGPU(params(), eos_path=eos_path)
         g.upload_state(U0)
         dt = float(g.run_steps(1)[0]) * 0.6
         g.close()
-        boxes = {prec: gpumhd.MuramGPU(gpumhd.default_params(n, n, n, 3.2e6, precision=prec, autostep=0, dt=dt),
-                                       eos_path=eos_path) for prec in (64, 32)}
+        boxes = {prec: gpumhd.MuramGPU(params(precision=prec, autostep=0, dt=dt), eos_path=eos_path)
+                 for prec in (64, 32)}
         g = boxes[64]
 
         def forward(box, U):
@@ -707,6 +721,7 @@ def run_adjoint(args):
                 "objective": {"fp64": J(UT), "fp32": J(UT32), "fp32_rel_diff": abs(J(UT32) - J(UT)) / abs(J(UT))}}
 
     smooth = case(eos_ideal, 32)
+    smooth_no_tvd = case(eos_ideal, 32, tvd_off=True)
     saha = case(EOS_BENCH, 8)
     line = {
         "metric": "adjoint/forward time, with dJ/dU0 checked by central differences",
@@ -716,6 +731,7 @@ def run_adjoint(args):
         "config": {"workload": f"periodic {n}^3, objective: mask-weighted B_x^2 over the top 8 layers of "
                                "dimension 0, fixed dt", "checkpoint_every": every},
         "ideal_gas_table": smooth,
+        "ideal_gas_table_tvd_off": smooth_no_tvd,
         "saha_table": saha,
     }
     print(json.dumps(line))
