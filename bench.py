@@ -421,6 +421,11 @@ def run_ours(args):
                 "roofline": {"bound": "fp64", "kernel": "k_stage_tm (FP64, RK stages 1-4)",
                              "achieved": round(ach64, 4), "peak": round(peak64, 4), "unit": "TFLOP/s",
                              "frac": round(ach64 / peak64, 4), "mean_launch_ms": round(stage64_ms, 4),
+                             # the FP64 mode is compiled without FMA contraction (parity with the
+                             # reference's no-FMA build): one flop per FP64 instruction, half the
+                             # DGEMM's flops per instruction
+                             "peak_without_fma": round(peak64 / 2, 4),
+                             "frac_without_fma": round(ach64 / (peak64 / 2), 4),
                              "flops_per_cell_per_launch": FLOPS_STAGE_PER_CELL,
                              "peak_source": "measured: cuBLAS DGEMM 8192^3 via torch.matmul",
                              "hbm_frac": round(ALGO_STAGE_WORDS / 4 * 8 * n_cells / (stage64_ms / 1e3) / 1e9
