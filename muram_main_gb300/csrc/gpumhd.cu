@@ -75,6 +75,10 @@ struct gpumhd_ctx {
   // Qres, Qvis (GridData, 10 x N), allocated when first switched on
   void* diag = nullptr;
   bool need_diag = false;
+  // Res holds zeros as far as the API is concerned, but the buffer was not
+  // cleared: Source_Integrate_Tcheck and the fused steps leave it so, the next
+  // MHD_Residual writes it without adding, any other access clears it first
+  bool res_zero_pending = false;
   void* phi = nullptr;   // divB cleaning potential (GridData::phi, N), persists between calls
   void* divb = nullptr;  // last divergence of B (GridData::divB, N)
   double* bnd_part = nullptr;  // per-plane sums of the physical x boundaries (nz * BND_NQ)
@@ -699,10 +703,18 @@ extern "C" int gpumhd_eos_init(gpumhd_ctx* ctx, const char* path) {
   return GPUMHD_OK;
 }
 
+// Clears Res where the context only marked it as zero.
+static void materialize_res(gpumhd_ctx* ctx) {
+  if (!ctx->res_zero_pending) return;
+  cudaMemsetAsync(ctx->S[ctx->iRes], 0, 8 * ctx->c.g.N * ctx->rsz, ctx->stream);
+  ctx->res_zero_pending = false;
+}
+
 static void* field_ptr(gpumhd_ctx* ctx, int which, int* nf, int* rc) {
   *rc = GPUMHD_OK;
   if (which >= 0 && which <= 2) {
     *nf = 8;
+    if (which == 2) materialize_res(ctx);
     return ctx->S[which == 0 ? ctx->iU : (which == 1 ? ctx->iU0 : ctx->iRes)];
   }
   *nf = 1;
@@ -1034,15 +1046,18 @@ extern "C" int gpumhd_mhd_residual(gpumhd_ctx* ctx, double* dt_mhd) {
                               (double*)ctx->spt[4], ctx->dyn, 0, ctx->stream);
     nl += 1;
   }
+  // Res += residual; a Res only marked as zero is written without being read
+  const void* res_in = ctx->res_zero_pending ? nullptr : ctx->S[ctx->iRes];
+  ctx->res_zero_pending = false;
   if (ctx->f32) {
-    Launch<float>::stage(ctx->c, (const float*)ctx->S[ctx->iU], (const float*)ctx->P[ctx->iP], nullptr, nullptr, nullptr,
-                         (float*)ctx->S[ctx->iRes], ctx->dyn, 0, true, 0, ctx->stream, map_u(ctx, ctx->iU),
-                         map_p(ctx, ctx->iP));
+    Launch<float>::stage(ctx->c, (const float*)ctx->S[ctx->iU], (const float*)ctx->P[ctx->iP], (const float*)res_in,
+                         nullptr, nullptr, (float*)ctx->S[ctx->iRes], ctx->dyn, 0, true, 0, ctx->stream,
+                         map_u(ctx, ctx->iU), map_p(ctx, ctx->iP));
     Launch<float>::cmax_faces(ctx->c, (const float*)ctx->S[ctx->iU], (const float*)ctx->P[ctx->iP], ctx->dyn, ctx->stream);
   } else {
-    Launch<double>::stage(ctx->c, (const double*)ctx->S[ctx->iU], (const double*)ctx->P[ctx->iP], nullptr, nullptr,
-                          nullptr, (double*)ctx->S[ctx->iRes], ctx->dyn, 0, true, 0, ctx->stream,
-                          map_u(ctx, ctx->iU), map_p(ctx, ctx->iP));
+    Launch<double>::stage(ctx->c, (const double*)ctx->S[ctx->iU], (const double*)ctx->P[ctx->iP],
+                          (const double*)res_in, nullptr, nullptr, (double*)ctx->S[ctx->iRes], ctx->dyn, 0, true, 0,
+                          ctx->stream, map_u(ctx, ctx->iU), map_p(ctx, ctx->iP));
     Launch<double>::cmax_faces(ctx->c, (const double*)ctx->S[ctx->iU], (const double*)ctx->P[ctx->iP], ctx->dyn, ctx->stream);
   }
   if (ctx->need_diag) {  // tvar1..3 of the output step
@@ -1103,6 +1118,7 @@ extern "C" int gpumhd_sync_timestep(gpumhd_ctx* ctx, double dt_rad, double dt_mh
 extern "C" int gpumhd_source_integrate_tcheck(gpumhd_ctx* ctx, int stage) {
   if (!ctx || stage < 1 || stage > 4) return GPUMHD_E_INVALID;
   CK(cudaSetDevice(ctx->device));
+  materialize_res(ctx);  // it reads Res
   const double invdt = 1.0 / ctx->hdyn.dt;  // src/Add_Sources_Integrate_SR.C:84
   if (ctx->f32)
     Launch<float>::source_integrate(ctx->c, (float*)ctx->S[ctx->iU], (const float*)ctx->S[ctx->iU0],
@@ -1112,6 +1128,7 @@ extern "C" int gpumhd_source_integrate_tcheck(gpumhd_ctx* ctx, int stage) {
     Launch<double>::source_integrate(ctx->c, (double*)ctx->S[ctx->iU], (const double*)ctx->S[ctx->iU0],
                                      (double*)ctx->S[ctx->iRes], ctx->dyn, stage, ctx->stream,
                                      ctx->need_diag ? (double*)ctx->diag : nullptr, invdt);
+  ctx->res_zero_pending = true;  // Res = 0 (src/Add_Sources_Integrate_SR.C:394-408), not stored
   int nl = 1;
   if (ctx->c.has_spitzer) {  // sflx = sflx0 + wdt*Rflx, Rflx = 0 (src/Add_Sources_Integrate_SR.C:410-419)
     int rc = ensure_spitzer(ctx);
@@ -1240,20 +1257,41 @@ extern "C" int gpumhd_tvdlimit(gpumhd_ctx* ctx, double dt_tvd) {
   ctx->hdyn.two_half = 0;
   int rc = push_dyn(ctx);
   if (rc) return rc;
+  // The sweeps update U in place in the reference; here each reads one
+  // buffer and writes another: x T -> U, y U -> T, z T -> U, from one copy of
+  // U into T.  A sweep writes only the cells it updates (x: interior x, every
+  // y and z row; y: interior x and y, every z row; z: the interior), so every
+  // cell a sweep reads holds the previous sweep's value, and at the end U holds
+  // the reference's values everywhere but in the z ghost planes at interior y,
+  // which the y sweep updated in T: those rows are copied back.
+  CK(cudaMemcpyAsync(ctx->T, ctx->S[ctx->iU], 8 * N * ctx->rsz, cudaMemcpyDeviceToDevice, ctx->stream));
+  // an output step's diagnostics (src/tvdlimit_SR.C:115-116): per unit of the full step's time
+  const double idt_full = 1.0 / ctx->hdyn.dt, dt_fac = dt_tvd / ctx->hdyn.dt;
+  const TvdDiag<float> dgf{(float*)ctx->diag, (float)idt_full, (float)dt_fac};
+  const TvdDiag<double> dgd{(double*)ctx->diag, idt_full, dt_fac};
+  void* const bufs[2] = {ctx->T, ctx->S[ctx->iU]};  // [d & 1]: the input of sweep d
   for (int d = 0; d < 3; d++) {
-    CK(cudaMemcpyAsync(ctx->T, ctx->S[ctx->iU], 8 * N * ctx->rsz, cudaMemcpyDeviceToDevice, ctx->stream));
-    // an output step's diagnostics (src/tvdlimit_SR.C:115-116): per unit of the full step's time
-    const double idt_full = 1.0 / ctx->hdyn.dt, dt_fac = dt_tvd / ctx->hdyn.dt;
-    const TvdDiag<float> dgf{(float*)ctx->diag, (float)idt_full, (float)dt_fac};
-    const TvdDiag<double> dgd{(double*)ctx->diag, idt_full, dt_fac};
+    const void* in = bufs[d & 1];
+    void* out = bufs[1 - (d & 1)];
     if (ctx->f32)
-      Launch<float>::tvd(ctx->c, d, 0, 0, (const float*)ctx->T, (const float*)ctx->P[ctx->iP], (float*)ctx->S[ctx->iU],
-                         ctx->dyn, ctx->stream, 0, ctx->need_diag ? &dgf : nullptr);
+      Launch<float>::tvd(ctx->c, d, 0, 0, (const float*)in, (const float*)ctx->P[ctx->iP], (float*)out, ctx->dyn,
+                         ctx->stream, 0, ctx->need_diag ? &dgf : nullptr);
     else
-      Launch<double>::tvd(ctx->c, d, 0, 0, (const double*)ctx->T, (const double*)ctx->P[ctx->iP],
-                          (double*)ctx->S[ctx->iU], ctx->dyn, ctx->stream, 0, ctx->need_diag ? &dgd : nullptr);
+      Launch<double>::tvd(ctx->c, d, 0, 0, (const double*)in, (const double*)ctx->P[ctx->iP], (double*)out,
+                          ctx->dyn, ctx->stream, 0, ctx->need_diag ? &dgd : nullptr);
     rc = check_launch(ctx, 1);
     if (rc) return rc;
+  }
+  {  // the z ghost planes' rows at interior y: the y sweep's values (in T)
+    const Geom& g = ctx->c.g;
+    const size_t plane = (size_t)g.sx * g.sy * ctx->rsz, row = (size_t)g.sx * ctx->rsz;
+    for (int f = 0; f < 8; f++)
+      for (int side = 0; side < 2; side++) {
+        const size_t k0 = side == 0 ? 0 : (size_t)(GH + g.nz);
+        const size_t off = (size_t)f * N * ctx->rsz + k0 * plane + GH * row;
+        CK(cudaMemcpy2DAsync((char*)ctx->S[ctx->iU] + off, plane, (const char*)ctx->T + off, plane,
+                             (size_t)g.ny * row, GH, cudaMemcpyDeviceToDevice, ctx->stream));
+      }
   }
   return GPUMHD_OK;
 }
@@ -1572,9 +1610,9 @@ extern "C" int gpumhd_enqueue_steps(gpumhd_ctx* ctx, int nsteps) {
       if (rc) return rc;
     }
   }
-  // the fused step uses U0 and Res as work space; Res returns to zero as after
-  // Source_Integrate_Tcheck, so per-routine calls can follow
-  if (nsteps > 0) CK(cudaMemsetAsync(ctx->S[ctx->iRes], 0, 8 * ctx->c.g.N * ctx->rsz, ctx->stream));
+  // the fused step uses U0 and Res as work space; Res counts as zero again, as
+  // after Source_Integrate_Tcheck, so per-routine calls can follow
+  if (nsteps > 0) ctx->res_zero_pending = true;
   ctx->have_pres = true;
   return GPUMHD_OK;
 }
@@ -1653,7 +1691,7 @@ extern "C" int gpumhd_profile_steps(gpumhd_ctx* ctx, int nsteps, double* ms_phas
   }
   for (int q = 0; q < 14; q++) cudaEventDestroy(ev[q]);
   if (rc) return rc;
-  CK(cudaMemsetAsync(ctx->S[ctx->iRes], 0, 8 * ctx->c.g.N * ctx->rsz, ctx->stream));
+  ctx->res_zero_pending = true;
   return gpumhd_synchronize(ctx);
 }
 
@@ -1935,7 +1973,7 @@ extern "C" int gpumhd_ensemble_enqueue_steps(gpumhd_ensemble* e, int nsteps) {
   k_set_counter<<<1, 32, 0, e->stream>>>(e->d_counter, nsteps);
   ECK(cudaGraphLaunch(e->exec, e->stream));
   for (gpumhd_ctx* x : e->box) {
-    ECK(cudaMemsetAsync(x->S[x->iRes], 0, 8 * x->c.g.N * x->rsz, e->stream));
+    x->res_zero_pending = true;  // Res served as work space
     x->have_pres = true;
     x->launches += (long long)graph_step_launches(x) * nsteps;
   }

@@ -467,7 +467,8 @@ struct StageSmem {
 //   Pin: its pressure (ghosts included), U0: the step's initial state,
 //   Uout/Pout: the new state and its pressure (interior and ghost images).
 // RESID = true: MHD_Residual.  Uin holds primitives (after ConsToPrim),
-//   Res += residual over the interior, dyn->cmax_bits gets the interior CFL speed.
+//   Res = U0 + residual over the interior (U0: the residual accumulated so
+//   far, null when it is zero), dyn->cmax_bits gets the interior CFL speed.
 //
 // A block owns a TX x TY column tile and marches along z.  Per plane, each
 // thread converts its own cell to primitives and computes that cell's x and y
@@ -590,9 +591,10 @@ __global__ void __launch_bounds__(TX* TY, 2) k_stage(Consts c, const R* __restri
     // this cell's U0 (fused stage) or Res (residual mode), used at the end
     R base[NV];
     if (active) {
-      const R* src = RESID ? Res : U0;
+      // RESID: U0 is the residual to add to (null: start from zero)
+      const R* src = U0;
 #pragma unroll
-      for (int q = 0; q < NV; q++) base[q] = src[id + (unsigned)q * g.N32];
+      for (int q = 0; q < NV; q++) base[q] = src ? src[id + (unsigned)q * g.N32] : (R)0;
     }
     __syncthreads();
     if (active) {
@@ -1485,10 +1487,9 @@ __global__ void __launch_bounds__(256, EwBlocks<R>::v) k_source_integrate(Consts
     r[1] += b0; r[2] += b1; r[3] += b2; r[4] += b3;
     R un[NV];
 #pragma unroll
-    for (int v = 0; v < NV; v++) {
-      un[v] = U0[(unsigned)v * N + id] + wdt * r[v];
-      Res[(unsigned)v * N + id] = (R)0;
-    }
+    for (int v = 0; v < NV; v++) un[v] = U0[(unsigned)v * N + id] + wdt * r[v];
+    // Res is zero for the next MHD_Residual: the host marks it so and the
+    // next residual writes it without reading it (no pass stores the zeros)
     const R ee = un[4];
     tcheck_cell<R>(c, vmax, emax, un[0], un[1], un[2], un[3], un[4]);
     if (diag) {

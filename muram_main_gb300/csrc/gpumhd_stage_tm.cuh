@@ -399,9 +399,10 @@ __global__ void __launch_bounds__(TX* TY, 2)
     const unsigned id = own0 + (unsigned)k * plane;
     R base[NV];
     if (active) {
-      const R* src = RESID ? Res : U0;
+      // RESID: U0 is the residual to add to (null: start from zero)
+      const R* src = U0;
 #pragma unroll
-      for (int q = 0; q < NV; q++) base[q] = src[id + (unsigned)q * g.N32];
+      for (int q = 0; q < NV; q++) base[q] = src ? src[id + (unsigned)q * g.N32] : (R)0;
     }
     if (pend) finish_pressure(k - 1);
     tm::tmem_wait_st();
