@@ -52,9 +52,10 @@ typedef struct gpumhd_params {
   /* RunData */
   double CFL, CFL_tvd, dt, time, outcad;
   int autostep;          /* RunData::autostep (dt computed from the CFL condition) */
-  int compensated;       /* FP32 only: 1 = compensated (Kahan) RK updates -- a per-cell FP32
-                            remainder carries what rounding the state dropped at each step's
-                            last stage (8 more words per cell); 0 = plain updates */
+  int compensated;       /* FP32 fused steps only: 1 = compensated (Kahan) updates -- a per-cell
+                            FP32 remainder carries what rounding the state has dropped: every
+                            RK stage sum adds it, stage 4 and each TVD sweep store the new one
+                            (zero where Tcheck or a floor changed the value); 0 = plain */
   /* PhysicsData::params */
   double grav, va_max, va_adjust, max_fill;
   /* PhysicsData TVD settings */

@@ -1421,31 +1421,31 @@ static int enqueue_one_step(gpumhd_ctx* ctx, cudaEvent_t* ev = nullptr) {
               map_u(ctx, b), map_p(ctx, pb), ctx->tune_zc, comp);
     if (xb) L::bc(c, S[a], (float*)nullptr, ctx->dyn, ctx->bnd_part, 0, s, sf0);  // TVD keeps the stale pressure
     mark();
-    L::tvd(c, 0, 0, 0, S[a], P[pb], S[d], ctx->dyn, s, ctx->tune_td);
+    L::tvd(c, 0, 0, 0, S[a], P[pb], S[d], ctx->dyn, s, ctx->tune_td, nullptr, comp);
     mark();
-    L::tvd(c, 1, 0, 0, S[d], P[pb], S[b], ctx->dyn, s, ctx->tune_td);
+    L::tvd(c, 1, 0, 0, S[d], P[pb], S[b], ctx->dyn, s, ctx->tune_td, nullptr, comp);
     mark();
-    L::tvd(c, 2, 1, 0, S[b], P[pb], S[a], ctx->dyn, s, ctx->tune_td);
+    L::tvd(c, 2, 1, 0, S[b], P[pb], S[a], ctx->dyn, s, ctx->tune_td, nullptr, comp);
     if (cond) {
       const int rc2 = capture_if(ctx, tvd2, [&](cudaStream_t q) {
-        L::tvd(c, 0, 0, 1, S[a], P[pb], S[d], ctx->dyn, q, ctx->tune_td);
-        L::tvd(c, 1, 0, 1, S[d], P[pb], S[b], ctx->dyn, q, ctx->tune_td);
-        L::tvd(c, 2, 2, 1, S[b], P[pb], S[a], ctx->dyn, q, ctx->tune_td);
+        L::tvd(c, 0, 0, 1, S[a], P[pb], S[d], ctx->dyn, q, ctx->tune_td, nullptr, comp);
+        L::tvd(c, 1, 0, 1, S[d], P[pb], S[b], ctx->dyn, q, ctx->tune_td, nullptr, comp);
+        L::tvd(c, 2, 2, 1, S[b], P[pb], S[a], ctx->dyn, q, ctx->tune_td, nullptr, comp);
       });
       if (rc2) return rc2;
     } else {
       mark();
-      L::tvd(c, 0, 0, 1, S[a], P[pb], S[d], ctx->dyn, s, ctx->tune_td);
+      L::tvd(c, 0, 0, 1, S[a], P[pb], S[d], ctx->dyn, s, ctx->tune_td, nullptr, comp);
       mark();
-      L::tvd(c, 1, 0, 1, S[d], P[pb], S[b], ctx->dyn, s, ctx->tune_td);
+      L::tvd(c, 1, 0, 1, S[d], P[pb], S[b], ctx->dyn, s, ctx->tune_td, nullptr, comp);
       mark();
-      L::tvd(c, 2, 2, 1, S[b], P[pb], S[a], ctx->dyn, s, ctx->tune_td);
+      L::tvd(c, 2, 2, 1, S[b], P[pb], S[a], ctx->dyn, s, ctx->tune_td, nullptr, comp);
     }
     mark();
     if (c.divb_on) L::divb_clean(c, S[a], (float*)ctx->phi, (float*)ctx->divb, ctx->dyn, s);
     mark();
     {
-      L::step_finish(c, S[a], P[pa], ctx->dyn, s);
+      L::step_finish(c, S[a], P[pa], ctx->dyn, s, comp);
     }
     if (xb) {
       L::bc(c, S[a], P[pa], ctx->dyn, ctx->bnd_part, 1, s, sf0);  // the next step's ghosts, pressure and CFL speed

@@ -592,9 +592,13 @@ __global__ void __launch_bounds__(TX* TY, 2) k_stage(Consts c, const R* __restri
     R base[NV];
     if (active) {
       // RESID: U0 is the residual to add to (null: start from zero)
-      const R* src = U0;
+      if (!RESID || U0) {
 #pragma unroll
-      for (int q = 0; q < NV; q++) base[q] = src ? src[id + (unsigned)q * g.N32] : (R)0;
+        for (int q = 0; q < NV; q++) base[q] = U0[id + (unsigned)q * g.N32];
+      } else {
+#pragma unroll
+        for (int q = 0; q < NV; q++) base[q] = (R)0;
+      }
     }
     __syncthreads();
     if (active) {
@@ -673,6 +677,10 @@ __global__ void __launch_bounds__(TX* TY, 2) k_stage(Consts c, const R* __restri
 }
 
 // --------------------------------------------------------------- TVD sweep
+// y or z index t (0..n+3) of a cell -> the interior cell it images under the
+// periodic fill (itself when interior).
+__device__ __forceinline__ int wrap_interior(int t, int n) { return t < GH ? t + n : (t >= GH + n ? t - n : t); }
+
 // Per-cell quantities of TVDlimit's pencil (src/tvdlimit_SR.C:269-377).
 template <class R>
 struct TCell {
@@ -863,10 +871,16 @@ __device__ __forceinline__ void tvd_flux(const Consts& c, const TCell<R>& am, co
 // DIAG (an output step): the sweep's diagnostics of cell id accumulate in
 // dg (src/tvdlimit_SR.C:577-584, 601-604, 617-624, 659-667); qvp / qvm: the
 // viscous heating terms of its right / left interfaces.
+// Cin (FP32 compensated mode, else null): the remainders of the cell's
+// state, at stride N -- what rounding the state to FP32 has dropped so far;
+// the update then adds them (u = u_in + (res + C)) and Cout (null for a
+// ghost image, whose source cell keeps them) receives the new remainders,
+// zero where a floor changed the value.
 template <class R, bool DIAG = false>
 __device__ __forceinline__ void tvd_update(const Consts& c, R dtt, const R* Fp, const R* Fm, R qp, R qm,
                                            const TCell<R>& c0, const R* u_in, R* u, const TvdDiag<R>* dg = nullptr,
-                                           long long id = 0, R qvp = (R)0, R qvm = (R)0) {
+                                           long long id = 0, R qvp = (R)0, R qvm = (R)0, const R* Cin = nullptr,
+                                           R* Cout = nullptr) {
   const auto& kk_ = kc<R>(c);
   const long long N = c.g.N;
   R res[NV];
@@ -887,6 +901,28 @@ __device__ __forceinline__ void tvd_update(const Consts& c, R dtt, const R* Fp, 
     R qres = (R)0.5 * (qp + qm) * c0.qt;
     res[4] += dtt * qres;
     if (DIAG) dg->d[8 * N + id] += dg->dt_fac * qres;
+  }
+  if constexpr (std::is_same<R, float>::value) {
+    if (Cin) {  // compensated sum and the floors
+      R rem[NV];
+#pragma unroll
+      for (int v = 0; v < NV; v++) {
+        const R y = res[v] + Cin[(long long)v * N];
+        u[v] = u_in[v] + y;
+        rem[v] = y - (u[v] - u_in[v]);
+      }
+      const R d0 = u[0];
+      u[0] = smax((R)kk_.rho_min, u[0]);
+      const R e0 = u[4];
+      u[4] = smax(u[4], kk_.eps_min * u[0] + (R)0.5 * (u[1] * u[1] + u[2] * u[2] + u[3] * u[3]) / u[0]);
+      if (Cout) {
+        if (u[0] != d0) rem[0] = (R)0;
+        if (u[4] != e0) rem[4] = (R)0;
+#pragma unroll
+        for (int v = 0; v < NV; v++) Cout[(long long)v * N] = rem[v];
+      }
+      return;
+    }
   }
 #pragma unroll
   for (int v = 0; v < NV; v++) u[v] = u_in[v] + res[v];
@@ -971,9 +1007,10 @@ __device__ __forceinline__ bool same_bits<double>(double a, double b) {
 // resident blocks per SM the register budget is set for (FP32: 64 registers)
 template <class R> struct FinBlocks { static constexpr int v = sizeof(R) == 4 ? 4 : 2; };
 
-template <class R>
+// COMP (FP32 compensated mode; Cc its remainders): a field TCheck changes loses its remainder.
+template <class R, bool COMP = false>
 __global__ void __launch_bounds__(FIN_BX* FIN_BY, FinBlocks<R>::v) k_step_finish(Consts c, R* __restrict__ U, R* __restrict__ Pout,
-                                                               Dyn* __restrict__ dyn) {
+                                                               Dyn* __restrict__ dyn, R* __restrict__ Cc) {
   if (dyn->err) return;
   const Geom& g = c.g;
   const DynR<R>& dr = dynr<R>(dyn);
@@ -993,7 +1030,10 @@ __global__ void __launch_bounds__(FIN_BX* FIN_BY, FinBlocks<R>::v) k_step_finish
       tcheck_cell<R>(c, vmax, emax, u[0], u[1], u[2], u[3], u[4]);
 #pragma unroll
       for (int v = 0; v < 5; v++)
-        if (!same_bits(u[v], u0[v])) U[(unsigned)v * g.N32 + id] = u[v];
+        if (!same_bits(u[v], u0[v])) {
+          U[(unsigned)v * g.N32 + id] = u[v];
+          if (COMP) Cc[(unsigned)v * g.N32 + id] = (R)0;
+        }
       R v1, v2, v3, ei;
       prim_from_cons(u[0], u[1], u[2], u[3], u[4], v1, v2, v3, ei);
       const R pr = eos_pres(c, u[0], ei, (R)1.0 / u[0]);
@@ -1036,10 +1076,11 @@ __global__ void __launch_bounds__(FIN_BX* FIN_BY, FinBlocks<R>::v) k_step_finish
 // few spilled), the x sweep 0.623 -> 0.603 ms with 6 (85 registers).
 template <class R> struct TvdBlocks { static constexpr int pencil = sizeof(R) == 4 ? 4 : 1, lanes = sizeof(R) == 4 ? 6 : 1; };
 
-template <class R, int DIR, bool DIAG = false>
+// COMP: FP32 compensated fused steps (Cc: the state's rounding remainders).
+template <class R, int DIR, bool DIAG = false, bool COMP = false>
 __global__ void __launch_bounds__(128, TvdBlocks<R>::pencil) k_tvd_sweep(Consts c, const R* __restrict__ Uin, const R* __restrict__ Pst,
                                                    R* __restrict__ Uout, Dyn* __restrict__ dyn, TvdArgs ta,
-                                                   TvdDiag<R> dg) {
+                                                   TvdDiag<R> dg, R* __restrict__ Cc) {
   const Geom& g = c.g;
   if (dyn->err) return;
   if (ta.only_two_half && !dyn->two_half) return;   // second half pass not taken this step
@@ -1109,7 +1150,16 @@ __global__ void __launch_bounds__(128, TvdBlocks<R>::pencil) k_tvd_sweep(Consts 
       tvd_flux<R, DIR, DIAG>(c, cm1, c0, c1, c2, s0, s1, pos, sz, fac0, cmax_t, hyper, istart, F0, q0, &qv0);
       // update of cell pos (src/tvdlimit_SR.C:565-657)
       R u[NV];
-      tvd_update<R, DIAG>(c, dtt, F0, Fm, q0, qm, c0, uc, u, &dg, id, qv0, qvm);
+      const R* cin = nullptr;
+      R* cout = nullptr;
+      if (COMP) {  // FP32 compensated: the remainders of the interior cell this one is or images
+        const int ci = DIR == 0 ? pos : aa, cj = DIR == 1 ? pos : (DIR == 0 ? aa : bb), ck = DIR == 2 ? pos : bb;
+        const int sj = wrap_interior(cj, g.ny), sk = wrap_interior(ck, g.nz);
+        const long long src = (long long)ci + (long long)g.sx * ((long long)sj + (long long)g.sy * sk);
+        cin = Cc + src;
+        if (sj == cj && sk == ck) cout = Cc + id;
+      }
+      tvd_update<R, DIAG>(c, dtt, F0, Fm, q0, qm, c0, uc, u, &dg, id, qv0, qvm, cin, cout);
       if (!half_images) {
 #pragma unroll
         for (int v = 0; v < NV; v++) Uout[(long long)v * g.N + id] = u[v];
@@ -1137,9 +1187,10 @@ __global__ void __launch_bounds__(128, TvdBlocks<R>::pencil) k_tvd_sweep(Consts 
 template <class R>
 __device__ __forceinline__ R shfl(R v, int src) { return __shfl_sync(0xffffffffu, v, src); }
 
-template <class R>
+template <class R, bool COMP = false>
 __global__ void __launch_bounds__(128, TvdBlocks<R>::lanes) k_tvd_sweep_xlanes(Consts c, const R* __restrict__ Uin, const R* __restrict__ Pst,
-                                                          R* __restrict__ Uout, Dyn* __restrict__ dyn, int only_two_half) {
+                                                          R* __restrict__ Uout, Dyn* __restrict__ dyn, int only_two_half,
+                                                          R* __restrict__ Cc) {
   const Geom& g = c.g;
   if (dyn->err) return;
   if (only_two_half && !dyn->two_half) return;
@@ -1197,7 +1248,14 @@ __global__ void __launch_bounds__(128, TvdBlocks<R>::lanes) k_tvd_sweep_xlanes(C
     R uc[NV], u[NV];
 #pragma unroll
     for (int v = 0; v < NV; v++) uc[v] = Uin[(long long)v * g.N + id];
-    tvd_update<R>(c, dtt, F, Fm, qr, qm, c0, uc, u);
+    const R* cin = nullptr;
+    R* cout = nullptr;
+    if (COMP) {  // FP32 compensated: the remainders of the interior cell this one is or images
+      const int sj = wrap_interior((int)j, g.ny), sk = wrap_interior((int)k, g.nz);
+      cin = Cc + ((long long)g.sx * ((long long)sj + (long long)g.sy * sk) + pos);
+      if (sj == (int)j && sk == (int)k) cout = Cc + id;
+    }
+    tvd_update<R>(c, dtt, F, Fm, qr, qm, c0, uc, u, nullptr, 0, (R)0, (R)0, cin, cout);
 #pragma unroll
     for (int v = 0; v < NV; v++) Uout[(long long)v * g.N + id] = u[v];
   }

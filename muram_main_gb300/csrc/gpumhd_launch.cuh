@@ -46,11 +46,12 @@ struct Launch {
   // then ends the step
   // dg (per-routine TVDlimit on an output step): the diagnostics, through the
   // pencil kernel in every direction
+  // Cc (FP32 compensated fused steps, else null): the state's rounding remainders
   static void tvd(const Consts& c, int dir, int mode, int only_two_half, const R* Uin, const R* Pst, R* Uout,
-                  Dyn* dyn, cudaStream_t s, int td = 0, const TvdDiag<R>* dg = nullptr);
+                  Dyn* dyn, cudaStream_t s, int td = 0, const TvdDiag<R>* dg = nullptr, R* Cc = nullptr);
   // Clean_divB on U (phi, divb: N each); returns the number of launches
   static int divb_clean(const Consts& c, R* U, R* phi, R* divb, Dyn* dyn, cudaStream_t s);
-  static void step_finish(const Consts& c, R* U, R* P, Dyn* dyn, cudaStream_t s);
+  static void step_finish(const Consts& c, R* U, R* P, Dyn* dyn, cudaStream_t s, R* Cc = nullptr);
   // MURaM's physical x boundaries on U (P: ghost pressures, may be null;
   // with_cmax: ghost CFL speeds join the step maximum); part: nz*BND_NQ doubles.
   // Returns the number of launches.
@@ -214,7 +215,7 @@ void Launch<R>::stage(const Consts& c, const R* Uin, const R* Pin, const R* U0, 
 
 template <class R>
 void Launch<R>::tvd(const Consts& c, int dir, int mode, int only_two_half, const R* Uin, const R* Pst, R* Uout,
-                    Dyn* dyn, cudaStream_t s, int td, const TvdDiag<R>* dg) {
+                    Dyn* dyn, cudaStream_t s, int td, const TvdDiag<R>* dg, R* Cc) {
   const Geom& g = c.g;
   TvdArgs ta;
   ta.dir = dir;
@@ -241,9 +242,9 @@ void Launch<R>::tvd(const Consts& c, int dir, int mode, int only_two_half, const
   const int block = 128;
   const long long blocks = (total + block - 1) / block;
   if (dg) {
-    if (dir == 0) k_tvd_sweep<R, 0, true><<<(unsigned)blocks, block, 0, s>>>(c, Uin, Pst, Uout, dyn, ta, *dg);
-    else if (dir == 1) k_tvd_sweep<R, 1, true><<<(unsigned)blocks, block, 0, s>>>(c, Uin, Pst, Uout, dyn, ta, *dg);
-    else k_tvd_sweep<R, 2, true><<<(unsigned)blocks, block, 0, s>>>(c, Uin, Pst, Uout, dyn, ta, *dg);
+    if (dir == 0) k_tvd_sweep<R, 0, true><<<(unsigned)blocks, block, 0, s>>>(c, Uin, Pst, Uout, dyn, ta, *dg, nullptr);
+    else if (dir == 1) k_tvd_sweep<R, 1, true><<<(unsigned)blocks, block, 0, s>>>(c, Uin, Pst, Uout, dyn, ta, *dg, nullptr);
+    else k_tvd_sweep<R, 2, true><<<(unsigned)blocks, block, 0, s>>>(c, Uin, Pst, Uout, dyn, ta, *dg, nullptr);
     return;
   }
   const TvdDiag<R> nod{nullptr, (R)0, (R)0};
@@ -252,12 +253,12 @@ void Launch<R>::tvd(const Consts& c, int dir, int mode, int only_two_half, const
     const long long warps = (long long)g.sy * g.sz * ((g.nx + 27) / 28);
     long long nb = (warps * 32 + block - 1) / block;
     if (nb > 152LL * 16) nb = 152LL * 16;   // grid-stride: a few waves of resident blocks
-    k_tvd_sweep_xlanes<R><<<(unsigned)nb, block, 0, s>>>(c, Uin, Pst, Uout, dyn, only_two_half);
+    (Cc ? k_tvd_sweep_xlanes<R, true> : k_tvd_sweep_xlanes<R, false>)<<<(unsigned)nb, block, 0, s>>>(c, Uin, Pst, Uout, dyn, only_two_half, Cc);
     return;
   }
-  if (dir == 0) k_tvd_sweep<R, 0><<<(unsigned)blocks, block, 0, s>>>(c, Uin, Pst, Uout, dyn, ta, nod);
-  else if (dir == 1) k_tvd_sweep<R, 1><<<(unsigned)blocks, block, 0, s>>>(c, Uin, Pst, Uout, dyn, ta, nod);
-  else k_tvd_sweep<R, 2><<<(unsigned)blocks, block, 0, s>>>(c, Uin, Pst, Uout, dyn, ta, nod);
+  if (dir == 0) (Cc ? k_tvd_sweep<R, 0, false, true> : k_tvd_sweep<R, 0, false, false>)<<<(unsigned)blocks, block, 0, s>>>(c, Uin, Pst, Uout, dyn, ta, nod, Cc);
+  else if (dir == 1) (Cc ? k_tvd_sweep<R, 1, false, true> : k_tvd_sweep<R, 1, false, false>)<<<(unsigned)blocks, block, 0, s>>>(c, Uin, Pst, Uout, dyn, ta, nod, Cc);
+  else (Cc ? k_tvd_sweep<R, 2, false, true> : k_tvd_sweep<R, 2, false, false>)<<<(unsigned)blocks, block, 0, s>>>(c, Uin, Pst, Uout, dyn, ta, nod, Cc);
 }
 
 template <class R>
@@ -313,7 +314,7 @@ void Launch<R>::sflx_update(const Consts& c, R* S, const R* S0, R* Rflx, const D
   k_sflx_update<R><<<grid_for((long long)c.g.nx * c.g.ny * c.g.nz, 256), 256, 0, s>>>(c, S, S0, Rflx, dyn, stage);
 }
 template <class R>
-void Launch<R>::step_finish(const Consts& c, R* U, R* P, Dyn* dyn, cudaStream_t s) {
+void Launch<R>::step_finish(const Consts& c, R* U, R* P, Dyn* dyn, cudaStream_t s, R* Cc) {
   const Geom& g = c.g;
   const dim3 block(FIN_BX, FIN_BY);
   // z planes per block: one wave of resident blocks (each block marches
@@ -323,7 +324,7 @@ void Launch<R>::step_finish(const Consts& c, R* U, R* P, Dyn* dyn, cudaStream_t 
   int gz = (152 * FinBlocks<R>::v) / bxy;
   gz = gz < 1 ? 1 : (gz > g.nz ? g.nz : gz);
   const dim3 grid((g.nx + FIN_BX - 1) / FIN_BX, (g.ny + FIN_BY - 1) / FIN_BY, gz);
-  k_step_finish<R><<<grid, block, 0, s>>>(c, U, P, dyn);
+  (Cc ? k_step_finish<R, true> : k_step_finish<R, false>)<<<grid, block, 0, s>>>(c, U, P, dyn, Cc);
 }
 template <class R>
 void Launch<R>::cons_to_prim(const Consts& c, R* U, R* P, R* T, R* Ne, R* Ri, R* Am, cudaStream_t s) {

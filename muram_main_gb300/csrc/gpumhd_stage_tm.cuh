@@ -400,9 +400,13 @@ __global__ void __launch_bounds__(TX* TY, 2)
     R base[NV];
     if (active) {
       // RESID: U0 is the residual to add to (null: start from zero)
-      const R* src = U0;
+      if (!RESID || U0) {
 #pragma unroll
-      for (int q = 0; q < NV; q++) base[q] = src ? src[id + (unsigned)q * g.N32] : (R)0;
+        for (int q = 0; q < NV; q++) base[q] = U0[id + (unsigned)q * g.N32];
+      } else {
+#pragma unroll
+        for (int q = 0; q < NV; q++) base[q] = (R)0;
+      }
     }
     if (pend) finish_pressure(k - 1);
     tm::tmem_wait_st();

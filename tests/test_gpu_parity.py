@@ -291,6 +291,52 @@ def test_fp32_compensated_rk_updates(gpu_lib):
     assert not np.array_equal(states[0], states[1])
 
 
+def test_fp32_compensated_stratified_200_steps(gpu_lib):
+    """The stratified configuration at its run length (128 vertical x 64 x 64
+    at 16 km on the 3000 x 3000 table, closed x, gravity 2.74e4), 200 steps:
+    compensated FP32 -- the rounding remainders carried through the RK stage
+    sums and the TVD sweeps -- meets relative L2 <= 1e-5 per field against the
+    FP64 mode (which matches the reference to 1e-12), and improves on plain
+    FP32 in the vertical momentum, the field hydrostatic balance makes the
+    most sensitive to rounding."""
+    import bench
+    from muram_main_gb300 import eos_table
+    eos_table.ensure_table(bench.EOS_BENCH, "bench")
+    U = bench.make_state(128, 64, 64, seed=7)
+    res = {}
+    for prec, comp in ((64, 0), (32, 0), (32, 1)):
+        p = gpumhd.default_params(128, 64, 64, 1.6e6, precision=prec, periodic_x=0, grav=2.74e4, compensated=comp)
+        g = gpumhd.MuramGPU(p, eos_path=bench.EOS_BENCH)
+        g.upload_state(U)
+        g.run_steps(200)
+        res[(prec, comp)] = H.interior(g.download_state())
+        g.close()
+    ref = res[(64, 0)]
+    e0 = H.rel_l2(res[(32, 0)], ref)
+    e1 = H.rel_l2(res[(32, 1)], ref)
+    print("stratified 200 steps, FP32 rel L2 -- plain:", np.array2string(e0, precision=2),
+          "compensated:", np.array2string(e1, precision=2))
+    assert np.all(e1 <= TOL32_L2), e1
+    assert e1[1] < e0[1]
+
+
+@pytest.mark.parametrize("name", ["two_half_tvd", "closed_gravity"])
+def test_fp32_compensated_fixtures(gpu_lib, name):
+    """Compensated FP32 on the reference's fixtures: two half TVD passes (the
+    remainders carried through both), and the closed x with gravity (ghost
+    images of the mirror rule)."""
+    d, hp = H.load_case(name)
+    p = H.gpu_params(hp, 32)
+    p.compensated = 1
+    g = gpumhd.MuramGPU(p, eos_path=H.EOS_SMALL)
+    g.upload_state(d["input_U"])
+    dts = g.run_steps(int(d["steps"]))
+    assert np.allclose(dts, d["dts"].reshape(-1, 3)[:, 0], rtol=1e-5, atol=0)
+    e = H.rel_l2(H.interior(g.download_state()), H.interior(d["final_U"]))
+    print(f"compensated FP32 [{name}] rel L2:", np.array2string(e, precision=2))
+    assert np.all(e <= TOL32_L2), e
+
+
 def _oracle_run_p(p, U, steps):
     from oracle import oracle as O
     eos = O.Eos(H.EOS_SMALL)
