@@ -168,39 +168,79 @@ def time_device(g, steps, warmup):
     return e0.elapsed_time(e1), g.launch_count - n0
 
 
-def time_e2e(g, steps, U):
+def time_e2e(g, steps, U, host_dtype="float64"):
     """End to end through the C ABI: per step the host state (pinned, cState
-    layout, float64) goes to the device, one fused step runs, and the result
-    comes back to the host.  The transfers are the asynchronous ones, so one
-    step's upload and the previous step's download overlap the steps around
-    them; every byte of every step crosses the link inside the timed region.
-    Returns (ms, h2d bytes per step, d2h bytes per step, result check)."""
+    layout: float64 as MURaM's default build holds it, or float32 as its
+    SINGLE_PRECISION build does) goes to the device, one fused step runs, and
+    the result comes back to the host.  The transfers are the asynchronous
+    ones, so one step's upload and the previous step's download overlap the
+    steps around them; every byte of every step crosses the link inside the
+    timed region.  Returns (ms, h2d bytes per step, d2h bytes per step,
+    result check)."""
     import numpy as np
     import torch
     from muram_main_gb300 import gpumhd
-    aos = np.ascontiguousarray(np.moveaxis(U, 0, -1))
+    aos = np.ascontiguousarray(np.moveaxis(U, 0, -1), dtype=host_dtype)
     h_in = torch.from_numpy(aos.reshape(-1)).pin_memory()
     h_out = torch.empty_like(h_in).pin_memory()
     h_ref = torch.empty_like(h_in).pin_memory()
-    nbytes = h_in.numel() * 8
+    nbytes = h_in.numel() * h_in.element_size()
     # the expected result of one step from h_in, through the synchronous calls
-    g.upload_ptr(gpumhd.FIELD_U, h_in.data_ptr())
+    g.upload_ptr(gpumhd.FIELD_U, h_in.data_ptr(), host_dtype)
     g.run_steps(1)
-    g.download_ptr(gpumhd.FIELD_U, h_ref.data_ptr())
-    g.upload_ptr_async(gpumhd.FIELD_U, h_in.data_ptr())
+    g.download_ptr(gpumhd.FIELD_U, h_ref.data_ptr(), host_dtype)
+    g.upload_ptr_async(gpumhd.FIELD_U, h_in.data_ptr(), host_dtype)
     g.enqueue_steps(1)
-    g.download_ptr_async(gpumhd.FIELD_U, h_out.data_ptr())
+    g.download_ptr_async(gpumhd.FIELD_U, h_out.data_ptr(), host_dtype)
     g.synchronize()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(steps):
-        g.upload_ptr_async(gpumhd.FIELD_U, h_in.data_ptr())
+        g.upload_ptr_async(gpumhd.FIELD_U, h_in.data_ptr(), host_dtype)
         g.enqueue_steps(1)
-        g.download_ptr_async(gpumhd.FIELD_U, h_out.data_ptr())
+        g.download_ptr_async(gpumhd.FIELD_U, h_out.data_ptr(), host_dtype)
     g.synchronize()
     ms = (time.perf_counter() - t0) * 1e3
     same = bool(torch.equal(h_out, h_ref))
     return ms, nbytes, nbytes, same
+
+
+def time_link(nbytes, reps=4):
+    """The host link alone for one step's bytes: pinned host -> device,
+    device -> pinned host, and both at once on two streams (GB/s per direction,
+    best of reps, host clock around synchronised copies)."""
+    import torch
+    n = nbytes // 4
+    h_a = torch.empty(n, dtype=torch.float32).pin_memory()
+    h_b = torch.empty(n, dtype=torch.float32).pin_memory()
+    d_a = torch.empty(n, dtype=torch.float32, device="cuda")
+    d_b = torch.empty(n, dtype=torch.float32, device="cuda")
+    s_a, s_b = torch.cuda.Stream(), torch.cuda.Stream()
+
+    def best(fn):
+        fn()
+        torch.cuda.synchronize()
+        t = None
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            fn()
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t0
+            t = dt if t is None else min(t, dt)
+        return round(nbytes / t / 1e9, 1)
+
+    def both():
+        with torch.cuda.stream(s_a):
+            d_a.copy_(h_a, non_blocking=True)
+        with torch.cuda.stream(s_b):
+            h_b.copy_(d_b, non_blocking=True)
+
+    out = {"h2d_gbs": best(lambda: d_a.copy_(h_a, non_blocking=True)),
+           "d2h_gbs": best(lambda: h_b.copy_(d_b, non_blocking=True)),
+           "both_directions_gbs_each": best(both)}
+    del h_a, h_b, d_a, d_b
+    torch.cuda.empty_cache()
+    return out
 
 
 def words_per_cell(phase):
@@ -362,15 +402,27 @@ def run_ours(args):
     step_ms = ms / args.steps
     # end to end through the C ABI with host buffers
     e2e = None
+    e2e_f32_host = None
     if not args.no_e2e:
-        e2e_steps = max(4, min(args.steps, 20))
+        e2e_steps = max(4, min(args.steps, 50))
         e2e_ms, h2d, d2h, same = time_e2e(g, e2e_steps, U)
         e2e_ms = replica_max(e2e_ms)
         e2e = {"value": job_rate(ws, n_cells, e2e_steps, e2e_ms), "unit": UNIT,
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h, "steps": e2e_steps,
                "ms_per_step": round(e2e_ms / e2e_steps, 3),
+               "host_layout": "cState float64 (MURaM's default build)",
+               "link_alone": time_link(h2d),
                "transfers": "asynchronous upload / download on copy streams, overlapping the neighbouring steps",
                "result_equals_synchronous_path": same}
+        # the same with the float32 host layout of a SINGLE_PRECISION build
+        f_ms, f_h2d, f_d2h, f_same = time_e2e(g, e2e_steps, U, "float32")
+        f_ms = replica_max(f_ms)
+        e2e_f32_host = {"value": job_rate(ws, n_cells, e2e_steps, f_ms), "unit": UNIT,
+                        "h2d_bytes_per_step": f_h2d, "d2h_bytes_per_step": f_d2h, "steps": e2e_steps,
+                        "ms_per_step": round(f_ms / e2e_steps, 3),
+                        "host_layout": "cState float32 (MURaM built with SINGLE_PRECISION)",
+                        "link_alone": time_link(f_h2d),
+                        "result_equals_synchronous_path": f_same}
     # the per-routine entry points in ComputeSolution's order (how MURaM itself
     # calls the library through the drop-in shim), device-resident
     per_routine = None
@@ -471,6 +523,7 @@ def run_ours(args):
         "step_hbm_gbs": round(step_bytes / (step_ms / 1e3) / 1e9, 1),
         "phases_ms": {k: round(v, 4) for k, v in phases.items()},
         "e2e": e2e,
+        "e2e_f32_host": e2e_f32_host,
         "per_routine": per_routine,
         "gpu_launches": launches,
         "clocks": clocks.summary(),

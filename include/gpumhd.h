@@ -123,6 +123,13 @@ int gpumhd_eos_init(gpumhd_ctx* ctx, const char* path);
  * (GridData, see gpumhd_set_need_diagnostics); one double per node. */
 int gpumhd_upload(gpumhd_ctx* ctx, int which, const double* host);
 int gpumhd_download(gpumhd_ctx* ctx, int which, double* host);
+/* The same with float host arrays: the cState arrays (U, U0) of GridData in
+ * MURaM built with SINGLE_PRECISION (include/precision.h:4-10,
+ * include/physics.H:77: cState<real>, 8 floats per node; GridData's other
+ * arrays stay double, include/grid.H:53-100).  Any field takes either layout,
+ * and either precision of context accepts both. */
+int gpumhd_upload_f32(gpumhd_ctx* ctx, int which, const float* host);
+int gpumhd_download_f32(gpumhd_ctx* ctx, int which, float* host);
 /* The same transfers without waiting (no reference counterpart): each one
  * is ordered with the context's steps as the synchronous call is, but its
  * host copy runs on a copy stream of its own, so that the upload of one
@@ -135,6 +142,9 @@ int gpumhd_download(gpumhd_ctx* ctx, int which, double* host);
  * buffer, so any number may be queued. */
 int gpumhd_upload_async(gpumhd_ctx* ctx, int which, const double* host);
 int gpumhd_download_async(gpumhd_ctx* ctx, int which, double* host);
+/* The asynchronous transfers with float host arrays (SINGLE_PRECISION layout). */
+int gpumhd_upload_async_f32(gpumhd_ctx* ctx, int which, const float* host);
+int gpumhd_download_async_f32(gpumhd_ctx* ctx, int which, float* host);
 
 /* Clean_divB (include/divB.H:5, src/clean_divB.C:35-369): damped iterations
  * phi += fac*divB - 0.65*phi, B += grad phi, e += phi*divB on U, their count

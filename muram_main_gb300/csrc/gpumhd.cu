@@ -803,7 +803,9 @@ static int ensure_staging(gpumhd_ctx* ctx) {
   return GPUMHD_OK;
 }
 
-extern "C" int gpumhd_upload(gpumhd_ctx* ctx, int which, const double* host) {
+// Host element type H: double (MURaM's default build) or float (SINGLE_PRECISION).
+template <class H>
+static int upload_impl(gpumhd_ctx* ctx, int which, const H* host) {
   if (!ctx || !host) return GPUMHD_E_INVALID;
   CK(cudaSetDevice(ctx->device));
   int nf, rc;
@@ -812,9 +814,10 @@ extern "C" int gpumhd_upload(gpumhd_ctx* ctx, int which, const double* host) {
   rc = ensure_staging(ctx);
   if (rc) return rc;
   const long long N = ctx->c.g.N;
-  CK(cudaMemcpyAsync(ctx->staging, host, sizeof(double) * nf * N, cudaMemcpyHostToDevice, ctx->stream));
-  if (ctx->f32) Launch<float>::aos_to_soa(N, nf, ctx->staging, (float*)dst, ctx->stream);
-  else Launch<double>::aos_to_soa(N, nf, ctx->staging, (double*)dst, ctx->stream);
+  H* const stg = reinterpret_cast<H*>(ctx->staging);
+  CK(cudaMemcpyAsync(stg, host, sizeof(H) * nf * N, cudaMemcpyHostToDevice, ctx->stream));
+  if (ctx->f32) Launch<float>::aos_to_soa(N, nf, stg, (float*)dst, ctx->stream);
+  else Launch<double>::aos_to_soa(N, nf, stg, (double*)dst, ctx->stream);
   if (which == 0) {
     ctx->fused_ready = false;
     if (ctx->comp) CK(cudaMemsetAsync(ctx->comp, 0, sizeof(float) * 8 * N, ctx->stream));
@@ -822,6 +825,8 @@ extern "C" int gpumhd_upload(gpumhd_ctx* ctx, int which, const double* host) {
   if (which == 3) ctx->have_pres = true;
   return check_launch(ctx, 1);
 }
+extern "C" int gpumhd_upload(gpumhd_ctx* ctx, int which, const double* host) { return upload_impl(ctx, which, host); }
+extern "C" int gpumhd_upload_f32(gpumhd_ctx* ctx, int which, const float* host) { return upload_impl(ctx, which, host); }
 
 // dst's state (U) = periodic tiling of src's state; same precision, and dst's
 // interior sizes multiples of src's.  Ghosts filled with dst's boundary rule.
@@ -864,7 +869,8 @@ static int ensure_async(gpumhd_ctx* ctx) {
 // the conversion of the upload before last (two buffers in turn), so it
 // overlaps the steps enqueued before it; the conversion into the field runs
 // in stream order.
-extern "C" int gpumhd_upload_async(gpumhd_ctx* ctx, int which, const double* host) {
+template <class H>
+static int upload_async_impl(gpumhd_ctx* ctx, int which, const H* host) {
   if (!ctx || !host) return GPUMHD_E_INVALID;
   CK(cudaSetDevice(ctx->device));
   int nf, rc;
@@ -875,11 +881,12 @@ extern "C" int gpumhd_upload_async(gpumhd_ctx* ctx, int which, const double* hos
   const long long N = ctx->c.g.N;
   const int b = (int)(ctx->n_up++ & 1u);
   CK(cudaStreamWaitEvent(ctx->s_in, ctx->ev_in_free[b], 0));
-  CK(cudaMemcpyAsync(ctx->astage_in[b], host, sizeof(double) * nf * N, cudaMemcpyHostToDevice, ctx->s_in));
+  H* const stg = reinterpret_cast<H*>(ctx->astage_in[b]);
+  CK(cudaMemcpyAsync(stg, host, sizeof(H) * nf * N, cudaMemcpyHostToDevice, ctx->s_in));
   CK(cudaEventRecord(ctx->ev_in_ready[b], ctx->s_in));
   CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_in_ready[b], 0));
-  if (ctx->f32) Launch<float>::aos_to_soa(N, nf, ctx->astage_in[b], (float*)dst, ctx->stream);
-  else Launch<double>::aos_to_soa(N, nf, ctx->astage_in[b], (double*)dst, ctx->stream);
+  if (ctx->f32) Launch<float>::aos_to_soa(N, nf, stg, (float*)dst, ctx->stream);
+  else Launch<double>::aos_to_soa(N, nf, stg, (double*)dst, ctx->stream);
   CK(cudaEventRecord(ctx->ev_in_free[b], ctx->stream));
   if (which == 0) {
     ctx->fused_ready = false;
@@ -888,11 +895,18 @@ extern "C" int gpumhd_upload_async(gpumhd_ctx* ctx, int which, const double* hos
   if (which == 3) ctx->have_pres = true;
   return check_launch(ctx, 1);
 }
+extern "C" int gpumhd_upload_async(gpumhd_ctx* ctx, int which, const double* host) {
+  return upload_async_impl(ctx, which, host);
+}
+extern "C" int gpumhd_upload_async_f32(gpumhd_ctx* ctx, int which, const float* host) {
+  return upload_async_impl(ctx, which, host);
+}
 
 // Download through the copy-out stream: the field is converted in stream
 // order into a copy-out buffer (once the download before last has left it)
 // and copied to the host while later steps run.
-extern "C" int gpumhd_download_async(gpumhd_ctx* ctx, int which, double* host) {
+template <class H>
+static int download_async_impl(gpumhd_ctx* ctx, int which, H* host) {
   if (!ctx || !host) return GPUMHD_E_INVALID;
   CK(cudaSetDevice(ctx->device));
   int nf, rc;
@@ -903,18 +917,26 @@ extern "C" int gpumhd_download_async(gpumhd_ctx* ctx, int which, double* host) {
   const long long N = ctx->c.g.N;
   const int b = (int)(ctx->n_down++ & 1u);
   CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_out_free[b], 0));
-  if (ctx->f32) Launch<float>::soa_to_aos(N, nf, (const float*)src, ctx->astage_out[b], ctx->stream);
-  else Launch<double>::soa_to_aos(N, nf, (const double*)src, ctx->astage_out[b], ctx->stream);
+  H* const stg = reinterpret_cast<H*>(ctx->astage_out[b]);
+  if (ctx->f32) Launch<float>::soa_to_aos(N, nf, (const float*)src, stg, ctx->stream);
+  else Launch<double>::soa_to_aos(N, nf, (const double*)src, stg, ctx->stream);
   rc = check_launch(ctx, 1);
   if (rc) return rc;
   CK(cudaEventRecord(ctx->ev_out_ready[b], ctx->stream));
   CK(cudaStreamWaitEvent(ctx->s_out, ctx->ev_out_ready[b], 0));
-  CK(cudaMemcpyAsync(host, ctx->astage_out[b], sizeof(double) * nf * N, cudaMemcpyDeviceToHost, ctx->s_out));
+  CK(cudaMemcpyAsync(host, stg, sizeof(H) * nf * N, cudaMemcpyDeviceToHost, ctx->s_out));
   CK(cudaEventRecord(ctx->ev_out_free[b], ctx->s_out));
   return GPUMHD_OK;
 }
+extern "C" int gpumhd_download_async(gpumhd_ctx* ctx, int which, double* host) {
+  return download_async_impl(ctx, which, host);
+}
+extern "C" int gpumhd_download_async_f32(gpumhd_ctx* ctx, int which, float* host) {
+  return download_async_impl(ctx, which, host);
+}
 
-extern "C" int gpumhd_download(gpumhd_ctx* ctx, int which, double* host) {
+template <class H>
+static int download_impl(gpumhd_ctx* ctx, int which, H* host) {
   if (!ctx || !host) return GPUMHD_E_INVALID;
   CK(cudaSetDevice(ctx->device));
   int nf, rc;
@@ -923,14 +945,17 @@ extern "C" int gpumhd_download(gpumhd_ctx* ctx, int which, double* host) {
   rc = ensure_staging(ctx);
   if (rc) return rc;
   const long long N = ctx->c.g.N;
-  if (ctx->f32) Launch<float>::soa_to_aos(N, nf, (const float*)src, ctx->staging, ctx->stream);
-  else Launch<double>::soa_to_aos(N, nf, (const double*)src, ctx->staging, ctx->stream);
+  H* const stg = reinterpret_cast<H*>(ctx->staging);
+  if (ctx->f32) Launch<float>::soa_to_aos(N, nf, (const float*)src, stg, ctx->stream);
+  else Launch<double>::soa_to_aos(N, nf, (const double*)src, stg, ctx->stream);
   rc = check_launch(ctx, 1);
   if (rc) return rc;
-  CK(cudaMemcpyAsync(host, ctx->staging, sizeof(double) * nf * N, cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaMemcpyAsync(host, stg, sizeof(H) * nf * N, cudaMemcpyDeviceToHost, ctx->stream));
   CK(cudaStreamSynchronize(ctx->stream));
   return GPUMHD_OK;
 }
+extern "C" int gpumhd_download(gpumhd_ctx* ctx, int which, double* host) { return download_impl(ctx, which, host); }
+extern "C" int gpumhd_download_f32(gpumhd_ctx* ctx, int which, float* host) { return download_impl(ctx, which, host); }
 
 #define DISPATCH(call_f, call_d) (ctx->f32 ? (call_f) : (call_d))
 

@@ -1640,15 +1640,15 @@ __global__ void k_fill_ghosts(Geom g, R* __restrict__ U, int nfield, int with_bc
 }
 
 // Host cState (AoS, double) <-> device SoA (R)
-template <class R>
-__global__ void k_aos_to_soa(long long N, int nf, const double* __restrict__ A, R* __restrict__ S) {
+template <class R, class H>
+__global__ void k_aos_to_soa(long long N, int nf, const H* __restrict__ A, R* __restrict__ S) {
   for (long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x; id < N; id += (long long)gridDim.x * blockDim.x)
     for (int v = 0; v < nf; v++) S[(long long)v * N + id] = (R)A[id * nf + v];
 }
-template <class R>
-__global__ void k_soa_to_aos(long long N, int nf, const R* __restrict__ S, double* __restrict__ A) {
+template <class R, class H>
+__global__ void k_soa_to_aos(long long N, int nf, const R* __restrict__ S, H* __restrict__ A) {
   for (long long id = (long long)blockIdx.x * blockDim.x + threadIdx.x; id < N; id += (long long)gridDim.x * blockDim.x)
-    for (int v = 0; v < nf; v++) A[id * nf + v] = (double)S[(long long)v * N + id];
+    for (int v = 0; v < nf; v++) A[id * nf + v] = (H)S[(long long)v * N + id];
 }
 
 }  // namespace gpumhd

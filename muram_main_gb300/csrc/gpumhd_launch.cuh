@@ -80,8 +80,11 @@ struct Launch {
                             cudaStream_t s);
   static void fill_ghosts(const Consts& c, R* U, int nfield, int with_bc, cudaStream_t s);
   static void tile_state(const Geom& gd, const Geom& gs, const R* Us, R* Ud, cudaStream_t s);
+  // host cState layout (double, or float as in MURaM's SINGLE_PRECISION build) <-> device SoA
   static void aos_to_soa(long long N, int nf, const double* A, R* S, cudaStream_t s);
   static void soa_to_aos(long long N, int nf, const R* S, double* A, cudaStream_t s);
+  static void aos_to_soa(long long N, int nf, const float* A, R* S, cudaStream_t s);
+  static void soa_to_aos(long long N, int nf, const R* S, float* A, cudaStream_t s);
 };
 
 // Tile shapes of the stage kernel per state type.
@@ -380,11 +383,19 @@ void Launch<R>::fill_ghosts(const Consts& c, R* U, int nfield, int with_bc, cuda
 }
 template <class R>
 void Launch<R>::aos_to_soa(long long N, int nf, const double* A, R* S, cudaStream_t s) {
-  k_aos_to_soa<R><<<grid_for(N, 256), 256, 0, s>>>(N, nf, A, S);
+  k_aos_to_soa<R, double><<<grid_for(N, 256), 256, 0, s>>>(N, nf, A, S);
 }
 template <class R>
 void Launch<R>::soa_to_aos(long long N, int nf, const R* S, double* A, cudaStream_t s) {
-  k_soa_to_aos<R><<<grid_for(N, 256), 256, 0, s>>>(N, nf, S, A);
+  k_soa_to_aos<R, double><<<grid_for(N, 256), 256, 0, s>>>(N, nf, S, A);
+}
+template <class R>
+void Launch<R>::aos_to_soa(long long N, int nf, const float* A, R* S, cudaStream_t s) {
+  k_aos_to_soa<R, float><<<grid_for(N, 256), 256, 0, s>>>(N, nf, A, S);
+}
+template <class R>
+void Launch<R>::soa_to_aos(long long N, int nf, const R* S, float* A, cudaStream_t s) {
+  k_soa_to_aos<R, float><<<grid_for(N, 256), 256, 0, s>>>(N, nf, S, A);
 }
 #endif
 

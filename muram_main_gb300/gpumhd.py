@@ -74,7 +74,8 @@ EXPORTS = [
     "gpumhd_ensemble_destroy", "gpumhd_ensemble_enqueue_steps", "gpumhd_ensemble_synchronize",
     "gpumhd_ensemble_last_error", "gpumhd_ensemble_stream", "gpumhd_ensemble_launch_count",
     "gpumhd_clean_divB", "gpumhd_divb_info", "gpumhd_boundary_info", "gpumhd_test_tma_wait",
-    "gpumhd_set_divb_iters", "gpumhd_set_need_diagnostics",
+    "gpumhd_set_divb_iters", "gpumhd_set_need_diagnostics", "gpumhd_upload_f32", "gpumhd_download_f32",
+    "gpumhd_upload_async_f32", "gpumhd_download_async_f32",
 ]
 
 _lib = None
@@ -96,6 +97,7 @@ def load(build_if_missing=True):
     L = C.CDLL(_build.LIB)
     vp = C.c_void_p
     dp = C.POINTER(C.c_double)
+    fp = C.POINTER(C.c_float)
     P = C.POINTER(Params)
     sig = {
         "gpumhd_default_params": (C.c_int, [P, C.c_int, C.c_int, C.c_int, C.c_double]),
@@ -109,6 +111,10 @@ def load(build_if_missing=True):
         "gpumhd_upload_async": (C.c_int, [vp, C.c_int, dp]),
         "gpumhd_download_async": (C.c_int, [vp, C.c_int, dp]),
         "gpumhd_download": (C.c_int, [vp, C.c_int, dp]),
+        "gpumhd_upload_f32": (C.c_int, [vp, C.c_int, fp]),
+        "gpumhd_upload_async_f32": (C.c_int, [vp, C.c_int, fp]),
+        "gpumhd_download_async_f32": (C.c_int, [vp, C.c_int, fp]),
+        "gpumhd_download_f32": (C.c_int, [vp, C.c_int, fp]),
         "gpumhd_save_cons": (C.c_int, [vp]),
         "gpumhd_cons_to_prim": (C.c_int, [vp]),
         "gpumhd_adjust_valf_max": (C.c_int, [vp]),
@@ -208,13 +214,24 @@ class MuramGPU:
 
     # -- data movement (ACCH::UpdateGPU / UpdateCPU)
     def upload(self, which, aos):
+        """aos in cState layout: float64, or float32 as a SINGLE_PRECISION
+        MURaM build holds it (any other dtype is converted to float64)."""
+        if np.asarray(aos).dtype == np.float32:
+            a = np.ascontiguousarray(aos)
+            self._chk(self._L.gpumhd_upload_f32(self._h, which, a.ctypes.data_as(C.POINTER(C.c_float))))
+            return
         a = np.ascontiguousarray(aos, dtype=np.float64)
         self._chk(self._L.gpumhd_upload(self._h, which, _dptr(a)))
 
-    def download(self, which):
+    def download(self, which, dtype=np.float64):
         nf = 8 if which <= FIELD_RES else 1
-        out = np.empty(int(np.prod(self.shape)) * nf, dtype=np.float64)
-        self._chk(self._L.gpumhd_download(self._h, which, _dptr(out)))
+        out = np.empty(int(np.prod(self.shape)) * nf, dtype=dtype)
+        if out.dtype == np.float32:
+            self._chk(self._L.gpumhd_download_f32(self._h, which, out.ctypes.data_as(C.POINTER(C.c_float))))
+        elif out.dtype == np.float64:
+            self._chk(self._L.gpumhd_download(self._h, which, _dptr(out)))
+        else:
+            raise ValueError(f"download: host layout float64 or float32, not {out.dtype}")
         return out
 
     def upload_state(self, U, which=FIELD_U):
@@ -393,22 +410,32 @@ class MuramGPU:
         self._chk(self._L.gpumhd_profile_steps(self._h, nsteps, _dptr(ms)))
         return dict(zip(self.PHASES, ms.tolist()))
 
-    def upload_ptr(self, which, ptr):
-        """Upload from a raw host pointer (e.g. pinned memory) in cState layout."""
-        self._chk(self._L.gpumhd_upload(self._h, which, C.cast(ptr, C.POINTER(C.c_double))))
+    def _xfer(self, name, which, ptr, host_dtype):
+        if np.dtype(host_dtype) == np.float32:
+            fn, t = getattr(self._L, name + "_f32"), C.c_float
+        elif np.dtype(host_dtype) == np.float64:
+            fn, t = getattr(self._L, name), C.c_double
+        else:
+            raise ValueError(f"host layout float64 or float32, not {np.dtype(host_dtype)}")
+        self._chk(fn(self._h, which, C.cast(ptr, C.POINTER(t))))
 
-    def download_ptr(self, which, ptr):
-        self._chk(self._L.gpumhd_download(self._h, which, C.cast(ptr, C.POINTER(C.c_double))))
+    def upload_ptr(self, which, ptr, host_dtype=np.float64):
+        """Upload from a raw host pointer (e.g. pinned memory) in cState layout
+        of host_dtype (float64, or float32 as in a SINGLE_PRECISION build)."""
+        self._xfer("gpumhd_upload", which, ptr, host_dtype)
 
-    def upload_ptr_async(self, which, ptr):
+    def download_ptr(self, which, ptr, host_dtype=np.float64):
+        self._xfer("gpumhd_download", which, ptr, host_dtype)
+
+    def upload_ptr_async(self, which, ptr, host_dtype=np.float64):
         """Upload from a host pointer without waiting: the copy overlaps the
         steps enqueued before it; the buffer must stay valid and unchanged
         until synchronize()."""
-        self._chk(self._L.gpumhd_upload_async(self._h, which, C.cast(ptr, C.POINTER(C.c_double))))
+        self._xfer("gpumhd_upload_async", which, ptr, host_dtype)
 
-    def download_ptr_async(self, which, ptr):
+    def download_ptr_async(self, which, ptr, host_dtype=np.float64):
         """Download to a host pointer without waiting; the data are there after synchronize()."""
-        self._chk(self._L.gpumhd_download_async(self._h, which, C.cast(ptr, C.POINTER(C.c_double))))
+        self._xfer("gpumhd_download_async", which, ptr, host_dtype)
 
     def adjoint(self, nsteps, dJ_dUT, checkpoint_every=5):
         """dJ/dU_0 for J(U_T) over nsteps fixed-dt FP64 steps from the current

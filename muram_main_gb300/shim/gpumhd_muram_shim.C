@@ -58,6 +58,24 @@ void check(const char* where, int rc) {
   if (rc != GPUMHD_OK) die(where, rc);
 }
 
+// GridData's cState arrays (U, U0) hold `real`: float in a SINGLE_PRECISION
+// build (include/precision.h:4-10, include/physics.H:77), double otherwise;
+// its other arrays are double in both (include/grid.H:53-100).
+int upload_cstate(int which, const void* ptr) {
+#ifdef SINGLE_PRECISION
+  return gpumhd_upload_f32(g_ctx, which, static_cast<const float*>(ptr));
+#else
+  return gpumhd_upload(g_ctx, which, static_cast<const double*>(ptr));
+#endif
+}
+int download_cstate(int which, void* ptr) {
+#ifdef SINGLE_PRECISION
+  return gpumhd_download_f32(g_ctx, which, static_cast<float*>(ptr));
+#else
+  return gpumhd_download(g_ctx, which, static_cast<double*>(ptr));
+#endif
+}
+
 void fill_params(gpumhd_params& p, const RunData& Run, const GridData& Grid, const PhysicsData& Physics) {
   gpumhd_default_params(&p, Grid.lsize[0], Grid.lsize[1], Grid.lsize[2], Grid.dx[0]);
 #ifdef GPUMHD_FP32
@@ -239,8 +257,8 @@ void SetBoundaryConditions(const RunData& Run, GridData& Grid, const PhysicsData
 namespace ACCH {
 void UpdateCPU(void* ptr, std::size_t) {
   if (!g_ctx || !g_grid) return;
-  if (ptr == g_grid->U) check("download U", gpumhd_download(g_ctx, 0, (double*)ptr));
-  else if (ptr == g_grid->U0) check("download U0", gpumhd_download(g_ctx, 1, (double*)ptr));
+  if (ptr == g_grid->U) check("download U", download_cstate(0, ptr));
+  else if (ptr == g_grid->U0) check("download U0", download_cstate(1, ptr));
   else if (ptr == g_grid->pres) check("download pres", gpumhd_download(g_ctx, 3, (double*)ptr));
   else if (ptr == g_grid->temp) check("download temp", gpumhd_download(g_ctx, 4, (double*)ptr));
   else if (ptr == g_grid->ne) check("download ne", gpumhd_download(g_ctx, 5, (double*)ptr));
@@ -258,8 +276,8 @@ void UpdateCPU(void* ptr, std::size_t) {
 }
 void UpdateGPU(void* ptr, std::size_t) {
   if (!g_ctx || !g_grid) return;
-  if (ptr == g_grid->U) check("upload U", gpumhd_upload(g_ctx, 0, (const double*)ptr));
-  else if (ptr == g_grid->U0) check("upload U0", gpumhd_upload(g_ctx, 1, (const double*)ptr));
+  if (ptr == g_grid->U) check("upload U", upload_cstate(0, ptr));
+  else if (ptr == g_grid->U0) check("upload U0", upload_cstate(1, ptr));
   else if (ptr == g_grid->divB) check("upload divB", gpumhd_upload(g_ctx, 9, (const double*)ptr));
   else if (g_grid->sflx && ptr == g_grid->sflx) check("upload sflx", gpumhd_upload(g_ctx, 10, (const double*)ptr));
 }

@@ -92,3 +92,18 @@ def test_dropin_links_in_place_of_reference_routines():
         assert out.count(" T " + fn) == 1, fn
     ldd = subprocess.run(["ldd", refrun.DROPIN_BIN], capture_output=True, text=True, check=True).stdout
     assert "libgpumhd.so" in ldd
+
+
+def test_shim_single_precision_build_moves_float_cstate():
+    """Compiled as a SINGLE_PRECISION build of MURaM compiles it, the shim moves
+    GridData's cState arrays (floats there) through the float entry points and
+    the double arrays through the double ones (needs the reference headers)."""
+    from oracle import refrun
+    if not os.path.isdir(refrun.REF_ROOT):
+        pytest.skip("reference sources not available")
+    here = os.path.dirname(os.path.abspath(refrun.__file__))
+    subprocess.run(["make", "-s", "-C", here, "shim_sp", f"REF={refrun.REF_ROOT}"], check=True)
+    obj = os.path.join(here, "_ref", "obj", "gpumhd_muram_shim_sp.o")
+    und = subprocess.run(["nm", "-u", obj], capture_output=True, text=True, check=True).stdout.split()
+    for fn in ("gpumhd_upload_f32", "gpumhd_download_f32", "gpumhd_upload", "gpumhd_download"):
+        assert fn in und, fn

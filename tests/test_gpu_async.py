@@ -93,3 +93,40 @@ def test_async_and_synchronous_calls_mix(gpu_lib):
     g.download_ptr(gpumhd.FIELD_U, r2.ctypes.data)
     assert np.array_equal(r2, ref[0])
     g.close()
+
+
+@pytest.mark.parametrize("precision", [64, 32])
+def test_float_host_layout_equals_double_layout(gpu_lib, precision):
+    """gpumhd_upload_f32 / gpumhd_download_f32 (and the asynchronous pair):
+    a float32 cState array, as MURaM built with SINGLE_PRECISION holds it,
+    gives the device state that the float64 array of the same values gives,
+    and a float32 download is the float64 download rounded to nearest."""
+    ins = [a.astype(np.float32) for a in _inputs(3)]
+    g = _ctx(precision)
+    ref = _sync_results(g, [a.astype(np.float64) for a in ins])
+    # synchronous float32 transfers
+    for a, r in zip(ins, ref):
+        g.upload_ptr(gpumhd.FIELD_U, a.ctypes.data, np.float32)
+        g.run_steps(1)
+        out = np.full_like(a, np.nan)
+        g.download_ptr(gpumhd.FIELD_U, out.ctypes.data, np.float32)
+        assert np.array_equal(out, r.astype(np.float32)), precision
+        d64 = g.download(gpumhd.FIELD_U)
+        assert np.array_equal(d64.reshape(r.shape), r), precision
+    # queued float32 transfers from pinned memory
+    h_in = [torch.from_numpy(a.reshape(-1)).pin_memory() for a in ins]
+    h_out = [torch.full_like(t, float("nan")).pin_memory() for t in h_in]
+    for s in range(len(ins)):
+        g.upload_ptr_async(gpumhd.FIELD_U, h_in[s].data_ptr(), np.float32)
+        g.enqueue_steps(1)
+        g.download_ptr_async(gpumhd.FIELD_U, h_out[s].data_ptr(), np.float32)
+    g.synchronize()
+    for s in range(len(ins)):
+        assert np.array_equal(h_out[s].numpy().reshape(ins[s].shape), ref[s].astype(np.float32)), (precision, s)
+    # a one-value field (the pressure) through the numpy wrappers
+    p64 = g.download(gpumhd.FIELD_PRES)
+    p32 = g.download(gpumhd.FIELD_PRES, dtype=np.float32)
+    assert np.array_equal(p32, p64.astype(np.float32))
+    g.upload(gpumhd.FIELD_PRES, p32)
+    assert np.array_equal(g.download(gpumhd.FIELD_PRES), p32.astype(np.float64))
+    g.close()
