@@ -594,26 +594,47 @@ def run_ensemble(args):
     # the ensemble: one launch of the while-loop graph for all boxes and steps
     reset()
     ens = gpumhd.MuramEnsemble(boxes)
+    stream = torch.cuda.ExternalStream(ens.stream)
+
+    def timed(nsteps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        n0 = ens.launch_count
+        e0.record(stream)
+        ens.enqueue_steps(nsteps)
+        e1.record(stream)
+        ens.synchronize()
+        return e0.elapsed_time(e1), ens.launch_count - n0
+
+    # the schedule (steps of each box per loop iteration, branch order): a
+    # short timed trial of each candidate from the initial states, the best
+    # one then timed afresh
+    trials = {}
+    for unroll, largest in [(1, False), (1, True), (2, True), (4, True)]:
+        ens.set_schedule(unroll, largest)
+        reset()
+        ens.run_steps(max(args.warmup, unroll))
+        reset()
+        t_ms, _ = timed(8)
+        trials[f"{unroll}{'_largest_first' if largest else ''}"] = round(t_ms / 8, 3)
+    best = min(trials, key=trials.get)
+    best_unroll, best_largest = int(best.split("_")[0]), best.endswith("largest_first")
+    ens.set_schedule(best_unroll, best_largest)
+    reset()
     ens.run_steps(args.warmup)
     reset()
-    stream = torch.cuda.ExternalStream(ens.stream)
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    n0 = ens.launch_count
-    e0.record(stream)
-    ens.enqueue_steps(steps)
-    e1.record(stream)
-    ens.synchronize()
-    ms = e0.elapsed_time(e1)
-    launches = ens.launch_count - n0
+    ms, launches = timed(steps)
     value = cells * steps / (ms / 1e3)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": steps, "warmup": args.warmup,
         "ms_per_step": ms / steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded periodic boxes, generated EOS table 3000x3000)",
         "config": {"workload": f"ensemble of {nbox} periodic FP32 boxes, sides in {sides}", "cells": cells,
-                   "graph": "one launch: while-loop graph, body = one step of every box",
+                   "graph": "one launch: while-loop graph, body = "
+                            f"{best_unroll} step(s) of every box"
+                            + (", branches largest box first" if best_largest else ""),
                    "autotuned": True},
+        "schedule_trials_ms_per_step": trials,
         "one_box_per_launch": {"value": cells * steps / t_single, "unit": UNIT,
                                "wall_s": round(t_single, 4)},
         "ensemble_over_one_box_per_launch": value / (cells * steps / t_single),

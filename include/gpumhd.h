@@ -318,6 +318,14 @@ int gpumhd_ensemble_synchronize(gpumhd_ensemble* e);
 const char* gpumhd_ensemble_last_error(gpumhd_ensemble* e);
 void* gpumhd_ensemble_stream(gpumhd_ensemble* e);
 long long gpumhd_ensemble_launch_count(gpumhd_ensemble* e);
+/* The ensemble's schedule: steps_per_iteration (1..64) steps of each box per
+ * loop iteration (a chain of fused steps per box between one fork and one
+ * join, so the boxes meet once per that many steps; a call's remaining
+ * nsteps % steps_per_iteration steps run one per iteration), and
+ * largest_first != 0 captures the branches in order of decreasing cell
+ * count.  Rebuilds the graphs after waiting for the ensemble and its boxes;
+ * results do not depend on the schedule. */
+int gpumhd_ensemble_set_schedule(gpumhd_ensemble* e, int steps_per_iteration, int largest_first);
 
 #ifdef __cplusplus
 }

@@ -7,6 +7,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <algorithm>
 #include <vector>
 
 #include "../../include/gpumhd.h"
@@ -1869,7 +1870,10 @@ struct gpumhd_ensemble {
   cudaEvent_t fork = nullptr, done = nullptr;
   std::vector<cudaEvent_t> join;
   int* d_counter = nullptr;
-  cudaGraphExec_t exec = nullptr;
+  cudaGraphExec_t exec = nullptr;    // body: one step of every box
+  cudaGraphExec_t exec_k = nullptr;  // body: unroll steps of every box (unroll > 1)
+  int unroll = 1;                    // steps of each box per loop iteration
+  bool largest_first = false;        // branches captured in order of decreasing cell count
   long long launches = 0;
   char err[1024] = {0};
 };
@@ -1889,6 +1893,7 @@ static int efail(gpumhd_ensemble* e, int code, const char* msg) {
 static void ensemble_free(gpumhd_ensemble* e) {
   if (!e) return;
   if (e->exec) cudaGraphExecDestroy(e->exec);
+  if (e->exec_k) cudaGraphExecDestroy(e->exec_k);
   for (cudaEvent_t ev : e->join) cudaEventDestroy(ev);
   if (e->fork) cudaEventDestroy(e->fork);
   if (e->done) cudaEventDestroy(e->done);
@@ -1897,7 +1902,10 @@ static void ensemble_free(gpumhd_ensemble* e) {
   delete e;
 }
 
-static int ensemble_build(gpumhd_ensemble* e) {
+// The loop graph whose body advances every box by nstep steps (a chain of
+// nstep fused steps per box, the boxes as parallel branches between a fork
+// and a join), into *exec.
+static int ensemble_build(gpumhd_ensemble* e, int nstep, cudaGraphExec_t* exec) {
   cudaGraph_t g = nullptr;
   if (cudaGraphCreate(&g, 0) != cudaSuccess) return efail(e, GPUMHD_E_CUDA, "cudaGraphCreate failed");
   cudaGraphConditionalHandle h;
@@ -1923,11 +1931,19 @@ static int ensemble_build(gpumhd_ensemble* e) {
     return efail(e, GPUMHD_E_CUDA, "capture into the loop body failed");
   }
   cudaEventRecord(e->fork, e->stream);
-  for (size_t b = 0; b < e->box.size() && rc == 0; b++) {
+  std::vector<size_t> order(e->box.size());
+  for (size_t b = 0; b < order.size(); b++) order[b] = b;
+  if (e->largest_first)
+    std::stable_sort(order.begin(), order.end(),
+                     [&](size_t u, size_t v) { return e->box[u]->c.g.N > e->box[v]->c.g.N; });
+  for (size_t o = 0; o < order.size() && rc == 0; o++) {
+    const size_t b = order[o];
     gpumhd_ctx* x = e->box[b];
     cudaStreamWaitEvent(x->stream, e->fork, 0);
-    rc = enqueue_one_step(x);
-    x->launches -= step_launches(x);  // recorded into the graph, not launched
+    for (int t = 0; t < nstep && rc == 0; t++) {
+      rc = enqueue_one_step(x);
+      x->launches -= step_launches(x);  // recorded into the graph, not launched
+    }
     cudaEventRecord(e->join[b], x->stream);
     cudaStreamWaitEvent(e->stream, e->join[b], 0);
   }
@@ -1935,8 +1951,8 @@ static int ensemble_build(gpumhd_ensemble* e) {
   cudaGraph_t out = nullptr;
   const cudaError_t ce = cudaStreamEndCapture(e->stream, &out);
   if (rc == 0 && ce != cudaSuccess) rc = efail(e, GPUMHD_E_CUDA, cudaGetErrorString(ce));
-  if (rc == 0 && cudaGraphInstantiate(&e->exec, g, 0) != cudaSuccess) {
-    e->exec = nullptr;
+  if (rc == 0 && cudaGraphInstantiate(exec, g, 0) != cudaSuccess) {
+    *exec = nullptr;
     rc = efail(e, GPUMHD_E_CUDA, "instantiating the ensemble graph failed");
   }
   cudaGraphDestroy(g);
@@ -1971,10 +1987,25 @@ extern "C" int gpumhd_ensemble_create(gpumhd_ctx* const* boxes, int n, gpumhd_en
   }
   for (int b = 0; b < n && rc == 0; b++)
     if (cudaStreamSynchronize(e->box[b]->stream) != cudaSuccess) rc = efail(e, GPUMHD_E_CUDA, "ensemble: box stream");
-  if (rc == 0) rc = ensemble_build(e);
+  if (rc == 0) rc = ensemble_build(e, 1, &e->exec);
   if (rc) { ensemble_free(e); return rc; }
   *out = e;
   return GPUMHD_OK;
+}
+
+extern "C" int gpumhd_ensemble_set_schedule(gpumhd_ensemble* e, int steps_per_iteration, int largest_first) {
+  if (!e || steps_per_iteration < 1 || steps_per_iteration > 64) return GPUMHD_E_INVALID;
+  ECK(cudaSetDevice(e->device));
+  ECK(cudaStreamSynchronize(e->stream));
+  for (gpumhd_ctx* x : e->box) ECK(cudaStreamSynchronize(x->stream));
+  if (e->exec) cudaGraphExecDestroy(e->exec);
+  if (e->exec_k) cudaGraphExecDestroy(e->exec_k);
+  e->exec = e->exec_k = nullptr;
+  e->unroll = steps_per_iteration;
+  e->largest_first = largest_first != 0;
+  int rc = ensemble_build(e, 1, &e->exec);
+  if (rc == 0 && e->unroll > 1) rc = ensemble_build(e, e->unroll, &e->exec_k);
+  return rc;
 }
 
 extern "C" int gpumhd_ensemble_destroy(gpumhd_ensemble* e) {
@@ -1995,16 +2026,27 @@ extern "C" int gpumhd_ensemble_enqueue_steps(gpumhd_ensemble* e, int nsteps) {
     ECK(cudaEventRecord(e->join[b], e->box[b]->stream));
     ECK(cudaStreamWaitEvent(e->stream, e->join[b], 0));
   }
-  k_set_counter<<<1, 32, 0, e->stream>>>(e->d_counter, nsteps);
-  ECK(cudaGraphLaunch(e->exec, e->stream));
+  if (!e->exec) return efail(e, GPUMHD_E_INVALID, "ensemble has no graph (a failed schedule change)");
+  // nsteps / unroll iterations of the unrolled body, the rest one step at a time
+  const int nk = e->unroll > 1 ? nsteps / e->unroll : 0;
+  const int n1 = nsteps - nk * e->unroll;
+  if (nk > 0) {
+    k_set_counter<<<1, 32, 0, e->stream>>>(e->d_counter, nk);
+    ECK(cudaGraphLaunch(e->exec_k, e->stream));
+  }
+  if (n1 > 0) {
+    k_set_counter<<<1, 32, 0, e->stream>>>(e->d_counter, n1);
+    ECK(cudaGraphLaunch(e->exec, e->stream));
+  }
   for (gpumhd_ctx* x : e->box) {
     x->res_zero_pending = true;  // Res served as work space
     x->have_pres = true;
     x->launches += (long long)graph_step_launches(x) * nsteps;
   }
-  long long per_step = 1;
+  long long per_step = 0;
   for (gpumhd_ctx* x : e->box) per_step += graph_step_launches(x);
-  e->launches += per_step * nsteps + 1;
+  // the boxes' steps, one loop tick per iteration, one counter set per graph launch
+  e->launches += per_step * nsteps + (nk + n1) + (nk > 0) + (n1 > 0);
   ECK(cudaEventRecord(e->done, e->stream));
   for (gpumhd_ctx* x : e->box) ECK(cudaStreamWaitEvent(x->stream, e->done, 0));
   return GPUMHD_OK;

@@ -75,7 +75,7 @@ EXPORTS = [
     "gpumhd_ensemble_last_error", "gpumhd_ensemble_stream", "gpumhd_ensemble_launch_count",
     "gpumhd_clean_divB", "gpumhd_divb_info", "gpumhd_boundary_info", "gpumhd_test_tma_wait",
     "gpumhd_set_divb_iters", "gpumhd_set_need_diagnostics", "gpumhd_upload_f32", "gpumhd_download_f32",
-    "gpumhd_upload_async_f32", "gpumhd_download_async_f32",
+    "gpumhd_upload_async_f32", "gpumhd_download_async_f32", "gpumhd_ensemble_set_schedule",
 ]
 
 _lib = None
@@ -145,6 +145,7 @@ def load(build_if_missing=True):
         "gpumhd_ensemble_last_error": (C.c_char_p, [vp]),
         "gpumhd_ensemble_stream": (vp, [vp]),
         "gpumhd_ensemble_launch_count": (C.c_longlong, [vp]),
+        "gpumhd_ensemble_set_schedule": (C.c_int, [vp, C.c_int, C.c_int]),
         "gpumhd_clean_divB": (C.c_int, [vp]),
         "gpumhd_divb_info": (C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), dp, dp]),
         "gpumhd_boundary_info": (C.c_int, [vp, dp, dp]),
@@ -505,6 +506,10 @@ class MuramEnsemble:
     def run_steps(self, nsteps):
         self.enqueue_steps(nsteps)
         self.synchronize()
+
+    def set_schedule(self, steps_per_iteration=1, largest_first=False):
+        """Steps of each box per loop iteration, and the branch order."""
+        self._chk(self._L.gpumhd_ensemble_set_schedule(self._h, steps_per_iteration, 1 if largest_first else 0))
 
     @property
     def stream(self):

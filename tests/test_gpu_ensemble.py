@@ -52,6 +52,31 @@ def test_ensemble_equals_boxes_run_one_by_one(gpu_lib):
         g.close()
 
 
+@pytest.mark.parametrize("unroll,largest_first", [(3, False), (4, True)])
+def test_ensemble_schedule_keeps_results(gpu_lib, unroll, largest_first):
+    """Several steps of each box per loop iteration, and the branches in order
+    of decreasing size: the same steps of the same boxes, so the same bits;
+    10 steps = whole iterations plus a remainder run one step at a time."""
+    steps = 10
+    alone = []
+    for nx, ny, nz, prec, seed, closed in SHAPES:
+        g = _box(nx, ny, nz, prec, seed, closed)
+        g.run_steps(steps)
+        alone.append(g.download_state())
+        g.close()
+    boxes = [_box(*s) for s in SHAPES]
+    ens = gpumhd.MuramEnsemble(boxes)
+    ens.set_schedule(unroll, largest_first)
+    ens.run_steps(steps)
+    nk, n1 = steps // unroll, steps % unroll
+    assert ens.launch_count == 9 * len(boxes) * steps + nk + n1 + (nk > 0) + (n1 > 0)
+    for ref, g in zip(alone, boxes):
+        assert np.array_equal(g.download_state(), ref)
+    ens.close()
+    for g in boxes:
+        g.close()
+
+
 def test_box_calls_after_an_ensemble_launch(gpu_lib):
     """Per-box calls queued after an ensemble launch see its result."""
     g1 = _box(16, 12, 8, 64, 11)
