@@ -343,9 +343,10 @@ def run_ours(args):
     if args.spitzer > 0:
         divb_kw.update(spitzer=args.spitzer)
 
-    def context(prec):
+    def context(prec, compensated=0):
         p = gpumhd.default_params(wl["nx"], wl["ny"], wl["nz"], wl["dx"], precision=prec,
-                                  periodic_x=wl["periodic_x"], grav=wl["grav"], **divb_kw)
+                                  periodic_x=wl["periodic_x"], grav=wl["grav"], compensated=compensated,
+                                  **divb_kw)
         g = gpumhd.MuramGPU(p, device=lrank, eos_path=EOS_BENCH)
         g.upload_state(U)
         return g
@@ -442,6 +443,18 @@ def run_ours(args):
                        "exchange), TVDlimit, TCheck, exchange; host-timed, one host round trip per MHD_Residual"}
     g.close()
     del g
+    # the compensated FP32 mode (rounding remainders carried through the RK
+    # sums and the TVD sweeps) on the same box, timed the same way
+    gc = context(32, compensated=1)
+    gc.run_steps(1)
+    gc.upload_state(U)
+    ms_c, _ = time_device(gc, args.steps, args.warmup)
+    ms_c = replica_max(ms_c)
+    gc.close()
+    del gc
+    compensated = {"value": job_rate(ws, n_cells, args.steps, ms_c), "unit": UNIT,
+                   "ms_per_step": round(ms_c / args.steps, 4), "steps": args.steps,
+                   "cost_over_plain": round(ms_c / ms, 4)}
     # FP64 mode of the same box: throughput over --err-steps steps from the
     # initial state, and the per-field error of the FP32 runs (plain and
     # compensated) against it after the same steps.  The FP64 GPU mode matches
@@ -527,6 +540,7 @@ def run_ours(args):
         "per_routine": per_routine,
         "gpu_launches": launches,
         "clocks": clocks.summary(),
+        "fp32_compensated": compensated,
         "fp64": fp64,
         "fp32_error": fp32_err,
     }
@@ -560,7 +574,7 @@ def run_ensemble(args):
     rng = np.random.default_rng(2024)
     sides = [32, 48, 64, 96, 128]
     nbox = args.boxes
-    boxes, states, cells = [], [], 0
+    boxes, states, dims, cells = [], [], [], 0
     for b in range(nbox):
         nx, ny, nz = (int(x) for x in rng.choice(sides, 3))
         v_rms = float(np.exp(rng.uniform(np.log(0.2e5), np.log(2.0e5))))
@@ -571,6 +585,7 @@ def run_ensemble(args):
         g.upload_state(U)
         boxes.append(g)
         states.append(U)
+        dims.append((nx, ny, nz))
         cells += nx * ny * nz
     steps = args.steps
     tune = [g.autotune(trial_steps=2) for g in boxes]
@@ -606,19 +621,37 @@ def run_ensemble(args):
         ens.synchronize()
         return e0.elapsed_time(e1), ens.launch_count - n0
 
-    # the schedule (steps of each box per loop iteration, branch order): a
-    # short timed trial of each candidate from the initial states, the best
-    # one then timed afresh
+    # The launch shapes and the schedule.  Each box's autotuned shapes are
+    # the fastest for the box alone, where it must fill the GPU by itself
+    # (short z chunks, many blocks); inside the ensemble the other boxes fill
+    # it, so longer z marches (fewer prologue planes per block) may pay.
+    # Candidates: autotuned / whole-z / half-z stage chunks, times the steps
+    # of each box per loop iteration and the branch order; a short timed trial
+    # of each from the initial states, the best one then timed afresh.
+    def apply_tuning(kind):
+        # kind: "autotuned", or "<stage z chunk>_td<TVD cells per thread>"
+        for g, k, (nx, ny, nz) in zip(boxes, kernels, dims):
+            if kind == "autotuned":
+                g.set_tuning(k["stage_zchunk"], k["tvd_chunk"])
+                continue
+            zk, td = kind.split("_td")
+            g.set_tuning(nz if zk == "wholez" else max(1, nz // 2), int(td))
+
+    candidates = [("autotuned", 1, False), ("autotuned", 1, True), ("autotuned", 2, True), ("halfz_td64", 1, True),
+                  ("wholez_td64", 1, True), ("wholez_td128", 1, True), ("halfz_td128", 1, True),
+                  ("wholez_td128", 2, True)]
     trials = {}
-    for unroll, largest in [(1, False), (1, True), (2, True), (4, True)]:
+    for kind, unroll, largest in candidates:
+        apply_tuning(kind)
         ens.set_schedule(unroll, largest)
         reset()
         ens.run_steps(max(args.warmup, unroll))
         reset()
         t_ms, _ = timed(8)
-        trials[f"{unroll}{'_largest_first' if largest else ''}"] = round(t_ms / 8, 3)
-    best = min(trials, key=trials.get)
-    best_unroll, best_largest = int(best.split("_")[0]), best.endswith("largest_first")
+        trials[(kind, unroll, largest)] = t_ms / 8
+    best_kind, best_unroll, best_largest = min(trials, key=trials.get)
+    trials = {f"{k}_{u}{'_largest_first' if lf else ''}": round(v, 3) for (k, u, lf), v in trials.items()}
+    apply_tuning(best_kind)
     ens.set_schedule(best_unroll, best_largest)
     reset()
     ens.run_steps(args.warmup)
@@ -633,7 +666,7 @@ def run_ensemble(args):
                    "graph": "one launch: while-loop graph, body = "
                             f"{best_unroll} step(s) of every box"
                             + (", branches largest box first" if best_largest else ""),
-                   "autotuned": True},
+                   "autotuned": True, "stage_zchunks": best_kind},
         "schedule_trials_ms_per_step": trials,
         "one_box_per_launch": {"value": cells * steps / t_single, "unit": UNIT,
                                "wall_s": round(t_single, 4)},
