@@ -621,38 +621,18 @@ def run_ensemble(args):
         ens.synchronize()
         return e0.elapsed_time(e1), ens.launch_count - n0
 
-    # The launch shapes and the schedule.  Each box's autotuned shapes are
-    # the fastest for the box alone, where it must fill the GPU by itself
-    # (short z chunks, many blocks); inside the ensemble the other boxes fill
-    # it, so longer z marches (fewer prologue planes per block) may pay.
-    # Candidates: autotuned / whole-z / half-z stage chunks, times the steps
-    # of each box per loop iteration and the branch order; a short timed trial
-    # of each from the initial states, the best one then timed afresh.
-    def apply_tuning(kind):
-        # kind: "autotuned", or "<stage z chunk>_td<TVD cells per thread>"
-        for g, k, (nx, ny, nz) in zip(boxes, kernels, dims):
-            if kind == "autotuned":
-                g.set_tuning(k["stage_zchunk"], k["tvd_chunk"])
-                continue
-            zk, td = kind.split("_td")
-            g.set_tuning(nz if zk == "wholez" else max(1, nz // 2), int(td))
-
-    candidates = [("autotuned", 1, False), ("autotuned", 1, True), ("autotuned", 2, True), ("halfz_td64", 1, True),
-                  ("wholez_td64", 1, True), ("wholez_td128", 1, True), ("halfz_td128", 1, True),
-                  ("wholez_td128", 2, True)]
-    trials = {}
-    for kind, unroll, largest in candidates:
-        apply_tuning(kind)
-        ens.set_schedule(unroll, largest)
-        reset()
-        ens.run_steps(max(args.warmup, unroll))
-        reset()
-        t_ms, _ = timed(8)
-        trials[(kind, unroll, largest)] = t_ms / 8
-    best_kind, best_unroll, best_largest = min(trials, key=trials.get)
-    trials = {f"{k}_{u}{'_largest_first' if lf else ''}": round(v, 3) for (k, u, lf), v in trials.items()}
-    apply_tuning(best_kind)
-    ens.set_schedule(best_unroll, best_largest)
+    # Launch shapes for the ensemble (gpumhd_ensemble_autotune): each box's
+    # own autotuned shapes suit the box alone, which must fill the GPU by
+    # itself; inside the ensemble longer stage z chunks and TVD chunks may
+    # pay.  Timed from the current states, which the autotuner restores.
+    reset()
+    ens.run_steps(args.warmup)
+    reset()
+    tune_ms = ens.autotune(trial_steps=8)
+    chosen = [g.tuning() for g in boxes]
+    own = sum(1 for c, k in zip(chosen, kernels) if c["stage_zchunk"] == k["stage_zchunk"]
+              and c["tvd_chunk"] == k["tvd_chunk"])
+    whole = sum(1 for c, (nx, ny, nz) in zip(chosen, dims) if c["stage_zchunk"] == nz)
     reset()
     ens.run_steps(args.warmup)
     reset()
@@ -663,11 +643,12 @@ def run_ensemble(args):
         "ms_per_step": ms / steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic (seeded periodic boxes, generated EOS table 3000x3000)",
         "config": {"workload": f"ensemble of {nbox} periodic FP32 boxes, sides in {sides}", "cells": cells,
-                   "graph": "one launch: while-loop graph, body = "
-                            f"{best_unroll} step(s) of every box"
-                            + (", branches largest box first" if best_largest else ""),
-                   "autotuned": True, "stage_zchunks": best_kind},
-        "schedule_trials_ms_per_step": trials,
+                   "graph": "one launch: while-loop graph, body = one step of every box, branches largest "
+                            "box first",
+                   "autotuned": True},
+        "ensemble_autotune": {"trial_ms_per_step": round(tune_ms, 3), "boxes_on_own_shapes": own,
+                              "boxes_on_whole_z_chunks": whole,
+                              "tvd_chunks": sorted({c["tvd_chunk"] for c in chosen})},
         "one_box_per_launch": {"value": cells * steps / t_single, "unit": UNIT,
                                "wall_s": round(t_single, 4)},
         "ensemble_over_one_box_per_launch": value / (cells * steps / t_single),

@@ -326,6 +326,14 @@ long long gpumhd_ensemble_launch_count(gpumhd_ensemble* e);
  * count.  Rebuilds the graphs after waiting for the ensemble and its boxes;
  * results do not depend on the schedule. */
 int gpumhd_ensemble_set_schedule(gpumhd_ensemble* e, int steps_per_iteration, int largest_first);
+/* Launch shapes of the boxes for running inside the ensemble: each box's
+ * current shapes, or stage z chunks of half or all of its z extent with TVD
+ * chunks of 64 or 128 cells (longer marches pay when the other boxes fill the
+ * GPU), timed over trial_steps steps of the ensemble from the boxes' current
+ * states and restored states afterwards (state, pressure, divB potential,
+ * heat flux, step control); keeps the fastest, branches largest box first.
+ * *best_ms: its time per ensemble step. */
+int gpumhd_ensemble_autotune(gpumhd_ensemble* e, int trial_steps, double* best_ms);
 
 #ifdef __cplusplus
 }

@@ -1774,6 +1774,58 @@ extern "C" int gpumhd_get_tuning(gpumhd_ctx* ctx, int* stage_kernel, int* stage_
 
 // Mean time of `steps` fused steps (after one untimed step), CUDA events on the
 // context's stream.
+// What trial steps change and must give back: the state, its pressure, the
+// divB cleaning potential, the Spitzer heat flux and the step-control block.
+// Compensated remainders are left alone by running the trials uncompensated.
+struct TrialSave {
+  void* U = nullptr;
+  void* P = nullptr;
+  void* phi = nullptr;
+  void* sflx = nullptr;
+  Dyn dyn{};
+  int comp = 0;
+};
+
+static void trial_free(TrialSave& t) {
+  for (void* q : {t.U, t.P, t.phi, t.sflx})
+    if (q) cudaFree(q);
+  t.U = t.P = t.phi = t.sflx = nullptr;
+}
+
+static int trial_save(gpumhd_ctx* ctx, TrialSave& t) {
+  gpumhd_ctx* const x = ctx;
+  const size_t n = (size_t)x->c.g.N * x->rsz;
+  t.comp = x->p.compensated;
+  CK(cudaMalloc(&t.U, 8 * n));
+  CK(cudaMalloc(&t.P, n));
+  CK(cudaMemcpyAsync(t.U, x->S[x->iU], 8 * n, cudaMemcpyDeviceToDevice, x->stream));
+  CK(cudaMemcpyAsync(t.P, x->P[x->iP], n, cudaMemcpyDeviceToDevice, x->stream));
+  if (x->phi) {
+    CK(cudaMalloc(&t.phi, n));
+    CK(cudaMemcpyAsync(t.phi, x->phi, n, cudaMemcpyDeviceToDevice, x->stream));
+  }
+  if (x->spt[0]) {
+    CK(cudaMalloc(&t.sflx, n));
+    CK(cudaMemcpyAsync(t.sflx, x->spt[0], n, cudaMemcpyDeviceToDevice, x->stream));
+  }
+  const int rc = pull_dyn(x);
+  if (rc) return rc;
+  t.dyn = x->hdyn;
+  x->p.compensated = 0;
+  return GPUMHD_OK;
+}
+
+static int trial_restore(gpumhd_ctx* ctx, const TrialSave& t) {
+  gpumhd_ctx* const x = ctx;
+  const size_t n = (size_t)x->c.g.N * x->rsz;
+  CK(cudaMemcpyAsync(x->S[x->iU], t.U, 8 * n, cudaMemcpyDeviceToDevice, x->stream));
+  CK(cudaMemcpyAsync(x->P[x->iP], t.P, n, cudaMemcpyDeviceToDevice, x->stream));
+  if (t.phi) CK(cudaMemcpyAsync(x->phi, t.phi, n, cudaMemcpyDeviceToDevice, x->stream));
+  if (t.sflx) CK(cudaMemcpyAsync(x->spt[0], t.sflx, n, cudaMemcpyDeviceToDevice, x->stream));
+  x->hdyn = t.dyn;
+  return push_dyn(x);
+}
+
 static int time_steps(gpumhd_ctx* ctx, int steps, double* ms) {
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
@@ -1802,28 +1854,17 @@ extern "C" int gpumhd_autotune(gpumhd_ctx* ctx, int trial_steps, double* best_ms
   CK(cudaSetDevice(ctx->device));
   int rc = fused_prepare(ctx, trial_steps + 1);
   if (rc) return rc;
-  const long long N = ctx->c.g.N;
-  void* saveP = nullptr;
-  if (!ctx->T) CK(cudaMalloc(&ctx->T, 8 * N * ctx->rsz));
-  CK(cudaMalloc(&saveP, N * ctx->rsz));
-  CK(cudaMemcpyAsync(ctx->T, ctx->S[ctx->iU], 8 * N * ctx->rsz, cudaMemcpyDeviceToDevice, ctx->stream));
-  CK(cudaMemcpyAsync(saveP, ctx->P[ctx->iP], N * ctx->rsz, cudaMemcpyDeviceToDevice, ctx->stream));
-  rc = pull_dyn(ctx);
-  const Dyn saved = ctx->hdyn;
-  auto restore = [&]() {
-    cudaMemcpyAsync(ctx->S[ctx->iU], ctx->T, 8 * N * ctx->rsz, cudaMemcpyDeviceToDevice, ctx->stream);
-    cudaMemcpyAsync(ctx->P[ctx->iP], saveP, N * ctx->rsz, cudaMemcpyDeviceToDevice, ctx->stream);
-    ctx->hdyn = saved;
-    return push_dyn(ctx);
-  };
+  TrialSave sv;
+  rc = trial_save(ctx, sv);
+  if (rc) { ctx->p.compensated = sv.comp; trial_free(sv); return rc; }
+  auto restore = [&]() { return trial_restore(ctx, sv); };
   const int nz = ctx->c.g.nz;
   std::vector<int> zcs = {0, nz};
   for (int f = 2; f <= 16; f *= 2)
     if ((nz + f - 1) / f >= 4) zcs.push_back((nz + f - 1) / f);
   std::vector<int> kernels = {1};
   if (ctx->tma) kernels.insert(kernels.begin(), 0);
-  const int keep_kernel = ctx->p.stage_kernel, keep_td = ctx->tune_td, keep_comp = ctx->p.compensated;
-  ctx->p.compensated = 0;  // trial steps leave the compensation remainders alone
+  const int keep_kernel = ctx->p.stage_kernel, keep_td = ctx->tune_td;
   double best = 1e300;
   int bk = keep_kernel, bz = 0, btd = keep_td;
   for (int kern : kernels) {
@@ -1849,10 +1890,10 @@ extern "C" int gpumhd_autotune(gpumhd_ctx* ctx, int trial_steps, double* best_ms
     if (!rc && ms < best) { best = ms; btd = td; }
   }
   ctx->tune_td = btd;
-  ctx->p.compensated = keep_comp;
+  ctx->p.compensated = sv.comp;
   if (!rc) rc = restore();
   cudaStreamSynchronize(ctx->stream);
-  cudaFree(saveP);
+  trial_free(sv);
   if (ctx->graph) { cudaGraphExecDestroy(ctx->graph); ctx->graph = nullptr; }
   if (rc) return rc;
   if (best_ms) *best_ms = best;
@@ -2006,6 +2047,89 @@ extern "C" int gpumhd_ensemble_set_schedule(gpumhd_ensemble* e, int steps_per_it
   int rc = ensemble_build(e, 1, &e->exec);
   if (rc == 0 && e->unroll > 1) rc = ensemble_build(e, e->unroll, &e->exec_k);
   return rc;
+}
+
+// Launch shapes inside an ensemble.  A box's own autotuned shapes are the
+// fastest for the box alone, which must fill the GPU by itself (short z
+// chunks, short TVD chunks: many blocks, each with its own prologue planes and
+// stencil halo); inside an ensemble the other boxes fill it, so longer
+// marches can pay.  Candidates: each box's current shapes, and stage z chunks
+// of half or all of the box's z extent with TVD chunks of 64 or 128 cells;
+// timed over trial_steps steps of the whole ensemble (branches largest box
+// first) from the boxes' current states, which are restored afterwards.
+extern "C" int gpumhd_ensemble_autotune(gpumhd_ensemble* e, int trial_steps, double* best_ms) {
+  if (!e || trial_steps < 1) return GPUMHD_E_INVALID;
+  ECK(cudaSetDevice(e->device));
+  ECK(cudaStreamSynchronize(e->stream));
+  const size_t nb = e->box.size();
+  std::vector<TrialSave> sv(nb);
+  std::vector<int> zc0(nb), td0(nb);
+  const int keep_unroll = e->unroll;
+  int rc = GPUMHD_OK;
+  size_t saved = 0;  // boxes whose trial_save ran (its buffers and flag to give back)
+  for (; saved < nb && rc == 0; saved++) {
+    gpumhd_ctx* x = e->box[saved];
+    zc0[saved] = x->tune_zc;
+    td0[saved] = x->tune_td;
+    rc = trial_save(x, sv[saved]);
+  }
+  const bool all_saved = rc == 0;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (rc == 0 && (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess))
+    rc = efail(e, GPUMHD_E_CUDA, "ensemble autotune: events");
+  struct Cand { int z; int td; };  // z: 0 = each box's own shapes, 1 = half the z extent, 2 = all of it
+  const Cand cands[] = {{0, 0}, {1, 64}, {1, 128}, {2, 64}, {2, 128}};
+  auto apply = [&](const Cand& k) {
+    for (size_t b = 0; b < nb; b++) {
+      gpumhd_ctx* x = e->box[b];
+      const int nz = x->c.g.nz;
+      x->tune_zc = k.z == 0 ? zc0[b] : (k.z == 1 ? std::max(1, nz / 2) : nz);
+      x->tune_td = k.z == 0 ? td0[b] : k.td;
+      if (x->graph) { cudaGraphExecDestroy(x->graph); x->graph = nullptr; }
+    }
+  };
+  auto restore_all = [&]() {
+    int r = GPUMHD_OK;
+    for (size_t b = 0; b < nb && r == 0; b++) r = trial_restore(e->box[b], sv[b]);
+    return r;
+  };
+  double best = 1e300;
+  int bi = 0;
+  for (int ci = 0; ci < (int)(sizeof(cands) / sizeof(cands[0])) && rc == 0; ci++) {
+    apply(cands[ci]);
+    rc = gpumhd_ensemble_set_schedule(e, 1, 1);
+    if (!rc) rc = restore_all();
+    if (!rc) rc = gpumhd_ensemble_enqueue_steps(e, 1);  // untimed first step
+    if (rc) break;
+    float t = 0.f;
+    if (cudaEventRecord(e0, e->stream) != cudaSuccess) { rc = efail(e, GPUMHD_E_CUDA, "ensemble autotune: event"); break; }
+    rc = gpumhd_ensemble_enqueue_steps(e, trial_steps);
+    if (rc) break;
+    if (cudaEventRecord(e1, e->stream) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+        cudaEventElapsedTime(&t, e0, e1) != cudaSuccess) {
+      rc = efail(e, GPUMHD_E_CUDA, "ensemble autotune: timing failed");
+      break;
+    }
+    rc = gpumhd_ensemble_synchronize(e);
+    const double ms = (double)t / trial_steps;
+    if (!rc && ms < best) { best = ms; bi = ci; }
+  }
+  // keep the fastest candidate; the boxes' states, compensation and graphs as before
+  apply(cands[bi]);
+  for (size_t b = 0; b < saved; b++) e->box[b]->p.compensated = sv[b].comp;
+  const int rc2 = gpumhd_ensemble_set_schedule(e, keep_unroll, 1);
+  if (!rc) rc = rc2;
+  if (all_saved) {
+    const int rc3 = restore_all();
+    if (!rc) rc = rc3;
+  }
+  for (size_t b = 0; b < nb; b++) cudaStreamSynchronize(e->box[b]->stream);
+  for (size_t b = 0; b < saved; b++) trial_free(sv[b]);
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  if (rc) return rc;
+  if (best_ms) *best_ms = best;
+  return GPUMHD_OK;
 }
 
 extern "C" int gpumhd_ensemble_destroy(gpumhd_ensemble* e) {

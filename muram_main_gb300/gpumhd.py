@@ -76,6 +76,7 @@ EXPORTS = [
     "gpumhd_clean_divB", "gpumhd_divb_info", "gpumhd_boundary_info", "gpumhd_test_tma_wait",
     "gpumhd_set_divb_iters", "gpumhd_set_need_diagnostics", "gpumhd_upload_f32", "gpumhd_download_f32",
     "gpumhd_upload_async_f32", "gpumhd_download_async_f32", "gpumhd_ensemble_set_schedule",
+    "gpumhd_ensemble_autotune",
 ]
 
 _lib = None
@@ -146,6 +147,7 @@ def load(build_if_missing=True):
         "gpumhd_ensemble_stream": (vp, [vp]),
         "gpumhd_ensemble_launch_count": (C.c_longlong, [vp]),
         "gpumhd_ensemble_set_schedule": (C.c_int, [vp, C.c_int, C.c_int]),
+        "gpumhd_ensemble_autotune": (C.c_int, [vp, C.c_int, dp]),
         "gpumhd_clean_divB": (C.c_int, [vp]),
         "gpumhd_divb_info": (C.c_int, [vp, C.POINTER(C.c_int), C.POINTER(C.c_int), dp, dp]),
         "gpumhd_boundary_info": (C.c_int, [vp, dp, dp]),
@@ -510,6 +512,13 @@ class MuramEnsemble:
     def set_schedule(self, steps_per_iteration=1, largest_first=False):
         """Steps of each box per loop iteration, and the branch order."""
         self._chk(self._L.gpumhd_ensemble_set_schedule(self._h, steps_per_iteration, 1 if largest_first else 0))
+
+    def autotune(self, trial_steps=4):
+        """Launch shapes of the boxes for this ensemble, timed from their
+        current states (restored afterwards); returns ms per ensemble step."""
+        ms = C.c_double()
+        self._chk(self._L.gpumhd_ensemble_autotune(self._h, trial_steps, C.byref(ms)))
+        return ms.value
 
     @property
     def stream(self):

@@ -163,3 +163,66 @@ def test_tile_from_commutes_with_the_step(gpu_lib):
     assert np.array_equal(big.download_state()[:, 2:-2, 2:-2, 2:-2], np.tile(U1, (1, 2, 3, 2)))
     small.close()
     big.close()
+
+
+def _box_kw(nx, ny, nz, precision, seed, **kw):
+    tab = initial.EosTable(H.EOS_SMALL)
+    p = gpumhd.default_params(nx, ny, nz, 3.2e6, precision=precision, **kw)
+    g = gpumhd.MuramGPU(p, eos_path=H.EOS_SMALL)
+    g.upload_state(initial.periodic_box(tab, nx, ny, nz, seed=seed))
+    return g
+
+
+CARRIED = {"divb": dict(divB_switch=1, divB_itmax=4, divB_err=0.2), "spitzer": dict(spitzer=0.5)}
+
+
+@pytest.mark.parametrize("kind", sorted(CARRIED))
+def test_autotune_restores_carried_fields(gpu_lib, kind):
+    """The trial steps of the autotuner also advance what a step carries
+    besides the state (the cleaning potential phi, the heat flux); both are
+    given back, so a tuned box continues exactly as an untuned one (FP64:
+    the shapes do not change the bits)."""
+    a = _box_kw(32, 16, 24, 64, 71, **CARRIED[kind])
+    b = _box_kw(32, 16, 24, 64, 71, **CARRIED[kind])
+    a.run_steps(3)
+    b.run_steps(3)
+    a.autotune(trial_steps=2)
+    a.run_steps(4)
+    b.run_steps(4)
+    assert np.array_equal(a.download_state(), b.download_state())
+    field = gpumhd.FIELD_PHI if kind == "divb" else gpumhd.FIELD_SFLX
+    assert np.array_equal(a.download_field(field), b.download_field(field))
+    assert a.step_info()[2] == b.step_info()[2]
+    a.close()
+    b.close()
+
+
+def test_ensemble_autotune_keeps_results(gpu_lib):
+    """gpumhd_ensemble_autotune times launch shapes on the boxes' current
+    states and restores them: FP64 boxes (plain, with cleaning, with
+    conduction) continue bit for bit as when run alone; the FP32 box to the
+    FMA contractions of the two stage-kernel layouts its new z chunk may
+    select."""
+    specs = [(16, 12, 8, 64, 81, {}), (24, 16, 12, 64, 82, CARRIED["divb"]), (20, 12, 16, 64, 83, CARRIED["spitzer"]),
+             (32, 16, 24, 32, 84, {})]
+    alone = []
+    for nx, ny, nz, prec, seed, kw in specs:
+        g = _box_kw(nx, ny, nz, prec, seed, **kw)
+        g.run_steps(6)
+        alone.append(g.download_state())
+        g.close()
+    boxes = [_box_kw(nx, ny, nz, prec, seed, **kw) for nx, ny, nz, prec, seed, kw in specs]
+    ens = gpumhd.MuramEnsemble(boxes)
+    ens.run_steps(2)
+    ms = ens.autotune(trial_steps=2)
+    assert ms > 0
+    ens.run_steps(4)
+    for (nx, ny, nz, prec, seed, kw), ref, g in zip(specs, alone, boxes):
+        got = g.download_state()
+        if prec == 64:
+            assert np.array_equal(got, ref), (nx, ny, nz, kw)
+        else:
+            assert np.all(H.rel_linf(got, ref) <= 1e-6), H.rel_linf(got, ref)
+    ens.close()
+    for g in boxes:
+        g.close()
