@@ -181,7 +181,12 @@ int gpumhd_set_divb_iters(gpumhd_ctx* ctx, int next_iters);
 int gpumhd_set_need_diagnostics(gpumhd_ctx* ctx, int on);
 /* SaveCons (include/src_int_tck.H:10, src/Add_Sources_Integrate_SR.C:475-531). */
 int gpumhd_save_cons(gpumhd_ctx* ctx);
-/* ConsToPrim (include/eos.H:39, src/cons_to_prim.C:78-266). */
+/* ConsToPrim (include/eos.H:39, src/cons_to_prim.C:78-266).  The state
+ * becomes primitive in place and the pressure is stored; temperature, n_e,
+ * rho_i and amb (fields 4-7) are formed on their first access (download,
+ * upload of one of them, the Spitzer residual) from the density and internal
+ * energy this call saw, so they hold this call's values whatever happens to
+ * the state in between. */
 int gpumhd_cons_to_prim(gpumhd_ctx* ctx);
 /* Adjust_Valf_Max (include/limit_va.H:7, src/Adjust_Valf_Max.C:25-150). */
 int gpumhd_adjust_valf_max(gpumhd_ctx* ctx);

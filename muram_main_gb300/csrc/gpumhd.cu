@@ -80,6 +80,7 @@ struct gpumhd_ctx {
   // cleared: Source_Integrate_Tcheck and the fused steps leave it so, the next
   // MHD_Residual writes it without adding, any other access clears it first
   bool res_zero_pending = false;
+  bool aux_pending = false;  // temp and ne hold ConsToPrim's density and internal energy (see field_ptr)
   void* phi = nullptr;   // divB cleaning potential (GridData::phi, N), persists between calls
   void* divb = nullptr;  // last divergence of B (GridData::divB, N)
   double* bnd_part = nullptr;  // per-plane sums of the physical x boundaries (nz * BND_NQ)
@@ -711,6 +712,16 @@ static void materialize_res(gpumhd_ctx* ctx) {
   ctx->res_zero_pending = false;
 }
 
+// ConsToPrim's outputs temp, ne, rhoi, amb (t = 0..3), allocated zeroed on first use.
+static void* aux_alloc(gpumhd_ctx* ctx, int t, int* rc) {
+  void*& a = ctx->aux[t];
+  if (!a) {
+    if (cudaMalloc(&a, ctx->c.g.N * ctx->rsz) != cudaSuccess) { *rc = GPUMHD_E_NOMEM; return nullptr; }
+    cudaMemsetAsync(a, 0, ctx->c.g.N * ctx->rsz, ctx->stream);
+  }
+  return a;
+}
+
 static void* field_ptr(gpumhd_ctx* ctx, int which, int* nf, int* rc) {
   *rc = GPUMHD_OK;
   if (which >= 0 && which <= 2) {
@@ -744,10 +755,17 @@ static void* field_ptr(gpumhd_ctx* ctx, int which, int* nf, int* rc) {
     return (char*)ctx->diag + (size_t)(which - 11) * ctx->c.g.N * ctx->rsz;
   }
   if (which >= 4 && which <= 7) {
-    void*& a = ctx->aux[which - 4];
-    if (!a) {
-      if (cudaMalloc(&a, ctx->c.g.N * ctx->rsz) != cudaSuccess) { *rc = GPUMHD_E_NOMEM; return nullptr; }
-      cudaMemsetAsync(a, 0, ctx->c.g.N * ctx->rsz, ctx->stream);
+    void* a = aux_alloc(ctx, which - 4, rc);
+    if (a && ctx->aux_pending) {  // ConsToPrim left its EOS inputs: form the outputs now
+      if (ctx->f32)
+        Launch<float>::aux_of_snapshot(ctx->c, (float*)ctx->aux[0], (float*)ctx->aux[1], (float*)ctx->aux[2],
+                                       (float*)ctx->aux[3], ctx->stream);
+      else
+        Launch<double>::aux_of_snapshot(ctx->c, (double*)ctx->aux[0], (double*)ctx->aux[1], (double*)ctx->aux[2],
+                                        (double*)ctx->aux[3], ctx->stream);
+      ctx->aux_pending = false;
+      ctx->launches += 1;
+      if (cudaGetLastError() != cudaSuccess) { *rc = GPUMHD_E_CUDA; return nullptr; }
     }
     return a;
   }
@@ -990,18 +1008,24 @@ extern "C" int gpumhd_cons_to_prim(gpumhd_ctx* ctx) {
   if (!ctx) return GPUMHD_E_INVALID;
   if (!ctx->eos_loaded) return fail(ctx, GPUMHD_E_ORDER, "ConsToPrim before eos_init");
   CK(cudaSetDevice(ctx->device));
-  int nf, rc;
+  int rc = GPUMHD_OK;
   void* a[4];
   for (int t = 0; t < 4; t++) {
-    a[t] = field_ptr(ctx, 4 + t, &nf, &rc);
+    a[t] = aux_alloc(ctx, t, &rc);
     if (rc) return fail(ctx, rc, "allocation of the EOS output fields failed");
   }
+  // Temperature, n_e, rho_i and amb are read only when downloaded (or by the
+  // Spitzer residual): the kernel stores the density and internal energy they
+  // come from, and the first access forms them (field_ptr).  With Spitzer
+  // conduction, which reads the temperature every stage, they are formed here.
+  const bool snap = !ctx->c.has_spitzer;
   if (ctx->f32)
     Launch<float>::cons_to_prim(ctx->c, (float*)ctx->S[ctx->iU], (float*)ctx->P[ctx->iP], (float*)a[0], (float*)a[1],
-                                (float*)a[2], (float*)a[3], ctx->stream);
+                                (float*)a[2], (float*)a[3], snap, ctx->stream);
   else
     Launch<double>::cons_to_prim(ctx->c, (double*)ctx->S[ctx->iU], (double*)ctx->P[ctx->iP], (double*)a[0],
-                                 (double*)a[1], (double*)a[2], (double*)a[3], ctx->stream);
+                                 (double*)a[1], (double*)a[2], (double*)a[3], snap, ctx->stream);
+  ctx->aux_pending = snap;
   ctx->have_pres = true;
   ctx->fused_ready = false;
   return check_launch(ctx, 1);

@@ -1268,7 +1268,7 @@ __global__ void __launch_bounds__(128, TvdBlocks<R>::lanes) k_tvd_sweep_xlanes(C
 // the EOS gathers' latency hidden by more warps.  The same bound serves the
 // temperature and Source_Integrate kernels (0.97 -> 0.75 ms).
 template <class R> struct EwBlocks { static constexpr int v = sizeof(R) == 4 ? 6 : 1; };
-template <class R>
+template <class R, bool SNAP>
 __global__ void __launch_bounds__(256, EwBlocks<R>::v) k_cons_to_prim(Consts c, R* __restrict__ U, R* __restrict__ P, R* __restrict__ T, R* __restrict__ Ne,
                                R* __restrict__ Ri, R* __restrict__ Am) {
   const Geom& g = c.g;
@@ -1285,7 +1285,29 @@ __global__ void __launch_bounds__(256, EwBlocks<R>::v) k_cons_to_prim(Consts c, 
     U[3 * N + id] = v3;
     U[4 * N + id] = ei;
     P[id] = pr;
-    if (T) { T[id] = tm; Ne[id] = ne; Ri[id] = ri; Am[id] = am; }
+    if (SNAP) {  // the EOS inputs, from which k_aux_of_snapshot forms the other outputs
+      T[id] = d;
+      Ne[id] = ei;
+    } else if (T) {
+      T[id] = tm; Ne[id] = ne; Ri[id] = ri; Am[id] = am;
+    }
+  }
+}
+
+// ConsToPrim's temperature, n_e, rho_i and ambipolar coefficient from the
+// density and internal energy that k_cons_to_prim<R, true> left in T and Ne:
+// the same routine on the same inputs, so the same values as computing them
+// there.
+template <class R>
+__global__ void __launch_bounds__(256, EwBlocks<R>::v) k_aux_of_snapshot(Consts c, R* __restrict__ T, R* __restrict__ Ne,
+                                                                    R* __restrict__ Ri, R* __restrict__ Am) {
+  const unsigned N = c.g.N32;
+  for (unsigned id = gs_first(); id < N; id += gs_step()) {
+    const R d = T[id], ei = Ne[id];
+    const R dn = (R)1.0 / d;
+    R pr, tm, ne, ri, am;
+    c2p_outputs(c, d, ei, dn, pr, tm, ne, ri, am);
+    T[id] = tm; Ne[id] = ne; Ri[id] = ri; Am[id] = am;
   }
 }
 
@@ -1617,11 +1639,32 @@ __global__ void k_tile_state(Geom gd, Geom gs, const R* __restrict__ Us, R* __re
 template <class R>
 __global__ void k_fill_ghosts(Geom g, R* __restrict__ U, int nfield, int with_bc) {
   const unsigned N = g.N32;
-  for (unsigned id = gs_first(); id < N; id += gs_step()) {
+  // the ghost nodes only, in three x-fastest groups: the z-ghost planes, the
+  // y-ghost rows of interior planes, the x-ghost nodes of interior rows
+  const unsigned sx = (unsigned)g.sx, sy = (unsigned)g.sy;
+  const unsigned nA = 2u * GH * sx * sy;
+  const unsigned nB = 2u * GH * sx * (unsigned)g.nz;
+  const unsigned nC = 2u * GH * (unsigned)g.ny * (unsigned)g.nz;
+  for (unsigned t = gs_first(); t < nA + nB + nC; t += gs_step()) {
     int i, j, k;
-    node_ijk(g, id, i, j, k);
+    if (t < nA) {
+      const unsigned q = t / sx, p = q / sy;
+      i = (int)(t - q * sx);
+      j = (int)(q - p * sy);
+      k = p < (unsigned)GH ? (int)p : (int)p + g.nz;
+    } else if (t < nA + nB) {
+      const unsigned u = t - nA, q = u / sx, jj = q % (2u * GH);
+      i = (int)(u - q * sx);
+      j = jj < (unsigned)GH ? (int)jj : (int)jj + g.ny;
+      k = GH + (int)(q / (2u * GH));
+    } else {
+      const unsigned u = t - nA - nB, ii = u % (2u * GH), q = u / (2u * GH);
+      i = ii < (unsigned)GH ? (int)ii : (int)ii + g.nx;
+      j = GH + (int)(q % (unsigned)g.ny);
+      k = GH + (int)(q / (unsigned)g.ny);
+    }
+    const unsigned id = cidx32(g, i, j, k);
     const bool gx = (i < GH || i >= GH + g.nx), gy = (j < GH || j >= GH + g.ny), gz = (k < GH || k >= GH + g.nz);
-    if (!gx && !gy && !gz) continue;
     bool flip = false;
     if (gx) {
       if (g.periodic_x) i = i < GH ? i + g.nx : i - g.nx;

@@ -64,7 +64,9 @@ struct Launch {
   static void spitzer(const Consts& c, const R* U, bool prim, const R* T, const R* S, const R* S0, R* Sout, R* Rflx,
                       R* Rsp, const Dyn* dyn, int stage, cudaStream_t s);
   static void sflx_update(const Consts& c, R* S, const R* S0, R* Rflx, const Dyn* dyn, int stage, cudaStream_t s);
-  static void cons_to_prim(const Consts& c, R* U, R* P, R* T, R* Ne, R* Ri, R* Am, cudaStream_t s);
+  // snapshot: T and Ne receive the density and internal energy, aux_of_snapshot the outputs later
+  static void cons_to_prim(const Consts& c, R* U, R* P, R* T, R* Ne, R* Ri, R* Am, bool snapshot, cudaStream_t s);
+  static void aux_of_snapshot(const Consts& c, R* T, R* Ne, R* Ri, R* Am, cudaStream_t s);
   static void init_pass(const Consts& c, const R* U, R* P, Dyn* dyn, cudaStream_t s);
   static void adjust_stats(const Consts& c, const R* U, const R* P, Dyn* dyn, cudaStream_t s);
   static void cmax_faces(const Consts& c, const R* U, const R* P, Dyn* dyn, cudaStream_t s);
@@ -330,8 +332,13 @@ void Launch<R>::step_finish(const Consts& c, R* U, R* P, Dyn* dyn, cudaStream_t 
   (Cc ? k_step_finish<R, true> : k_step_finish<R, false>)<<<grid, block, 0, s>>>(c, U, P, dyn, Cc);
 }
 template <class R>
-void Launch<R>::cons_to_prim(const Consts& c, R* U, R* P, R* T, R* Ne, R* Ri, R* Am, cudaStream_t s) {
-  k_cons_to_prim<R><<<grid_for(c.g.N, 256), 256, 0, s>>>(c, U, P, T, Ne, Ri, Am);
+void Launch<R>::cons_to_prim(const Consts& c, R* U, R* P, R* T, R* Ne, R* Ri, R* Am, bool snapshot, cudaStream_t s) {
+  (snapshot ? k_cons_to_prim<R, true> : k_cons_to_prim<R, false>)<<<grid_for(c.g.N, 256), 256, 0, s>>>(c, U, P, T, Ne,
+                                                                                                      Ri, Am);
+}
+template <class R>
+void Launch<R>::aux_of_snapshot(const Consts& c, R* T, R* Ne, R* Ri, R* Am, cudaStream_t s) {
+  k_aux_of_snapshot<R><<<grid_for(c.g.N, 256), 256, 0, s>>>(c, T, Ne, Ri, Am);
 }
 template <class R>
 void Launch<R>::init_pass(const Consts& c, const R* U, R* P, Dyn* dyn, cudaStream_t s) {
@@ -379,7 +386,9 @@ void Launch<R>::tile_state(const Geom& gd, const Geom& gs, const R* Us, R* Ud, c
 
 template <class R>
 void Launch<R>::fill_ghosts(const Consts& c, R* U, int nfield, int with_bc, cudaStream_t s) {
-  k_fill_ghosts<R><<<grid_for(c.g.N, 256), 256, 0, s>>>(c.g, U, nfield, with_bc);
+  const Geom& g = c.g;
+  const long long ng = 2LL * GH * ((long long)g.sx * g.sy + (long long)g.sx * g.nz + (long long)g.ny * g.nz);
+  k_fill_ghosts<R><<<grid_for(ng, 256), 256, 0, s>>>(g, U, nfield, with_bc);
 }
 template <class R>
 void Launch<R>::aos_to_soa(long long N, int nf, const double* A, R* S, cudaStream_t s) {

@@ -216,6 +216,44 @@ def test_fp32_reference_order_steps_vs_fp64_oracle(gpu_lib):
     g.close()
 
 
+@pytest.mark.parametrize("precision", [64, 32])
+def test_cons_to_prim_outputs_are_those_of_the_call(gpu_lib, precision):
+    """ConsToPrim's temperature, n_e, rho_i and amb are formed on first access
+    from the density and internal energy the call saw: steps that change the
+    state afterwards leave them as they were, a second ConsToPrim replaces
+    them, and the values equal, bit for bit, those read right after the call."""
+    d, hp = H.load_case("periodic")
+    aux = range(gpumhd.FIELD_TEMP, gpumhd.FIELD_AMB + 1)
+    ref = ctx_for(hp, precision=precision)
+    ref.upload_state(d["init_U"])
+    ref.ConsToPrim()
+    at_once = np.stack([ref.download_field(w) for w in aux])
+    ref.close()
+    g = ctx_for(hp, precision=precision)
+    g.upload_state(d["init_U"])
+    g.exchange_grid(True)
+    g.SaveCons()
+    g.ConsToPrim()
+    g.Adjust_Valf_Max()
+    dt_mhd = g.MHD_Residual()
+    g.Sync_timestep(g.params.dt_rad, dt_mhd)
+    g.Source_Integrate_Tcheck(1)
+    g.exchange_grid(True)
+    later = np.stack([g.download_field(w) for w in aux])
+    assert np.array_equal(later, at_once)
+    # the next stage's ConsToPrim: its own outputs, as read at once from its state
+    U1 = g.download_state()
+    g.ConsToPrim()
+    second = np.stack([g.download_field(w) for w in aux])
+    h = ctx_for(hp, precision=precision)
+    h.upload_state(U1)
+    h.ConsToPrim()
+    assert np.array_equal(second, np.stack([h.download_field(w) for w in aux]))
+    assert not np.array_equal(second, at_once)
+    g.close()
+    h.close()
+
+
 def test_fp32_cons_to_prim_outputs(gpu_lib):
     """ConsToPrim's five EOS outputs in FP32 (float table lookups) against the
     FP64 routine on the reference fixture's state: the FP32 bar, relative L2
