@@ -48,6 +48,127 @@ __device__ __forceinline__ void to_dual(const double* x, Dual<K>* y, int m) {
   for (int q = 0; q < m; q++) y[q] = Dual<K>(x[q]);
 }
 
+// Reverse of apply_direction<double, D1> (eta = 0; src/mhdres_SR.C:373-412):
+// lR, the adjoint of the residual it adds to, back to the direction's 12
+// derivatives (l_dq, written), the cell's velocity and field (l_cen, added)
+// and the Boris factor (l_lf, added).
+template <int D1>
+__device__ __forceinline__ void apply_direction_rev(const double* Dq, const double* cen, double lf, const double* lR,
+                                                    double* l_dq, double* l_cen, double& l_lf) {
+  constexpr int d2 = Dirs<D1>::d2, d3 = Dirs<D1>::d3;
+  const double dB2 = Dq[10], dB3 = Dq[11];
+  const double Bd1 = cen[P_B1 + D1], Bd2 = cen[P_B1 + d2], Bd3 = cen[P_B1 + d3];
+  double cbb[3];
+  cbb[D1] = -Bd2 * dB2 - Bd3 * dB3;
+  cbb[d2] = Bd1 * dB2;
+  cbb[d3] = Bd1 * dB3;
+  double l_cbb[3];
+  for (int i = 0; i < 3; i++) {  // lrt_i = lf*Dq[7+i] + (1-lf)*cbb_i; res[1+i] += lrt_i; res[4] += v_i*lrt_i
+    const double lrt = lf * Dq[7 + i] + (1.0 - lf) * cbb[i];
+    const double l_lrt = lR[1 + i] + lR[4] * cen[P_V1 + i];
+    l_cen[P_V1 + i] += lR[4] * lrt;
+    l_dq[7 + i] = l_lrt * lf;
+    l_lf += l_lrt * (Dq[7 + i] - cbb[i]);
+    l_cbb[i] = l_lrt * (1.0 - lf);
+  }
+  l_dq[10] = -l_cbb[D1] * Bd2 + l_cbb[d2] * Bd1;
+  l_dq[11] = -l_cbb[D1] * Bd3 + l_cbb[d3] * Bd1;
+  l_cen[P_B1 + d2] -= l_cbb[D1] * dB2;
+  l_cen[P_B1 + d3] -= l_cbb[D1] * dB3;
+  l_cen[P_B1 + D1] += l_cbb[d2] * dB2 + l_cbb[d3] * dB3;
+  for (int q = 0; q < 5; q++) l_dq[q] = -lR[q];
+  l_dq[5] = -lR[Dirs<D1>::fa];
+  l_dq[6] = -lR[Dirs<D1>::fb];
+}
+
+// Reverse of stage_sources<double> (gravity and the Boris correction,
+// src/Add_Sources_Integrate_SR.C:331-392): lG, the adjoint of the residual
+// after them, back to the residual before them (l_R, written) and the cell's
+// density, velocity and field (l_cen, added); every max takes the forward's
+// branch.  The radiative term is zero on this path.
+__device__ __forceinline__ void stage_sources_rev(const double* R, const double* cen, double gx, double inv_va2max,
+                                                  const double* lG, double* l_R, double* l_cen) {
+  const double tiny = tiny100<double>();
+  const double rh = cen[P_D];
+  const double v[3] = {cen[P_V1], cen[P_V2], cen[P_V3]}, B[3] = {cen[P_B1], cen[P_B2], cen[P_B3]};
+  // ---- forward
+  const double dn2 = gx * rh - 0.0;
+  const double F[3] = {R[1] + dn2, R[2], R[3]};
+  const double rd = R[0];
+  const double bb = B[0] * B[0] + B[1] * B[1] + B[2] * B[2];
+  const double va2 = bb / rh;
+  const double x2 = va2 * inv_va2max, x4 = x2 * x2;
+  const double D = 1.0 + x2 + x4;
+  const double bf = x4 / D;
+  double f[3], bo[3];
+  for (int i = 0; i < 3; i++) f[i] = F[i] - v[i] * rd;
+  const double bq = d_fmax(tiny, bb);
+  const double q = (f[0] * B[0] + f[1] * B[1] + f[2] * B[2]) / bq;
+  for (int i = 0; i < 3; i++) bo[i] = -bf * (f[i] - q * B[i]);
+  // ---- reverse
+  double l_v[3] = {0.0, 0.0, 0.0}, l_B[3] = {0.0, 0.0, 0.0}, l_f[3];
+  double l_bf = 0.0, l_q = 0.0;
+  for (int i = 0; i < 3; i++) {  // R[1+i] += bo_i, R[4] += sum bo_i * v_i, bo_i = -bf*(f_i - q*B_i)
+    const double l_bo = lG[1 + i] + lG[4] * v[i];
+    l_v[i] += lG[4] * bo[i];
+    l_bf -= l_bo * (f[i] - q * B[i]);
+    l_f[i] = -bf * l_bo;
+    l_q += bf * l_bo * B[i];
+    l_B[i] += bf * l_bo * q;
+  }
+  const double l_Nq = l_q / bq;  // q = (f . B) / max(tiny, bb)
+  double l_bb = (tiny < bb) ? -l_q * q / bq : 0.0;
+  for (int i = 0; i < 3; i++) {
+    l_f[i] += l_Nq * B[i];
+    l_B[i] += l_Nq * f[i];
+  }
+  double l_rd = 0.0, l_F[3];
+  for (int i = 0; i < 3; i++) {  // f_i = F_i - v_i * rd
+    l_F[i] = l_f[i];
+    l_v[i] -= l_f[i] * rd;
+    l_rd -= l_f[i] * v[i];
+  }
+  const double l_D = -l_bf * bf / D;  // bf = x4 / ((1 + x2) + x4)
+  const double l_x4 = l_bf / D + l_D;
+  const double l_x2 = l_D + l_x4 * 2.0 * x2;
+  const double l_va2 = l_x2 * inv_va2max;
+  l_bb += l_va2 / rh;
+  double l_rh = -l_va2 * va2 / rh;
+  for (int i = 0; i < 3; i++) l_B[i] += l_bb * 2.0 * B[i];
+  const double l_R1 = lG[1] + l_F[0];  // R[1] + dn2 is both the output and fx
+  l_R[0] = lG[0] + l_rd;
+  l_R[1] = l_R1;
+  l_R[2] = lG[2] + l_F[1];
+  l_R[3] = lG[3] + l_F[2];
+  for (int o = 4; o < NV; o++) l_R[o] = lG[o];
+  const double l_dn2 = l_R1 + lG[4] * v[0];  // R[4] += dn2 * vx
+  l_v[0] += lG[4] * dn2;
+  l_rh += l_dn2 * gx;
+  l_cen[P_D] += l_rh;
+  for (int i = 0; i < 3; i++) {
+    l_cen[P_V1 + i] += l_v[i];
+    l_cen[P_B1 + i] += l_B[i];
+  }
+}
+
+// Reverse of boris_lf<double> (src/mhdres_SR.C:310-323): l_lf back to the
+// cell's density and field (l_cen, added).
+__device__ __forceinline__ void boris_lf_rev(const double* cen, double inv_va2max, double l_lf, double* l_cen) {
+  const double dn = 1.0 / cen[P_D];
+  const double B[3] = {cen[P_B1], cen[P_B2], cen[P_B3]};
+  const double bb = B[0] * B[0] + B[1] * B[1] + B[2] * B[2];
+  const double va2 = bb * dn;
+  const double x2 = va2 * inv_va2max, x4 = x2 * x2, s = 1.0 + x2;
+  const double E = s + x4, lf = s / E;
+  const double l_s = l_lf * (1.0 - lf) / E;  // lf = s / (s + x4)
+  const double l_x4 = -l_lf * lf / E;
+  const double l_x2 = l_s + l_x4 * 2.0 * x2;
+  const double l_va2 = l_x2 * inv_va2max;
+  const double l_bb = l_va2 * dn, l_dn = l_va2 * bb;
+  l_cen[P_D] += -l_dn * dn * dn;
+  for (int i = 0; i < 3; i++) l_cen[P_B1 + i] += l_bb * 2.0 * B[i];
+}
+
 // ------------------------------------------------------------- stage, part A
 // Per cell c: recompute the stage's forward residual G(c) and pre-Tcheck state
 // U0 + wdt*G, then: lamU0 += Tcheck^T lam_out; from lam_G = wdt * that, the
@@ -125,56 +246,23 @@ __global__ void k_stage_a(Consts c, const Dyn* dyn, Box b, const double* __restr
     double lg[NV];
 #pragma unroll
     for (int q = 0; q < NV; q++) lg[q] = wdt * lp[q];
-    // sources and Boris correction: G = sources(R, cen)
+    // sources and Boris correction (G = sources(R, cen)), the residual
+    // assembly of each direction (R = sum_d res_d(Dq_d, cen, lf)) and the
+    // Boris factor lf(cen), each transposed in one reverse pass
     double lR[NV], lcen[NF];
     for (int q = 0; q < NF; q++) lcen[q] = 0.0;
-    for (int q = 0; q < NV + 8; q++) {
-      D1 Ra[NV], cd[NF];
-      to_dual(R, Ra, NV);
-      to_dual(cen, cd, NF);
-      const int cq[8] = {P_D, P_V1, P_V2, P_V3, P_EI, P_B1, P_B2, P_B3};
-      if (q < NV) Ra[q].d[0] = 1.0;
-      else cd[cq[q - NV]].d[0] = 1.0;
-      stage_sources<D1>(Ra, cd, D1(k.gx), D1(inv_va2max), D1(invRdt));
-      double s = 0.0;
-      for (int o = 0; o < NV; o++) s += Ra[o].d[0] * lg[o];
-      if (q < NV) lR[q] = s;
-      else lcen[cq[q - NV]] += s;
-    }
-    // residual assembly per direction: R += res_d(Dq_d, cen, lf)
+    stage_sources_rev(R, cen, k.gx, inv_va2max, lg, lR, lcen);
     double llf = 0.0;
-    const int cu[6] = {P_V1, P_V2, P_V3, P_B1, P_B2, P_B3};
-#pragma unroll
-    for (int d = 0; d < 3; d++) {
-      for (int q = 0; q < NF + 7; q++) {
-        D1 acc[NV], dq[NF], cd[NF], lfd(lf);
-        for (int o = 0; o < NV; o++) acc[o] = D1(0.0);
-        to_dual(Dq[d], dq, NF);
-        to_dual(cen, cd, NF);
-        if (q < NF) dq[q].d[0] = 1.0;
-        else if (q < NF + 6) cd[cu[q - NF]].d[0] = 1.0;
-        else lfd.d[0] = 1.0;
-        if (d == 0) apply_direction<D1, 0>(acc, dq, cd, lfd);
-        else if (d == 1) apply_direction<D1, 1>(acc, dq, cd, lfd);
-        else apply_direction<D1, 2>(acc, dq, cd, lfd);
-        double s = 0.0;
-        for (int o = 0; o < NV; o++) s += acc[o].d[0] * lR[o];
-        if (q < NF) buf_dq[(long long)(d * NF + q) * b.n + li] = s;
-        else if (q < NF + 6) lcen[cu[q - NF]] += s;
-        else llf += s;
-      }
-    }
-    // Boris factor from the cell's primitives
     {
-      const int cb[4] = {P_D, P_B1, P_B2, P_B3};
-      for (int t = 0; t < 4; t++) {
-        D1 cd[NF];
-        to_dual(cen, cd, NF);
-        cd[cb[t]].d[0] = 1.0;
-        const D1 l = boris_lf<D1>(cd, D1(inv_va2max));
-        lcen[cb[t]] += l.d[0] * llf;
-      }
+      double ldq[NF];
+      apply_direction_rev<0>(Dq[0], cen, lf, lR, ldq, lcen, llf);
+      for (int q = 0; q < NF; q++) buf_dq[(long long)(0 * NF + q) * b.n + li] = ldq[q];
+      apply_direction_rev<1>(Dq[1], cen, lf, lR, ldq, lcen, llf);
+      for (int q = 0; q < NF; q++) buf_dq[(long long)(1 * NF + q) * b.n + li] = ldq[q];
+      apply_direction_rev<2>(Dq[2], cen, lf, lR, ldq, lcen, llf);
+      for (int q = 0; q < NF; q++) buf_dq[(long long)(2 * NF + q) * b.n + li] = ldq[q];
     }
+    boris_lf_rev(cen, inv_va2max, llf, lcen);
     for (int q = 0; q < NPRIM; q++) buf_wc[(long long)q * b.n + li] = lcen[q];
   }
 }
@@ -329,6 +417,289 @@ template <int DIR> __device__ __forceinline__ int pos_of(int i, int j, int k) {
   return GH + (DIR == 0 ? i : (DIR == 1 ? j : k));
 }
 
+// Reverse mode of tvd_flux<double, DIR> (DIAG off; src/tvdlimit_SR.C:436-563
+// as gpumhd_kernels.cuh restates it): the forward intermediates are
+// recomputed, then the adjoints lF (the 8 interface fluxes) and lq (the
+// resistive-heating term) are carried back to the inputs, each min / max /
+// |.| taking the branch the forward took -- the one-sided subgradient the
+// dual numbers give, in one pass instead of one dual pass per input.  Adds
+// into l_am, l_a, l_b, l_bp (NT TCell fields each) and l_sa, l_sb (slopes).
+template <int DIR>
+__device__ void tvd_flux_rev(const Consts& c, const TCell<double>& am, const TCell<double>& a, const TCell<double>& b,
+                             const TCell<double>& bp, const double* sa, const double* sb, int ia, int sz, double fac0,
+                             double cmax_t, bool hyper, int istart, const double* lF, double lq, double* l_am,
+                             double* l_a, double* l_b, double* l_bp, double* l_sa, double* l_sb) {
+  const KC<double>& k = c.kd;
+  const double tiny = tiny100<double>();
+  auto dn_field = [](int v) { return (v >= 1 && v <= 3) ? T_HV : ((v >= 5) ? T_HB : T_HE); };
+  // ---- forward
+  double sl[NV], sll[NV], den[NV], rf[NV], cfv[NV], G[NV], F0[NV], F[NV];
+#pragma unroll
+  for (int v = 0; v < NV; v++) {
+    sl[v] = b.q[v] - a.q[v];
+    sll[v] = b.q[v] - a.q[v] - (sa[v] + sb[v]);
+    const double dnv = tf(a)[dn_field(v)];
+    den[v] = smax(tiny, fabs(sl[v]));
+    rf[v] = fabs(sll[v]) / den[v];
+    cfv[v] = smax(0.0, smin(sll[v], sl[v])) + smin(0.0, smax(sll[v], sl[v]));
+    G[v] = smax(0.0, 1.0 + dnv * (rf[v] - 1.0));
+    F0[v] = G[v] * cfv[v];
+  }
+  const double M = smax(a.cm, b.cm);
+  const double fac = fac0 * smin(cmax_t, M);
+#pragma unroll
+  for (int v = 0; v < NV; v++) F[v] = F0[v] * fac;
+  F[5 + DIR] *= k.B_par_diff;
+  double F2[NV];  // before the coefficients
+#pragma unroll
+  for (int v = 0; v < NV; v++) F2[v] = F[v];
+  double argv = 0.0, arge = 0.0, cv = 1.0, ce = 1.0;
+  if (c.need_coeff) {
+    F[0] *= k.tvd_coeff[0];
+    argv = k.visc_coeff_bot * a.hb + k.visc_coeff_top * a.ht;
+    cv = smax(k.tvd_coeff[1], argv);
+    F[1] *= cv; F[2] *= cv; F[3] *= cv;
+    F[4] *= k.tvd_coeff[2];
+    arge = k.eta_coeff_bot * a.hb + k.eta_coeff_top * a.ht;
+    ce = smax(k.tvd_coeff[3], arge);
+    F[5] *= ce; F[6] *= ce; F[7] *= ce;
+  }
+  const bool hy = DIR == 0 && hyper && ia >= istart;
+  double dh = 0.0, X[NV] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  if (hy) {
+    dh = smax(a.hd, b.hd);
+    const int hv[3] = {0, 1, 4};
+    for (int t = 0; t < 3; t++) {
+      const int v = hv[t];
+      X[v] = 0.125 * (bp.q[v] - am.q[v]) - 0.375 * (b.q[v] - a.q[v]);
+      F[v] -= dh * X[v];
+    }
+  }
+  double u[5];
+#pragma unroll
+  for (int v = 0; v < 5; v++) u[v] = 0.5 * (a.q[v] + sa[v] + b.q[v] - sb[v]);
+  double U0 = u[0], U4 = u[4], f0 = F[0], f4a = F[4];
+  if (c.rho_log) {
+    U0 = exp(u[0]);
+    f0 = F[0] * U0;
+    U4 = exp(u[4]);
+    f4a = F[4] * U4;
+  }
+  const double CZ = smin(k.CZ, k.CZ);
+  const double mcz = f0 * CZ;
+  double fn[4];
+  for (int t = 1; t <= 3; t++) fn[t] = F[t] * U0 + u[t] * mcz;
+  const double S = u[1] * fn[1] + u[2] * fn[2] + u[3] * fn[3];
+  const bool zero5 = DIR == 0 && !c.g.periodic_x && (ia == sz - GH - 1 || ia == GH - 1);
+  const double Fq[3] = {zero5 ? 0.0 : F[5], F[6], F[7]};
+  // ---- reverse
+  double lo[NV];
+#pragma unroll
+  for (int v = 0; v < NV; v++) lo[v] = lF[v];
+  for (int t = 0; t < 3; t++) {  // qres = sum (b.q - a.q) * F, v = 5..7
+    const int v = 5 + t;
+    lo[v] += lq * (b.q[v] - a.q[v]);
+    l_b[v] += lq * Fq[t];
+    l_a[v] -= lq * Fq[t];
+  }
+  if (zero5) lo[5] = 0.0;
+  // F4 = (f4a*U0 + U4*mcz) + qt*S
+  double l_u[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+  double l_U4 = lo[4] * mcz, l_mcz = lo[4] * U4;
+  l_a[T_QT] += lo[4] * S;
+  const double l_S = lo[4] * a.qt;
+  double l_U0 = lo[4] * f4a;
+  const double l_f4a = lo[4] * U0;
+  double lFc[NV] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0, 0.0};  // adjoints of F after coefficients and hyperdiffusion
+  for (int t = 1; t <= 3; t++) {  // fn = F*U0 + u*mcz
+    const double l_fn = lo[t] + l_S * u[t];
+    l_u[t] += l_S * fn[t] + l_fn * mcz;
+    lFc[t] += l_fn * U0;
+    l_U0 += l_fn * F[t];
+    l_mcz += l_fn * u[t];
+  }
+  const double l_f0 = lo[0] + l_mcz * CZ;
+  if (c.rho_log) {
+    lFc[0] += l_f0 * U0;
+    l_U0 += l_f0 * F[0];
+    lFc[4] += l_f4a * U4;
+    l_U4 += l_f4a * F[4];
+    l_u[0] += l_U0 * U0;
+    l_u[4] += l_U4 * U4;
+  } else {
+    lFc[0] += l_f0;
+    lFc[4] += l_f4a;
+    l_u[0] += l_U0;
+    l_u[4] += l_U4;
+  }
+  for (int v = 5; v < NV; v++) lFc[v] += lo[v];
+#pragma unroll
+  for (int v = 0; v < 5; v++) {  // u = 0.5 * (a.q + sa + b.q - sb)
+    const double h = 0.5 * l_u[v];
+    l_a[v] += h;
+    l_sa[v] += h;
+    l_b[v] += h;
+    l_sb[v] -= h;
+  }
+  if (hy) {  // F -= dh * X
+    double l_dh = 0.0;
+    const int hv[3] = {0, 1, 4};
+    for (int t = 0; t < 3; t++) {
+      const int v = hv[t];
+      l_dh -= lFc[v] * X[v];
+      const double lX = -lFc[v] * dh;
+      l_bp[v] += 0.125 * lX;
+      l_am[v] -= 0.125 * lX;
+      l_b[v] -= 0.375 * lX;
+      l_a[v] += 0.375 * lX;
+    }
+    if (a.hd < b.hd) l_b[T_HD] += l_dh;
+    else l_a[T_HD] += l_dh;
+  }
+  double l1[NV];  // adjoints of F after the scaling by fac (and B_par_diff)
+  if (c.need_coeff) {
+    l1[0] = lFc[0] * k.tvd_coeff[0];
+    l1[4] = lFc[4] * k.tvd_coeff[2];
+    double l_cv = 0.0, l_ce = 0.0;
+    for (int v = 1; v <= 3; v++) { l1[v] = lFc[v] * cv; l_cv += lFc[v] * F2[v]; }
+    for (int v = 5; v <= 7; v++) { l1[v] = lFc[v] * ce; l_ce += lFc[v] * F2[v]; }
+    if (k.tvd_coeff[1] < argv) { l_a[T_HBOT] += l_cv * k.visc_coeff_bot; l_a[T_HTOP] += l_cv * k.visc_coeff_top; }
+    if (k.tvd_coeff[3] < arge) { l_a[T_HBOT] += l_ce * k.eta_coeff_bot; l_a[T_HTOP] += l_ce * k.eta_coeff_top; }
+  } else {
+#pragma unroll
+    for (int v = 0; v < NV; v++) l1[v] = lFc[v];
+  }
+  l1[5 + DIR] *= k.B_par_diff;
+  double l_fac = 0.0;
+#pragma unroll
+  for (int v = 0; v < NV; v++) l_fac += l1[v] * F0[v];
+  if (M < cmax_t) {  // fac = fac0 * min(cmax_t, max(a.cm, b.cm))
+    const double l_M = l_fac * fac0;
+    if (a.cm < b.cm) l_b[T_CM] += l_M;
+    else l_a[T_CM] += l_M;
+  }
+#pragma unroll
+  for (int v = 0; v < NV; v++) {
+    const double l_F0 = l1[v] * fac;
+    const double l_G = l_F0 * cfv[v], l_cf = l_F0 * G[v];
+    const int df = dn_field(v);
+    const double dnv = tf(a)[df];
+    double l_rf = 0.0;
+    if (0.0 < 1.0 + dnv * (rf[v] - 1.0)) {  // G = max(0, 1 + dn*(rf - 1))
+      l_a[df] += l_G * (rf[v] - 1.0);
+      l_rf = l_G * dnv;
+    }
+    double l_sl = 0.0, l_sll = 0.0;
+    l_sll += (l_rf / den[v]) * (sll[v] < 0.0 ? -1.0 : 1.0);  // rf = |sll| / den
+    if (tiny < fabs(sl[v])) l_sl += (-l_rf * rf[v] / den[v]) * (sl[v] < 0.0 ? -1.0 : 1.0);
+    if (0.0 < smin(sll[v], sl[v])) {  // cf = max(0, min(sll, sl)) + min(0, max(sll, sl))
+      if (sl[v] < sll[v]) l_sl += l_cf;
+      else l_sll += l_cf;
+    }
+    if (smax(sll[v], sl[v]) < 0.0) {
+      if (sll[v] < sl[v]) l_sl += l_cf;
+      else l_sll += l_cf;
+    }
+    l_b[v] += l_sl + l_sll;  // sl = b.q - a.q, sll = sl - (sa + sb)
+    l_a[v] -= l_sl + l_sll;
+    l_sa[v] -= l_sll;
+    l_sb[v] -= l_sll;
+  }
+}
+
+// Reverse mode of tvd_update<double> (DIAG off, no compensation;
+// src/tvdlimit_SR.C:565-657): given lu (the adjoint of the updated state),
+// the adjoints of u_in (l_in), of the cell's TCell (l_c0: q, BC2, bsqr, qt),
+// of the fluxes at its right / left interfaces (l_fp, l_fm) and of their
+// heating terms (l_qp, l_qm), each floor taking the forward's branch.
+__device__ void tvd_update_rev(const Consts& c, double dtt, const double* Fp, const double* Fm, double qp, double qm,
+                               const TCell<double>& c0, const double* u_in, const double* lu, double* l_in,
+                               double* l_c0, double* l_fp, double* l_fm, double& l_qp, double& l_qm) {
+  const KC<double>& k = c.kd;
+  const double tiny = tiny100<double>();
+  // ---- forward
+  double res[NV];
+#pragma unroll
+  for (int v = 0; v < NV; v++) res[v] = dtt * (Fp[v] - Fm[v]);
+  const double W = res[1] * c0.q[1] + res[2] * c0.q[2] + res[3] * c0.q[3];
+  const double r4a = res[4] + (1.0 - c0.qt) * W;
+  const double bs = smax(tiny, c0.bsqr);
+  const double num = res[1] * c0.q[5] + res[2] * c0.q[6] + res[3] * c0.q[7];
+  const double dn = num / bs;
+  double bb[3];
+  for (int t = 0; t < 3; t++) bb[t] = -c0.BC2 * (res[1 + t] - dn * c0.q[5 + t]);
+  const double b3 = bb[0] * c0.q[1] + bb[1] * c0.q[2] + bb[2] * c0.q[3];
+  double r[NV];
+#pragma unroll
+  for (int v = 0; v < NV; v++) r[v] = res[v];
+  for (int t = 0; t < 3; t++) r[1 + t] += bb[t];
+  const double qres = 0.5 * (qp + qm) * c0.qt;
+  r[4] = (r4a + b3) + dtt * qres;
+  double u[NV];
+#pragma unroll
+  for (int v = 0; v < NV; v++) u[v] = u_in[v] + r[v];
+  const double u0f = smax(k.rho_min, u[0]);
+  const double K = u[1] * u[1] + u[2] * u[2] + u[3] * u[3];
+  const double ef = k.eps_min * u0f + 0.5 * K / u0f;
+  // ---- reverse
+  double l_u[NV];
+#pragma unroll
+  for (int v = 0; v < NV; v++) l_u[v] = lu[v];
+  double l_ef = 0.0;
+  if (u[4] < ef) {  // u4 = max(u4, ef)
+    l_ef = lu[4];
+    l_u[4] = 0.0;
+  }
+  double l_u0f = lu[0] + l_ef * (k.eps_min - 0.5 * K / (u0f * u0f));
+  for (int t = 1; t <= 3; t++) l_u[t] += l_ef * u[t] / u0f;
+  l_u[0] = (k.rho_min < u[0]) ? l_u0f : 0.0;  // u0 = max(rho_min, u0)
+#pragma unroll
+  for (int v = 0; v < NV; v++) l_in[v] = l_u[v];
+  // r4 = (r4a + b3) + dtt * 0.5 * (qp + qm) * qt
+  const double l_qres = l_u[4] * dtt;
+  l_qp = 0.5 * l_qres * c0.qt;
+  l_qm = l_qp;
+  l_c0[T_QT] += l_qres * 0.5 * (qp + qm);
+  double l_res[NV];
+#pragma unroll
+  for (int v = 0; v < NV; v++) l_res[v] = l_u[v];  // r = res (+ bb on 1..3)
+  const double l_b3 = l_u[4];
+  double l_bb[3];
+  for (int t = 0; t < 3; t++) {
+    l_bb[t] = l_u[1 + t] + l_b3 * c0.q[1 + t];  // b3 = sum bb * q(1..3)
+    l_c0[1 + t] += l_b3 * bb[t];
+  }
+  double l_dn = 0.0;
+  for (int t = 0; t < 3; t++) {  // bb = -BC2 * (res - dn * qB)
+    const double in = res[1 + t] - dn * c0.q[5 + t];
+    l_c0[T_BC2] -= l_bb[t] * in;
+    const double l_inn = -c0.BC2 * l_bb[t];
+    l_res[1 + t] += l_inn;
+    l_dn -= l_inn * c0.q[5 + t];
+    l_c0[5 + t] -= l_inn * dn;
+  }
+  const double l_num = l_dn / bs;  // dn = num / bs
+  if (tiny < c0.bsqr) l_c0[T_BSQR] += -l_dn * dn / bs;
+  for (int t = 0; t < 3; t++) {
+    l_res[1 + t] += l_num * c0.q[5 + t];
+    l_c0[5 + t] += l_num * res[1 + t];
+  }
+  // r4a = res4 + (1 - qt) * W, W = sum res(1..3) * q(1..3)
+  const double l_r4a = l_u[4];
+  l_res[4] = l_r4a;
+  l_c0[T_QT] -= l_r4a * W;
+  const double l_W = l_r4a * (1.0 - c0.qt);
+  for (int t = 1; t <= 3; t++) {
+    l_res[t] += l_W * c0.q[t];
+    l_c0[t] += l_W * res[t];
+  }
+#pragma unroll
+  for (int v = 0; v < NV; v++) {  // res = dtt * (Fp - Fm)
+    l_fp[v] = l_res[v] * dtt;
+    l_fm[v] = -l_res[v] * dtt;
+  }
+}
+
 // T1: per cell i, the update transposed.  Outputs: lam_in_direct (8), the
 // adjoint of the cell's TCell (19), and of its right / left interface fluxes
 // and heating terms (9 + 9).
@@ -371,30 +742,23 @@ __global__ void k_tvd_t1(Consts c, const Dyn* dyn, Box b, const double* __restri
       }
       for (int q = 0; q < 5; q++) lo[q] = l5[q];
     }
-    // inputs of tvd_update: u_in (8), c0 {q 0..7, BC2, bsqr, qt}, Fp (8), Fm (8), qp, qm
-    const int cf[11] = {0, 1, 2, 3, 4, 5, 6, 7, T_BC2, T_BSQR, T_QT};
-    for (int q = 0; q < 37; q++) {
-      D1 ui[NV], fp[NV], fm[NV], u[NV];
-      D1 qpd(qp), qmd(qm);
-      to_dual(r0.v, ui, NV);
-      to_dual(Fp, fp, NV);
-      to_dual(Fm, fm, NV);
-      TCell<D1> t0 = dual_cell(T[2]);
-      if (q < 8) ui[q].d[0] = 1.0;
-      else if (q < 19) tf(t0)[cf[q - 8]].d[0] = 1.0;
-      else if (q < 27) fp[q - 19].d[0] = 1.0;
-      else if (q < 35) fm[q - 27].d[0] = 1.0;
-      else if (q == 35) qpd.d[0] = 1.0;
-      else qmd.d[0] = 1.0;
-      tvd_update<D1>(c, D1(s.dtt), fp, fm, qpd, qmd, t0, ui, u);
-      double acc = 0.0;
-      for (int o = 0; o < NV; o++) acc += u[o].d[0] * lo[o];
-      if (q < 8) o_in[(long long)q * b.n + li] = acc;
-      else if (q < 19) o_cell[(long long)cf[q - 8] * b.n + li] = acc;
-      else if (q < 27) o_fp[(long long)(q - 19) * b.n + li] = acc;
-      else if (q < 35) o_fm[(long long)(q - 27) * b.n + li] = acc;
-      else if (q == 35) o_fp[(long long)8 * b.n + li] = acc;
-      else o_fm[(long long)8 * b.n + li] = acc;
+    // the update transposed in one reverse pass (inputs: u_in, the cell's
+    // q, BC2, bsqr, qt, the fluxes and heating terms of both interfaces)
+    {
+      double l_in[NV], l_c0[NT], l_fp[NV], l_fm[NV], l_qp = 0.0, l_qm = 0.0;
+      for (int f = 0; f < NT; f++) l_c0[f] = 0.0;
+      tvd_update_rev(c, s.dtt, Fp, Fm, qp, qm, T[2], r0.v, lo, l_in, l_c0, l_fp, l_fm, l_qp, l_qm);
+      for (int q = 0; q < NV; q++) {
+        o_in[(long long)q * b.n + li] = l_in[q];
+        o_cell[(long long)q * b.n + li] = l_c0[q];
+        o_fp[(long long)q * b.n + li] = l_fp[q];
+        o_fm[(long long)q * b.n + li] = l_fm[q];
+      }
+      o_cell[(long long)T_BC2 * b.n + li] = l_c0[T_BC2];
+      o_cell[(long long)T_BSQR * b.n + li] = l_c0[T_BSQR];
+      o_cell[(long long)T_QT * b.n + li] = l_c0[T_QT];
+      o_fp[(long long)8 * b.n + li] = l_qp;
+      o_fm[(long long)8 * b.n + li] = l_qm;
     }
     const int unused[8] = {T_CM, T_HE, T_HV, T_HB, T_VSQR, T_HD, T_HBOT, T_HTOP};
     for (int f = 0; f < 8; f++) o_cell[(long long)unused[f] * b.n + li] = 0.0;
@@ -421,30 +785,18 @@ __global__ void k_tvd_t2(Consts c, const Dyn* dyn, Box b, const double* __restri
     tvd_slope<double>(c, T[0], T[1], T[2], s.vsqr_diff, sa);
     tvd_slope<double>(c, T[1], T[2], T[3], s.vsqr_diff, sb);
     const int p = pos_of<DIR>(i, j, k);
-    for (int t = 0; t < 4 * NT + 2 * NV; t++) o_if[(long long)t * b.n + li] = 0.0;
-    // seeds: (role, field)
-    const int fa[16] = {0, 1, 2, 3, 4, 5, 6, 7, T_CM, T_HE, T_HV, T_HB, T_HD, T_HBOT, T_HTOP, T_QT};
-    const int fb[10] = {0, 1, 2, 3, 4, 5, 6, 7, T_CM, T_HD};
-    const int fh[3] = {0, 1, 4};
-    const int nseed = 16 + 10 + 16 + (s.hyper ? 6 : 0);
-    for (int q = 0; q < nseed; q++) {
-      TCell<D1> am = dual_cell(T[0]), a = dual_cell(T[1]), bb = dual_cell(T[2]), bp = dual_cell(T[3]);
-      D1 sad[NV], sbd[NV], F[NV], qr;
-      to_dual(sa, sad, NV);
-      to_dual(sb, sbd, NV);
-      int role, f;
-      if (q < 16) { role = 1; f = fa[q]; tf(a)[f].d[0] = 1.0; }
-      else if (q < 26) { role = 2; f = fb[q - 16]; tf(bb)[f].d[0] = 1.0; }
-      else if (q < 34) { role = 4; f = q - 26; sad[f].d[0] = 1.0; }
-      else if (q < 42) { role = 5; f = q - 34; sbd[f].d[0] = 1.0; }
-      else if (q < 45) { role = 0; f = fh[q - 42]; tf(am)[f].d[0] = 1.0; }
-      else { role = 3; f = fh[q - 45]; tf(bp)[f].d[0] = 1.0; }
-      tvd_flux<D1, DIR>(c, am, a, bb, bp, sad, sbd, p, s.sz, D1(s.fac0), D1(s.cmax_t), s.hyper, s.istart, F, qr);
-      double acc = qr.d[0] * lF[NV];
-      for (int o = 0; o < NV; o++) acc += F[o].d[0] * lF[o];
-      const int slot = role < 4 ? role * NT + f : 4 * NT + (role - 4) * NV + f;
-      o_if[(long long)slot * b.n + li] = acc;
-    }
+    // the interface flux transposed in one reverse pass onto its four cells'
+    // TCells (am, a, b, bp) and its two slopes
+    double l_t[4][NT], l_s[2][NV];
+    for (int r = 0; r < 4; r++)
+      for (int f = 0; f < NT; f++) l_t[r][f] = 0.0;
+    for (int q = 0; q < NV; q++) l_s[0][q] = l_s[1][q] = 0.0;
+    tvd_flux_rev<DIR>(c, T[0], T[1], T[2], T[3], sa, sb, p, s.sz, s.fac0, s.cmax_t, s.hyper, s.istart, lF, lF[NV],
+                      l_t[0], l_t[1], l_t[2], l_t[3], l_s[0], l_s[1]);
+    for (int r = 0; r < 4; r++)
+      for (int f = 0; f < NT; f++) o_if[(long long)(r * NT + f) * b.n + li] = l_t[r][f];
+    for (int r = 0; r < 2; r++)
+      for (int q = 0; q < NV; q++) o_if[(long long)(4 * NT + r * NV + q) * b.n + li] = l_s[r][q];
   }
 }
 
