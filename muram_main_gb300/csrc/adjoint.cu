@@ -169,6 +169,76 @@ __device__ __forceinline__ void boris_lf_rev(const double* cen, double inv_va2ma
   for (int i = 0; i < 3; i++) l_cen[P_B1 + i] += l_bb * 2.0 * B[i];
 }
 
+// Reverse of flux12<double, D1> (src/mhdres_SR.C:330-347): lF, the adjoints
+// of the 12 directional quantities, back to the cell's primitives (lw, added).
+template <int D1>
+__device__ __forceinline__ void flux12_rev(const double* p, const double* lF, double* lw) {
+  const double d = p[P_D], v[3] = {p[P_V1], p[P_V2], p[P_V3]}, ei = p[P_EI], B[3] = {p[P_B1], p[P_B2], p[P_B3]};
+  const double pr = p[P_P], ekin = p[P_EK];
+  const double vel = v[D1], mag = B[D1];
+  const double mflx = vel * d;
+  double l_v[3] = {0.0, 0.0, 0.0}, l_B[3] = {0.0, 0.0, 0.0};
+  double l_mflx = lF[0], l_vel = 0.0, l_mag = 0.0;
+  for (int t = 0; t < 3; t++) {  // f(1+t) = mflx * v_t + (t == D1) * pr
+    l_mflx += lF[1 + t] * v[t];
+    l_v[t] += lF[1 + t] * mflx;
+  }
+  lw[P_P] += lF[1 + D1];
+  l_vel += lF[4] * (ei + ekin + pr);  // f4 = vel * (ei + ekin + pr)
+  lw[P_EI] += lF[4] * vel;
+  lw[P_EK] += lF[4] * vel;
+  lw[P_P] += lF[4] * vel;
+  for (int t = 0; t < 3; t++) {  // induction flux of component t: vel * B_t - v_t * mag
+    const double l = (Dirs<D1>::fa == 5 + t ? lF[5] : 0.0) + (Dirs<D1>::fb == 5 + t ? lF[6] : 0.0);
+    l_vel += l * B[t];
+    l_B[t] += l * vel;
+    l_v[t] -= l * mag;
+    l_mag -= l * v[t];
+  }
+  for (int t = 0; t < 3; t++) {  // Maxwell stress: mag * B_t - (t == D1) * pmag
+    l_mag += lF[7 + t] * B[t];
+    l_B[t] += lF[7 + t] * mag;
+  }
+  lw[P_PM] -= lF[7 + D1];
+  l_B[Dirs<D1>::d2] += lF[10];
+  l_B[Dirs<D1>::d3] += lF[11];
+  l_vel += l_mflx * d;  // mflx = vel * d
+  lw[P_D] += l_mflx * vel;
+  l_v[D1] += l_vel;
+  l_B[D1] += l_mag;
+  for (int t = 0; t < 3; t++) {
+    lw[P_V1 + t] += l_v[t];
+    lw[P_B1 + t] += l_B[t];
+  }
+}
+
+// Reverse of prim_of_raw<double, false> (src/cons_to_prim.C:148-159 and the
+// residual's kinetic and magnetic pressures): lw, the adjoints of the 11
+// primitives, back to the cell's 9 stored values (lr, written).
+__device__ __forceinline__ void prim_of_raw_rev(const Raw9<double>& r, const double* lw, double* lr) {
+  const double d = r.v[0], dn = 1.0 / d;
+  const double m[3] = {r.v[1], r.v[2], r.v[3]};
+  double v[3];
+  for (int t = 0; t < 3; t++) v[t] = m[t] * dn;
+  const double vv = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+  double l_d = lw[P_D] + lw[P_EK] * 0.5 * vv;  // ekin = 0.5 * d * vv
+  double l_vv = lw[P_EK] * 0.5 * d;
+  const double l_e = lw[P_EI];  // ei = e - 0.5 * vv * d
+  l_vv -= lw[P_EI] * 0.5 * d;
+  l_d -= lw[P_EI] * 0.5 * vv;
+  double l_dn = 0.0;
+  for (int t = 0; t < 3; t++) {
+    const double l_v = lw[P_V1 + t] + l_vv * 2.0 * v[t];
+    lr[1 + t] = l_v * dn;  // v = m * dn
+    l_dn += l_v * m[t];
+  }
+  l_d -= l_dn * dn * dn;  // dn = 1 / d
+  lr[0] = l_d;
+  lr[4] = l_e;
+  for (int t = 0; t < 3; t++) lr[5 + t] = lw[P_B1 + t] + lw[P_PM] * r.v[5 + t];  // pmag = 0.5 * |B|^2
+  lr[8] = lw[P_P];
+}
+
 // ------------------------------------------------------------- stage, part A
 // Per cell c: recompute the stage's forward residual G(c) and pre-Tcheck state
 // U0 + wdt*G, then: lamU0 += Tcheck^T lam_out; from lam_G = wdt * that, the
@@ -301,29 +371,14 @@ __global__ void k_stage_b(Consts c, Box b, const double* __restrict__ Uin, const
         const double* B = buf_dq + (long long)(d * NF + q) * b.n;
         lF[q] = k.w1[d] * (B[nb[1]] - B[nb[2]]) + k.w2[d] * (B[nb[0]] - B[nb[3]]);
       }
-      for (int q = 0; q < NPRIM; q++) {
-        D1 wd[NF], f[NF];
-        to_dual(w, wd, NF);
-        wd[q].d[0] = 1.0;
-        if (d == 0) flux12<D1, 0>(wd, 1, f, 1);
-        else if (d == 1) flux12<D1, 1>(wd, 1, f, 1);
-        else flux12<D1, 2>(wd, 1, f, 1);
-        double s = 0.0;
-        for (int o = 0; o < NF; o++) s += f[o].d[0] * lF[o];
-        lw[q] += s;
-      }
+      if (d == 0) flux12_rev<0>(w, lF, lw);  // flux12 transposed onto the cell's primitives
+      else if (d == 1) flux12_rev<1>(w, lF, lw);
+      else flux12_rev<2>(w, lF, lw);
     }
-    for (int q = 0; q < 9; q++) {
-      Raw9<D1> rd;
-      for (int t = 0; t < 9; t++) rd.v[t] = D1(r.v[t]);
-      rd.v[q].d[0] = 1.0;
-      D1 wd[NF];
-      prim_of_raw<D1, false>(rd, wd);
-      double s = 0.0;
-      for (int o = 0; o < NPRIM; o++) s += wd[o].d[0] * lw[o];
-      if (q < NV) lam_uin[(long long)q * b.n + li] = s;
-      else lam_pin[li] += s;
-    }
+    double lr[9];  // the primitive conversion transposed onto the stage input
+    prim_of_raw_rev(r, lw, lr);
+    for (int q = 0; q < NV; q++) lam_uin[(long long)q * b.n + li] = lr[q];
+    lam_pin[li] += lr[8];
   }
 }
 
@@ -700,6 +755,69 @@ __device__ void tvd_update_rev(const Consts& c, double dtt, const double* Fp, co
   }
 }
 
+// Reverse of tvd_slope<double> (src/tvdlimit_SR.C:388-434): ls, the adjoint
+// of the limited slope at the middle cell b, back to the TCells of a, b, n
+// (added): q of all three, and b's boundary profiles hb, ht.  The zeroings
+// (large density jump, speed limit) pass nothing back, as for the dual
+// numbers, and every min / max takes the forward's branch.
+__device__ void tvd_slope_rev(const Consts& c, const TCell<double>& a, const TCell<double>& b, const TCell<double>& n,
+                              double vsqr_diff, const double* ls_in, double* l_a, double* l_b, double* l_n) {
+  const KC<double>& k = c.kd;
+  double ls[NV];
+#pragma unroll
+  for (int v = 0; v < NV; v++) ls[v] = ls_in[v];
+  const double qr = c.rho_log ? fabs(b.q[0] - n.q[0]) : fabs(log(b.q[0]) - log(n.q[0]));
+  if (qr > k.q_rho_max) ls[0] = 0.0;
+  if (k.has_vmax_lim && b.vsqr > vsqr_diff) ls[1] = ls[2] = ls[3] = 0.0;
+  double s0[NV];  // the limited slopes before the boundary factors
+#pragma unroll
+  for (int v = 0; v < NV; v++) {
+    const double sl = b.q[v] - a.q[v], sr = n.q[v] - b.q[v];
+    const double slm = 0.25 * (sl + sr);
+    const double lower = smin(smin(sl, sr), slm), upper = smax(smax(sl, sr), slm);
+    s0[v] = smax(0.0, lower) + smin(0.0, upper);
+  }
+  if (k.has_visc_slope) {
+    const double fb = 1.0 - k.visc_slope_bot * b.hb, ft = 1.0 - k.visc_slope_top * b.ht;
+    const double cf = fb * ft;
+    double l_cf = 0.0;
+    for (int v = 1; v <= 3; v++) { l_cf += ls[v] * s0[v]; ls[v] *= cf; }
+    l_b[T_HBOT] -= l_cf * ft * k.visc_slope_bot;
+    l_b[T_HTOP] -= l_cf * fb * k.visc_slope_top;
+  }
+  if (k.has_eta_slope) {
+    const double fb = 1.0 - k.eta_slope_bot * b.hb, ft = 1.0 - k.eta_slope_top * b.ht;
+    const double cf = fb * ft;
+    double l_cf = 0.0;
+    for (int v = 5; v <= 7; v++) { l_cf += ls[v] * s0[v]; ls[v] *= cf; }
+    l_b[T_HBOT] -= l_cf * ft * k.eta_slope_bot;
+    l_b[T_HTOP] -= l_cf * fb * k.eta_slope_top;
+  }
+#pragma unroll
+  for (int v = 0; v < NV; v++) {
+    const double sl = b.q[v] - a.q[v], sr = n.q[v] - b.q[v];
+    const double slm = 0.25 * (sl + sr);
+    const double m = smin(sl, sr), M = smax(sl, sr);
+    const double lower = smin(m, slm), upper = smax(M, slm);
+    double l_sl = 0.0, l_sr = 0.0, l_slm = 0.0;
+    if (0.0 < lower) {  // max(0, lower), lower = min(min(sl, sr), slm)
+      if (slm < m) l_slm += ls[v];
+      else if (sr < sl) l_sr += ls[v];
+      else l_sl += ls[v];
+    }
+    if (upper < 0.0) {  // min(0, upper), upper = max(max(sl, sr), slm)
+      if (M < slm) l_slm += ls[v];
+      else if (sl < sr) l_sr += ls[v];
+      else l_sl += ls[v];
+    }
+    l_sl += 0.25 * l_slm;
+    l_sr += 0.25 * l_slm;
+    l_b[v] += l_sl - l_sr;
+    l_a[v] -= l_sl;
+    l_n[v] += l_sr;
+  }
+}
+
 // T1: per cell i, the update transposed.  Outputs: lam_in_direct (8), the
 // adjoint of the cell's TCell (19), and of its right / left interface fluxes
 // and heating terms (9 + 9).
@@ -816,20 +934,13 @@ __global__ void k_tvd_t3(Consts c, const Dyn* dyn, Box b, const double* __restri
       ls[q] = i_if[(long long)(4 * NT + q) * b.n + li] + i_if[(long long)(4 * NT + NV + q) * b.n + ll];
     TCell<double> T[3];
     for (int o = -1; o <= 1; o++) cell_at<DIR>(c, s, V, P, i, j, k, o, T[o + 1]);
-    for (int t = 0; t < 3 * NT; t++) o_sl[(long long)t * b.n + li] = 0.0;
-    const int fc[11] = {0, 1, 2, 3, 4, 5, 6, 7, T_HBOT, T_HTOP, T_VSQR};
-    for (int q = 0; q < 27; q++) {
-      TCell<D1> a = dual_cell(T[0]), bb = dual_cell(T[1]), n = dual_cell(T[2]);
-      int role, f;
-      if (q < 8) { role = 0; f = q; tf(a)[f].d[0] = 1.0; }
-      else if (q < 19) { role = 1; f = fc[q - 8]; tf(bb)[f].d[0] = 1.0; }
-      else { role = 2; f = q - 19; tf(n)[f].d[0] = 1.0; }
-      D1 sl[NV];
-      tvd_slope<D1>(c, a, bb, n, D1(s.vsqr_diff), sl);
-      double acc = 0.0;
-      for (int o = 0; o < NV; o++) acc += sl[o].d[0] * ls[o];
-      o_sl[(long long)(role * NT + f) * b.n + li] = acc;
-    }
+    // the slope transposed in one reverse pass onto its three cells
+    double l_t[3][NT];
+    for (int r = 0; r < 3; r++)
+      for (int f = 0; f < NT; f++) l_t[r][f] = 0.0;
+    tvd_slope_rev(c, T[0], T[1], T[2], s.vsqr_diff, ls, l_t[0], l_t[1], l_t[2]);
+    for (int r = 0; r < 3; r++)
+      for (int f = 0; f < NT; f++) o_sl[(long long)(r * NT + f) * b.n + li] = l_t[r][f];
   }
 }
 
