@@ -818,6 +818,92 @@ __device__ void tvd_slope_rev(const Consts& c, const TCell<double>& a, const TCe
   }
 }
 
+// Reverse of tvd_cell<double> (src/tvdlimit_SR.C:269-377): lt, the adjoints
+// of a cell's TCell fields, back to its 9 stored values (lr, written).  The
+// boundary profiles hb, ht, qt are fixed by x; the switch CME is a step in
+// the values and passes nothing back; every min / max / floor takes the
+// forward's branch, as the dual numbers do.
+__device__ void tvd_cell_rev(const Consts& c, const Raw9<double>& r, double hb, double ht, double cmax_t, double fac0,
+                             bool hyper, double inv_va2max, const double* lt, double* lr) {
+  const KC<double>& k = c.kd;
+  // ---- forward
+  const double d0 = r.v[0];
+  const double d = smax(k.rho_min, d0);
+  const double dn = 1.0 / d;
+  double v[3], Bc[3];
+  for (int t = 0; t < 3; t++) { v[t] = r.v[1 + t] * dn; Bc[t] = r.v[5 + t]; }
+  const double vv = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+  const double bb = Bc[0] * Bc[0] + Bc[1] * Bc[1] + Bc[2] * Bc[2];
+  const double e = r.v[4] * dn - 0.5 * vv;
+  const double vs = sqrt(vv);
+  const double va2 = bb * dn;
+  const double x2 = va2 * inv_va2max, x4 = x2 * x2, s = 1.0 + x2, E = s + x4;
+  const double lf = s / E;
+  const double cs2 = (5.0 / 3.0) * r.v[8] * dn;
+  const double cfast = sqrt(va2 + cs2);
+  const double CME = (1.0 - k.CZ) * ((double)(vs >= k.CME_thresh * cfast));
+  const double d2 = d * d;
+  const double rl = d2 / (d2 + k.rho_lev);
+  const double rf = smin(lf, rl);
+  const double hh = 1.0 - hb - ht;
+  const double cfa = hb * k.tvd_cs[0] + (rf * k.tvd_cs[1] + (1.0 - rf) * k.tvd_cs[2]) * hh + ht * k.tvd_cs[3];
+  const double cf = smax(cfa, CME);
+  const double cs2b = cs2 * (cf * cf);
+  const double A = lf * (cs2b + va2);
+  const double mx = smax(cs2b, A);
+  const double sq = sqrt(mx);
+  const double cm = 0.0 + vs + sq;
+  // ---- reverse
+  double l_d = c.rho_log ? lt[0] / d : lt[0];
+  const double l_e = c.rho_log ? lt[4] / e : lt[4];
+  double l_v[3], l_B[3];
+  for (int t = 0; t < 3; t++) { l_v[t] = lt[1 + t]; l_B[t] = lt[5 + t]; }
+  double l_cm = lt[T_CM], l_vv = lt[T_VSQR], l_bb = lt[T_BSQR], l_lf = -lt[T_BC2];
+  if (hyper) {  // hd = fac0 * max(0, min(vhyp * sqrt(vsqr), cmax_t - cm))
+    const double hv = k.vhyp * vs, g = cmax_t - cm;
+    const double mn = smin(hv, g);
+    if (0.0 < mn) {
+      const double l_mn = lt[T_HD] * fac0;
+      if (g < hv) l_cm -= l_mn;
+      else if (vs > 0.0) l_vv += l_mn * k.vhyp * 0.5 / vs;
+    }
+  }
+  const double h1 = k.tvd_h[1], h2 = k.tvd_h[2];
+  double l_rf = (lt[T_HE] * (1.0 - CME) * (h1 - h2) + lt[T_HV] * (1.0 - CME) * (h1 - h2 * k.pm_v) +
+                 lt[T_HB] * (h1 - h2 * k.pm_B)) * hh;
+  double l_vs = l_cm;  // cm = (0 + vs) + sqrt(mx)
+  const double l_mx = sq > 0.0 ? l_cm * 0.5 / sq : 0.0;
+  double l_cs2b = 0.0, l_A = 0.0;
+  if (cs2b < A) l_A = l_mx;
+  else l_cs2b = l_mx;
+  l_lf += l_A * (cs2b + va2);
+  l_cs2b += l_A * lf;
+  double l_va2 = l_A * lf;
+  double l_cs2 = l_cs2b * (cf * cf);
+  const double l_cf = l_cs2b * cs2 * 2.0 * cf;
+  if (!(cfa < CME)) l_rf += l_cf * (k.tvd_cs[1] - k.tvd_cs[2]) * hh;
+  if (rl < lf) l_d += l_rf * k.rho_lev / ((d2 + k.rho_lev) * (d2 + k.rho_lev)) * 2.0 * d;
+  else l_lf += l_rf;
+  double l_dn = l_cs2 * (5.0 / 3.0) * r.v[8];
+  lr[8] = l_cs2 * (5.0 / 3.0) * dn;
+  const double l_x2 = l_lf * (1.0 - lf) / E + (-l_lf * lf / E) * 2.0 * x2;  // lf = s / (s + x4)
+  l_va2 += l_x2 * inv_va2max;
+  l_bb += l_va2 * dn;  // va2 = bb * dn
+  l_dn += l_va2 * bb;
+  if (vs > 0.0) l_vv += l_vs * 0.5 / vs;
+  lr[4] = l_e * dn;  // e = r4 * dn - 0.5 * vv
+  l_dn += l_e * r.v[4];
+  l_vv -= 0.5 * l_e;
+  for (int t = 0; t < 3; t++) {
+    const double lvt = l_v[t] + l_vv * 2.0 * v[t];
+    lr[1 + t] = lvt * dn;
+    l_dn += lvt * r.v[1 + t];
+    lr[5 + t] = l_B[t] + l_bb * 2.0 * Bc[t];
+  }
+  l_d -= l_dn * dn * dn;
+  lr[0] = (k.rho_min < d0) ? l_d : 0.0;
+}
+
 // T1: per cell i, the update transposed.  Outputs: lam_in_direct (8), the
 // adjoint of the cell's TCell (19), and of its right / left interface fluxes
 // and heating terms (9 + 9).
@@ -974,18 +1060,10 @@ __global__ void k_tvd_t4(Consts c, const Dyn* dyn, Box b, const double* __restri
     const Geom& g = c.g;
     raw_at(g, V, P, fwd(g, i, j, k), r);
     const int xi = GH + i;
-    for (int q = 0; q < 9; q++) {
-      Raw9<D1> rd;
-      for (int t = 0; t < 9; t++) rd.v[t] = D1(r.v[t]);
-      rd.v[q].d[0] = 1.0;
-      TCell<D1> t;
-      tvd_cell<D1>(c, rd, D1(c.kd.hfb[xi]), D1(c.kd.hft[xi]), D1(c.kd.qft[xi]), D1(s.cmax_t), D1(s.fac0), s.hyper,
-                   D1(s.inv_va2max), t);
-      double acc = 0.0;
-      for (int f = 0; f < NT; f++) acc += tf(t)[f].d[0] * lt[f];
-      if (q < NV) lam_in[(long long)q * b.n + li] = i_in[(long long)q * b.n + li] + acc;
-      else lam_p[li] += acc;
-    }
+    double lr[9];  // the cell quantities transposed onto the sweep input
+    tvd_cell_rev(c, r, c.kd.hfb[xi], c.kd.hft[xi], s.cmax_t, s.fac0, s.hyper, s.inv_va2max, lt, lr);
+    for (int q = 0; q < NV; q++) lam_in[(long long)q * b.n + li] = i_in[(long long)q * b.n + li] + lr[q];
+    lam_p[li] += lr[8];
   }
 }
 
