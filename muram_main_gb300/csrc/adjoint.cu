@@ -904,13 +904,45 @@ __device__ void tvd_cell_rev(const Consts& c, const Raw9<double>& r, double hb, 
   lr[0] = (k.rho_min < d0) ? l_d : 0.0;
 }
 
+// T0: the per-cell TVD quantities of every cell the sweep's transposes read
+// (interior in the other directions, two ghosts on either side along the
+// sweep), once, into tc (19 per node of the ghosted box).
+template <int DIR>
+__global__ void k_tvd_t0(Consts c, const Dyn* dyn, Box b, const double* __restrict__ V, const double* __restrict__ P,
+                         double* __restrict__ tc) {
+  const Sweep s = sweep_of<DIR>(c, dyn);
+  const Geom& g = c.g;
+  const int na = DIR == 0 ? b.nx + 2 * GH : b.nx, nb = DIR == 1 ? b.ny + 2 * GH : b.ny;
+  const int nc = DIR == 2 ? b.nz + 2 * GH : b.nz;
+  const long long m = (long long)na * nb * nc;
+  for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < m; t += (long long)gridDim.x * blockDim.x) {
+    int i = (int)(t % na), j = (int)((t / na) % nb), k = (int)(t / ((long long)na * nb));
+    if (DIR == 0) i -= GH;
+    if (DIR == 1) j -= GH;
+    if (DIR == 2) k -= GH;
+    TCell<double> T;
+    cell_at<DIR>(c, s, V, P, i, j, k, 0, T);
+    const long long id = fwd(g, i, j, k);
+    for (int f = 0; f < NT; f++) tc[(long long)f * g.N + id] = tf(T)[f];
+  }
+}
+
+// the cell `o` steps along DIR from interior (i, j, k), from k_tvd_t0's store
+template <int DIR>
+__device__ __forceinline__ void cell_load(const Geom& g, const double* __restrict__ tc, int i, int j, int k, int o,
+                                          TCell<double>& t) {
+  const long long id = fwd(g, i + (DIR == 0 ? o : 0), j + (DIR == 1 ? o : 0), k + (DIR == 2 ? o : 0));
+  for (int f = 0; f < NT; f++) tf(t)[f] = tc[(long long)f * g.N + id];
+}
+
 // T1: per cell i, the update transposed.  Outputs: lam_in_direct (8), the
 // adjoint of the cell's TCell (19), and of its right / left interface fluxes
 // and heating terms (9 + 9).
 template <int DIR>
 __global__ void k_tvd_t1(Consts c, const Dyn* dyn, Box b, const double* __restrict__ V, const double* __restrict__ P,
-                         const double* __restrict__ lam_out, int final_pass, double* __restrict__ o_in,
-                         double* __restrict__ o_cell, double* __restrict__ o_fp, double* __restrict__ o_fm) {
+                         const double* __restrict__ tc, const double* __restrict__ lam_out, int final_pass,
+                         double* __restrict__ o_in, double* __restrict__ o_cell, double* __restrict__ o_fp,
+                         double* __restrict__ o_fm) {
   const Sweep s = sweep_of<DIR>(c, dyn);
   const DynR<double>& dr = dyn->rd;
   for (long long li = (long long)blockIdx.x * blockDim.x + threadIdx.x; li < b.n;
@@ -919,7 +951,8 @@ __global__ void k_tvd_t1(Consts c, const Dyn* dyn, Box b, const double* __restri
     ijk(b, li, i, j, k);
     TCell<double> T[5];
     Raw9<double> r0;
-    for (int o = -2; o <= 2; o++) cell_at<DIR>(c, s, V, P, i, j, k, o, T[o + 2], o == 0 ? &r0 : nullptr);
+    raw_at(c.g, V, P, fwd(c.g, i, j, k), r0);
+    for (int o = -2; o <= 2; o++) cell_load<DIR>(c.g, tc, i, j, k, o, T[o + 2]);
     double sl[3][NV];
     for (int o = 0; o < 3; o++) tvd_slope<double>(c, T[o], T[o + 1], T[o + 2], s.vsqr_diff, sl[o]);
     const int p = pos_of<DIR>(i, j, k);
@@ -973,7 +1006,7 @@ __global__ void k_tvd_t1(Consts c, const Dyn* dyn, Box b, const double* __restri
 // transposed onto its four cells' TCells (am, a, b, bp: 19 each) and its two
 // slopes (8 each): 92 values per interface.
 template <int DIR>
-__global__ void k_tvd_t2(Consts c, const Dyn* dyn, Box b, const double* __restrict__ V, const double* __restrict__ P,
+__global__ void k_tvd_t2(Consts c, const Dyn* dyn, Box b, const double* __restrict__ tc,
                          const double* __restrict__ i_fp, const double* __restrict__ i_fm, double* __restrict__ o_if) {
   const Sweep s = sweep_of<DIR>(c, dyn);
   for (long long li = (long long)blockIdx.x * blockDim.x + threadIdx.x; li < b.n;
@@ -984,7 +1017,7 @@ __global__ void k_tvd_t2(Consts c, const Dyn* dyn, Box b, const double* __restri
     double lF[NV + 1];
     for (int q = 0; q <= NV; q++) lF[q] = i_fp[(long long)q * b.n + li] + i_fm[(long long)q * b.n + lr];
     TCell<double> T[4];
-    for (int o = -1; o <= 2; o++) cell_at<DIR>(c, s, V, P, i, j, k, o, T[o + 1]);
+    for (int o = -1; o <= 2; o++) cell_load<DIR>(c.g, tc, i, j, k, o, T[o + 1]);
     double sa[NV], sb[NV];
     tvd_slope<double>(c, T[0], T[1], T[2], s.vsqr_diff, sa);
     tvd_slope<double>(c, T[1], T[2], T[3], s.vsqr_diff, sb);
@@ -1007,7 +1040,7 @@ __global__ void k_tvd_t2(Consts c, const Dyn* dyn, Box b, const double* __restri
 // T3: per cell i, its slope transposed onto the three cells it reads
 // (i-1: q; i: q, hb, ht, vsqr; i+1: q): 3 x 19 values.
 template <int DIR>
-__global__ void k_tvd_t3(Consts c, const Dyn* dyn, Box b, const double* __restrict__ V, const double* __restrict__ P,
+__global__ void k_tvd_t3(Consts c, const Dyn* dyn, Box b, const double* __restrict__ tc,
                          const double* __restrict__ i_if, double* __restrict__ o_sl) {
   const Sweep s = sweep_of<DIR>(c, dyn);
   for (long long li = (long long)blockIdx.x * blockDim.x + threadIdx.x; li < b.n;
@@ -1019,7 +1052,7 @@ __global__ void k_tvd_t3(Consts c, const Dyn* dyn, Box b, const double* __restri
     for (int q = 0; q < NV; q++)
       ls[q] = i_if[(long long)(4 * NT + q) * b.n + li] + i_if[(long long)(4 * NT + NV + q) * b.n + ll];
     TCell<double> T[3];
-    for (int o = -1; o <= 1; o++) cell_at<DIR>(c, s, V, P, i, j, k, o, T[o + 1]);
+    for (int o = -1; o <= 1; o++) cell_load<DIR>(c.g, tc, i, j, k, o, T[o + 1]);
     // the slope transposed in one reverse pass onto its three cells
     double l_t[3][NT];
     for (int r = 0; r < 3; r++)
@@ -1127,9 +1160,10 @@ static void tvd_dir(const Consts& c, const Dyn* dyn, const adj::Box& b, const do
                     const double* lam_out, int final_pass, double* lam_in, double* lam_p, const AdjTvdScratch& w,
                     cudaStream_t s) {
   const int gr = adj_grid(b.n);
-  adj::k_tvd_t1<DIR><<<gr, 128, 0, s>>>(c, dyn, b, V, P, lam_out, final_pass, w.in, w.cell, w.fp, w.fm);
-  adj::k_tvd_t2<DIR><<<gr, 128, 0, s>>>(c, dyn, b, V, P, w.fp, w.fm, w.iface);
-  adj::k_tvd_t3<DIR><<<gr, 128, 0, s>>>(c, dyn, b, V, P, w.iface, w.slope);
+  adj::k_tvd_t0<DIR><<<gr, 128, 0, s>>>(c, dyn, b, V, P, w.tcell);
+  adj::k_tvd_t1<DIR><<<gr, 128, 0, s>>>(c, dyn, b, V, P, w.tcell, lam_out, final_pass, w.in, w.cell, w.fp, w.fm);
+  adj::k_tvd_t2<DIR><<<gr, 128, 0, s>>>(c, dyn, b, w.tcell, w.fp, w.fm, w.iface);
+  adj::k_tvd_t3<DIR><<<gr, 128, 0, s>>>(c, dyn, b, w.tcell, w.iface, w.slope);
   adj::k_tvd_t4<DIR><<<gr, 128, 0, s>>>(c, dyn, b, V, P, w.in, w.cell, w.iface, w.slope, lam_in, lam_p);
 }
 

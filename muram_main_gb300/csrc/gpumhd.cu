@@ -2278,6 +2278,7 @@ extern "C" int gpumhd_adjoint(gpumhd_ctx* ctx, int nsteps, int checkpoint_every,
   double *lU0 = m.get(ctx, 8 * n, &rc), *lP3 = m.get(ctx, n, &rc), *lP = m.get(ctx, n, &rc);
   double *bdq = m.get(ctx, 36 * n, &rc), *bwc = m.get(ctx, 11 * n, &rc);
   double* tv = m.get(ctx, (size_t)ADJ_TVD_DOUBLES * n, &rc);
+  double* tcell = m.get(ctx, 19 * N, &rc);
   Dyn* adyn = nullptr;
   if (!rc && cudaMalloc(&adyn, sizeof(Dyn)) != cudaSuccess) rc = fail(ctx, GPUMHD_E_NOMEM, "adjoint: Dyn");
   if (rc) { cudaFree(adyn); return rc; }
@@ -2291,6 +2292,7 @@ extern "C" int gpumhd_adjoint(gpumhd_ctx* ctx, int nsteps, int checkpoint_every,
   w.fm = w.fp + 9 * n;
   w.iface = w.fm + 9 * n;
   w.slope = w.iface + 92 * n;
+  w.tcell = tcell;
   using L = Launch<double>;
   // one recorded forward step: (A, Q0) -> (An, Qn), intermediates kept
   auto record = [&]() {

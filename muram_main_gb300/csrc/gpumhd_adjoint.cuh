@@ -15,6 +15,7 @@ struct AdjTvdScratch {
   double* fm;
   double* iface;
   double* slope;
+  double* tcell;  // the sweep's per-cell TVD quantities, 19 per node of the ghosted box
 };
 constexpr int ADJ_TVD_DOUBLES = 8 + 19 + 9 + 9 + 92 + 57;
 constexpr int ADJ_STAGE_DOUBLES = 36 + 11;
