@@ -53,7 +53,7 @@ typedef struct gpumhd_params {
   double CFL, CFL_tvd, dt, time, outcad;
   int autostep;          /* RunData::autostep (dt computed from the CFL condition) */
   int compensated;       /* FP32 fused steps only: 1 = compensated (Kahan) updates -- a per-cell
-                            FP32 remainder carries what rounding the state has dropped: every
+                            remainder (stored as bfloat16) carries what rounding the state has dropped: every
                             RK stage sum adds it, stage 4 and each TVD sweep store the new one
                             (zero where Tcheck or a floor changed the value); 0 = plain */
   /* PhysicsData::params */

@@ -839,7 +839,7 @@ static int upload_impl(gpumhd_ctx* ctx, int which, const H* host) {
   else Launch<double>::aos_to_soa(N, nf, stg, (double*)dst, ctx->stream);
   if (which == 0) {
     ctx->fused_ready = false;
-    if (ctx->comp) CK(cudaMemsetAsync(ctx->comp, 0, sizeof(float) * 8 * N, ctx->stream));
+    if (ctx->comp) CK(cudaMemsetAsync(ctx->comp, 0, sizeof(Rem<float>) * 8 * N, ctx->stream));
   }
   if (which == 3) ctx->have_pres = true;
   return check_launch(ctx, 1);
@@ -864,7 +864,7 @@ extern "C" int gpumhd_tile_from(gpumhd_ctx* ctx, gpumhd_ctx* src) {
     Launch<double>::tile_state(gd, gs, (const double*)src->S[src->iU], (double*)ctx->S[ctx->iU], ctx->stream);
     Launch<double>::fill_ghosts(ctx->c, (double*)ctx->S[ctx->iU], 8, 1, ctx->stream);
   }
-  if (ctx->comp) CK(cudaMemsetAsync(ctx->comp, 0, sizeof(float) * 8 * gd.N, ctx->stream));
+  if (ctx->comp) CK(cudaMemsetAsync(ctx->comp, 0, sizeof(Rem<float>) * 8 * gd.N, ctx->stream));
   ctx->fused_ready = false;
   return check_launch(ctx, 2);
 }
@@ -909,7 +909,7 @@ static int upload_async_impl(gpumhd_ctx* ctx, int which, const H* host) {
   CK(cudaEventRecord(ctx->ev_in_free[b], ctx->stream));
   if (which == 0) {
     ctx->fused_ready = false;
-    if (ctx->comp) CK(cudaMemsetAsync(ctx->comp, 0, sizeof(float) * 8 * N, ctx->stream));
+    if (ctx->comp) CK(cudaMemsetAsync(ctx->comp, 0, sizeof(Rem<float>) * 8 * N, ctx->stream));
   }
   if (which == 3) ctx->have_pres = true;
   return check_launch(ctx, 1);
@@ -1447,7 +1447,7 @@ static int enqueue_one_step(gpumhd_ctx* ctx, cudaEvent_t* ev = nullptr) {
     float* const sf1 = sp ? SF[1] : nullptr;
     float* const sf2 = sp ? SF[2] : nullptr;
     float* const sf0 = sp ? SF[0] : nullptr;
-    float* const comp = (ctx->p.compensated && ctx->comp) ? (float*)ctx->comp : nullptr;
+    Rem<float>* const comp = (ctx->p.compensated && ctx->comp) ? (Rem<float>*)ctx->comp : nullptr;
     float* const* S = (float* const*)ctx->S;
     float* const* P = (float* const*)ctx->P;
     mark();
@@ -1595,8 +1595,8 @@ static int fused_prepare(gpumhd_ctx* ctx, int nsteps) {
     if (rc1) return rc1;
   }
   if (ctx->f32 && ctx->p.compensated && !ctx->comp) {
-    CK(cudaMalloc(&ctx->comp, sizeof(float) * 8 * ctx->c.g.N));
-    CK(cudaMemsetAsync(ctx->comp, 0, sizeof(float) * 8 * ctx->c.g.N, ctx->stream));
+    CK(cudaMalloc(&ctx->comp, sizeof(Rem<float>) * 8 * ctx->c.g.N));
+    CK(cudaMemsetAsync(ctx->comp, 0, sizeof(Rem<float>) * 8 * ctx->c.g.N, ctx->stream));
   }
   if (!ctx->fused_ready) {
     // exchange + boundaries before the loop (src/solver.C:80-81), then the

@@ -6,6 +6,7 @@
 // FP32 instantiation uses the same formulas in float (with contraction) and
 // an interpolation form of the pressure lookup that keeps float accuracy.
 #pragma once
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -232,6 +233,18 @@ template <> __device__ __forceinline__ float smin<float>(float a, float b) { ret
 template <class R> struct Tiny100 { static __device__ __forceinline__ double get() { return 1e-100; } };
 template <> struct Tiny100<float> { static __device__ __forceinline__ float get() { return 1e-30f; } };
 template <class R> __device__ __forceinline__ R tiny100() { return (R)Tiny100<R>::get(); }
+
+// Storage of the FP32 compensated mode's rounding remainders: bfloat16.  A
+// remainder is below half an ulp of the value it belongs to, so its 8
+// significant bits carry the state to about 2^-33 relative, at half the
+// bytes of a float (the other precisions keep their own type, unused).
+template <class R> struct RemOf { using T = R; };
+template <> struct RemOf<float> { using T = __nv_bfloat16; };
+template <class R> using Rem = typename RemOf<R>::T;
+template <class R> __device__ __forceinline__ R rem_ld(const Rem<R>* p) { return (R)*p; }
+template <> __device__ __forceinline__ float rem_ld<float>(const __nv_bfloat16* p) { return __bfloat162float(*p); }
+template <class R> __device__ __forceinline__ void rem_st(Rem<R>* p, R v) { *p = v; }
+template <> __device__ __forceinline__ void rem_st<float>(__nv_bfloat16* p, float v) { *p = __float2bfloat16_rn(v); }
 
 __device__ __forceinline__ double d_log(double x) { return log(x); }
 __device__ __forceinline__ float d_log(float x) { return logf(x); }

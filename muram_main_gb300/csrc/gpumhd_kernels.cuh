@@ -384,7 +384,7 @@ __device__ __forceinline__ void store_cell(double* p, const double v[12]) {
 // (un = base + (wdt * R + C)) and stage 4 stores the new remainder -- zero
 // where Tcheck changed the value.
 template <class R>
-__device__ __forceinline__ void rk_update(const Consts& c, R* __restrict__ Cc, unsigned id, int stage, R wdt,
+__device__ __forceinline__ void rk_update(const Consts& c, Rem<R>* __restrict__ Cc, unsigned id, int stage, R wdt,
                                           const R* base, const R* Racc, R vmax, R emax, R* un) {
   if (Cc == nullptr) {
 #pragma unroll
@@ -396,14 +396,15 @@ __device__ __forceinline__ void rk_update(const Consts& c, R* __restrict__ Cc, u
   R y[NV], t[NV];
 #pragma unroll
   for (int v = 0; v < NV; v++) {
-    y[v] = wdt * Racc[v] + Cc[id + (unsigned)v * N32];
+    y[v] = wdt * Racc[v] + rem_ld<R>(Cc + id + (unsigned)v * N32);
     t[v] = base[v] + y[v];
     un[v] = t[v];
   }
   tcheck_cell<R>(c, vmax, emax, un[0], un[1], un[2], un[3], un[4]);
   if (stage == 4) {
 #pragma unroll
-    for (int v = 0; v < NV; v++) Cc[id + (unsigned)v * N32] = (un[v] == t[v]) ? y[v] - (t[v] - base[v]) : (R)0;
+    for (int v = 0; v < NV; v++)
+      rem_st<R>(Cc + id + (unsigned)v * N32, (un[v] == t[v]) ? y[v] - (t[v] - base[v]) : (R)0);
   }
 }
 
@@ -482,7 +483,7 @@ template <class R, int TX, int TY, bool RESID>
 __global__ void __launch_bounds__(TX* TY, 2) k_stage(Consts c, const R* __restrict__ Uin, const R* __restrict__ Pin,
                                                      const R* __restrict__ U0, R* __restrict__ Uout,
                                                      R* __restrict__ Pout, R* __restrict__ Res, Dyn* __restrict__ dyn,
-                                                     int stage, int zc, int write_pres, R* __restrict__ Cc) {
+                                                     int stage, int zc, int write_pres, Rem<R>* __restrict__ Cc) {
   using S = StageSmem<TX, TY>;
   constexpr int CW = CellW<R>::W;
   constexpr int NT = TX * TY;
@@ -879,8 +880,8 @@ __device__ __forceinline__ void tvd_flux(const Consts& c, const TCell<R>& am, co
 template <class R, bool DIAG = false>
 __device__ __forceinline__ void tvd_update(const Consts& c, R dtt, const R* Fp, const R* Fm, R qp, R qm,
                                            const TCell<R>& c0, const R* u_in, R* u, const TvdDiag<R>* dg = nullptr,
-                                           long long id = 0, R qvp = (R)0, R qvm = (R)0, const R* Cin = nullptr,
-                                           R* Cout = nullptr) {
+                                           long long id = 0, R qvp = (R)0, R qvm = (R)0, const Rem<R>* Cin = nullptr,
+                                           Rem<R>* Cout = nullptr) {
   const auto& kk_ = kc<R>(c);
   const long long N = c.g.N;
   R res[NV];
@@ -907,7 +908,7 @@ __device__ __forceinline__ void tvd_update(const Consts& c, R dtt, const R* Fp, 
       R rem[NV];
 #pragma unroll
       for (int v = 0; v < NV; v++) {
-        const R y = res[v] + Cin[(long long)v * N];
+        const R y = res[v] + rem_ld<R>(Cin + (long long)v * N);
         u[v] = u_in[v] + y;
         rem[v] = y - (u[v] - u_in[v]);
       }
@@ -919,7 +920,7 @@ __device__ __forceinline__ void tvd_update(const Consts& c, R dtt, const R* Fp, 
         if (u[0] != d0) rem[0] = (R)0;
         if (u[4] != e0) rem[4] = (R)0;
 #pragma unroll
-        for (int v = 0; v < NV; v++) Cout[(long long)v * N] = rem[v];
+        for (int v = 0; v < NV; v++) rem_st<R>(Cout + (long long)v * N, rem[v]);
       }
       return;
     }
@@ -1010,7 +1011,7 @@ template <class R> struct FinBlocks { static constexpr int v = sizeof(R) == 4 ? 
 // COMP (FP32 compensated mode; Cc its remainders): a field TCheck changes loses its remainder.
 template <class R, bool COMP = false>
 __global__ void __launch_bounds__(FIN_BX* FIN_BY, FinBlocks<R>::v) k_step_finish(Consts c, R* __restrict__ U, R* __restrict__ Pout,
-                                                               Dyn* __restrict__ dyn, R* __restrict__ Cc) {
+                                                               Dyn* __restrict__ dyn, Rem<R>* __restrict__ Cc) {
   if (dyn->err) return;
   const Geom& g = c.g;
   const DynR<R>& dr = dynr<R>(dyn);
@@ -1032,7 +1033,7 @@ __global__ void __launch_bounds__(FIN_BX* FIN_BY, FinBlocks<R>::v) k_step_finish
       for (int v = 0; v < 5; v++)
         if (!same_bits(u[v], u0[v])) {
           U[(unsigned)v * g.N32 + id] = u[v];
-          if (COMP) Cc[(unsigned)v * g.N32 + id] = (R)0;
+          if (COMP) rem_st<R>(Cc + (unsigned)v * g.N32 + id, (R)0);
         }
       R v1, v2, v3, ei;
       prim_from_cons(u[0], u[1], u[2], u[3], u[4], v1, v2, v3, ei);
@@ -1080,7 +1081,7 @@ template <class R> struct TvdBlocks { static constexpr int pencil = sizeof(R) ==
 template <class R, int DIR, bool DIAG = false, bool COMP = false>
 __global__ void __launch_bounds__(128, TvdBlocks<R>::pencil) k_tvd_sweep(Consts c, const R* __restrict__ Uin, const R* __restrict__ Pst,
                                                    R* __restrict__ Uout, Dyn* __restrict__ dyn, TvdArgs ta,
-                                                   TvdDiag<R> dg, R* __restrict__ Cc) {
+                                                   TvdDiag<R> dg, Rem<R>* __restrict__ Cc) {
   const Geom& g = c.g;
   if (dyn->err) return;
   if (ta.only_two_half && !dyn->two_half) return;   // second half pass not taken this step
@@ -1150,8 +1151,8 @@ __global__ void __launch_bounds__(128, TvdBlocks<R>::pencil) k_tvd_sweep(Consts 
       tvd_flux<R, DIR, DIAG>(c, cm1, c0, c1, c2, s0, s1, pos, sz, fac0, cmax_t, hyper, istart, F0, q0, &qv0);
       // update of cell pos (src/tvdlimit_SR.C:565-657)
       R u[NV];
-      const R* cin = nullptr;
-      R* cout = nullptr;
+      const Rem<R>* cin = nullptr;
+      Rem<R>* cout = nullptr;
       if (COMP) {  // FP32 compensated: the remainders of the interior cell this one is or images
         const int ci = DIR == 0 ? pos : aa, cj = DIR == 1 ? pos : (DIR == 0 ? aa : bb), ck = DIR == 2 ? pos : bb;
         const int sj = wrap_interior(cj, g.ny), sk = wrap_interior(ck, g.nz);
@@ -1190,7 +1191,7 @@ __device__ __forceinline__ R shfl(R v, int src) { return __shfl_sync(0xffffffffu
 template <class R, bool COMP = false>
 __global__ void __launch_bounds__(128, TvdBlocks<R>::lanes) k_tvd_sweep_xlanes(Consts c, const R* __restrict__ Uin, const R* __restrict__ Pst,
                                                           R* __restrict__ Uout, Dyn* __restrict__ dyn, int only_two_half,
-                                                          R* __restrict__ Cc) {
+                                                          Rem<R>* __restrict__ Cc) {
   const Geom& g = c.g;
   if (dyn->err) return;
   if (only_two_half && !dyn->two_half) return;
@@ -1248,8 +1249,8 @@ __global__ void __launch_bounds__(128, TvdBlocks<R>::lanes) k_tvd_sweep_xlanes(C
     R uc[NV], u[NV];
 #pragma unroll
     for (int v = 0; v < NV; v++) uc[v] = Uin[(long long)v * g.N + id];
-    const R* cin = nullptr;
-    R* cout = nullptr;
+    const Rem<R>* cin = nullptr;
+    Rem<R>* cout = nullptr;
     if (COMP) {  // FP32 compensated: the remainders of the interior cell this one is or images
       const int sj = wrap_interior((int)j, g.ny), sk = wrap_interior((int)k, g.nz);
       cin = Cc + ((long long)g.sx * ((long long)sj + (long long)g.sy * sk) + pos);

@@ -40,7 +40,7 @@ struct Launch {
   // zc: z planes per block (0: chosen from the occupancy, see stage())
   static void stage(const Consts& c, const R* Uin, const R* Pin, const R* U0, R* Uout, R* Pout, R* Res, Dyn* dyn,
                     int stage, bool resid, int write_pres, cudaStream_t s, const CUtensorMap* mu = nullptr,
-                    const CUtensorMap* mp = nullptr, int zc = 0, R* Cc = nullptr);
+                    const CUtensorMap* mp = nullptr, int zc = 0, Rem<R>* Cc = nullptr);
   // td: cells per thread along the y / z sweeps (0: 32); the sweeps store the
   // interior (and after a first half pass the periodic images), step_finish
   // then ends the step
@@ -48,10 +48,10 @@ struct Launch {
   // pencil kernel in every direction
   // Cc (FP32 compensated fused steps, else null): the state's rounding remainders
   static void tvd(const Consts& c, int dir, int mode, int only_two_half, const R* Uin, const R* Pst, R* Uout,
-                  Dyn* dyn, cudaStream_t s, int td = 0, const TvdDiag<R>* dg = nullptr, R* Cc = nullptr);
+                  Dyn* dyn, cudaStream_t s, int td = 0, const TvdDiag<R>* dg = nullptr, Rem<R>* Cc = nullptr);
   // Clean_divB on U (phi, divb: N each); returns the number of launches
   static int divb_clean(const Consts& c, R* U, R* phi, R* divb, Dyn* dyn, cudaStream_t s);
-  static void step_finish(const Consts& c, R* U, R* P, Dyn* dyn, cudaStream_t s, R* Cc = nullptr);
+  static void step_finish(const Consts& c, R* U, R* P, Dyn* dyn, cudaStream_t s, Rem<R>* Cc = nullptr);
   // MURaM's physical x boundaries on U (P: ghost pressures, may be null;
   // with_cmax: ghost CFL speeds join the step maximum); part: nz*BND_NQ doubles.
   // Returns the number of launches.
@@ -157,7 +157,7 @@ cudaError_t Launch<R>::setup() {
 template <class R>
 void Launch<R>::stage(const Consts& c, const R* Uin, const R* Pin, const R* U0, R* Uout, R* Pout, R* Res, Dyn* dyn,
                       int stage, bool resid, int write_pres, cudaStream_t s, const CUtensorMap* mu,
-                      const CUtensorMap* mp, int zc_force, R* Cc) {
+                      const CUtensorMap* mp, int zc_force, Rem<R>* Cc) {
   const bool tma = mu && mp;
   const int TX = tma ? StageTileTm<R>::TX : StageTile<R>::TX, TY = tma ? StageTileTm<R>::TY : StageTile<R>::TY;
   const Geom& g = c.g;
@@ -220,7 +220,7 @@ void Launch<R>::stage(const Consts& c, const R* Uin, const R* Pin, const R* U0, 
 
 template <class R>
 void Launch<R>::tvd(const Consts& c, int dir, int mode, int only_two_half, const R* Uin, const R* Pst, R* Uout,
-                    Dyn* dyn, cudaStream_t s, int td, const TvdDiag<R>* dg, R* Cc) {
+                    Dyn* dyn, cudaStream_t s, int td, const TvdDiag<R>* dg, Rem<R>* Cc) {
   const Geom& g = c.g;
   TvdArgs ta;
   ta.dir = dir;
@@ -319,7 +319,7 @@ void Launch<R>::sflx_update(const Consts& c, R* S, const R* S0, R* Rflx, const D
   k_sflx_update<R><<<grid_for((long long)c.g.nx * c.g.ny * c.g.nz, 256), 256, 0, s>>>(c, S, S0, Rflx, dyn, stage);
 }
 template <class R>
-void Launch<R>::step_finish(const Consts& c, R* U, R* P, Dyn* dyn, cudaStream_t s, R* Cc) {
+void Launch<R>::step_finish(const Consts& c, R* U, R* P, Dyn* dyn, cudaStream_t s, Rem<R>* Cc) {
   const Geom& g = c.g;
   const dim3 block(FIN_BX, FIN_BY);
   // z planes per block: one wave of resident blocks (each block marches

@@ -225,7 +225,7 @@ __global__ void __launch_bounds__(TX* TY, 2)
     k_stage_tm(const __grid_constant__ CUtensorMap mapU, const __grid_constant__ CUtensorMap mapP, Consts c,
                const R* __restrict__ Ug, const R* __restrict__ U0, R* __restrict__ Uout, R* __restrict__ Pout,
                R* __restrict__ Res,
-               Dyn* __restrict__ dyn, int stage, int zc, int write_pres, R* __restrict__ Cc) {
+               Dyn* __restrict__ dyn, int stage, int zc, int write_pres, Rem<R>* __restrict__ Cc) {
   using L = StageTm<R, TX, TY, DB>;
   static_assert(!DB || sizeof(R) == 4, "the double-buffered layout is for FP32");
   constexpr int CW = CellW<R>::W;
