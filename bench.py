@@ -168,7 +168,7 @@ def time_device(g, steps, warmup):
     return e0.elapsed_time(e1), g.launch_count - n0
 
 
-def time_e2e(g, steps, U, host_dtype="float64", reps=3):
+def time_e2e(g, steps, U, host_dtype="float64", reps=5):
     """End to end through the C ABI: per step the host state (pinned, cState
     layout: float64 as MURaM's default build holds it, or float32 as its
     SINGLE_PRECISION build does) goes to the device, one fused step runs, and
