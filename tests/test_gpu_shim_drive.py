@@ -31,7 +31,7 @@ CASES = ["periodic", "two_half_tvd", "open_bottom", "spitzer", "va_adjust", "dia
 
 
 @pytest.fixture(scope="module")
-def drivers(gpu_lib):
+def drive_programs(gpu_lib):
     build.build()
     subprocess.run(["make", "-s", "-C", DRIVE, f"GPULIB={os.path.dirname(build.LIB)}"], check=True)
     return {64: os.path.join(DRIVE, "_build", "shim_drive"), 32: os.path.join(DRIVE, "_build", "shim_drive_sp")}
@@ -54,11 +54,11 @@ def run_drive(exe, hp, U, steps, diag_step, tmp):
 
 
 @pytest.mark.parametrize("name", CASES)
-def test_shim_in_compute_solution_order_matches_reference(drivers, name, tmp_path):
+def test_shim_in_compute_solution_order_matches_reference(drive_programs, name, tmp_path):
     d, hp = H.load_case(name)
     steps = int(d["steps"])
     ds = int(hp.get("diag_step", 0))
-    final, dts, diag, _ = run_drive(drivers[64], hp, d["input_U"], steps, ds, str(tmp_path))
+    final, dts, diag, _ = run_drive(drive_programs[64], hp, d["input_U"], steps, ds, str(tmp_path))
     assert np.allclose(dts[:, 0], d["dts"].reshape(-1, 3)[:steps, 0], rtol=1e-12, atol=0)
     e = H.rel_linf(final, d["final_U"])
     print(f"shim [{name}]: rel Linf per field {np.array2string(e, precision=2)}")
@@ -68,14 +68,14 @@ def test_shim_in_compute_solution_order_matches_reference(drivers, name, tmp_pat
 
 
 @pytest.mark.parametrize("name", ["periodic", "open_bottom"])
-def test_shim_single_precision_build(drivers, name, tmp_path):
+def test_shim_single_precision_build(drive_programs, name, tmp_path):
     """cState of floats (MURaM built with SINGLE_PRECISION) through the float
     transfers, FP64 on the device: the per-routine path on the same
     float-rounded state gives the same float results."""
     d, hp = H.load_case(name)
     steps = int(d["steps"])
     U32 = d["input_U"].astype(np.float32).astype(np.float64)
-    final, dts, _, pres = run_drive(drivers[32], hp, U32, steps, 0, str(tmp_path))
+    final, dts, _, pres = run_drive(drive_programs[32], hp, U32, steps, 0, str(tmp_path))
     g = gpumhd.MuramGPU(H.gpu_params(hp, 64), eos_path=H.EOS_SMALL)
     g.upload_state(U32)
     g.exchange_grid(True)
