@@ -107,3 +107,19 @@ def test_shim_single_precision_build_moves_float_cstate():
     und = subprocess.run(["nm", "-u", obj], capture_output=True, text=True, check=True).stdout.split()
     for fn in ("gpumhd_upload_f32", "gpumhd_download_f32", "gpumhd_upload", "gpumhd_download"):
         assert fn in und, fn
+
+
+def test_shim_drive_program_builds():
+    """The MURaM-side shim compiled against the stand-in MURaM headers and
+    linked with libgpumhd.so, in both cState precisions (no GPU needed to
+    build; tests/test_gpu_shim_drive.py runs them)."""
+    build.build()
+    here = os.path.join(H.ROOT, "tests", "shim_drive")
+    subprocess.run(["make", "-s", "-C", here, f"GPULIB={os.path.dirname(build.LIB)}"], check=True)
+    for exe in ("shim_drive", "shim_drive_sp"):
+        path = os.path.join(here, "_build", exe)
+        assert os.access(path, os.X_OK), path
+        und = subprocess.run(["nm", "-u", path], capture_output=True, text=True, check=True).stdout
+        assert "gpumhd_mhd_residual" in und and "gpumhd_tvdlimit" in und
+        if exe == "shim_drive_sp":
+            assert "gpumhd_upload_f32" in und and "gpumhd_download_f32" in und
